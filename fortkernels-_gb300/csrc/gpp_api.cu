@@ -1,0 +1,355 @@
+// C ABI of the GPP path: plans, device-resident execution and the
+// host-pointer drop-in for BGW-Kernels/gppKer.cpp:303-439.
+#include <cstring>
+#include <vector>
+
+#include "sigma_gpp.h"
+#include "sigma_internal.cuh"
+#include "runtime.h"
+
+namespace sigma {
+int sch_blocks_per_sm_fp64();
+int ssx_blocks_per_sm_fp64();
+int sch_blocks_per_sm_mixed();
+int ssx_blocks_per_sm_mixed();
+}  // namespace sigma
+
+struct sigma_gpp_plan_s {
+  int device = 0;
+  int nb = 0, nvband = 0, nc = 0, ng = 0, precision = 0;
+  int valid_columns = 0;
+  int sch_grid = 0, ssx_grid = 0;
+  sigma::GppWork sch{}, ssx{};
+  void* block = nullptr;      // one device allocation for everything below
+  int* igp_of = nullptr;      // [ng]
+  int* counters = nullptr;    // [2]
+  double2* acht_n1 = nullptr; // [nb + nvband][3]
+  std::vector<int> host_inv, host_indinv;  // kept for the host drop-in's plan cache
+};
+
+namespace sigma {
+namespace {
+
+constexpr int kSsxBN = 8, kSsxBP = 256;
+constexpr int kItemsPerSlot = 48;  // work items per resident CTA (load balance of the tail)
+
+void size_work(GppWork& w, int band_begin, int band_count, int bn, int bp, int nc, int ng,
+               int grid, int items_per_slot) {
+  w.band_begin = band_begin;
+  w.band_count = band_count;
+  w.n_band_blocks = (band_count + bn - 1) / bn;
+  w.n_col_blocks = (ng + bp - 1) / bp;
+  const long long base = (long long)w.n_band_blocks * w.n_col_blocks;
+  if (base == 0) {
+    w.n_splits = 1;
+    w.split_len = nc;
+    w.n_items = 0;
+    return;
+  }
+  const long long want = (long long)items_per_slot * grid;
+  long long s = (want + base - 1) / base;
+  if (s < 1) s = 1;
+  int len = (int)((nc + s - 1) / s);
+  len = (len + kCK - 1) / kCK * kCK;
+  if (len < kCK) len = kCK;
+  w.split_len = len;
+  w.n_splits = (nc + len - 1) / len;
+  w.n_items = (int)(base * w.n_splits);
+}
+
+// Column map of BGW-Kernels/gppKer.cpp:322-328.  Returns SIGMA_OK or
+// SIGMA_ERR_INDEX_RANGE where the reference would read out of bounds
+// (indinv at indigp > ncouls, aqsmtemp / vcoul at igp == ncouls).
+int map_columns(int nc, int ng, const int* inv, const int* indinv, int indinv_len,
+                std::vector<int>& igp_of, int& valid) {
+  igp_of.resize(ng);
+  valid = 0;
+  for (int my_igp = 0; my_igp < ng; ++my_igp) {
+    const int indigp = inv[my_igp];
+    if (indigp < 0 || indigp > nc) return SIGMA_ERR_INDEX_RANGE;
+    int igp;
+    if (indigp == nc) {
+      igp = nc - 1;
+    } else {
+      if (indigp >= indinv_len) return SIGMA_ERR_INDEX_RANGE;
+      igp = indinv[indigp];
+    }
+    if (igp > nc || igp < 0) {
+      igp_of[my_igp] = -1;
+      continue;
+    }
+    if (igp == nc) return SIGMA_ERR_INDEX_RANGE;
+    igp_of[my_igp] = igp;
+    ++valid;
+  }
+  return SIGMA_OK;
+}
+
+int check_shape(int nb, int nvband, int nc, int ng, int nstart, int nend) {
+  if (nb <= 0 || nc <= 0 || ng <= 0 || ng > nc || nvband < 0 || nvband > nb) return SIGMA_ERR_INVALID_SHAPE;
+  if (nstart != 0 || nend - nstart != kNW) return SIGMA_ERR_INVALID_SHAPE;
+  return SIGMA_OK;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+}  // namespace sigma
+
+extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands, int nvband,
+                                     int ncouls, int ngpown, int nstart, int nend,
+                                     const int* inv_igp_index, const int* indinv,
+                                     int indinv_len, int precision) {
+  using namespace sigma;
+  if (!plan_out || !inv_igp_index || !indinv) return SIGMA_ERR_NULL;
+  *plan_out = nullptr;
+  int st = check_shape(number_bands, nvband, ncouls, ngpown, nstart, nend);
+  if (st != SIGMA_OK) return st;
+  if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED) return SIGMA_ERR_UNSUPPORTED;
+  if (indinv_len < ncouls) return SIGMA_ERR_INVALID_SHAPE;
+  std::vector<int> igp_of;
+  int valid = 0;
+  st = map_columns(ncouls, ngpown, inv_igp_index, indinv, indinv_len, igp_of, valid);
+  if (st != SIGMA_OK) return st;
+
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return SIGMA_ERR_NO_DEVICE;
+  }
+  const int sms = device_sm_count();
+  if (sms <= 0) return SIGMA_ERR_NO_DEVICE;
+
+  auto* p = new sigma_gpp_plan_s();
+  p->device = dev;
+  p->nb = number_bands;
+  p->nvband = nvband;
+  p->nc = ncouls;
+  p->ng = ngpown;
+  p->precision = precision;
+  p->valid_columns = valid;
+  const bool mixed = precision == SIGMA_PREC_MIXED;
+  p->sch_grid = sms * (mixed ? sch_blocks_per_sm_mixed() : sch_blocks_per_sm_fp64());
+  p->ssx_grid = sms * (mixed ? ssx_blocks_per_sm_mixed() : ssx_blocks_per_sm_fp64());
+  size_work(p->sch, 0, number_bands, kBN, kBP, ncouls, ngpown, p->sch_grid, kItemsPerSlot);
+  size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
+  if (p->sch.n_items < p->sch_grid) p->sch_grid = p->sch.n_items;
+  if (p->ssx.n_items < p->ssx_grid) p->ssx_grid = p->ssx.n_items;
+
+  const size_t b_igp = align_up(sizeof(int) * ngpown, 256);
+  const size_t b_cnt = 256;
+  const size_t b_n1 = align_up(sizeof(double2) * (size_t)(number_bands + nvband) * kNW, 256);
+  const size_t b_sch = align_up(sizeof(double2) * (size_t)p->sch.n_items * kBN * kNW, 256);
+  const size_t b_ssx = align_up(sizeof(double2) * (size_t)p->ssx.n_items * kSsxBN * kNW, 256);
+  cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_last_cuda_error(e, "cudaMalloc(plan)", __LINE__);
+    delete p;
+    return SIGMA_ERR_ALLOC;
+  }
+  char* base = static_cast<char*>(p->block);
+  p->igp_of = reinterpret_cast<int*>(base);
+  p->counters = reinterpret_cast<int*>(base + b_igp);
+  p->acht_n1 = reinterpret_cast<double2*>(base + b_igp + b_cnt);
+  p->sch.partial = reinterpret_cast<double2*>(base + b_igp + b_cnt + b_n1);
+  p->ssx.partial = reinterpret_cast<double2*>(base + b_igp + b_cnt + b_n1 + b_sch);
+  p->sch.counter = p->counters;
+  p->ssx.counter = p->counters + 1;
+  e = cudaMemcpy(p->igp_of, igp_of.data(), sizeof(int) * ngpown, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "cudaMemcpy(igp_of)", __LINE__);
+    cudaFree(p->block);
+    delete p;
+    return SIGMA_ERR_CUDA;
+  }
+  p->host_inv.assign(inv_igp_index, inv_igp_index + ngpown);
+  p->host_indinv.assign(indinv, indinv + ncouls);
+  *plan_out = p;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_plan_destroy(sigma_gpp_plan plan) {
+  if (!plan) return SIGMA_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(plan->device);
+  if (plan->block) cudaFree(plan->block);
+  cudaSetDevice(cur);
+  delete plan;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_plan_info(sigma_gpp_plan plan, int* valid_columns, long long* terms) {
+  if (!plan) return SIGMA_ERR_NULL;
+  if (valid_columns) *valid_columns = plan->valid_columns;
+  if (terms) *terms = (long long)plan->nb * plan->valid_columns * plan->nc * sigma::kNW;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, int wx_band_stride,
+                                 double occ, const sigma_complex128* aqsmtemp,
+                                 const sigma_complex128* aqsntemp,
+                                 const sigma_complex128* I_eps_array,
+                                 const sigma_complex128* wtilde_array, const double* vcoul,
+                                 sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                                 sigma_complex128* acht_n1_loc, void* stream) {
+  using namespace sigma;
+  if (!plan) return SIGMA_ERR_NULL;
+  if (!wx_array || !aqsmtemp || !aqsntemp || !I_eps_array || !wtilde_array || !vcoul || !achtemp ||
+      !asxtemp)
+    return SIGMA_ERR_NULL;
+  if (wx_band_stride != 0 && wx_band_stride < kNW) return SIGMA_ERR_INVALID_SHAPE;
+  int dev = 0;
+  SIGMA_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != plan->device) return SIGMA_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  GppDev p;
+  p.nb = plan->nb;
+  p.nvband = plan->nvband;
+  p.nc = plan->nc;
+  p.ng = plan->ng;
+  p.wx_stride = wx_band_stride;
+  p.occ = occ;
+  p.aqsm = reinterpret_cast<const double2*>(aqsmtemp);
+  p.aqsn = reinterpret_cast<const double2*>(aqsntemp);
+  p.ieps = reinterpret_cast<const double2*>(I_eps_array);
+  p.wt = reinterpret_cast<const double2*>(wtilde_array);
+  p.vcoul = vcoul;
+  p.wx = wx_array;
+  p.igp_of = plan->igp_of;
+
+  SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 2 * sizeof(int), s));
+  const bool mixed = plan->precision == SIGMA_PREC_MIXED;
+  if (plan->sch.n_items > 0)
+    SIGMA_CUDA_TRY(mixed ? launch_sch_mixed(p, plan->sch, plan->sch_grid, s)
+                         : launch_sch_fp64(p, plan->sch, plan->sch_grid, s));
+  if (plan->ssx.n_items > 0)
+    SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed(p, plan->ssx, plan->ssx_grid, s)
+                         : launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
+  SIGMA_CUDA_TRY(launch_gpp_reduce(plan->sch, plan->ssx, plan->nb, plan->acht_n1,
+                                   reinterpret_cast<double2*>(achtemp),
+                                   reinterpret_cast<double2*>(asxtemp),
+                                   reinterpret_cast<double2*>(acht_n1_loc), s));
+  return SIGMA_OK;
+}
+
+// ---------------------------------------------------------------- host drop-in
+namespace sigma {
+namespace {
+
+sigma_gpp_plan g_cached_plan = nullptr;
+
+void drop_cached_plan() {
+  if (g_cached_plan) sigma_gpp_plan_destroy(g_cached_plan);
+  g_cached_plan = nullptr;
+}
+
+struct HookOnce {
+  HookOnce() { register_shutdown_hook(drop_cached_plan); }
+};
+
+int cached_plan(int nb, int nvband, int nc, int ng, const int* inv, const int* indinv,
+                int precision, sigma_gpp_plan* out) {
+  static HookOnce once;
+  int dev = 0;
+  SIGMA_CUDA_TRY(cudaGetDevice(&dev));
+  sigma_gpp_plan c = g_cached_plan;
+  if (c && c->device == dev && c->nb == nb && c->nvband == nvband && c->nc == nc && c->ng == ng &&
+      c->precision == precision &&
+      std::memcmp(c->host_inv.data(), inv, sizeof(int) * ng) == 0 &&
+      std::memcmp(c->host_indinv.data(), indinv, sizeof(int) * nc) == 0) {
+    *out = c;
+    return SIGMA_OK;
+  }
+  drop_cached_plan();
+  sigma_gpp_plan p = nullptr;
+  int st = sigma_gpp_plan_create(&p, nb, nvband, nc, ng, 0, kNW, inv, indinv, nc, precision);
+  if (st != SIGMA_OK) return st;
+  g_cached_plan = p;
+  *out = p;
+  return SIGMA_OK;
+}
+
+int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int nend,
+             const int* inv, const int* indinv, const double* wx, double occ,
+             const sigma_complex128* aqsm, const sigma_complex128* aqsn,
+             const sigma_complex128* ieps, const sigma_complex128* wt, const double* vcoul,
+             sigma_complex128* achtemp, sigma_complex128* asxtemp, sigma_complex128* acht_n1_loc,
+             void* stream) {
+  if (!inv || !indinv || !wx || !aqsm || !aqsn || !ieps || !wt || !vcoul || !achtemp || !asxtemp)
+    return SIGMA_ERR_NULL;
+  int st = check_shape(nb, nvband, nc, ng, nstart, nend);
+  if (st != SIGMA_OK) return st;
+  std::lock_guard<std::mutex> lk(api_mutex());
+  sigma_gpp_plan plan = nullptr;
+  st = cached_plan(nb, nvband, nc, ng, inv, indinv, precision, &plan);
+  if (st != SIGMA_OK) return st;
+
+  const size_t band_bytes = sizeof(sigma_complex128) * (size_t)nb * nc;
+  const size_t col_bytes = sizeof(sigma_complex128) * (size_t)ng * nc;
+  size_t off[9];
+  size_t total = 0;
+  const size_t sizes[9] = {band_bytes, band_bytes, col_bytes, col_bytes, sizeof(double) * (size_t)nc,
+                           sizeof(double) * kNW, sizeof(sigma_complex128) * kNW,
+                           sizeof(sigma_complex128) * kNW, sizeof(sigma_complex128) * (size_t)nb};
+  for (int i = 0; i < 9; ++i) {
+    off[i] = total;
+    total += align_up(sizes[i], 256);
+  }
+  void* arena = nullptr;
+  st = arena_get(kArenaGppInputs, total, &arena);
+  if (st != SIGMA_OK) return st;
+  char* a = static_cast<char*>(arena);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const void* src[6] = {aqsm, aqsn, ieps, wt, vcoul, wx};
+  for (int i = 0; i < 6; ++i)
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[i], src[i], sizes[i], cudaMemcpyHostToDevice, s));
+  auto* d_ach = reinterpret_cast<sigma_complex128*>(a + off[6]);
+  auto* d_asx = reinterpret_cast<sigma_complex128*>(a + off[7]);
+  auto* d_n1 = reinterpret_cast<sigma_complex128*>(a + off[8]);
+  st = sigma_gpp_execute(plan, reinterpret_cast<const double*>(a + off[5]), 0, occ,
+                         reinterpret_cast<const sigma_complex128*>(a + off[0]),
+                         reinterpret_cast<const sigma_complex128*>(a + off[1]),
+                         reinterpret_cast<const sigma_complex128*>(a + off[2]),
+                         reinterpret_cast<const sigma_complex128*>(a + off[3]),
+                         reinterpret_cast<const double*>(a + off[4]), d_ach, d_asx,
+                         acht_n1_loc ? d_n1 : nullptr, stream);
+  if (st != SIGMA_OK) return st;
+  SIGMA_CUDA_TRY(cudaMemcpyAsync(achtemp, d_ach, sizes[6], cudaMemcpyDeviceToHost, s));
+  SIGMA_CUDA_TRY(cudaMemcpyAsync(asxtemp, d_asx, sizes[7], cudaMemcpyDeviceToHost, s));
+  if (acht_n1_loc)
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(acht_n1_loc, d_n1, sizes[8], cudaMemcpyDeviceToHost, s));
+  SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+  return SIGMA_OK;
+}
+
+}  // namespace
+}  // namespace sigma
+
+extern "C" int sigma_gpp_fp64(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
+                              int nend, const int* inv_igp_index, const int* indinv,
+                              const double* wx_array, double occ, const sigma_complex128* aqsmtemp,
+                              const sigma_complex128* aqsntemp,
+                              const sigma_complex128* I_eps_array,
+                              const sigma_complex128* wtilde_array, const double* vcoul,
+                              sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                              sigma_complex128* acht_n1_loc, void* stream) {
+  return sigma::gpp_host(SIGMA_PREC_FP64, number_bands, nvband, ncouls, ngpown, nstart, nend,
+                         inv_igp_index, indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array,
+                         wtilde_array, vcoul, achtemp, asxtemp, acht_n1_loc, stream);
+}
+
+extern "C" int sigma_gpp_mixed(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
+                               int nend, const int* inv_igp_index, const int* indinv,
+                               const double* wx_array, double occ,
+                               const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
+                               const sigma_complex128* I_eps_array,
+                               const sigma_complex128* wtilde_array, const double* vcoul,
+                               sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                               sigma_complex128* acht_n1_loc, void* stream) {
+  return sigma::gpp_host(SIGMA_PREC_MIXED, number_bands, nvband, ncouls, ngpown, nstart, nend,
+                         inv_igp_index, indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array,
+                         wtilde_array, vcoul, achtemp, asxtemp, acht_n1_loc, stream);
+}

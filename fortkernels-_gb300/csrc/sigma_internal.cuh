@@ -1,0 +1,160 @@
+// Internal declarations shared by the sigma CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+#include "sigma_common.h"
+
+#define SIGMA_CUDA_TRY(expr)                                  \
+  do {                                                        \
+    cudaError_t sigma_err_ = (expr);                          \
+    if (sigma_err_ != cudaSuccess) {                          \
+      sigma::set_last_cuda_error(sigma_err_, #expr, __LINE__); \
+      return SIGMA_ERR_CUDA;                                  \
+    }                                                         \
+  } while (0)
+
+namespace sigma {
+
+void set_last_cuda_error(cudaError_t err, const char* what, int line);
+
+// ---------------------------------------------------------------- constants
+// Physics constants of the mini-app (BGW-Kernels/gppKer.cpp:23-27, 195-199).
+constexpr double kTo1 = 1e-6;
+constexpr double kLimitTwo = 0.25;          // pow(0.5, 2)
+constexpr double kInvLimitOne = 4e-6;       // 1 / limitone, limitone = 1 / (4 * to1)
+constexpr double kInvTo1 = 1e6;             // 1 / to1
+constexpr int kNW = 3;                      // nend - nstart
+
+// Relative half-width of the band around a pole-guard threshold inside which
+// the mixed path re-takes its decision in FP64 (its FP32 |wdiff|^2 is within
+// 4e-7 relative of the FP64 value; the band is 2^-19 ~ 1.9e-6).
+constexpr float kGuardBand = 1.9073486328125e-06f;
+
+// ---------------------------------------------------------------- problem
+// Device view of one GPP instance.  igp_of[my_igp] is the mapped column or -1
+// for a column the reference skips (BGW-Kernels/gppKer.cpp:322-328).
+struct GppDev {
+  int nb, nvband, nc, ng;
+  int wx_stride;
+  double occ;
+  const double2* aqsm;   // [nb][nc]
+  const double2* aqsn;   // [nb][nc]
+  const double2* ieps;   // [ng][nc]
+  const double2* wt;     // [ng][nc]
+  const double* vcoul;   // [nc]
+  const double* wx;      // [nb * wx_stride + 3]
+  const int* igp_of;     // [ng]
+};
+
+// Work decomposition of one pass (sch over all bands, or ssx over the
+// occupied bands): items are (band block, column block, g-vector split).
+struct GppWork {
+  int band_begin, band_count;  // bands covered by this pass
+  int n_band_blocks, n_col_blocks, n_splits, split_len;
+  int n_items;
+  int* counter;                // dynamic item counter (zeroed before launch)
+  double2* partial;            // [n_band_blocks][n_col_blocks][n_splits][BN][3]
+};
+
+// Tile shape shared by the kernels of one precision.
+constexpr int kBN = 32;   // bands per tile
+constexpr int kBP = 32;   // columns (my_igp) per tile
+constexpr int kCK = 32;   // g-vectors per staged chunk
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------- launchers
+cudaError_t launch_sch_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+cudaError_t launch_ssx_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+int sch_blocks_per_sm(int precision);
+int ssx_blocks_per_sm(int precision);
+
+// Sums the partials of the sch and ssx passes in a fixed order into
+// acht_n1[nb][3] (workspace), achtemp[3], asxtemp[3] and acht_n1_loc[nb].
+cudaError_t launch_gpp_reduce(const GppWork& sch, const GppWork& ssx, int nb, double2* acht_n1,
+                              double2* achtemp, double2* asxtemp, double2* acht_n1_loc,
+                              cudaStream_t s);
+
+// ---------------------------------------------------------------- device helpers
+__device__ __forceinline__ double rcp_f64(double w) {
+  // Hardware approximation of the high word (MUFU.RCP64H), then one cubic
+  // Newton-Raphson step r = r0 (1 + e + e^2), e = 1 - w r0: the relative error
+  // goes from ~2^-20 to below the FP64 rounding unit.
+  double r0;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r0) : "d"(w));
+  double e = fma(-w, r0, 1.0);
+  double e2 = fma(e, e, e);
+  return fma(r0, e2, r0);
+}
+
+__device__ __forceinline__ float rcp_f32(float w) {
+  // MUFU.RCP plus one Newton-Raphson step r = r0 (2 - w r0).
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(w));
+  float e = fmaf(-w, r0, 1.0f);
+  return fmaf(r0, e, r0);
+}
+
+// Pole-guard quantities of one (column, g-vector) in FP64.  Both precisions
+// take the keep/drop decision from exactly these expressions:
+//   |wdiff|^2 = fma(c, c, b*b),  c = wx - a
+//   threshold = max(0.25, (a*a + b*b) * 4e-6)
+// |wdiff|^2 > threshold is the reference's (wdiffr > limittwo) &&
+// (delwr < limitone), since |delw|^2 = |wtilde|^2 / |wdiff|^2.
+__device__ __forceinline__ double guard_b2(double b) { return __dmul_rn(b, b); }
+__device__ __forceinline__ double guard_thr(double a, double b2) {
+  return fmax(kLimitTwo, __dmul_rn(fma(a, a, b2), kInvLimitOne));
+}
+__device__ __forceinline__ double guard_w(double wx, double a, double b2) {
+  double c = __dsub_rn(wx, a);
+  return fma(c, c, b2);
+}
+// Second occupied-band branch (delwr > to1  <=>  |wdiff|^2 < |wtilde|^2 / to1).
+__device__ __forceinline__ double guard_thr2(double a, double b2) {
+  return __dmul_rn(fma(a, a, b2), kInvTo1);
+}
+
+// Ordered compare of non-negative doubles on the integer pipe (keeps the
+// FP64 pipe for arithmetic).
+__device__ __forceinline__ bool gt_nonneg(double x, double y) {
+  return __double_as_longlong(x) > __double_as_longlong(y);
+}
+
+// Error-free sum (Knuth TwoSum).
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bv = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
+}
+__device__ __forceinline__ void two_sum_d(double a, double b, double& s, double& e) {
+  s = __dadd_rn(a, b);
+  double bv = __dsub_rn(s, a);
+  e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bv)), __dsub_rn(b, bv));
+}
+
+// float-float accumulator: (hi, lo) += x
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
+  float s, e;
+  two_sum_f(hi, x, s, e);
+  e = __fadd_rn(e, lo);
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
+// Neumaier-compensated double accumulator
+struct Comp {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double x) {
+    double t, e;
+    two_sum_d(s, x, t, e);
+    s = t;
+    c = __dadd_rn(c, e);
+  }
+  __device__ __forceinline__ double value() const { return __dadd_rn(s, c); }
+};
+
+}  // namespace sigma

@@ -1,0 +1,216 @@
+"""ctypes binding of libsigma_gb300.so, the sigma GPP / FF C ABI (include/*.h).
+
+The functions mirror the reference's calls: `gpp_fp64` / `gpp_mixed` take the
+arrays BGW-Kernels/gppKer.cpp builds in main() and return achtemp, asxtemp and
+acht_n1_loc as its loop nest :303-439 would leave them.  There is no CPU
+fallback: loading fails with an exception when the library is missing or no
+CUDA device is present, and every non-zero status raises SigmaError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+PKG = pathlib.Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libsigma_gb300.so"
+
+OK = 0
+PREC_FP64, PREC_MIXED = 0, 1
+FF_MODE_FP64, FF_MODE_OZAKI_BF16 = 0, 1
+
+STATUS = {
+    0: "ok", -1: "invalid shape", -2: "index out of range", -3: "allocation failed",
+    -4: "CUDA error", -5: "device wait timed out", -6: "null pointer", -7: "no usable CUDA device",
+    -8: "unsupported argument combination", -9: "workspace too small",
+}
+
+
+class SigmaError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        msg = f"{where}: {STATUS.get(status, 'unknown')} ({status})"
+        if detail:
+            msg += f": {detail}"
+        super().__init__(msg)
+
+
+_lib = None
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_LL = C.c_longlong
+_ULL = C.c_ulonglong
+
+# name -> argtypes (restype int unless noted)
+SIGNATURES = {
+    "sigma_status_string": ([_I], C.c_char_p),
+    "sigma_last_error_message": ([], C.c_char_p),
+    "sigma_shutdown": ([], _I),
+    "sigma_version": ([], C.c_char_p),
+    "sigma_gpp_fp64": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_mixed": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I, _I], _I),
+    "sigma_gpp_execute": ([_P, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_plan_destroy": ([_P], _I),
+    "sigma_gpp_plan_info": ([_P, _P, _P], _I),
+    "sigma_fill_uniform": ([_P, _LL, _LL, _ULL, _ULL, _LL, _LL, _D, _D, _P], _I),
+    "sigma_fill_stress": ([_P, _LL, _ULL, _ULL, _P, _I, _D, _D, _P], _I),
+    "sigma_measure_fma_peaks": ([_P, _P, _P], _I),
+}
+
+
+def load(path: pathlib.Path | str | None = None):
+    """Loads the CUDA library (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = pathlib.Path(path) if path else LIB_PATH
+    if not p.exists():
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_sigma_build", PKG / "build.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = C.CDLL(str(p))
+    for name, (args, res) in SIGNATURES.items():
+        if hasattr(lib, name):
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return list(SIGNATURES)
+
+
+def _check(status: int, where: str):
+    if status != OK:
+        detail = ""
+        if status == -4 and _lib is not None:
+            detail = _lib.sigma_last_error_message().decode(errors="replace")
+        raise SigmaError(status, where, detail)
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    # torch tensors (device or host)
+    return a.data_ptr()
+
+
+def _c128(a: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def gpp_host(prob, precision: int = PREC_FP64, stream: int = 0, want_n1: bool = True):
+    """Runs the host-pointer drop-in on a workload.GppProblem; returns
+    (achtemp[3], asxtemp[3], acht_n1_loc[nb]) as complex128 arrays."""
+    lib = load()
+    inv = np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, dtype=np.int32)
+    wx = np.ascontiguousarray(prob.wx_array, dtype=np.float64)
+    arrs = [_c128(prob.aqsmtemp), _c128(prob.aqsntemp), _c128(prob.I_eps_array), _c128(prob.wtilde_array)]
+    vcoul = np.ascontiguousarray(prob.vcoul, dtype=np.float64)
+    ach = np.zeros(3, np.complex128)
+    asx = np.zeros(3, np.complex128)
+    n1 = np.zeros(prob.number_bands, np.complex128) if want_n1 else None
+    fn = lib.sigma_gpp_fp64 if precision == PREC_FP64 else lib.sigma_gpp_mixed
+    st = fn(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart, prob.nend,
+            _ptr(inv), _ptr(indinv), _ptr(wx), prob.occ, *[_ptr(a) for a in arrs], _ptr(vcoul),
+            _ptr(ach), _ptr(asx), _ptr(n1), stream)
+    _check(st, fn.__name__)
+    return ach, asx, n1
+
+
+class GppPlan:
+    """Device-resident GPP plan (sigma_gpp_plan_create / execute / destroy)."""
+
+    def __init__(self, number_bands, nvband, ncouls, ngpown, inv_igp_index, indinv,
+                 precision=PREC_FP64, nstart=0, nend=3):
+        self.lib = load()
+        self.inv = np.ascontiguousarray(inv_igp_index, dtype=np.int32)
+        self.indinv = np.ascontiguousarray(indinv, dtype=np.int32)
+        h = C.c_void_p()
+        st = self.lib.sigma_gpp_plan_create(C.byref(h), number_bands, nvband, ncouls, ngpown, nstart,
+                                            nend, _ptr(self.inv), _ptr(self.indinv), len(self.indinv),
+                                            precision)
+        _check(st, "sigma_gpp_plan_create")
+        self.handle = h
+        self.number_bands = number_bands
+
+    def info(self):
+        v = C.c_int()
+        t = C.c_longlong()
+        _check(self.lib.sigma_gpp_plan_info(self.handle, C.byref(v), C.byref(t)), "sigma_gpp_plan_info")
+        return v.value, t.value
+
+    def execute(self, wx, aqsm, aqsn, ieps, wt, vcoul, achtemp, asxtemp, acht_n1_loc=None,
+                occ=1.0, wx_band_stride=0, stream=0):
+        """All array arguments are device pointers (ints) or CUDA tensors."""
+        st = self.lib.sigma_gpp_execute(self.handle, _ptr(wx) if not isinstance(wx, int) else wx,
+                                        wx_band_stride, occ,
+                                        *[a if isinstance(a, int) else _ptr(a)
+                                          for a in (aqsm, aqsn, ieps, wt, vcoul, achtemp, asxtemp)],
+                                        None if acht_n1_loc is None else
+                                        (acht_n1_loc if isinstance(acht_n1_loc, int) else _ptr(acht_n1_loc)),
+                                        stream)
+        _check(st, "sigma_gpp_execute")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sigma_gpp_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fill_uniform(dst_ptr: int, count: int, dst_stride: int, seed: int, array_id: int,
+                 draw_offset: int, draw_stride: int, lo: float, span: float, stream: int = 0):
+    lib = load()
+    _check(lib.sigma_fill_uniform(dst_ptr, count, dst_stride, seed, array_id, draw_offset,
+                                  draw_stride, lo, span, stream), "sigma_fill_uniform")
+
+
+def fill_complex_device(dst_ptr: int, n: int, seed: int, array_id: int, re: tuple, im: tuple,
+                        stream: int = 0):
+    """Device twin of workload.fill_complex."""
+    fill_uniform(dst_ptr, n, 2, seed, array_id, 0, 2, float(re[0]), float(re[1]) - float(re[0]), stream)
+    fill_uniform(dst_ptr + 8, n, 2, seed, array_id, 1, 2, float(im[0]), float(im[1]) - float(im[0]), stream)
+
+
+def fill_real_device(dst_ptr: int, n: int, seed: int, array_id: int, lo: float, hi: float,
+                     stream: int = 0):
+    fill_uniform(dst_ptr, n, 1, seed, array_id, 0, 1, float(lo), float(hi) - float(lo), stream)
+
+
+def fill_stress_device(wt_ptr: int, n: int, seed: int, array_id: int, wx, fraction=0.05,
+                       width=1e-3, stream: int = 0):
+    lib = load()
+    w = np.ascontiguousarray(wx, dtype=np.float64)
+    _check(lib.sigma_fill_stress(wt_ptr, n, seed, array_id, _ptr(w), len(w), fraction, width, stream),
+           "sigma_fill_stress")
+
+
+def measure_fma_peaks(stream: int = 0):
+    """(fp64_tflops, fp32_tflops) measured on the current device."""
+    lib = load()
+    a = C.c_double()
+    b = C.c_double()
+    _check(lib.sigma_measure_fma_peaks(C.byref(a), C.byref(b), stream), "sigma_measure_fma_peaks")
+    return a.value, b.value
+
+
+def shutdown():
+    if _lib is not None:
+        _lib.sigma_shutdown()

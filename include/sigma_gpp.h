@@ -1,0 +1,103 @@
+/* sigma_gpp.h - GPP (generalized plasmon-pole) sigma sum on GB300.
+ *
+ * Computes, for bands n1 in [0, number_bands), columns my_igp in [0, ngpown)
+ * (igp = indinv[inv_igp_index[my_igp]], clamped to ncouls-1 when the index is
+ * ncouls, column skipped when igp < 0 or igp > ncouls), g-vectors ig in
+ * [0, ncouls) and the three frequencies iw:
+ *
+ *   wdiff  = wx[iw] - wtilde[my_igp][ig]
+ *   delw   = wtilde * conj(wdiff) / |wdiff|^2
+ *   scha   = conj(aqsm[n1][igp]) * aqsn[n1][ig] * delw * I_eps[my_igp][ig]
+ *            kept when |wdiff|^2 > 0.25 and |delw|^2 < 1/(4e-6)   (pole guard)
+ *   achtemp[iw]     += 0.5 * vcoul[igp] * sum_ig scha
+ *   acht_n1_loc[n1] += 0.5 * vcoul[igp] * sum_ig scha(iw = 2)
+ *   asxtemp[iw]     += occ * vcoul[igp] * sum_ig ssxa        (bands n1 < nvband)
+ *
+ * with ssxa the occupied-band screened-exchange term of ssxt_scht_solver.
+ * Reference: BGW-Kernels/gppKer.cpp:19-65 (ssxt_scht_solver), :130-159
+ * (flagOCC_solver), :303-439 (band loop, hot loop :387-413, epilogue
+ * :416-424, reduction :431-439), index map :322-328, frequencies :310-314.
+ *
+ * Outputs are overwritten, not accumulated (the reference zero-initialises
+ * them, :222-232, :255).  wx_array holds the caller's frequencies: three per
+ * band with stride wx_band_stride, or stride 0 for one set shared by every
+ * band (the mini-app's case: e_n1kq is one constant, :201, :312).
+ *
+ * Arrays (row-major, interleaved complex128):
+ *   aqsmtemp, aqsntemp          [number_bands][ncouls]
+ *   I_eps_array, wtilde_array   [ngpown][ncouls]
+ *   vcoul                       [ncouls]
+ *   inv_igp_index               [ngpown]
+ *   indinv                      [indinv_len]  (>= ncouls; indinv[ncouls] is never read)
+ *   achtemp, asxtemp            [3]
+ *   acht_n1_loc                 [number_bands]  (may be NULL)
+ */
+#ifndef SIGMA_GPP_H
+#define SIGMA_GPP_H
+
+#include "sigma_common.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------
+ * Host-pointer drop-in.  Takes the arrays gppKer.cpp builds in main()
+ * (BGW-Kernels/gppKer.cpp:222-299) and replaces its loop nest :303-439 with
+ * one call.  The library copies the inputs into its cached device buffers on
+ * `stream` (NULL: the legacy default stream), runs the kernels and copies
+ * the outputs back; it returns after the stream has drained.  indinv has
+ * ncouls entries, as in the reference; wx_array has 3 entries shared by every
+ * band.  Host buffers in pinned memory copy fastest.
+ * ------------------------------------------------------------------------- */
+int sigma_gpp_fp64(int number_bands, int nvband, int ncouls, int ngpown, int nstart, int nend,
+                   const int* inv_igp_index, const int* indinv, const double* wx_array,
+                   double occ, const sigma_complex128* aqsmtemp,
+                   const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                   const sigma_complex128* wtilde_array, const double* vcoul,
+                   sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                   sigma_complex128* acht_n1_loc, void* stream);
+
+/* Same contract; FP32 bulk arithmetic with the pole-guard decisions taken as
+ * the FP64 path takes them and compensated FP64 reductions.  Every output is
+ * within 1e-6 relative of the FP64 result on the production value ranges. */
+int sigma_gpp_mixed(int number_bands, int nvband, int ncouls, int ngpown, int nstart, int nend,
+                    const int* inv_igp_index, const int* indinv, const double* wx_array,
+                    double occ, const sigma_complex128* aqsmtemp,
+                    const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                    const sigma_complex128* wtilde_array, const double* vcoul,
+                    sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                    sigma_complex128* acht_n1_loc, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Device-resident path.  A plan validates the index maps on the host (where
+ * the reference would read out of bounds it returns SIGMA_ERR_INDEX_RANGE),
+ * uploads the column map and owns the partial-sum buffers; executing it is
+ * asynchronous on `stream`, allocates nothing and can be captured in a CUDA
+ * graph.  Inputs and outputs of sigma_gpp_execute are device pointers.
+ * One plan may be executed by one stream at a time (its partial buffers are
+ * reused by every execution).
+ * ------------------------------------------------------------------------- */
+typedef struct sigma_gpp_plan_s* sigma_gpp_plan;
+
+int sigma_gpp_plan_create(sigma_gpp_plan* plan, int number_bands, int nvband, int ncouls,
+                          int ngpown, int nstart, int nend, const int* inv_igp_index,
+                          const int* indinv, int indinv_len, int precision);
+
+int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, int wx_band_stride, double occ,
+                      const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
+                      const sigma_complex128* I_eps_array, const sigma_complex128* wtilde_array,
+                      const double* vcoul, sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                      sigma_complex128* acht_n1_loc, void* stream);
+
+int sigma_gpp_plan_destroy(sigma_gpp_plan plan);
+
+/* Number of valid columns (my_igp whose igp survives the reference's range
+ * test) and of terms number_bands * valid_columns * ncouls * 3. */
+int sigma_gpp_plan_info(sigma_gpp_plan plan, int* valid_columns, long long* terms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIGMA_GPP_H */

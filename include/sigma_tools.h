@@ -1,0 +1,44 @@
+/* sigma_tools.h - workload generation and measurement helpers.
+ *
+ * The reference drivers fill their inputs with constants inside main()
+ * (BGW-Kernels/gppKer.cpp:275-299, FFKer_cori/ffKernel.cpp:398-433).  These
+ * helpers generate the seeded synthetic inputs of the production shapes
+ * directly in device memory, bit-identical to the host generator in
+ * fortkernels-_gb300/workload.py (SplitMix64 as a counter-based stream), and
+ * measure the FP64 / FP32 FMA throughput the roofline is quoted against.
+ */
+#ifndef SIGMA_TOOLS_H
+#define SIGMA_TOOLS_H
+
+#include "sigma_common.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* dst[i * dst_stride] = lo + span * u(draw_offset + i * draw_stride), i < count,
+ * where u(k) is draw k of stream (seed, array_id) as a double in [0, 1).
+ * dst is a device pointer.  Asynchronous on `stream`. */
+int sigma_fill_uniform(double* dst, long long count, long long dst_stride,
+                       unsigned long long seed, unsigned long long array_id,
+                       long long draw_offset, long long draw_stride, double lo, double span,
+                       void* stream);
+
+/* Moves a fraction of the wtilde elements (interleaved complex128, device) to
+ * re = wx[k] + offset, offset in (-width, width), k among the nw frequencies,
+ * using draws 3e, 3e+1, 3e+2 of stream (seed, array_id) for element e; the
+ * same rule as workload.stress_wtilde. */
+int sigma_fill_stress(double* wtilde, long long count, unsigned long long seed,
+                      unsigned long long array_id, const double* wx_host, int nw,
+                      double fraction, double width, void* stream);
+
+/* Measured issue-limited throughput of dependent-free DFMA and FFMA streams
+ * on the current device, in TFLOP/s (an FMA counts as 2 flop).  Runs a few
+ * milliseconds of kernels on `stream` and synchronises it. */
+int sigma_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIGMA_TOOLS_H */

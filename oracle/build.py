@@ -1,0 +1,69 @@
+"""Build recipe of the CPU oracle (test infrastructure only).
+
+  oracle/_build/liboracle.so  <- oracle/gpp_oracle.cpp (the C++ restatement)
+  oracle/_ref/gppKer          <- BGW-Kernels/gppKer.cpp of the reference, unmodified
+  oracle/_ref/libgppref.so    <- the same file (main renamed by -D) + oracle/ref_harness.cpp
+
+The two oracle/_ref products are built only where the reference checkout is
+present (REFERENCE_ROOT, default /root/reference); they are compiled from the
+reference's own source file in place and nothing of it is copied.
+"""
+from __future__ import annotations
+
+import os
+import pathlib
+import subprocess
+
+HERE = pathlib.Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF_OUT = HERE / "_ref"
+ORACLE_LIB = BUILD / "liboracle.so"
+REF_BIN = REF_OUT / "gppKer"
+REF_LIB = REF_OUT / "libgppref.so"
+REFERENCE_ROOT = pathlib.Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
+REF_SRC = REFERENCE_ROOT / "BGW-Kernels" / "gppKer.cpp"
+
+ORACLE_FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+REF_FLAGS = ["-O3", "-std=c++11", "-fopenmp"]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{' '.join(map(str, cmd))}\n{r.stdout}\n{r.stderr}")
+
+
+def _newer(target: pathlib.Path, *deps: pathlib.Path) -> bool:
+    return target.exists() and all(target.stat().st_mtime >= d.stat().st_mtime for d in deps)
+
+
+def build_oracle() -> pathlib.Path:
+    src = HERE / "gpp_oracle.cpp"
+    if _newer(ORACLE_LIB, src):
+        return ORACLE_LIB
+    BUILD.mkdir(exist_ok=True)
+    _run(["g++", *ORACLE_FLAGS, str(src), "-o", str(ORACLE_LIB)])
+    return ORACLE_LIB
+
+
+def reference_available() -> bool:
+    return REF_SRC.exists()
+
+
+def build_reference() -> bool:
+    """Builds oracle/_ref from the reference source; False when it is absent."""
+    if not reference_available():
+        return False
+    REF_OUT.mkdir(exist_ok=True)
+    if not _newer(REF_BIN, REF_SRC):
+        _run(["g++", *REF_FLAGS, str(REF_SRC), "-o", str(REF_BIN)])
+    harness = HERE / "ref_harness.cpp"
+    if not _newer(REF_LIB, REF_SRC, harness):
+        _run(["g++", *REF_FLAGS, "-fPIC", "-shared", "-Dmain=gppker_reference_main",
+              str(REF_SRC), str(harness), "-o", str(REF_LIB)])
+    return True
+
+
+if __name__ == "__main__":
+    print(build_oracle())
+    print("reference:", build_reference())

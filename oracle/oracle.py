@@ -1,0 +1,170 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module, as the checker; the product library never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import pathlib
+import re
+import subprocess
+import resource
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+_P, _I, _D = C.c_void_p, C.c_int, C.c_double
+
+_GPP_ARGS = [_I, _I, _I, _I, _I, _I, _P, _P, _I, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        l = C.CDLL(str(path))
+        l.oracle_gpp.argtypes = _GPP_ARGS
+        l.oracle_gpp_port.argtypes = _GPP_ARGS
+        l.oracle_gpp_columns.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P,
+                                         _I, _I, _I]
+        l.oracle_ff_schdt.argtypes = [_I, _I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _I]
+        _lib = l
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _prep(prob):
+    c = lambda a: np.ascontiguousarray(a, dtype=np.complex128)
+    return (np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32),
+            np.ascontiguousarray(prob.indinv, dtype=np.int32),
+            np.ascontiguousarray(prob.wx_array, dtype=np.float64),
+            c(prob.aqsmtemp), c(prob.aqsntemp), c(prob.I_eps_array), c(prob.wtilde_array),
+            np.ascontiguousarray(prob.vcoul, dtype=np.float64))
+
+
+def gpp(prob, band_begin=0, band_end=None, nthreads=0, port=False, wx_band_stride=0):
+    """Compensated oracle (or, port=True, the reference-order port) on a
+    workload.GppProblem.  Returns (achtemp, asxtemp, acht_n1_loc) where
+    acht_n1_loc holds zeros outside [band_begin, band_end)."""
+    if band_end is None:
+        band_end = prob.number_bands
+    inv, indinv, wx, aqsm, aqsn, ieps, wt, vcoul = _prep(prob)
+    ach = np.zeros(3, np.complex128)
+    asx = np.zeros(3, np.complex128)
+    n1 = np.zeros(prob.number_bands, np.complex128)
+    fn = lib().oracle_gpp_port if port else lib().oracle_gpp
+    st = fn(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart, prob.nend,
+            _p(inv), _p(indinv), len(indinv), _p(wx), wx_band_stride, prob.occ, _p(aqsm), _p(aqsn),
+            _p(ieps), _p(wt), _p(vcoul), _p(ach), _p(asx), _p(n1), band_begin, band_end, nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_gpp status {st}")
+    return ach, asx, n1
+
+
+def gpp_columns(prob, band_begin=0, band_end=None, nthreads=0, wx_band_stride=0):
+    """Per-(band, column, frequency) sch_array (0.5*scht) and ssx_array sums."""
+    if band_end is None:
+        band_end = prob.number_bands
+    inv, indinv, wx, aqsm, aqsn, ieps, wt, _ = _prep(prob)
+    nbr = band_end - band_begin
+    sch = np.zeros((nbr, prob.ngpown, 3), np.complex128)
+    ssx = np.zeros((nbr, prob.ngpown, 3), np.complex128)
+    st = lib().oracle_gpp_columns(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, _p(inv),
+                                  _p(indinv), len(indinv), _p(wx), wx_band_stride, _p(aqsm),
+                                  _p(aqsn), _p(ieps), _p(wt), _p(sch), _p(ssx), band_begin,
+                                  band_end, nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_gpp_columns status {st}")
+    return sch, ssx
+
+
+def ff_schdt(prob, entries=None, nthreads=0):
+    """schDt[n1][ifreq] for the (n1, ifreq) pairs in `entries` (default all)."""
+    if entries is None:
+        entries = [(n, f) for n in range(prob.number_bands) for f in range(prob.nfreq)]
+    en = np.ascontiguousarray([e[0] for e in entries], dtype=np.int32)
+    ef = np.ascontiguousarray([e[1] for e in entries], dtype=np.int32)
+    out = np.zeros(len(entries), np.complex128)
+    c = lambda a: np.ascontiguousarray(a, dtype=np.complex128)
+    inv = np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, dtype=np.int32)
+    epsr, aqsn, aqsm = c(prob.I_epsR), c(prob.aqsntemp), c(prob.aqsmtemp)
+    st = lib().oracle_ff_schdt(prob.number_bands, prob.ncouls, prob.ngpown, prob.nfreq, _p(inv),
+                               _p(indinv), _p(epsr), _p(aqsn), _p(aqsm), len(entries), _p(en),
+                               _p(ef), _p(out), nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_ff_schdt status {st}")
+    return out
+
+
+# ---------------------------------------------------------------- the reference itself
+def reference_lib():
+    """The reference's flagOCC_solver through oracle/ref_harness.cpp (None when
+    the reference checkout is absent)."""
+    global _ref
+    if _ref is None:
+        if not _build.build_reference():
+            return None
+        l = C.CDLL(str(_build.REF_LIB))
+        l.ref_flagocc_columns.argtypes = [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]
+        l.ref_main.argtypes = [_I, _I, _I, _I]
+        _ref = l
+    return _ref
+
+
+def reference_flagocc_columns(prob, igp_of):
+    """(ssx_array, sch_array) per (band, column, frequency) from the reference's
+    own flagOCC_solver on the problem's arrays."""
+    l = reference_lib()
+    if l is None:
+        return None
+    nb, ng = prob.number_bands, prob.ngpown
+    arrs = [np.array(a, dtype=np.complex128, order="C", copy=True)
+            for a in (prob.aqsmtemp, prob.aqsntemp, prob.I_eps_array, prob.wtilde_array)]
+    ssx = np.zeros((nb, ng, 3), np.complex128)
+    sch = np.zeros((nb, ng, 3), np.complex128)
+    igp = np.ascontiguousarray(igp_of, dtype=np.int32)
+    wx = np.ascontiguousarray(prob.wx_array, dtype=np.float64)
+    l.ref_flagocc_columns(nb, prob.ncouls, ng, _p(igp), _p(wx), *[_p(a) for a in arrs], _p(ssx), _p(sch))
+    return ssx, sch
+
+
+_ACH = re.compile(r"achtemp\[(\d+)\] = \(([-+0-9.eE]+),([-+0-9.eE]+)\)")
+_TIME = re.compile(r"Chrono Time Taken \*+= ([0-9.eE+-]+) secs")
+
+
+def run_reference_binary(number_bands, nvband, ncouls, nodes_per_group, threads=None, timeout=900):
+    """Runs the unmodified reference driver; returns (achtemp[3], seconds, stdout)."""
+    if not _build.build_reference():
+        return None
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    env.setdefault("OMP_STACKSIZE", "64M")
+
+    def _unlimit_stack():
+        try:
+            resource.setrlimit(resource.RLIMIT_STACK, (resource.RLIM_INFINITY, resource.RLIM_INFINITY))
+        except (ValueError, OSError):
+            pass
+
+    r = subprocess.run([str(_build.REF_BIN), str(number_bands), str(nvband), str(ncouls),
+                        str(nodes_per_group)], capture_output=True, text=True, env=env,
+                       timeout=timeout, preexec_fn=_unlimit_stack)
+    ach = np.zeros(3, np.complex128)
+    for m in _ACH.finditer(r.stdout):
+        ach[int(m.group(1))] = complex(float(m.group(2)), float(m.group(3)))
+    t = _TIME.search(r.stdout)
+    return ach, (float(t.group(1)) if t else float("nan")), r.stdout

@@ -1,0 +1,86 @@
+"""Regenerates the golden fixtures from the reference itself.
+
+Needs the reference checkout (REFERENCE_ROOT, default /root/reference); the
+fixtures it writes are committed so the tests run without it.
+
+  gpp_reference_constfill.json  achtemp printed by the unmodified
+      BGW-Kernels/gppKer.cpp driver (constant fill) at several shapes and
+      OpenMP thread counts, plus the closed form of the constant fill.
+  gpp_flagocc_<case>.npz        ssx_array / sch_array per (band, column,
+      frequency) from the reference's own flagOCC_solver
+      (BGW-Kernels/gppKer.cpp:130-159) on seeded inputs that
+      fortkernels-_gb300/workload.py regenerates from the recorded seed.
+
+Run:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import pathlib
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT / "fortkernels-_gb300"))
+sys.path.insert(0, str(ROOT))
+
+import workload as W  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+CONST_SHAPES = [(16, 2, 1024, 8), (32, 4, 2048, 10), (64, 1, 4096, 16), (128, 2, 8192, 20)]
+FLAGOCC_CASES = {
+    # name: (number_bands, ncouls, ngpown, seed, stress)
+    "random_a": (3, 512, 32, 7, False),
+    "random_b": (2, 999, 17, 21, False),
+    "stress_a": (3, 512, 32, 8, True),
+}
+
+
+def closed_form(nb, nvband, ncouls, npg):
+    ng = ncouls // npg
+    wt = 0.5 + 0.5j
+    wx = W.wx_frequencies()
+    delw = wt * np.conj(wx - wt) / np.abs(wx - wt) ** 2
+    ach = nb * ng * ncouls * 0.5 * 0.5 * delw * (0.5 + 0.5j)
+    asx = nvband * ng * ncouls * 0.5 * (wt ** 2 * (0.5 + 0.5j) / wx ** 2)
+    return ach, asx
+
+
+def igp_map(prob):
+    out = []
+    for ind in prob.inv_igp_index:
+        out.append(prob.ncouls - 1 if ind == prob.ncouls else int(prob.indinv[ind]))
+    return np.array(out, dtype=np.int32)
+
+
+def main():
+    if O.reference_lib() is None:
+        sys.exit("reference checkout not found; set REFERENCE_ROOT")
+    rows = []
+    for shape in CONST_SHAPES:
+        for threads in (1, 4):
+            ach, secs, _ = O.run_reference_binary(*shape, threads=threads)
+            exact, exact_asx = closed_form(*shape)
+            rows.append({
+                "shape": list(shape), "omp_threads": threads,
+                "achtemp": [[z.real, z.imag] for z in ach],
+                "closed_form_achtemp": [[z.real, z.imag] for z in exact],
+                "closed_form_asxtemp": [[z.real, z.imag] for z in exact_asx],
+            })
+            print(shape, threads, ach)
+    (HERE / "gpp_reference_constfill.json").write_text(json.dumps({
+        "source": "BGW-Kernels/gppKer.cpp, unmodified, g++ -O3 -fopenmp -std=c++11; stdout achtemp (15 digits)",
+        "runs": rows}, indent=1))
+
+    for name, (nb, nc, ng, seed, stress) in FLAGOCC_CASES.items():
+        prob = W.gpp_random(nb, nb, nc, ng, seed, stress=stress)
+        ssx, sch = O.reference_flagocc_columns(prob, igp_map(prob))
+        np.savez_compressed(HERE / f"gpp_flagocc_{name}.npz", ssx=ssx, sch=sch,
+                            meta=np.array([nb, nc, ng, seed, int(stress)]))
+        print(name, np.abs(sch).max(), np.abs(ssx).max())
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+"""The CPU oracle pinned against the reference's own outputs and closed forms.
+
+Fixtures in tests/golden/ come from the reference itself
+(tests/golden/make_golden.py): the unmodified BGW-Kernels/gppKer.cpp driver's
+printed achtemp on the constant fill, and its flagOCC_solver's per-column
+sums on seeded inputs.
+"""
+import json
+import pathlib
+
+import numpy as np
+import pytest
+
+import workload as W
+from conftest import rel_err
+from oracle import oracle as O
+
+GOLD = pathlib.Path(__file__).resolve().parent / "golden"
+
+
+def _igp_map(prob):
+    return np.array([prob.ncouls - 1 if i == prob.ncouls else int(prob.indinv[i])
+                     for i in prob.inv_igp_index], dtype=np.int32)
+
+
+@pytest.mark.parametrize("run", json.loads((GOLD / "gpp_reference_constfill.json").read_text())["runs"],
+                         ids=lambda r: f"{'x'.join(map(str, r['shape']))}-t{r['omp_threads']}")
+def test_oracle_matches_reference_driver_constant_fill(run):
+    nb, nvb, nc, npg = run["shape"]
+    if nb * nc * (nc // npg) > 2e8:
+        pytest.skip("large constant-fill shape checked in the slow tier")
+    prob = W.gpp_constant(nb, nvb, nc, npg)
+    ach, asx, n1 = O.gpp(prob)
+    ref = np.array([complex(*z) for z in run["achtemp"]])
+    exact = np.array([complex(*z) for z in run["closed_form_achtemp"]])
+    exact_asx = np.array([complex(*z) for z in run["closed_form_asxtemp"]])
+    # the oracle's compensated sums sit on the closed form ...
+    assert rel_err(ach, exact).max() < 1e-15
+    assert rel_err(asx, exact_asx).max() < 1e-15
+    # ... and the reference's printed values within its own rounding (15 digits,
+    # plain OpenMP sums: up to ~1e-12 relative at these shapes)
+    assert rel_err(ref, ach).max() < 2e-12
+    # acht_n1_loc sums to achtemp[2]
+    assert abs(n1.sum() - ach[2]) / abs(ach[2]) < 1e-14
+
+
+def test_oracle_production_constant_fill_closed_form():
+    # the largest golden shape (config 128 2 8192 20), compensated oracle vs exact
+    runs = json.loads((GOLD / "gpp_reference_constfill.json").read_text())["runs"]
+    run = [r for r in runs if r["shape"] == [128, 2, 8192, 20]][0]
+    prob = W.gpp_constant(128, 2, 8192, 20)
+    ach, asx, _ = O.gpp(prob)
+    exact = np.array([complex(*z) for z in run["closed_form_achtemp"]])
+    ref = np.array([complex(*z) for z in run["achtemp"]])
+    assert rel_err(ach, exact).max() < 1e-15
+    assert rel_err(ref, exact).max() < 2e-12
+
+
+@pytest.mark.parametrize("name", ["random_a", "random_b", "stress_a"])
+def test_oracle_terms_match_reference_flagocc(name):
+    g = np.load(GOLD / f"gpp_flagocc_{name}.npz")
+    nb, nc, ng, seed, stress = (int(x) for x in g["meta"])
+    prob = W.gpp_random(nb, nb, nc, ng, seed, stress=bool(stress))
+    sch, ssx = O.gpp_columns(prob)
+    scale_sch = np.abs(g["sch"]).max()
+    scale_ssx = np.abs(g["ssx"]).max()
+    assert np.abs(sch - g["sch"]).max() / scale_sch < 1e-13
+    assert np.abs(ssx - g["ssx"]).max() / scale_ssx < 1e-13
+
+
+def test_oracle_unoccupied_term_equals_occupied_sch():
+    # achtemp semantics are uniform over bands: the hot-loop term
+    # (gppKer.cpp:396-407) and flagOCC's sch (:38-40, :64) agree
+    prob = W.gpp_random(4, 0, 300, 11, 5)
+    sch_unocc, _ = O.gpp_columns(prob)
+    prob.nvband = 4
+    sch_occ, _ = O.gpp_columns(prob)
+    assert np.abs(sch_unocc - sch_occ).max() / np.abs(sch_occ).max() < 1e-14
+
+
+def test_port_agrees_with_compensated_oracle():
+    prob = W.gpp_random(12, 2, 1536, 60, 3)
+    a1, s1, n1 = O.gpp(prob)
+    a2, s2, n2 = O.gpp(prob, port=True)
+    assert rel_err(a2, a1).max() < 1e-12
+    assert rel_err(s2, s1).max() < 1e-12
+    assert np.abs(n2 - n1).max() / np.abs(n1).max() < 1e-12
+
+
+def test_oracle_thread_count_independent():
+    prob = W.gpp_random(6, 2, 777, 19, 4, stress=True)
+    r1 = O.gpp(prob, nthreads=1)
+    r4 = O.gpp(prob, nthreads=4)
+    for x, y in zip(r1, r4):
+        assert np.array_equal(x, y)
+
+
+def test_oracle_band_ranges_sum():
+    prob = W.gpp_random(10, 3, 512, 16, 9)
+    full = O.gpp(prob)
+    a = O.gpp(prob, 0, 4)
+    b = O.gpp(prob, 4, 10)
+    assert rel_err(a[0] + b[0], full[0]).max() < 1e-14
+    assert rel_err(a[1] + b[1], full[1]).max() < 1e-14
+    assert np.array_equal(full[2][:4], a[2][:4]) and np.array_equal(full[2][4:], b[2][4:])
+
+
+def test_oracle_rejects_reference_out_of_bounds_indices():
+    prob = W.gpp_random(2, 1, 64, 4, 1)
+    prob.inv_igp_index = np.array([0, 1, 65, 3], np.int32)  # indigp > ncouls
+    with pytest.raises(O.OracleError):
+        O.gpp(prob)
+    prob.inv_igp_index = np.array([0, 1, 2, 3], np.int32)
+    prob.indinv = np.arange(64, dtype=np.int32)
+    prob.indinv[2] = 64  # igp == ncouls: the reference reads past the row
+    with pytest.raises(O.OracleError):
+        O.gpp(prob)
+
+
+def test_oracle_skips_columns_like_reference():
+    # igp < 0 or igp > ncouls: the column is skipped (gppKer.cpp:328)
+    prob = W.gpp_random(3, 1, 64, 4, 2)
+    prob.indinv = prob.indinv.copy()
+    target = prob.inv_igp_index[1]
+    prob.indinv[target] = -5
+    sch, _ = O.gpp_columns(prob)
+    assert np.all(sch[:, 1, :] == 0)
+    ach, _, _ = O.gpp(prob)
+    ach_ref = np.zeros(3, complex)
+    for my_igp in (0, 2, 3):
+        igp = prob.ncouls - 1 if prob.inv_igp_index[my_igp] == prob.ncouls else prob.indinv[prob.inv_igp_index[my_igp]]
+        ach_ref += (sch[:, my_igp, :] * prob.vcoul[igp]).sum(axis=0)
+    assert rel_err(ach, ach_ref).max() < 1e-13
+
+
+def test_oracle_exact_pole_is_dropped():
+    # wtilde == wx exactly: |wdiff|^2 = 0, the reference's delw is NaN and the
+    # guard drops the term; ssx is 0 (its delwr > to1 test is false for NaN)
+    prob = W.gpp_random(2, 2, 128, 8, 6)
+    prob.wtilde_array = prob.wtilde_array.copy()
+    prob.wtilde_array[3, 5] = complex(prob.wx_array[1], 0.0)
+    ach, asx, n1 = O.gpp(prob)
+    assert np.all(np.isfinite(ach)) and np.all(np.isfinite(asx)) and np.all(np.isfinite(n1))
+
+
+def test_ff_oracle_matches_matmul_and_closed_form():
+    p = W.ff_random(5, 257, 7, 3, 4)
+    out = O.ff_schdt(p)
+    igp = p.indinv[p.inv_igp_index]
+    tempz = np.einsum("fgi,ni->fgn", p.I_epsR, p.aqsntemp)
+    ref = np.einsum("fgn,ng->nf", tempz, np.conj(p.aqsmtemp[:, igp]))
+    assert np.abs(out.reshape(5, 3) - ref).max() / np.abs(ref).max() < 1e-13
+    c = W.ff_constant(4, 100, 6, 2)
+    outc = O.ff_schdt(c).reshape(4, 2)
+    exact = 6 * 100 * 0.5 * (0.5 + 0.5j)
+    assert np.abs(outc - exact).max() / abs(exact) < 1e-15

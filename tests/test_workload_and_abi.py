@@ -1,0 +1,119 @@
+"""Host-side tests: the seeded generator, the C-ABI library's exports, and
+argument validation that happens before any device work."""
+import ctypes as C
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+import workload as W
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def test_splitmix64_known_answer():
+    # SplitMix64 from state 0 (Steele, Lea, Flood 2014): first output
+    z = W._fmix(np.array([W.GOLDEN], dtype=np.uint64))
+    assert int(z[0]) == 0xE220A8397B1DCDAF
+    z2 = W._fmix(np.array([(2 * W.GOLDEN) & W.MASK], dtype=np.uint64))
+    assert int(z2[0]) == 0x6E789E6AA1B965F4
+
+
+def test_fill_is_deterministic_and_chunk_independent():
+    a = W.fill_complex(5, W.AID_AQSM, 10_000, (-1, 1), (-1, 1))
+    b = W.fill_complex(5, W.AID_AQSM, 10_000, (-1, 1), (-1, 1))
+    assert np.array_equal(a, b)
+    # a prefix equals a shorter fill (counter-based stream)
+    c = W.fill_complex(5, W.AID_AQSM, 1234, (-1, 1), (-1, 1))
+    assert np.array_equal(a[:1234], c)
+    assert a.real.min() >= -1 and a.real.max() < 1
+    w = W.fill_complex(1, W.AID_WTILDE, 50_000, (0.5, 5.0), (-0.1, 0.1))
+    assert w.real.min() >= 0.5 and w.real.max() < 5 and np.abs(w.imag).max() <= 0.1
+    # different array ids are different streams
+    assert not np.array_equal(a, W.fill_complex(5, W.AID_AQSN, 10_000, (-1, 1), (-1, 1)))
+
+
+def test_stress_moves_five_percent_near_poles():
+    wt = W.fill_complex(2, W.AID_WTILDE, 200_000, (0.5, 5.0), (-0.1, 0.1))
+    moved = W.stress_wtilde(wt, W.wx_frequencies(), 2)
+    assert 0.045 < moved / wt.size < 0.055
+    d = np.min(np.abs(wt.real[:, None] - W.wx_frequencies()[None, :]), axis=1)
+    assert np.sum(d < 1e-3) >= moved
+
+
+def test_reference_shapes_and_index_maps():
+    sh = W.gpp_shape(**W.GPP_PRODUCTION)
+    assert sh["ngpown"] == 1638
+    inv, indinv = W.gpp_index_maps(32768, 1638)
+    assert inv[0] == 32768 // 1638 and inv[-1] == 32768  # clamped to ncouls-1 downstream
+    assert np.array_equal(W.wx_frequencies(), [3.0, 4.0, 5.0])
+    shapes = W.batched_shapes()
+    assert len(shapes) == 48
+    for s in shapes:
+        assert 64 <= s["number_bands"] <= 512 and 4096 <= s["ncouls"] <= 32768
+        assert s["ncouls"] % 256 == 0 and 10 <= s["nodes_per_group"] <= 40 and 1 <= s["nvband"] <= 8
+
+
+def _declared_functions():
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*(?:int|const char\*|size_t|void)\s+(sigma_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    import build as B
+    return B.build()
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    lib = C.CDLL(str(libpath))
+    declared = _declared_functions()
+    assert len(declared) >= 10
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, missing
+    import sigma_gb300
+    assert set(declared) <= set(sigma_gb300.exported_symbols())
+
+
+def test_status_strings(libpath):
+    lib = C.CDLL(str(libpath))
+    lib.sigma_status_string.restype = C.c_char_p
+    assert lib.sigma_status_string(0) == b"ok"
+    assert lib.sigma_status_string(-2) == b"index out of range"
+
+
+def test_validation_precedes_device_work(libpath):
+    """Bad shapes and out-of-bounds index maps are rejected on the host with
+    the reference's failure points, before the device is touched."""
+    lib = C.CDLL(str(libpath))
+    f = lib.sigma_gpp_plan_create
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                  C.c_void_p, C.c_int, C.c_int]
+    h = C.c_void_p()
+    nc, ng = 64, 4
+    inv = np.array([16, 32, 48, 64], np.int32)
+    indinv = np.arange(nc, dtype=np.int32)
+    args = lambda nb, nv, nc_, ng_, ns, ne, inv_, ind_, prec: f(C.byref(h), nb, nv, nc_, ng_, ns, ne,
+                                                                inv_.ctypes.data, ind_.ctypes.data,
+                                                                len(ind_), prec)
+    assert args(2, 1, nc, ng, 0, 4, inv, indinv, 0) == -1      # nend - nstart != 3
+    assert args(2, 3, nc, ng, 0, 3, inv, indinv, 0) == -1      # nvband > number_bands
+    assert args(2, 1, 3, ng, 0, 3, inv, indinv, 0) == -1       # ngpown > ncouls
+    assert args(2, 1, nc, ng, 0, 3, inv, indinv, 7) == -8      # unknown precision
+    bad = inv.copy()
+    bad[2] = 65                                                  # indigp > ncouls
+    assert args(2, 1, nc, ng, 0, 3, bad, indinv, 0) == -2
+    ind_bad = indinv.copy()
+    ind_bad[32] = 64                                             # igp == ncouls
+    assert args(2, 1, nc, ng, 0, 3, inv, ind_bad, 0) == -2
+    st = args(2, 1, nc, ng, 0, 3, inv, indinv, 0)
+    # valid arguments reach the device step: OK on a GPU host, no-device here
+    assert st in (0, -7, -4)
+    if st == 0:
+        lib.sigma_gpp_plan_destroy.argtypes = [C.c_void_p]
+        lib.sigma_gpp_plan_destroy(h)
