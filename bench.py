@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Benchmark of the sigma GPP hot path on GB300.
+
+Workload: the GPP sigma sum of BGW-Kernels/gppKer.cpp at its production shape
+(512 bands, nvband 2, ncouls 32768, nodes_per_group 20 -> ngpown 1638, three
+frequencies), seeded synthetic inputs (aqsm, aqsn, I_eps ~ U(-1,1) per part,
+wtilde re ~ U(0.5,5) im ~ U(-0.1,0.1), vcoul ~ U(0.1,10)) generated on the
+device.  One step = one full evaluation of achtemp / asxtemp / acht_n1_loc.
+
+  value      FP64 drop-in, device-resident inputs, Gterms/s
+             (terms = number_bands * valid columns * ncouls * 3)
+  e2e        the same through the host-pointer C ABI (sigma_gpp_fp64) from
+             pinned host buffers: the H2D copy of every input and the D2H of
+             the outputs happen inside each timed step
+  mixed      the mixed-precision path on the same inputs, its Gterms/s and
+             the relative error of every achtemp / asxtemp output against the
+             FP64 path (and on the stress fill with 5% near-pole wtilde)
+  roofline   the main FP64 kernel: 27 flop per term (algorithmic count of the
+             reference's term) over its CUDA-event time, against the FP64 FMA
+             peak measured on this device at start-up
+  cpu_baseline  the reference algorithm (oracle port with the reference's
+             loop nest and OpenMP schedule) on a bounded band sample, all host
+             cores
+
+--impl reference times the reference's CPU implementation of the same
+workload on the host cores (bounded band samples per step) and prints the
+same line with "impl": "reference".
+
+Multi-GPU (torchrun): every rank evaluates its own instance (seed 1 + rank)
+with no collective on the data path; value is all ranks' terms over the
+slowest rank's time (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+for _p in (str(ROOT / "fortkernels-_gb300"), str(ROOT)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "GPP Gterms/s FP64 vs mixed @≤1e-6 rel err, % of measured peak; FF TF/s"
+UNIT = "Gterms/s"
+WORKLOAD = "GPP sigma sum, FP64 drop-in, 512 bands x 1638 columns x 32768 g-vectors x 3 frequencies"
+FLOP_PER_TERM = 27  # algorithmic count of one (n1, igp, ig, iw) term of the reference
+NB, NVB, NC, NPG = 512, 2, 32768, 20
+NG = NC // NPG
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={','.join(self.FIELDS)}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_sample_problem(seed, bands):
+    """Host arrays for the reference CPU code: the last `bands` bands of the
+    production instance (non-occupied bands, 99.6% of the terms) and all
+    columns, generated with the host twin of the device fill."""
+    import workload as W
+    lo = NB - bands
+    aqsm = np.zeros((NB, NC), np.complex128)
+    aqsn = np.zeros((NB, NC), np.complex128)
+    aqsm[lo:] = W.fill_complex(seed, W.AID_AQSM, bands * NC, (-1, 1), (-1, 1), start=lo * NC).reshape(bands, NC)
+    aqsn[lo:] = W.fill_complex(seed, W.AID_AQSN, bands * NC, (-1, 1), (-1, 1), start=lo * NC).reshape(bands, NC)
+    ieps = W.fill_complex(seed, W.AID_IEPS, NG * NC, (-1, 1), (-1, 1)).reshape(NG, NC)
+    wt = W.fill_complex(seed, W.AID_WTILDE, NG * NC, (0.5, 5.0), (-0.1, 0.1)).reshape(NG, NC)
+    vcoul = W.fill_real(seed, W.AID_VCOUL, NC, 0.1, 10.0)
+    inv, indinv = W.gpp_index_maps(NC, NG)
+    return W.GppProblem(NB, NVB, NC, NG, inv, indinv, W.wx_frequencies(), aqsm, aqsn, ieps, wt, vcoul)
+
+
+def time_cpu_reference(prob, band_lo, band_hi, threads):
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    O.gpp(prob, band_lo, band_hi, nthreads=threads, port=True)
+    dt = time.perf_counter() - t0
+    terms = (band_hi - band_lo) * NG * NC * 3
+    return terms / dt / 1e9, dt
+
+
+def cpu_baseline(prob, target_s=15.0):
+    """Bounded sample of the production workload on all host cores."""
+    threads = os.cpu_count() or 1
+    calib = 2
+    _, dt = time_cpu_reference(prob, NB - calib, NB, threads)
+    bands = max(2, min(64, int(target_s / (dt / calib))))
+    rate, dt = time_cpu_reference(prob, NB - bands, NB, threads)
+    return {"value": round(rate, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"bands {NB - bands}..{NB - 1} of the production instance (all 1638 columns, "
+                      f"32768 g-vectors, 3 frequencies; {bands * NG * NC * 3:.3e} terms, {dt:.1f} s); "
+                      "oracle port of BGW-Kernels/gppKer.cpp:303-439 with its OpenMP dynamic schedule, "
+                      "g++ -O2 -fopenmp; the reference's own binary needs its source checkout, absent "
+                      "on this host"}
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    prob = cpu_sample_problem(1, 32)
+    # size one step to ~3 s of CPU work
+    _, dt2 = time_cpu_reference(prob, NB - 2, NB, threads)
+    bands = max(1, min(32, int(3.0 / (dt2 / 2))))
+    for _ in range(args.warmup):
+        time_cpu_reference(prob, NB - bands, NB, threads)
+    times = []
+    for _ in range(args.steps):
+        _, dt = time_cpu_reference(prob, NB - bands, NB, threads)
+        times.append(dt)
+    terms = bands * NG * NC * 3
+    total = sum(times)
+    value = terms * len(times) / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total / len(times), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "number_bands": NB, "nvband": NVB, "ncouls": NC,
+                   "ngpown": NG, "sample_bands_per_step": bands},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{bands} non-occupied bands per step, all columns and g-vectors; "
+                                   "the reference's own binary needs the reference checkout, absent "
+                                   "on this host, so the oracle port of its loop nest runs"},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+class Instance:
+    def __init__(self, S, W, torch, seed, stress=False):
+        d = "cuda"
+        self.aqsm = torch.empty(2 * NB * NC, dtype=torch.float64, device=d)
+        self.aqsn = torch.empty_like(self.aqsm)
+        self.ieps = torch.empty(2 * NG * NC, dtype=torch.float64, device=d)
+        self.wt = torch.empty_like(self.ieps)
+        self.vcoul = torch.empty(NC, dtype=torch.float64, device=d)
+        S.fill_complex_device(self.aqsm.data_ptr(), NB * NC, seed, W.AID_AQSM, (-1, 1), (-1, 1))
+        S.fill_complex_device(self.aqsn.data_ptr(), NB * NC, seed, W.AID_AQSN, (-1, 1), (-1, 1))
+        S.fill_complex_device(self.ieps.data_ptr(), NG * NC, seed, W.AID_IEPS, (-1, 1), (-1, 1))
+        S.fill_complex_device(self.wt.data_ptr(), NG * NC, seed, W.AID_WTILDE, (0.5, 5.0), (-0.1, 0.1))
+        if stress:
+            S.fill_stress_device(self.wt.data_ptr(), NG * NC, seed, W.AID_STRESS, W.wx_frequencies())
+        S.fill_real_device(self.vcoul.data_ptr(), NC, seed, W.AID_VCOUL, 0.1, 10.0)
+        self.wx = torch.tensor(W.wx_frequencies(), dtype=torch.float64, device=d)
+        self.inv, self.indinv = W.gpp_index_maps(NC, NG)
+        self.ach = torch.zeros(6, dtype=torch.float64, device=d)
+        self.asx = torch.zeros(6, dtype=torch.float64, device=d)
+        self.n1 = torch.zeros(2 * NB, dtype=torch.float64, device=d)
+
+    def run(self, plan, stream):
+        plan.execute(self.wx, self.aqsm, self.aqsn, self.ieps, self.wt, self.vcoul, self.ach,
+                     self.asx, self.n1, stream=stream)
+
+    def outputs(self):
+        return tuple(t.cpu().numpy().view(np.complex128).copy() for t in (self.ach, self.asx, self.n1))
+
+
+def rel(a, b):
+    return [float(x) for x in (np.abs(a - b) / np.abs(b))]
+
+
+def timed(torch, dist, world, fn, steps, stream):
+    """Runs fn() `steps` times between barriers + synchronize; CUDA-event ms, max over ranks."""
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def profile_traffic_per_term():
+    """DRAM bytes per term of the main FP64 kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "gpp_sch_fp64_production.md"
+    if not p.exists():
+        return None
+    m = re.search(r"dram_bytes_per_term:\s*([0-9.eE+-]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import sigma_gb300 as S
+    import workload as W
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    S.load()
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    fp64_peak, fp32_peak = S.measure_fma_peaks(sptr)
+    inst = Instance(S, W, torch, seed=1 + rank)
+    plan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_FP64)
+    valid, terms = plan.info()
+
+    # ---- device-resident FP64 drop-in
+    for _ in range(args.warmup):
+        inst.run(plan, sptr)
+    plan.set_timing(True)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ms = timed(torch, dist, world, lambda: inst.run(plan, sptr), args.steps, stream)
+    clk = clocks.stop()
+    kt = plan.timing()
+    plan.set_timing(False)
+    fp64_out = inst.outputs()
+    ms_step = ms / args.steps
+    value = terms * world / (ms_step * 1e-3) / 1e9
+    main_s = kt["main_ms"] / max(1, kt["executions"]) * 1e-3
+    achieved = FLOP_PER_TERM * terms / main_s / 1e12
+    tpt = profile_traffic_per_term()
+
+    # ---- end to end through the host C ABI (pinned host buffers)
+    host = {k: torch.empty(getattr(inst, k).numel(), dtype=torch.float64, pin_memory=True)
+            for k in ("aqsm", "aqsn", "ieps", "wt", "vcoul")}
+    for k, t in host.items():
+        t.copy_(getattr(inst, k))
+    inv = np.ascontiguousarray(inst.inv, np.int32)
+    indinv = np.ascontiguousarray(inst.indinv, np.int32)
+    wx = np.ascontiguousarray(W.wx_frequencies())
+    h_ach = torch.zeros(6, dtype=torch.float64, pin_memory=True)
+    h_asx = torch.zeros(6, dtype=torch.float64, pin_memory=True)
+    h_n1 = torch.zeros(2 * NB, dtype=torch.float64, pin_memory=True)
+    lib = S.load()
+
+    def e2e_step():
+        st = lib.sigma_gpp_fp64(NB, NVB, NC, NG, 0, 3, inv.ctypes.data, indinv.ctypes.data,
+                                wx.ctypes.data, 1.0, host["aqsm"].data_ptr(), host["aqsn"].data_ptr(),
+                                host["ieps"].data_ptr(), host["wt"].data_ptr(), host["vcoul"].data_ptr(),
+                                h_ach.data_ptr(), h_asx.data_ptr(), h_n1.data_ptr(), sptr)
+        if st != 0:
+            raise S.SigmaError(st, "sigma_gpp_fp64")
+
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(min(args.warmup, 2)):
+        e2e_step()
+    ms_e2e = timed(torch, dist, world, e2e_step, e2e_steps, stream)
+    e2e_value = terms * world / (ms_e2e / e2e_steps * 1e-3) / 1e9
+    h2d = sum(t.numel() * 8 for t in host.values()) + wx.nbytes
+    d2h = (6 + 6 + 2 * NB) * 8
+    e2e_match = bool(np.array_equal(h_ach.numpy().view(np.complex128), fp64_out[0]))
+    del host
+    S.shutdown()  # frees the drop-in's cached device copy of the inputs
+
+    # ---- mixed precision on the same inputs, then the stress fill
+    mplan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_MIXED)
+    for _ in range(args.warmup):
+        inst.run(mplan, sptr)
+    mplan.set_timing(True)
+    msteps = max(args.steps, 10)
+    ms_mixed = timed(torch, dist, world, lambda: inst.run(mplan, sptr), msteps, stream)
+    mkt = mplan.timing()
+    mixed_out = inst.outputs()
+    mixed_value = terms * world / (ms_mixed / msteps * 1e-3) / 1e9
+    mixed_err = {"achtemp": rel(mixed_out[0], fp64_out[0]), "asxtemp": rel(mixed_out[1], fp64_out[1]),
+                 "acht_n1_loc_normwise": float(np.linalg.norm(mixed_out[2] - fp64_out[2]) /
+                                               np.linalg.norm(fp64_out[2]))}
+    mixed_main_s = mkt["main_ms"] / max(1, mkt["executions"]) * 1e-3
+    cpu_prob = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # host copy of the instance for the CPU baseline: 64 trailing bands + all columns
+        c = lambda t, r: t.view(-1, 2).cpu().numpy().view(np.complex128).reshape(r, NC)
+        aqsm = np.zeros((NB, NC), np.complex128)
+        aqsn = np.zeros((NB, NC), np.complex128)
+        aqsm[NB - 64:] = c(inst.aqsm, NB)[NB - 64:]
+        aqsn[NB - 64:] = c(inst.aqsn, NB)[NB - 64:]
+        cpu_prob = W.GppProblem(NB, NVB, NC, NG, inst.inv, inst.indinv, W.wx_frequencies(), aqsm, aqsn,
+                                c(inst.ieps, NG), c(inst.wt, NG), inst.vcoul.cpu().numpy())
+    del inst
+    torch.cuda.empty_cache()
+    sinst = Instance(S, W, torch, seed=W.GPP_STRESS_SEED, stress=True)
+    sinst.run(plan, sptr)
+    s64 = sinst.outputs()
+    sinst.run(mplan, sptr)
+    smx = sinst.outputs()
+    stress_err = {"achtemp": rel(smx[0], s64[0]), "asxtemp": rel(smx[1], s64[1])}
+    del sinst
+    plan.close()
+    mplan.close()
+    torch.cuda.empty_cache()
+
+    worst = max(max(mixed_err["achtemp"]), max(mixed_err["asxtemp"]),
+                max(stress_err["achtemp"]), max(stress_err["asxtemp"]))
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded SplitMix64 fill of the production shape; no dataset exists)",
+        "config": {"workload": WORKLOAD, "number_bands": NB, "nvband": NVB, "ncouls": NC,
+                   "nodes_per_group": NPG, "ngpown": NG, "valid_columns": valid,
+                   "terms_per_step": terms, "l2": "inputs (2.25 GB) larger than L2 (129 MB)",
+                   "parallelism": f"replicas x{world} (one independent instance per GPU)"},
+        "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                "path": "sigma_gpp_fp64 host C ABI, pinned buffers", "matches_device_path": e2e_match},
+        "roofline": {"bound": "fp64", "kernel": "sch_fp64_kernel",
+                     "achieved": round(achieved, 4), "peak": round(fp64_peak, 4), "unit": "TFLOP/s",
+                     "frac": round(achieved / fp64_peak, 4),
+                     "traffic": (round(tpt * terms) if tpt else None),
+                     "flop_per_term": FLOP_PER_TERM,
+                     "kernel_ms_per_launch": round(main_s * 1e3, 3),
+                     "peak_source": "FP64 FMA throughput measured on this device by "
+                                    "sigma_measure_fma_peaks (not in the driver's peak file)"},
+        "mixed": {"value": round(mixed_value, 4), "unit": UNIT,
+                  "speedup_vs_fp64": round(mixed_value / value, 3),
+                  "ms_per_step": round(ms_mixed / msteps, 3),
+                  "kernel_ms_per_launch": round(mixed_main_s * 1e3, 3),
+                  "rel_err_vs_fp64": mixed_err, "stress_rel_err_vs_fp64": stress_err,
+                  "max_rel_err": worst, "within_1e-6": worst <= 1e-6,
+                  "roofline": {"bound": "fp32", "achieved": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12, 3),
+                               "peak": round(fp32_peak, 3), "unit": "TFLOP/s",
+                               "frac": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12 / fp32_peak, 4)}},
+        "peaks_measured": {"fp64_tflops": round(fp64_peak, 4), "fp32_tflops": round(fp32_peak, 3)},
+        "clocks": clk,
+        "gpu_launches": int(kt["launches"]) * args.steps,
+    }
+    if cpu_prob is not None:
+        line["cpu_baseline"] = cpu_baseline(cpu_prob)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    return run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -20,17 +20,27 @@ struct sigma_gpp_plan_s {
   int valid_columns = 0;
   int sch_grid = 0, ssx_grid = 0;
   sigma::GppWork sch{}, ssx{};
+  sigma::MixedPrep prep{};    // FP32 operands of the mixed path (unused for FP64)
   void* block = nullptr;      // one device allocation for everything below
   int* igp_of = nullptr;      // [ng]
-  int* counters = nullptr;    // [2]
+  int* counters = nullptr;    // [2] item counters, [2] device status word
   double2* acht_n1 = nullptr; // [nb + nvband][3]
   std::vector<int> host_inv, host_indinv;  // kept for the host drop-in's plan cache
+  // optional per-launch timing: events around the main pass, the occupied-band
+  // pass and the rest (pre-pass and reductions) of each execution
+  bool timing = false;
+  std::vector<cudaEvent_t> events;  // 4 per recorded execution
+  int recorded = 0;
 };
+
+namespace {
+constexpr int kMaxTimedExecutions = 256;
+}
 
 namespace sigma {
 namespace {
 
-constexpr int kSsxBN = 8, kSsxBP = 256;
+constexpr int kSsxBP = 256;
 constexpr int kItemsPerSlot = 48;  // work items per resident CTA (load balance of the tail)
 
 void size_work(GppWork& w, int band_begin, int band_count, int bn, int bp, int nc, int ng,
@@ -131,7 +141,8 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   const bool mixed = precision == SIGMA_PREC_MIXED;
   p->sch_grid = sms * (mixed ? sch_blocks_per_sm_mixed() : sch_blocks_per_sm_fp64());
   p->ssx_grid = sms * (mixed ? ssx_blocks_per_sm_mixed() : ssx_blocks_per_sm_fp64());
-  size_work(p->sch, 0, number_bands, kBN, kBP, ncouls, ngpown, p->sch_grid, kItemsPerSlot);
+  size_work(p->sch, 0, number_bands, kBN, mixed ? kBPM : kBP, ncouls, ngpown, p->sch_grid,
+            kItemsPerSlot);
   size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
   if (p->sch.n_items < p->sch_grid) p->sch_grid = p->sch.n_items;
   if (p->ssx.n_items < p->ssx_grid) p->ssx_grid = p->ssx.n_items;
@@ -141,7 +152,13 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   const size_t b_n1 = align_up(sizeof(double2) * (size_t)(number_bands + nvband) * kNW, 256);
   const size_t b_sch = align_up(sizeof(double2) * (size_t)p->sch.n_items * kBN * kNW, 256);
   const size_t b_ssx = align_up(sizeof(double2) * (size_t)p->ssx.n_items * kSsxBN * kNW, 256);
-  cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx);
+  const int nc_pad = (ncouls + kCK - 1) / kCK * kCK;
+  const size_t col_elems = mixed ? (size_t)p->sch.n_col_blocks * kBPM * nc_pad : 0;
+  const size_t band_elems = mixed ? (size_t)p->sch.n_band_blocks * kBN * nc_pad : 0;
+  const size_t b_colA = align_up(sizeof(float4) * col_elems, 256);
+  const size_t b_colB = align_up(sizeof(float2) * col_elems, 256);
+  const size_t b_band = align_up(sizeof(float2) * band_elems, 256);
+  cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx + b_colA + b_colB + b_band);
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_last_cuda_error(e, "cudaMalloc(plan)", __LINE__);
@@ -156,6 +173,14 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   p->ssx.partial = reinterpret_cast<double2*>(base + b_igp + b_cnt + b_n1 + b_sch);
   p->sch.counter = p->counters;
   p->ssx.counter = p->counters + 1;
+  {
+    char* q = base + b_igp + b_cnt + b_n1 + b_sch + b_ssx;
+    p->prep.colA = mixed ? reinterpret_cast<float4*>(q) : nullptr;
+    p->prep.colB = mixed ? reinterpret_cast<float2*>(q + b_colA) : nullptr;
+    p->prep.band = mixed ? reinterpret_cast<float2*>(q + b_colA + b_colB) : nullptr;
+    p->prep.nc_pad = nc_pad;
+    p->prep.status = p->counters + 2;
+  }
   e = cudaMemcpy(p->igp_of, igp_of.data(), sizeof(int) * ngpown, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     set_last_cuda_error(e, "cudaMemcpy(igp_of)", __LINE__);
@@ -174,6 +199,7 @@ extern "C" int sigma_gpp_plan_destroy(sigma_gpp_plan plan) {
   int cur = 0;
   cudaGetDevice(&cur);
   cudaSetDevice(plan->device);
+  for (cudaEvent_t e : plan->events) cudaEventDestroy(e);
   if (plan->block) cudaFree(plan->block);
   cudaSetDevice(cur);
   delete plan;
@@ -185,6 +211,57 @@ extern "C" int sigma_gpp_plan_info(sigma_gpp_plan plan, int* valid_columns, long
   if (valid_columns) *valid_columns = plan->valid_columns;
   if (terms) *terms = (long long)plan->nb * plan->valid_columns * plan->nc * sigma::kNW;
   return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_plan_set_timing(sigma_gpp_plan plan, int enable) {
+  if (!plan) return SIGMA_ERR_NULL;
+  if (enable && plan->events.empty()) {
+    plan->events.resize(4 * kMaxTimedExecutions);
+    for (auto& e : plan->events) SIGMA_CUDA_TRY(cudaEventCreate(&e));
+  }
+  plan->timing = enable != 0;
+  plan->recorded = 0;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, double* main_ms,
+                                     double* occupied_ms, double* other_ms,
+                                     int* launches_per_execution) {
+  if (!plan) return SIGMA_ERR_NULL;
+  double tm = 0.0, to = 0.0, tr = 0.0;
+  const int n = plan->recorded < kMaxTimedExecutions ? plan->recorded : kMaxTimedExecutions;
+  for (int i = 0; i < n; ++i) {
+    cudaEvent_t* e = &plan->events[4 * i];
+    SIGMA_CUDA_TRY(cudaEventSynchronize(e[3]));
+    float a = 0.f, b = 0.f, c = 0.f, t = 0.f;
+    SIGMA_CUDA_TRY(cudaEventElapsedTime(&a, e[0], e[1]));
+    SIGMA_CUDA_TRY(cudaEventElapsedTime(&b, e[1], e[2]));
+    SIGMA_CUDA_TRY(cudaEventElapsedTime(&t, e[0], e[3]));
+    c = t - a - b;
+    tm += a;
+    to += b;
+    tr += c;
+  }
+  if (executions) *executions = n;
+  if (main_ms) *main_ms = tm;
+  if (occupied_ms) *occupied_ms = to;
+  if (other_ms) *other_ms = tr;
+  if (launches_per_execution) {
+    const bool mixed = plan->precision == SIGMA_PREC_MIXED;
+    *launches_per_execution = (plan->sch.n_items > 0 ? (mixed ? 3 : 1) : 0) +
+                              (plan->ssx.n_items > 0 ? 1 : 0) + 2;
+  }
+  plan->recorded = 0;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_plan_status(sigma_gpp_plan plan, void* stream) {
+  if (!plan) return SIGMA_ERR_NULL;
+  int st = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  SIGMA_CUDA_TRY(cudaMemcpyAsync(&st, plan->prep.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+  return st;
 }
 
 extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, int wx_band_stride,
@@ -220,18 +297,25 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   p.wx = wx_array;
   p.igp_of = plan->igp_of;
 
-  SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 2 * sizeof(int), s));
+  cudaEvent_t* ev = nullptr;
+  if (plan->timing && plan->recorded < kMaxTimedExecutions) ev = &plan->events[4 * plan->recorded++];
+  SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
   const bool mixed = plan->precision == SIGMA_PREC_MIXED;
+  if (mixed && plan->sch.n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->sch, plan->prep, s));
+  if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
   if (plan->sch.n_items > 0)
-    SIGMA_CUDA_TRY(mixed ? launch_sch_mixed(p, plan->sch, plan->sch_grid, s)
+    SIGMA_CUDA_TRY(mixed ? launch_sch_mixed(p, plan->sch, plan->prep, plan->sch_grid, s)
                          : launch_sch_fp64(p, plan->sch, plan->sch_grid, s));
+  if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
   if (plan->ssx.n_items > 0)
     SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed(p, plan->ssx, plan->ssx_grid, s)
                          : launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
+  if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[2], s));
   SIGMA_CUDA_TRY(launch_gpp_reduce(plan->sch, plan->ssx, plan->nb, plan->acht_n1,
                                    reinterpret_cast<double2*>(achtemp),
                                    reinterpret_cast<double2*>(asxtemp),
                                    reinterpret_cast<double2*>(acht_n1_loc), s));
+  if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[3], s));
   return SIGMA_OK;
 }
 
@@ -283,6 +367,11 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
   int st = check_shape(nb, nvband, nc, ng, nstart, nend);
   if (st != SIGMA_OK) return st;
   std::lock_guard<std::mutex> lk(api_mutex());
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || device_sm_count() <= 0) {
+    cudaGetLastError();
+    return SIGMA_ERR_NO_DEVICE;
+  }
   sigma_gpp_plan plan = nullptr;
   st = cached_plan(nb, nvband, nc, ng, inv, indinv, precision, &plan);
   if (st != SIGMA_OK) return st;
@@ -321,8 +410,10 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
   SIGMA_CUDA_TRY(cudaMemcpyAsync(asxtemp, d_asx, sizes[7], cudaMemcpyDeviceToHost, s));
   if (acht_n1_loc)
     SIGMA_CUDA_TRY(cudaMemcpyAsync(acht_n1_loc, d_n1, sizes[8], cudaMemcpyDeviceToHost, s));
+  int dev_status = 0;
+  SIGMA_CUDA_TRY(cudaMemcpyAsync(&dev_status, plan->prep.status, sizeof(int), cudaMemcpyDeviceToHost, s));
   SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
-  return SIGMA_OK;
+  return dev_status == 0 ? SIGMA_OK : dev_status;
 }
 
 }  // namespace

@@ -34,6 +34,7 @@ struct SchSmem {
   double2 n[kCK][kBN + kPad];
 };
 static_assert(sizeof(double2) * kBN * kNW * kBP <= sizeof(SchSmem), "epilogue reuses staging memory");
+static_assert(sizeof(SchSmem) <= 100 * 1024, "two CTAs per SM");
 
 __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
   return make_double2(fma(x.x, y.x, -__dmul_rn(x.y, y.y)), fma(x.x, y.y, __dmul_rn(x.y, y.x)));
@@ -52,9 +53,8 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    const int split = item % w.n_splits;
-    const int cb = (item / w.n_splits) % w.n_col_blocks;
-    const int bb = item / (w.n_splits * w.n_col_blocks);
+    const ItemCoord ic = decode_item(w, item);
+    const int split = ic.s, cb = ic.cb, bb = ic.bb;
     const int n1_0 = w.band_begin + bb * kBN;
     const int p0 = cb * kBP;
     const int ig_begin = split * w.split_len;
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
         sx += red[bl][iw][pl].x;
         sy += red[bl][iw][pl].y;
       }
-      w.partial[(size_t)item * kBN * kNW + tid] = make_double2(sx, sy);
+      w.partial[ic.pidx * kBN * kNW + tid] = make_double2(sx, sy);
     }
   }
 }
@@ -190,16 +190,17 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
 //                              (= -Omega2 conj(cden) delw / |cden|^2, cden = 4 wtilde^2 (delw + 1/2))
 //   otherwise (incl. exact poles, where the reference's delw is NaN): 0
 // and asxtemp[iw] += occ vcoul[igp] conj(aqsm[n1][igp]) sum_ig aqsn[n1][ig] ssx.
-constexpr int kSsxBN = 8;      // bands per item
 constexpr int kSsxBP = 256;    // columns per item, one per thread
+constexpr int kSsxCK = 8;      // g-vectors per staged chunk
 
 struct SsxSmem {
-  double a[kCK][kSsxBP];
-  double b[kCK][kSsxBP];
-  double2 g[kCK][kSsxBP];
-  double2 om[kCK][kSsxBP];
-  double2 n[kCK][kSsxBN];
+  double a[kSsxCK][kSsxBP];
+  double b[kSsxCK][kSsxBP];
+  double2 g[kSsxCK][kSsxBP];
+  double2 om[kSsxCK][kSsxBP];
+  double2 n[kSsxCK][kSsxBN];
 };
+static_assert(sizeof(SsxSmem) <= 200 * 1024, "shared memory budget");
 
 __global__ void __launch_bounds__(kThreads) ssx_fp64_kernel(GppDev p, GppWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -216,9 +217,8 @@ __global__ void __launch_bounds__(kThreads) ssx_fp64_kernel(GppDev p, GppWork w)
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    const int split = item % w.n_splits;
-    const int cb = (item / w.n_splits) % w.n_col_blocks;
-    const int bb = item / (w.n_splits * w.n_col_blocks);
+    const ItemCoord ic = decode_item(w, item);
+    const int split = ic.s, cb = ic.cb, bb = ic.bb;
     const int n1_0 = w.band_begin + bb * kSsxBN;
     const int nbl = min(kSsxBN, band_end - n1_0);
     const int p0 = cb * kSsxBP;
@@ -237,10 +237,10 @@ __global__ void __launch_bounds__(kThreads) ssx_fp64_kernel(GppDev p, GppWork w)
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) acc[i][iw] = make_double2(0.0, 0.0);
 
-    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCK) {
+    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kSsxCK) {
       __syncthreads();
-      for (int e = tid; e < kCK * kSsxBP; e += kThreads) {
-        const int k = e % kCK, pl = e / kCK;
+      for (int e = tid; e < kSsxCK * kSsxBP; e += kThreads) {
+        const int k = e % kSsxCK, pl = e / kSsxCK;
         const int ig = ig0 + k, my_igp = p0 + pl;
         double2 wt = make_double2(0.0, 0.0), ie = make_double2(0.0, 0.0);
         if (ig < ig_end && my_igp < p.ng) {
@@ -253,8 +253,8 @@ __global__ void __launch_bounds__(kThreads) ssx_fp64_kernel(GppDev p, GppWork w)
         sm.g[k][pl] = cmul(ie, wt);
         sm.om[k][pl] = cmul(cmul(wt, wt), ie);
       }
-      for (int e = tid; e < kCK * kSsxBN; e += kThreads) {
-        const int k = e % kCK, bl = e / kCK;
+      for (int e = tid; e < kSsxCK * kSsxBN; e += kThreads) {
+        const int k = e % kSsxCK, bl = e / kSsxCK;
         const int ig = ig0 + k, n1 = n1_0 + bl;
         double2 v = make_double2(0.0, 0.0);
         if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kThreads) ssx_fp64_kernel(GppDev p, GppWork w)
       }
       __syncthreads();
 
-      for (int k = 0; k < kCK; ++k) {
+      for (int k = 0; k < kSsxCK; ++k) {
         const double a = sm.a[k][tid], b = sm.b[k][tid];
         const double2 g = sm.g[k][tid], om = sm.om[k][tid];
         const double b2 = guard_b2(b);
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(kThreads) ssx_fp64_kernel(GppDev p, GppWork w)
         sx += s_red[i][iw][q].x;
         sy += s_red[i][iw][q].y;
       }
-      w.partial[(size_t)item * kSsxBN * kNW + tid] = make_double2(sx, sy);
+      w.partial[ic.pidx * kSsxBN * kNW + tid] = make_double2(sx, sy);
     }
   }
 }

@@ -1,13 +1,18 @@
 // GPP sigma sum, mixed-precision path (sm_103a).
 //
-// Same work decomposition and term algebra as the FP64 path (gpp_fp64.cu),
-// with the bulk arithmetic in FP32:
-//   * wtilde's real part is staged as an FP32 (hi, lo) pair and wx likewise,
-//     so c = wx - Re wtilde = (wx_hi - a_hi) + (wx_lo - a_lo) keeps ~2^-24
-//     relative accuracy even when wx and Re wtilde nearly cancel;
+// Same term algebra as the FP64 path (gpp_fp64.cu), with the bulk arithmetic
+// in FP32:
+//   * a pre-pass turns each (column, g-vector) into FP32 operands once per
+//     execution: Re wtilde as an FP32 (hi, lo) pair so that
+//     c = wx - Re wtilde = (wx_hi - a_hi) + (wx_lo - a_lo) keeps ~2^-24
+//     relative accuracy when wx and Re wtilde nearly cancel; Im wtilde;
+//     G = I_eps * wtilde; and the pole-guard threshold.  aqsn is converted
+//     too.  The layouts are tile-interleaved so that the main kernel stages a
+//     chunk with three TMA bulk copies (cp.async.bulk) into a double-buffered
+//     shared-memory ring, completion tracked by mbarriers;
 //   * 1/|wdiff|^2 is the FP32 hardware reciprocal refined by one
 //     Newton-Raphson step;
-//   * each thread sums 16 g-vectors in FP32, then folds that run into a
+//   * each thread sums 8 g-vectors in FP32, then folds that run into a
 //     float-float (TwoSum) accumulator; partials leave the tile in FP64 and
 //     are reduced with compensated FP64 sums (gpp_reduce.cu).
 // The pole guard must take exactly the FP64 path's decision: a term whose
@@ -21,22 +26,24 @@
 namespace sigma {
 namespace {
 
-constexpr int kPad = 1;
-constexpr int kTN = 2, kTP = 2;
-constexpr int kRun = 16;  // g-vectors summed in FP32 before the float-float fold
+constexpr int kTN = 2;    // bands per thread (one column per thread)
+constexpr int kRun = 8;   // g-vectors summed in FP32 before the float-float fold
+constexpr uint32_t kChunkBytes =
+    kCK * kBPM * sizeof(float4) + kCK * kBPM * sizeof(float2) + kCK * kBN * sizeof(float2);
+constexpr int kWaitSpins = 1 << 22;  // bound on mbarrier polls before reporting a timeout
 
-struct __align__(16) ColF {
-  float ahi, alo, b, b2;
-  float tlo, thi, gx, gy;
+struct __align__(16) Stage {
+  float4 a[kCK][kBPM];
+  float2 b[kCK][kBPM];
+  float2 n[kCK][kBN];
 };
-
-struct SchSmemF {
-  ColF col[kCK][kBP + kPad];
-  float2 n[kCK][kBN + kPad];
+struct __align__(16) SchSmemM {
+  Stage st[2];
+  double2 red[kBN][kNW][kBPM];
+  unsigned long long bar[2];
 };
-constexpr size_t kSchSmemBytes =
-    sizeof(SchSmemF) > sizeof(double2) * kBN * kNW * kBP ? sizeof(SchSmemF)
-                                                         : sizeof(double2) * kBN * kNW * kBP;
+static_assert(sizeof(Stage) == kChunkBytes, "one chunk is one contiguous copy per operand");
+static_assert(sizeof(SchSmemM) <= 72 * 1024, "three CTAs per SM");
 
 __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
   return make_double2(fma(x.x, y.x, -__dmul_rn(x.y, y.y)), fma(x.x, y.y, __dmul_rn(x.y, y.x)));
@@ -44,26 +51,155 @@ __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
 __device__ __forceinline__ float2 cmulf(float2 x, float2 y) {
   return make_float2(fmaf(x.x, y.x, -x.y * y.y), fmaf(x.x, y.y, x.y * y.x));
 }
-
 __device__ __forceinline__ void split_f(double v, float& hi, float& lo) {
   hi = __double2float_rn(v);
   lo = __double2float_rn(v - (double)hi);
 }
 
+// ---- TMA bulk copies and mbarriers (PTX ISA: cp.async.bulk, mbarrier)
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: after kWaitSpins polls it records SIGMA_ERR_TIMEOUT and keeps
+// waiting once more with the same bound (a bulk copy from valid global memory
+// always lands; the bound only keeps a fault elsewhere from becoming a hang).
+__device__ __forceinline__ void mbar_wait(unsigned long long* bar, uint32_t parity, int* status) {
+  for (int i = 0; i < kWaitSpins; ++i)
+    if (mbar_try_wait(bar, parity)) return;
+  atomicExch(status, (int)SIGMA_ERR_TIMEOUT);
+  for (int i = 0; i < kWaitSpins; ++i)
+    if (mbar_try_wait(bar, parity)) return;
+}
+
+// Issues the three bulk copies of chunk (cb, bb, ig0) into stage `st`.
+__device__ __forceinline__ void issue_chunk(const MixedPrep& m, int cb, int bb, int ig0, Stage& st,
+                                            unsigned long long* bar) {
+  mbar_expect_tx(bar, kChunkBytes);
+  const size_t col_off = ((size_t)cb * m.nc_pad + ig0) * kBPM;
+  const size_t band_off = ((size_t)bb * m.nc_pad + ig0) * kBN;
+  bulk_load(&st.a[0][0], m.colA + col_off, sizeof(st.a), bar);
+  bulk_load(&st.b[0][0], m.colB + col_off, sizeof(st.b), bar);
+  bulk_load(&st.n[0][0], m.band + band_off, sizeof(st.n), bar);
+}
+
 // Exact FP64 keep/drop decision of term (column my_igp, g-vector ig, frequency wx).
-__device__ __noinline__ bool keep_exact(const GppDev& p, int my_igp, int ig, double wx) {
+__device__ __forceinline__ bool keep_exact(const GppDev& p, int my_igp, int ig, double wx) {
   const double2 wt = p.wt[(size_t)my_igp * p.nc + ig];
   const double b2 = guard_b2(wt.y);
   return gt_nonneg(guard_w(wx, wt.x, b2), guard_thr(wt.x, b2));
 }
 
-__global__ void __launch_bounds__(kThreads, 2) sch_mixed_kernel(GppDev p, GppWork w) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SchSmemF& sm = *reinterpret_cast<SchSmemF*>(smem_raw);
+// ---- pre-pass: FP32 operands in tile-interleaved layouts
+__global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, int n_col_blocks) {
+  __shared__ float4 ta[32][kBPM + 1];
+  __shared__ float2 tb[32][kBPM + 1];
+  const int tid = threadIdx.x;
+  const long long tiles = (long long)n_col_blocks * (m.nc_pad / 32);
+  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int cb = (int)(t / (m.nc_pad / 32));
+    const int ig0 = (int)(t % (m.nc_pad / 32)) * 32;
+    __syncthreads();
+    for (int e = tid; e < 32 * kBPM; e += 256) {
+      const int pl = e / 32, k = e % 32;  // reads run along g-vectors
+      const int my_igp = cb * kBPM + pl, ig = ig0 + k;
+      float4 a = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7f800000));
+      float2 g = make_float2(0.f, 0.f);
+      if (my_igp < p.ng && ig < p.nc) {
+        const size_t off = (size_t)my_igp * p.nc + ig;
+        const double2 wt = p.wt[off];
+        const double2 ie = p.ieps[off];
+        const double b2 = guard_b2(wt.y);
+        split_f(wt.x, a.x, a.y);
+        a.z = __double2float_rn(wt.y);
+        a.w = __double2float_rn(guard_thr(wt.x, b2));
+        const double2 gg = cmul(ie, wt);
+        g = make_float2(__double2float_rn(gg.x), __double2float_rn(gg.y));
+      }
+      ta[k][pl] = a;
+      tb[k][pl] = g;
+    }
+    __syncthreads();
+    for (int e = tid; e < 32 * kBPM; e += 256) {
+      const int k = e / kBPM, pl = e % kBPM;  // writes run along columns
+      const size_t o = ((size_t)cb * m.nc_pad + ig0 + k) * kBPM + pl;
+      m.colA[o] = ta[k][pl];
+      m.colB[o] = tb[k][pl];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) prep_bands_kernel(GppDev p, MixedPrep m, int band_begin,
+                                                         int band_count, int n_band_blocks) {
+  __shared__ float2 tn[32][kBN + 1];
+  const int tid = threadIdx.x;
+  const long long tiles = (long long)n_band_blocks * (m.nc_pad / 32);
+  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int bb = (int)(t / (m.nc_pad / 32));
+    const int ig0 = (int)(t % (m.nc_pad / 32)) * 32;
+    __syncthreads();
+    for (int e = tid; e < 32 * kBN; e += 256) {
+      const int bl = e / 32, k = e % 32;
+      const int n1 = band_begin + bb * kBN + bl, ig = ig0 + k;
+      float2 v = make_float2(0.f, 0.f);
+      if (bb * kBN + bl < band_count && ig < p.nc) {
+        const double2 d = p.aqsn[(size_t)n1 * p.nc + ig];
+        v = make_float2(__double2float_rn(d.x), __double2float_rn(d.y));
+      }
+      tn[k][bl] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < 32 * kBN; e += 256) {
+      const int k = e / kBN, bl = e % kBN;
+      m.band[((size_t)bb * m.nc_pad + ig0 + k) * kBN + bl] = tn[k][bl];
+    }
+  }
+}
+
+// ---- main pass
+__global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWork w, MixedPrep m) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SchSmemM& sm = *reinterpret_cast<SchSmemM*>(smem_raw);
   __shared__ int s_item;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int band_end = w.band_begin + w.band_count;
   const float band_lo = 1.0f - kGuardBand, band_hi = 1.0f + kGuardBand;
+  if (tid == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_fence_init();
+  }
+  uint32_t phase0 = 0, phase1 = 0;
 
   for (;;) {
     __syncthreads();
@@ -71,13 +207,13 @@ __global__ void __launch_bounds__(kThreads, 2) sch_mixed_kernel(GppDev p, GppWor
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    const int split = item % w.n_splits;
-    const int cb = (item / w.n_splits) % w.n_col_blocks;
-    const int bb = item / (w.n_splits * w.n_col_blocks);
-    const int n1_0 = w.band_begin + bb * kBN;
-    const int p0 = cb * kBP;
-    const int ig_begin = split * w.split_len;
+    const ItemCoord ic = decode_item(w, item);
+    const int n1_0 = w.band_begin + ic.bb * kBN;
+    const int ig_begin = ic.s * w.split_len;
     const int ig_end = min(ig_begin + w.split_len, p.nc);
+    const int n_chunks = (ig_end - ig_begin + kCK - 1) / kCK;
+    const int pl = tx;
+    const int my_igp = ic.cb * kBPM + pl;
 
     float wxh[kTN][kNW], wxl[kTN][kNW];
 #pragma unroll
@@ -89,175 +225,171 @@ __global__ void __launch_bounds__(kThreads, 2) sch_mixed_kernel(GppDev p, GppWor
         split_f(wx, wxh[i][iw], wxl[i][iw]);
       }
     }
-    float2 acc[kTN][kTP][kNW];
-    float2 hi[kTN][kTP][kNW], lo[kTN][kTP][kNW];
+    float2 acc[kTN][kNW], hi[kTN][kNW], lo[kTN][kNW];
 #pragma unroll
     for (int i = 0; i < kTN; ++i)
 #pragma unroll
-      for (int j = 0; j < kTP; ++j)
-#pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) {
-          acc[i][j][iw] = make_float2(0.f, 0.f);
-          hi[i][j][iw] = make_float2(0.f, 0.f);
-          lo[i][j][iw] = make_float2(0.f, 0.f);
-        }
+      for (int iw = 0; iw < kNW; ++iw) {
+        acc[i][iw] = make_float2(0.f, 0.f);
+        hi[i][iw] = make_float2(0.f, 0.f);
+        lo[i][iw] = make_float2(0.f, 0.f);
+      }
 
-    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCK) {
-      __syncthreads();
-      for (int e = tid; e < kCK * kBP; e += kThreads) {
-        const int k = e % kCK, pl = e / kCK;
-        const int ig = ig0 + k, my_igp = p0 + pl;
-        ColF c;
-        c.ahi = c.alo = c.b = c.b2 = c.gx = c.gy = 0.f;
-        c.tlo = c.thi = __int_as_float(0x7f800000);
-        if (ig < ig_end && my_igp < p.ng) {
-          const size_t off = (size_t)my_igp * p.nc + ig;
-          const double2 wt = p.wt[off];
-          const double2 ie = p.ieps[off];
-          const double b2 = guard_b2(wt.y);
-          const float thr = __double2float_rn(guard_thr(wt.x, b2));
-          split_f(wt.x, c.ahi, c.alo);
-          c.b = __double2float_rn(wt.y);
-          c.b2 = __double2float_rn(b2);
-          c.tlo = thr * band_lo;
-          c.thi = thr * band_hi;
-          const double2 g = cmul(ie, wt);
-          c.gx = __double2float_rn(g.x);
-          c.gy = __double2float_rn(g.y);
-        }
-        sm.col[k][pl] = c;
+    if (tid == 0) issue_chunk(m, ic.cb, ic.bb, ig_begin, sm.st[0], &sm.bar[0]);
+    for (int c = 0; c < n_chunks; ++c) {
+      const int buf = c & 1;
+      const int ig0 = ig_begin + c * kCK;
+      if (tid == 0 && c + 1 < n_chunks)
+        issue_chunk(m, ic.cb, ic.bb, ig0 + kCK, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
+      if (buf == 0) {
+        mbar_wait(&sm.bar[0], phase0, m.status);
+        phase0 ^= 1;
+      } else {
+        mbar_wait(&sm.bar[1], phase1, m.status);
+        phase1 ^= 1;
       }
-      for (int e = tid; e < kCK * kBN; e += kThreads) {
-        const int k = e % kCK, bl = e / kCK;
-        const int ig = ig0 + k, n1 = n1_0 + bl;
-        float2 v = make_float2(0.f, 0.f);
-        if (ig < ig_end && n1 < band_end) {
-          const double2 d = p.aqsn[(size_t)n1 * p.nc + ig];
-          v = make_float2(__double2float_rn(d.x), __double2float_rn(d.y));
-        }
-        sm.n[k][bl] = v;
-      }
-      __syncthreads();
+      const Stage& st = sm.st[buf];
 
 #pragma unroll 1
       for (int kr = 0; kr < kCK; kr += kRun) {
-#pragma unroll 4
+#pragma unroll 2
         for (int k = kr; k < kr + kRun; ++k) {
-          ColF col[kTP];
+          const float4 a = st.a[k][pl];
+          const float2 g = st.b[k][pl];
           float2 nn[kTN];
 #pragma unroll
-          for (int j = 0; j < kTP; ++j) col[j] = sm.col[k][tx + 16 * j];
-#pragma unroll
-          for (int i = 0; i < kTN; ++i) nn[i] = sm.n[k][ty + 16 * i];
+          for (int i = 0; i < kTN; ++i) nn[i] = st.n[k][ty + 16 * i];
+          const float thi = a.w * band_hi, tlo = a.w * band_lo;
+          const float b2 = a.z * a.z;
           bool unc = false;
 #pragma unroll
-          for (int i = 0; i < kTN; ++i)
+          for (int i = 0; i < kTN; ++i) {
+            const float2 R = cmulf(nn[i], g);
+            const float bRre = a.z * R.x, bRim = a.z * R.y;
 #pragma unroll
-            for (int j = 0; j < kTP; ++j) {
-              const float2 R = cmulf(nn[i], make_float2(col[j].gx, col[j].gy));
-              const float bRre = col[j].b * R.x, bRim = col[j].b * R.y;
-#pragma unroll
-              for (int iw = 0; iw < kNW; ++iw) {
-                const float c = (wxh[i][iw] - col[j].ahi) + (wxl[i][iw] - col[j].alo);
-                const float wv = fmaf(c, c, col[j].b2);
-                const float r = rcp_f32(wv);
-                const bool keep = wv > col[j].thi;
-                unc |= (wv > col[j].tlo) && !keep;
-                const float rm = keep ? r : 0.f;
-                const float ure = fmaf(R.x, c, -bRim);
-                const float uim = fmaf(R.y, c, bRre);
-                acc[i][j][iw].x = fmaf(ure, rm, acc[i][j][iw].x);
-                acc[i][j][iw].y = fmaf(uim, rm, acc[i][j][iw].y);
-              }
+            for (int iw = 0; iw < kNW; ++iw) {
+              const float c = (wxh[i][iw] - a.x) + (wxl[i][iw] - a.y);
+              const float wv = fmaf(c, c, b2);
+              const float r = rcp_f32(wv);
+              const bool keep = wv > thi;
+              unc |= (wv > tlo) && !keep;
+              const float rm = keep ? r : 0.f;
+              acc[i][iw].x = fmaf(fmaf(R.x, c, -bRim), rm, acc[i][iw].x);
+              acc[i][iw].y = fmaf(fmaf(R.y, c, bRre), rm, acc[i][iw].y);
             }
+          }
           if (__any_sync(0xffffffffu, unc)) {
             // Terms near a threshold were dropped above; add back the ones the
             // FP64 decision keeps.
+            const int ig = ig0 + k;
 #pragma unroll
-            for (int i = 0; i < kTN; ++i)
+            for (int i = 0; i < kTN; ++i) {
+              const int n1 = n1_0 + ty + 16 * i;
+              const float2 R = cmulf(nn[i], g);
+              const float bRre = a.z * R.x, bRim = a.z * R.y;
 #pragma unroll
-              for (int j = 0; j < kTP; ++j) {
-                const int n1 = n1_0 + ty + 16 * i, my_igp = p0 + tx + 16 * j, ig = ig0 + k;
-                const float2 R = cmulf(nn[i], make_float2(col[j].gx, col[j].gy));
-                const float bRre = col[j].b * R.x, bRim = col[j].b * R.y;
-#pragma unroll
-                for (int iw = 0; iw < kNW; ++iw) {
-                  const float c = (wxh[i][iw] - col[j].ahi) + (wxl[i][iw] - col[j].alo);
-                  const float wv = fmaf(c, c, col[j].b2);
-                  if (wv > col[j].tlo && !(wv > col[j].thi) && n1 < band_end &&
-                      my_igp < p.ng && ig < ig_end &&
-                      keep_exact(p, my_igp, ig, p.wx[(size_t)n1 * p.wx_stride + iw])) {
-                    const float r = rcp_f32(wv);
-                    acc[i][j][iw].x = fmaf(fmaf(R.x, c, -bRim), r, acc[i][j][iw].x);
-                    acc[i][j][iw].y = fmaf(fmaf(R.y, c, bRre), r, acc[i][j][iw].y);
-                  }
+              for (int iw = 0; iw < kNW; ++iw) {
+                const float c = (wxh[i][iw] - a.x) + (wxl[i][iw] - a.y);
+                const float wv = fmaf(c, c, b2);
+                if (wv > tlo && !(wv > thi) && n1 < band_end && my_igp < p.ng && ig < ig_end &&
+                    keep_exact(p, my_igp, ig, p.wx[(size_t)n1 * p.wx_stride + iw])) {
+                  const float r = rcp_f32(wv);
+                  acc[i][iw].x = fmaf(fmaf(R.x, c, -bRim), r, acc[i][iw].x);
+                  acc[i][iw].y = fmaf(fmaf(R.y, c, bRre), r, acc[i][iw].y);
                 }
               }
+            }
           }
         }
         // fold the FP32 run into the float-float accumulators
 #pragma unroll
         for (int i = 0; i < kTN; ++i)
 #pragma unroll
-          for (int j = 0; j < kTP; ++j)
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) {
-              float s, e;
-              two_sum_f(hi[i][j][iw].x, acc[i][j][iw].x, s, e);
-              hi[i][j][iw].x = s;
-              lo[i][j][iw].x += e;
-              two_sum_f(hi[i][j][iw].y, acc[i][j][iw].y, s, e);
-              hi[i][j][iw].y = s;
-              lo[i][j][iw].y += e;
-              acc[i][j][iw] = make_float2(0.f, 0.f);
-            }
+          for (int iw = 0; iw < kNW; ++iw) {
+            float s, e;
+            two_sum_f(hi[i][iw].x, acc[i][iw].x, s, e);
+            hi[i][iw].x = s;
+            lo[i][iw].x += e;
+            two_sum_f(hi[i][iw].y, acc[i][iw].y, s, e);
+            hi[i][iw].y = s;
+            lo[i][iw].y += e;
+            acc[i][iw] = make_float2(0.f, 0.f);
+          }
       }
+      __syncthreads();  // every thread is done with this stage before it is refilled
     }
 
-    __syncthreads();
-    double2(*red)[kNW][kBP] = reinterpret_cast<double2(*)[kNW][kBP]>(smem_raw);
+    // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp] in FP64, then a
+    // fixed-order compensated sum over the tile's columns
+    const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
 #pragma unroll
-    for (int i = 0; i < kTN; ++i)
+    for (int i = 0; i < kTN; ++i) {
+      const int bl = ty + 16 * i;
+      const int n1 = n1_0 + bl;
+      if (n1 < band_end && igp >= 0) {
+        const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+        const double2 mm = make_double2(am.x, -am.y);
+        const double f = 0.5 * p.vcoul[igp];
 #pragma unroll
-      for (int j = 0; j < kTP; ++j) {
-        const int bl = ty + 16 * i, pl = tx + 16 * j;
-        const int n1 = n1_0 + bl, my_igp = p0 + pl;
-        const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
-        if (n1 < band_end && igp >= 0) {
-          const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
-          const double2 m = make_double2(am.x, -am.y);
-          const double f = 0.5 * p.vcoul[igp];
-#pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) {
-            const double2 s = make_double2((double)hi[i][j][iw].x + (double)lo[i][j][iw].x,
-                                           (double)hi[i][j][iw].y + (double)lo[i][j][iw].y);
-            const double2 v = cmul(s, m);
-            red[bl][iw][pl] = make_double2(v.x * f, v.y * f);
-          }
-        } else {
-#pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) red[bl][iw][pl] = make_double2(0.0, 0.0);
+        for (int iw = 0; iw < kNW; ++iw) {
+          const double2 sv = make_double2((double)hi[i][iw].x + (double)lo[i][iw].x,
+                                          (double)hi[i][iw].y + (double)lo[i][iw].y);
+          const double2 v = cmul(sv, mm);
+          sm.red[bl][iw][pl] = make_double2(v.x * f, v.y * f);
         }
+      } else {
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) sm.red[bl][iw][pl] = make_double2(0.0, 0.0);
       }
+    }
     __syncthreads();
     if (tid < kBN * kNW) {
       const int bl = tid / kNW, iw = tid % kNW;
       Comp sx, sy;
-      for (int pl = 0; pl < kBP; ++pl) {
-        sx.add(red[bl][iw][pl].x);
-        sy.add(red[bl][iw][pl].y);
+      for (int q = 0; q < kBPM; ++q) {
+        sx.add(sm.red[bl][iw][q].x);
+        sy.add(sm.red[bl][iw][q].y);
       }
-      w.partial[(size_t)item * kBN * kNW + tid] = make_double2(sx.value(), sy.value());
+      w.partial[ic.pidx * kBN * kNW + tid] = make_double2(sx.value(), sy.value());
     }
   }
 }
+
+}  // namespace
+
+int sch_blocks_per_sm_mixed() {
+  int n = 0;
+  cudaFuncSetAttribute(sch_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SchSmemM));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sch_mixed_kernel, kThreads, sizeof(SchSmemM));
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_prep_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, cudaStream_t s) {
+  const int sms = 152;
+  prep_cols_kernel<<<sms * 8, 256, 0, s>>>(p, m, w.n_col_blocks);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  prep_bands_kernel<<<sms * 4, 256, 0, s>>>(p, m, w.band_begin, w.band_count, w.n_band_blocks);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
+                             cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(sch_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       sizeof(SchSmemM));
+  if (e != cudaSuccess) return e;
+  sch_mixed_kernel<<<grid, kThreads, sizeof(SchSmemM), s>>>(p, w, m);
+  return cudaGetLastError();
+}
+
+namespace {
 
 // ---------------------------------------------------------------- occupied bands
 // FP32 form of ssx_fp64_kernel.  The three branch decisions (keep, the
 // |delw|^2 > to1 test, and the exact-pole test |wdiff|^2 > 0) fall back to the
 // FP64 expressions whenever FP32 |wdiff|^2 is near the corresponding threshold.
-constexpr int kSsxBN = 8;
 constexpr int kSsxBP = 256;
+constexpr int kSsxCK = 8;
 
 struct __align__(16) ColS {
   float ahi, alo, b, b2;
@@ -266,12 +398,13 @@ struct __align__(16) ColS {
 };
 
 struct SsxSmemF {
-  ColS col[kCK][kSsxBP];
-  float2 n[kCK][kSsxBN];
+  ColS col[kSsxCK][kSsxBP];
+  float2 n[kSsxCK][kSsxBN];
 };
+static_assert(sizeof(SsxSmemF) <= 200 * 1024, "shared memory budget");
 
 // FP64 branch of one occupied-band term: 0 dropped, 1 kept, 2 second branch.
-__device__ __noinline__ int ssx_branch_exact(const GppDev& p, int my_igp, int ig, double wx) {
+__device__ __forceinline__ int ssx_branch_exact(const GppDev& p, int my_igp, int ig, double wx) {
   const double2 wt = p.wt[(size_t)my_igp * p.nc + ig];
   const double b2 = guard_b2(wt.y);
   const double wv = guard_w(wx, wt.x, b2);
@@ -297,9 +430,8 @@ __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    const int split = item % w.n_splits;
-    const int cb = (item / w.n_splits) % w.n_col_blocks;
-    const int bb = item / (w.n_splits * w.n_col_blocks);
+    const ItemCoord ic = decode_item(w, item);
+    const int split = ic.s, cb = ic.cb, bb = ic.bb;
     const int n1_0 = w.band_begin + bb * kSsxBN;
     const int nbl = min(kSsxBN, band_end - n1_0);
     const int p0 = cb * kSsxBP;
@@ -313,21 +445,24 @@ __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w
       s_iwx2[i][iw] = __double2float_rn(rcp_f64(wx * wx));
     }
 
-    float2 acc[kSsxBN][kNW];
+    float2 acc[kSsxBN][kNW], accl[kSsxBN][kNW];
 #pragma unroll
     for (int i = 0; i < kSsxBN; ++i)
 #pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) acc[i][iw] = make_float2(0.f, 0.f);
+      for (int iw = 0; iw < kNW; ++iw) {
+        acc[i][iw] = make_float2(0.f, 0.f);
+        accl[i][iw] = make_float2(0.f, 0.f);
+      }
     double2 accd[kSsxBN][kNW];
 #pragma unroll
     for (int i = 0; i < kSsxBN; ++i)
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) accd[i][iw] = make_double2(0.0, 0.0);
 
-    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCK) {
+    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kSsxCK) {
       __syncthreads();
-      for (int e = tid; e < kCK * kSsxBP; e += kThreads) {
-        const int k = e % kCK, pl = e / kCK;
+      for (int e = tid; e < kSsxCK * kSsxBP; e += kThreads) {
+        const int k = e % kSsxCK, pl = e / kSsxCK;
         const int ig = ig0 + k, my_igp = p0 + pl;
         ColS c;
         c.ahi = c.alo = c.b = c.b2 = c.gx = c.gy = c.ox = c.oy = c.pad0 = c.pad1 = 0.f;
@@ -351,8 +486,8 @@ __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w
         }
         sm.col[k][pl] = c;
       }
-      for (int e = tid; e < kCK * kSsxBN; e += kThreads) {
-        const int k = e % kCK, bl = e / kCK;
+      for (int e = tid; e < kSsxCK * kSsxBN; e += kThreads) {
+        const int k = e % kSsxCK, bl = e / kSsxCK;
         const int ig = ig0 + k, n1 = n1_0 + bl;
         float2 v = make_float2(0.f, 0.f);
         if (ig < ig_end && n1 < band_end) {
@@ -363,7 +498,7 @@ __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w
       }
       __syncthreads();
 
-      for (int k = 0; k < kCK; ++k) {
+      for (int k = 0; k < kSsxCK; ++k) {
         const ColS col = sm.col[k][tid];
 #pragma unroll
         for (int i = 0; i < kSsxBN; ++i) {
@@ -393,21 +528,32 @@ __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w
                 s = make_float2(fmaf(col.gx, zr, col.gy * col.b) * q,
                                 fmaf(col.gy, zr, -col.gx * col.b) * q);
               }
-              acc[i][iw].x = fmaf(an.x, s.x, fmaf(-an.y, s.y, acc[i][iw].x));
-              acc[i][iw].y = fmaf(an.x, s.y, fmaf(an.y, s.x, acc[i][iw].y));
+              // term in FP32, added to a float-float accumulator (TwoSum)
+              const float tx = fmaf(an.x, s.x, -an.y * s.y);
+              const float ty = fmaf(an.x, s.y, an.y * s.x);
+              float t, e;
+              two_sum_f(acc[i][iw].x, tx, t, e);
+              acc[i][iw].x = t;
+              accl[i][iw].x += e;
+              two_sum_f(acc[i][iw].y, ty, t, e);
+              acc[i][iw].y = t;
+              accl[i][iw].y += e;
             }
           }
         }
       }
-      // fold the chunk's FP32 sums into FP64 (32 g-vectors per run)
+      // fold the float-float sums into FP64 every 16 chunks
+      const bool last_chunk = ig0 + kSsxCK >= ig_end;
+      if (((ig0 - ig_begin) / kSsxCK) % 16 != 15 && !last_chunk) continue;
 #pragma unroll
       for (int i = 0; i < kSsxBN; ++i)
         if (i < nbl) {
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            accd[i][iw].x += (double)acc[i][iw].x;
-            accd[i][iw].y += (double)acc[i][iw].y;
+            accd[i][iw].x += (double)acc[i][iw].x + (double)accl[i][iw].x;
+            accd[i][iw].y += (double)acc[i][iw].y + (double)accl[i][iw].y;
             acc[i][iw] = make_float2(0.f, 0.f);
+            accl[i][iw] = make_float2(0.f, 0.f);
           }
         }
     }
@@ -441,33 +587,18 @@ __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w
         sx.add(s_red[i][iw][q].x);
         sy.add(s_red[i][iw][q].y);
       }
-      w.partial[(size_t)item * kSsxBN * kNW + tid] = make_double2(sx.value(), sy.value());
+      w.partial[ic.pidx * kSsxBN * kNW + tid] = make_double2(sx.value(), sy.value());
     }
   }
 }
 
 }  // namespace
 
-int sch_blocks_per_sm_mixed() {
-  int n = 0;
-  cudaFuncSetAttribute(sch_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSchSmemBytes);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sch_mixed_kernel, kThreads, kSchSmemBytes);
-  return n > 0 ? n : 1;
-}
-
 int ssx_blocks_per_sm_mixed() {
   int n = 0;
   cudaFuncSetAttribute(ssx_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SsxSmemF));
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssx_mixed_kernel, kThreads, sizeof(SsxSmemF));
   return n > 0 ? n : 1;
-}
-
-cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(sch_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kSchSmemBytes);
-  if (e != cudaSuccess) return e;
-  sch_mixed_kernel<<<grid, kThreads, kSchSmemBytes, s>>>(p, w);
-  return cudaGetLastError();
 }
 
 cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s) {

@@ -11,7 +11,6 @@
 namespace sigma {
 namespace {
 
-constexpr int kSsxBN = 8;  // bands per occupied-band item (gpp_fp64.cu / gpp_mixed.cu)
 
 // Butterfly combine of compensated pairs; every lane ends with the same value
 // (TwoSum's error term is exact, so a+b and b+a agree bit for bit).

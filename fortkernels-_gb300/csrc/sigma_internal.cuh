@@ -59,16 +59,54 @@ struct GppWork {
   double2* partial;            // [n_band_blocks][n_col_blocks][n_splits][BN][3]
 };
 
-// Tile shape shared by the kernels of one precision.
-constexpr int kBN = 32;   // bands per tile
-constexpr int kBP = 32;   // columns (my_igp) per tile
-constexpr int kCK = 32;   // g-vectors per staged chunk
+// Tile shapes.  Every pass uses kBN-band blocks (partial-sum layout of the
+// reduction); the column block width differs per precision.
+constexpr int kBN = 32;    // bands per sch tile
+constexpr int kBP = 32;    // columns (my_igp) per FP64 sch tile
+constexpr int kBPM = 16;   // columns per mixed sch tile
+constexpr int kCK = 32;    // g-vectors per staged chunk
 constexpr int kThreads = 256;
+constexpr int kSsxBN = 4;   // bands per occupied-band item
+
+// Item -> (band block, column block, g-vector split).  Band blocks vary
+// fastest so that CTAs running at the same time share column data in L2.
+// pidx is the item's slot in the partial-sum array, ordered
+// [band block][column block][split] whatever the schedule.
+struct ItemCoord {
+  int bb, cb, s;
+  size_t pidx;
+};
+__device__ __forceinline__ ItemCoord decode_item(const GppWork& w, int item) {
+  ItemCoord c;
+  c.bb = item % w.n_band_blocks;
+  const int r = item / w.n_band_blocks;
+  c.s = r % w.n_splits;
+  c.cb = r / w.n_splits;
+  c.pidx = ((size_t)c.bb * w.n_col_blocks + c.cb) * w.n_splits + c.s;
+  return c;
+}
+
+// FP32 operands of the mixed sch pass, prepared once per execution in
+// tile-interleaved layouts so that one staged chunk is one contiguous block:
+//   colA[cb][ig][pl] = (Re wtilde hi, Re wtilde lo, Im wtilde, pole-guard threshold)
+//   colB[cb][ig][pl] = I_eps * wtilde
+//   band[bb][ig][bl] = aqsn
+// with my_igp = cb*kBPM + pl, n1 = bb*kBN + bl, ig < nc_pad (padding: zero
+// operands and an infinite threshold, so padded terms are dropped).
+struct MixedPrep {
+  float4* colA;
+  float2* colB;
+  float2* band;
+  int nc_pad;
+  int* status;  // device status word (0, or SIGMA_ERR_TIMEOUT after a bounded wait gave up)
+};
 
 // ---------------------------------------------------------------- launchers
 cudaError_t launch_sch_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
 cudaError_t launch_ssx_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
-cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
+                             cudaStream_t s);
+cudaError_t launch_prep_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, cudaStream_t s);
 cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
 int sch_blocks_per_sm(int precision);
 int ssx_blocks_per_sm(int precision);

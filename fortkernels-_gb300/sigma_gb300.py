@@ -56,6 +56,9 @@ SIGNATURES = {
     "sigma_gpp_execute": ([_P, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_plan_destroy": ([_P], _I),
     "sigma_gpp_plan_info": ([_P, _P, _P], _I),
+    "sigma_gpp_plan_status": ([_P, _P], _I),
+    "sigma_gpp_plan_set_timing": ([_P, _I], _I),
+    "sigma_gpp_plan_timing": ([_P, _P, _P, _P, _P, _P], _I),
     "sigma_fill_uniform": ([_P, _LL, _LL, _ULL, _ULL, _LL, _LL, _D, _D, _P], _I),
     "sigma_fill_stress": ([_P, _LL, _ULL, _ULL, _P, _I, _D, _D, _P], _I),
     "sigma_measure_fma_peaks": ([_P, _P, _P], _I),
@@ -162,6 +165,24 @@ class GppPlan:
                                         (acht_n1_loc if isinstance(acht_n1_loc, int) else _ptr(acht_n1_loc)),
                                         stream)
         _check(st, "sigma_gpp_execute")
+
+    def set_timing(self, enable=True):
+        _check(self.lib.sigma_gpp_plan_set_timing(self.handle, int(enable)), "sigma_gpp_plan_set_timing")
+
+    def timing(self):
+        """dict(executions, main_ms, occupied_ms, other_ms, launches) summed
+        over the executions recorded since timing was enabled / last read."""
+        n = C.c_int()
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        l = C.c_int()
+        _check(self.lib.sigma_gpp_plan_timing(self.handle, C.byref(n), C.byref(a), C.byref(b),
+                                              C.byref(c), C.byref(l)), "sigma_gpp_plan_timing")
+        return dict(executions=n.value, main_ms=a.value, occupied_ms=b.value, other_ms=c.value,
+                    launches=l.value)
+
+    def status(self, stream=0):
+        """Device status of the last execution (0, or -5 after a bounded wait gave up)."""
+        return self.lib.sigma_gpp_plan_status(self.handle, stream)
 
     def close(self):
         if getattr(self, "handle", None):

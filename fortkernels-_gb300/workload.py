@@ -59,24 +59,26 @@ def draws_u01(seed: int, array_id: int, start: int, count: int) -> np.ndarray:
     return (z >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
 
 
-def fill_real(seed: int, array_id: int, n: int, lo: float, hi: float) -> np.ndarray:
+def fill_real(seed: int, array_id: int, n: int, lo: float, hi: float, start: int = 0) -> np.ndarray:
+    """float64 elements start..start+n-1 of a real array (draw k -> element k)."""
     out = np.empty(n, dtype=np.float64)
     span = float(hi) - float(lo)
     for s in range(0, n, _CHUNK):
         c = min(_CHUNK, n - s)
-        out[s:s + c] = lo + span * draws_u01(seed, array_id, s, c)
+        out[s:s + c] = lo + span * draws_u01(seed, array_id, start + s, c)
     return out
 
 
-def fill_complex(seed: int, array_id: int, n: int, re: tuple, im: tuple) -> np.ndarray:
-    """complex128[n]: real part from even draws, imaginary part from odd draws."""
+def fill_complex(seed: int, array_id: int, n: int, re: tuple, im: tuple, start: int = 0) -> np.ndarray:
+    """complex128 elements start..start+n-1: real part from even draws,
+    imaginary part from odd draws."""
     out = np.empty(n, dtype=np.complex128)
     view = out.view(np.float64)
     rspan = float(re[1]) - float(re[0])
     ispan = float(im[1]) - float(im[0])
     for s in range(0, n, _CHUNK // 2):
         c = min(_CHUNK // 2, n - s)
-        u = draws_u01(seed, array_id, 2 * s, 2 * c)
+        u = draws_u01(seed, array_id, 2 * (start + s), 2 * c)
         view[2 * s:2 * (s + c):2] = re[0] + rspan * u[0::2]
         view[2 * s + 1:2 * (s + c):2] = im[0] + ispan * u[1::2]
     return out

@@ -92,6 +92,22 @@ int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, int wx_band_s
 
 int sigma_gpp_plan_destroy(sigma_gpp_plan plan);
 
+/* Waits for `stream` and returns the device-side status of the plan's last
+ * execution: SIGMA_OK, or SIGMA_ERR_TIMEOUT when a bounded wait inside a
+ * kernel gave up (results of that execution are then not valid). */
+int sigma_gpp_plan_status(sigma_gpp_plan plan, void* stream);
+
+/* Per-launch timing, the device-side counterpart of the reference's chrono
+ * timer around its band loop (BGW-Kernels/gppKer.cpp:301, 441).  While
+ * enabled, each execution records CUDA events on its stream around the main
+ * (all-band) kernel, the occupied-band kernel and the remaining launches
+ * (pre-pass, reductions); up to 256 executions are kept.  sigma_gpp_plan_timing
+ * waits for them, returns the summed milliseconds of each part and the number
+ * of kernels one execution launches, and clears the record. */
+int sigma_gpp_plan_set_timing(sigma_gpp_plan plan, int enable);
+int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, double* main_ms,
+                          double* occupied_ms, double* other_ms, int* launches_per_execution);
+
 /* Number of valid columns (my_igp whose igp survives the reference's range
  * test) and of terms number_bands * valid_columns * ncouls * 3. */
 int sigma_gpp_plan_info(sigma_gpp_plan plan, int* valid_columns, long long* terms);

@@ -18,12 +18,15 @@ HERE = pathlib.Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 ORACLE_LIB = BUILD / "liboracle.so"
+PORT_LIB = BUILD / "libport.so"
 REF_BIN = REF_OUT / "gppKer"
 REF_LIB = REF_OUT / "libgppref.so"
 REFERENCE_ROOT = pathlib.Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
 REF_SRC = REFERENCE_ROOT / "BGW-Kernels" / "gppKer.cpp"
 
 ORACLE_FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+# the timing build of the same file: the reference's own optimisation flags
+PORT_FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared"]
 REF_FLAGS = ["-O3", "-std=c++11", "-fopenmp"]
 
 
@@ -46,6 +49,16 @@ def build_oracle() -> pathlib.Path:
     return ORACLE_LIB
 
 
+def build_port() -> pathlib.Path:
+    """oracle/gpp_oracle.cpp built with -O3 like the reference, for CPU timing."""
+    src = HERE / "gpp_oracle.cpp"
+    if _newer(PORT_LIB, src):
+        return PORT_LIB
+    BUILD.mkdir(exist_ok=True)
+    _run(["g++", *PORT_FLAGS, str(src), "-o", str(PORT_LIB)])
+    return PORT_LIB
+
+
 def reference_available() -> bool:
     return REF_SRC.exists()
 
@@ -66,4 +79,5 @@ def build_reference() -> bool:
 
 if __name__ == "__main__":
     print(build_oracle())
+    print(build_port())
     print("reference:", build_reference())

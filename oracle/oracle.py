@@ -17,6 +17,7 @@ import numpy as np
 from . import build as _build
 
 _lib = None
+_port = None
 _ref = None
 _P, _I, _D = C.c_void_p, C.c_int, C.c_double
 
@@ -35,6 +36,16 @@ def lib():
         l.oracle_ff_schdt.argtypes = [_I, _I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _I]
         _lib = l
     return _lib
+
+
+def port_lib():
+    """The same restatement built with the reference's -O3 flags (CPU timing)."""
+    global _port
+    if _port is None:
+        l = C.CDLL(str(_build.build_port()))
+        l.oracle_gpp_port.argtypes = _GPP_ARGS
+        _port = l
+    return _port
 
 
 def _p(a):
@@ -64,7 +75,7 @@ def gpp(prob, band_begin=0, band_end=None, nthreads=0, port=False, wx_band_strid
     ach = np.zeros(3, np.complex128)
     asx = np.zeros(3, np.complex128)
     n1 = np.zeros(prob.number_bands, np.complex128)
-    fn = lib().oracle_gpp_port if port else lib().oracle_gpp
+    fn = port_lib().oracle_gpp_port if port else lib().oracle_gpp
     st = fn(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart, prob.nend,
             _p(inv), _p(indinv), len(indinv), _p(wx), wx_band_stride, prob.occ, _p(aqsm), _p(aqsn),
             _p(ieps), _p(wt), _p(vcoul), _p(ach), _p(asx), _p(n1), band_begin, band_end, nthreads)
