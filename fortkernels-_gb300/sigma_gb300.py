@@ -59,6 +59,7 @@ SIGNATURES = {
     "sigma_gpp_plan_status": ([_P, _P], _I),
     "sigma_gpp_plan_set_timing": ([_P, _I], _I),
     "sigma_gpp_plan_timing": ([_P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_fp64_noalloc": ([_I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_fill_uniform": ([_P, _LL, _LL, _ULL, _ULL, _LL, _LL, _D, _D, _P], _I),
     "sigma_fill_stress": ([_P, _LL, _ULL, _ULL, _P, _I, _D, _D, _P], _I),
     "sigma_measure_fma_peaks": ([_P, _P, _P], _I),

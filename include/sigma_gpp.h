@@ -112,6 +112,41 @@ int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, double* main_ms,
  * test) and of terms number_bands * valid_columns * ncouls * 3. */
 int sigma_gpp_plan_info(sigma_gpp_plan plan, int* valid_columns, long long* terms);
 
+/* ---------------------------------------------------------------------------
+ * FP64 evaluation that allocates nothing.  This entry point has no
+ * counterpart in the reference; it exists for callers that cannot allocate
+ * GPU memory: code inside a framework whose memory pool owns the device, a
+ * plug-in in a process that forbids allocation after start-up, or a
+ * real-time loop where an allocation could stall.
+ *
+ * Same result as sigma_gpp_execute with an FP64 plan (within 1e-12 relative;
+ * the g-vector split differs), same arrays, all device pointers except the
+ * host index maps (indinv with ncouls entries; wx_array: 3 device doubles
+ * shared by every band).  Its scratch (item counters, column map, partial
+ * sums) is one fixed 32 MiB __device__ array inside the library, held by
+ * every GPU that loads the library until the process exits; the call makes
+ * no cudaMalloc, cudaFree or other allocation.
+ *   - Limits: ngpown <= 65536, and the partial sums of the problem must fit
+ *     the 32 MiB (the production shape 512 x 1638 x 32768 uses ~9 MB);
+ *     larger problems return SIGMA_ERR_WORKSPACE with a message in
+ *     sigma_last_error_message().
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call shares the one array.  Calls that overlap on the GPU (on
+ *     different streams, or from threads that do not wait for each other's
+ *     stream) race on it and give wrong results; serialise them.
+ *   - The column map is copied from pageable host memory, so the call may
+ *     wait for work already queued on `stream`.
+ * Asynchronous on `stream` otherwise; outputs are valid once it drains.
+ * ------------------------------------------------------------------------- */
+int sigma_gpp_fp64_noalloc(int number_bands, int nvband, int ncouls, int ngpown,
+                           const int* inv_igp_index, const int* indinv, const double* wx_array,
+                           double occ, const sigma_complex128* aqsmtemp,
+                           const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                           const sigma_complex128* wtilde_array, const double* vcoul,
+                           sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                           sigma_complex128* acht_n1_loc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
