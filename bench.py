@@ -272,6 +272,51 @@ def profile_traffic_per_term():
     return float(m.group(1)) if m else None
 
 
+FF_SHAPE = (512, 16384, 820, 15)  # number_bands, ncouls, ngpown, nfreq
+
+
+def run_ff(S, W, torch, dist, world, stream, sptr, args):
+    """FF schDt contraction at its production shape: FP64 form and the
+    split-BF16 tensor-core form, TF/s = 8 * (nfreq*ngpown) * number_bands *
+    ncouls / time, and the tensor form's error against the FP64 form."""
+    nb, nc, ng, nf = FF_SHAPE
+    epsr = torch.empty(2 * nf * ng * nc, dtype=torch.float64, device="cuda")
+    aqsn = torch.empty(2 * nb * nc, dtype=torch.float64, device="cuda")
+    aqsm = torch.empty_like(aqsn)
+    S.fill_complex_device(epsr.data_ptr(), nf * ng * nc, W.FF_SEED, W.AID_IEPSR, (-1, 1), (-1, 1), sptr)
+    S.fill_complex_device(aqsn.data_ptr(), nb * nc, W.FF_SEED, W.AID_AQSN, (-1, 1), (-1, 1), sptr)
+    S.fill_complex_device(aqsm.data_ptr(), nb * nc, W.FF_SEED, W.AID_AQSM, (-1, 1), (-1, 1), sptr)
+    inv, indinv = W.ff_index_maps(nc, ng)
+    flops = 8.0 * nf * ng * nb * nc
+    res = {"workload": f"FF schDt: {nb} bands x {nf}x{ng} (ifreq, my_igp) rows x {nc} g-vectors",
+           "unit": "TFLOP/s (FP64-equivalent, 8 flop per complex multiply-add)"}
+    outs = {}
+    for mode, name, steps in ((1, "ozaki_bf16", 20), (0, "fp64", 3)):
+        plan = S.FfPlan(nb, nc, ng, nf, inv, indinv, mode)
+        out = torch.zeros(2 * nb * nf, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            plan.execute(epsr, aqsn, aqsm, out, sptr)
+        plan.set_timing(True)
+        ms = timed(torch, dist, world, lambda: plan.execute(epsr, aqsn, aqsm, out, sptr), steps, stream)
+        t = plan.timing()
+        main_s = t["main_ms"] / max(1, t["executions"]) * 1e-3
+        res[name] = {"value": round(flops * world / (ms / steps * 1e-3) / 1e12, 3),
+                     "ms_per_step": round(ms / steps, 3),
+                     "kernel_ms_per_launch": round(main_s * 1e3, 3), "steps": steps,
+                     "status": plan.status(sptr)}
+        outs[name] = out.cpu().numpy().view(np.complex128)
+        plan.close()
+    d = outs["ozaki_bf16"] - outs["fp64"]
+    res["ozaki_bf16"]["rel_err_vs_fp64"] = {
+        "normwise": float(np.linalg.norm(d) / np.linalg.norm(outs["fp64"])),
+        "max_abs_over_max": float(np.abs(d).max() / np.abs(outs["fp64"]).max())}
+    res["ozaki_bf16"]["tensor_tflops"] = round(6 * flops / (res["ozaki_bf16"]["kernel_ms_per_launch"] * 1e-3) / 1e12, 1)
+    res["speedup_ozaki_vs_fp64"] = round(res["ozaki_bf16"]["value"] / res["fp64"]["value"], 1)
+    del epsr, aqsn, aqsm
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import sigma_gb300 as S
@@ -387,6 +432,7 @@ def run_ours(args, rank, world, local_rank):
     # FP64 pipe: 2 DFMA / clk / SM, FP32: 128 FFMA / clk / SM (ncu peak_sustained on GB300)
     fp64_pipe_peak = 2 * 2 * sms * clock_mhz * 1e6 / 1e12
     fp32_pipe_peak = 2 * 128 * sms * clock_mhz * 1e6 / 1e12
+    ff = None if args.no_ff else run_ff(S, W, torch, dist, world, stream, sptr, args)
     worst = max(max(mixed_err["achtemp"]), max(mixed_err["asxtemp"]),
                 max(stress_err["achtemp"]), max(stress_err["asxtemp"]))
     line = {
@@ -426,6 +472,7 @@ def run_ours(args, rank, world, local_rank):
                                "peak": round(fp32_pipe_peak, 3), "unit": "TFLOP/s",
                                "frac": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12 / fp32_pipe_peak, 4),
                                "peak_source": "FP32 pipe 128 FFMA/clk/SM at the sampled SM clock"}},
+        "ff": ff,
         "peaks_measured": {"fp64_fma_probe_tflops": round(fp64_peak, 4),
                            "fp32_fma_probe_tflops": round(fp32_peak, 3),
                            "fp64_pipe_tflops_at_clock": round(fp64_pipe_peak, 4),
@@ -450,6 +497,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ff", action="store_true")
     ap.add_argument("--bands", type=int, default=NB,
                     help="number_bands of the instance (512 = the production shape; smaller only "
                          "for profiling captures)")

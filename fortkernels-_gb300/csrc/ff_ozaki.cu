@@ -1,0 +1,486 @@
+// FF schDt contraction on tcgen05 tensor cores (sm_103a), split-BF16 form.
+//
+// tempz = I_epsR * aqsn^T (ffkernel.deslippe.best.f90:404) is one real GEMM
+// per tile with the complex parts laid along K (ff_ozaki.cuh), so a TMEM lane
+// holds Re and Im of tempz for its row and 64 bands.
+//
+// Splitting: each FP64 value x is rounded to FP32 and split exactly into three
+// BF16 slices x = s1 + s2 + s3 (8 significant bits each; the subtractions
+// are exact in FP32).  A*B ~ A1*B1 + (A1*B2 + A2*B1 + A1*B3 + A2*B2 + A3*B1);
+// products of order 2^-24 and below are dropped.  The leading product and
+// the five corrections accumulate in two TMEM accumulators so that the
+// corrections' roundings are 2^-8 smaller.
+//
+// Accumulation: the tensor core's FP32 accumulation rounds every MMA step
+// toward zero (a measured relative bias that grows linearly with the number
+// of steps: 1.8e-5 over 1024 steps at the production K).  So accumulators
+// live only 8 K-steps: TMEM holds two accumulator pairs, and while the
+// tensor cores fill one, four drain warps read the other (tcgen05.ld) into
+// round-to-nearest FP32 running sums held in registers.
+//
+// Roles (160 threads): warp 4 lane 0 streams 96 KB K-tiles (three A and three
+// B slices, one bulk copy each) into a two-stage shared ring and issues 24
+// tcgen05.mma (M=128, N=128, K=16) per tile; warps 0-3 drain TMEM and run the
+// epilogue, which multiplies tempz by conj(aqsm[n1][igp(my_igp)]) and sums
+// the tile's rows per frequency (:408-418) with a reduce-scatter butterfly.
+// Items are (row block, band block, K split), scheduled statically.
+#include <cuda_bf16.h>
+
+#include "ff_ozaki.cuh"
+#include "sigma_tma.cuh"
+
+namespace sigma {
+namespace {
+
+using namespace tma;
+
+constexpr int kOzThreads = 160;
+constexpr int kDrainThreads = 128;
+constexpr uint32_t kSliceBytes = 128 * 64 * 2;          // 16 KB
+constexpr uint32_t kOperandBytes = 3 * kSliceBytes;     // 48 KB
+constexpr uint32_t kStageBytes = 2 * kOperandBytes;     // 96 KB
+constexpr uint32_t kSmemBytes = 2 * kStageBytes + 1024; // + alignment slack
+constexpr uint32_t kTmemCols = 512;                     // 2 x (leading + correction) accumulators
+constexpr int kChunkStages = 2;                         // K tiles per accumulator lifetime
+constexpr int kMaxSeg = 8;                              // frequencies per row block (host checks)
+constexpr uint32_t kIdesc = idesc_bf16_f32(128, 128);
+
+__device__ __forceinline__ void split3(double v, unsigned short& a, unsigned short& b,
+                                       unsigned short& c) {
+  const float x = __double2float_rn(v);
+  const __nv_bfloat16 s1 = __float2bfloat16_rn(x);
+  const float t1 = x - __bfloat162float(s1);
+  const __nv_bfloat16 s2 = __float2bfloat16_rn(t1);
+  const float t2 = t1 - __bfloat162float(s2);
+  const __nv_bfloat16 s3 = __float2bfloat16_rn(t2);
+  a = __bfloat16_as_ushort(s1);
+  b = __bfloat16_as_ushort(s2);
+  c = __bfloat16_as_ushort(s3);
+}
+
+// Slices of 8 consecutive K values of one row, written as three 16-byte
+// chunks (one per slice tile) of a 48 KB block.
+__device__ __forceinline__ void put_row_chunk(unsigned char* blk, int r, int ch, const double (&v)[8]) {
+  unsigned short sl[3][8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) split3(v[j], sl[0][j], sl[1][j], sl[2][j]);
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    uint4 q;
+    q.x = sl[s][0] | ((uint32_t)sl[s][1] << 16);
+    q.y = sl[s][2] | ((uint32_t)sl[s][3] << 16);
+    q.z = sl[s][4] | ((uint32_t)sl[s][5] << 16);
+    q.w = sl[s][6] | ((uint32_t)sl[s][7] << 16);
+    *reinterpret_cast<uint4*>(blk + s * kSliceBytes + sw128_offset(r, ch * 8)) = q;
+  }
+}
+
+// A' = [Re | Im] of I_epsR rows.  Thread = (row block, K tile, row, 8-K chunk);
+// it writes the real-part tile kt and the imaginary-part tile kt + oz.kt.
+__global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz) {
+  const long long total = (long long)oz.n_row_blocks * oz.kt * 128 * 8;
+  const int rows = p.nf * p.ng;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int ch = (int)(t & 7);
+    const int r = (int)((t >> 3) & 127);
+    const long long rest = t >> 10;
+    const int kt = (int)(rest % oz.kt);
+    const int rb = (int)(rest / oz.kt);
+    const int R = rb * kOzRows + r;
+    const int k0 = kt * kOzKTile + ch * 8;
+    double re[8], im[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = k0 + j;
+      const double2 v = (R < rows && k < p.nc) ? p.epsr[(size_t)R * p.nc + k] : make_double2(0.0, 0.0);
+      re[j] = v.x;
+      im[j] = v.y;
+    }
+    unsigned char* base = oz.a_tiles + (size_t)rb * 2 * oz.kt * kOperandBytes;
+    put_row_chunk(base + (size_t)kt * kOperandBytes, r, ch, re);
+    put_row_chunk(base + (size_t)(oz.kt + kt) * kOperandBytes, r, ch, im);
+  }
+}
+
+// B' rows: [Re | -Im] (real part of the product) and [Im | Re] (imaginary part).
+__global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz) {
+  const long long total = (long long)oz.n_col_blocks * oz.kt * 64 * 8;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int ch = (int)(t & 7);
+    const int nl = (int)((t >> 3) & 63);
+    const long long rest = t >> 9;
+    const int kt = (int)(rest % oz.kt);
+    const int cb = (int)(rest / oz.kt);
+    const int n = cb * kOzCols + nl;
+    const int k0 = kt * kOzKTile + ch * 8;
+    double re[8], im[8], nim[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = k0 + j;
+      const double2 v = (n < p.nb && k < p.nc) ? p.aqsn[(size_t)n * p.nc + k] : make_double2(0.0, 0.0);
+      re[j] = v.x;
+      im[j] = v.y;
+      nim[j] = -v.y;
+    }
+    unsigned char* base = oz.b_tiles + (size_t)cb * 2 * oz.kt * kOperandBytes;
+    unsigned char* lo = base + (size_t)kt * kOperandBytes;            // K' < K: real parts of aqsn
+    unsigned char* hi = base + (size_t)(oz.kt + kt) * kOperandBytes;  // K' >= K: imaginary parts
+    put_row_chunk(lo, nl, ch, re);
+    put_row_chunk(lo, 64 + nl, ch, im);
+    put_row_chunk(hi, nl, ch, nim);
+    put_row_chunk(hi, 64 + nl, ch, re);
+  }
+}
+
+struct OzItem {
+  int rb, cb, s;
+  size_t pidx;
+};
+__device__ __forceinline__ OzItem oz_decode(const OzakiPrep& oz, int item) {
+  OzItem t;
+  t.cb = item % oz.n_col_blocks;
+  const int r = item / oz.n_col_blocks;
+  t.s = r % oz.n_splits;
+  t.rb = r / oz.n_splits;
+  t.pidx = ((size_t)t.rb * oz.n_col_blocks + t.cb) * oz.n_splits + t.s;
+  return t;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void drain_barrier() {
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWork w, OzakiPrep oz) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bars[8];  // full[2], empty[2], accf[2], acce[2]
+  __shared__ uint32_t tmem_slot;
+  __shared__ float2 s_red[4][kMaxSeg][kOzCols];
+
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]);
+  const uint32_t accf0 = smem_u32(&bars[4]), acce0 = smem_u32(&bars[6]);
+  const int two_kt = 2 * oz.kt;
+
+  if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), kTmemCols);
+  if (tid == 0) {
+    for (int i = 0; i < 6; ++i) mbar_init(smem_u32(&bars[i]), 1);
+    mbar_init(smem_u32(&bars[6]), 4);
+    mbar_init(smem_u32(&bars[7]), 4);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 4) {
+    // ------------------------------------------------ producer: TMA + MMA issue
+    if (lane == 0) {
+      uint32_t ph_full0 = 0, ph_full1 = 0, ph_empty0 = 0, ph_empty1 = 0, ph_acce0 = 0, ph_acce1 = 0;
+      bool pend0 = false, pend1 = false, used0 = false, used1 = false;
+      uint32_t gc = 0;  // chunks issued by this CTA
+      for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
+        const OzItem it = oz_decode(oz, item);
+        const int kt_begin = it.s * oz.split_tiles;
+        const int nst = min(oz.split_tiles, two_kt - kt_begin);
+        const unsigned char* a_src = oz.a_tiles + ((size_t)it.rb * two_kt + kt_begin) * kOperandBytes;
+        const unsigned char* b_src = oz.b_tiles + ((size_t)it.cb * two_kt + kt_begin) * kOperandBytes;
+        auto issue = [&](int s, int buf) {
+          const uint32_t bar = full0 + 8u * buf;
+          const uint32_t dst = sbase + (uint32_t)buf * kStageBytes;
+          mbar_expect_tx(bar, kStageBytes);
+          bulk_load(dst, a_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
+          bulk_load(dst + kOperandBytes, b_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
+        };
+        issue(0, 0);
+        for (int s = 0; s < nst; ++s) {
+          const int buf = s & 1;
+          const int cs = s % kChunkStages;
+          const uint32_t tb = gc & 1u;
+          if (cs == 0) {  // first tile of an accumulator lifetime: buffer tb must be drained
+            if (tb == 0 && used0) {
+              mbar_wait(acce0, ph_acce0, w.status);
+              ph_acce0 ^= 1u;
+            }
+            if (tb == 1 && used1) {
+              mbar_wait(acce0 + 8u, ph_acce1, w.status);
+              ph_acce1 ^= 1u;
+            }
+            if (tb == 0) used0 = true; else used1 = true;
+            tc_fence_after();
+          }
+          if (buf == 0) {
+            mbar_wait(full0, ph_full0, w.status);
+            ph_full0 ^= 1u;
+          } else {
+            mbar_wait(full0 + 8u, ph_full1, w.status);
+            ph_full1 ^= 1u;
+          }
+          tc_fence_after();
+          const uint32_t a_addr = sbase + (uint32_t)buf * kStageBytes;
+          const uint32_t b_addr = a_addr + kOperandBytes;
+          const uint32_t d_big = tmem + tb * 256u, d_small = d_big + 128u;
+#pragma unroll
+          for (int kk = 0; kk < kOzKTile / 16; ++kk) {
+            const uint64_t a1 = sw128_desc(a_addr + kk * 32);
+            const uint64_t a2 = sw128_desc(a_addr + kSliceBytes + kk * 32);
+            const uint64_t a3 = sw128_desc(a_addr + 2 * kSliceBytes + kk * 32);
+            const uint64_t b1 = sw128_desc(b_addr + kk * 32);
+            const uint64_t b2 = sw128_desc(b_addr + kSliceBytes + kk * 32);
+            const uint64_t b3 = sw128_desc(b_addr + 2 * kSliceBytes + kk * 32);
+            const uint32_t acc = (cs > 0 || kk > 0) ? 1u : 0u;
+            mma_f16(d_big, a1, b1, kIdesc, acc);
+            mma_f16(d_small, a1, b2, kIdesc, acc);
+            mma_f16(d_small, a2, b1, kIdesc, 1u);
+            mma_f16(d_small, a1, b3, kIdesc, 1u);
+            mma_f16(d_small, a2, b2, kIdesc, 1u);
+            mma_f16(d_small, a3, b1, kIdesc, 1u);
+          }
+          mma_commit(empty0 + 8u * buf);
+          if (buf == 0) pend0 = true; else pend1 = true;
+          if (cs == kChunkStages - 1 || s == nst - 1) {
+            mma_commit(accf0 + 8u * tb);  // accumulator pair tb complete
+            ++gc;
+          }
+          if (s + 1 < nst) {
+            const int nb = buf ^ 1;
+            if (nb == 0 && pend0) {
+              mbar_wait(empty0, ph_empty0, w.status);
+              ph_empty0 ^= 1u;
+              pend0 = false;
+            }
+            if (nb == 1 && pend1) {
+              mbar_wait(empty0 + 8u, ph_empty1, w.status);
+              ph_empty1 ^= 1u;
+              pend1 = false;
+            }
+            issue(s + 1, nb);
+          }
+        }
+        if (pend0) {
+          mbar_wait(empty0, ph_empty0, w.status);
+          ph_empty0 ^= 1u;
+          pend0 = false;
+        }
+        if (pend1) {
+          mbar_wait(empty0 + 8u, ph_empty1, w.status);
+          ph_empty1 ^= 1u;
+          pend1 = false;
+        }
+      }
+      // wait until the drain warps released every accumulator pair in use
+      if (used0) mbar_wait(acce0, ph_acce0, w.status);
+      if (used1) mbar_wait(acce0 + 8u, ph_acce1, w.status);
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------ drain + epilogue (warps 0-3)
+    uint32_t ph_accf0 = 0, ph_accf1 = 0;
+    uint32_t gc = 0;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const int rows = p.nf * p.ng;
+    for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
+      const OzItem it = oz_decode(oz, item);
+      const int kt_begin = it.s * oz.split_tiles;
+      const int nst = min(oz.split_tiles, two_kt - kt_begin);
+      const int nchunks = (nst + kChunkStages - 1) / kChunkStages;
+      float acc[128];
+#pragma unroll
+      for (int i = 0; i < 128; ++i) acc[i] = 0.f;
+      for (int c = 0; c < nchunks; ++c) {
+        const uint32_t tb = gc & 1u;
+        if (tb == 0) {
+          mbar_wait(accf0, ph_accf0, w.status);
+          ph_accf0 ^= 1u;
+        } else {
+          mbar_wait(accf0 + 8u, ph_accf1, w.status);
+          ph_accf1 ^= 1u;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float big[32], small[32];
+          tmem_ld32(lane_base + tb * 256u + q * 32, big);
+          tmem_ld32(lane_base + tb * 256u + 128u + q * 32, small);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) acc[q * 32 + i] += big[i] + small[i];
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce0 + 8u * tb);
+        ++gc;
+      }
+
+      // epilogue: row R of this lane, 64 bands; tempz * conj(aqsm[n1][igp])
+      const int R = it.rb * kOzRows + warp * 32 + lane;
+      const bool row_ok = R < rows;
+      const int f = row_ok ? R / p.ng : 0;
+      const int g = row_ok ? R % p.ng : 0;
+      const int f_first = (it.rb * kOzRows) / p.ng;
+      const int f_last = (min(it.rb * kOzRows + kOzRows, rows) - 1) / p.ng;
+      const int igp = row_ok ? p.igp_of[g] : 0;
+      // acc[n] <- Re, acc[64 + n] <- Im of tempz * conj(aqsm[n1][igp])
+#pragma unroll
+      for (int n = 0; n < 64; ++n) {
+        const int nn = it.cb * kOzCols + n;
+        float mr = 0.f, mi = 0.f;
+        if (row_ok && nn < p.nb) {
+          const double2 md = p.aqsm[(size_t)nn * p.nc + igp];
+          mr = __double2float_rn(md.x);
+          mi = __double2float_rn(md.y);
+        }
+        const float cr = acc[n], ci = acc[64 + n];
+        acc[n] = fmaf(cr, mr, ci * mi);
+        acc[64 + n] = fmaf(ci, mr, -cr * mi);
+      }
+      for (int seg = 0; seg <= f_last - f_first; ++seg) {
+        const bool mine = row_ok && (f - f_first) == seg;
+        // 16 bands at a time: a reduce-scatter butterfly over the warp leaves
+        // lanes 2j and 2j+1 with the sum of band j of the batch
+#pragma unroll
+        for (int b0 = 0; b0 < 64; b0 += 16) {
+          float xr[16], xi[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            xr[i] = mine ? acc[b0 + i] : 0.f;
+            xi[i] = mine ? acc[64 + b0 + i] : 0.f;
+          }
+#pragma unroll
+          for (int o = 16, h = 8; o >= 2; o >>= 1, h >>= 1) {
+            const bool up = (lane & o) != 0;
+#pragma unroll
+            for (int i = 0; i < h; ++i) {
+              const float sr = up ? xr[i] : xr[i + h];
+              const float si = up ? xi[i] : xi[i + h];
+              const float rr = __shfl_xor_sync(0xffffffffu, sr, o);
+              const float ri = __shfl_xor_sync(0xffffffffu, si, o);
+              xr[i] = (up ? xr[i + h] : xr[i]) + rr;
+              xi[i] = (up ? xi[i + h] : xi[i]) + ri;
+            }
+          }
+          xr[0] += __shfl_xor_sync(0xffffffffu, xr[0], 1);
+          xi[0] += __shfl_xor_sync(0xffffffffu, xi[0], 1);
+          if ((lane & 1) == 0) s_red[warp][seg][b0 + (lane >> 1)] = make_float2(xr[0], xi[0]);
+        }
+      }
+      drain_barrier();
+      const int nseg = f_last - f_first + 1;
+      for (int e = tid; e < nseg * kOzCols; e += kDrainThreads) {
+        const int seg = e / kOzCols, n = e % kOzCols;
+        double sr = 0.0, si = 0.0;
+        for (int q = 0; q < 4; ++q) {
+          sr += (double)s_red[q][seg][n].x;
+          si += (double)s_red[q][seg][n].y;
+        }
+        oz.partial[(it.pidx * oz.max_seg + seg) * kOzCols + n] = make_double2(sr, si);
+      }
+      drain_barrier();
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+// schDt[n1][ifreq]: one warp per entry, fixed-order compensated sum over the
+// row blocks that hold frequency ifreq and over the K splits.
+__global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, double2* schdt) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= p.nb * p.nf) return;
+  const int n = warp / p.nf, f = warp % p.nf;
+  const int cb = n / kOzCols, c = n % kOzCols;
+  const int rb_lo = (f * p.ng) / kOzRows, rb_hi = ((f + 1) * p.ng - 1) / kOzRows;
+  const int count = (rb_hi - rb_lo + 1) * oz.n_splits;
+  Comp sx, sy;
+  for (int q = lane; q < count; q += 32) {
+    const int rb = rb_lo + q / oz.n_splits, s = q % oz.n_splits;
+    const int seg = f - (rb * kOzRows) / p.ng;
+    const size_t pidx = ((size_t)rb * oz.n_col_blocks + cb) * oz.n_splits + s;
+    const double2 v = oz.partial[(pidx * oz.max_seg + seg) * kOzCols + c];
+    sx.add(v.x);
+    sy.add(v.y);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double a = __shfl_xor_sync(0xffffffffu, sx.s, o), b = __shfl_xor_sync(0xffffffffu, sx.c, o);
+    const double c2 = __shfl_xor_sync(0xffffffffu, sy.s, o), d = __shfl_xor_sync(0xffffffffu, sy.c, o);
+    double t, e;
+    two_sum_d(sx.s, a, t, e);
+    sx.s = t;
+    sx.c = __dadd_rn(__dadd_rn(sx.c, b), e);
+    two_sum_d(sy.s, c2, t, e);
+    sy.s = t;
+    sy.c = __dadd_rn(__dadd_rn(sy.c, d), e);
+  }
+  if (lane == 0) schdt[(size_t)n * p.nf + f] = make_double2(sx.value(), sy.value());
+}
+
+}  // namespace
+
+void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid) {
+  oz.kt = (d.nc + kOzKTile - 1) / kOzKTile;
+  const int rows = d.nf * d.ng;
+  oz.n_row_blocks = (rows + kOzRows - 1) / kOzRows;
+  oz.n_col_blocks = (d.nb + kOzCols - 1) / kOzCols;
+  oz.max_seg = (kOzRows + d.ng - 2) / d.ng + 1;
+  const long long base = (long long)oz.n_row_blocks * oz.n_col_blocks;
+  const int two_kt = 2 * oz.kt;
+  long long s = (20LL * grid + base - 1) / base;
+  if (s < 1) s = 1;
+  if (s > two_kt) s = two_kt;
+  oz.split_tiles = (int)((two_kt + s - 1) / s);
+  oz.n_splits = (two_kt + oz.split_tiles - 1) / oz.split_tiles;
+  oz.n_items = (int)(base * oz.n_splits);
+}
+
+int ozaki_max_segments() { return kMaxSeg; }
+
+size_t ozaki_prep_bytes(const OzakiPrep& oz) {
+  const size_t tiles = ((size_t)oz.n_row_blocks + oz.n_col_blocks) * 2 * oz.kt * kOperandBytes;
+  const size_t part = sizeof(double2) * (size_t)oz.n_items * oz.max_seg * kOzCols;
+  return tiles + part + 2048;
+}
+
+void ozaki_prep_bind(OzakiPrep& oz, void* base) {
+  uintptr_t b = (reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023);
+  oz.a_tiles = reinterpret_cast<unsigned char*>(b);
+  oz.b_tiles = oz.a_tiles + (size_t)oz.n_row_blocks * 2 * oz.kt * kOperandBytes;
+  uintptr_t pp = reinterpret_cast<uintptr_t>(oz.b_tiles + (size_t)oz.n_col_blocks * 2 * oz.kt * kOperandBytes);
+  pp = (pp + 255) & ~uintptr_t(255);
+  oz.partial = reinterpret_cast<double2*>(pp);
+}
+
+cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s) {
+  ozaki_prep_a_kernel<<<152 * 16, 256, 0, s>>>(d, oz);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  ozaki_prep_b_kernel<<<152 * 4, 256, 0, s>>>(d, oz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& oz, int grid,
+                              cudaStream_t s) {
+  cudaError_t e =
+      cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (e != cudaSuccess) return e;
+  ozaki_gemm_kernel<<<grid, kOzThreads, kSmemBytes, s>>>(d, w, oz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s) {
+  const int warps = d.nb * d.nf;
+  const int blocks = (warps * 32 + 255) / 256;
+  ozaki_reduce_kernel<<<blocks, 256, 0, s>>>(d, oz, schdt);
+  return cudaGetLastError();
+}
+
+}  // namespace sigma

@@ -1,0 +1,42 @@
+// FF schDt contraction on tcgen05 tensor cores with split BF16 operands.
+#pragma once
+
+#include "ff_internal.cuh"
+
+namespace sigma {
+
+constexpr int kOzKTile = 64;    // K elements per staged tile (one 128-byte swizzle row)
+constexpr int kOzRows = 128;    // complex rows (ifreq, my_igp) per tile, frequencies flattened
+constexpr int kOzCols = 64;     // complex bands per tile
+
+// Operands in the shared-memory image the tensor cores read (K-major,
+// 128-byte swizzle).  The complex product is one real product with the real
+// and imaginary parts laid along K:
+//   A'[R][k']   = Re I_epsR[R][k]          (k' <  K)   Im I_epsR[R][k]  (k' >= K)
+//   B'[n][k']   = Re aqsn[n][k], -Im ...   (rows 0..63: real part of the product)
+//   B'[64+n][k']= Im aqsn[n][k],  Re ...   (rows 64..127: imaginary part)
+// so C'[R][n] = Re tempz and C'[R][64+n] = Im tempz sit in one TMEM lane.
+// One 48 KB block per (row block, K' tile) holds three 16 KB BF16 slices.
+struct OzakiPrep {
+  unsigned char* a_tiles;   // [n_row_blocks][2*kt][3][128][64] bf16
+  unsigned char* b_tiles;   // [n_col_blocks][2*kt][3][128][64] bf16
+  int kt;                   // K tiles per real/imaginary half (ncouls padded to 64)
+  int n_row_blocks;         // ceil(nfreq * ngpown / 128)
+  int n_col_blocks;         // ceil(number_bands / 64)
+  int n_splits, split_tiles;  // K' split into n_splits ranges of split_tiles tiles
+  int n_items;
+  int max_seg;              // frequencies one row block can touch
+  double2* partial;         // [row block][col block][split][max_seg][64]
+};
+
+// Work sizing and buffers of the split-BF16 form (partials + slices).
+void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid);
+int ozaki_max_segments();
+size_t ozaki_prep_bytes(const OzakiPrep& oz);
+void ozaki_prep_bind(OzakiPrep& oz, void* base);
+cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s);
+cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& oz, int grid,
+                              cudaStream_t s);
+cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s);
+
+}  // namespace sigma

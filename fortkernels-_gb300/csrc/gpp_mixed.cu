@@ -414,7 +414,7 @@ __device__ __forceinline__ int ssx_branch_exact(const GppDev& p, int my_igp, int
 }
 
 __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   SsxSmemF& sm = *reinterpret_cast<SsxSmemF*>(smem_raw);
   __shared__ int s_item;
   __shared__ double2 s_red[kSsxBN][kNW][kThreads / 32];

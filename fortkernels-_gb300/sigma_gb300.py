@@ -60,6 +60,13 @@ SIGNATURES = {
     "sigma_gpp_plan_set_timing": ([_P, _I], _I),
     "sigma_gpp_plan_timing": ([_P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_fp64_noalloc": ([_I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_ff_schdt": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _I, _P], _I),
+    "sigma_ff_plan_create": ([_P, _I, _I, _I, _I, _P, _P, _I], _I),
+    "sigma_ff_execute": ([_P, _P, _P, _P, _P, _P], _I),
+    "sigma_ff_plan_destroy": ([_P], _I),
+    "sigma_ff_plan_set_timing": ([_P, _I], _I),
+    "sigma_ff_plan_timing": ([_P, _P, _P, _P, _P], _I),
+    "sigma_ff_plan_status": ([_P, _P], _I),
     "sigma_fill_uniform": ([_P, _LL, _LL, _ULL, _ULL, _LL, _LL, _D, _D, _P], _I),
     "sigma_fill_stress": ([_P, _LL, _ULL, _ULL, _P, _I, _D, _D, _P], _I),
     "sigma_measure_fma_peaks": ([_P, _P, _P], _I),
@@ -188,6 +195,62 @@ class GppPlan:
     def close(self):
         if getattr(self, "handle", None):
             self.lib.sigma_gpp_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ff_host(prob, mode: int = FF_MODE_FP64, stream: int = 0):
+    """Host-pointer FF drop-in on a workload.FFProblem; returns schDt[nb][nfreq]."""
+    lib = load()
+    inv = np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, dtype=np.int32)
+    epsr, aqsn, aqsm = _c128(prob.I_epsR), _c128(prob.aqsntemp), _c128(prob.aqsmtemp)
+    out = np.zeros((prob.number_bands, prob.nfreq), np.complex128)
+    st = lib.sigma_ff_schdt(prob.number_bands, prob.ncouls, prob.ngpown, prob.nfreq, _ptr(inv),
+                            _ptr(indinv), _ptr(epsr), _ptr(aqsn), _ptr(aqsm), _ptr(out), mode, stream)
+    _check(st, "sigma_ff_schdt")
+    return out
+
+
+class FfPlan:
+    """Device-resident FF plan (sigma_ff_plan_create / execute / destroy)."""
+
+    def __init__(self, number_bands, ncouls, ngpown, nfreq, inv_igp_index, indinv, mode=FF_MODE_FP64):
+        self.lib = load()
+        self.inv = np.ascontiguousarray(inv_igp_index, dtype=np.int32)
+        self.indinv = np.ascontiguousarray(indinv, dtype=np.int32)
+        h = C.c_void_p()
+        _check(self.lib.sigma_ff_plan_create(C.byref(h), number_bands, ncouls, ngpown, nfreq,
+                                             _ptr(self.inv), _ptr(self.indinv), mode),
+               "sigma_ff_plan_create")
+        self.handle = h
+
+    def execute(self, epsr, aqsn, aqsm, schdt, stream=0):
+        p = lambda a: a if isinstance(a, int) else _ptr(a)
+        _check(self.lib.sigma_ff_execute(self.handle, p(epsr), p(aqsn), p(aqsm), p(schdt), stream),
+               "sigma_ff_execute")
+
+    def set_timing(self, enable=True):
+        _check(self.lib.sigma_ff_plan_set_timing(self.handle, int(enable)), "sigma_ff_plan_set_timing")
+
+    def timing(self):
+        n, l = C.c_int(), C.c_int()
+        a, b = C.c_double(), C.c_double()
+        _check(self.lib.sigma_ff_plan_timing(self.handle, C.byref(n), C.byref(a), C.byref(b), C.byref(l)),
+               "sigma_ff_plan_timing")
+        return dict(executions=n.value, main_ms=a.value, other_ms=b.value, launches=l.value)
+
+    def status(self, stream=0):
+        return self.lib.sigma_ff_plan_status(self.handle, stream)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sigma_ff_plan_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

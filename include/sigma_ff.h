@@ -1,0 +1,75 @@
+/* sigma_ff.h - full-frequency (FF) sigma: the schDt contraction on GB300.
+ *
+ *   schDt[n1][ifreq] = sum_{my_igp} conj(aqsm[n1][igp])
+ *                        * sum_{ig} I_epsR[ifreq][my_igp][ig] * aqsn[n1][ig]
+ *   igp = indinv[inv_igp_index[my_igp]]
+ *
+ * This is the contraction of ffkernel.deslippe.best.f90:402-418 (a zgemm
+ * tempz = I_epsR^T aqsn followed by a conj(aqsm) reduction over my_igp, kept
+ * commented out in the reference) in the C layouts of FFKer_cori/ffKernel.cpp:
+ * I_epsR[ifreq][my_igp][ig] (:366, :430), aqsn/aqsm[n1][ig] (:360-363, :416),
+ * schDt_matrix[n1][ifreq] as achDtemp_Kernel reads it (:165).  The live
+ * reference code zeroes schDt_matrix instead (FFKer_cori/ffKernel.cpp:421-422).
+ * No vcoul factor, as in the source.  Every igp must lie in [0, ncouls)
+ * (the reference applies no clamp here); otherwise SIGMA_ERR_INDEX_RANGE.
+ *
+ * Arrays (row-major, interleaved complex128):
+ *   I_epsR        [nfreq][ngpown][ncouls]
+ *   aqsntemp      [number_bands][ncouls]
+ *   aqsmtemp      [number_bands][ncouls]
+ *   schDt_matrix  [number_bands][nfreq]   (output, overwritten)
+ */
+#ifndef SIGMA_FF_H
+#define SIGMA_FF_H
+
+#include "sigma_common.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum sigma_ff_mode {
+  SIGMA_FF_FP64 = 0,        /* complex FP64 GEMM on the FP64 pipe */
+  SIGMA_FF_OZAKI_BF16 = 1   /* each FP64 operand rounded to FP32 and split exactly into 3 BF16
+                               slices; the 6 leading slice products run on tcgen05 tensor cores
+                               with FP32 accumulation in tensor memory (leading product and
+                               corrections in separate accumulators); FP64 final reduction */
+};
+
+/* Host-pointer drop-in for the commented zgemm + reduction of
+ * ffkernel.deslippe.best.f90:402-418: copies the inputs to the device on
+ * `stream`, evaluates, copies schDt_matrix back and returns after the stream
+ * has drained. */
+int sigma_ff_schdt(int number_bands, int ncouls, int ngpown, int nfreq,
+                   const int* inv_igp_index, const int* indinv,
+                   const sigma_complex128* I_epsR, const sigma_complex128* aqsntemp,
+                   const sigma_complex128* aqsmtemp, sigma_complex128* schDt_matrix, int mode,
+                   void* stream);
+
+/* Device-resident plan: validates the index maps on the host, owns the
+ * partial-sum (and, for the Ozaki mode, BF16 slice) buffers.  Execution is
+ * asynchronous and allocates nothing; arrays are device pointers. */
+typedef struct sigma_ff_plan_s* sigma_ff_plan;
+
+int sigma_ff_plan_create(sigma_ff_plan* plan, int number_bands, int ncouls, int ngpown, int nfreq,
+                         const int* inv_igp_index, const int* indinv, int mode);
+int sigma_ff_execute(sigma_ff_plan plan, const sigma_complex128* I_epsR,
+                     const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
+                     sigma_complex128* schDt_matrix, void* stream);
+int sigma_ff_plan_destroy(sigma_ff_plan plan);
+
+/* Per-launch timing like sigma_gpp_plan_set_timing: the contraction kernel
+ * (main) and everything else (slicing pre-pass, reduction). */
+int sigma_ff_plan_set_timing(sigma_ff_plan plan, int enable);
+int sigma_ff_plan_timing(sigma_ff_plan plan, int* executions, double* main_ms, double* other_ms,
+                         int* launches_per_execution);
+
+/* Waits for `stream`; SIGMA_OK or SIGMA_ERR_TIMEOUT when a bounded device
+ * wait of the last execution gave up. */
+int sigma_ff_plan_status(sigma_ff_plan plan, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIGMA_FF_H */

@@ -117,3 +117,29 @@ def test_validation_precedes_device_work(libpath):
     if st == 0:
         lib.sigma_gpp_plan_destroy.argtypes = [C.c_void_p]
         lib.sigma_gpp_plan_destroy(h)
+
+
+def test_ff_validation_precedes_device_work(libpath):
+    lib = C.CDLL(str(libpath))
+    f = lib.sigma_ff_plan_create
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+    h = C.c_void_p()
+    nc, ng = 64, 8
+    inv = np.arange(ng, dtype=np.int32)
+    indinv = np.arange(nc, dtype=np.int32)
+    call = lambda nb, nc_, ng_, nf, inv_, ind_, mode: f(C.byref(h), nb, nc_, ng_, nf, inv_.ctypes.data,
+                                                       ind_.ctypes.data, mode)
+    assert call(4, nc, 65, 2, np.arange(65, dtype=np.int32), indinv, 0) == -1  # ngpown > ncouls
+    assert call(4, nc, ng, 0, inv, indinv, 0) == -1                             # no frequency
+    assert call(4, nc, ng, 2, inv, indinv, 5) == -8                             # unknown mode
+    bad = inv.copy()
+    bad[1] = nc                                  # indinv read past its end
+    assert call(4, nc, ng, 2, bad, indinv, 0) == -2
+    ind_bad = indinv.copy()
+    ind_bad[3] = -1                              # igp outside [0, ncouls)
+    assert call(4, nc, ng, 2, inv, ind_bad, 1) == -2
+    st = call(4, nc, ng, 2, inv, indinv, 0)
+    assert st in (0, -7, -4)
+    if st == 0:
+        lib.sigma_ff_plan_destroy.argtypes = [C.c_void_p]
+        lib.sigma_ff_plan_destroy(h)
