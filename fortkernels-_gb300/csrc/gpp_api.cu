@@ -41,7 +41,8 @@ namespace sigma {
 namespace {
 
 constexpr int kSsxBP = 256;
-constexpr int kItemsPerSlot = 48;  // work items per resident CTA (load balance of the tail)
+constexpr int kItemsPerSlot = 48;       // work items per resident CTA (load balance of the tail)
+constexpr int kItemsPerSlotMixed = 12;  // mixed items are 64x cheaper: fewer, longer items
 
 void size_work(GppWork& w, int band_begin, int band_count, int bn, int bp, int nc, int ng,
                int grid, int items_per_slot) {
@@ -142,7 +143,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   p->sch_grid = sms * (mixed ? sch_blocks_per_sm_mixed() : sch_blocks_per_sm_fp64());
   p->ssx_grid = sms * (mixed ? ssx_blocks_per_sm_mixed() : ssx_blocks_per_sm_fp64());
   size_work(p->sch, 0, number_bands, kBN, mixed ? kBPM : kBP, ncouls, ngpown, p->sch_grid,
-            kItemsPerSlot);
+            mixed ? kItemsPerSlotMixed : kItemsPerSlot);
   size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
   if (p->sch.n_items < p->sch_grid) p->sch_grid = p->sch.n_items;
   if (p->ssx.n_items < p->ssx_grid) p->ssx_grid = p->ssx.n_items;

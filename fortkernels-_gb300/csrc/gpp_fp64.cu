@@ -7,9 +7,10 @@
 // shared memory with coalesced 16-byte loads, and every thread evaluates a
 // 2 x 2 (band x column) register tile over the three frequencies.
 //
-// GB300 runs FP64 at 1/74 of its FP32 rate, so the term is rewritten to
-// spend as few FP64 pipe instructions as possible (9 per term plus 6 per
-// band/column/g-vector shared by the three frequencies):
+// GB300 runs FP64 at 1/64 of its FP32 rate, so the term is rewritten to
+// spend as few FP64 pipe instructions as possible (8 per term plus 6 per
+// band/column/g-vector shared by the three frequencies; the reciprocal is an
+// FP32 hardware seed refined by one FP64 Newton step, rcp_f64_seed32):
 //   scha / conj(aqsm[n1][igp]) = aqsn * I_eps * wtilde * conj(wdiff) / |wdiff|^2
 //                              = R * (c + i b) * r,   R = aqsn * (I_eps * wtilde),
 //   c = wx - Re wtilde, b = Im wtilde, r = 1 / (c^2 + b^2).
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
             for (int iw = 0; iw < kNW; ++iw) {
               const double c = __dsub_rn(wxr[i][iw], a[j]);
               const double wv = fma(c, c, b2[j]);
-              double r = rcp_f64(wv);
+              double r = rcp_f64_seed32(wv);
               r = gt_nonneg(wv, thr[j]) ? r : 0.0;
               const double ure = fma(R.x, c, -bRim);
               const double uim = fma(R.y, c, bRre);

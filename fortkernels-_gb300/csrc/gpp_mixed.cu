@@ -39,7 +39,7 @@ struct __align__(16) Stage {
 };
 struct __align__(16) SchSmemM {
   Stage st[2];
-  double2 red[kBN][kNW][kBPM];
+  double2 red[kNW][kBPM][kBN];
   unsigned long long bar[2];
 };
 static_assert(sizeof(Stage) == kChunkBytes, "one chunk is one contiguous copy per operand");
@@ -121,10 +121,18 @@ __device__ __forceinline__ bool keep_exact(const GppDev& p, int my_igp, int ig, 
 }
 
 // ---- pre-pass: FP32 operands in tile-interleaved layouts
+// With one frequency set for every band (wx_stride 0) the fourth operand
+// is a bit mask of the terms kept for frequency iw (bit iw), decided exactly
+// as the FP64 path decides; otherwise it is the FP32 threshold and the main
+// kernel decides per term.
 __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, int n_col_blocks) {
   __shared__ float4 ta[32][kBPM + 1];
   __shared__ float2 tb[32][kBPM + 1];
   const int tid = threadIdx.x;
+  const bool shared_wx = p.wx_stride == 0;
+  float wxh[kNW], wxl[kNW];
+#pragma unroll
+  for (int iw = 0; iw < kNW; ++iw) split_f(p.wx[iw], wxh[iw], wxl[iw]);
   const long long tiles = (long long)n_col_blocks * (m.nc_pad / 32);
   for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int cb = (int)(t / (m.nc_pad / 32));
@@ -135,6 +143,7 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
       const int my_igp = cb * kBPM + pl, ig = ig0 + k;
       float4 a = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7f800000));
       float2 g = make_float2(0.f, 0.f);
+      if (shared_wx) a.w = __uint_as_float(0u);  // padding: no term kept
       if (my_igp < p.ng && ig < p.nc) {
         const size_t off = (size_t)my_igp * p.nc + ig;
         const double2 wt = p.wt[off];
@@ -142,7 +151,30 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
         const double b2 = guard_b2(wt.y);
         split_f(wt.x, a.x, a.y);
         a.z = __double2float_rn(wt.y);
-        a.w = __double2float_rn(guard_thr(wt.x, b2));
+        const double thr = guard_thr(wt.x, b2);
+        if (shared_wx) {
+          // keep/drop of the three frequencies, decided once per (column,
+          // g-vector): FP32 when clear of the threshold, FP64 otherwise
+          const float t32 = __double2float_rn(thr);
+          const float bb = a.z * a.z;
+          unsigned mask = 0u;
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            const float c = (wxh[iw] - a.x) + (wxl[iw] - a.y);
+            const float wv = fmaf(c, c, bb);
+            bool keep;
+            if (wv > t32 * (1.0f + kGuardBand))
+              keep = true;
+            else if (wv <= t32 * (1.0f - kGuardBand))
+              keep = false;
+            else
+              keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2), thr);
+            mask |= keep ? (1u << iw) : 0u;
+          }
+          a.w = __uint_as_float(mask);
+        } else {
+          a.w = __double2float_rn(thr);
+        }
         const double2 gg = cmul(ie, wt);
         g = make_float2(__double2float_rn(gg.x), __double2float_rn(gg.y));
       }
@@ -187,13 +219,111 @@ __global__ void __launch_bounds__(256) prep_bands_kernel(GppDev p, MixedPrep m, 
 }
 
 // ---- main pass
+// The terms of one staged chunk (kCK g-vectors) for the thread's 2 bands x 1
+// column x 3 frequencies, folded into the float-float accumulators every
+// kRun g-vectors.  kMask: the keep decisions come as a per-(column,
+// g-vector) bit mask from the pre-pass; otherwise each term compares its FP32
+// |wdiff|^2 with the threshold and near-threshold terms are re-decided in
+// FP64.  kWxl: the frequencies are not exact in FP32 and carry a low part.
+template <bool kMask, bool kWxl>
+__device__ __forceinline__ void chunk_terms(const Stage& st, int pl, int ty, const float (&wxh)[kTN][kNW],
+                                            const float (&wxl)[kTN][kNW], float2 (&acc)[kTN][kNW],
+                                            float2 (&hi)[kTN][kNW], float2 (&lo)[kTN][kNW],
+                                            const GppDev& p, int n1_0, int my_igp, int ig0,
+                                            int ig_end, int band_end) {
+  const float band_lo = 1.0f - kGuardBand, band_hi = 1.0f + kGuardBand;
+#pragma unroll 1
+  for (int kr = 0; kr < kCK; kr += kRun) {
+#pragma unroll 2
+    for (int k = kr; k < kr + kRun; ++k) {
+      const float4 a = st.a[k][pl];
+      const float2 g = st.b[k][pl];
+      float2 nn[kTN];
+#pragma unroll
+      for (int i = 0; i < kTN; ++i) nn[i] = st.n[k][ty + 16 * i];
+      const float b2 = a.z * a.z;
+      if constexpr (kMask) {
+        const unsigned mask = __float_as_uint(a.w);
+#pragma unroll
+        for (int i = 0; i < kTN; ++i) {
+          const float2 R = cmulf(nn[i], g);
+          const float bRre = a.z * R.x, bRim = a.z * R.y;
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            const float c = kWxl ? (wxh[i][iw] - a.x) + (wxl[i][iw] - a.y) : (wxh[i][iw] - a.x) - a.y;
+            const float r = rcp_f32(fmaf(c, c, b2));
+            const float rm = (mask & (1u << iw)) ? r : 0.f;
+            acc[i][iw].x = fmaf(fmaf(R.x, c, -bRim), rm, acc[i][iw].x);
+            acc[i][iw].y = fmaf(fmaf(R.y, c, bRre), rm, acc[i][iw].y);
+          }
+        }
+      } else {
+        const float thi = a.w * band_hi, tlo = a.w * band_lo;
+        bool unc = false;
+#pragma unroll
+        for (int i = 0; i < kTN; ++i) {
+          const float2 R = cmulf(nn[i], g);
+          const float bRre = a.z * R.x, bRim = a.z * R.y;
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            const float c = (wxh[i][iw] - a.x) + (wxl[i][iw] - a.y);
+            const float wv = fmaf(c, c, b2);
+            const float r = rcp_f32(wv);
+            const bool keep = wv > thi;
+            unc |= (wv > tlo) && !keep;
+            const float rm = keep ? r : 0.f;
+            acc[i][iw].x = fmaf(fmaf(R.x, c, -bRim), rm, acc[i][iw].x);
+            acc[i][iw].y = fmaf(fmaf(R.y, c, bRre), rm, acc[i][iw].y);
+          }
+        }
+        if (__any_sync(0xffffffffu, unc)) {
+          // Terms near a threshold were dropped above; add back the ones the
+          // FP64 decision keeps.
+          const int ig = ig0 + k;
+#pragma unroll
+          for (int i = 0; i < kTN; ++i) {
+            const int n1 = n1_0 + ty + 16 * i;
+            const float2 R = cmulf(nn[i], g);
+            const float bRre = a.z * R.x, bRim = a.z * R.y;
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const float c = (wxh[i][iw] - a.x) + (wxl[i][iw] - a.y);
+              const float wv = fmaf(c, c, b2);
+              if (wv > tlo && !(wv > thi) && n1 < band_end && my_igp < p.ng && ig < ig_end &&
+                  keep_exact(p, my_igp, ig, p.wx[(size_t)n1 * p.wx_stride + iw])) {
+                const float r = rcp_f32(wv);
+                acc[i][iw].x = fmaf(fmaf(R.x, c, -bRim), r, acc[i][iw].x);
+                acc[i][iw].y = fmaf(fmaf(R.y, c, bRre), r, acc[i][iw].y);
+              }
+            }
+          }
+        }
+      }
+    }
+    // fold the FP32 run into the float-float accumulators
+#pragma unroll
+    for (int i = 0; i < kTN; ++i)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        float sum, err;
+        two_sum_f(hi[i][iw].x, acc[i][iw].x, sum, err);
+        hi[i][iw].x = sum;
+        lo[i][iw].x += err;
+        two_sum_f(hi[i][iw].y, acc[i][iw].y, sum, err);
+        hi[i][iw].y = sum;
+        lo[i][iw].y += err;
+        acc[i][iw] = make_float2(0.f, 0.f);
+      }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWork w, MixedPrep m) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SchSmemM& sm = *reinterpret_cast<SchSmemM*>(smem_raw);
   __shared__ int s_item;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int band_end = w.band_begin + w.band_count;
-  const float band_lo = 1.0f - kGuardBand, band_hi = 1.0f + kGuardBand;
+  const bool shared_wx = p.wx_stride == 0;
   if (tid == 0) {
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);
@@ -216,6 +346,7 @@ __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWor
     const int my_igp = ic.cb * kBPM + pl;
 
     float wxh[kTN][kNW], wxl[kTN][kNW];
+    bool exact = true;
 #pragma unroll
     for (int i = 0; i < kTN; ++i) {
       const int n1 = n1_0 + ty + 16 * i;
@@ -223,8 +354,10 @@ __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWor
       for (int iw = 0; iw < kNW; ++iw) {
         const double wx = n1 < band_end ? p.wx[(size_t)n1 * p.wx_stride + iw] : 0.0;
         split_f(wx, wxh[i][iw], wxl[i][iw]);
+        exact = exact && wxl[i][iw] == 0.f;
       }
     }
+    const bool wx_exact = __syncthreads_and(exact) != 0;  // every frequency exact in FP32
     float2 acc[kTN][kNW], hi[kTN][kNW], lo[kTN][kNW];
 #pragma unroll
     for (int i = 0; i < kTN; ++i)
@@ -249,72 +382,13 @@ __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWor
         phase1 ^= 1;
       }
       const Stage& st = sm.st[buf];
-
-#pragma unroll 1
-      for (int kr = 0; kr < kCK; kr += kRun) {
-#pragma unroll 2
-        for (int k = kr; k < kr + kRun; ++k) {
-          const float4 a = st.a[k][pl];
-          const float2 g = st.b[k][pl];
-          float2 nn[kTN];
-#pragma unroll
-          for (int i = 0; i < kTN; ++i) nn[i] = st.n[k][ty + 16 * i];
-          const float thi = a.w * band_hi, tlo = a.w * band_lo;
-          const float b2 = a.z * a.z;
-          bool unc = false;
-#pragma unroll
-          for (int i = 0; i < kTN; ++i) {
-            const float2 R = cmulf(nn[i], g);
-            const float bRre = a.z * R.x, bRim = a.z * R.y;
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) {
-              const float c = (wxh[i][iw] - a.x) + (wxl[i][iw] - a.y);
-              const float wv = fmaf(c, c, b2);
-              const float r = rcp_f32(wv);
-              const bool keep = wv > thi;
-              unc |= (wv > tlo) && !keep;
-              const float rm = keep ? r : 0.f;
-              acc[i][iw].x = fmaf(fmaf(R.x, c, -bRim), rm, acc[i][iw].x);
-              acc[i][iw].y = fmaf(fmaf(R.y, c, bRre), rm, acc[i][iw].y);
-            }
-          }
-          if (__any_sync(0xffffffffu, unc)) {
-            // Terms near a threshold were dropped above; add back the ones the
-            // FP64 decision keeps.
-            const int ig = ig0 + k;
-#pragma unroll
-            for (int i = 0; i < kTN; ++i) {
-              const int n1 = n1_0 + ty + 16 * i;
-              const float2 R = cmulf(nn[i], g);
-              const float bRre = a.z * R.x, bRim = a.z * R.y;
-#pragma unroll
-              for (int iw = 0; iw < kNW; ++iw) {
-                const float c = (wxh[i][iw] - a.x) + (wxl[i][iw] - a.y);
-                const float wv = fmaf(c, c, b2);
-                if (wv > tlo && !(wv > thi) && n1 < band_end && my_igp < p.ng && ig < ig_end &&
-                    keep_exact(p, my_igp, ig, p.wx[(size_t)n1 * p.wx_stride + iw])) {
-                  const float r = rcp_f32(wv);
-                  acc[i][iw].x = fmaf(fmaf(R.x, c, -bRim), r, acc[i][iw].x);
-                  acc[i][iw].y = fmaf(fmaf(R.y, c, bRre), r, acc[i][iw].y);
-                }
-              }
-            }
-          }
-        }
-        // fold the FP32 run into the float-float accumulators
-#pragma unroll
-        for (int i = 0; i < kTN; ++i)
-#pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) {
-            float s, e;
-            two_sum_f(hi[i][iw].x, acc[i][iw].x, s, e);
-            hi[i][iw].x = s;
-            lo[i][iw].x += e;
-            two_sum_f(hi[i][iw].y, acc[i][iw].y, s, e);
-            hi[i][iw].y = s;
-            lo[i][iw].y += e;
-            acc[i][iw] = make_float2(0.f, 0.f);
-          }
+      if (shared_wx) {
+        if (wx_exact)
+          chunk_terms<true, false>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
+        else
+          chunk_terms<true, true>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
+      } else {
+        chunk_terms<false, true>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
       }
       __syncthreads();  // every thread is done with this stage before it is refilled
     }
@@ -335,22 +409,22 @@ __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWor
           const double2 sv = make_double2((double)hi[i][iw].x + (double)lo[i][iw].x,
                                           (double)hi[i][iw].y + (double)lo[i][iw].y);
           const double2 v = cmul(sv, mm);
-          sm.red[bl][iw][pl] = make_double2(v.x * f, v.y * f);
+          sm.red[iw][pl][bl] = make_double2(v.x * f, v.y * f);
         }
       } else {
 #pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) sm.red[bl][iw][pl] = make_double2(0.0, 0.0);
+        for (int iw = 0; iw < kNW; ++iw) sm.red[iw][pl][bl] = make_double2(0.0, 0.0);
       }
     }
     __syncthreads();
     if (tid < kBN * kNW) {
-      const int bl = tid / kNW, iw = tid % kNW;
+      const int iw = tid / kBN, bl = tid % kBN;
       Comp sx, sy;
       for (int q = 0; q < kBPM; ++q) {
-        sx.add(sm.red[bl][iw][q].x);
-        sy.add(sm.red[bl][iw][q].y);
+        sx.add(sm.red[iw][q][bl].x);
+        sy.add(sm.red[iw][q][bl].y);
       }
-      w.partial[ic.pidx * kBN * kNW + tid] = make_double2(sx.value(), sy.value());
+      w.partial[ic.pidx * kBN * kNW + bl * kNW + iw] = make_double2(sx.value(), sy.value());
     }
   }
 }

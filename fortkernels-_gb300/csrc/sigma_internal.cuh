@@ -129,6 +129,28 @@ __device__ __forceinline__ double rcp_f64(double w) {
   return fma(r0, e2, r0);
 }
 
+// 1/w for a positive normal double with two DFMA: an FP32 seed from the
+// hardware reciprocal of w's leading 23 mantissa bits (the exponent handled
+// on the integer pipe), then one Newton-Raphson step.  The seed is within
+// 2^-22.4 (23-bit truncation plus the 2^-23.3 error of rcp.approx.f32), so
+// the result is within 2^-44.8 ~ 3.2e-14 relative, from below.  For w that is
+// zero, denormal or not finite the result is meaningless; callers drop those
+// terms.
+__device__ __forceinline__ double rcp_f64_seed32(double w) {
+  const int hi = __double2hiint(w);
+  const unsigned lo = (unsigned)__double2loint(w);
+  const unsigned mant = (((unsigned)hi & 0xFFFFFu) << 3) | (lo >> 29);
+  const float m = __uint_as_float(0x3F800000u | mant);  // 1.mant in [1, 2)
+  float rm;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rm) : "f"(m));
+  const unsigned rb = __float_as_uint(rm);
+  const int e = (int)((rb >> 23) & 0xFFu) - 127 - (((hi >> 20) & 0x7FF) - 1023) + 1023;
+  const double r0 = __hiloint2double((int)(((unsigned)e << 20) | ((rb & 0x7FFFFFu) >> 3)),
+                                     (int)((rb & 0x7u) << 29));
+  const double eps = fma(-w, r0, 1.0);
+  return fma(r0, eps, r0);
+}
+
 __device__ __forceinline__ float rcp_f32(float w) {
   // MUFU.RCP plus one Newton-Raphson step r = r0 (2 - w r0).
   float r0;

@@ -155,6 +155,17 @@ def test_per_band_frequencies(sigma_lib, prec):
 
 
 @pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
+def test_frequencies_not_exact_in_fp32(sigma_lib, prec):
+    # shared frequencies with a low part below FP32 precision (the mixed path
+    # then carries wx as an FP32 hi/lo pair)
+    prob = W.gpp_random(30, 2, 1500, 40, 25)
+    prob.wx_array = np.array([3.1, 4.2 + 1e-9, 5.3])
+    o = O.gpp(prob)
+    g = _run_plan(sigma_lib, prob, prec)[0]
+    _check(g, o, prec)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
 def test_bitwise_repeatable(sigma_lib, prec):
     prob = W.gpp_random(50, 2, 3000, 75, 24, stress=True)
     outs = _run_plan(sigma_lib, prob, prec, reps=3)
