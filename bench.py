@@ -317,6 +317,54 @@ def run_ff(S, W, torch, dist, world, stream, sptr, args):
     return res
 
 
+def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
+    """48 uneven GPP instances (workload.batched_shapes) through the batched
+    API, one CUDA-graph replay per step, FP64 (tiles from the tuning table)
+    and mixed; Gterms/s over the whole batch and the mixed outputs' error
+    against the FP64 ones."""
+    import autotune
+    import batched
+
+    xs = batched.device_instances()
+    dicts = [x.as_dict() for x in xs]
+    tiles = [autotune.tile_for(x.nb, x.ng) for x in xs]
+    res = {"workload": "48 GPP instances, number_bands U{64..512}, ncouls U{4096..32768}/256, "
+                       "nodes_per_group U{10..40}, nvband U{1..8}, seeds 1000+i",
+           "instances": len(xs), "input_bytes": int(sum(x.input_bytes for x in xs)),
+           "tiles": {"table": autotune.load_table() is not None,
+                     "counts": {autotune.TILES[t] if t >= 0 else "library": tiles.count(t)
+                                for t in sorted(set(tiles))}}}
+    outs = {}
+    gs = torch.cuda.Stream()  # graphs are captured on a non-default stream
+    gptr = gs.cuda_stream
+    torch.cuda.synchronize()
+    for prec, name, steps in ((S.PREC_FP64, "fp64", 2), (S.PREC_MIXED, "mixed", 5)):
+        b = S.GppBatch(dicts, precision=prec, tiles=tiles if prec == S.PREC_FP64 else None)
+        terms, items, launches = b.info()
+        b.launch_graph(gptr)  # capture, and the warm-up replay
+        ms = timed(torch, dist, world, lambda: b.launch_graph(gptr), steps, gs)
+        st = b.status(gptr)
+        outs[name] = [x.outputs() for x in xs]
+        res[name] = {"value": round(terms * world / (ms / steps * 1e-3) / 1e9, 4), "unit": UNIT,
+                     "ms_per_step": round(ms / steps, 3), "steps": steps, "terms_per_step": terms,
+                     "items": items, "kernels_per_step": launches, "status": st}
+        b.close()
+    worst, over = 0.0, 0
+    for a, m in zip(outs["fp64"], outs["mixed"]):
+        for k in (0, 1):
+            e = np.abs(m[k] - a[k]) / np.abs(a[k])
+            worst = max(worst, float(e.max()))
+            over += int(np.sum(e > 1e-6))
+    res["mixed"]["max_rel_err_vs_fp64"] = worst
+    res["mixed"]["outputs_over_1e-6"] = over
+    res["mixed"]["outputs"] = 6 * len(xs)
+    res["mixed"]["speedup_vs_fp64_batched"] = round(res["mixed"]["value"] / res["fp64"]["value"], 2)
+    res["mixed"]["speedup_vs_fp64_dropin"] = round(res["mixed"]["value"] / dropin_value, 2)
+    del xs, dicts
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import sigma_gb300 as S
@@ -433,6 +481,7 @@ def run_ours(args, rank, world, local_rank):
     fp64_pipe_peak = 2 * 2 * sms * clock_mhz * 1e6 / 1e12
     fp32_pipe_peak = 2 * 128 * sms * clock_mhz * 1e6 / 1e12
     ff = None if args.no_ff else run_ff(S, W, torch, dist, world, stream, sptr, args)
+    batch = None if args.no_batched else run_batched(S, W, torch, dist, world, stream, sptr, args, value)
     worst = max(max(mixed_err["achtemp"]), max(mixed_err["asxtemp"]),
                 max(stress_err["achtemp"]), max(stress_err["asxtemp"]))
     line = {
@@ -473,6 +522,7 @@ def run_ours(args, rank, world, local_rank):
                                "frac": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12 / fp32_pipe_peak, 4),
                                "peak_source": "FP32 pipe 128 FFMA/clk/SM at the sampled SM clock"}},
         "ff": ff,
+        "batched": batch,
         "peaks_measured": {"fp64_fma_probe_tflops": round(fp64_peak, 4),
                            "fp32_fma_probe_tflops": round(fp32_peak, 3),
                            "fp64_pipe_tflops_at_clock": round(fp64_pipe_peak, 4),
@@ -498,6 +548,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ff", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--bands", type=int, default=NB,
                     help="number_bands of the instance (512 = the production shape; smaller only "
                          "for profiling captures)")

@@ -1,0 +1,124 @@
+"""Tile-shape tuner for the batched FP64 GPP main pass.
+
+Each work item of the main pass covers a (band block x column block x
+g-vector split) tile.  Three tile shapes are compiled: 32 bands x 32 columns,
+16 x 64 and 64 x 16 (same 1024 (band, column) pairs per item, 256 threads
+with 2 x 2 pairs each).  Which one is fastest depends on how the instance's
+number_bands and ngpown pad to the block sizes and on how much staged data
+each item re-reads, so the choice is made per shape class:
+
+    class "b{i}c{j}":  i = ((ceil(number_bands / 16) - 1) mod 4),
+                       j = ((ceil(ngpown / 16) - 1) mod 4)
+
+i.e. how many 16-band (16-column) slabs the last 64-wide block holds.  The
+tuner times every tile on one representative instance per class (nc = 4096;
+all tiles scale the same way in ncouls) through a one-instance batch replayed
+as a CUDA graph, and writes the fastest tile per class to
+`tuning/gpp_tiles_gb300.json`.  `tile_for()` reads that table; without it the
+library picks the least-padded tile itself.
+
+    python fortkernels-_gb300/autotune.py --out <path>
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import pathlib
+
+PKG = pathlib.Path(__file__).resolve().parent
+TABLE = PKG / "tuning" / "gpp_tiles_gb300.json"
+TILES = {0: "32x32", 1: "16x64", 2: "64x16"}
+_table = None
+
+
+def shape_class(number_bands: int, ngpown: int) -> str:
+    i = ((number_bands + 15) // 16 - 1) % 4
+    j = ((ngpown + 15) // 16 - 1) % 4
+    return f"b{i}c{j}"
+
+
+def load_table(path=None):
+    global _table
+    if path is None and _table is not None:
+        return _table
+    p = pathlib.Path(path) if path else TABLE
+    t = json.loads(p.read_text()) if p.exists() else None
+    if path is None:
+        _table = t
+    return t
+
+
+def tile_for(number_bands: int, ngpown: int, table=None) -> int:
+    """Tuned tile for this shape (-1 = the library's least-padding choice)."""
+    t = table if table is not None else load_table()
+    if not t:
+        return -1
+    return int(t["classes"].get(shape_class(number_bands, ngpown), -1))
+
+
+def representative(cls_i: int, cls_j: int):
+    """number_bands, ngpown of the class's representative instance."""
+    return 256 + 16 * cls_i + 9, 512 + 16 * cls_j + 9
+
+
+def tune(reps=5, ncouls=4096, log=print):
+    import torch
+
+    import batched
+    import sigma_gb300 as S
+
+    S.load()
+    stream = torch.cuda.Stream()
+    classes, timings = {}, {}
+    for i in range(4):
+        for j in range(4):
+            nb, ng = representative(i, j)
+            key = shape_class(nb, ng)
+            inst = batched.DeviceInstance(nb, 2, ncouls, ng, seed=5000 + 4 * i + j)
+            ms = {}
+            for tile in TILES:
+                b = S.GppBatch([inst.as_dict()], precision=S.PREC_FP64, tiles=[tile])
+                b.launch_graph(stream.cuda_stream)  # capture + warm-up
+                b.launch_graph(stream.cuda_stream)
+                stream.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    b.launch_graph(stream.cuda_stream)
+                e1.record(stream)
+                stream.synchronize()
+                if b.status(stream.cuda_stream) != 0:
+                    raise RuntimeError(f"batch status {b.status(stream.cuda_stream)} in tuning")
+                ms[TILES[tile]] = e0.elapsed_time(e1) / reps
+                b.close()
+            best = min(ms, key=ms.get)
+            classes[key] = [k for k, v in TILES.items() if v == best][0]
+            timings[key] = {"number_bands": nb, "ngpown": ng, "ncouls": ncouls,
+                            "ms": {k: round(v, 4) for k, v in ms.items()}}
+            log(key, nb, ng, {k: round(v, 3) for k, v in ms.items()}, "->", best)
+            del inst
+            torch.cuda.empty_cache()
+    return {"version": 1, "device": torch.cuda.get_device_name(),
+            "tiles": {str(k): v for k, v in TILES.items()},
+            "class_rule": "b{i}c{j}: i = (ceil(number_bands/16)-1) mod 4, j = (ceil(ngpown/16)-1) mod 4",
+            "classes": classes, "timings": timings}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=str(TABLE))
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args()
+    t = tune(a.reps)
+    out = pathlib.Path(a.out)
+    out.parent.mkdir(parents=True, exist_ok=True)
+    out.write_text(json.dumps(t, indent=1) + "\n")
+    print(f"wrote {out}")
+
+
+if __name__ == "__main__":
+    import sys
+    for p in (str(PKG), str(PKG.parent)):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    main()

@@ -38,16 +38,12 @@ constexpr int kMaxTimedExecutions = 256;
 }
 
 namespace sigma {
-namespace {
 
-constexpr int kSsxBP = 256;
-constexpr int kItemsPerSlot = 48;       // work items per resident CTA (load balance of the tail)
-constexpr int kItemsPerSlotMixed = 12;  // mixed items are 64x cheaper: fewer, longer items
-
-void size_work(GppWork& w, int band_begin, int band_count, int bn, int bp, int nc, int ng,
+void gpp_size_work(GppWork& w, int band_begin, int band_count, int bn, int bp, int nc, int ng,
                int grid, int items_per_slot) {
   w.band_begin = band_begin;
   w.band_count = band_count;
+  w.bn = bn;
   w.n_band_blocks = (band_count + bn - 1) / bn;
   w.n_col_blocks = (ng + bp - 1) / bp;
   const long long base = (long long)w.n_band_blocks * w.n_col_blocks;
@@ -71,7 +67,7 @@ void size_work(GppWork& w, int band_begin, int band_count, int bn, int bp, int n
 // Column map of BGW-Kernels/gppKer.cpp:322-328.  Returns SIGMA_OK or
 // SIGMA_ERR_INDEX_RANGE where the reference would read out of bounds
 // (indinv at indigp > ncouls, aqsmtemp / vcoul at igp == ncouls).
-int map_columns(int nc, int ng, const int* inv, const int* indinv, int indinv_len,
+int gpp_map_columns(int nc, int ng, const int* inv, const int* indinv, int indinv_len,
                 std::vector<int>& igp_of, int& valid) {
   igp_of.resize(ng);
   valid = 0;
@@ -96,11 +92,16 @@ int map_columns(int nc, int ng, const int* inv, const int* indinv, int indinv_le
   return SIGMA_OK;
 }
 
-int check_shape(int nb, int nvband, int nc, int ng, int nstart, int nend) {
+int gpp_check_shape(int nb, int nvband, int nc, int ng, int nstart, int nend) {
   if (nb <= 0 || nc <= 0 || ng <= 0 || ng > nc || nvband < 0 || nvband > nb) return SIGMA_ERR_INVALID_SHAPE;
   if (nstart != 0 || nend - nstart != kNW) return SIGMA_ERR_INVALID_SHAPE;
   return SIGMA_OK;
 }
+
+namespace {
+
+constexpr int kItemsPerSlot = 48;       // work items per resident CTA (load balance of the tail)
+constexpr int kItemsPerSlotMixed = 12;  // mixed items are 64x cheaper: fewer, longer items
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -114,13 +115,13 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   using namespace sigma;
   if (!plan_out || !inv_igp_index || !indinv) return SIGMA_ERR_NULL;
   *plan_out = nullptr;
-  int st = check_shape(number_bands, nvband, ncouls, ngpown, nstart, nend);
+  int st = gpp_check_shape(number_bands, nvband, ncouls, ngpown, nstart, nend);
   if (st != SIGMA_OK) return st;
   if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED) return SIGMA_ERR_UNSUPPORTED;
   if (indinv_len < ncouls) return SIGMA_ERR_INVALID_SHAPE;
   std::vector<int> igp_of;
   int valid = 0;
-  st = map_columns(ncouls, ngpown, inv_igp_index, indinv, indinv_len, igp_of, valid);
+  st = gpp_map_columns(ncouls, ngpown, inv_igp_index, indinv, indinv_len, igp_of, valid);
   if (st != SIGMA_OK) return st;
 
   int dev = 0;
@@ -142,9 +143,9 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   const bool mixed = precision == SIGMA_PREC_MIXED;
   p->sch_grid = sms * (mixed ? sch_blocks_per_sm_mixed() : sch_blocks_per_sm_fp64());
   p->ssx_grid = sms * (mixed ? ssx_blocks_per_sm_mixed() : ssx_blocks_per_sm_fp64());
-  size_work(p->sch, 0, number_bands, kBN, mixed ? kBPM : kBP, ncouls, ngpown, p->sch_grid,
+  gpp_size_work(p->sch, 0, number_bands, kBN, mixed ? kBPM : kBP, ncouls, ngpown, p->sch_grid,
             mixed ? kItemsPerSlotMixed : kItemsPerSlot);
-  size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
+  gpp_size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
   if (p->sch.n_items < p->sch_grid) p->sch_grid = p->sch.n_items;
   if (p->ssx.n_items < p->ssx_grid) p->ssx_grid = p->ssx.n_items;
 
@@ -365,7 +366,7 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
              void* stream) {
   if (!inv || !indinv || !wx || !aqsm || !aqsn || !ieps || !wt || !vcoul || !achtemp || !asxtemp)
     return SIGMA_ERR_NULL;
-  int st = check_shape(nb, nvband, nc, ng, nstart, nend);
+  int st = gpp_check_shape(nb, nvband, nc, ng, nstart, nend);
   if (st != SIGMA_OK) return st;
   std::lock_guard<std::mutex> lk(api_mutex());
   int dev = 0;

@@ -1,0 +1,356 @@
+// Batched GPP: many sigma instances through one work queue per pass.
+//
+// The reference evaluates one instance per run of its driver
+// (BGW-Kernels/gppKer.cpp:161-449).  A production sigma calculation has many
+// (q-points, band windows) of uneven shape.  Here the main pass and the
+// occupied-band pass of all instances each run as ONE persistent kernel over
+// the concatenation of every instance's work items; per-instance pre-passes
+// (mixed form) and the fixed-order reductions run around them, and the whole
+// sequence is captured once in a CUDA graph and replayed.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "sigma_gpp.h"
+#include "sigma_internal.cuh"
+#include "gpp_batch.cuh"
+#include "runtime.h"
+
+namespace sigma {
+int sch_blocks_per_sm_fp64();
+}
+
+struct sigma_gpp_batch_s {
+  int device = 0, n = 0, precision = 0;
+  std::vector<sigma::GppDev> dev;
+  std::vector<sigma::GppWork> sch, ssx;
+  std::vector<sigma::MixedPrep> prep;
+  std::vector<int> tile, sch_off, ssx_off;
+  std::vector<double2*> acht_n1;
+  std::vector<sigma_gpp_instance> inst;
+  long long terms = 0;
+  int sch_grid = 0, ssx_grid = 0, launches = 0;
+  void* block = nullptr;
+  sigma::GppBatchView sch_view{}, ssx_view{};
+  int* counters = nullptr;  // [0] main pass, [1] occupied-band pass, [2] status
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace sigma {
+namespace {
+
+constexpr int kBatchItemsPerSlot = 16;
+size_t up256(size_t v) { return (v + 255) / 256 * 256; }
+
+// Least padded work among the FP64 tile shapes (bands and columns padded up
+// to the tile), ties to the square tile.
+int least_padding_tile(int nb, int ng) {
+  int best = kTile32x32;
+  double best_cost = 1e300;
+  for (int t = 0; t < kTileCount; ++t) {
+    const double cost = (double)((nb + tile_bn(t) - 1) / tile_bn(t) * tile_bn(t)) *
+                        (double)((ng + tile_bp(t) - 1) / tile_bp(t) * tile_bp(t));
+    if (cost < best_cost - 0.5) {
+      best_cost = cost;
+      best = t;
+    }
+  }
+  return best;
+}
+
+// Splits so that one item of this instance holds about `target` terms.
+void size_instance(GppWork& w, int band_count, int bn, int bp, int nc, int ng, double target) {
+  gpp_size_work(w, 0, band_count, bn, bp, nc, ng, 1, 1);
+  if (w.n_items == 0) return;
+  const double per_block = (double)bn * bp * nc * kNW;
+  int s = (int)(per_block / target + 0.5);
+  if (s < 1) s = 1;
+  int len = (nc + s - 1) / s;
+  len = (len + kCK - 1) / kCK * kCK;
+  w.split_len = len;
+  w.n_splits = (nc + len - 1) / len;
+  w.n_items = w.n_band_blocks * w.n_col_blocks * w.n_splits;
+}
+
+}  // namespace
+}  // namespace sigma
+
+extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
+                                      const sigma_gpp_instance* inst, int precision,
+                                      const int* tile_shape) {
+  using namespace sigma;
+  if (!out || !inst) return SIGMA_ERR_NULL;
+  *out = nullptr;
+  if (n_instances <= 0) return SIGMA_ERR_INVALID_SHAPE;
+  if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED) return SIGMA_ERR_UNSUPPORTED;
+  const bool mixed = precision == SIGMA_PREC_MIXED;
+  std::vector<std::vector<int>> igp(n_instances);
+  long long terms = 0;
+  for (int i = 0; i < n_instances; ++i) {
+    const sigma_gpp_instance& q = inst[i];
+    if (!q.inv_igp_index || !q.indinv || !q.wx_array || !q.aqsmtemp || !q.aqsntemp ||
+        !q.I_eps_array || !q.wtilde_array || !q.vcoul || !q.achtemp || !q.asxtemp)
+      return SIGMA_ERR_NULL;
+    int st = gpp_check_shape(q.number_bands, q.nvband, q.ncouls, q.ngpown, 0, kNW);
+    if (st != SIGMA_OK) return st;
+    if (q.wx_band_stride != 0 && q.wx_band_stride < kNW) return SIGMA_ERR_INVALID_SHAPE;
+    if (tile_shape && (tile_shape[i] < -1 || tile_shape[i] >= kTileCount)) return SIGMA_ERR_UNSUPPORTED;
+    int valid = 0;
+    st = gpp_map_columns(q.ncouls, q.ngpown, q.inv_igp_index, q.indinv, q.ncouls, igp[i], valid);
+    if (st != SIGMA_OK) return st;
+    terms += (long long)q.number_bands * valid * q.ncouls * kNW;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return SIGMA_ERR_NO_DEVICE;
+  }
+  const int sms = device_sm_count();
+  if (sms <= 0) return SIGMA_ERR_NO_DEVICE;
+
+  auto* b = new sigma_gpp_batch_s();
+  b->device = dev;
+  b->n = n_instances;
+  b->precision = precision;
+  b->terms = terms;
+  b->inst.assign(inst, inst + n_instances);
+  b->sch_grid = sms * (mixed ? sch_batch_blocks_per_sm_mixed() : sch_batch_blocks_per_sm_fp64());
+  b->ssx_grid = sms * (mixed ? ssx_batch_blocks_per_sm_mixed() : ssx_batch_blocks_per_sm_fp64());
+  b->dev.resize(n_instances);
+  b->sch.resize(n_instances);
+  b->ssx.resize(n_instances);
+  b->prep.resize(n_instances);
+  b->tile.resize(n_instances);
+  b->acht_n1.resize(n_instances);
+  b->sch_off.assign(n_instances + 1, 0);
+  b->ssx_off.assign(n_instances + 1, 0);
+
+  // item size: the batch's terms spread over ~kBatchItemsPerSlot items per resident CTA
+  const double target = std::max(1.0, (double)terms / ((double)b->sch_grid * kBatchItemsPerSlot));
+  long long ssx_terms = 0;
+  for (int i = 0; i < n_instances; ++i)
+    ssx_terms += (long long)inst[i].nvband * inst[i].ngpown * inst[i].ncouls * kNW;
+  const double ssx_target = std::max(1.0, (double)ssx_terms / ((double)b->ssx_grid * 8));
+
+  // device layout: per-instance buffers, then the descriptor arrays
+  std::vector<size_t> o_igp(n_instances), o_n1(n_instances), o_sch(n_instances), o_ssx(n_instances),
+      o_a(n_instances), o_b(n_instances), o_band(n_instances);
+  size_t total = 256;  // counters
+  for (int i = 0; i < n_instances; ++i) {
+    const sigma_gpp_instance& q = inst[i];
+    const int t = mixed ? kTile32x32
+                        : (tile_shape && tile_shape[i] >= 0 ? tile_shape[i]
+                                                            : least_padding_tile(q.number_bands, q.ngpown));
+    b->tile[i] = t;
+    const int bn = mixed ? kBN : tile_bn(t), bp = mixed ? kBPM : tile_bp(t);
+    size_instance(b->sch[i], q.number_bands, bn, bp, q.ncouls, q.ngpown, target);
+    size_instance(b->ssx[i], q.nvband, kSsxBN, kSsxBP, q.ncouls, q.ngpown, ssx_target);
+    b->sch_off[i + 1] = b->sch_off[i] + b->sch[i].n_items;
+    b->ssx_off[i + 1] = b->ssx_off[i] + b->ssx[i].n_items;
+    const int nc_pad = (q.ncouls + kCK - 1) / kCK * kCK;
+    o_igp[i] = total;
+    total += up256(sizeof(int) * q.ngpown);
+    o_n1[i] = total;
+    total += up256(sizeof(double2) * (size_t)(q.number_bands + q.nvband) * kNW);
+    o_sch[i] = total;
+    total += up256(sizeof(double2) * (size_t)b->sch[i].n_items * bn * kNW);
+    o_ssx[i] = total;
+    total += up256(sizeof(double2) * (size_t)b->ssx[i].n_items * kSsxBN * kNW);
+    if (mixed) {
+      const size_t col = (size_t)b->sch[i].n_col_blocks * kBPM * nc_pad;
+      const size_t band = (size_t)b->sch[i].n_band_blocks * kBN * nc_pad;
+      o_a[i] = total;
+      total += up256(sizeof(float4) * col);
+      o_b[i] = total;
+      total += up256(sizeof(float2) * col);
+      o_band[i] = total;
+      total += up256(sizeof(float2) * band);
+    }
+  }
+  const size_t o_dev = total;
+  total += up256(sizeof(GppDev) * n_instances);
+  const size_t o_wsch = total;
+  total += up256(sizeof(GppWork) * n_instances);
+  const size_t o_wssx = total;
+  total += up256(sizeof(GppWork) * n_instances);
+  const size_t o_prep = total;
+  total += up256(sizeof(MixedPrep) * n_instances);
+  const size_t o_schoff = total;
+  total += up256(sizeof(int) * (n_instances + 1));
+  const size_t o_ssxoff = total;
+  total += up256(sizeof(int) * (n_instances + 1));
+  const size_t o_tile = total;
+  total += up256(sizeof(int) * n_instances);
+
+  cudaError_t e = cudaMalloc(&b->block, total);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_last_cuda_error(e, "cudaMalloc(batch)", __LINE__);
+    delete b;
+    return SIGMA_ERR_ALLOC;
+  }
+  char* base = static_cast<char*>(b->block);
+  b->counters = reinterpret_cast<int*>(base);
+  for (int i = 0; i < n_instances; ++i) {
+    const sigma_gpp_instance& q = inst[i];
+    GppDev& p = b->dev[i];
+    p.nb = q.number_bands;
+    p.nvband = q.nvband;
+    p.nc = q.ncouls;
+    p.ng = q.ngpown;
+    p.wx_stride = q.wx_band_stride;
+    p.occ = q.occ;
+    p.aqsm = reinterpret_cast<const double2*>(q.aqsmtemp);
+    p.aqsn = reinterpret_cast<const double2*>(q.aqsntemp);
+    p.ieps = reinterpret_cast<const double2*>(q.I_eps_array);
+    p.wt = reinterpret_cast<const double2*>(q.wtilde_array);
+    p.vcoul = q.vcoul;
+    p.wx = q.wx_array;
+    p.igp_of = reinterpret_cast<const int*>(base + o_igp[i]);
+    b->sch[i].counter = b->counters;
+    b->ssx[i].counter = b->counters + 1;
+    b->sch[i].partial = reinterpret_cast<double2*>(base + o_sch[i]);
+    b->ssx[i].partial = reinterpret_cast<double2*>(base + o_ssx[i]);
+    b->acht_n1[i] = reinterpret_cast<double2*>(base + o_n1[i]);
+    MixedPrep& m = b->prep[i];
+    m.nc_pad = (q.ncouls + kCK - 1) / kCK * kCK;
+    m.status = b->counters + 2;
+    m.colA = mixed ? reinterpret_cast<float4*>(base + o_a[i]) : nullptr;
+    m.colB = mixed ? reinterpret_cast<float2*>(base + o_b[i]) : nullptr;
+    m.band = mixed ? reinterpret_cast<float2*>(base + o_band[i]) : nullptr;
+  }
+  int rc = SIGMA_OK;
+  auto up = [&](size_t off, const void* src, size_t bytes) {
+    if (rc != SIGMA_OK) return;
+    cudaError_t ce = cudaMemcpy(base + off, src, bytes, cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+      set_last_cuda_error(ce, "cudaMemcpy(batch)", __LINE__);
+      rc = SIGMA_ERR_CUDA;
+    }
+  };
+  for (int i = 0; i < n_instances; ++i) up(o_igp[i], igp[i].data(), sizeof(int) * igp[i].size());
+  up(o_dev, b->dev.data(), sizeof(GppDev) * n_instances);
+  up(o_wsch, b->sch.data(), sizeof(GppWork) * n_instances);
+  up(o_wssx, b->ssx.data(), sizeof(GppWork) * n_instances);
+  up(o_prep, b->prep.data(), sizeof(MixedPrep) * n_instances);
+  up(o_schoff, b->sch_off.data(), sizeof(int) * (n_instances + 1));
+  up(o_ssxoff, b->ssx_off.data(), sizeof(int) * (n_instances + 1));
+  up(o_tile, b->tile.data(), sizeof(int) * n_instances);
+  if (rc != SIGMA_OK) {
+    cudaFree(b->block);
+    delete b;
+    return rc;
+  }
+  GppBatchView& v = b->sch_view;
+  v.dev = reinterpret_cast<const GppDev*>(base + o_dev);
+  v.work = reinterpret_cast<const GppWork*>(base + o_wsch);
+  v.prep = reinterpret_cast<const MixedPrep*>(base + o_prep);
+  v.item_off = reinterpret_cast<const int*>(base + o_schoff);
+  v.tile = reinterpret_cast<const int*>(base + o_tile);
+  v.n_inst = n_instances;
+  v.total = b->sch_off[n_instances];
+  v.counter = b->counters;
+  b->ssx_view = v;
+  b->ssx_view.work = reinterpret_cast<const GppWork*>(base + o_wssx);
+  b->ssx_view.item_off = reinterpret_cast<const int*>(base + o_ssxoff);
+  b->ssx_view.total = b->ssx_off[n_instances];
+  b->ssx_view.counter = b->counters + 1;
+  if (b->sch_grid > v.total) b->sch_grid = std::max(1, v.total);
+  if (b->ssx_grid > b->ssx_view.total) b->ssx_grid = std::max(1, b->ssx_view.total);
+  b->launches = (mixed ? 2 * n_instances : 0) + 1 + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
+  *out = b;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
+  using namespace sigma;
+  if (!b) return SIGMA_ERR_NULL;
+  int dev = 0;
+  SIGMA_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != b->device) return SIGMA_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool mixed = b->precision == SIGMA_PREC_MIXED;
+  SIGMA_CUDA_TRY(cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), s));
+  if (mixed)
+    for (int i = 0; i < b->n; ++i)
+      if (b->sch[i].n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->sch[i], b->prep[i], s));
+  if (b->sch_view.total > 0)
+    SIGMA_CUDA_TRY(mixed ? launch_sch_mixed_batch(b->sch_view, b->sch_grid, s)
+                         : launch_sch_fp64_batch(b->sch_view, b->sch_grid, s));
+  if (b->ssx_view.total > 0)
+    SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed_batch(b->ssx_view, b->ssx_grid, s)
+                         : launch_ssx_fp64_batch(b->ssx_view, b->ssx_grid, s));
+  for (int i = 0; i < b->n; ++i)
+    SIGMA_CUDA_TRY(launch_gpp_reduce(b->sch[i], b->ssx[i], b->dev[i].nb, b->acht_n1[i],
+                                     reinterpret_cast<double2*>(b->inst[i].achtemp),
+                                     reinterpret_cast<double2*>(b->inst[i].asxtemp),
+                                     reinterpret_cast<double2*>(b->inst[i].acht_n1_loc), s));
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_batch_launch_graph(sigma_gpp_batch b, void* stream) {
+  using namespace sigma;
+  if (!b) return SIGMA_ERR_NULL;
+  if (!stream) return SIGMA_ERR_UNSUPPORTED;  // the legacy NULL stream cannot be captured
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!b->exec) {
+    SIGMA_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int st = sigma_gpp_batch_execute(b, stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (st != SIGMA_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ce != cudaSuccess) {
+      set_last_cuda_error(ce, "cudaStreamEndCapture", __LINE__);
+      return SIGMA_ERR_CUDA;
+    }
+    b->graph = g;
+    SIGMA_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  }
+  SIGMA_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_batch_info(sigma_gpp_batch b, long long* terms, int* items, int* launches) {
+  if (!b) return SIGMA_ERR_NULL;
+  if (terms) *terms = b->terms;
+  if (items) *items = b->sch_view.total;
+  if (launches) *launches = b->launches;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_batch_status(sigma_gpp_batch b, void* stream) {
+  if (!b) return SIGMA_ERR_NULL;
+  int st = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  SIGMA_CUDA_TRY(cudaMemcpyAsync(&st, b->counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+  return st;
+}
+
+extern "C" int sigma_gpp_batch_destroy(sigma_gpp_batch b) {
+  if (!b) return SIGMA_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(b->device);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->block) cudaFree(b->block);
+  cudaSetDevice(cur);
+  delete b;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_batched(int n_instances, const sigma_gpp_instance* inst, int precision,
+                                 void* stream) {
+  sigma_gpp_batch b = nullptr;
+  int st = sigma_gpp_batch_create(&b, n_instances, inst, precision, nullptr);
+  if (st != SIGMA_OK) return st;
+  st = sigma_gpp_batch_execute(b, stream);
+  if (st == SIGMA_OK) st = sigma_gpp_batch_status(b, stream);
+  sigma_gpp_batch_destroy(b);
+  return st;
+}

@@ -1,0 +1,45 @@
+// Batched GPP: many instances in one persistent work queue per pass.
+#pragma once
+
+#include "sigma_internal.cuh"
+
+namespace sigma {
+
+// Tile shapes of the FP64 main pass (bands x columns per item).
+enum GppTile { kTile32x32 = 0, kTile16x64 = 1, kTile64x16 = 2, kTileCount = 3 };
+__host__ __device__ constexpr int tile_bn(int t) { return t == kTile16x64 ? 16 : (t == kTile64x16 ? 64 : 32); }
+__host__ __device__ constexpr int tile_bp(int t) { return t == kTile16x64 ? 64 : (t == kTile64x16 ? 16 : 32); }
+
+// One pass over every instance: items of instance i are the global items
+// [item_off[i], item_off[i+1]) of a single device counter.
+struct GppBatchView {
+  const GppDev* dev;
+  const GppWork* work;
+  const MixedPrep* prep;
+  const int* item_off;   // [n_inst + 1]
+  const int* tile;       // [n_inst] GppTile (FP64 main pass)
+  int n_inst;
+  int total;
+  int* counter;
+};
+
+// The instance that owns global item g: the last one whose offset is <= g.
+__device__ __forceinline__ int batch_owner(const int* off, int n, int g) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+cudaError_t launch_sch_fp64_batch(const GppBatchView& b, int grid, cudaStream_t s);
+cudaError_t launch_ssx_fp64_batch(const GppBatchView& b, int grid, cudaStream_t s);
+cudaError_t launch_sch_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s);
+cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s);
+int sch_batch_blocks_per_sm_fp64();
+int ssx_batch_blocks_per_sm_fp64();
+int sch_batch_blocks_per_sm_mixed();
+int ssx_batch_blocks_per_sm_mixed();
+
+}  // namespace sigma

@@ -22,6 +22,7 @@
 // ranges), so the re-check runs in a warp-uniform fix-up after each
 // g-vector step.
 #include "sigma_internal.cuh"
+#include "gpp_batch.cuh"
 
 namespace sigma {
 namespace {
@@ -317,115 +318,145 @@ __device__ __forceinline__ void chunk_terms(const Stage& st, int pl, int ty, con
   }
 }
 
+// One work item of the main pass (TMA ring barriers and their phases persist
+// across the items a CTA takes).
+__device__ __forceinline__ void sch_mixed_item(const GppDev& p, const GppWork& w, const MixedPrep& m,
+                                               int item, SchSmemM& sm, int tid, uint32_t& phase0,
+                                               uint32_t& phase1) {
+  const int tx = tid & 15, ty = tid >> 4;
+  const int band_end = w.band_begin + w.band_count;
+  const bool shared_wx = p.wx_stride == 0;
+  const ItemCoord ic = decode_item(w, item);
+  const int n1_0 = w.band_begin + ic.bb * kBN;
+  const int ig_begin = ic.s * w.split_len;
+  const int ig_end = min(ig_begin + w.split_len, p.nc);
+  const int n_chunks = (ig_end - ig_begin + kCK - 1) / kCK;
+  const int pl = tx;
+  const int my_igp = ic.cb * kBPM + pl;
+
+  float wxh[kTN][kNW], wxl[kTN][kNW];
+  bool exact = true;
+#pragma unroll
+  for (int i = 0; i < kTN; ++i) {
+    const int n1 = n1_0 + ty + 16 * i;
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) {
+      const double wx = n1 < band_end ? p.wx[(size_t)n1 * p.wx_stride + iw] : 0.0;
+      split_f(wx, wxh[i][iw], wxl[i][iw]);
+      exact = exact && wxl[i][iw] == 0.f;
+    }
+  }
+  const bool wx_exact = __syncthreads_and(exact) != 0;  // every frequency exact in FP32
+  float2 acc[kTN][kNW], hi[kTN][kNW], lo[kTN][kNW];
+#pragma unroll
+  for (int i = 0; i < kTN; ++i)
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) {
+      acc[i][iw] = make_float2(0.f, 0.f);
+      hi[i][iw] = make_float2(0.f, 0.f);
+      lo[i][iw] = make_float2(0.f, 0.f);
+    }
+
+  if (tid == 0) issue_chunk(m, ic.cb, ic.bb, ig_begin, sm.st[0], &sm.bar[0]);
+  for (int c = 0; c < n_chunks; ++c) {
+    const int buf = c & 1;
+    const int ig0 = ig_begin + c * kCK;
+    if (tid == 0 && c + 1 < n_chunks)
+      issue_chunk(m, ic.cb, ic.bb, ig0 + kCK, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
+    if (buf == 0) {
+      mbar_wait(&sm.bar[0], phase0, m.status);
+      phase0 ^= 1;
+    } else {
+      mbar_wait(&sm.bar[1], phase1, m.status);
+      phase1 ^= 1;
+    }
+    const Stage& st = sm.st[buf];
+    if (shared_wx) {
+      if (wx_exact)
+        chunk_terms<true, false>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
+      else
+        chunk_terms<true, true>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
+    } else {
+      chunk_terms<false, true>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
+    }
+    __syncthreads();  // every thread is done with this stage before it is refilled
+  }
+
+  // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp] in FP64, then a
+  // fixed-order compensated sum over the tile's columns
+  const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
+#pragma unroll
+  for (int i = 0; i < kTN; ++i) {
+    const int bl = ty + 16 * i;
+    const int n1 = n1_0 + bl;
+    if (n1 < band_end && igp >= 0) {
+      const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+      const double2 mm = make_double2(am.x, -am.y);
+      const double f = 0.5 * p.vcoul[igp];
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        const double2 sv = make_double2((double)hi[i][iw].x + (double)lo[i][iw].x,
+                                        (double)hi[i][iw].y + (double)lo[i][iw].y);
+        const double2 v = cmul(sv, mm);
+        sm.red[iw][pl][bl] = make_double2(v.x * f, v.y * f);
+      }
+    } else {
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) sm.red[iw][pl][bl] = make_double2(0.0, 0.0);
+    }
+  }
+  __syncthreads();
+  if (tid < kBN * kNW) {
+    const int iw = tid / kBN, bl = tid % kBN;
+    Comp sx, sy;
+    for (int q = 0; q < kBPM; ++q) {
+      sx.add(sm.red[iw][q][bl].x);
+      sy.add(sm.red[iw][q][bl].y);
+    }
+    w.partial[ic.pidx * kBN * kNW + bl * kNW + iw] = make_double2(sx.value(), sy.value());
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWork w, MixedPrep m) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SchSmemM& sm = *reinterpret_cast<SchSmemM*>(smem_raw);
   __shared__ int s_item;
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int band_end = w.band_begin + w.band_count;
-  const bool shared_wx = p.wx_stride == 0;
+  const int tid = threadIdx.x;
   if (tid == 0) {
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);
     mbar_fence_init();
   }
   uint32_t phase0 = 0, phase1 = 0;
-
   for (;;) {
     __syncthreads();
     if (tid == 0) s_item = atomicAdd(w.counter, 1);
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    const ItemCoord ic = decode_item(w, item);
-    const int n1_0 = w.band_begin + ic.bb * kBN;
-    const int ig_begin = ic.s * w.split_len;
-    const int ig_end = min(ig_begin + w.split_len, p.nc);
-    const int n_chunks = (ig_end - ig_begin + kCK - 1) / kCK;
-    const int pl = tx;
-    const int my_igp = ic.cb * kBPM + pl;
+    sch_mixed_item(p, w, m, item, sm, tid, phase0, phase1);
+  }
+}
 
-    float wxh[kTN][kNW], wxl[kTN][kNW];
-    bool exact = true;
-#pragma unroll
-    for (int i = 0; i < kTN; ++i) {
-      const int n1 = n1_0 + ty + 16 * i;
-#pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) {
-        const double wx = n1 < band_end ? p.wx[(size_t)n1 * p.wx_stride + iw] : 0.0;
-        split_f(wx, wxh[i][iw], wxl[i][iw]);
-        exact = exact && wxl[i][iw] == 0.f;
-      }
-    }
-    const bool wx_exact = __syncthreads_and(exact) != 0;  // every frequency exact in FP32
-    float2 acc[kTN][kNW], hi[kTN][kNW], lo[kTN][kNW];
-#pragma unroll
-    for (int i = 0; i < kTN; ++i)
-#pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) {
-        acc[i][iw] = make_float2(0.f, 0.f);
-        hi[i][iw] = make_float2(0.f, 0.f);
-        lo[i][iw] = make_float2(0.f, 0.f);
-      }
-
-    if (tid == 0) issue_chunk(m, ic.cb, ic.bb, ig_begin, sm.st[0], &sm.bar[0]);
-    for (int c = 0; c < n_chunks; ++c) {
-      const int buf = c & 1;
-      const int ig0 = ig_begin + c * kCK;
-      if (tid == 0 && c + 1 < n_chunks)
-        issue_chunk(m, ic.cb, ic.bb, ig0 + kCK, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
-      if (buf == 0) {
-        mbar_wait(&sm.bar[0], phase0, m.status);
-        phase0 ^= 1;
-      } else {
-        mbar_wait(&sm.bar[1], phase1, m.status);
-        phase1 ^= 1;
-      }
-      const Stage& st = sm.st[buf];
-      if (shared_wx) {
-        if (wx_exact)
-          chunk_terms<true, false>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
-        else
-          chunk_terms<true, true>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
-      } else {
-        chunk_terms<false, true>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
-      }
-      __syncthreads();  // every thread is done with this stage before it is refilled
-    }
-
-    // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp] in FP64, then a
-    // fixed-order compensated sum over the tile's columns
-    const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
-#pragma unroll
-    for (int i = 0; i < kTN; ++i) {
-      const int bl = ty + 16 * i;
-      const int n1 = n1_0 + bl;
-      if (n1 < band_end && igp >= 0) {
-        const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
-        const double2 mm = make_double2(am.x, -am.y);
-        const double f = 0.5 * p.vcoul[igp];
-#pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) {
-          const double2 sv = make_double2((double)hi[i][iw].x + (double)lo[i][iw].x,
-                                          (double)hi[i][iw].y + (double)lo[i][iw].y);
-          const double2 v = cmul(sv, mm);
-          sm.red[iw][pl][bl] = make_double2(v.x * f, v.y * f);
-        }
-      } else {
-#pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) sm.red[iw][pl][bl] = make_double2(0.0, 0.0);
-      }
-    }
+__global__ void __launch_bounds__(kThreads, 3) sch_mixed_batch_kernel(GppBatchView b) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SchSmemM& sm = *reinterpret_cast<SchSmemM*>(smem_raw);
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_fence_init();
+  }
+  uint32_t phase0 = 0, phase1 = 0;
+  for (;;) {
     __syncthreads();
-    if (tid < kBN * kNW) {
-      const int iw = tid / kBN, bl = tid % kBN;
-      Comp sx, sy;
-      for (int q = 0; q < kBPM; ++q) {
-        sx.add(sm.red[iw][q][bl].x);
-        sy.add(sm.red[iw][q][bl].y);
-      }
-      w.partial[ic.pidx * kBN * kNW + bl * kNW + iw] = make_double2(sx.value(), sy.value());
-    }
+    if (tid == 0) s_item = atomicAdd(b.counter, 1);
+    __syncthreads();
+    const int g = s_item;
+    if (g >= b.total) break;
+    const int inst = batch_owner(b.item_off, b.n_inst, g);
+    sch_mixed_item(b.dev[inst], b.work[inst], b.prep[inst], g - b.item_off[inst], sm, tid, phase0, phase1);
   }
 }
 
@@ -462,7 +493,6 @@ namespace {
 // FP32 form of ssx_fp64_kernel.  The three branch decisions (keep, the
 // |delw|^2 > to1 test, and the exact-pole test |wdiff|^2 > 0) fall back to the
 // FP64 expressions whenever FP32 |wdiff|^2 is near the corresponding threshold.
-constexpr int kSsxBP = 256;
 constexpr int kSsxCK = 8;
 
 struct __align__(16) ColS {
@@ -487,182 +517,206 @@ __device__ __forceinline__ int ssx_branch_exact(const GppDev& p, int my_igp, int
   return 0;
 }
 
-__global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+struct SsxSharedF {
+  double2 red[kSsxBN][kNW][kThreads / 32];
+  float wxh[kSsxBN][kNW], wxl[kSsxBN][kNW], iwx2[kSsxBN][kNW];
+  double wx[kSsxBN][kNW];
+};
+
+__device__ __forceinline__ void ssx_mixed_item(const GppDev& p, const GppWork& w, int item,
+                                               unsigned char* smem_raw, SsxSharedF& sh, int tid) {
   SsxSmemF& sm = *reinterpret_cast<SsxSmemF*>(smem_raw);
-  __shared__ int s_item;
-  __shared__ double2 s_red[kSsxBN][kNW][kThreads / 32];
-  __shared__ float s_wxh[kSsxBN][kNW], s_wxl[kSsxBN][kNW], s_iwx2[kSsxBN][kNW];
-  __shared__ double s_wx[kSsxBN][kNW];
-  const int tid = threadIdx.x;
   const int band_end = w.band_begin + w.band_count;
   const float blo = 1.0f - kGuardBand, bhi = 1.0f + kGuardBand;
+  const ItemCoord ic = decode_item(w, item);
+  const int split = ic.s, cb = ic.cb, bb = ic.bb;
+  const int n1_0 = w.band_begin + bb * kSsxBN;
+  const int nbl = min(kSsxBN, band_end - n1_0);
+  const int p0 = cb * kSsxBP;
+  const int ig_begin = split * w.split_len;
+  const int ig_end = min(ig_begin + w.split_len, p.nc);
+  if (tid < kSsxBN * kNW) {
+    const int i = tid / kNW, iw = tid % kNW;
+    const double wx = i < nbl ? p.wx[(size_t)(n1_0 + i) * p.wx_stride + iw] : 1.0;
+    sh.wx[i][iw] = wx;
+    split_f(wx, sh.wxh[i][iw], sh.wxl[i][iw]);
+    sh.iwx2[i][iw] = __double2float_rn(rcp_f64(wx * wx));
+  }
 
+  float2 acc[kSsxBN][kNW], accl[kSsxBN][kNW];
+#pragma unroll
+  for (int i = 0; i < kSsxBN; ++i)
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) {
+      acc[i][iw] = make_float2(0.f, 0.f);
+      accl[i][iw] = make_float2(0.f, 0.f);
+    }
+  double2 accd[kSsxBN][kNW];
+#pragma unroll
+  for (int i = 0; i < kSsxBN; ++i)
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) accd[i][iw] = make_double2(0.0, 0.0);
+
+  for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kSsxCK) {
+    __syncthreads();
+    for (int e = tid; e < kSsxCK * kSsxBP; e += kThreads) {
+      const int k = e % kSsxCK, pl = e / kSsxCK;
+      const int ig = ig0 + k, my_igp = p0 + pl;
+      ColS c;
+      c.ahi = c.alo = c.b = c.b2 = c.gx = c.gy = c.ox = c.oy = c.pad0 = c.pad1 = 0.f;
+      c.thr = __int_as_float(0x7f800000);
+      c.thr2 = 0.f;
+      if (ig < ig_end && my_igp < p.ng) {
+        const size_t off = (size_t)my_igp * p.nc + ig;
+        const double2 wt = p.wt[off];
+        const double2 ie = p.ieps[off];
+        const double b2 = guard_b2(wt.y);
+        split_f(wt.x, c.ahi, c.alo);
+        c.b = __double2float_rn(wt.y);
+        c.b2 = __double2float_rn(b2);
+        c.thr = __double2float_rn(guard_thr(wt.x, b2));
+        c.thr2 = __double2float_rn(guard_thr2(wt.x, b2));
+        const double2 g = cmul(ie, wt), om = cmul(cmul(wt, wt), ie);
+        c.gx = __double2float_rn(g.x);
+        c.gy = __double2float_rn(g.y);
+        c.ox = __double2float_rn(om.x);
+        c.oy = __double2float_rn(om.y);
+      }
+      sm.col[k][pl] = c;
+    }
+    for (int e = tid; e < kSsxCK * kSsxBN; e += kThreads) {
+      const int k = e % kSsxCK, bl = e / kSsxCK;
+      const int ig = ig0 + k, n1 = n1_0 + bl;
+      float2 v = make_float2(0.f, 0.f);
+      if (ig < ig_end && n1 < band_end) {
+        const double2 d = p.aqsn[(size_t)n1 * p.nc + ig];
+        v = make_float2(__double2float_rn(d.x), __double2float_rn(d.y));
+      }
+      sm.n[k][bl] = v;
+    }
+    __syncthreads();
+
+    for (int k = 0; k < kSsxCK; ++k) {
+      const ColS col = sm.col[k][tid];
+#pragma unroll
+      for (int i = 0; i < kSsxBN; ++i) {
+        if (i < nbl) {
+          const float2 an = sm.n[k][i];
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            const float c = (sh.wxh[i][iw] - col.ahi) + (sh.wxl[i][iw] - col.alo);
+            const float wv = fmaf(c, c, col.b2);
+            int br;
+            const bool near = (wv > col.thr * blo && wv <= col.thr * bhi) ||
+                              (wv >= col.thr2 * blo && wv < col.thr2 * bhi) ||
+                              wv < 1e-30f;
+            if (near) {
+              br = (p0 + tid < p.ng && ig0 + k < ig_end)
+                       ? ssx_branch_exact(p, p0 + tid, ig0 + k, sh.wx[i][iw])
+                       : 0;
+            } else {
+              br = wv > col.thr ? 1 : (wv < col.thr2 ? 2 : 0);
+            }
+            float2 s = make_float2(0.f, 0.f);
+            if (br == 1) {
+              s = make_float2(col.ox * sh.iwx2[i][iw], col.oy * sh.iwx2[i][iw]);
+            } else if (br == 2) {
+              const float zr = (sh.wxh[i][iw] + col.ahi) + (sh.wxl[i][iw] + col.alo);
+              const float q = -0.5f * rcp_f32(fmaf(zr, zr, col.b2));
+              s = make_float2(fmaf(col.gx, zr, col.gy * col.b) * q,
+                              fmaf(col.gy, zr, -col.gx * col.b) * q);
+            }
+            // term in FP32, added to a float-float accumulator (TwoSum)
+            const float tx = fmaf(an.x, s.x, -an.y * s.y);
+            const float ty = fmaf(an.x, s.y, an.y * s.x);
+            float t, e;
+            two_sum_f(acc[i][iw].x, tx, t, e);
+            acc[i][iw].x = t;
+            accl[i][iw].x += e;
+            two_sum_f(acc[i][iw].y, ty, t, e);
+            acc[i][iw].y = t;
+            accl[i][iw].y += e;
+          }
+        }
+      }
+    }
+    // fold the float-float sums into FP64 every 16 chunks
+    const bool last_chunk = ig0 + kSsxCK >= ig_end;
+    if (((ig0 - ig_begin) / kSsxCK) % 16 != 15 && !last_chunk) continue;
+#pragma unroll
+    for (int i = 0; i < kSsxBN; ++i)
+      if (i < nbl) {
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          accd[i][iw].x += (double)acc[i][iw].x + (double)accl[i][iw].x;
+          accd[i][iw].y += (double)acc[i][iw].y + (double)accl[i][iw].y;
+          acc[i][iw] = make_float2(0.f, 0.f);
+          accl[i][iw] = make_float2(0.f, 0.f);
+        }
+      }
+  }
+
+  const int my_igp = p0 + tid;
+  const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int i = 0; i < kSsxBN; ++i)
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) {
+      double2 v = make_double2(0.0, 0.0);
+      if (i < nbl && igp >= 0) {
+        const double2 am = p.aqsm[(size_t)(n1_0 + i) * p.nc + igp];
+        const double f = p.occ * p.vcoul[igp];
+        v = cmul(accd[i][iw], make_double2(am.x, -am.y));
+        v.x *= f;
+        v.y *= f;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) sh.red[i][iw][warp] = v;
+    }
+  __syncthreads();
+  if (tid < kSsxBN * kNW) {
+    const int i = tid / kNW, iw = tid % kNW;
+    Comp sx, sy;
+    for (int q = 0; q < kThreads / 32; ++q) {
+      sx.add(sh.red[i][iw][q].x);
+      sy.add(sh.red[i][iw][q].y);
+    }
+    w.partial[ic.pidx * kSsxBN * kNW + tid] = make_double2(sx.value(), sy.value());
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ SsxSharedF sh;
+  const int tid = threadIdx.x;
   for (;;) {
     __syncthreads();
     if (tid == 0) s_item = atomicAdd(w.counter, 1);
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    const ItemCoord ic = decode_item(w, item);
-    const int split = ic.s, cb = ic.cb, bb = ic.bb;
-    const int n1_0 = w.band_begin + bb * kSsxBN;
-    const int nbl = min(kSsxBN, band_end - n1_0);
-    const int p0 = cb * kSsxBP;
-    const int ig_begin = split * w.split_len;
-    const int ig_end = min(ig_begin + w.split_len, p.nc);
-    if (tid < kSsxBN * kNW) {
-      const int i = tid / kNW, iw = tid % kNW;
-      const double wx = i < nbl ? p.wx[(size_t)(n1_0 + i) * p.wx_stride + iw] : 1.0;
-      s_wx[i][iw] = wx;
-      split_f(wx, s_wxh[i][iw], s_wxl[i][iw]);
-      s_iwx2[i][iw] = __double2float_rn(rcp_f64(wx * wx));
-    }
+    ssx_mixed_item(p, w, item, smem_raw, sh, tid);
+  }
+}
 
-    float2 acc[kSsxBN][kNW], accl[kSsxBN][kNW];
-#pragma unroll
-    for (int i = 0; i < kSsxBN; ++i)
-#pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) {
-        acc[i][iw] = make_float2(0.f, 0.f);
-        accl[i][iw] = make_float2(0.f, 0.f);
-      }
-    double2 accd[kSsxBN][kNW];
-#pragma unroll
-    for (int i = 0; i < kSsxBN; ++i)
-#pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) accd[i][iw] = make_double2(0.0, 0.0);
-
-    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kSsxCK) {
-      __syncthreads();
-      for (int e = tid; e < kSsxCK * kSsxBP; e += kThreads) {
-        const int k = e % kSsxCK, pl = e / kSsxCK;
-        const int ig = ig0 + k, my_igp = p0 + pl;
-        ColS c;
-        c.ahi = c.alo = c.b = c.b2 = c.gx = c.gy = c.ox = c.oy = c.pad0 = c.pad1 = 0.f;
-        c.thr = __int_as_float(0x7f800000);
-        c.thr2 = 0.f;
-        if (ig < ig_end && my_igp < p.ng) {
-          const size_t off = (size_t)my_igp * p.nc + ig;
-          const double2 wt = p.wt[off];
-          const double2 ie = p.ieps[off];
-          const double b2 = guard_b2(wt.y);
-          split_f(wt.x, c.ahi, c.alo);
-          c.b = __double2float_rn(wt.y);
-          c.b2 = __double2float_rn(b2);
-          c.thr = __double2float_rn(guard_thr(wt.x, b2));
-          c.thr2 = __double2float_rn(guard_thr2(wt.x, b2));
-          const double2 g = cmul(ie, wt), om = cmul(cmul(wt, wt), ie);
-          c.gx = __double2float_rn(g.x);
-          c.gy = __double2float_rn(g.y);
-          c.ox = __double2float_rn(om.x);
-          c.oy = __double2float_rn(om.y);
-        }
-        sm.col[k][pl] = c;
-      }
-      for (int e = tid; e < kSsxCK * kSsxBN; e += kThreads) {
-        const int k = e % kSsxCK, bl = e / kSsxCK;
-        const int ig = ig0 + k, n1 = n1_0 + bl;
-        float2 v = make_float2(0.f, 0.f);
-        if (ig < ig_end && n1 < band_end) {
-          const double2 d = p.aqsn[(size_t)n1 * p.nc + ig];
-          v = make_float2(__double2float_rn(d.x), __double2float_rn(d.y));
-        }
-        sm.n[k][bl] = v;
-      }
-      __syncthreads();
-
-      for (int k = 0; k < kSsxCK; ++k) {
-        const ColS col = sm.col[k][tid];
-#pragma unroll
-        for (int i = 0; i < kSsxBN; ++i) {
-          if (i < nbl) {
-            const float2 an = sm.n[k][i];
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) {
-              const float c = (s_wxh[i][iw] - col.ahi) + (s_wxl[i][iw] - col.alo);
-              const float wv = fmaf(c, c, col.b2);
-              int br;
-              const bool near = (wv > col.thr * blo && wv <= col.thr * bhi) ||
-                                (wv >= col.thr2 * blo && wv < col.thr2 * bhi) ||
-                                wv < 1e-30f;
-              if (near) {
-                br = (p0 + tid < p.ng && ig0 + k < ig_end)
-                         ? ssx_branch_exact(p, p0 + tid, ig0 + k, s_wx[i][iw])
-                         : 0;
-              } else {
-                br = wv > col.thr ? 1 : (wv < col.thr2 ? 2 : 0);
-              }
-              float2 s = make_float2(0.f, 0.f);
-              if (br == 1) {
-                s = make_float2(col.ox * s_iwx2[i][iw], col.oy * s_iwx2[i][iw]);
-              } else if (br == 2) {
-                const float zr = (s_wxh[i][iw] + col.ahi) + (s_wxl[i][iw] + col.alo);
-                const float q = -0.5f * rcp_f32(fmaf(zr, zr, col.b2));
-                s = make_float2(fmaf(col.gx, zr, col.gy * col.b) * q,
-                                fmaf(col.gy, zr, -col.gx * col.b) * q);
-              }
-              // term in FP32, added to a float-float accumulator (TwoSum)
-              const float tx = fmaf(an.x, s.x, -an.y * s.y);
-              const float ty = fmaf(an.x, s.y, an.y * s.x);
-              float t, e;
-              two_sum_f(acc[i][iw].x, tx, t, e);
-              acc[i][iw].x = t;
-              accl[i][iw].x += e;
-              two_sum_f(acc[i][iw].y, ty, t, e);
-              acc[i][iw].y = t;
-              accl[i][iw].y += e;
-            }
-          }
-        }
-      }
-      // fold the float-float sums into FP64 every 16 chunks
-      const bool last_chunk = ig0 + kSsxCK >= ig_end;
-      if (((ig0 - ig_begin) / kSsxCK) % 16 != 15 && !last_chunk) continue;
-#pragma unroll
-      for (int i = 0; i < kSsxBN; ++i)
-        if (i < nbl) {
-#pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) {
-            accd[i][iw].x += (double)acc[i][iw].x + (double)accl[i][iw].x;
-            accd[i][iw].y += (double)acc[i][iw].y + (double)accl[i][iw].y;
-            acc[i][iw] = make_float2(0.f, 0.f);
-            accl[i][iw] = make_float2(0.f, 0.f);
-          }
-        }
-    }
-
-    const int my_igp = p0 + tid;
-    const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
-    const int lane = tid & 31, warp = tid >> 5;
-    for (int i = 0; i < kSsxBN; ++i)
-#pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) {
-        double2 v = make_double2(0.0, 0.0);
-        if (i < nbl && igp >= 0) {
-          const double2 am = p.aqsm[(size_t)(n1_0 + i) * p.nc + igp];
-          const double f = p.occ * p.vcoul[igp];
-          v = cmul(accd[i][iw], make_double2(am.x, -am.y));
-          v.x *= f;
-          v.y *= f;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-        }
-        if (lane == 0) s_red[i][iw][warp] = v;
-      }
+__global__ void __launch_bounds__(kThreads) ssx_mixed_batch_kernel(GppBatchView b) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ SsxSharedF sh;
+  const int tid = threadIdx.x;
+  for (;;) {
     __syncthreads();
-    if (tid < kSsxBN * kNW) {
-      const int i = tid / kNW, iw = tid % kNW;
-      Comp sx, sy;
-      for (int q = 0; q < kThreads / 32; ++q) {
-        sx.add(s_red[i][iw][q].x);
-        sy.add(s_red[i][iw][q].y);
-      }
-      w.partial[ic.pidx * kSsxBN * kNW + tid] = make_double2(sx.value(), sy.value());
-    }
+    if (tid == 0) s_item = atomicAdd(b.counter, 1);
+    __syncthreads();
+    const int g = s_item;
+    if (g >= b.total) break;
+    const int inst = batch_owner(b.item_off, b.n_inst, g);
+    ssx_mixed_item(b.dev[inst], b.work[inst], g - b.item_off[inst], smem_raw, sh, tid);
   }
 }
 
@@ -673,6 +727,36 @@ int ssx_blocks_per_sm_mixed() {
   cudaFuncSetAttribute(ssx_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SsxSmemF));
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssx_mixed_kernel, kThreads, sizeof(SsxSmemF));
   return n > 0 ? n : 1;
+}
+
+int sch_batch_blocks_per_sm_mixed() {
+  int n = 0;
+  cudaFuncSetAttribute(sch_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SchSmemM));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sch_mixed_batch_kernel, kThreads, sizeof(SchSmemM));
+  return n > 0 ? n : 1;
+}
+
+int ssx_batch_blocks_per_sm_mixed() {
+  int n = 0;
+  cudaFuncSetAttribute(ssx_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SsxSmemF));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssx_mixed_batch_kernel, kThreads, sizeof(SsxSmemF));
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_sch_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(sch_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       sizeof(SchSmemM));
+  if (e != cudaSuccess) return e;
+  sch_mixed_batch_kernel<<<grid, kThreads, sizeof(SchSmemM), s>>>(b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(ssx_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       sizeof(SsxSmemF));
+  if (e != cudaSuccess) return e;
+  ssx_mixed_batch_kernel<<<grid, kThreads, sizeof(SsxSmemF), s>>>(b);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s) {

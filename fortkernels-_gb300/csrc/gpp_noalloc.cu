@@ -40,6 +40,7 @@ void size_pass(GppWork& w, int band_count, int bn, int bp, int nc, int ng, int g
                int per_slot) {
   w.band_begin = 0;
   w.band_count = band_count;
+  w.bn = bn;
   w.n_band_blocks = (band_count + bn - 1) / bn;
   w.n_col_blocks = (ng + bp - 1) / bp;
   const long long base = (long long)w.n_band_blocks * w.n_col_blocks;

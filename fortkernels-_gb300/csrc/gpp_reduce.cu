@@ -29,7 +29,7 @@ __device__ __forceinline__ double warp_sum_comp(Comp c) {
 
 struct ReduceArgs {
   const double2* sch_partial;
-  int sch_ncb, sch_splits;
+  int sch_ncb, sch_splits, sch_bn;
   const double2* ssx_partial;
   int ssx_ncb, ssx_splits;
   int nb, nvband;
@@ -45,7 +45,7 @@ __global__ void reduce_bands_kernel(ReduceArgs a) {
   const bool is_sch = warp < n_sch;
   const int e = is_sch ? warp : warp - n_sch;
   const int n1 = e / kNW, iw = e % kNW;
-  const int bn = is_sch ? kBN : kSsxBN;
+  const int bn = is_sch ? a.sch_bn : kSsxBN;
   const int ncb = is_sch ? a.sch_ncb : a.ssx_ncb;
   const int ns = is_sch ? a.sch_splits : a.ssx_splits;
   const double2* part = is_sch ? a.sch_partial : a.ssx_partial;
@@ -98,6 +98,7 @@ cudaError_t launch_gpp_reduce(const GppWork& sch, const GppWork& ssx, int nb, do
   a.sch_partial = sch.partial;
   a.sch_ncb = sch.n_col_blocks;
   a.sch_splits = sch.n_splits;
+  a.sch_bn = sch.bn;
   a.ssx_partial = ssx.partial;
   a.ssx_ncb = ssx.n_col_blocks;
   a.ssx_splits = ssx.n_splits;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstddef>
+#include <vector>
 
 #include "sigma_common.h"
 
@@ -53,6 +54,7 @@ struct GppDev {
 // occupied bands): items are (band block, column block, g-vector split).
 struct GppWork {
   int band_begin, band_count;  // bands covered by this pass
+  int bn;                      // bands per item (partial-sum rows per item)
   int n_band_blocks, n_col_blocks, n_splits, split_len;
   int n_items;
   int* counter;                // dynamic item counter (zeroed before launch)
@@ -67,6 +69,7 @@ constexpr int kBPM = 16;   // columns per mixed sch tile
 constexpr int kCK = 32;    // g-vectors per staged chunk
 constexpr int kThreads = 256;
 constexpr int kSsxBN = 4;   // bands per occupied-band item
+constexpr int kSsxBP = 256; // columns per occupied-band item, one per thread
 
 // Item -> (band block, column block, g-vector split).  Band blocks vary
 // fastest so that CTAs running at the same time share column data in L2.
@@ -100,6 +103,17 @@ struct MixedPrep {
   int nc_pad;
   int* status;  // device status word (0, or SIGMA_ERR_TIMEOUT after a bounded wait gave up)
 };
+
+// ---------------------------------------------------------------- host helpers (gpp_api.cu)
+// Sizes a pass: band blocks of bn, column blocks of bp, g-vector splits so
+// that the grid gets about items_per_slot items per resident CTA.
+void gpp_size_work(GppWork& w, int band_begin, int band_count, int bn, int bp, int nc, int ng,
+                   int grid, int items_per_slot);
+// Column map of BGW-Kernels/gppKer.cpp:322-328 (-1 marks a skipped column);
+// SIGMA_ERR_INDEX_RANGE where the reference would read out of bounds.
+int gpp_map_columns(int nc, int ng, const int* inv, const int* indinv, int indinv_len,
+                    std::vector<int>& igp_of, int& valid);
+int gpp_check_shape(int nb, int nvband, int nc, int ng, int nstart, int nend);
 
 // ---------------------------------------------------------------- launchers
 cudaError_t launch_sch_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);

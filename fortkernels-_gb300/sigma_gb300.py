@@ -60,6 +60,13 @@ SIGNATURES = {
     "sigma_gpp_plan_set_timing": ([_P, _I], _I),
     "sigma_gpp_plan_timing": ([_P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_fp64_noalloc": ([_I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_batch_create": ([_P, _I, _P, _I, _P], _I),
+    "sigma_gpp_batch_execute": ([_P, _P], _I),
+    "sigma_gpp_batch_launch_graph": ([_P, _P], _I),
+    "sigma_gpp_batch_info": ([_P, _P, _P, _P], _I),
+    "sigma_gpp_batch_status": ([_P, _P], _I),
+    "sigma_gpp_batch_destroy": ([_P], _I),
+    "sigma_gpp_batched": ([_I, _P, _I, _P], _I),
     "sigma_ff_schdt": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "sigma_ff_plan_create": ([_P, _I, _I, _I, _I, _P, _P, _I], _I),
     "sigma_ff_execute": ([_P, _P, _P, _P, _P, _P], _I),
@@ -195,6 +202,98 @@ class GppPlan:
     def close(self):
         if getattr(self, "handle", None):
             self.lib.sigma_gpp_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GppInstance(C.Structure):
+    """sigma_gpp_instance: one GPP evaluation of a batch (device arrays, host index maps)."""
+    _fields_ = [("number_bands", _I), ("nvband", _I), ("ncouls", _I), ("ngpown", _I),
+                ("inv_igp_index", _P), ("indinv", _P), ("wx_array", _P), ("wx_band_stride", _I),
+                ("occ", _D), ("aqsmtemp", _P), ("aqsntemp", _P), ("I_eps_array", _P),
+                ("wtilde_array", _P), ("vcoul", _P), ("achtemp", _P), ("asxtemp", _P),
+                ("acht_n1_loc", _P)]
+
+
+def _dptr(a):
+    return a if (a is None or isinstance(a, int)) else _ptr(a)
+
+
+def _instance_array(instances, keep):
+    arr = (GppInstance * len(instances))()
+    for k, d in enumerate(instances):
+        inv = np.ascontiguousarray(d["inv_igp_index"], dtype=np.int32)
+        ind = np.ascontiguousarray(d["indinv"], dtype=np.int32)
+        keep += [inv, ind]
+        q = arr[k]
+        q.number_bands, q.nvband, q.ncouls, q.ngpown = (d["number_bands"], d["nvband"],
+                                                         d["ncouls"], d["ngpown"])
+        q.inv_igp_index, q.indinv = _ptr(inv), _ptr(ind)
+        q.wx_array = _dptr(d["wx_array"])
+        q.wx_band_stride = d.get("wx_band_stride", 0)
+        q.occ = d.get("occ", 1.0)
+        for f in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul", "achtemp", "asxtemp"):
+            setattr(q, f, _dptr(d[f]))
+        q.acht_n1_loc = _dptr(d.get("acht_n1_loc"))
+    return arr
+
+
+def gpp_batched(instances, precision=PREC_FP64, stream=0):
+    """One-shot sigma_gpp_batched: evaluates every instance and waits."""
+    lib = load()
+    keep = []
+    arr = _instance_array(instances, keep)
+    _check(lib.sigma_gpp_batched(len(instances), C.addressof(arr), precision, stream), "sigma_gpp_batched")
+
+
+class GppBatch:
+    """Many GPP instances through one work queue per pass
+    (sigma_gpp_batch_create / execute / launch_graph / destroy).
+
+    `instances` is a list of dicts with the sigma_gpp_instance fields: host
+    index maps as numpy int arrays, every other array a CUDA tensor or a
+    device pointer.  `tiles` (optional) gives the FP64 main-pass tile per
+    instance (-1 library choice, 0 = 32x32, 1 = 16x64, 2 = 64x16)."""
+
+    def __init__(self, instances, precision=PREC_FP64, tiles=None):
+        self.lib = load()
+        self._keep = []
+        arr = _instance_array(instances, self._keep)
+        self._arr = arr
+        t = None
+        if tiles is not None:
+            t = np.ascontiguousarray(tiles, dtype=np.int32)
+            self._keep.append(t)
+        h = C.c_void_p()
+        st = self.lib.sigma_gpp_batch_create(C.byref(h), len(instances), C.addressof(arr), precision,
+                                             None if t is None else _ptr(t))
+        _check(st, "sigma_gpp_batch_create")
+        self.handle = h
+
+    def info(self):
+        """(terms, main-pass items, kernels per execution)."""
+        t, i, l = C.c_longlong(), C.c_int(), C.c_int()
+        _check(self.lib.sigma_gpp_batch_info(self.handle, C.byref(t), C.byref(i), C.byref(l)),
+               "sigma_gpp_batch_info")
+        return t.value, i.value, l.value
+
+    def execute(self, stream=0):
+        _check(self.lib.sigma_gpp_batch_execute(self.handle, stream), "sigma_gpp_batch_execute")
+
+    def launch_graph(self, stream):
+        _check(self.lib.sigma_gpp_batch_launch_graph(self.handle, stream), "sigma_gpp_batch_launch_graph")
+
+    def status(self, stream=0):
+        return self.lib.sigma_gpp_batch_status(self.handle, stream)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sigma_gpp_batch_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -113,6 +113,60 @@ int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, double* main_ms,
 int sigma_gpp_plan_info(sigma_gpp_plan plan, int* valid_columns, long long* terms);
 
 /* ---------------------------------------------------------------------------
+ * Batched evaluation: many sigma instances (q-points, band windows) of
+ * different number_bands / ncouls / ngpown / nvband at once.  The reference
+ * evaluates one instance per run of its driver; here every instance's work
+ * items go into one device work queue per pass, drained by one persistent
+ * kernel (main pass, then occupied-band pass), with per-instance pre-passes
+ * and reductions around them.  The whole sequence can be captured once into
+ * a CUDA graph and replayed.
+ * ------------------------------------------------------------------------- */
+typedef struct sigma_gpp_instance {
+  int number_bands, nvband, ncouls, ngpown;
+  const int* inv_igp_index;        /* host [ngpown] */
+  const int* indinv;               /* host [ncouls] */
+  const double* wx_array;          /* device: [3], or [number_bands][wx_band_stride] */
+  int wx_band_stride;
+  double occ;
+  const sigma_complex128* aqsmtemp;      /* device [number_bands][ncouls] */
+  const sigma_complex128* aqsntemp;      /* device [number_bands][ncouls] */
+  const sigma_complex128* I_eps_array;   /* device [ngpown][ncouls] */
+  const sigma_complex128* wtilde_array;  /* device [ngpown][ncouls] */
+  const double* vcoul;                   /* device [ncouls] */
+  sigma_complex128* achtemp;             /* device out [3] */
+  sigma_complex128* asxtemp;             /* device out [3] */
+  sigma_complex128* acht_n1_loc;         /* device out [number_bands], may be NULL */
+} sigma_gpp_instance;
+
+typedef struct sigma_gpp_batch_s* sigma_gpp_batch;
+
+/* Validates every instance like sigma_gpp_plan_create and sizes the queues.
+ * tile_shape (may be NULL) picks the FP64 main-pass tile per instance:
+ * -1 the library's choice (least padding), 0 = 32 bands x 32 columns,
+ * 1 = 16 x 64, 2 = 64 x 16 (the tuning table of fortkernels-_gb300/autotune.py
+ * chooses per shape class).  The mixed form has one tile shape. */
+int sigma_gpp_batch_create(sigma_gpp_batch* batch, int n_instances, const sigma_gpp_instance* inst,
+                           int precision, const int* tile_shape);
+
+/* Launches the batch on `stream` (asynchronous; allocates nothing). */
+int sigma_gpp_batch_execute(sigma_gpp_batch batch, void* stream);
+
+/* First call captures sigma_gpp_batch_execute into a CUDA graph on `stream`
+ * (which must not be the legacy NULL stream); every call launches the graph. */
+int sigma_gpp_batch_launch_graph(sigma_gpp_batch batch, void* stream);
+
+/* Terms of the whole batch, work items of the main pass, kernels per execution. */
+int sigma_gpp_batch_info(sigma_gpp_batch batch, long long* terms, int* items, int* launches);
+
+/* Waits for `stream`; SIGMA_OK or SIGMA_ERR_TIMEOUT from a bounded device wait. */
+int sigma_gpp_batch_status(sigma_gpp_batch batch, void* stream);
+
+int sigma_gpp_batch_destroy(sigma_gpp_batch batch);
+
+/* One-shot form: create, execute, wait, destroy. */
+int sigma_gpp_batched(int n_instances, const sigma_gpp_instance* inst, int precision, void* stream);
+
+/* ---------------------------------------------------------------------------
  * FP64 evaluation that allocates nothing.  This entry point has no
  * counterpart in the reference; it exists for callers that cannot allocate
  * GPU memory: code inside a framework whose memory pool owns the device, a

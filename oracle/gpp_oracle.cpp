@@ -428,6 +428,69 @@ int oracle_gpp_columns(int number_bands, int nvband, int ncouls, int ngpown,
   return kOk;
 }
 
+// Sum of squared term magnitudes of every output: ach_abs2[iw] = sum over
+// the terms that enter achtemp[iw] of |scha * 0.5 * vcoul[igp]|^2, and
+// asx_abs2[iw] likewise for asxtemp[iw] (|ssxa * occ * vcoul[igp]|^2).  A
+// method whose per-term relative error is e (independent, rms) misses the
+// exact sum by about e * sqrt(abs2); sqrt(abs2) / |sum| is the output's
+// cancellation factor.  Same terms and guard as oracle_gpp; only bands
+// [band_begin, band_end) are summed (a band sample, for large instances).
+int oracle_gpp_abs2(int number_bands, int nvband, int ncouls, int ngpown,
+                    const int* inv_igp_index, const int* indinv, int indinv_len,
+                    const double* wx_array, int wx_band_stride, double occ,
+                    const double* aqsmtemp, const double* aqsntemp, const double* I_eps_array,
+                    const double* wtilde_array, const double* vcoul, double* ach_abs2,
+                    double* asx_abs2, int band_begin, int band_end, int nthreads) {
+  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0 || nvband < 0) return kErrShape;
+  if (band_begin < 0 || band_end > number_bands || band_begin > band_end) return kErrShape;
+  std::vector<int> igp_of(ngpown);
+  for (int my_igp = 0; my_igp < ngpown; ++my_igp) {
+    int g = map_igp(inv_igp_index, indinv, indinv_len, ncouls, my_igp);
+    if (g == -2) return kErrIndex;
+    igp_of[my_igp] = g;
+  }
+  const cd* aqsm = reinterpret_cast<const cd*>(aqsmtemp);
+  const cd* aqsn = reinterpret_cast<const cd*>(aqsntemp);
+  const cd* ieps = reinterpret_cast<const cd*>(I_eps_array);
+  const cd* wtil = reinterpret_cast<const cd*>(wtilde_array);
+  const size_t nc = static_cast<size_t>(ncouls);
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  std::vector<double> per(static_cast<size_t>(ngpown) * 6, 0.0);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+  for (int my_igp = 0; my_igp < ngpown; ++my_igp) {
+    const int igp = igp_of[my_igp];
+    if (igp < 0) continue;
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    const double v = vcoul[igp];
+    for (int n1 = band_begin; n1 < band_end; ++n1) {
+      const cd mygpvar1 = std::conj(aqsm[n1 * nc + igp]);
+      const double* wx = wx_array + static_cast<size_t>(wx_band_stride) * n1;
+      for (int iw = 0; iw < 3; ++iw)
+        for (size_t ig = 0; ig < nc; ++ig) {
+          const cd wt = wtil[my_igp * nc + ig], ie = ieps[my_igp * nc + ig], an = aqsn[n1 * nc + ig];
+          if (n1 < nvband) {
+            cd ssxa, scha;
+            term_occ(wx[iw], wt, mygpvar1, an, ie, ssxa, scha);
+            s[iw] += std::norm(scha * (0.5 * v));
+            s[3 + iw] += std::norm(ssxa * (occ * v));
+          } else {
+            bool keep;
+            cd scha = term_unocc(wx[iw], wt, mygpvar1, an, ie, keep);
+            if (keep) s[iw] += std::norm(scha * (0.5 * v));
+          }
+        }
+    }
+    for (int k = 0; k < 6; ++k) per[static_cast<size_t>(my_igp) * 6 + k] = s[k];
+  }
+  for (int k = 0; k < 3; ++k) ach_abs2[k] = asx_abs2[k] = 0.0;
+  for (int my_igp = 0; my_igp < ngpown; ++my_igp)
+    for (int k = 0; k < 3; ++k) {
+      ach_abs2[k] += per[static_cast<size_t>(my_igp) * 6 + k];
+      asx_abs2[k] += per[static_cast<size_t>(my_igp) * 6 + 3 + k];
+    }
+  return kOk;
+}
+
 // FF schDt contraction for a list of (n1, ifreq) entries:
 //   schDt[n1][ifreq] = sum_my_igp (sum_ig I_epsR[ifreq][my_igp][ig] * aqsn[n1][ig])
 //                      * conj(aqsm[n1][igp(my_igp)])

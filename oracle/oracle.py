@@ -34,6 +34,8 @@ def lib():
         l.oracle_gpp_columns.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P,
                                          _I, _I, _I]
         l.oracle_ff_schdt.argtypes = [_I, _I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _I]
+        l.oracle_gpp_abs2.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P,
+                                      _I, _I, _I]
         _lib = l
     return _lib
 
@@ -99,6 +101,23 @@ def gpp_columns(prob, band_begin=0, band_end=None, nthreads=0, wx_band_stride=0)
     if st != 0:
         raise OracleError(f"oracle_gpp_columns status {st}")
     return sch, ssx
+
+
+def gpp_abs2(prob, band_begin=0, band_end=None, nthreads=0, wx_band_stride=0):
+    """Sum of squared term magnitudes per output over bands [band_begin,
+    band_end): (ach_abs2[3], asx_abs2[3])."""
+    if band_end is None:
+        band_end = prob.number_bands
+    inv, indinv, wx, aqsm, aqsn, ieps, wt, vcoul = _prep(prob)
+    a = np.zeros(3)
+    x = np.zeros(3)
+    st = lib().oracle_gpp_abs2(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, _p(inv),
+                               _p(indinv), len(indinv), _p(wx), wx_band_stride, prob.occ, _p(aqsm),
+                               _p(aqsn), _p(ieps), _p(wt), _p(vcoul), _p(a), _p(x), band_begin,
+                               band_end, nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_gpp_abs2 status {st}")
+    return a, x
 
 
 def ff_schdt(prob, entries=None, nthreads=0):

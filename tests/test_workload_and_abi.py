@@ -143,3 +143,53 @@ def test_ff_validation_precedes_device_work(libpath):
     if st == 0:
         lib.sigma_ff_plan_destroy.argtypes = [C.c_void_p]
         lib.sigma_ff_plan_destroy(h)
+
+
+def test_batch_validation_precedes_device_work(libpath):
+    """sigma_gpp_batch_create checks every instance on the host first."""
+    import sigma_gb300 as S
+    lib = C.CDLL(str(libpath))
+    f = lib.sigma_gpp_batch_create
+    f.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+    nc, ng = 64, 4
+    inv, indinv = W.gpp_index_maps(nc, ng)
+    fake = 256  # device pointers are not touched before the device step
+    good = dict(number_bands=2, nvband=1, ncouls=nc, ngpown=ng, inv_igp_index=inv, indinv=indinv,
+                wx_array=fake, aqsmtemp=fake, aqsntemp=fake, I_eps_array=fake, wtilde_array=fake,
+                vcoul=fake, achtemp=fake, asxtemp=fake)
+    h = C.c_void_p()
+
+    def create(insts, prec=0, tiles=None):
+        keep = []
+        arr = S._instance_array(insts, keep)
+        t = None if tiles is None else np.asarray(tiles, np.int32)
+        return f(C.byref(h), len(insts), C.addressof(arr), prec, None if t is None else t.ctypes.data)
+
+    assert create([]) == -1
+    assert create([good, dict(good, ngpown=65, inv_igp_index=np.arange(65, dtype=np.int32))]) == -1
+    assert create([good, dict(good, inv_igp_index=np.array([16, 32, 65, 64], np.int32))]) == -2
+    assert create([good, dict(good, aqsntemp=None)]) == -6
+    assert create([good], prec=2) == -8
+    assert create([good, good], tiles=[0, 5]) == -8
+    assert create([dict(good, wx_band_stride=2)]) == -1
+    st = create([good, good], tiles=[1, -1])
+    assert st in (0, -7, -4)
+    if st == 0:
+        lib.sigma_gpp_batch_destroy.argtypes = [C.c_void_p]
+        lib.sigma_gpp_batch_destroy(h)
+
+
+def test_tile_table_covers_every_shape_class():
+    import autotune as A
+    t = A.load_table()
+    assert t is not None and t["device"].startswith("NVIDIA")
+    keys = {A.shape_class(nb, ng) for nb in range(1, 200) for ng in range(1, 200)}
+    assert keys == set(t["classes"]) and len(keys) == 16
+    assert all(v in (0, 1, 2) for v in t["classes"].values())
+    # the tuned tile of a class is the fastest one it timed
+    for k, v in t["classes"].items():
+        ms = t["timings"][k]["ms"]
+        assert A.TILES[v] == min(ms, key=ms.get)
+    assert A.shape_class(16, 16) == "b0c0" and A.shape_class(17, 64) == "b1c3"
+    for s in W.batched_shapes():
+        assert A.tile_for(s["number_bands"], s["ngpown"]) in (0, 1, 2)
