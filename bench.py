@@ -317,6 +317,38 @@ def run_ff(S, W, torch, dist, world, stream, sptr, args):
     return res
 
 
+def run_static(S, W, torch, dist, world, stream, sptr, inst):
+    """Static remainder (sigma_gpp_static_execute) on the production
+    instance's device arrays: both contraction forms, FP64-equivalent TF/s
+    (8 flop per complex multiply-add of the bands x columns x g-vectors
+    GEMM) and the tensor form's error against the FP64 form."""
+    flops = 8.0 * NB * NG * NC
+    res = {"workload": f"GPP static remainder: {NB} bands x {NG} columns x {NC} g-vectors",
+           "unit": "TFLOP/s (FP64-equivalent)"}
+    outs = {}
+    for mode, name, steps in ((1, "ozaki_bf16", 10), (0, "fp64", 2)):
+        plan = S.StaticPlan(NB, NC, NG, inst.inv, inst.indinv, mode)
+        tot = torch.zeros(2, dtype=torch.float64, device="cuda")
+        n1 = torch.zeros(2 * NB, dtype=torch.float64, device="cuda")
+        run = lambda: plan.execute(inst.aqsm, inst.aqsn, inst.ieps, inst.vcoul, tot, n1, sptr)
+        run()
+        plan.set_timing(True)
+        ms = timed(torch, dist, world, run, steps, stream)
+        t = plan.timing()
+        res[name] = {"value": round(flops * world / (ms / steps * 1e-3) / 1e12, 3),
+                     "ms_per_step": round(ms / steps, 3),
+                     "kernel_ms_per_launch": round(t["main_ms"] / max(1, t["executions"]), 3),
+                     "status": plan.status(sptr)}
+        outs[name] = (tot.cpu().numpy().view(np.complex128)[0], n1.cpu().numpy().view(np.complex128).copy())
+        plan.close()
+    a, b = outs["fp64"], outs["ozaki_bf16"]
+    res["ozaki_bf16"]["rel_err_vs_fp64"] = {"achstemp": float(abs(b[0] - a[0]) / abs(a[0])),
+                                            "per_band_normwise": float(np.linalg.norm(b[1] - a[1]) /
+                                                                       np.linalg.norm(a[1]))}
+    res["speedup_ozaki_vs_fp64"] = round(res["ozaki_bf16"]["value"] / res["fp64"]["value"], 1)
+    return res
+
+
 def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     """48 uneven GPP instances (workload.batched_shapes) through the batched
     API, one CUDA-graph replay per step, FP64 (tiles from the tuning table)
@@ -325,10 +357,11 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     import autotune
     import batched
 
-    xs = batched.device_instances()
+    shapes = W.batched_shapes()[: args.batch_instances]
+    xs = batched.device_instances(shapes)
     dicts = [x.as_dict() for x in xs]
     tiles = [autotune.tile_for(x.nb, x.ng) for x in xs]
-    res = {"workload": "48 GPP instances, number_bands U{64..512}, ncouls U{4096..32768}/256, "
+    res = {"workload": f"{len(xs)} GPP instances, number_bands U{{64..512}}, ncouls U{{4096..32768}}/256, "
                        "nodes_per_group U{10..40}, nvband U{1..8}, seeds 1000+i",
            "instances": len(xs), "input_bytes": int(sum(x.input_bytes for x in xs)),
            "tiles": {"table": autotune.load_table() is not None,
@@ -338,7 +371,7 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     gs = torch.cuda.Stream()  # graphs are captured on a non-default stream
     gptr = gs.cuda_stream
     torch.cuda.synchronize()
-    for prec, name, steps in ((S.PREC_FP64, "fp64", 2), (S.PREC_MIXED, "mixed", 5)):
+    for prec, name, steps in ((S.PREC_FP64, "fp64", args.batch_fp64_steps), (S.PREC_MIXED, "mixed", 5)):
         b = S.GppBatch(dicts, precision=prec, tiles=tiles if prec == S.PREC_FP64 else None)
         terms, items, launches = b.info()
         b.launch_graph(gptr)  # capture, and the warm-up replay
@@ -379,6 +412,11 @@ def run_ours(args, rank, world, local_rank):
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
 
+    if args.only_batched:
+        res = run_batched(S, W, torch, dist, world, stream, sptr, args, float("nan"))
+        if rank == 0:
+            print(json.dumps({"batched": res}), flush=True)
+        return 0
     fp64_peak, fp32_peak = S.measure_fma_peaks(sptr)
     inst = Instance(S, W, torch, seed=1 + rank)
     plan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_FP64)
@@ -450,6 +488,7 @@ def run_ours(args, rank, world, local_rank):
                  "acht_n1_loc_normwise": float(np.linalg.norm(mixed_out[2] - fp64_out[2]) /
                                                np.linalg.norm(fp64_out[2]))}
     mixed_main_s = mkt["main_ms"] / max(1, mkt["executions"]) * 1e-3
+    static = None if args.no_static else run_static(S, W, torch, dist, world, stream, sptr, inst)
     cpu_prob = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # host copy of the instance for the CPU baseline: trailing bands + all columns
@@ -523,6 +562,7 @@ def run_ours(args, rank, world, local_rank):
                                "peak_source": "FP32 pipe 128 FFMA/clk/SM at the sampled SM clock"}},
         "ff": ff,
         "batched": batch,
+        "static_remainder": static,
         "peaks_measured": {"fp64_fma_probe_tflops": round(fp64_peak, 4),
                            "fp32_fma_probe_tflops": round(fp32_peak, 3),
                            "fp64_pipe_tflops_at_clock": round(fp64_pipe_peak, 4),
@@ -549,6 +589,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ff", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-static", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=48,
+                    help="leading instances of the 48-instance batched set (fewer only for profiling)")
+    ap.add_argument("--batch-fp64-steps", type=int, default=2)
+    ap.add_argument("--only-batched", action="store_true",
+                    help="run the batched measurement alone (profiling captures)")
     ap.add_argument("--bands", type=int, default=NB,
                     help="number_bands of the instance (512 = the production shape; smaller only "
                          "for profiling captures)")

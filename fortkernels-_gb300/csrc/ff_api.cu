@@ -5,6 +5,7 @@
 #include "sigma_ff.h"
 #include "ff_internal.cuh"
 #include "ff_ozaki.cuh"
+#include "ff_plan.h"
 #include "runtime.h"
 
 struct sigma_ff_plan_s {
@@ -47,18 +48,13 @@ int ff_check_shape(int nb, int nc, int ng, int nf) {
 }  // namespace
 }  // namespace sigma
 
-extern "C" int sigma_ff_plan_create(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown,
-                                    int nfreq, const int* inv_igp_index, const int* indinv,
-                                    int mode) {
-  using namespace sigma;
-  if (!out || !inv_igp_index || !indinv) return SIGMA_ERR_NULL;
+namespace sigma {
+
+// Plan over an already validated column map (igp_of[my_igp], -1 = column
+// left out).  Shared by the FF contraction and the static remainders.
+int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
+                  const std::vector<int>& igp_of, int mode) {
   *out = nullptr;
-  int st = ff_check_shape(number_bands, ncouls, ngpown, nfreq);
-  if (st != SIGMA_OK) return st;
-  if (mode != SIGMA_FF_FP64 && mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
-  std::vector<int> igp_of;
-  st = ff_map_columns(ncouls, ngpown, inv_igp_index, indinv, igp_of);
-  if (st != SIGMA_OK) return st;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
@@ -139,6 +135,23 @@ extern "C" int sigma_ff_plan_create(sigma_ff_plan* out, int number_bands, int nc
   return SIGMA_OK;
 }
 
+}  // namespace sigma
+
+extern "C" int sigma_ff_plan_create(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown,
+                                    int nfreq, const int* inv_igp_index, const int* indinv,
+                                    int mode) {
+  using namespace sigma;
+  if (!out || !inv_igp_index || !indinv) return SIGMA_ERR_NULL;
+  *out = nullptr;
+  int st = ff_check_shape(number_bands, ncouls, ngpown, nfreq);
+  if (st != SIGMA_OK) return st;
+  if (mode != SIGMA_FF_FP64 && mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
+  std::vector<int> igp_of;
+  st = ff_map_columns(ncouls, ngpown, inv_igp_index, indinv, igp_of);
+  if (st != SIGMA_OK) return st;
+  return ff_plan_build(out, number_bands, ncouls, ngpown, nfreq, igp_of, mode);
+}
+
 extern "C" int sigma_ff_plan_destroy(sigma_ff_plan plan) {
   if (!plan) return SIGMA_OK;
   int cur = 0;
@@ -184,6 +197,12 @@ extern "C" int sigma_ff_plan_timing(sigma_ff_plan plan, int* executions, double*
   return SIGMA_OK;
 }
 
+extern "C" int sigma_ff_plan_bands(sigma_ff_plan plan, int* number_bands) {
+  if (!plan || !number_bands) return SIGMA_ERR_NULL;
+  *number_bands = plan->nb;
+  return SIGMA_OK;
+}
+
 extern "C" int sigma_ff_plan_status(sigma_ff_plan plan, void* stream) {
   if (!plan) return SIGMA_ERR_NULL;
   int st = 0;
@@ -193,10 +212,12 @@ extern "C" int sigma_ff_plan_status(sigma_ff_plan plan, void* stream) {
   return st;
 }
 
-extern "C" int sigma_ff_execute(sigma_ff_plan plan, const sigma_complex128* I_epsR,
-                                const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
-                                sigma_complex128* schDt_matrix, void* stream) {
-  using namespace sigma;
+namespace sigma {
+
+int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
+                        const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
+                        const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
+                        void* stream) {
   if (!plan) return SIGMA_ERR_NULL;
   if (!I_epsR || !aqsntemp || !aqsmtemp || !schDt_matrix) return SIGMA_ERR_NULL;
   int dev = 0;
@@ -207,6 +228,8 @@ extern "C" int sigma_ff_execute(sigma_ff_plan plan, const sigma_complex128* I_ep
   d.epsr = reinterpret_cast<const double2*>(I_epsR);
   d.aqsn = reinterpret_cast<const double2*>(aqsntemp);
   d.aqsm = reinterpret_cast<const double2*>(aqsmtemp);
+  d.vcoul = vcoul;
+  d.vfac = vfac;
   cudaEvent_t* ev = nullptr;
   if (plan->timing && plan->recorded < kFfMaxTimed) ev = &plan->events[3 * plan->recorded++];
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->work.counter, 0, 2 * sizeof(int), s));
@@ -224,6 +247,15 @@ extern "C" int sigma_ff_execute(sigma_ff_plan plan, const sigma_complex128* I_ep
   }
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[2], s));
   return SIGMA_OK;
+}
+
+}  // namespace sigma
+
+extern "C" int sigma_ff_execute(sigma_ff_plan plan, const sigma_complex128* I_epsR,
+                                const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
+                                sigma_complex128* schDt_matrix, void* stream) {
+  return sigma::ff_execute_weighted(plan, I_epsR, aqsntemp, aqsmtemp, nullptr, 1.0, schDt_matrix,
+                                    stream);
 }
 
 extern "C" int sigma_ff_schdt(int number_bands, int ncouls, int ngpown, int nfreq,

@@ -96,11 +96,15 @@ __global__ void __launch_bounds__(kFfThreads, 2) ff_fp64_kernel(FfDev p, FfWork 
       const int g = g0 + tr + 16 * i;
       if (g >= p.ng) continue;
       const int igp = p.igp_of[g];
+      if (igp < 0) continue;
+      const double wgt = ff_column_weight(p, igp);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int n = n0 + tc + 16 * j;
         if (n >= p.nb) continue;
-        const double2 m = p.aqsm[(size_t)n * p.nc + igp];  // conj(m) applied below
+        double2 m = p.aqsm[(size_t)n * p.nc + igp];  // conj(m) applied below
+        m.x *= wgt;
+        m.y *= wgt;
         part[j].x += acc[i][j].x * m.x + acc[i][j].y * m.y;
         part[j].y += acc[i][j].y * m.x - acc[i][j].x * m.y;
       }

@@ -17,8 +17,19 @@ struct FfDev {
   const double2* epsr;     // [nf][ng][nc]
   const double2* aqsn;     // [nb][nc]
   const double2* aqsm;     // [nb][nc]
-  const int* igp_of;       // [ng]
+  const int* igp_of;       // [ng]; -1 marks a column left out of the sum
+  // Optional column weight: the epilogue multiplies tempz by
+  // vfac * vcoul[igp] * conj(aqsm[n1][igp]) when vcoul is set (static
+  // remainders), by conj(aqsm[n1][igp]) alone otherwise (schDt).
+  const double* vcoul;
+  double vfac;
 };
+
+// Column weight of the contraction epilogue (0 for a column left out).
+__device__ __forceinline__ double ff_column_weight(const FfDev& p, int igp) {
+  if (igp < 0) return 0.0;
+  return p.vcoul ? p.vfac * p.vcoul[igp] : 1.0;
+}
 
 struct FfWork {
   int n_row_blocks;        // nf * ngp / kFfRows

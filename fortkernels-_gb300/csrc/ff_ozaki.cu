@@ -325,16 +325,19 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
       const int g = row_ok ? R % p.ng : 0;
       const int f_first = (it.rb * kOzRows) / p.ng;
       const int f_last = (min(it.rb * kOzRows + kOzRows, rows) - 1) / p.ng;
-      const int igp = row_ok ? p.igp_of[g] : 0;
-      // acc[n] <- Re, acc[64 + n] <- Im of tempz * conj(aqsm[n1][igp])
+      const int igp_raw = row_ok ? p.igp_of[g] : -1;
+      const bool col_ok = igp_raw >= 0;
+      const int igp = col_ok ? igp_raw : 0;
+      const double wgt = ff_column_weight(p, igp_raw);
+      // acc[n] <- Re, acc[64 + n] <- Im of tempz * weight * conj(aqsm[n1][igp])
 #pragma unroll
       for (int n = 0; n < 64; ++n) {
         const int nn = it.cb * kOzCols + n;
         float mr = 0.f, mi = 0.f;
-        if (row_ok && nn < p.nb) {
+        if (col_ok && nn < p.nb) {
           const double2 md = p.aqsm[(size_t)nn * p.nc + igp];
-          mr = __double2float_rn(md.x);
-          mi = __double2float_rn(md.y);
+          mr = __double2float_rn(md.x * wgt);
+          mi = __double2float_rn(md.y * wgt);
         }
         const float cr = acc[n], ci = acc[64 + n];
         acc[n] = fmaf(cr, mr, ci * mi);

@@ -1,0 +1,22 @@
+// Internal entry points of the FF plan shared with the static remainders.
+#pragma once
+
+#include <vector>
+
+#include "sigma_ff.h"
+
+namespace sigma {
+
+// Plan over an already validated column map (igp_of[my_igp] in [0, ncouls),
+// or -1 for a column left out of every sum).
+int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
+                  const std::vector<int>& igp_of, int mode);
+
+// sigma_ff_execute with the column weight vfac * vcoul[igp] (vcoul a device
+// array, or nullptr for weight 1).
+int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
+                        const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
+                        const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
+                        void* stream);
+
+}  // namespace sigma

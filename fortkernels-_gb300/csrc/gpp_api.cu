@@ -160,7 +160,9 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   const size_t b_colA = align_up(sizeof(float4) * col_elems, 256);
   const size_t b_colB = align_up(sizeof(float2) * col_elems, 256);
   const size_t b_band = align_up(sizeof(float2) * band_elems, 256);
-  cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx + b_colA + b_colB + b_band);
+  const size_t b_colC = nvband > 0 ? b_colB : 0;
+  cudaError_t e =
+      cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx + b_colA + b_colB + b_band + b_colC);
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_last_cuda_error(e, "cudaMalloc(plan)", __LINE__);
@@ -180,6 +182,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
     p->prep.colA = mixed ? reinterpret_cast<float4*>(q) : nullptr;
     p->prep.colB = mixed ? reinterpret_cast<float2*>(q + b_colA) : nullptr;
     p->prep.band = mixed ? reinterpret_cast<float2*>(q + b_colA + b_colB) : nullptr;
+    p->prep.colC = mixed && nvband > 0 ? reinterpret_cast<float2*>(q + b_colA + b_colB + b_band) : nullptr;
     p->prep.nc_pad = nc_pad;
     p->prep.status = p->counters + 2;
   }
@@ -310,7 +313,7 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
                          : launch_sch_fp64(p, plan->sch, plan->sch_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
   if (plan->ssx.n_items > 0)
-    SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed(p, plan->ssx, plan->ssx_grid, s)
+    SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed(p, plan->ssx, plan->prep, plan->ssx_grid, s)
                          : launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[2], s));
   SIGMA_CUDA_TRY(launch_gpp_reduce(plan->sch, plan->ssx, plan->nb, plan->acht_n1,

@@ -30,6 +30,7 @@ struct sigma_gpp_batch_s {
   std::vector<sigma_gpp_instance> inst;
   long long terms = 0;
   int sch_grid = 0, ssx_grid = 0, launches = 0;
+  bool all_shared_wx = true;  // every instance has one frequency set for all bands
   void* block = nullptr;
   sigma::GppBatchView sch_view{}, ssx_view{};
   int* counters = nullptr;  // [0] main pass, [1] occupied-band pass, [2] status
@@ -115,6 +116,7 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   b->precision = precision;
   b->terms = terms;
   b->inst.assign(inst, inst + n_instances);
+  for (int i = 0; i < n_instances; ++i) b->all_shared_wx = b->all_shared_wx && inst[i].wx_band_stride == 0;
   b->sch_grid = sms * (mixed ? sch_batch_blocks_per_sm_mixed() : sch_batch_blocks_per_sm_fp64());
   b->ssx_grid = sms * (mixed ? ssx_batch_blocks_per_sm_mixed() : ssx_batch_blocks_per_sm_fp64());
   b->dev.resize(n_instances);
@@ -135,7 +137,7 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
 
   // device layout: per-instance buffers, then the descriptor arrays
   std::vector<size_t> o_igp(n_instances), o_n1(n_instances), o_sch(n_instances), o_ssx(n_instances),
-      o_a(n_instances), o_b(n_instances), o_band(n_instances);
+      o_a(n_instances), o_b(n_instances), o_band(n_instances), o_c(n_instances);
   size_t total = 256;  // counters
   for (int i = 0; i < n_instances; ++i) {
     const sigma_gpp_instance& q = inst[i];
@@ -166,6 +168,8 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
       total += up256(sizeof(float2) * col);
       o_band[i] = total;
       total += up256(sizeof(float2) * band);
+      o_c[i] = total;
+      if (q.nvband > 0) total += up256(sizeof(float2) * col);
     }
   }
   const size_t o_dev = total;
@@ -218,6 +222,7 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
     m.status = b->counters + 2;
     m.colA = mixed ? reinterpret_cast<float4*>(base + o_a[i]) : nullptr;
     m.colB = mixed ? reinterpret_cast<float2*>(base + o_b[i]) : nullptr;
+    m.colC = mixed && q.nvband > 0 ? reinterpret_cast<float2*>(base + o_c[i]) : nullptr;
     m.band = mixed ? reinterpret_cast<float2*>(base + o_band[i]) : nullptr;
   }
   int rc = SIGMA_OK;
@@ -279,7 +284,7 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
     SIGMA_CUDA_TRY(mixed ? launch_sch_mixed_batch(b->sch_view, b->sch_grid, s)
                          : launch_sch_fp64_batch(b->sch_view, b->sch_grid, s));
   if (b->ssx_view.total > 0)
-    SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed_batch(b->ssx_view, b->ssx_grid, s)
+    SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed_batch(b->ssx_view, b->ssx_grid, b->all_shared_wx, s)
                          : launch_ssx_fp64_batch(b->ssx_view, b->ssx_grid, s));
   for (int i = 0; i < b->n; ++i)
     SIGMA_CUDA_TRY(launch_gpp_reduce(b->sch[i], b->ssx[i], b->dev[i].nb, b->acht_n1[i],

@@ -36,7 +36,7 @@ __device__ __forceinline__ int batch_owner(const int* off, int n, int g) {
 cudaError_t launch_sch_fp64_batch(const GppBatchView& b, int grid, cudaStream_t s);
 cudaError_t launch_ssx_fp64_batch(const GppBatchView& b, int grid, cudaStream_t s);
 cudaError_t launch_sch_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s);
-cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s);
+cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, bool all_shared_wx, cudaStream_t s);
 int sch_batch_blocks_per_sm_fp64();
 int ssx_batch_blocks_per_sm_fp64();
 int sch_batch_blocks_per_sm_mixed();

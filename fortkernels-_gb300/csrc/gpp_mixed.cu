@@ -129,6 +129,7 @@ __device__ __forceinline__ bool keep_exact(const GppDev& p, int my_igp, int ig, 
 __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, int n_col_blocks) {
   __shared__ float4 ta[32][kBPM + 1];
   __shared__ float2 tb[32][kBPM + 1];
+  __shared__ float2 tc[32][kBPM + 1];
   const int tid = threadIdx.x;
   const bool shared_wx = p.wx_stride == 0;
   float wxh[kNW], wxl[kNW];
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
       const int pl = e / 32, k = e % 32;  // reads run along g-vectors
       const int my_igp = cb * kBPM + pl, ig = ig0 + k;
       float4 a = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7f800000));
-      float2 g = make_float2(0.f, 0.f);
+      float2 g = make_float2(0.f, 0.f), om = make_float2(0.f, 0.f);
       if (shared_wx) a.w = __uint_as_float(0u);  // padding: no term kept
       if (my_igp < p.ng && ig < p.nc) {
         const size_t off = (size_t)my_igp * p.nc + ig;
@@ -155,8 +156,13 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
         const double thr = guard_thr(wt.x, b2);
         if (shared_wx) {
           // keep/drop of the three frequencies, decided once per (column,
-          // g-vector): FP32 when clear of the threshold, FP64 otherwise
+          // g-vector): FP32 when clear of the threshold, FP64 otherwise.
+          // With occupied bands, bits 3..5 also hold the second branch of
+          // their ssx term (dropped, and |wdiff|^2 below |wtilde|^2 / to1),
+          // decided the same way.
           const float t32 = __double2float_rn(thr);
+          const double thr2 = p.nvband > 0 ? guard_thr2(wt.x, b2) : 0.0;
+          const float t2_32 = __double2float_rn(thr2);
           const float bb = a.z * a.z;
           unsigned mask = 0u;
 #pragma unroll
@@ -171,6 +177,18 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
             else
               keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2), thr);
             mask |= keep ? (1u << iw) : 0u;
+            if (p.nvband > 0 && !keep) {
+              bool second;
+              if (wv > 1e-30f && wv < t2_32 * (1.0f - kGuardBand))
+                second = true;
+              else if (wv >= t2_32 * (1.0f + kGuardBand))
+                second = false;
+              else {
+                const double w64 = guard_w(p.wx[iw], wt.x, b2);
+                second = gt_nonneg(w64, 0.0) && gt_nonneg(thr2, w64);
+              }
+              mask |= second ? (8u << iw) : 0u;
+            }
           }
           a.w = __uint_as_float(mask);
         } else {
@@ -178,9 +196,14 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
         }
         const double2 gg = cmul(ie, wt);
         g = make_float2(__double2float_rn(gg.x), __double2float_rn(gg.y));
+        if (m.colC) {
+          const double2 o2 = cmul(wt, gg);  // Omega2 = wtilde^2 I_eps
+          om = make_float2(__double2float_rn(o2.x), __double2float_rn(o2.y));
+        }
       }
       ta[k][pl] = a;
       tb[k][pl] = g;
+      tc[k][pl] = om;
     }
     __syncthreads();
     for (int e = tid; e < 32 * kBPM; e += 256) {
@@ -188,6 +211,7 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
       const size_t o = ((size_t)cb * m.nc_pad + ig0 + k) * kBPM + pl;
       m.colA[o] = ta[k][pl];
       m.colB[o] = tb[k][pl];
+      if (m.colC) m.colC[o] = tc[k][pl];
     }
   }
 }
@@ -689,6 +713,165 @@ __device__ __forceinline__ void ssx_mixed_item(const GppDev& p, const GppWork& w
   }
 }
 
+// Occupied-band pass when every band shares one frequency set: the main
+// pass's pre-pass already holds what each (column, g-vector) needs in FP32
+// (Re wtilde as hi/lo, Im wtilde, G = I_eps wtilde, Omega2 = wtilde^2 I_eps
+// and the exact branch of every frequency in the mask bits), so this pass
+// reads those instead of staging and converting the FP64 inputs.  The
+// branch values are
+//   kept:           ssx = Omega2 / wx^2
+//   second branch:  ssx = -G / (2 (wtilde + wx))
+// (see ssx_fp64_item), computed once per (column, g-vector) and shared by
+// the item's bands.  Thread = column; each term goes into a float-float
+// (TwoSum) accumulator, which leaves the thread in FP64.
+struct SsxMaskShared {
+  double2 red[kSsxBN][kNW][kThreads / 32];
+};
+
+__device__ __forceinline__ void ssx_masked_item(const GppDev& p, const GppWork& w, const MixedPrep& m,
+                                                int item, SsxMaskShared& sh, int tid) {
+  const int band_end = w.band_begin + w.band_count;
+  const ItemCoord ic = decode_item(w, item);
+  const int n1_0 = w.band_begin + ic.bb * kSsxBN;
+  const int nbl = min(kSsxBN, band_end - n1_0);
+  const int my_igp = ic.cb * kSsxBP + tid;
+  const int ig_begin = ic.s * w.split_len;
+  const int ig_end = min(ig_begin + w.split_len, p.nc);
+  const int n_prep_cols = (p.ng + kBPM - 1) / kBPM * kBPM;  // columns the pre-pass laid out
+  const bool col_in = my_igp < n_prep_cols;
+
+  float wxh[kNW], wxl[kNW], iwx2[kNW];
+#pragma unroll
+  for (int iw = 0; iw < kNW; ++iw) {
+    split_f(p.wx[iw], wxh[iw], wxl[iw]);
+    iwx2[iw] = __double2float_rn(rcp_f64(p.wx[iw] * p.wx[iw]));
+  }
+  float2 acc[kSsxBN][kNW], accl[kSsxBN][kNW];
+#pragma unroll
+  for (int i = 0; i < kSsxBN; ++i)
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) {
+      acc[i][iw] = make_float2(0.f, 0.f);
+      accl[i][iw] = make_float2(0.f, 0.f);
+    }
+
+  if (col_in) {
+    const size_t cbase = (size_t)(my_igp / kBPM) * m.nc_pad * kBPM + (my_igp % kBPM);
+    const float4* ca = m.colA + cbase;
+    const float2* cg = m.colB + cbase;
+    const float2* co = m.colC + cbase;
+    const float2* bands[kSsxBN];
+#pragma unroll
+    for (int i = 0; i < kSsxBN; ++i) {
+      const int n1 = min(n1_0 + i, band_end - 1);
+      bands[i] = m.band + ((size_t)(n1 / kBN) * m.nc_pad) * kBN + (n1 % kBN);
+    }
+#pragma unroll 4
+    for (int ig = ig_begin; ig < ig_end; ++ig) {
+      {
+        const float4 a = ca[(size_t)ig * kBPM];
+        const unsigned mask = __float_as_uint(a.w);
+        if ((mask & 0x3Fu) == 0u) continue;
+        const float2 g = cg[(size_t)ig * kBPM];
+        const float2 om = co[(size_t)ig * kBPM];
+        const float b = a.z;
+        const float omx = om.x, omy = om.y;
+        float2 sv[kNW];
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          const float zr = (wxh[iw] + a.x) + (wxl[iw] + a.y);
+          const float q = -0.5f * rcp_f32(fmaf(zr, zr, b * b));
+          const float2 s2 = make_float2(fmaf(g.x, zr, g.y * b) * q, fmaf(g.y, zr, -g.x * b) * q);
+          const float2 s1 = make_float2(omx * iwx2[iw], omy * iwx2[iw]);
+          sv[iw] = (mask & (1u << iw)) ? s1 : ((mask & (8u << iw)) ? s2 : make_float2(0.f, 0.f));
+        }
+#pragma unroll
+        for (int i = 0; i < kSsxBN; ++i) {
+          if (i < nbl) {
+            const float2 an = bands[i][(size_t)ig * kBN];
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const float tx = fmaf(an.x, sv[iw].x, -an.y * sv[iw].y);
+              const float ty = fmaf(an.x, sv[iw].y, an.y * sv[iw].x);
+              float t, e;
+              two_sum_f(acc[i][iw].x, tx, t, e);
+              acc[i][iw].x = t;
+              accl[i][iw].x += e;
+              two_sum_f(acc[i][iw].y, ty, t, e);
+              acc[i][iw].y = t;
+              accl[i][iw].y += e;
+            }
+          }
+        }
+      }
+    }
+  }
+
+  const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
+  const int lane = tid & 31, warp = tid >> 5;
+  __syncthreads();  // the previous item's epilogue is done with sh.red
+#pragma unroll
+  for (int i = 0; i < kSsxBN; ++i)
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) {
+      double2 v = make_double2(0.0, 0.0);
+      if (i < nbl && igp >= 0) {
+        const double2 am = p.aqsm[(size_t)(n1_0 + i) * p.nc + igp];
+        const double f = p.occ * p.vcoul[igp];
+        const double2 sum = make_double2((double)acc[i][iw].x + (double)accl[i][iw].x,
+                                         (double)acc[i][iw].y + (double)accl[i][iw].y);
+        v = cmul(sum, make_double2(am.x, -am.y));
+        v.x *= f;
+        v.y *= f;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) sh.red[i][iw][warp] = v;
+    }
+  __syncthreads();
+  if (tid < kSsxBN * kNW) {
+    const int i = tid / kNW, iw = tid % kNW;
+    Comp sx, sy;
+    for (int q = 0; q < kThreads / 32; ++q) {
+      sx.add(sh.red[i][iw][q].x);
+      sy.add(sh.red[i][iw][q].y);
+    }
+    w.partial[ic.pidx * kSsxBN * kNW + tid] = make_double2(sx.value(), sy.value());
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 2) ssx_masked_kernel(GppDev p, GppWork w, MixedPrep m) {
+  __shared__ int s_item;
+  __shared__ SsxMaskShared sh;
+  const int tid = threadIdx.x;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(w.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= w.n_items) break;
+    ssx_masked_item(p, w, m, item, sh, tid);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 2) ssx_masked_batch_kernel(GppBatchView b) {
+  __shared__ int s_item;
+  __shared__ SsxMaskShared sh;
+  const int tid = threadIdx.x;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(b.counter, 1);
+    __syncthreads();
+    const int g = s_item;
+    if (g >= b.total) break;
+    const int inst = batch_owner(b.item_off, b.n_inst, g);
+    ssx_masked_item(b.dev[inst], b.work[inst], b.prep[inst], g - b.item_off[inst], sh, tid);
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) ssx_mixed_kernel(GppDev p, GppWork w) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ int s_item;
@@ -722,10 +905,11 @@ __global__ void __launch_bounds__(kThreads) ssx_mixed_batch_kernel(GppBatchView 
 
 }  // namespace
 
+// Grid of the occupied-band pass: sized for the masked kernel (the common
+// case); the staged fallback takes the same items with fewer CTAs resident.
 int ssx_blocks_per_sm_mixed() {
   int n = 0;
-  cudaFuncSetAttribute(ssx_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SsxSmemF));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssx_mixed_kernel, kThreads, sizeof(SsxSmemF));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssx_masked_kernel, kThreads, 0);
   return n > 0 ? n : 1;
 }
 
@@ -738,8 +922,7 @@ int sch_batch_blocks_per_sm_mixed() {
 
 int ssx_batch_blocks_per_sm_mixed() {
   int n = 0;
-  cudaFuncSetAttribute(ssx_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SsxSmemF));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssx_mixed_batch_kernel, kThreads, sizeof(SsxSmemF));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ssx_masked_batch_kernel, kThreads, 0);
   return n > 0 ? n : 1;
 }
 
@@ -751,7 +934,11 @@ cudaError_t launch_sch_mixed_batch(const GppBatchView& b, int grid, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s) {
+cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, bool all_shared_wx, cudaStream_t s) {
+  if (all_shared_wx) {
+    ssx_masked_batch_kernel<<<grid, kThreads, 0, s>>>(b);
+    return cudaGetLastError();
+  }
   cudaError_t e = cudaFuncSetAttribute(ssx_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        sizeof(SsxSmemF));
   if (e != cudaSuccess) return e;
@@ -759,7 +946,12 @@ cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s) {
+cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
+                             cudaStream_t s) {
+  if (p.wx_stride == 0) {
+    ssx_masked_kernel<<<grid, kThreads, 0, s>>>(p, w, m);
+    return cudaGetLastError();
+  }
   cudaError_t e = cudaFuncSetAttribute(ssx_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        sizeof(SsxSmemF));
   if (e != cudaSuccess) return e;

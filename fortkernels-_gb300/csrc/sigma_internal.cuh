@@ -93,12 +93,14 @@ __device__ __forceinline__ ItemCoord decode_item(const GppWork& w, int item) {
 // tile-interleaved layouts so that one staged chunk is one contiguous block:
 //   colA[cb][ig][pl] = (Re wtilde hi, Re wtilde lo, Im wtilde, pole-guard threshold)
 //   colB[cb][ig][pl] = I_eps * wtilde
+//   colC[cb][ig][pl] = Omega2 = wtilde^2 * I_eps (only with occupied bands)
 //   band[bb][ig][bl] = aqsn
 // with my_igp = cb*kBPM + pl, n1 = bb*kBN + bl, ig < nc_pad (padding: zero
 // operands and an infinite threshold, so padded terms are dropped).
 struct MixedPrep {
   float4* colA;
   float2* colB;
+  float2* colC;
   float2* band;
   int nc_pad;
   int* status;  // device status word (0, or SIGMA_ERR_TIMEOUT after a bounded wait gave up)
@@ -121,7 +123,9 @@ cudaError_t launch_ssx_fp64(const GppDev& p, const GppWork& w, int grid, cudaStr
 cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
                              cudaStream_t s);
 cudaError_t launch_prep_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, cudaStream_t s);
-cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+// The pre-pass (launch_prep_mixed) must have run for the same execution.
+cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
+                             cudaStream_t s);
 int sch_blocks_per_sm(int precision);
 int ssx_blocks_per_sm(int precision);
 

@@ -67,6 +67,11 @@ SIGNATURES = {
     "sigma_gpp_batch_status": ([_P, _P], _I),
     "sigma_gpp_batch_destroy": ([_P], _I),
     "sigma_gpp_batched": ([_I, _P, _I, _P], _I),
+    "sigma_gpp_achstemp": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
+    "sigma_gpp_static_plan_create": ([_P, _I, _I, _I, _P, _P, _I], _I),
+    "sigma_gpp_static_execute": ([_P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_ff_plan_bands": ([_P, _P], _I),
+    "sigma_ff_sigma": ([_I] * 6 + [_P] * 11 + [_D] * 4 + [_P] * 7 + [_I, _P], _I),
     "sigma_ff_schdt": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "sigma_ff_plan_create": ([_P, _I, _I, _I, _I, _P, _P, _I], _I),
     "sigma_ff_execute": ([_P, _P, _P, _P, _P, _P], _I),
@@ -301,6 +306,93 @@ class GppBatch:
             self.close()
         except Exception:
             pass
+
+
+def gpp_achstemp(prob, mode: int = FF_MODE_FP64, stream: int = 0):
+    """Static remainder of the GPP sum (sigma_gpp_achstemp) on a
+    workload.GppProblem: returns (achstemp, achstemp_n1[number_bands])."""
+    lib = load()
+    inv = np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, dtype=np.int32)
+    arrs = [_c128(prob.aqsmtemp), _c128(prob.aqsntemp), _c128(prob.I_eps_array)]
+    vcoul = np.ascontiguousarray(prob.vcoul, dtype=np.float64)
+    out = np.zeros(1, np.complex128)
+    n1 = np.zeros(prob.number_bands, np.complex128)
+    st = lib.sigma_gpp_achstemp(prob.number_bands, prob.ncouls, prob.ngpown, _ptr(inv), _ptr(indinv),
+                                *[_ptr(a) for a in arrs], _ptr(vcoul), _ptr(out), _ptr(n1), mode, stream)
+    _check(st, "sigma_gpp_achstemp")
+    return out[0], n1
+
+
+class StaticPlan:
+    """Device-resident static remainder (sigma_gpp_static_plan_create /
+    sigma_gpp_static_execute; an FF plan underneath)."""
+
+    def __init__(self, number_bands, ncouls, ngpown, inv_igp_index, indinv, mode=FF_MODE_FP64):
+        self.lib = load()
+        self.inv = np.ascontiguousarray(inv_igp_index, dtype=np.int32)
+        self.indinv = np.ascontiguousarray(indinv, dtype=np.int32)
+        h = C.c_void_p()
+        _check(self.lib.sigma_gpp_static_plan_create(C.byref(h), number_bands, ncouls, ngpown,
+                                                     _ptr(self.inv), _ptr(self.indinv), mode),
+               "sigma_gpp_static_plan_create")
+        self.handle = h
+
+    def execute(self, aqsm, aqsn, ieps, vcoul, achstemp, achstemp_n1, stream=0):
+        _check(self.lib.sigma_gpp_static_execute(self.handle, *[_dptr(a) for a in (aqsm, aqsn, ieps, vcoul,
+                                                                                 achstemp, achstemp_n1)],
+                                                 stream), "sigma_gpp_static_execute")
+
+    def set_timing(self, enable=True):
+        _check(self.lib.sigma_ff_plan_set_timing(self.handle, int(enable)), "sigma_ff_plan_set_timing")
+
+    def timing(self):
+        n, a, o, l = C.c_int(), C.c_double(), C.c_double(), C.c_int()
+        _check(self.lib.sigma_ff_plan_timing(self.handle, C.byref(n), C.byref(a), C.byref(o), C.byref(l)),
+               "sigma_ff_plan_timing")
+        return dict(executions=n.value, main_ms=a.value, other_ms=o.value, launches=l.value)
+
+    def status(self, stream=0):
+        return self.lib.sigma_ff_plan_status(self.handle, stream)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sigma_ff_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+FF_SIGMA_OUTPUTS = ("achsDtemp", "asxDtemp", "achDtemp", "achDtemp_cor", "achDtemp_corb", "ach2Dtemp")
+
+
+def ff_sigma(prob, mode: int = FF_MODE_FP64, schdt="zero", stream: int = 0):
+    """Full-frequency sigma (sigma_ff_sigma) on a workload.FFSigmaProblem.
+    schdt: "zero" (the live Fortran's zeroed schDt_matrix), "compute" (the
+    library contracts I_epsR itself), or a complex [number_bands][nfreq]
+    array.  Returns a dict of the six outputs."""
+    lib = load()
+    p = prob
+    c = lambda a: np.ascontiguousarray(a, dtype=np.complex128)
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    if isinstance(schdt, str):
+        sd = np.zeros((p.number_bands, p.nfreq), np.complex128) if schdt == "zero" else None
+    else:
+        sd = c(schdt)
+    args = [i32(p.inv_igp_index), i32(p.indinv), c(p.aqsmtemp), c(p.aqsntemp), c(p.I_epsR), c(p.I_epsA),
+            f(p.vcoul), f(p.ekq), f(p.dFreqGrid), c(p.dFreqBrd), f(p.pref)]
+    out = {k: np.zeros(1 if k == "achsDtemp" else p.nfreqeval, np.complex128) for k in FF_SIGMA_OUTPUTS}
+    st = lib.sigma_ff_sigma(p.number_bands, p.nvband, p.ncouls, p.ngpown, p.nfreq, p.nfreqeval,
+                            *[_ptr(a) for a in args], p.pref_zb, p.freqevalmin, p.freqevalstep, p.occ,
+                            _ptr(sd), *[_ptr(out[k]) for k in FF_SIGMA_OUTPUTS], mode, stream)
+    _check(st, "sigma_ff_sigma")
+    out["achsDtemp"] = out["achsDtemp"][0]
+    return out
 
 
 def ff_host(prob, mode: int = FF_MODE_FP64, stream: int = 0):

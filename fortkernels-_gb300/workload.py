@@ -246,3 +246,77 @@ def ff_random(number_bands, ncouls, ngpown, nfreq, seed) -> FFProblem:
     aqsn = fill_complex(seed, AID_AQSN, nb * nc, (-1, 1), (-1, 1)).reshape(nb, nc)
     r = fill_complex(seed, AID_IEPSR, nfreq * ngpown * nc, (-1, 1), (-1, 1)).reshape(nfreq, ngpown, nc)
     return FFProblem(nb, nc, ngpown, nfreq, inv, indinv, r, aqsn, aqsm)
+
+
+# ---------------------------------------------------------------- FF sigma
+@dataclasses.dataclass
+class FFSigmaProblem:
+    """Inputs of the full-frequency sigma band loop (ffkernel.deslippe.best.f90
+    :201-626) in the C layouts of FFKer_cori/ffKernel.cpp."""
+    number_bands: int
+    nvband: int
+    ncouls: int
+    ngpown: int
+    nfreq: int
+    nfreqeval: int
+    inv_igp_index: np.ndarray
+    indinv: np.ndarray
+    aqsmtemp: np.ndarray    # complex128 [NB][NC]
+    aqsntemp: np.ndarray    # complex128 [NB][NC]
+    I_epsR: np.ndarray      # complex128 [nfreq][NG][NC]
+    I_epsA: np.ndarray      # complex128 [nfreq][NG][NC]
+    vcoul: np.ndarray       # float64 [NC]
+    ekq: np.ndarray         # float64 [NB]
+    dFreqGrid: np.ndarray   # float64 [nfreq]
+    dFreqBrd: np.ndarray    # complex128 [nfreq]
+    pref: np.ndarray        # float64 [nfreq]
+    pref_zb: float = 0.5 / 3.14
+    freqevalmin: float = 0.0
+    freqevalstep: float = 0.5
+    occ: float = 1.0
+
+    def ff_problem(self) -> "FFProblem":
+        """The schDt contraction of the same inputs (I_epsR)."""
+        return FFProblem(self.number_bands, self.ncouls, self.ngpown, self.nfreq, self.inv_igp_index,
+                         self.indinv, self.I_epsR, self.aqsntemp, self.aqsmtemp)
+
+
+def ff_sigma_grid(number_bands, nfreq):
+    """The mini-app's energies and frequency grid (ffkernel.deslippe.best.f90
+    :103-150): ekq[n1] = -10 + n1, dFreqGrid[f] = 2 f, pref[f] = (grid[f+1] -
+    grid[f]) / 3.14 with both ends halved, dFreqBrd = 0.1 i."""
+    ekq = -10.0 + np.arange(number_bands, dtype=np.float64)
+    grid = 2.0 * np.arange(nfreq, dtype=np.float64)
+    pref = np.empty(nfreq)
+    pref[:-1] = (grid[1:] - grid[:-1]) / 3.14
+    pref[-1] = pref[-2]
+    pref[0] *= 0.5
+    pref[-1] *= 0.5
+    brd = np.full(nfreq, 0.1j)
+    return ekq, grid, brd, pref
+
+
+def ff_sigma_constant(number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval) -> FFSigmaProblem:
+    """The mini-app's own fill: aqsm = aqsn = I_epsR = 0.5+0.5i, I_epsA =
+    0.5-0.5i, vcoul = 1, identity index maps."""
+    inv, indinv = ff_index_maps(ncouls, ngpown)
+    ekq, grid, brd, pref = ff_sigma_grid(number_bands, nfreq)
+    a = np.full((number_bands, ncouls), 0.5 + 0.5j)
+    r = np.full((nfreq, ngpown, ncouls), 0.5 + 0.5j)
+    return FFSigmaProblem(number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval, inv, indinv, a,
+                          a.copy(), r, np.conj(r), np.ones(ncouls), ekq, grid, brd, pref)
+
+
+def ff_sigma_random(number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval, seed) -> FFSigmaProblem:
+    """Seeded inputs: aqsm, aqsn, I_epsR, I_epsA ~ U(-1,1) per part, vcoul ~
+    U(0.1,10); energies and grid as the mini-app sets them."""
+    inv, indinv = ff_index_maps(ncouls, ngpown)
+    nb, nc = number_bands, ncouls
+    ekq, grid, brd, pref = ff_sigma_grid(nb, nfreq)
+    aqsm = fill_complex(seed, AID_AQSM, nb * nc, (-1, 1), (-1, 1)).reshape(nb, nc)
+    aqsn = fill_complex(seed, AID_AQSN, nb * nc, (-1, 1), (-1, 1)).reshape(nb, nc)
+    r = fill_complex(seed, AID_IEPSR, nfreq * ngpown * nc, (-1, 1), (-1, 1)).reshape(nfreq, ngpown, nc)
+    a = fill_complex(seed, AID_IEPSA, nfreq * ngpown * nc, (-1, 1), (-1, 1)).reshape(nfreq, ngpown, nc)
+    vcoul = fill_real(seed, AID_VCOUL, nc, 0.1, 10.0)
+    return FFSigmaProblem(nb, nvband, nc, ngpown, nfreq, nfreqeval, inv, indinv, aqsm, aqsn, r, a, vcoul,
+                          ekq, grid, brd, pref)

@@ -64,9 +64,48 @@ int sigma_ff_plan_set_timing(sigma_ff_plan plan, int enable);
 int sigma_ff_plan_timing(sigma_ff_plan plan, int* executions, double* main_ms, double* other_ms,
                          int* launches_per_execution);
 
+/* number_bands the plan was made for. */
+int sigma_ff_plan_bands(sigma_ff_plan plan, int* number_bands);
+
 /* Waits for `stream`; SIGMA_OK or SIGMA_ERR_TIMEOUT when a bounded device
  * wait of the last execution gave up. */
 int sigma_ff_plan_status(sigma_ff_plan plan, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Full-frequency sigma: the band loop of ffkernel.deslippe.best.f90
+ * (:201-626) around the contraction, in the C layouts above plus
+ *   I_epsA [nfreq][ngpown][ncouls], vcoul [ncouls], ekq [number_bands],
+ *   dFreqGrid [nfreq] (ascending), dFreqBrd [nfreq] (complex), pref [nfreq].
+ * Outputs (host, overwritten): achsDtemp [1] (static CH, :240-253),
+ * asxDtemp (SX of the occupied bands, :279-389), achDtemp (sigma1),
+ * achDtemp_corb (sigma3), ach2Dtemp (sigma2 + delta terms) and achDtemp_cor
+ * (sigma4 + delta terms), each [nfreqeval] (:459-613), with
+ * wx = freqevalmin - ekq[n1] + iw * freqevalstep, band n1 occupied when
+ * n1 < nvband.  These replace achsDtemp_Kernel, asxDtemp_Kernel,
+ * achDtemp_Kernel and achDtemp_cor_Kernel (FFKer_cori/ffKernel.cpp:107-245)
+ * with the Fortran's semantics where the C++ port departs from them
+ * (frequency index of the static term, the (iw-1) * freqevalstep of wx,
+ * I_epsA for wx < 0 in SX, the separate achDtemp array, the interval
+ * search at grid points and outside the grid).
+ * schDt_matrix [number_bands][nfreq]: used as given (achDtemp_Kernel's
+ * input); NULL computes it from I_epsR with the contraction of this header
+ * (the Fortran zeroes it: its contraction is commented out).
+ * Columns whose igp = indinv[inv_igp_index[my_igp]] falls outside
+ * [0, ncouls) are left out, as the Fortran cycles them.  mode picks the
+ * contraction form (SIGMA_FF_FP64 or SIGMA_FF_OZAKI_BF16) of the three
+ * g-vector contractions; the rest runs in FP64.  Returns after `stream`
+ * drains.
+ * ------------------------------------------------------------------------- */
+int sigma_ff_sigma(int number_bands, int nvband, int ncouls, int ngpown, int nfreq, int nfreqeval,
+                   const int* inv_igp_index, const int* indinv, const sigma_complex128* aqsmtemp,
+                   const sigma_complex128* aqsntemp, const sigma_complex128* I_epsR,
+                   const sigma_complex128* I_epsA, const double* vcoul, const double* ekq,
+                   const double* dFreqGrid, const sigma_complex128* dFreqBrd, const double* pref,
+                   double pref_zb, double freqevalmin, double freqevalstep, double occ,
+                   const sigma_complex128* schDt_matrix, sigma_complex128* achsDtemp,
+                   sigma_complex128* asxDtemp, sigma_complex128* achDtemp,
+                   sigma_complex128* achDtemp_cor, sigma_complex128* achDtemp_corb,
+                   sigma_complex128* ach2Dtemp, int mode, void* stream);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,7 @@
 #define SIGMA_GPP_H
 
 #include "sigma_common.h"
+#include "sigma_ff.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -200,6 +201,45 @@ int sigma_gpp_fp64_noalloc(int number_bands, int nvband, int ncouls, int ngpown,
                            const sigma_complex128* wtilde_array, const double* vcoul,
                            sigma_complex128* achtemp, sigma_complex128* asxtemp,
                            sigma_complex128* acht_n1_loc, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Static remainder of the GPP sum (the exact static COH term):
+ *
+ *   achstemp_n1[n1] = sum_{my_igp} -0.5 vcoul[igp] conj(aqsm[n1][igp])
+ *                       * sum_{ig} aqsn[n1][ig] I_eps[my_igp][ig]
+ *   achstemp = sum_{n1} achstemp_n1[n1]
+ *
+ * Replaces reduce_achstemp (BGW-Kernels/gppKer.cpp:67-128), called there
+ * once per band inside the band loop (:308).  The formula is the Fortran
+ * kernel's (gppkernel.deslippe.09.30.2014.f90:195-228); the C++ function
+ * reads the single element I_eps[my_igp][igp] instead of the g-vector sum,
+ * never resets schstemp between columns, and discards its result.  Index map
+ * and skipped columns as sigma_gpp_fp64 (BGW-Kernels/gppKer.cpp:322-328).
+ * The sums are one complex GEMM (bands x columns x g-vectors) with the
+ * conj(aqsm) vcoul reduction fused, run in either form of the FF
+ * contraction: mode SIGMA_FF_FP64 or SIGMA_FF_OZAKI_BF16 (sigma_ff.h).
+ *
+ * Host pointers: aqsmtemp / aqsntemp [number_bands][ncouls], I_eps_array
+ * [ngpown][ncouls], vcoul [ncouls]; achstemp [1] and achstemp_n1
+ * [number_bands] (may be NULL) are written.  Returns after `stream` drains.
+ * ------------------------------------------------------------------------- */
+int sigma_gpp_achstemp(int number_bands, int ncouls, int ngpown, const int* inv_igp_index,
+                       const int* indinv, const sigma_complex128* aqsmtemp,
+                       const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                       const double* vcoul, sigma_complex128* achstemp,
+                       sigma_complex128* achstemp_n1, int mode, void* stream);
+
+/* Device-resident form: a plan of the contraction (an FF plan with one
+ * frequency and the GPP column map; destroy it with sigma_ff_plan_destroy,
+ * time it with sigma_ff_plan_set_timing / sigma_ff_plan_timing) and an
+ * asynchronous execution on device arrays.  achstemp [1] and achstemp_n1
+ * [number_bands] are device outputs (both required). */
+int sigma_gpp_static_plan_create(sigma_ff_plan* plan, int number_bands, int ncouls, int ngpown,
+                                 const int* inv_igp_index, const int* indinv, int mode);
+int sigma_gpp_static_execute(sigma_ff_plan plan, const sigma_complex128* aqsmtemp,
+                             const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                             const double* vcoul, sigma_complex128* achstemp,
+                             sigma_complex128* achstemp_n1, void* stream);
 
 #ifdef __cplusplus
 }

@@ -3,6 +3,8 @@
   oracle/_build/liboracle.so  <- oracle/gpp_oracle.cpp (the C++ restatement)
   oracle/_ref/gppKer          <- BGW-Kernels/gppKer.cpp of the reference, unmodified
   oracle/_ref/libgppref.so    <- the same file (main renamed by -D) + oracle/ref_harness.cpp
+  oracle/_ref/ffKernel        <- FFKer_cori/ffKernel.cpp of the reference, unmodified
+  oracle/_ref/libffref.so     <- the same file (main renamed by -D) + oracle/ff_ref_harness.cpp
 
 The two oracle/_ref products are built only where the reference checkout is
 present (REFERENCE_ROOT, default /root/reference); they are compiled from the
@@ -23,6 +25,10 @@ REF_BIN = REF_OUT / "gppKer"
 REF_LIB = REF_OUT / "libgppref.so"
 REFERENCE_ROOT = pathlib.Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
 REF_SRC = REFERENCE_ROOT / "BGW-Kernels" / "gppKer.cpp"
+FF_REF_DIR = REFERENCE_ROOT / "FFKer_cori"
+FF_REF_SRC = FF_REF_DIR / "ffKernel.cpp"
+FF_REF_BIN = REF_OUT / "ffKernel"
+FF_REF_LIB = REF_OUT / "libffref.so"
 
 ORACLE_FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 # the timing build of the same file: the reference's own optimisation flags
@@ -74,6 +80,14 @@ def build_reference() -> bool:
     if not _newer(REF_LIB, REF_SRC, harness):
         _run(["g++", *REF_FLAGS, "-fPIC", "-shared", "-Dmain=gppker_reference_main",
               str(REF_SRC), str(harness), "-o", str(REF_LIB)])
+    if FF_REF_SRC.exists():
+        inc = ["-I", str(FF_REF_DIR)]
+        if not _newer(FF_REF_BIN, FF_REF_SRC):
+            _run(["g++", *REF_FLAGS, *inc, str(FF_REF_SRC), "-o", str(FF_REF_BIN)])
+        ffh = HERE / "ff_ref_harness.cpp"
+        if not _newer(FF_REF_LIB, FF_REF_SRC, ffh):
+            _run(["g++", *REF_FLAGS, *inc, "-fPIC", "-shared", "-Dmain=ffker_reference_main",
+                  str(FF_REF_SRC), str(ffh), "-o", str(FF_REF_LIB)])
     return True
 
 

@@ -491,6 +491,59 @@ int oracle_gpp_abs2(int number_bands, int nvband, int ncouls, int ngpown,
   return kOk;
 }
 
+// Static remainder of the GPP sum, Fortran formula
+// (gppkernel.deslippe.09.30.2014.f90:195-228; the C++ reduce_achstemp,
+// BGW-Kernels/gppKer.cpp:67-128, is not a usable statement of it):
+//   schstemp = sum_ig -aqsn[n1][ig] * I_eps[my_igp][ig] * conj(aqsm[n1][igp])
+//   achstemp += schstemp * vcoul[igp] * 0.5
+// in that operation order, index map and skipped columns as oracle_gpp,
+// double-double sums.  out_n1 (complex[number_bands], may be NULL) receives
+// each band's sum, out (complex[1]) the total.
+int oracle_gpp_achstemp(int number_bands, int ncouls, int ngpown, const int* inv_igp_index,
+                        const int* indinv, int indinv_len, const double* aqsmtemp,
+                        const double* aqsntemp, const double* I_eps_array, const double* vcoul,
+                        double* out, double* out_n1, int nthreads) {
+  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0) return kErrShape;
+  std::vector<int> igp_of(ngpown);
+  for (int my_igp = 0; my_igp < ngpown; ++my_igp) {
+    int g = map_igp(inv_igp_index, indinv, indinv_len, ncouls, my_igp);
+    if (g == -2) return kErrIndex;
+    igp_of[my_igp] = g;
+  }
+  const cd* aqsm = reinterpret_cast<const cd*>(aqsmtemp);
+  const cd* aqsn = reinterpret_cast<const cd*>(aqsntemp);
+  const cd* ieps = reinterpret_cast<const cd*>(I_eps_array);
+  const size_t nc = static_cast<size_t>(ncouls);
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  std::vector<CDD> band(number_bands);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int n1 = 0; n1 < number_bands; ++n1) {
+    CDD acc;
+    for (int my_igp = 0; my_igp < ngpown; ++my_igp) {
+      const int igp = igp_of[my_igp];
+      if (igp < 0) continue;
+      const cd mygpvar1 = std::conj(aqsm[n1 * nc + igp]);
+      CDD sch;
+      for (size_t ig = 0; ig < nc; ++ig) sch.add(-(aqsn[n1 * nc + ig] * ieps[my_igp * nc + ig] * mygpvar1));
+      acc.add(sch.scaled(vcoul[igp]).scaled(0.5));
+    }
+    band[n1] = acc;
+  }
+  CDD total;
+  for (int n1 = 0; n1 < number_bands; ++n1) {
+    total.add(band[n1]);
+    if (out_n1) {
+      cd v = band[n1].value();
+      out_n1[2 * n1] = v.real();
+      out_n1[2 * n1 + 1] = v.imag();
+    }
+  }
+  cd t = total.value();
+  out[0] = t.real();
+  out[1] = t.imag();
+  return kOk;
+}
+
 // FF schDt contraction for a list of (n1, ifreq) entries:
 //   schDt[n1][ifreq] = sum_my_igp (sum_ig I_epsR[ifreq][my_igp][ig] * aqsn[n1][ig])
 //                      * conj(aqsm[n1][igp(my_igp)])
@@ -552,3 +605,223 @@ int oracle_ff_schdt(int number_bands, int ncouls, int ngpown, int nfreq,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Full-frequency sigma: the band loop of ffkernel.deslippe.best.f90
+// (:201-626) around the schDt contraction, 0-based, in the C layouts of
+// FFKer_cori/ffKernel.cpp (I_epsR / I_epsA [nfreq][ngpown][ncouls],
+// aqsm / aqsn [number_bands][ncouls], schDt_matrix [number_bands][nfreq]).
+// Outputs (complex): achsDtemp[1], asxDtemp, achDtemp, achDtemp_cor,
+// achDtemp_corb, ach2Dtemp [nfreqeval] each, overwritten.
+//   static CH (:236-254)          achsDtemp
+//   SX, occupied bands (:279-389) asxDtemp
+//   CH from schDt (:459-521)      achDtemp (sigma1), achDtemp_corb (sigma3),
+//                                 ach2Dtemp (sigma2), achDtemp_cor (sigma4)
+//   delta-function terms (:530-613) ach2Dtemp, achDtemp_cor
+// with wx = freqevalmin - ekq[n1] + iw * freqevalstep.  schDt_matrix is an
+// input, as achDtemp_Kernel takes it (FFKer_cori/ffKernel.cpp:155); the live
+// Fortran zeroes it (:395) because its contraction is commented out.
+// Columns whose igp falls outside [0, ncouls) are skipped as the Fortran
+// skips them.  Sums in double-double, each band's terms in the Fortran
+// operation order.
+
+namespace {
+
+// Last grid interval [g[k], g[k+1]) holding w, k in 0..nfreq-2; nfreq-2 when
+// none does (both searches of the Fortran end there: :288-311, :536-545).
+int ff_interval(double w, const double* grid, int nfreq) {
+  int k = -1;
+  for (int j = 0; j < nfreq - 1; ++j)
+    if (w >= grid[j] && w < grid[j + 1]) k = j;
+  return k < 0 ? nfreq - 2 : k;
+}
+
+// sum_{my_igp valid} vcoul[igp] * sum_ig aqsn[n1][ig] conj(aqsm[n1][igp])
+//     * (f1 X1[my_igp][ig] + f2 X2[my_igp][ig])   (:339-346, :582-589)
+// with X = a - b when b is given (I_epsR - I_epsA), the element combination
+// and product order of the Fortran.
+cd ff_weighted_pair(int n1, int ncouls, int ngpown, const std::vector<int>& igp_of, const cd* aqsm,
+                    const cd* aqsn, const double* vcoul, const cd* a1, const cd* b1, const cd* a2,
+                    const cd* b2, double f1, double f2, double scale) {
+  const size_t nc = static_cast<size_t>(ncouls);
+  CDD tot;
+  for (int g = 0; g < ngpown; ++g) {
+    const int igp = igp_of[g];
+    if (igp < 0) continue;
+    CDD t;
+    const cd m = std::conj(aqsm[n1 * nc + igp]);
+    for (size_t ig = 0; ig < nc; ++ig) {
+      const size_t o = static_cast<size_t>(g) * nc + ig;
+      cd x;
+      if (b1)
+        x = (a1[o] - b1[o]) * f1 + (a2[o] - b2[o]) * f2;
+      else
+        x = a1[o] * f1 + a2[o] * f2;
+      if (scale != 1.0) x = scale * x;
+      t.add(aqsn[n1 * nc + ig] * m * x);
+    }
+    tot.add(t.scaled(vcoul[igp]));
+  }
+  return tot.value();
+}
+
+}  // namespace
+
+extern "C" int oracle_ff_sigma(int number_bands, int nvband, int ncouls, int ngpown, int nfreq,
+                               int nfreqeval, const int* inv_igp_index, const int* indinv,
+                               const double* aqsmtemp, const double* aqsntemp, const double* I_epsR,
+                               const double* I_epsA, const double* vcoul, const double* ekq,
+                               const double* dFreqGrid, const double* dFreqBrd, const double* pref,
+                               double pref_zb, double freqevalmin, double freqevalstep, double occ,
+                               const double* schDt_matrix, double* achsDtemp, double* asxDtemp,
+                               double* achDtemp, double* achDtemp_cor, double* achDtemp_corb,
+                               double* ach2Dtemp, int nthreads) {
+  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0 || nfreq < 2 || nfreqeval <= 0 || nvband < 0)
+    return kErrShape;
+  std::vector<int> igp_of(ngpown);
+  for (int g = 0; g < ngpown; ++g) {
+    const int ind = inv_igp_index[g];
+    if (ind < 0 || ind >= ncouls) return kErrIndex;
+    const int igp = indinv[ind];
+    igp_of[g] = (igp < 0 || igp >= ncouls) ? -1 : igp;
+  }
+  const cd* aqsm = reinterpret_cast<const cd*>(aqsmtemp);
+  const cd* aqsn = reinterpret_cast<const cd*>(aqsntemp);
+  const cd* epsR = reinterpret_cast<const cd*>(I_epsR);
+  const cd* epsA = reinterpret_cast<const cd*>(I_epsA);
+  const cd* brd = reinterpret_cast<const cd*>(dFreqBrd);
+  const cd* sdt = reinterpret_cast<const cd*>(schDt_matrix);
+  const size_t nc = static_cast<size_t>(ncouls);
+  const size_t slab = static_cast<size_t>(ngpown) * nc;
+  const cd I(0.0, 1.0);
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  const int ne = nfreqeval;
+  // per band: [0] achs, then 5 arrays of ne: asx, ach, ach_cor, ach_corb, ach2
+  std::vector<CDD> per(static_cast<size_t>(number_bands) * (1 + 5 * ne));
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int n1 = 0; n1 < number_bands; ++n1) {
+    CDD* r = &per[static_cast<size_t>(n1) * (1 + 5 * ne)];
+    CDD* asx = r + 1;
+    CDD* schDi = asx + ne;
+    CDD* schDi_cor = schDi + ne;
+    CDD* schDi_corb = schDi_cor + ne;
+    CDD* sch2Di = schDi_corb + ne;
+    const bool flag_occ = n1 < nvband;
+    // static CH (:240-253)
+    for (int g = 0; g < ngpown; ++g) {
+      const int igp = igp_of[g];
+      if (igp < 0) continue;
+      CDD t;
+      const cd m = std::conj(aqsm[n1 * nc + igp]);
+      for (size_t ig = 0; ig < nc; ++ig)
+        t.add(-(aqsn[n1 * nc + ig] * m * epsR[static_cast<size_t>(g) * nc + ig]));
+      r[0].add(t.scaled(vcoul[igp]).scaled(0.5));
+    }
+    // SX of the occupied bands (:279-389)
+    if (flag_occ) {
+      for (int iw = 0; iw < ne; ++iw) {
+        const double wx = freqevalmin - ekq[n1] + iw * freqevalstep;
+        const bool pos = wx >= 0.0;
+        const int f = ff_interval(pos ? wx : -wx, dFreqGrid, nfreq);
+        const double d = dFreqGrid[f + 1] - dFreqGrid[f];
+        const double f1 = pos ? (dFreqGrid[f + 1] - wx) / d : (dFreqGrid[f + 1] + wx) / d;
+        const double f2 = pos ? (wx - dFreqGrid[f]) / d : (-dFreqGrid[f] - wx) / d;
+        const cd* src = pos ? epsR : epsA;
+        const cd v = ff_weighted_pair(n1, ncouls, ngpown, igp_of, aqsm, aqsn, vcoul, src + f * slab,
+                                      nullptr, src + (f + 1) * slab, nullptr, f1, f2, 1.0);
+        asx[iw].add(v * occ);
+      }
+    }
+    // CH from schDt (:459-521)
+    for (int f = 0; f < nfreq; ++f) {
+      const cd sd = sdt[static_cast<size_t>(n1) * nfreq + f];
+      const double zb = dFreqGrid[f];
+      const cd coh = cd(zb, 0.0) - brd[f];
+      const cd cor = flag_occ ? -1.0 * cd(zb, 0.0) - brd[f] : cd(zb, 0.0) - brd[f];
+      cd left(0.0), lin(0.0), lin2(0.0), avg(0.0);
+      double zr = 0.0, zl = 0.0;
+      if (f != 0) {
+        zr = zb;
+        zl = dFreqGrid[f - 1];
+        const cd right = sd;
+        left = sdt[static_cast<size_t>(n1) * nfreq + f - 1];
+        avg = 0.5 * (right + left);
+        lin = right - left;
+        lin2 = lin / (zr - zl);
+      }
+      if (f != nfreq - 1)
+        for (int iw = 0; iw < ne; ++iw) {
+          const double wx = freqevalmin - ekq[n1] + iw * freqevalstep;
+          schDi[iw].add(-(cd(0.0, pref[f]) * sd / (wx - coh)));
+          schDi_corb[iw].add(-(cd(0.0, pref[f]) * sd / (wx - cor)));
+        }
+      if (f != 0)
+        for (int iw = 0; iw < ne; ++iw) {
+          const double e = freqevalmin - ekq[n1] + iw * freqevalstep;
+          double t = std::fabs((e - zr) / (e - zl));
+          if (t < 1e-4) t = 1e-4;
+          if (t > 1e4) t = 1e4;
+          t = -std::log(t);
+          sch2Di[iw].add(-(cd(0.0, pref_zb) * avg * t));
+          cd lin3;
+          if (flag_occ) {
+            double t4 = std::fabs((e + zr) / (e + zl));
+            if (t4 < 1e-4) t4 = 1e-4;
+            if (t4 > 1e4) t4 = 1e4;
+            t4 = std::log(t4);
+            lin3 = (left + lin2 * (-freqevalmin - ekq[n1] + iw * freqevalstep - zl)) * t4;
+          } else {
+            lin3 = (left + lin2 * (e - zl)) * t;
+          }
+          lin3 = lin3 + lin;
+          schDi_cor[iw].add(-(cd(0.0, pref_zb) * lin3));
+        }
+    }
+    // delta-function contributions (:530-613)
+    for (int iw = 0; iw < ne; ++iw) {
+      const double wx = freqevalmin - ekq[n1] + iw * freqevalstep;
+      if (wx >= 0.0) {
+        const int f = ff_interval(wx, dFreqGrid, nfreq);
+        const double d = dFreqGrid[f + 1] - dFreqGrid[f];
+        const double f1 = -0.5 * (dFreqGrid[f + 1] - wx) / d;
+        const double f2 = -0.5 * (wx - dFreqGrid[f]) / d;
+        const cd v = ff_weighted_pair(n1, ncouls, ngpown, igp_of, aqsm, aqsn, vcoul, epsR + f * slab,
+                                      epsA + f * slab, epsR + (f + 1) * slab, epsA + (f + 1) * slab, f1,
+                                      f2, 1.0);
+        sch2Di[iw].add(v);
+        if (!flag_occ) schDi_cor[iw].add(v);
+      } else if (flag_occ) {
+        const double w = -wx;
+        const int f = ff_interval(w, dFreqGrid, nfreq);
+        const double d = dFreqGrid[f + 1] - dFreqGrid[f];
+        const double f1 = (dFreqGrid[f + 1] - w) / d;
+        const double f2 = (w - dFreqGrid[f]) / d;
+        const cd v = ff_weighted_pair(n1, ncouls, ngpown, igp_of, aqsm, aqsn, vcoul, epsR + f * slab,
+                                      epsA + f * slab, epsR + (f + 1) * slab, epsA + (f + 1) * slab, f1,
+                                      f2, -0.5);
+        schDi_cor[iw].add(v);
+      }
+    }
+  }
+  CDD achs;
+  std::vector<CDD> tot(static_cast<size_t>(5) * ne);
+  for (int n1 = 0; n1 < number_bands; ++n1) {
+    const CDD* r = &per[static_cast<size_t>(n1) * (1 + 5 * ne)];
+    achs.add(r[0]);
+    for (int k = 0; k < 5 * ne; ++k) tot[k].add(r[1 + k]);
+  }
+  auto put = [](double* out, const CDD& v) {
+    const cd x = v.value();
+    out[0] = x.real();
+    out[1] = x.imag();
+  };
+  put(achsDtemp, achs);
+  for (int iw = 0; iw < ne; ++iw) {
+    put(asxDtemp + 2 * iw, tot[iw]);
+    put(achDtemp + 2 * iw, tot[ne + iw]);
+    put(achDtemp_cor + 2 * iw, tot[2 * ne + iw]);
+    put(achDtemp_corb + 2 * iw, tot[3 * ne + iw]);
+    put(ach2Dtemp + 2 * iw, tot[4 * ne + iw]);
+  }
+  return kOk;
+}

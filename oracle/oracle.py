@@ -34,6 +34,9 @@ def lib():
         l.oracle_gpp_columns.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _P, _P, _P, _P,
                                          _I, _I, _I]
         l.oracle_ff_schdt.argtypes = [_I, _I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _I]
+        l.oracle_ff_sigma.argtypes = [_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                      _D, _D, _D, _D, _P, _P, _P, _P, _P, _P, _P, _I]
+        l.oracle_gpp_achstemp.argtypes = [_I, _I, _I, _P, _P, _I, _P, _P, _P, _P, _P, _P, _I]
         l.oracle_gpp_abs2.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P,
                                       _I, _I, _I]
         _lib = l
@@ -120,6 +123,19 @@ def gpp_abs2(prob, band_begin=0, band_end=None, nthreads=0, wx_band_stride=0):
     return a, x
 
 
+def gpp_achstemp(prob, nthreads=0):
+    """Static remainder (Fortran formula): (achstemp, achstemp_n1[number_bands])."""
+    inv, indinv, _, aqsm, aqsn, ieps, _, vcoul = _prep(prob)
+    out = np.zeros(1, np.complex128)
+    n1 = np.zeros(prob.number_bands, np.complex128)
+    st = lib().oracle_gpp_achstemp(prob.number_bands, prob.ncouls, prob.ngpown, _p(inv), _p(indinv),
+                                   len(indinv), _p(aqsm), _p(aqsn), _p(ieps), _p(vcoul), _p(out), _p(n1),
+                                   nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_gpp_achstemp status {st}")
+    return out[0], n1
+
+
 def ff_schdt(prob, entries=None, nthreads=0):
     """schDt[n1][ifreq] for the (n1, ifreq) pairs in `entries` (default all)."""
     if entries is None:
@@ -198,3 +214,85 @@ def run_reference_binary(number_bands, nvband, ncouls, nodes_per_group, threads=
         ach[int(m.group(1))] = complex(float(m.group(2)), float(m.group(3)))
     t = _TIME.search(r.stdout)
     return ach, (float(t.group(1)) if t else float("nan")), r.stdout
+
+
+_ffref = None
+
+
+def reference_ff_lib():
+    """The reference's FF kernels through oracle/ff_ref_harness.cpp (None when
+    the reference checkout is absent)."""
+    global _ffref
+    if _ffref is None:
+        if not _build.build_reference() or not _build.FF_REF_LIB.exists():
+            return None
+        l = C.CDLL(str(_build.FF_REF_LIB))
+        l.ref_ff_kernels.argtypes = [_I] * 6 + [_D] * 3 + [_P] * 12
+        _ffref = l
+    return _ffref
+
+
+def reference_ff_kernels(prob, freqevalmin):
+    """(achsDtemp, asxDtemp[nfreqeval], achDtemp_cor[nfreqeval]) from the
+    reference's own achsDtemp_Kernel / asxDtemp_Kernel / achDtemp_cor_Kernel
+    (FFKer_cori/ffKernel.cpp:107-245) on the problem's arrays."""
+    l = reference_ff_lib()
+    if l is None:
+        return None
+    c = lambda a: np.array(a, dtype=np.complex128, order="C", copy=True)
+    i32 = lambda a: np.array(a, dtype=np.int32, order="C", copy=True)
+    f = lambda a: np.array(a, dtype=np.float64, order="C", copy=True)
+    p = prob
+    arrs = [i32(p.inv_igp_index), i32(p.indinv), c(p.aqsmtemp), c(p.aqsntemp), c(p.I_epsR), c(p.I_epsA),
+            f(p.vcoul), f(p.ekq), f(p.dFreqGrid)]
+    achs = np.zeros(1, np.complex128)
+    asx = np.zeros(p.nfreqeval, np.complex128)
+    cor = np.zeros(p.nfreqeval, np.complex128)
+    l.ref_ff_kernels(p.number_bands, p.nvband, p.ncouls, p.ngpown, p.nfreq, p.nfreqeval, freqevalmin,
+                     p.freqevalstep, p.occ, *[_p(a) for a in arrs], _p(achs), _p(asx), _p(cor))
+    return achs[0], asx, cor
+
+
+_FFOUT = re.compile(r"(achsDtemp|asxDtemp|achDtemp_cor) = \( *([-+0-9.eE]+), *([-+0-9.eE]+)\)")
+
+
+def run_reference_ff_binary(number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval, threads=None,
+                            timeout=600):
+    """Runs the unmodified FFKer_cori/ffKernel.cpp driver (its constant fill);
+    returns its printed achsDtemp, asxDtemp[0], achDtemp_cor[0]."""
+    if not _build.build_reference() or not _build.FF_REF_BIN.exists():
+        return None
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    r = subprocess.run([str(_build.FF_REF_BIN), str(number_bands), str(nvband), str(ncouls), str(ngpown),
+                        str(nfreq), str(nfreqeval)], capture_output=True, text=True, env=env,
+                       timeout=timeout)
+    return {m.group(1): complex(float(m.group(2)), float(m.group(3))) for m in _FFOUT.finditer(r.stdout)}
+
+
+def ff_sigma(prob, schdt=None, nthreads=0):
+    """Full-frequency sigma (Fortran band loop) on a workload.FFSigmaProblem.
+    schdt: complex [number_bands][nfreq] (default zeros, as the live Fortran
+    leaves it).  Returns dict(achsDtemp, asxDtemp, achDtemp, achDtemp_cor,
+    achDtemp_corb, ach2Dtemp)."""
+    c = lambda a: np.ascontiguousarray(a, dtype=np.complex128)
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    p = prob
+    if schdt is None:
+        schdt = np.zeros((p.number_bands, p.nfreq), np.complex128)
+    args = [i32(p.inv_igp_index), i32(p.indinv), c(p.aqsmtemp), c(p.aqsntemp), c(p.I_epsR), c(p.I_epsA),
+            f(p.vcoul), f(p.ekq), f(p.dFreqGrid), c(p.dFreqBrd), f(p.pref)]
+    sd = c(schdt)
+    out = {k: np.zeros(1 if k == "achsDtemp" else p.nfreqeval, np.complex128)
+           for k in ("achsDtemp", "asxDtemp", "achDtemp", "achDtemp_cor", "achDtemp_corb", "ach2Dtemp")}
+    st = lib().oracle_ff_sigma(p.number_bands, p.nvband, p.ncouls, p.ngpown, p.nfreq, p.nfreqeval,
+                               *[_p(a) for a in args], p.pref_zb, p.freqevalmin, p.freqevalstep, p.occ,
+                               _p(sd), *[_p(out[k]) for k in ("achsDtemp", "asxDtemp", "achDtemp",
+                                                               "achDtemp_cor", "achDtemp_corb",
+                                                               "ach2Dtemp")], nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_ff_sigma status {st}")
+    out["achsDtemp"] = out["achsDtemp"][0]
+    return out

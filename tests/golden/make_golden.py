@@ -11,6 +11,19 @@ fixtures it writes are committed so the tests run without it.
       (BGW-Kernels/gppKer.cpp:130-159) on seeded inputs that
       fortkernels-_gb300/workload.py regenerates from the recorded seed.
 
+  ff_sigma_reference.json       the unmodified FFKer_cori/ffKernel.cpp
+      driver's printed achsDtemp / asxDtemp(1) / achDtemp_cor(1) on its
+      constant fill, and its achsDtemp_Kernel / asxDtemp_Kernel /
+      achDtemp_cor_Kernel (through oracle/ff_ref_harness.cpp) on seeded
+      inputs that workload.ff_sigma_random regenerates.  The C++ kernels
+      differ from the Fortran loop in places that these inputs avoid or
+      undo (recorded per case): achsDtemp_Kernel reads frequency 1 (the
+      Fortran frequency 1 is index 0), so slab 1 holds slab 0; wx lacks the
+      (iw-1) * freqevalstep term, so the C++ kernels run with freqevalmin
+      one step lower and every iw equals the Fortran iw = 0; no wx falls on
+      a grid point or outside the grid, where the C++ interval search
+      differs.
+
 Run:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -55,6 +68,40 @@ def igp_map(prob):
     return np.array(out, dtype=np.int32)
 
 
+FF_CONST_SHAPES = [(4, 2, 512, 32, 6, 5), (12, 3, 1000, 50, 8, 4), (20, 1, 777, 40, 12, 3)]
+FF_RANDOM_CASES = {
+    # name: (number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval, seed, freqevalmin)
+    "ff_random_a": (12, 2, 300, 20, 8, 4, 7, 0.3),
+    "ff_random_b": (9, 3, 257, 13, 10, 3, 8, 0.7),
+}
+
+
+def ff_main():
+    const = []
+    for shape in FF_CONST_SHAPES:
+        out = O.run_reference_ff_binary(*shape, threads=4)
+        const.append({"shape": list(shape), **{k: [v.real, v.imag] for k, v in out.items()}})
+        print(shape, out)
+    rand = []
+    for name, (nb, nv, nc, ng, nf, nfe, seed, fmin) in FF_RANDOM_CASES.items():
+        p = W.ff_sigma_random(nb, nv, nc, ng, nf, nfe, seed)
+        p.freqevalmin = fmin
+        q = W.FFSigmaProblem(**p.__dict__)
+        q.I_epsR = p.I_epsR.copy()
+        q.I_epsR[1] = p.I_epsR[0]
+        achs, _, _ = O.reference_ff_kernels(q, fmin - p.freqevalstep)
+        _, asx, cor = O.reference_ff_kernels(p, fmin - p.freqevalstep)
+        rand.append({"name": name, "args": [nb, nv, nc, ng, nf, nfe, seed], "freqevalmin": fmin,
+                     "achsDtemp": [achs.real, achs.imag],
+                     "asxDtemp_iw0": [[z.real, z.imag] for z in asx],
+                     "achDtemp_cor_iw0": [[z.real, z.imag] for z in cor]})
+        print(name, achs, asx[0], cor[0])
+    (HERE / "ff_sigma_reference.json").write_text(json.dumps({
+        "source": "FFKer_cori/ffKernel.cpp, unmodified, g++ -O3 -fopenmp -std=c++11: driver stdout "
+                  "(6 decimals) on its constant fill; its kernels on seeded inputs",
+        "constant_fill": const, "random": rand}, indent=1))
+
+
 def main():
     if O.reference_lib() is None:
         sys.exit("reference checkout not found; set REFERENCE_ROOT")
@@ -84,3 +131,4 @@ def main():
 
 if __name__ == "__main__":
     main()
+    ff_main()

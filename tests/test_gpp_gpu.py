@@ -2,7 +2,12 @@
 
 Bars (written in each test): FP64 path <= 1e-12 relative per output, mixed
 path <= 1e-6 relative per achtemp / asxtemp output.  acht_n1_loc is checked
-per band for FP64 and normwise for the mixed path.
+per band for FP64 and normwise for the mixed path.  On the seeded random
+cases the mixed bar is max(1e-6 |exact|, 8 * 2^-24 * sqrt(sum |term|^2)) per
+output: FP32 terms carry independent errors of ~1.5 * 2^-24 rms, so an
+output whose terms cancel (sqrt(sum |term|^2) / |sum| above ~10) can sit
+above 1e-6 relative while within the method's error; the second bound is
+that model at more than five standard deviations.
 """
 import numpy as np
 import pytest
@@ -16,11 +21,22 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
 MIXED_TOL = 1e-6
+FP32_TERM_BOUND = 8 * 2.0 ** -24
 
 
-def _check(g, o, prec, check_n1=True):
+def _mixed_bound(exact, abs2):
+    return np.maximum(MIXED_TOL * np.abs(exact), FP32_TERM_BOUND * np.sqrt(abs2))
+
+
+def _check(g, o, prec, check_n1=True, abs2=None):
     ach, asx, n1 = g
     oach, oasx, on1 = o
+    if prec == 1 and abs2 is not None:
+        assert np.all(np.abs(ach - oach) <= _mixed_bound(oach, abs2[0]))
+        assert np.all(np.abs(asx - oasx) <= _mixed_bound(oasx, abs2[1]))
+        if check_n1:
+            assert normwise_err(n1, on1) <= MIXED_TOL
+        return
     if prec == 0:
         assert rel_err(ach, oach).max() <= FP64_TOL
         if np.any(oasx != 0):
@@ -73,7 +89,7 @@ def test_random_matches_oracle(sigma_lib, case, prec):
     prob = W.gpp_random(nb, nvb, nc, ng, seed, stress=stress)
     o = O.gpp(prob)
     g = sigma_lib.gpp_host(prob, prec)
-    _check(g, o, prec)
+    _check(g, o, prec, abs2=O.gpp_abs2(prob) if prec == 1 else None)
 
 
 @pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])

@@ -154,3 +154,77 @@ def test_ff_oracle_matches_matmul_and_closed_form():
     outc = O.ff_schdt(c).reshape(4, 2)
     exact = 6 * 100 * 0.5 * (0.5 + 0.5j)
     assert np.abs(outc - exact).max() / abs(exact) < 1e-15
+
+
+def _achstemp_numpy(p):
+    igp = _igp_map(p)
+    ok = (igp >= 0) & (igp <= p.ncouls)
+    M = p.aqsntemp @ p.I_eps_array.T                       # sum_ig aqsn[n1][ig] I_eps[my_igp][ig]
+    w = np.where(ok, -0.5 * p.vcoul[np.clip(igp, 0, p.ncouls - 1)], 0.0)
+    am = np.conj(p.aqsmtemp[:, np.clip(igp, 0, p.ncouls - 1)])
+    return (w[None, :] * am * M).sum(axis=1)
+
+
+def test_static_remainder_oracle_closed_form_and_matmul():
+    # gppkernel.deslippe.09.30.2014.f90:195-228 on the constant fill: every
+    # term is -0.5 * |0.5+0.5i|^2 * (0.5+0.5i) = -0.125-0.125i
+    c = W.gpp_constant(16, 2, 1024, 8)
+    tot, n1 = O.gpp_achstemp(c)
+    exact = c.number_bands * c.ngpown * c.ncouls * (-0.125 - 0.125j)
+    assert tot == exact
+    assert np.all(n1 == exact / c.number_bands)
+    p = W.gpp_random(9, 1, 700, 31, 12)
+    p.indinv = p.indinv.copy()
+    p.indinv[p.inv_igp_index[4]] = -3                     # a skipped column
+    tot, n1 = O.gpp_achstemp(p)
+    ref = _achstemp_numpy(p)
+    assert np.abs(n1 - ref).max() / np.abs(ref).max() < 1e-13
+    assert abs(tot - ref.sum()) / abs(tot) < 1e-13
+
+
+FF_REF = json.loads((GOLD / "ff_sigma_reference.json").read_text())
+
+
+@pytest.mark.parametrize("run", FF_REF["constant_fill"], ids=lambda r: "x".join(map(str, r["shape"])))
+def test_ff_sigma_oracle_matches_reference_driver_constant_fill(run):
+    """The unmodified FFKer_cori/ffKernel.cpp driver's printed results on its
+    constant fill (its schDt_matrix stays zero, as in the Fortran)."""
+    p = W.ff_sigma_constant(*run["shape"])
+    o = O.ff_sigma(p)
+    for key, ours in (("achsDtemp", o["achsDtemp"]), ("asxDtemp", o["asxDtemp"][0]),
+                      ("achDtemp_cor", o["achDtemp_cor"][0])):
+        ref = complex(*run[key])
+        assert abs(ours - ref) <= 1e-6 + 1e-12 * abs(ref)   # the driver prints 6 decimals
+
+
+@pytest.mark.parametrize("case", FF_REF["random"], ids=lambda c: c["name"])
+def test_ff_sigma_oracle_matches_reference_kernels(case):
+    """The reference's own achsDtemp / asxDtemp / achDtemp_cor kernels on
+    seeded inputs (see tests/golden/make_golden.py for the C++ deviations the
+    case avoids)."""
+    p = W.ff_sigma_random(*case["args"])
+    p.freqevalmin = case["freqevalmin"]
+    o = O.ff_sigma(p)
+    ach = complex(*case["achsDtemp"])
+    assert abs(o["achsDtemp"] - ach) <= 1e-13 * abs(ach)
+    for z in case["asxDtemp_iw0"]:
+        assert abs(o["asxDtemp"][0] - complex(*z)) <= 1e-13 * abs(complex(*z))
+    for z in case["achDtemp_cor_iw0"]:
+        assert abs(o["achDtemp_cor"][0] - complex(*z)) <= 1e-13 * abs(complex(*z))
+
+
+def test_ff_sigma_oracle_schdt_epilogue_is_linear():
+    # the CH terms from schDt_matrix are linear in it; doubling it doubles
+    # achDtemp and achDtemp_corb and the schDt parts of the other two
+    p = W.ff_sigma_random(6, 2, 64, 8, 7, 4, 3)
+    rng = np.random.default_rng(5)
+    sd = rng.standard_normal((6, 7)) + 1j * rng.standard_normal((6, 7))
+    z = O.ff_sigma(p)
+    a = O.ff_sigma(p, sd)
+    b = O.ff_sigma(p, 2 * sd)
+    for k in ("achDtemp", "achDtemp_corb"):
+        assert np.all(z[k] == 0)
+        assert np.abs(b[k] - 2 * a[k]).max() <= 1e-13 * np.abs(a[k]).max()
+    for k in ("achDtemp_cor", "ach2Dtemp"):
+        assert np.abs((b[k] - z[k]) - 2 * (a[k] - z[k])).max() <= 1e-12 * np.abs(a[k] - z[k]).max()
+    assert a["achsDtemp"] == z["achsDtemp"] and np.array_equal(a["asxDtemp"], z["asxDtemp"])
