@@ -317,6 +317,63 @@ def run_ff(S, W, torch, dist, world, stream, sptr, args):
     return res
 
 
+FF_SIGMA_NVBAND, FF_SIGMA_NFREQEVAL = 2, 15
+
+
+def run_ff_sigma(S, W, torch, dist, world, stream, sptr):
+    """Full-frequency sigma band loop at the FF production shape (512 bands,
+    ncouls 16384, ngpown 820, nfreq 15, nfreqeval 15, nvband 2; seeded
+    I_epsR / I_epsA, the mini-app's energies and grid): the two vcoul-weighted
+    contractions plus the schDt contraction and the band algebra, in both
+    contraction forms; the tensor form's outputs against the FP64 form's."""
+    nb, nc, ng, nf = FF_SHAPE
+    ne, nv = FF_SIGMA_NFREQEVAL, FF_SIGMA_NVBAND
+    f64 = dict(dtype=torch.float64, device="cuda")
+    epsr = torch.empty(2 * nf * ng * nc, **f64)
+    epsa = torch.empty_like(epsr)
+    aqsn = torch.empty(2 * nb * nc, **f64)
+    aqsm = torch.empty_like(aqsn)
+    vc = torch.empty(nc, **f64)
+    S.fill_complex_device(epsr.data_ptr(), nf * ng * nc, W.FF_SEED, W.AID_IEPSR, (-1, 1), (-1, 1), sptr)
+    S.fill_complex_device(epsa.data_ptr(), nf * ng * nc, W.FF_SEED, W.AID_IEPSA, (-1, 1), (-1, 1), sptr)
+    S.fill_complex_device(aqsn.data_ptr(), nb * nc, W.FF_SEED, W.AID_AQSN, (-1, 1), (-1, 1), sptr)
+    S.fill_complex_device(aqsm.data_ptr(), nb * nc, W.FF_SEED, W.AID_AQSM, (-1, 1), (-1, 1), sptr)
+    S.fill_real_device(vc.data_ptr(), nc, W.FF_SEED, W.AID_VCOUL, 0.1, 10.0, sptr)
+    ekq, grid, brd, pref = W.ff_sigma_grid(nb, nf)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.float64).copy()).cuda()
+    d_ekq, d_grid, d_brd, d_pref = dev(ekq), dev(grid), dev(brd.astype(np.complex128)), dev(pref)
+    inv, indinv = W.ff_index_maps(nc, ng)
+    flops = 3 * 8.0 * nf * ng * nb * nc  # three contractions per step
+    res = {"workload": f"FF sigma band loop: {nb} bands x {nf}x{ng} rows x {nc} g-vectors, "
+                       f"nfreqeval {ne}, nvband {nv}; 3 contractions + band algebra per step",
+           "unit": "TFLOP/s (FP64-equivalent, contractions)"}
+    outs = {}
+    for mode, name, steps in ((1, "ozaki_bf16", 10), (0, "fp64", 1)):
+        plan = S.FfSigmaPlan(nb, nv, nc, ng, nf, ne, inv, indinv, mode)
+        out = torch.zeros(2 * (1 + 5 * ne), **f64)
+        run = lambda: plan.execute(aqsm, aqsn, epsr, epsa, vc, d_ekq, d_grid, d_brd, d_pref, 0.5 / 3.14, 0.0,
+                                   0.5, 1.0, None, out, sptr)
+        run()
+        plan.set_timing(True)
+        ms = timed(torch, dist, world, run, steps, stream)
+        t = plan.timing()
+        res[name] = {"value": round(flops * world / (ms / steps * 1e-3) / 1e12, 3),
+                     "ms_per_step": round(ms / steps, 3),
+                     "contraction_ms_per_step": round(t["contraction_ms"] / steps, 3),
+                     "status": plan.status(sptr)}
+        outs[name] = S.FfSigmaPlan.unpack(out.cpu().numpy(), ne)
+        plan.close()
+    errs = {}
+    for k, v in outs["fp64"].items():
+        w = outs["ozaki_bf16"][k]
+        errs[k] = float(np.linalg.norm(np.atleast_1d(w - v)) / max(np.linalg.norm(np.atleast_1d(v)), 1e-300))
+    res["ozaki_bf16"]["rel_err_vs_fp64_normwise"] = errs
+    res["speedup_ozaki_vs_fp64"] = round(res["ozaki_bf16"]["value"] / res["fp64"]["value"], 1)
+    del epsr, epsa, aqsn, aqsm
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_static(S, W, torch, dist, world, stream, sptr, inst):
     """Static remainder (sigma_gpp_static_execute) on the production
     instance's device arrays: both contraction forms, FP64-equivalent TF/s
@@ -360,7 +417,7 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     shapes = W.batched_shapes()[: args.batch_instances]
     xs = batched.device_instances(shapes)
     dicts = [x.as_dict() for x in xs]
-    tiles = [autotune.tile_for(x.nb, x.ng) for x in xs]
+    tiles = [autotune.tile_for(x.nb, x.ng, shared=True) for x in xs]
     res = {"workload": f"{len(xs)} GPP instances, number_bands U{{64..512}}, ncouls U{{4096..32768}}/256, "
                        "nodes_per_group U{10..40}, nvband U{1..8}, seeds 1000+i",
            "instances": len(xs), "input_bytes": int(sum(x.input_bytes for x in xs)),
@@ -520,6 +577,7 @@ def run_ours(args, rank, world, local_rank):
     fp64_pipe_peak = 2 * 2 * sms * clock_mhz * 1e6 / 1e12
     fp32_pipe_peak = 2 * 128 * sms * clock_mhz * 1e6 / 1e12
     ff = None if args.no_ff else run_ff(S, W, torch, dist, world, stream, sptr, args)
+    ffs = None if args.no_ff else run_ff_sigma(S, W, torch, dist, world, stream, sptr)
     batch = None if args.no_batched else run_batched(S, W, torch, dist, world, stream, sptr, args, value)
     worst = max(max(mixed_err["achtemp"]), max(mixed_err["asxtemp"]),
                 max(stress_err["achtemp"]), max(stress_err["asxtemp"]))
@@ -561,6 +619,7 @@ def run_ours(args, rank, world, local_rank):
                                "frac": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12 / fp32_pipe_peak, 4),
                                "peak_source": "FP32 pipe 128 FFMA/clk/SM at the sampled SM clock"}},
         "ff": ff,
+        "ff_sigma": ffs,
         "batched": batch,
         "static_remainder": static,
         "peaks_measured": {"fp64_fma_probe_tflops": round(fp64_peak, 4),

@@ -1,21 +1,23 @@
 """Tile-shape tuner for the batched FP64 GPP main pass.
 
 Each work item of the main pass covers a (band block x column block x
-g-vector split) tile.  Three tile shapes are compiled: 32 bands x 32 columns,
-16 x 64 and 64 x 16 (same 1024 (band, column) pairs per item, 256 threads
-with 2 x 2 pairs each).  Which one is fastest depends on how the instance's
-number_bands and ngpown pad to the block sizes and on how much staged data
-each item re-reads, so the choice is made per shape class:
+g-vector split) tile.  Two kernel families are compiled, each with three
+tile shapes: the shared-frequency kernel (every band uses the same three
+frequencies, the mini-app's case): 64 bands x 32 columns, 32 x 64, 32 x 32
+(tiles 3, 4, 5); and the per-band-frequency kernel: 32 x 32, 16 x 64,
+64 x 16 (tiles 0, 1, 2).  Which shape is fastest depends on how the
+instance's number_bands and ngpown pad to the block sizes and on how much
+staged data each item re-reads, so the choice is made per shape class:
 
     class "b{i}c{j}":  i = ((ceil(number_bands / 16) - 1) mod 4),
                        j = ((ceil(ngpown / 16) - 1) mod 4)
 
 i.e. how many 16-band (16-column) slabs the last 64-wide block holds.  The
-tuner times every tile on one representative instance per class (nc = 4096;
-all tiles scale the same way in ncouls) through a one-instance batch replayed
-as a CUDA graph, and writes the fastest tile per class to
-`tuning/gpp_tiles_gb300.json`.  `tile_for()` reads that table; without it the
-library picks the least-padded tile itself.
+tuner times every tile of both families on one representative instance per
+class (nc = 4096; all tiles scale the same way in ncouls) through a
+one-instance batch replayed as a CUDA graph, and writes the fastest tile per
+class and family to `tuning/gpp_tiles_gb300.json`.  `tile_for()` reads that
+table; without it the library picks the least-padded tile itself.
 
     python fortkernels-_gb300/autotune.py --out <path>
 """
@@ -27,7 +29,9 @@ import pathlib
 
 PKG = pathlib.Path(__file__).resolve().parent
 TABLE = PKG / "tuning" / "gpp_tiles_gb300.json"
-TILES = {0: "32x32", 1: "16x64", 2: "64x16"}
+TILES = {0: "32x32", 1: "16x64", 2: "64x16", 3: "y64x32", 4: "y32x64", 5: "y32x32"}
+FAMILIES = {"shared": (3, 4, 5), "per_band": (0, 1, 2)}
+TABLE_KEY = {"shared": "classes", "per_band": "classes_per_band"}
 _table = None
 
 
@@ -48,12 +52,14 @@ def load_table(path=None):
     return t
 
 
-def tile_for(number_bands: int, ngpown: int, table=None) -> int:
-    """Tuned tile for this shape (-1 = the library's least-padding choice)."""
+def tile_for(number_bands: int, ngpown: int, table=None, shared=True) -> int:
+    """Tuned tile for this shape and kernel family (-1 = the library's
+    least-padding choice)."""
     t = table if table is not None else load_table()
-    if not t:
+    if not t or TABLE_KEY["shared" if shared else "per_band"] not in t:
         return -1
-    return int(t["classes"].get(shape_class(number_bands, ngpown), -1))
+    v = int(t[TABLE_KEY["shared" if shared else "per_band"]].get(shape_class(number_bands, ngpown), -1))
+    return v if v in FAMILIES["shared" if shared else "per_band"] else -1
 
 
 def representative(cls_i: int, cls_j: int):
@@ -69,39 +75,43 @@ def tune(reps=5, ncouls=4096, log=print):
 
     S.load()
     stream = torch.cuda.Stream()
-    classes, timings = {}, {}
-    for i in range(4):
-        for j in range(4):
-            nb, ng = representative(i, j)
-            key = shape_class(nb, ng)
-            inst = batched.DeviceInstance(nb, 2, ncouls, ng, seed=5000 + 4 * i + j)
-            ms = {}
-            for tile in TILES:
-                b = S.GppBatch([inst.as_dict()], precision=S.PREC_FP64, tiles=[tile])
-                b.launch_graph(stream.cuda_stream)  # capture + warm-up
-                b.launch_graph(stream.cuda_stream)
-                stream.synchronize()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                for _ in range(reps):
+    out = {"version": 2, "device": torch.cuda.get_device_name(),
+           "tiles": {str(k): v for k, v in TILES.items()},
+           "class_rule": "b{i}c{j}: i = (ceil(number_bands/16)-1) mod 4, j = (ceil(ngpown/16)-1) mod 4"}
+    for family, tiles in FAMILIES.items():
+        classes, timings = {}, {}
+        for i in range(4):
+            for j in range(4):
+                nb, ng = representative(i, j)
+                key = shape_class(nb, ng)
+                inst = batched.DeviceInstance(nb, 2, ncouls, ng, seed=5000 + 4 * i + j,
+                                              per_band_wx=family == "per_band")
+                ms = {}
+                for tile in tiles:
+                    b = S.GppBatch([inst.as_dict()], precision=S.PREC_FP64, tiles=[tile])
+                    b.launch_graph(stream.cuda_stream)  # capture + warm-up
                     b.launch_graph(stream.cuda_stream)
-                e1.record(stream)
-                stream.synchronize()
-                if b.status(stream.cuda_stream) != 0:
-                    raise RuntimeError(f"batch status {b.status(stream.cuda_stream)} in tuning")
-                ms[TILES[tile]] = e0.elapsed_time(e1) / reps
-                b.close()
-            best = min(ms, key=ms.get)
-            classes[key] = [k for k, v in TILES.items() if v == best][0]
-            timings[key] = {"number_bands": nb, "ngpown": ng, "ncouls": ncouls,
-                            "ms": {k: round(v, 4) for k, v in ms.items()}}
-            log(key, nb, ng, {k: round(v, 3) for k, v in ms.items()}, "->", best)
-            del inst
-            torch.cuda.empty_cache()
-    return {"version": 1, "device": torch.cuda.get_device_name(),
-            "tiles": {str(k): v for k, v in TILES.items()},
-            "class_rule": "b{i}c{j}: i = (ceil(number_bands/16)-1) mod 4, j = (ceil(ngpown/16)-1) mod 4",
-            "classes": classes, "timings": timings}
+                    stream.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    for _ in range(reps):
+                        b.launch_graph(stream.cuda_stream)
+                    e1.record(stream)
+                    stream.synchronize()
+                    if b.status(stream.cuda_stream) != 0:
+                        raise RuntimeError(f"batch status {b.status(stream.cuda_stream)} in tuning")
+                    ms[TILES[tile]] = e0.elapsed_time(e1) / reps
+                    b.close()
+                best = min(ms, key=ms.get)
+                classes[key] = [k for k, v in TILES.items() if v == best][0]
+                timings[key] = {"number_bands": nb, "ngpown": ng, "ncouls": ncouls,
+                                "ms": {k: round(v, 4) for k, v in ms.items()}}
+                log(family, key, nb, ng, {k: round(v, 3) for k, v in ms.items()}, "->", best)
+                del inst
+                torch.cuda.empty_cache()
+        out[TABLE_KEY[family]] = classes
+        out["timings" if family == "shared" else "timings_per_band"] = timings
+    return out
 
 
 def main():

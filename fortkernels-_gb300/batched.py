@@ -16,7 +16,7 @@ import workload as W
 
 
 class DeviceInstance:
-    def __init__(self, number_bands, nvband, ncouls, ngpown, seed, stress=False, **_):
+    def __init__(self, number_bands, nvband, ncouls, ngpown, seed, stress=False, per_band_wx=False, **_):
         nb, nc, ng = number_bands, ncouls, ngpown
         self.nb, self.nvb, self.nc, self.ng, self.seed = nb, nvband, nc, ng, seed
         f64 = dict(dtype=torch.float64, device="cuda")
@@ -33,7 +33,11 @@ class DeviceInstance:
             S.fill_stress_device(self.wt.data_ptr(), ng * nc, seed, W.AID_STRESS, W.wx_frequencies())
         S.fill_real_device(self.vcoul.data_ptr(), nc, seed, W.AID_VCOUL, 0.1, 10.0)
         self.inv, self.indinv = W.gpp_index_maps(nc, ng)
-        self.wx = torch.tensor(W.wx_frequencies(), **f64)
+        # per_band_wx: the same three frequencies stored once per band
+        # (wx_array[n1][3], stride 3), which selects the per-band kernels
+        wx = W.wx_frequencies()
+        self.wx_stride = 3 if per_band_wx else 0
+        self.wx = torch.tensor(np.tile(wx, nb) if per_band_wx else wx, **f64)
         self.ach = torch.zeros(6, **f64)
         self.asx = torch.zeros(6, **f64)
         self.n1 = torch.zeros(2 * nb, **f64)
@@ -49,7 +53,8 @@ class DeviceInstance:
 
     def as_dict(self):
         return dict(number_bands=self.nb, nvband=self.nvb, ncouls=self.nc, ngpown=self.ng,
-                    inv_igp_index=self.inv, indinv=self.indinv, wx_array=self.wx, wx_band_stride=0,
+                    inv_igp_index=self.inv, indinv=self.indinv, wx_array=self.wx,
+                    wx_band_stride=self.wx_stride,
                     occ=1.0, aqsmtemp=self.aqsm, aqsntemp=self.aqsn, I_eps_array=self.ieps,
                     wtilde_array=self.wt, vcoul=self.vcoul, achtemp=self.ach, asxtemp=self.asx,
                     acht_n1_loc=self.n1)
@@ -63,7 +68,8 @@ class DeviceInstance:
         plan = S.GppPlan(self.nb, self.nvb, self.nc, self.ng, self.inv, self.indinv, precision=precision)
         f64 = dict(dtype=torch.float64, device="cuda")
         ach, asx, n1 = torch.zeros(6, **f64), torch.zeros(6, **f64), torch.zeros(2 * self.nb, **f64)
-        plan.execute(self.wx, self.aqsm, self.aqsn, self.ieps, self.wt, self.vcoul, ach, asx, n1)
+        plan.execute(self.wx, self.aqsm, self.aqsn, self.ieps, self.wt, self.vcoul, ach, asx, n1,
+                     wx_band_stride=self.wx_stride)
         torch.cuda.synchronize()
         plan.close()
         return tuple(t.cpu().numpy().view(np.complex128) for t in (ach, asx, n1))

@@ -176,6 +176,150 @@ __global__ void ff_sigma_sum_kernel(int nb, int nf, int ne, const double2* cr, c
 }  // namespace
 }  // namespace sigma
 
+using sigma::FfSigmaArgs;
+using sigma::kOut;
+using sigma::up256;
+using sigma::ff_sigma_band_kernel;
+using sigma::ff_sigma_sum_kernel;
+
+struct sigma_ff_sigma_plan_s {
+  int device = 0, nb = 0, nvband = 0, nf = 0, ne = 0;
+  sigma_ff_plan ff = nullptr;
+  void* block = nullptr;
+  double2 *cr = nullptr, *ca = nullptr, *sd = nullptr, *per = nullptr;
+};
+
+extern "C" int sigma_ff_sigma_plan_create(sigma_ff_sigma_plan* out, int number_bands, int nvband,
+                                          int ncouls, int ngpown, int nfreq, int nfreqeval,
+                                          const int* inv_igp_index, const int* indinv, int mode) {
+  using namespace sigma;
+  if (!out || !inv_igp_index || !indinv) return SIGMA_ERR_NULL;
+  *out = nullptr;
+  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0 || ngpown > ncouls || nfreq < 2 ||
+      nfreqeval <= 0 || nvband < 0 || nvband > number_bands)
+    return SIGMA_ERR_INVALID_SHAPE;
+  if (mode != SIGMA_FF_FP64 && mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
+  // column map of the Fortran loop: igp = indinv[inv_igp_index[my_igp]];
+  // columns with igp outside [0, ncouls) are left out (:324-327)
+  std::vector<int> igp_of(ngpown);
+  for (int g = 0; g < ngpown; ++g) {
+    const int ind = inv_igp_index[g];
+    if (ind < 0 || ind >= ncouls) return SIGMA_ERR_INDEX_RANGE;
+    const int igp = indinv[ind];
+    igp_of[g] = (igp < 0 || igp >= ncouls) ? -1 : igp;
+  }
+  auto* p = new sigma_ff_sigma_plan_s();
+  int st = ff_plan_build(&p->ff, number_bands, ncouls, ngpown, nfreq, igp_of, mode);
+  if (st != SIGMA_OK) {
+    delete p;
+    return st;
+  }
+  cudaGetDevice(&p->device);
+  p->nb = number_bands;
+  p->nvband = nvband;
+  p->nf = nfreq;
+  p->ne = nfreqeval;
+  const size_t mat = up256(sizeof(double2) * (size_t)number_bands * nfreq);
+  const size_t per = up256(sizeof(double2) * (size_t)number_bands * kOut * nfreqeval);
+  cudaError_t e = cudaMalloc(&p->block, 3 * mat + per);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_last_cuda_error(e, "cudaMalloc(ff sigma plan)", __LINE__);
+    sigma_ff_plan_destroy(p->ff);
+    delete p;
+    return SIGMA_ERR_ALLOC;
+  }
+  char* b = static_cast<char*>(p->block);
+  p->cr = reinterpret_cast<double2*>(b);
+  p->ca = reinterpret_cast<double2*>(b + mat);
+  p->sd = reinterpret_cast<double2*>(b + 2 * mat);
+  p->per = reinterpret_cast<double2*>(b + 3 * mat);
+  *out = p;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_ff_sigma_plan_destroy(sigma_ff_sigma_plan p) {
+  if (!p) return SIGMA_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(p->device);
+  if (p->block) cudaFree(p->block);
+  sigma_ff_plan_destroy(p->ff);
+  cudaSetDevice(cur);
+  delete p;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_ff_sigma_plan_set_timing(sigma_ff_sigma_plan p, int enable) {
+  if (!p) return SIGMA_ERR_NULL;
+  return sigma_ff_plan_set_timing(p->ff, enable);
+}
+
+extern "C" int sigma_ff_sigma_plan_timing(sigma_ff_sigma_plan p, int* contractions,
+                                          double* contraction_ms, double* other_ms) {
+  if (!p) return SIGMA_ERR_NULL;
+  int launches = 0;
+  return sigma_ff_plan_timing(p->ff, contractions, contraction_ms, other_ms, &launches);
+}
+
+extern "C" int sigma_ff_sigma_plan_status(sigma_ff_sigma_plan p, void* stream) {
+  if (!p) return SIGMA_ERR_NULL;
+  return sigma_ff_plan_status(p->ff, stream);
+}
+
+extern "C" int sigma_ff_sigma_execute(sigma_ff_sigma_plan p, const sigma_complex128* aqsmtemp,
+                                      const sigma_complex128* aqsntemp,
+                                      const sigma_complex128* I_epsR,
+                                      const sigma_complex128* I_epsA, const double* vcoul,
+                                      const double* ekq, const double* dFreqGrid,
+                                      const sigma_complex128* dFreqBrd, const double* pref,
+                                      double pref_zb, double freqevalmin, double freqevalstep,
+                                      double occ, const sigma_complex128* schDt_matrix,
+                                      sigma_complex128* out, void* stream) {
+  using namespace sigma;
+  if (!p) return SIGMA_ERR_NULL;
+  if (!aqsmtemp || !aqsntemp || !I_epsR || !I_epsA || !vcoul || !ekq || !dFreqGrid || !dFreqBrd ||
+      !pref || !out)
+    return SIGMA_ERR_NULL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  auto C = [](double2* x) { return reinterpret_cast<sigma_complex128*>(x); };
+  int r = ff_execute_weighted(p->ff, I_epsR, aqsntemp, aqsmtemp, vcoul, 1.0, C(p->cr), stream);
+  if (r != SIGMA_OK) return r;
+  r = ff_execute_weighted(p->ff, I_epsA, aqsntemp, aqsmtemp, vcoul, 1.0, C(p->ca), stream);
+  if (r != SIGMA_OK) return r;
+  const double2* sd = reinterpret_cast<const double2*>(schDt_matrix);
+  if (!schDt_matrix) {
+    r = ff_execute_weighted(p->ff, I_epsR, aqsntemp, aqsmtemp, nullptr, 1.0, C(p->sd), stream);
+    if (r != SIGMA_OK) return r;
+    sd = p->sd;
+  }
+  FfSigmaArgs g;
+  g.nb = p->nb;
+  g.nvband = p->nvband;
+  g.nf = p->nf;
+  g.ne = p->ne;
+  g.ekq = ekq;
+  g.grid = dFreqGrid;
+  g.brd = reinterpret_cast<const double2*>(dFreqBrd);
+  g.pref = pref;
+  g.pref_zb = pref_zb;
+  g.fmin = freqevalmin;
+  g.fstep = freqevalstep;
+  g.occ = occ;
+  g.cr = p->cr;
+  g.ca = p->ca;
+  g.sdt = sd;
+  g.per = p->per;
+  const int threads = 256, items = p->nb * p->ne;
+  ff_sigma_band_kernel<<<(items + threads - 1) / threads, threads, 0, s>>>(g);
+  SIGMA_CUDA_TRY(cudaGetLastError());
+  const int warps = 1 + kOut * p->ne;
+  ff_sigma_sum_kernel<<<(warps * 32 + threads - 1) / threads, threads, 0, s>>>(
+      p->nb, p->nf, p->ne, p->cr, p->per, reinterpret_cast<double2*>(out));
+  SIGMA_CUDA_TRY(cudaGetLastError());
+  return SIGMA_OK;
+}
+
 extern "C" int sigma_ff_sigma(int number_bands, int nvband, int ncouls, int ngpown, int nfreq,
                               int nfreqeval, const int* inv_igp_index, const int* indinv,
                               const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
@@ -192,25 +336,13 @@ extern "C" int sigma_ff_sigma(int number_bands, int nvband, int ncouls, int ngpo
       !dFreqGrid || !dFreqBrd || !pref || !achsDtemp || !asxDtemp || !achDtemp || !achDtemp_cor ||
       !achDtemp_corb || !ach2Dtemp)
     return SIGMA_ERR_NULL;
-  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0 || ngpown > ncouls || nfreq < 2 ||
-      nfreqeval <= 0 || nvband < 0 || nvband > number_bands)
-    return SIGMA_ERR_INVALID_SHAPE;
-  if (mode != SIGMA_FF_FP64 && mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
-  for (int f = 0; f + 1 < nfreq; ++f)
-    if (!(dFreqGrid[f + 1] > dFreqGrid[f])) return SIGMA_ERR_INVALID_SHAPE;  // ascending grid
-  // column map of the Fortran loop: igp = indinv[inv_igp_index[my_igp]];
-  // columns with igp outside [0, ncouls) are left out (:324-327)
-  std::vector<int> igp_of(ngpown);
-  for (int g = 0; g < ngpown; ++g) {
-    const int ind = inv_igp_index[g];
-    if (ind < 0 || ind >= ncouls) return SIGMA_ERR_INDEX_RANGE;
-    const int igp = indinv[ind];
-    igp_of[g] = (igp < 0 || igp >= ncouls) ? -1 : igp;
-  }
-
+  if (nfreq >= 2)
+    for (int f = 0; f + 1 < nfreq; ++f)
+      if (!(dFreqGrid[f + 1] > dFreqGrid[f])) return SIGMA_ERR_INVALID_SHAPE;  // ascending grid
   std::lock_guard<std::mutex> lk(api_mutex());
-  sigma_ff_plan plan = nullptr;
-  int st = ff_plan_build(&plan, number_bands, ncouls, ngpown, nfreq, igp_of, mode);
+  sigma_ff_sigma_plan plan = nullptr;
+  int st = sigma_ff_sigma_plan_create(&plan, number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval,
+                                      inv_igp_index, indinv, mode);
   if (st != SIGMA_OK) return st;
   const int nb = number_bands, nf = nfreq, ne = nfreqeval;
   const size_t eps_b = sizeof(sigma_complex128) * (size_t)nf * ngpown * ncouls;
@@ -225,13 +357,12 @@ extern "C" int sigma_ff_sigma(int number_bands, int nvband, int ncouls, int ngpo
   const size_t o_r = take(eps_b), o_a = take(eps_b), o_n = take(band_b), o_m = take(band_b),
                o_v = take(sizeof(double) * ncouls), o_ekq = take(sizeof(double) * nb),
                o_grid = take(sizeof(double) * nf), o_brd = take(sizeof(double2) * nf),
-               o_pref = take(sizeof(double) * nf), o_cr = take(mat_b), o_ca = take(mat_b),
-               o_sd = take(mat_b), o_per = take(sizeof(double2) * (size_t)nb * kOut * ne),
+               o_pref = take(sizeof(double) * nf), o_sd = take(mat_b),
                o_out = take(sizeof(double2) * (1 + kOut * ne));
   void* arena = nullptr;
   st = arena_get(kArenaFfInputs, off, &arena);
   if (st != SIGMA_OK) {
-    sigma_ff_plan_destroy(plan);
+    sigma_ff_sigma_plan_destroy(plan);
     return st;
   }
   char* a = static_cast<char*>(arena);
@@ -248,47 +379,21 @@ extern "C" int sigma_ff_sigma(int number_bands, int nvband, int ncouls, int ngpo
     SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_grid, dFreqGrid, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
     SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_brd, dFreqBrd, sizeof(double2) * nf, cudaMemcpyHostToDevice, s));
     SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_pref, pref, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
-    const double* dv = reinterpret_cast<const double*>(a + o_v);
-    int r = ff_execute_weighted(plan, D(o_r), D(o_n), D(o_m), dv, 1.0, D(o_cr), stream);
-    if (r != SIGMA_OK) return r;
-    r = ff_execute_weighted(plan, D(o_a), D(o_n), D(o_m), dv, 1.0, D(o_ca), stream);
-    if (r != SIGMA_OK) return r;
-    if (schDt_matrix) {
+    if (schDt_matrix)
       SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_sd, schDt_matrix, mat_b, cudaMemcpyHostToDevice, s));
-    } else {
-      r = ff_execute_weighted(plan, D(o_r), D(o_n), D(o_m), nullptr, 1.0, D(o_sd), stream);
-      if (r != SIGMA_OK) return r;
-    }
-    FfSigmaArgs g;
-    g.nb = nb;
-    g.nvband = nvband;
-    g.nf = nf;
-    g.ne = ne;
-    g.ekq = reinterpret_cast<const double*>(a + o_ekq);
-    g.grid = reinterpret_cast<const double*>(a + o_grid);
-    g.brd = reinterpret_cast<const double2*>(a + o_brd);
-    g.pref = reinterpret_cast<const double*>(a + o_pref);
-    g.pref_zb = pref_zb;
-    g.fmin = freqevalmin;
-    g.fstep = freqevalstep;
-    g.occ = occ;
-    g.cr = reinterpret_cast<const double2*>(a + o_cr);
-    g.ca = reinterpret_cast<const double2*>(a + o_ca);
-    g.sdt = reinterpret_cast<const double2*>(a + o_sd);
-    g.per = reinterpret_cast<double2*>(a + o_per);
-    const int threads = 256, items = nb * ne;
-    ff_sigma_band_kernel<<<(items + threads - 1) / threads, threads, 0, s>>>(g);
-    SIGMA_CUDA_TRY(cudaGetLastError());
-    const int warps = 1 + kOut * ne;
-    ff_sigma_sum_kernel<<<(warps * 32 + threads - 1) / threads, threads, 0, s>>>(
-        nb, nf, ne, g.cr, g.per, reinterpret_cast<double2*>(a + o_out));
-    SIGMA_CUDA_TRY(cudaGetLastError());
+    int r = sigma_ff_sigma_execute(plan, D(o_m), D(o_n), D(o_r), D(o_a),
+                                   reinterpret_cast<const double*>(a + o_v),
+                                   reinterpret_cast<const double*>(a + o_ekq),
+                                   reinterpret_cast<const double*>(a + o_grid), D(o_brd),
+                                   reinterpret_cast<const double*>(a + o_pref), pref_zb, freqevalmin,
+                                   freqevalstep, occ, schDt_matrix ? D(o_sd) : nullptr, D(o_out), stream);
+    if (r != SIGMA_OK) return r;
     SIGMA_CUDA_TRY(cudaMemcpyAsync(out.data(), a + o_out, sizeof(double2) * out.size(),
                                    cudaMemcpyDeviceToHost, s));
-    return sigma_ff_plan_status(plan, stream);
+    return sigma_ff_sigma_plan_status(plan, stream);
   };
   const int rc = run();
-  sigma_ff_plan_destroy(plan);
+  sigma_ff_sigma_plan_destroy(plan);
   if (rc != SIGMA_OK) return rc;
   auto put = [](sigma_complex128* dst, double2 v) {
     dst->re = v.x;

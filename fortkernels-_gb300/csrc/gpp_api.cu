@@ -1,5 +1,6 @@
 // C ABI of the GPP path: plans, device-resident execution and the
 // host-pointer drop-in for BGW-Kernels/gppKer.cpp:303-439.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -18,8 +19,9 @@ struct sigma_gpp_plan_s {
   int device = 0;
   int nb = 0, nvband = 0, nc = 0, ng = 0, precision = 0;
   int valid_columns = 0;
-  int sch_grid = 0, ssx_grid = 0;
+  int sch_grid = 0, ssx_grid = 0, schy_grid = 0;
   sigma::GppWork sch{}, ssx{};
+  sigma::GppWork schy{};      // FP64 main pass for shared frequencies (shares sch's buffers)
   sigma::MixedPrep prep{};    // FP32 operands of the mixed path (unused for FP64)
   void* block = nullptr;      // one device allocation for everything below
   int* igp_of = nullptr;      // [ng]
@@ -102,6 +104,7 @@ namespace {
 
 constexpr int kItemsPerSlot = 48;       // work items per resident CTA (load balance of the tail)
 constexpr int kItemsPerSlotMixed = 12;  // mixed items are 64x cheaper: fewer, longer items
+constexpr int kItemsPerSlotY = 24;      // shared-frequency FP64 items (64 x 32 tiles, 1 CTA per SM)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -148,11 +151,17 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   gpp_size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
   if (p->sch.n_items < p->sch_grid) p->sch_grid = p->sch.n_items;
   if (p->ssx.n_items < p->ssx_grid) p->ssx_grid = p->ssx.n_items;
+  if (!mixed) {
+    p->schy_grid = sms * sch_blocks_per_sm_fp64y();
+    gpp_size_work(p->schy, 0, number_bands, kBNY, kBPY, ncouls, ngpown, p->schy_grid, kItemsPerSlotY);
+    if (p->schy.n_items < p->schy_grid) p->schy_grid = p->schy.n_items;
+  }
 
   const size_t b_igp = align_up(sizeof(int) * ngpown, 256);
   const size_t b_cnt = 256;
   const size_t b_n1 = align_up(sizeof(double2) * (size_t)(number_bands + nvband) * kNW, 256);
-  const size_t b_sch = align_up(sizeof(double2) * (size_t)p->sch.n_items * kBN * kNW, 256);
+  const size_t b_sch = align_up(sizeof(double2) * std::max((size_t)p->sch.n_items * kBN,
+                                                           (size_t)p->schy.n_items * kBNY) * kNW, 256);
   const size_t b_ssx = align_up(sizeof(double2) * (size_t)p->ssx.n_items * kSsxBN * kNW, 256);
   const int nc_pad = (ncouls + kCK - 1) / kCK * kCK;
   const size_t col_elems = mixed ? (size_t)p->sch.n_col_blocks * kBPM * nc_pad : 0;
@@ -177,6 +186,8 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   p->ssx.partial = reinterpret_cast<double2*>(base + b_igp + b_cnt + b_n1 + b_sch);
   p->sch.counter = p->counters;
   p->ssx.counter = p->counters + 1;
+  p->schy.partial = p->sch.partial;
+  p->schy.counter = p->counters;
   {
     char* q = base + b_igp + b_cnt + b_n1 + b_sch + b_ssx;
     p->prep.colA = mixed ? reinterpret_cast<float4*>(q) : nullptr;
@@ -307,8 +318,13 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
   const bool mixed = plan->precision == SIGMA_PREC_MIXED;
   if (mixed && plan->sch.n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->sch, plan->prep, s));
+  // FP64 with one frequency set for every band: the shared-factor kernel
+  const bool ypath = !mixed && wx_band_stride == 0 && plan->schy.n_items > 0;
+  const GppWork& main = ypath ? plan->schy : plan->sch;
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
-  if (plan->sch.n_items > 0)
+  if (ypath)
+    SIGMA_CUDA_TRY(launch_sch_fp64y(p, plan->schy, plan->schy_grid, s));
+  else if (plan->sch.n_items > 0)
     SIGMA_CUDA_TRY(mixed ? launch_sch_mixed(p, plan->sch, plan->prep, plan->sch_grid, s)
                          : launch_sch_fp64(p, plan->sch, plan->sch_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
@@ -316,7 +332,7 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
     SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed(p, plan->ssx, plan->prep, plan->ssx_grid, s)
                          : launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[2], s));
-  SIGMA_CUDA_TRY(launch_gpp_reduce(plan->sch, plan->ssx, plan->nb, plan->acht_n1,
+  SIGMA_CUDA_TRY(launch_gpp_reduce(main, plan->ssx, plan->nb, plan->acht_n1,
                                    reinterpret_cast<double2*>(achtemp),
                                    reinterpret_cast<double2*>(asxtemp),
                                    reinterpret_cast<double2*>(acht_n1_loc), s));

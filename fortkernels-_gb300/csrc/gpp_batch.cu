@@ -44,12 +44,13 @@ namespace {
 constexpr int kBatchItemsPerSlot = 16;
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 
-// Least padded work among the FP64 tile shapes (bands and columns padded up
-// to the tile), ties to the square tile.
-int least_padding_tile(int nb, int ng) {
-  int best = kTile32x32;
+// Least padded work among the FP64 tile shapes of one kernel family (bands
+// and columns padded up to the tile), ties to the family's first tile.
+int least_padding_tile(int nb, int ng, bool shared) {
+  const int t0 = shared ? kTileY64x32 : kTile32x32, t1 = shared ? kTileCount : kTileY64x32;
+  int best = t0;
   double best_cost = 1e300;
-  for (int t = 0; t < kTileCount; ++t) {
+  for (int t = t0; t < t1; ++t) {
     const double cost = (double)((nb + tile_bn(t) - 1) / tile_bn(t) * tile_bn(t)) *
                         (double)((ng + tile_bp(t) - 1) / tile_bp(t) * tile_bp(t));
     if (cost < best_cost - 0.5) {
@@ -86,6 +87,8 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   if (n_instances <= 0) return SIGMA_ERR_INVALID_SHAPE;
   if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED) return SIGMA_ERR_UNSUPPORTED;
   const bool mixed = precision == SIGMA_PREC_MIXED;
+  bool all_shared = true;
+  for (int i = 0; i < n_instances; ++i) all_shared = all_shared && inst[i].wx_band_stride == 0;
   std::vector<std::vector<int>> igp(n_instances);
   long long terms = 0;
   for (int i = 0; i < n_instances; ++i) {
@@ -96,7 +99,9 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
     int st = gpp_check_shape(q.number_bands, q.nvband, q.ncouls, q.ngpown, 0, kNW);
     if (st != SIGMA_OK) return st;
     if (q.wx_band_stride != 0 && q.wx_band_stride < kNW) return SIGMA_ERR_INVALID_SHAPE;
-    if (tile_shape && (tile_shape[i] < -1 || tile_shape[i] >= kTileCount)) return SIGMA_ERR_UNSUPPORTED;
+    if (tile_shape && tile_shape[i] != -1 &&
+        (tile_shape[i] < 0 || tile_shape[i] >= kTileCount || tile_shared(tile_shape[i]) != all_shared))
+      return SIGMA_ERR_UNSUPPORTED;
     int valid = 0;
     st = gpp_map_columns(q.ncouls, q.ngpown, q.inv_igp_index, q.indinv, q.ncouls, igp[i], valid);
     if (st != SIGMA_OK) return st;
@@ -117,7 +122,8 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   b->terms = terms;
   b->inst.assign(inst, inst + n_instances);
   for (int i = 0; i < n_instances; ++i) b->all_shared_wx = b->all_shared_wx && inst[i].wx_band_stride == 0;
-  b->sch_grid = sms * (mixed ? sch_batch_blocks_per_sm_mixed() : sch_batch_blocks_per_sm_fp64());
+  b->sch_grid = sms * (mixed ? sch_batch_blocks_per_sm_mixed()
+                             : (all_shared ? sch_batch_blocks_per_sm_fp64y() : sch_batch_blocks_per_sm_fp64()));
   b->ssx_grid = sms * (mixed ? ssx_batch_blocks_per_sm_mixed() : ssx_batch_blocks_per_sm_fp64());
   b->dev.resize(n_instances);
   b->sch.resize(n_instances);
@@ -142,8 +148,9 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   for (int i = 0; i < n_instances; ++i) {
     const sigma_gpp_instance& q = inst[i];
     const int t = mixed ? kTile32x32
-                        : (tile_shape && tile_shape[i] >= 0 ? tile_shape[i]
-                                                            : least_padding_tile(q.number_bands, q.ngpown));
+                        : (tile_shape && tile_shape[i] >= 0
+                               ? tile_shape[i]
+                               : least_padding_tile(q.number_bands, q.ngpown, all_shared));
     b->tile[i] = t;
     const int bn = mixed ? kBN : tile_bn(t), bp = mixed ? kBPM : tile_bp(t);
     size_instance(b->sch[i], q.number_bands, bn, bp, q.ncouls, q.ngpown, target);
@@ -282,7 +289,8 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
       if (b->sch[i].n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->sch[i], b->prep[i], s));
   if (b->sch_view.total > 0)
     SIGMA_CUDA_TRY(mixed ? launch_sch_mixed_batch(b->sch_view, b->sch_grid, s)
-                         : launch_sch_fp64_batch(b->sch_view, b->sch_grid, s));
+                         : (b->all_shared_wx ? launch_sch_fp64y_batch(b->sch_view, b->sch_grid, s)
+                                             : launch_sch_fp64_batch(b->sch_view, b->sch_grid, s)));
   if (b->ssx_view.total > 0)
     SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed_batch(b->ssx_view, b->ssx_grid, b->all_shared_wx, s)
                          : launch_ssx_fp64_batch(b->ssx_view, b->ssx_grid, s));

@@ -5,10 +5,20 @@
 
 namespace sigma {
 
-// Tile shapes of the FP64 main pass (bands x columns per item).
-enum GppTile { kTile32x32 = 0, kTile16x64 = 1, kTile64x16 = 2, kTileCount = 3 };
-__host__ __device__ constexpr int tile_bn(int t) { return t == kTile16x64 ? 16 : (t == kTile64x16 ? 64 : 32); }
-__host__ __device__ constexpr int tile_bp(int t) { return t == kTile16x64 ? 64 : (t == kTile64x16 ? 16 : 32); }
+// Tile shapes of the FP64 main pass (bands x columns per item).  Tiles 0-2
+// belong to the per-band-frequency kernel, tiles 3-5 to the shared-frequency
+// kernel (sch_fp64y_item); a batch runs one kernel for all its instances.
+enum GppTile {
+  kTile32x32 = 0, kTile16x64 = 1, kTile64x16 = 2,
+  kTileY64x32 = 3, kTileY32x64 = 4, kTileY32x32 = 5, kTileCount = 6
+};
+__host__ __device__ constexpr int tile_bn(int t) {
+  return (t == kTile16x64) ? 16 : ((t == kTile64x16 || t == kTileY64x32) ? 64 : 32);
+}
+__host__ __device__ constexpr int tile_bp(int t) {
+  return (t == kTile16x64 || t == kTileY32x64) ? 64 : (t == kTile64x16 ? 16 : 32);
+}
+__host__ __device__ constexpr bool tile_shared(int t) { return t >= kTileY64x32; }
 
 // One pass over every instance: items of instance i are the global items
 // [item_off[i], item_off[i+1]) of a single device counter.
@@ -37,7 +47,9 @@ cudaError_t launch_sch_fp64_batch(const GppBatchView& b, int grid, cudaStream_t 
 cudaError_t launch_ssx_fp64_batch(const GppBatchView& b, int grid, cudaStream_t s);
 cudaError_t launch_sch_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s);
 cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, bool all_shared_wx, cudaStream_t s);
+cudaError_t launch_sch_fp64y_batch(const GppBatchView& b, int grid, cudaStream_t s);
 int sch_batch_blocks_per_sm_fp64();
+int sch_batch_blocks_per_sm_fp64y();
 int ssx_batch_blocks_per_sm_fp64();
 int sch_batch_blocks_per_sm_mixed();
 int ssx_batch_blocks_per_sm_mixed();

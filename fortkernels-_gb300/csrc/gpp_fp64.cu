@@ -195,6 +195,190 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
   }
 }
 
+// ---------------------------------------------------------------- shared frequencies
+// When every band uses the same three frequencies (the mini-app's case,
+// BGW-Kernels/gppKer.cpp:310-314: e_n1kq is the same for every band), the
+// frequency factor of a term,
+//   Y_iw = G (c + i b) r   (0 when the pole guard drops the term),
+// depends on the column and the g-vector only.  Each staged chunk forms Y
+// once for its columns (10 FP64 operations per column, g-vector and
+// frequency, shared by the item's BN bands), and every term is then one
+// complex multiply-add acc += aqsn * Y: 4 DFMA, against 10 FP64 operations
+// per term when the factor is rebuilt for every band.  The sum over
+// g-vectors is then a complex GEMM (bands x g-vectors times g-vectors x
+// (column, frequency)) on the FP64 pipe, 16 x 16 threads with a
+// (BN/16 bands x BP/16 columns x 3 frequencies) register tile each.
+constexpr int kCKY = 16;  // g-vectors per staged chunk
+
+template <int BN, int BP>
+struct SchYSmem {
+  double2 y[kCKY][kNW][BP];
+  double2 n[kCKY][BN];
+};
+
+template <int BN, int BP>
+__device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w, int item,
+                                               unsigned char* smem_raw, int tid) {
+  constexpr int TB = BN / 16, TC = BP / 16;
+  SchYSmem<BN, BP>& sm = *reinterpret_cast<SchYSmem<BN, BP>*>(smem_raw);
+  const int tx = tid & 15, ty = tid >> 4;
+  const int band_end = w.band_begin + w.band_count;
+  const ItemCoord ic = decode_item(w, item);
+  const int n1_0 = w.band_begin + ic.bb * BN;
+  const int p0 = ic.cb * BP;
+  const int ig_begin = ic.s * w.split_len;
+  const int ig_end = min(ig_begin + w.split_len, p.nc);
+  const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
+
+  double2 acc[TB][TC][kNW];
+#pragma unroll
+  for (int i = 0; i < TB; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = make_double2(0.0, 0.0);
+
+  for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCKY) {
+    __syncthreads();
+    // frequency factors of the chunk's (g-vector, column) pairs; reads run
+    // along g-vectors
+    for (int e = tid; e < kCKY * BP; e += kThreads) {
+      const int k = e % kCKY, pl = e / kCKY;
+      const int ig = ig0 + k, my_igp = p0 + pl;
+      double2 y0 = make_double2(0.0, 0.0), y1 = y0, y2 = y0;
+      if (ig < ig_end && my_igp < p.ng) {
+        const size_t off = (size_t)my_igp * p.nc + ig;
+        const double2 wt = p.wt[off];
+        const double2 g = cmul(p.ieps[off], wt);
+        const double b = wt.y, b2 = guard_b2(b);
+        const double thr = guard_thr(wt.x, b2);
+        auto factor = [&](double wx) {
+          const double c = __dsub_rn(wx, wt.x);
+          const double wv = fma(c, c, b2);
+          const double r = gt_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
+          const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
+          return make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
+        };
+        y0 = factor(wx0);
+        y1 = factor(wx1);
+        y2 = factor(wx2);
+      }
+      sm.y[k][0][pl] = y0;
+      sm.y[k][1][pl] = y1;
+      sm.y[k][2][pl] = y2;
+    }
+    for (int e = tid; e < kCKY * BN; e += kThreads) {
+      const int k = e % kCKY, bl = e / kCKY;
+      const int ig = ig0 + k, n1 = n1_0 + bl;
+      double2 v = make_double2(0.0, 0.0);
+      if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
+      sm.n[k][bl] = v;
+    }
+    __syncthreads();
+
+#pragma unroll 2
+    for (int k = 0; k < kCKY; ++k) {
+      double2 nn[TB], y[TC][kNW];
+#pragma unroll
+      for (int i = 0; i < TB; ++i) nn[i] = sm.n[k][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < TC; ++j)
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) y[j][iw] = sm.y[k][iw][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < TB; ++i)
+#pragma unroll
+        for (int j = 0; j < TC; ++j)
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            double2& a = acc[i][j][iw];
+            a.x = fma(nn[i].x, y[j][iw].x, a.x);
+            a.x = fma(-nn[i].y, y[j][iw].y, a.x);
+            a.y = fma(nn[i].x, y[j][iw].y, a.y);
+            a.y = fma(nn[i].y, y[j][iw].x, a.y);
+          }
+    }
+  }
+
+  // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp]; the 16 lanes of a
+  // half-warp hold the item's columns for the same bands and sum them with
+  // a fixed butterfly
+#pragma unroll
+  for (int i = 0; i < TB; ++i) {
+    const int bl = ty + 16 * i, n1 = n1_0 + bl;
+    double2 part[kNW];
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) part[iw] = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int j = 0; j < TC; ++j) {
+      const int my_igp = p0 + tx + 16 * j;
+      const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
+      if (n1 < band_end && igp >= 0) {
+        const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+        const double2 m = make_double2(am.x, -am.y);
+        const double f = 0.5 * p.vcoul[igp];
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          const double2 v = cmul(acc[i][j][iw], m);
+          part[iw].x = fma(v.x, f, part[iw].x);
+          part[iw].y = fma(v.y, f, part[iw].y);
+        }
+      }
+    }
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw)
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) {
+        part[iw].x += __shfl_xor_sync(0xffffffffu, part[iw].x, o);
+        part[iw].y += __shfl_xor_sync(0xffffffffu, part[iw].y, o);
+      }
+    if (tx == 0) {
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) w.partial[ic.pidx * BN * kNW + bl * kNW + iw] = part[iw];
+    }
+  }
+}
+
+template <int BN, int BP>
+__global__ void __launch_bounds__(kThreads, 1) sch_fp64y_kernel(GppDev p, GppWork w) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(w.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= w.n_items) break;
+    sch_fp64y_item<BN, BP>(p, w, item, smem_raw, tid);
+  }
+}
+
+constexpr size_t kSchYBatchSmem =
+    sizeof(SchYSmem<64, 32>) > sizeof(SchYSmem<32, 64>) ? sizeof(SchYSmem<64, 32>) : sizeof(SchYSmem<32, 64>);
+
+__global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchView b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(b.counter, 1);
+    __syncthreads();
+    const int g = s_item;
+    if (g >= b.total) break;
+    const int inst = batch_owner(b.item_off, b.n_inst, g);
+    const GppDev p = b.dev[inst];
+    const GppWork w = b.work[inst];
+    const int local = g - b.item_off[inst];
+    switch (b.tile[inst]) {
+      case kTileY32x64: sch_fp64y_item<32, 64>(p, w, local, smem_raw, tid); break;
+      case kTileY32x32: sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid); break;
+      default: sch_fp64y_item<64, 32>(p, w, local, smem_raw, tid); break;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- occupied bands
 // Screened exchange of the occupied bands (ssxt_scht_solver branches,
 // BGW-Kernels/gppKer.cpp:38-58):
@@ -402,8 +586,29 @@ int blocks_per_sm(K kernel, size_t smem) {
 }  // namespace
 
 int sch_blocks_per_sm_fp64() { return blocks_per_sm(sch_fp64_kernel<kBN, kBP>, sizeof(SchSmem<kBN, kBP>)); }
+int sch_blocks_per_sm_fp64y() {
+  return blocks_per_sm(sch_fp64y_kernel<kBNY, kBPY>, sizeof(SchYSmem<kBNY, kBPY>));
+}
+
+cudaError_t launch_sch_fp64y(const GppDev& p, const GppWork& w, int grid, cudaStream_t s) {
+  constexpr size_t smem = sizeof(SchYSmem<kBNY, kBPY>);
+  cudaError_t e = cudaFuncSetAttribute(sch_fp64y_kernel<kBNY, kBPY>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  sch_fp64y_kernel<kBNY, kBPY><<<grid, kThreads, smem, s>>>(p, w);
+  return cudaGetLastError();
+}
 int ssx_blocks_per_sm_fp64() { return blocks_per_sm(ssx_fp64_kernel, sizeof(SsxSmem)); }
 int sch_batch_blocks_per_sm_fp64() { return blocks_per_sm(sch_fp64_batch_kernel, kSchBatchSmem); }
+int sch_batch_blocks_per_sm_fp64y() { return blocks_per_sm(sch_fp64y_batch_kernel, kSchYBatchSmem); }
+
+cudaError_t launch_sch_fp64y_batch(const GppBatchView& b, int grid, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(sch_fp64y_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kSchYBatchSmem);
+  if (e != cudaSuccess) return e;
+  sch_fp64y_batch_kernel<<<grid, kThreads, kSchYBatchSmem, s>>>(b);
+  return cudaGetLastError();
+}
 int ssx_batch_blocks_per_sm_fp64() { return blocks_per_sm(ssx_fp64_batch_kernel, sizeof(SsxSmem)); }
 
 cudaError_t launch_sch_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s) {

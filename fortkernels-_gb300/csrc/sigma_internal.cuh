@@ -68,6 +68,8 @@ constexpr int kBP = 32;    // columns (my_igp) per FP64 sch tile
 constexpr int kBPM = 16;   // columns per mixed sch tile
 constexpr int kCK = 32;    // g-vectors per staged chunk
 constexpr int kThreads = 256;
+constexpr int kBNY = 64;   // bands per FP64 item when the frequencies are shared
+constexpr int kBPY = 32;   // columns per FP64 item when the frequencies are shared
 constexpr int kSsxBN = 4;   // bands per occupied-band item
 constexpr int kSsxBP = 256; // columns per occupied-band item, one per thread
 
@@ -120,6 +122,10 @@ int gpp_check_shape(int nb, int nvband, int nc, int ng, int nstart, int nend);
 // ---------------------------------------------------------------- launchers
 cudaError_t launch_sch_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
 cudaError_t launch_ssx_fp64(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+// FP64 main pass for one frequency set shared by every band (wx_stride 0):
+// items of kBNY bands x kBPY columns.
+cudaError_t launch_sch_fp64y(const GppDev& p, const GppWork& w, int grid, cudaStream_t s);
+int sch_blocks_per_sm_fp64y();
 cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
                              cudaStream_t s);
 cudaError_t launch_prep_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, cudaStream_t s);

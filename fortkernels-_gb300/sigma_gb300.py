@@ -72,6 +72,12 @@ SIGNATURES = {
     "sigma_gpp_static_execute": ([_P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_ff_plan_bands": ([_P, _P], _I),
     "sigma_ff_sigma": ([_I] * 6 + [_P] * 11 + [_D] * 4 + [_P] * 7 + [_I, _P], _I),
+    "sigma_ff_sigma_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I], _I),
+    "sigma_ff_sigma_execute": ([_P] * 10 + [_D] * 4 + [_P, _P, _P], _I),
+    "sigma_ff_sigma_plan_set_timing": ([_P, _I], _I),
+    "sigma_ff_sigma_plan_timing": ([_P, _P, _P, _P], _I),
+    "sigma_ff_sigma_plan_status": ([_P, _P], _I),
+    "sigma_ff_sigma_plan_destroy": ([_P], _I),
     "sigma_ff_schdt": ([_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "sigma_ff_plan_create": ([_P, _I, _I, _I, _I, _P, _P, _I], _I),
     "sigma_ff_execute": ([_P, _P, _P, _P, _P, _P], _I),
@@ -393,6 +399,63 @@ def ff_sigma(prob, mode: int = FF_MODE_FP64, schdt="zero", stream: int = 0):
     _check(st, "sigma_ff_sigma")
     out["achsDtemp"] = out["achsDtemp"][0]
     return out
+
+
+class FfSigmaPlan:
+    """Device-resident full-frequency sigma (sigma_ff_sigma_plan_create /
+    sigma_ff_sigma_execute).  execute() takes device arrays (CUDA tensors or
+    pointers) and a device output of 1 + 5 * nfreqeval complex values."""
+
+    def __init__(self, number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval, inv_igp_index, indinv,
+                 mode=FF_MODE_FP64):
+        self.lib = load()
+        self.inv = np.ascontiguousarray(inv_igp_index, dtype=np.int32)
+        self.indinv = np.ascontiguousarray(indinv, dtype=np.int32)
+        self.nfreqeval = nfreqeval
+        h = C.c_void_p()
+        _check(self.lib.sigma_ff_sigma_plan_create(C.byref(h), number_bands, nvband, ncouls, ngpown, nfreq,
+                                                   nfreqeval, _ptr(self.inv), _ptr(self.indinv), mode),
+               "sigma_ff_sigma_plan_create")
+        self.handle = h
+
+    def execute(self, aqsm, aqsn, epsr, epsa, vcoul, ekq, grid, brd, pref, pref_zb, freqevalmin,
+                freqevalstep, occ, schdt, out, stream=0):
+        _check(self.lib.sigma_ff_sigma_execute(self.handle, *[_dptr(a) for a in (aqsm, aqsn, epsr, epsa, vcoul,
+                                                                               ekq, grid, brd, pref)],
+                                               pref_zb, freqevalmin, freqevalstep, occ, _dptr(schdt),
+                                               _dptr(out), stream), "sigma_ff_sigma_execute")
+
+    @staticmethod
+    def unpack(out_host, nfreqeval):
+        """Splits the output vector into the six named results."""
+        z = np.asarray(out_host).view(np.complex128)
+        res = {"achsDtemp": z[0]}
+        for k, name in enumerate(FF_SIGMA_OUTPUTS[1:]):
+            res[name] = z[1 + k * nfreqeval: 1 + (k + 1) * nfreqeval].copy()
+        return res
+
+    def set_timing(self, enable=True):
+        _check(self.lib.sigma_ff_sigma_plan_set_timing(self.handle, int(enable)), "sigma_ff_sigma_plan_set_timing")
+
+    def timing(self):
+        n, a, o = C.c_int(), C.c_double(), C.c_double()
+        _check(self.lib.sigma_ff_sigma_plan_timing(self.handle, C.byref(n), C.byref(a), C.byref(o)),
+               "sigma_ff_sigma_plan_timing")
+        return dict(contractions=n.value, contraction_ms=a.value, other_ms=o.value)
+
+    def status(self, stream=0):
+        return self.lib.sigma_ff_sigma_plan_status(self.handle, stream)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sigma_ff_sigma_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ff_host(prob, mode: int = FF_MODE_FP64, stream: int = 0):

@@ -107,6 +107,30 @@ int sigma_ff_sigma(int number_bands, int nvband, int ncouls, int ngpown, int nfr
                    sigma_complex128* achDtemp_cor, sigma_complex128* achDtemp_corb,
                    sigma_complex128* ach2Dtemp, int mode, void* stream);
 
+/* Device-resident form: a plan (column map validated on the host, the FF
+ * contraction plan and the per-band workspace) and an asynchronous
+ * execution on device arrays.  dFreqGrid must be ascending (the host
+ * drop-in checks it).  out is device complex[1 + 5 * nfreqeval]:
+ * achsDtemp, then asxDtemp, achDtemp, achDtemp_cor, achDtemp_corb,
+ * ach2Dtemp, nfreqeval values each.  Timing counts the contraction kernels
+ * (two or three per execution) and everything else. */
+typedef struct sigma_ff_sigma_plan_s* sigma_ff_sigma_plan;
+int sigma_ff_sigma_plan_create(sigma_ff_sigma_plan* plan, int number_bands, int nvband, int ncouls,
+                               int ngpown, int nfreq, int nfreqeval, const int* inv_igp_index,
+                               const int* indinv, int mode);
+int sigma_ff_sigma_execute(sigma_ff_sigma_plan plan, const sigma_complex128* aqsmtemp,
+                           const sigma_complex128* aqsntemp, const sigma_complex128* I_epsR,
+                           const sigma_complex128* I_epsA, const double* vcoul, const double* ekq,
+                           const double* dFreqGrid, const sigma_complex128* dFreqBrd,
+                           const double* pref, double pref_zb, double freqevalmin,
+                           double freqevalstep, double occ, const sigma_complex128* schDt_matrix,
+                           sigma_complex128* out, void* stream);
+int sigma_ff_sigma_plan_set_timing(sigma_ff_sigma_plan plan, int enable);
+int sigma_ff_sigma_plan_timing(sigma_ff_sigma_plan plan, int* contractions, double* contraction_ms,
+                               double* other_ms);
+int sigma_ff_sigma_plan_status(sigma_ff_sigma_plan plan, void* stream);
+int sigma_ff_sigma_plan_destroy(sigma_ff_sigma_plan plan);
+
 #ifdef __cplusplus
 }
 #endif

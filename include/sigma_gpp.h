@@ -142,10 +142,14 @@ typedef struct sigma_gpp_instance {
 typedef struct sigma_gpp_batch_s* sigma_gpp_batch;
 
 /* Validates every instance like sigma_gpp_plan_create and sizes the queues.
- * tile_shape (may be NULL) picks the FP64 main-pass tile per instance:
- * -1 the library's choice (least padding), 0 = 32 bands x 32 columns,
- * 1 = 16 x 64, 2 = 64 x 16 (the tuning table of fortkernels-_gb300/autotune.py
- * chooses per shape class).  The mixed form has one tile shape. */
+ * tile_shape (may be NULL) picks the FP64 main-pass tile per instance, -1
+ * for the library's choice (least padding).  A batch whose instances all
+ * share one frequency set per instance (wx_band_stride 0) runs the
+ * shared-frequency kernel: tiles 3 = 64 bands x 32 columns, 4 = 32 x 64,
+ * 5 = 32 x 32; otherwise the per-band kernel: 0 = 32 x 32, 1 = 16 x 64,
+ * 2 = 64 x 16.  A tile of the other family is SIGMA_ERR_UNSUPPORTED.  The
+ * tuning table of fortkernels-_gb300/autotune.py chooses per shape class.
+ * The mixed form has one tile shape. */
 int sigma_gpp_batch_create(sigma_gpp_batch* batch, int n_instances, const sigma_gpp_instance* inst,
                            int precision, const int* tile_shape);
 

@@ -100,3 +100,26 @@ def test_ff_sigma_argument_errors(sigma_lib):
     with pytest.raises(sigma_lib.SigmaError) as e:
         sigma_lib.ff_sigma(q, 0)
     assert e.value.status == -1
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["fp64", "ozaki"])
+def test_ff_sigma_plan_matches_host_dropin(sigma_lib, mode):
+    import torch
+    p = _prob(CASES[1])
+    g = sigma_lib.ff_sigma(p, mode, schdt="compute")
+    dc = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex128).view(np.float64).copy()).cuda()
+    df = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64).copy()).cuda()
+    plan = sigma_lib.FfSigmaPlan(p.number_bands, p.nvband, p.ncouls, p.ngpown, p.nfreq, p.nfreqeval,
+                                 p.inv_igp_index, p.indinv, mode)
+    out = torch.zeros(2 * (1 + 5 * p.nfreqeval), dtype=torch.float64, device="cuda")
+    args = [dc(p.aqsmtemp), dc(p.aqsntemp), dc(p.I_epsR), dc(p.I_epsA), df(p.vcoul), df(p.ekq),
+            df(p.dFreqGrid), dc(p.dFreqBrd), df(p.pref)]
+    for _ in range(2):
+        plan.execute(*args, p.pref_zb, p.freqevalmin, p.freqevalstep, p.occ, None, out)
+        torch.cuda.synchronize()
+        assert plan.status() == 0
+        r = sigma_lib.FfSigmaPlan.unpack(out.cpu().numpy(), p.nfreqeval)
+        assert r["achsDtemp"] == g["achsDtemp"]
+        for k in KEYS:
+            assert np.array_equal(r[k], g[k])
+    plan.close()

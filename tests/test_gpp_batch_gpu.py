@@ -141,6 +141,23 @@ def test_batch_every_tile_shape_matches_oracle(sigma_lib, small_set, tile):
         _check(x.outputs(), o, 0)
 
 
+@pytest.mark.parametrize("tile", [3, 4, 5], ids=["y64x32", "y32x64", "y32x32"])
+def test_batch_shared_frequency_tiles_match_oracle(sigma_lib, small_set, tile):
+    """Instances that all share one frequency set run the shared-factor
+    kernel (tiles 3-5)."""
+    xs, oracles, _ = small_set
+    keep = [k for k, x in enumerate(xs) if x.wx_stride == 0]
+    b = sigma_lib.GppBatch([xs[k].as_dict() for k in keep], precision=0, tiles=[tile] * len(keep))
+    b.execute()
+    assert b.status() == 0
+    b.close()
+    for k in keep:
+        _check(xs[k].outputs(), oracles[k], 0)
+    with pytest.raises(sigma_lib.SigmaError) as e:
+        sigma_lib.GppBatch([xs[k].as_dict() for k in keep], precision=0, tiles=[0] * len(keep))
+    assert e.value.status == -8
+
+
 def test_batch_mixed_tiles_in_one_queue(sigma_lib, small_set):
     xs, oracles, _ = small_set
     tiles = [k % 3 for k in range(len(xs))]

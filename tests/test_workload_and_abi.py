@@ -172,7 +172,9 @@ def test_batch_validation_precedes_device_work(libpath):
     assert create([good], prec=2) == -8
     assert create([good, good], tiles=[0, 5]) == -8
     assert create([dict(good, wx_band_stride=2)]) == -1
-    st = create([good, good], tiles=[1, -1])
+    assert create([good, good], tiles=[1, -1]) == -8   # per-band-kernel tile, shared frequencies
+    assert create([good, dict(good, wx_band_stride=3)], tiles=[4, 0]) == -8  # mixed families
+    st = create([good, good], tiles=[4, -1])
     assert st in (0, -7, -4)
     if st == 0:
         lib.sigma_gpp_batch_destroy.argtypes = [C.c_void_p]
@@ -184,12 +186,18 @@ def test_tile_table_covers_every_shape_class():
     t = A.load_table()
     assert t is not None and t["device"].startswith("NVIDIA")
     keys = {A.shape_class(nb, ng) for nb in range(1, 200) for ng in range(1, 200)}
-    assert keys == set(t["classes"]) and len(keys) == 16
-    assert all(v in (0, 1, 2) for v in t["classes"].values())
-    # the tuned tile of a class is the fastest one it timed
-    for k, v in t["classes"].items():
-        ms = t["timings"][k]["ms"]
-        assert A.TILES[v] == min(ms, key=ms.get)
+    assert len(keys) == 16
+    for family, key in A.TABLE_KEY.items():
+        if key not in t:
+            continue
+        assert keys == set(t[key])
+        assert all(v in A.FAMILIES[family] for v in t[key].values())
+        timings = t["timings" if family == "shared" else "timings_per_band"]
+        # the tuned tile of a class is the fastest one it timed
+        for k, v in t[key].items():
+            ms = timings[k]["ms"]
+            assert A.TILES[v] == min(ms, key=ms.get)
     assert A.shape_class(16, 16) == "b0c0" and A.shape_class(17, 64) == "b1c3"
     for s in W.batched_shapes():
-        assert A.tile_for(s["number_bands"], s["ngpown"]) in (0, 1, 2)
+        assert A.tile_for(s["number_bands"], s["ngpown"]) in (-1, 3, 4, 5)
+        assert A.tile_for(s["number_bands"], s["ngpown"], shared=False) in (-1, 0, 1, 2)
