@@ -545,6 +545,20 @@ def run_ours(args, rank, world, local_rank):
                  "acht_n1_loc_normwise": float(np.linalg.norm(mixed_out[2] - fp64_out[2]) /
                                                np.linalg.norm(fp64_out[2]))}
     mixed_main_s = mkt["main_ms"] / max(1, mkt["executions"]) * 1e-3
+
+    # ---- tensor-core form on the same inputs
+    tplan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_TENSOR)
+    for _ in range(args.warmup):
+        inst.run(tplan, sptr)
+    tplan.set_timing(True)
+    tsteps = max(args.steps, 10)
+    ms_tensor = timed(torch, dist, world, lambda: inst.run(tplan, sptr), tsteps, stream)
+    tkt = tplan.timing()
+    tensor_out = inst.outputs()
+    tensor_value = terms * world / (ms_tensor / tsteps * 1e-3) / 1e9
+    tensor_err = {"achtemp": rel(tensor_out[0], fp64_out[0]), "asxtemp": rel(tensor_out[1], fp64_out[1]),
+                  "acht_n1_loc_normwise": float(np.linalg.norm(tensor_out[2] - fp64_out[2]) /
+                                                np.linalg.norm(fp64_out[2]))}
     static = None if args.no_static else run_static(S, W, torch, dist, world, stream, sptr, inst)
     cpu_prob = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -565,6 +579,10 @@ def run_ours(args, rank, world, local_rank):
     sinst.run(mplan, sptr)
     smx = sinst.outputs()
     stress_err = {"achtemp": rel(smx[0], s64[0]), "asxtemp": rel(smx[1], s64[1])}
+    sinst.run(tplan, sptr)
+    stc = sinst.outputs()
+    tensor_stress_err = {"achtemp": rel(stc[0], s64[0]), "asxtemp": rel(stc[1], s64[1])}
+    tplan.close()
     del sinst
     plan.close()
     mplan.close()
@@ -618,6 +636,15 @@ def run_ours(args, rank, world, local_rank):
                                "peak": round(fp32_pipe_peak, 3), "unit": "TFLOP/s",
                                "frac": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12 / fp32_pipe_peak, 4),
                                "peak_source": "FP32 pipe 128 FFMA/clk/SM at the sampled SM clock"}},
+        "tensor": {"value": round(tensor_value, 4), "unit": UNIT,
+                   "speedup_vs_fp64": round(tensor_value / value, 3),
+                   "ms_per_step": round(ms_tensor / tsteps, 3),
+                   "main_ms_per_step": round(tkt["main_ms"] / max(1, tkt["executions"]), 3),
+                   "rel_err_vs_fp64": tensor_err, "stress_rel_err_vs_fp64": tensor_stress_err,
+                   "max_rel_err": max(max(tensor_err["achtemp"]), max(tensor_err["asxtemp"]),
+                                      max(tensor_stress_err["achtemp"]), max(tensor_stress_err["asxtemp"])),
+                   "path": "frequency factors in FP64, band sum as split-BF16 tcgen05 GEMM (FF kernel), "
+                           "occupied bands as in the mixed form"},
         "ff": ff,
         "ff_sigma": ffs,
         "batched": batch,

@@ -6,6 +6,7 @@
 
 #include "sigma_gpp.h"
 #include "sigma_internal.cuh"
+#include "ff_plan.h"
 #include "runtime.h"
 
 namespace sigma {
@@ -22,6 +23,8 @@ struct sigma_gpp_plan_s {
   int sch_grid = 0, ssx_grid = 0, schy_grid = 0;
   sigma::GppWork sch{}, ssx{};
   sigma::GppWork schy{};      // FP64 main pass for shared frequencies (shares sch's buffers)
+  sigma_ff_plan ff = nullptr; // tensor form: the contraction plan (3 slabs = 3 frequencies)
+  double2* yfac = nullptr;    // tensor form: frequency factors Y[3][ng][nc]
   sigma::MixedPrep prep{};    // FP32 operands of the mixed path (unused for FP64)
   void* block = nullptr;      // one device allocation for everything below
   int* igp_of = nullptr;      // [ng]
@@ -120,7 +123,8 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   *plan_out = nullptr;
   int st = gpp_check_shape(number_bands, nvband, ncouls, ngpown, nstart, nend);
   if (st != SIGMA_OK) return st;
-  if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED) return SIGMA_ERR_UNSUPPORTED;
+  if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED && precision != SIGMA_PREC_TENSOR)
+    return SIGMA_ERR_UNSUPPORTED;
   if (indinv_len < ncouls) return SIGMA_ERR_INVALID_SHAPE;
   std::vector<int> igp_of;
   int valid = 0;
@@ -143,7 +147,9 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   p->ng = ngpown;
   p->precision = precision;
   p->valid_columns = valid;
-  const bool mixed = precision == SIGMA_PREC_MIXED;
+  const bool tensor = precision == SIGMA_PREC_TENSOR;
+  // the tensor form keeps the mixed form's pre-pass for the occupied bands
+  const bool mixed = precision == SIGMA_PREC_MIXED || tensor;
   p->sch_grid = sms * (mixed ? sch_blocks_per_sm_mixed() : sch_blocks_per_sm_fp64());
   p->ssx_grid = sms * (mixed ? ssx_blocks_per_sm_mixed() : ssx_blocks_per_sm_fp64());
   gpp_size_work(p->sch, 0, number_bands, kBN, mixed ? kBPM : kBP, ncouls, ngpown, p->sch_grid,
@@ -170,11 +176,20 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   const size_t b_colB = align_up(sizeof(float2) * col_elems, 256);
   const size_t b_band = align_up(sizeof(float2) * band_elems, 256);
   const size_t b_colC = nvband > 0 ? b_colB : 0;
-  cudaError_t e =
-      cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx + b_colA + b_colB + b_band + b_colC);
+  const size_t b_y = tensor ? align_up(sizeof(double2) * 3 * (size_t)ngpown * ncouls, 256) : 0;
+  if (tensor) {
+    int st2 = ff_plan_build(&p->ff, number_bands, ncouls, ngpown, kNW, igp_of, SIGMA_FF_OZAKI_BF16);
+    if (st2 != SIGMA_OK) {
+      delete p;
+      return st2;
+    }
+  }
+  cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx + b_colA + b_colB + b_band +
+                                            b_colC + b_y);
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_last_cuda_error(e, "cudaMalloc(plan)", __LINE__);
+    if (p->ff) sigma_ff_plan_destroy(p->ff);
     delete p;
     return SIGMA_ERR_ALLOC;
   }
@@ -194,6 +209,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
     p->prep.colB = mixed ? reinterpret_cast<float2*>(q + b_colA) : nullptr;
     p->prep.band = mixed ? reinterpret_cast<float2*>(q + b_colA + b_colB) : nullptr;
     p->prep.colC = mixed && nvband > 0 ? reinterpret_cast<float2*>(q + b_colA + b_colB + b_band) : nullptr;
+    p->yfac = tensor ? reinterpret_cast<double2*>(q + b_colA + b_colB + b_band + b_colC) : nullptr;
     p->prep.nc_pad = nc_pad;
     p->prep.status = p->counters + 2;
   }
@@ -201,6 +217,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   if (e != cudaSuccess) {
     set_last_cuda_error(e, "cudaMemcpy(igp_of)", __LINE__);
     cudaFree(p->block);
+    if (p->ff) sigma_ff_plan_destroy(p->ff);
     delete p;
     return SIGMA_ERR_CUDA;
   }
@@ -217,6 +234,7 @@ extern "C" int sigma_gpp_plan_destroy(sigma_gpp_plan plan) {
   cudaSetDevice(plan->device);
   for (cudaEvent_t e : plan->events) cudaEventDestroy(e);
   if (plan->block) cudaFree(plan->block);
+  if (plan->ff) sigma_ff_plan_destroy(plan->ff);
   cudaSetDevice(cur);
   delete plan;
   return SIGMA_OK;
@@ -264,8 +282,11 @@ extern "C" int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, doubl
   if (other_ms) *other_ms = tr;
   if (launches_per_execution) {
     const bool mixed = plan->precision == SIGMA_PREC_MIXED;
-    *launches_per_execution = (plan->sch.n_items > 0 ? (mixed ? 3 : 1) : 0) +
-                              (plan->ssx.n_items > 0 ? 1 : 0) + 2;
+    if (plan->precision == SIGMA_PREC_TENSOR)  // pre-pass (2), factors, slicing (2), GEMM, its reduction
+      *launches_per_execution = 7 + (plan->ssx.n_items > 0 ? 1 : 0) + 2;
+    else
+      *launches_per_execution = (plan->sch.n_items > 0 ? (mixed ? 3 : 1) : 0) +
+                                (plan->ssx.n_items > 0 ? 1 : 0) + 2;
   }
   plan->recorded = 0;
   return SIGMA_OK;
@@ -277,6 +298,7 @@ extern "C" int sigma_gpp_plan_status(sigma_gpp_plan plan, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   SIGMA_CUDA_TRY(cudaMemcpyAsync(&st, plan->prep.status, sizeof(int), cudaMemcpyDeviceToHost, s));
   SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st == SIGMA_OK && plan->ff) return sigma_ff_plan_status(plan->ff, stream);
   return st;
 }
 
@@ -315,22 +337,32 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
 
   cudaEvent_t* ev = nullptr;
   if (plan->timing && plan->recorded < kMaxTimedExecutions) ev = &plan->events[4 * plan->recorded++];
+  const bool tensor = plan->precision == SIGMA_PREC_TENSOR;
+  if (tensor && wx_band_stride != 0) return SIGMA_ERR_UNSUPPORTED;  // needs one frequency set
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
   const bool mixed = plan->precision == SIGMA_PREC_MIXED;
-  if (mixed && plan->sch.n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->sch, plan->prep, s));
+  if ((mixed || (tensor && plan->ssx.n_items > 0)) && plan->sch.n_items > 0)
+    SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->sch, plan->prep, s));
   // FP64 with one frequency set for every band: the shared-factor kernel
   const bool ypath = !mixed && wx_band_stride == 0 && plan->schy.n_items > 0;
-  const GppWork& main = ypath ? plan->schy : plan->sch;
+  GppWork main = ypath ? plan->schy : plan->sch;
+  if (tensor) main.partial = nullptr;  // band sums land in acht_n1 directly
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
-  if (ypath)
+  if (tensor) {
+    SIGMA_CUDA_TRY(launch_gpp_y_factor(p, plan->yfac, s));
+    const int st = ff_execute_weighted(plan->ff, reinterpret_cast<const sigma_complex128*>(plan->yfac),
+                                       aqsntemp, aqsmtemp, vcoul, 0.5,
+                                       reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream);
+    if (st != SIGMA_OK) return st;
+  } else if (ypath)
     SIGMA_CUDA_TRY(launch_sch_fp64y(p, plan->schy, plan->schy_grid, s));
   else if (plan->sch.n_items > 0)
     SIGMA_CUDA_TRY(mixed ? launch_sch_mixed(p, plan->sch, plan->prep, plan->sch_grid, s)
                          : launch_sch_fp64(p, plan->sch, plan->sch_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
   if (plan->ssx.n_items > 0)
-    SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed(p, plan->ssx, plan->prep, plan->ssx_grid, s)
-                         : launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
+    SIGMA_CUDA_TRY((mixed || tensor) ? launch_ssx_mixed(p, plan->ssx, plan->prep, plan->ssx_grid, s)
+                                     : launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[2], s));
   SIGMA_CUDA_TRY(launch_gpp_reduce(main, plan->ssx, plan->nb, plan->acht_n1,
                                    reinterpret_cast<double2*>(achtemp),
@@ -434,6 +466,7 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
   int dev_status = 0;
   SIGMA_CUDA_TRY(cudaMemcpyAsync(&dev_status, plan->prep.status, sizeof(int), cudaMemcpyDeviceToHost, s));
   SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+  if (dev_status == 0 && plan->ff) dev_status = sigma_ff_plan_status(plan->ff, stream);
   return dev_status == 0 ? SIGMA_OK : dev_status;
 }
 
@@ -462,6 +495,19 @@ extern "C" int sigma_gpp_mixed(int number_bands, int nvband, int ncouls, int ngp
                                sigma_complex128* achtemp, sigma_complex128* asxtemp,
                                sigma_complex128* acht_n1_loc, void* stream) {
   return sigma::gpp_host(SIGMA_PREC_MIXED, number_bands, nvband, ncouls, ngpown, nstart, nend,
+                         inv_igp_index, indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array,
+                         wtilde_array, vcoul, achtemp, asxtemp, acht_n1_loc, stream);
+}
+
+extern "C" int sigma_gpp_tensor(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
+                                int nend, const int* inv_igp_index, const int* indinv,
+                                const double* wx_array, double occ,
+                                const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
+                                const sigma_complex128* I_eps_array,
+                                const sigma_complex128* wtilde_array, const double* vcoul,
+                                sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                                sigma_complex128* acht_n1_loc, void* stream) {
+  return sigma::gpp_host(SIGMA_PREC_TENSOR, number_bands, nvband, ncouls, ngpown, nstart, nend,
                          inv_igp_index, indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array,
                          wtilde_array, vcoul, achtemp, asxtemp, acht_n1_loc, stream);
 }

@@ -28,6 +28,7 @@ __device__ __forceinline__ double warp_sum_comp(Comp c) {
 }
 
 struct ReduceArgs {
+  int sch_rows;       // bands whose sums come from sch partials (0: acht_n1 already holds them)
   const double2* sch_partial;
   int sch_ncb, sch_splits, sch_bn;
   const double2* ssx_partial;
@@ -40,7 +41,7 @@ struct ReduceArgs {
 __global__ void reduce_bands_kernel(ReduceArgs a) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  const int n_sch = a.nb * kNW, n_ssx = a.nvband * kNW;
+  const int n_sch = a.sch_rows * kNW, n_ssx = a.nvband * kNW;
   if (warp >= n_sch + n_ssx) return;
   const bool is_sch = warp < n_sch;
   const int e = is_sch ? warp : warp - n_sch;
@@ -95,6 +96,7 @@ cudaError_t launch_gpp_reduce(const GppWork& sch, const GppWork& ssx, int nb, do
                               double2* achtemp, double2* asxtemp, double2* acht_n1_loc,
                               cudaStream_t s) {
   ReduceArgs a;
+  a.sch_rows = sch.partial ? nb : 0;
   a.sch_partial = sch.partial;
   a.sch_ncb = sch.n_col_blocks;
   a.sch_splits = sch.n_splits;
@@ -106,12 +108,14 @@ cudaError_t launch_gpp_reduce(const GppWork& sch, const GppWork& ssx, int nb, do
   a.nvband = ssx.band_count;
   a.acht_n1 = acht_n1;
   a.asx_n1 = acht_n1 + (size_t)nb * kNW;
-  const int warps = (nb + a.nvband) * kNW;
+  const int warps = (a.sch_rows + a.nvband) * kNW;
   const int threads = 256;
   const int blocks = (warps * 32 + threads - 1) / threads;
-  reduce_bands_kernel<<<blocks, threads, 0, s>>>(a);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (blocks > 0) {
+    reduce_bands_kernel<<<blocks, threads, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   reduce_total_kernel<<<1, 256, 0, s>>>(acht_n1, a.asx_n1, nb, a.nvband, achtemp, asxtemp,
                                         acht_n1_loc);
   return cudaGetLastError();

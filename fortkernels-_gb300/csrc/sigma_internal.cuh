@@ -135,8 +135,13 @@ cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, const MixedPrep&
 int sch_blocks_per_sm(int precision);
 int ssx_blocks_per_sm(int precision);
 
+// Tensor form: frequency factors y[iw][my_igp][ig] of one shared frequency
+// set (gpp_tensor.cu).
+cudaError_t launch_gpp_y_factor(const GppDev& p, double2* y, cudaStream_t s);
+
 // Sums the partials of the sch and ssx passes in a fixed order into
 // acht_n1[nb][3] (workspace), achtemp[3], asxtemp[3] and acht_n1_loc[nb].
+// With sch.partial null, acht_n1's first nb rows already hold the band sums.
 cudaError_t launch_gpp_reduce(const GppWork& sch, const GppWork& ssx, int nb, double2* acht_n1,
                               double2* achtemp, double2* asxtemp, double2* acht_n1_loc,
                               cudaStream_t s);

@@ -17,7 +17,7 @@ PKG = pathlib.Path(__file__).resolve().parent
 LIB_PATH = PKG / "lib" / "libsigma_gb300.so"
 
 OK = 0
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_TENSOR = 0, 1, 2
 FF_MODE_FP64, FF_MODE_OZAKI_BF16 = 0, 1
 
 STATUS = {
@@ -52,6 +52,7 @@ SIGNATURES = {
     "sigma_version": ([], C.c_char_p),
     "sigma_gpp_fp64": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_mixed": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_tensor": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I, _I], _I),
     "sigma_gpp_execute": ([_P, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_plan_destroy": ([_P], _I),
@@ -150,7 +151,8 @@ def gpp_host(prob, precision: int = PREC_FP64, stream: int = 0, want_n1: bool = 
     ach = np.zeros(3, np.complex128)
     asx = np.zeros(3, np.complex128)
     n1 = np.zeros(prob.number_bands, np.complex128) if want_n1 else None
-    fn = lib.sigma_gpp_fp64 if precision == PREC_FP64 else lib.sigma_gpp_mixed
+    fn = {PREC_FP64: lib.sigma_gpp_fp64, PREC_MIXED: lib.sigma_gpp_mixed,
+          PREC_TENSOR: lib.sigma_gpp_tensor}[precision]
     st = fn(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart, prob.nend,
             _ptr(inv), _ptr(indinv), _ptr(wx), prob.occ, *[_ptr(a) for a in arrs], _ptr(vcoul),
             _ptr(ach), _ptr(asx), _ptr(n1), stream)

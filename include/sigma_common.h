@@ -41,7 +41,11 @@ enum sigma_status {
 /* Arithmetic forms. */
 enum sigma_precision {
   SIGMA_PREC_FP64 = 0,  /* plain FP64: every term in double precision */
-  SIGMA_PREC_MIXED = 1  /* FP32 bulk, FP64 pole-guard decisions, compensated FP64 reductions */
+  SIGMA_PREC_MIXED = 1, /* FP32 bulk, FP64 pole-guard decisions, compensated FP64 reductions */
+  SIGMA_PREC_TENSOR = 2 /* one frequency set for all bands only: the band sum as a complex GEMM
+                           on tcgen05 tensor cores (split-BF16 operands, FP32 accumulation
+                           drained into FP32 sums, FP64 partials), frequency factors and
+                           pole-guard decisions in FP64; occupied bands as in the mixed form */
 };
 
 /* Human-readable name of a status code (static string). */

@@ -70,6 +70,19 @@ int sigma_gpp_mixed(int number_bands, int nvband, int ncouls, int ngpown, int ns
                     sigma_complex128* achtemp, sigma_complex128* asxtemp,
                     sigma_complex128* acht_n1_loc, void* stream);
 
+/* Same contract, tensor-core form (SIGMA_PREC_TENSOR): one frequency set for
+ * every band (wx_array[3]); the band sum runs as a complex GEMM on tcgen05
+ * tensor cores with split-BF16 operands.  ngpown must be at least ~18 (the
+ * contraction tiles hold at most 8 frequency segments; smaller returns
+ * SIGMA_ERR_UNSUPPORTED). */
+int sigma_gpp_tensor(int number_bands, int nvband, int ncouls, int ngpown, int nstart, int nend,
+                     const int* inv_igp_index, const int* indinv, const double* wx_array,
+                     double occ, const sigma_complex128* aqsmtemp,
+                     const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                     const sigma_complex128* wtilde_array, const double* vcoul,
+                     sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                     sigma_complex128* acht_n1_loc, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Device-resident path.  A plan validates the index maps on the host (where
  * the reference would read out of bounds it returns SIGMA_ERR_INDEX_RANGE),

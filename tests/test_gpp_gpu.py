@@ -290,3 +290,43 @@ def test_production_stress_mixed_within_bar(sigma_lib):
     torch.cuda.empty_cache()
     assert rel_err(gmx[0], g64[0]).max() <= MIXED_TOL
     assert rel_err(gmx[1], g64[1]).max() <= MIXED_TOL
+
+
+# ------------------------------------------------------------ tensor-core form
+TENSOR_CASES = [c for c in RANDOM_CASES if c[3] >= 20]
+
+
+@pytest.mark.parametrize("case", TENSOR_CASES, ids=lambda c: f"nb{c[0]}-nv{c[1]}-nc{c[2]}-ng{c[3]}{'-stress' if c[5] else ''}")
+def test_tensor_random_matches_oracle(sigma_lib, case):
+    """Split-BF16 tensor-core band sum: the same error model as the FP32
+    path (terms carry FP32-level relative errors)."""
+    nb, nvb, nc, ng, seed, stress = case
+    prob = W.gpp_random(nb, nvb, nc, ng, seed, stress=stress)
+    o = O.gpp(prob)
+    g = sigma_lib.gpp_host(prob, sigma_lib.PREC_TENSOR)
+    _check(g, o, 1, abs2=O.gpp_abs2(prob))
+
+
+def test_tensor_constant_fill_and_limits(sigma_lib):
+    prob = W.gpp_constant(128, 2, 8192, 20)
+    o = O.gpp(prob)
+    g = sigma_lib.gpp_host(prob, sigma_lib.PREC_TENSOR)
+    _check(g, o, 1)
+    # per-band frequencies have no shared factor: the tensor form refuses them
+    prob = W.gpp_random(37, 3, 900, 29, 23)
+    wxb = np.ascontiguousarray(np.repeat(prob.wx_array[None, :], prob.number_bands, 0)).reshape(-1)
+    with pytest.raises(sigma_lib.SigmaError) as e:
+        _run_plan(sigma_lib, prob, sigma_lib.PREC_TENSOR, wx=wxb, wx_stride=3)
+    assert e.value.status == -8
+    # fewer than ~18 columns: more frequency segments per tile than the kernel holds
+    with pytest.raises(sigma_lib.SigmaError) as e:
+        sigma_lib.gpp_host(W.gpp_random(7, 1, 333, 5, 14), sigma_lib.PREC_TENSOR)
+    assert e.value.status == -8
+
+
+def test_production_tensor_within_bar_of_fp64(production):
+    g64 = production.run(0)
+    gtc = production.run(2)
+    assert rel_err(gtc[0], g64[0]).max() <= MIXED_TOL
+    assert rel_err(gtc[1], g64[1]).max() <= MIXED_TOL
+    assert normwise_err(gtc[2], g64[2]) <= MIXED_TOL
