@@ -374,6 +374,41 @@ def run_ff_sigma(S, W, torch, dist, world, stream, sptr):
     return res
 
 
+def run_real(S, W, torch, dist, world, stream, sptr, args):
+    """Real-valued GPP (gppKer_real.cpp) at the production shape with seeded
+    real inputs (aqsm, aqsn, I_eps ~ U(-1,1), wtilde ~ U(0.5,5), vcoul ~
+    U(0.1,10)): FP64 Gterms/s of the device-resident plan."""
+    f64 = dict(dtype=torch.float64, device="cuda")
+    aqsm = torch.empty(NB * NC, **f64)
+    aqsn = torch.empty_like(aqsm)
+    ieps = torch.empty(NG * NC, **f64)
+    wt = torch.empty_like(ieps)
+    vc = torch.empty(NC, **f64)
+    seed = W.GPP_PRODUCTION_SEED
+    S.fill_real_device(aqsm.data_ptr(), NB * NC, seed, W.AID_AQSM, -1, 1, sptr)
+    S.fill_real_device(aqsn.data_ptr(), NB * NC, seed, W.AID_AQSN, -1, 1, sptr)
+    S.fill_real_device(ieps.data_ptr(), NG * NC, seed, W.AID_IEPS, -1, 1, sptr)
+    S.fill_real_device(wt.data_ptr(), NG * NC, seed, W.AID_WTILDE, 0.5, 5.0, sptr)
+    S.fill_real_device(vc.data_ptr(), NC, seed, W.AID_VCOUL, 0.1, 10.0, sptr)
+    inv, indinv = W.gpp_index_maps(NC, NG)
+    wx = torch.tensor(W.wx_frequencies(), **f64)
+    ach, asx, n1 = torch.zeros(3, **f64), torch.zeros(3, **f64), torch.zeros(NB, **f64)
+    plan = S.GppRealPlan(NB, NVB, NC, NG, inv, indinv)
+    run = lambda: plan.execute(wx, aqsm, aqsn, ieps, wt, vc, ach, asx, n1, stream=sptr)
+    for _ in range(args.warmup):
+        run()
+    steps = max(args.steps, 5)
+    ms = timed(torch, dist, world, run, steps, stream)
+    plan.close()
+    terms = NB * NG * NC * 3
+    res = {"workload": f"real-valued GPP, {NB} bands x {NG} columns x {NC} g-vectors x 3 frequencies, FP64",
+           "value": round(terms * world / (ms / steps * 1e-3) / 1e9, 4), "unit": UNIT,
+           "ms_per_step": round(ms / steps, 3), "steps": steps}
+    del aqsm, aqsn, ieps, wt
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_static(S, W, torch, dist, world, stream, sptr, inst):
     """Static remainder (sigma_gpp_static_execute) on the production
     instance's device arrays: both contraction forms, FP64-equivalent TF/s
@@ -596,6 +631,7 @@ def run_ours(args, rank, world, local_rank):
     fp32_pipe_peak = 2 * 128 * sms * clock_mhz * 1e6 / 1e12
     ff = None if args.no_ff else run_ff(S, W, torch, dist, world, stream, sptr, args)
     ffs = None if args.no_ff else run_ff_sigma(S, W, torch, dist, world, stream, sptr)
+    real = None if args.no_real else run_real(S, W, torch, dist, world, stream, sptr, args)
     batch = None if args.no_batched else run_batched(S, W, torch, dist, world, stream, sptr, args, value)
     worst = max(max(mixed_err["achtemp"]), max(mixed_err["asxtemp"]),
                 max(stress_err["achtemp"]), max(stress_err["asxtemp"]))
@@ -649,6 +685,7 @@ def run_ours(args, rank, world, local_rank):
         "ff_sigma": ffs,
         "batched": batch,
         "static_remainder": static,
+        "real": real,
         "peaks_measured": {"fp64_fma_probe_tflops": round(fp64_peak, 4),
                            "fp32_fma_probe_tflops": round(fp32_peak, 3),
                            "fp64_pipe_tflops_at_clock": round(fp64_pipe_peak, 4),
@@ -676,6 +713,7 @@ def main():
     ap.add_argument("--no-ff", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-static", action="store_true")
+    ap.add_argument("--no-real", action="store_true")
     ap.add_argument("--batch-instances", type=int, default=48,
                     help="leading instances of the 48-instance batched set (fewer only for profiling)")
     ap.add_argument("--batch-fp64-steps", type=int, default=2)

@@ -68,6 +68,10 @@ SIGNATURES = {
     "sigma_gpp_batch_status": ([_P, _P], _I),
     "sigma_gpp_batch_destroy": ([_P], _I),
     "sigma_gpp_batched": ([_I, _P, _I, _P], _I),
+    "sigma_gpp_real_fp64": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_real_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I], _I),
+    "sigma_gpp_real_execute": ([_P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_real_plan_destroy": ([_P], _I),
     "sigma_gpp_achstemp": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "sigma_gpp_static_plan_create": ([_P, _I, _I, _I, _P, _P, _I], _I),
     "sigma_gpp_static_execute": ([_P, _P, _P, _P, _P, _P, _P, _P], _I),
@@ -158,6 +162,55 @@ def gpp_host(prob, precision: int = PREC_FP64, stream: int = 0, want_n1: bool = 
             _ptr(ach), _ptr(asx), _ptr(n1), stream)
     _check(st, fn.__name__)
     return ach, asx, n1
+
+
+def gpp_real_host(prob, stream: int = 0, want_n1: bool = True):
+    """Real-valued GPP host drop-in (sigma_gpp_real_fp64) on a
+    workload.GppProblem with real arrays; returns (achtemp[3], asxtemp[3],
+    acht_n1_loc[nb]) float64."""
+    lib = load()
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    inv = np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, dtype=np.int32)
+    arrs = [f(prob.wx_array), f(prob.aqsmtemp), f(prob.aqsntemp), f(prob.I_eps_array), f(prob.wtilde_array),
+            f(prob.vcoul)]
+    ach, asx = np.zeros(3), np.zeros(3)
+    n1 = np.zeros(prob.number_bands) if want_n1 else None
+    st = lib.sigma_gpp_real_fp64(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart,
+                                 prob.nend, _ptr(inv), _ptr(indinv), _ptr(arrs[0]), prob.occ,
+                                 *[_ptr(a) for a in arrs[1:]], _ptr(ach), _ptr(asx), _ptr(n1), stream)
+    _check(st, "sigma_gpp_real_fp64")
+    return ach, asx, n1
+
+
+class GppRealPlan:
+    """Device-resident real-valued GPP (sigma_gpp_real_plan_create / execute)."""
+
+    def __init__(self, number_bands, nvband, ncouls, ngpown, inv_igp_index, indinv):
+        self.lib = load()
+        self.inv = np.ascontiguousarray(inv_igp_index, dtype=np.int32)
+        self.indinv = np.ascontiguousarray(indinv, dtype=np.int32)
+        h = C.c_void_p()
+        _check(self.lib.sigma_gpp_real_plan_create(C.byref(h), number_bands, nvband, ncouls, ngpown, 0, 3,
+                                                   _ptr(self.inv), _ptr(self.indinv), len(self.indinv)),
+               "sigma_gpp_real_plan_create")
+        self.handle = h
+
+    def execute(self, wx, aqsm, aqsn, ieps, wt, vcoul, achtemp, asxtemp, acht_n1_loc=None, occ=1.0, stream=0):
+        _check(self.lib.sigma_gpp_real_execute(self.handle, _dptr(wx), occ,
+                                               *[_dptr(a) for a in (aqsm, aqsn, ieps, wt, vcoul, achtemp, asxtemp)],
+                                               _dptr(acht_n1_loc), stream), "sigma_gpp_real_execute")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sigma_gpp_real_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class GppPlan:

@@ -320,3 +320,29 @@ def ff_sigma_random(number_bands, nvband, ncouls, ngpown, nfreq, nfreqeval, seed
     vcoul = fill_real(seed, AID_VCOUL, nc, 0.1, 10.0)
     return FFSigmaProblem(nb, nvband, nc, ngpown, nfreq, nfreqeval, inv, indinv, aqsm, aqsn, r, a, vcoul,
                           ekq, grid, brd, pref)
+
+
+# ---------------------------------------------------------------- real-valued GPP
+def gpp_real_constant(number_bands, nvband, ncouls, nodes_per_group) -> GppProblem:
+    """gppKer_real.cpp's own fill (:262-282): every array 0.5, vcoul 1, the
+    mini-app's index maps and frequencies.  Arrays are float64."""
+    sh = gpp_shape(number_bands, nvband, ncouls, nodes_per_group)
+    nb, nc, ng = number_bands, ncouls, sh["ngpown"]
+    inv, indinv = gpp_index_maps(nc, ng)
+    a = np.full((nb, nc), 0.5)
+    e = np.full((ng, nc), 0.5)
+    return GppProblem(nb, nvband, nc, ng, inv, indinv, wx_frequencies(), a, a.copy(), e, e.copy(),
+                      np.ones(nc))
+
+
+def gpp_real_random(number_bands, nvband, ncouls, ngpown, seed) -> GppProblem:
+    """Seeded real inputs: aqsm, aqsn, I_eps ~ U(-1,1), wtilde ~ U(0.5,5),
+    vcoul ~ U(0.1,10); index maps and frequencies of the mini-app."""
+    nb, nc, ng = number_bands, ncouls, ngpown
+    inv, indinv = gpp_index_maps(nc, ng)
+    aqsm = fill_real(seed, AID_AQSM, nb * nc, -1, 1).reshape(nb, nc)
+    aqsn = fill_real(seed, AID_AQSN, nb * nc, -1, 1).reshape(nb, nc)
+    ieps = fill_real(seed, AID_IEPS, ng * nc, -1, 1).reshape(ng, nc)
+    wt = fill_real(seed, AID_WTILDE, ng * nc, 0.5, 5.0).reshape(ng, nc)
+    vcoul = fill_real(seed, AID_VCOUL, nc, 0.1, 10.0)
+    return GppProblem(nb, nvband, nc, ng, inv, indinv, wx_frequencies(), aqsm, aqsn, ieps, wt, vcoul)

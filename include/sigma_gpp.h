@@ -258,6 +258,36 @@ int sigma_gpp_static_execute(sigma_ff_plan plan, const sigma_complex128* aqsmtem
                              const double* vcoul, sigma_complex128* achstemp,
                              sigma_complex128* achstemp_n1, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Real-valued GPP (gppKer_real.cpp:17-155, 296-390, gppKerFort_real.f90):
+ * the same sums with real arrays, one frequency set for every band
+ * (wx_array[3]), FP64.  Term scha = aqsm[n1][igp] aqsn[n1][ig] delw I_eps
+ * (no conjugate), delw = wtilde / (wx - wtilde), the complex path's pole
+ * guard; occupied bands add ssx = Omega2 / wx^2 or -Omega2 cden delw / cden^2,
+ * cden = 4 wtilde^2 (delw + 1/2).  Arrays: aqsmtemp / aqsntemp
+ * [number_bands][ncouls], I_eps_array / wtilde_array [ngpown][ncouls],
+ * vcoul [ncouls] (all double); outputs achtemp[3], asxtemp[3] and
+ * acht_n1_loc[number_bands] (may be NULL), overwritten.  Where the
+ * reference adds a stale scha[ig] for a term its guard drops (:367-371
+ * write it only when kept), this path adds 0.
+ * ------------------------------------------------------------------------- */
+int sigma_gpp_real_fp64(int number_bands, int nvband, int ncouls, int ngpown, int nstart, int nend,
+                        const int* inv_igp_index, const int* indinv, const double* wx_array,
+                        double occ, const double* aqsmtemp, const double* aqsntemp,
+                        const double* I_eps_array, const double* wtilde_array, const double* vcoul,
+                        double* achtemp, double* asxtemp, double* acht_n1_loc, void* stream);
+
+/* Device-resident form (device arrays, asynchronous on `stream`). */
+typedef struct sigma_gpp_real_plan_s* sigma_gpp_real_plan;
+int sigma_gpp_real_plan_create(sigma_gpp_real_plan* plan, int number_bands, int nvband, int ncouls,
+                               int ngpown, int nstart, int nend, const int* inv_igp_index,
+                               const int* indinv, int indinv_len);
+int sigma_gpp_real_execute(sigma_gpp_real_plan plan, const double* wx_array, double occ,
+                           const double* aqsmtemp, const double* aqsntemp, const double* I_eps_array,
+                           const double* wtilde_array, const double* vcoul, double* achtemp,
+                           double* asxtemp, double* acht_n1_loc, void* stream);
+int sigma_gpp_real_plan_destroy(sigma_gpp_real_plan plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,6 +5,8 @@
   oracle/_ref/libgppref.so    <- the same file (main renamed by -D) + oracle/ref_harness.cpp
   oracle/_ref/ffKernel        <- FFKer_cori/ffKernel.cpp of the reference, unmodified
   oracle/_ref/libffref.so     <- the same file (main renamed by -D) + oracle/ff_ref_harness.cpp
+  oracle/_ref/gppKer_real     <- gppKer_real.cpp of the reference, unmodified
+  oracle/_ref/libgpprealref.so <- the same file (main renamed by -D) + oracle/ref_real_harness.cpp
 
 The two oracle/_ref products are built only where the reference checkout is
 present (REFERENCE_ROOT, default /root/reference); they are compiled from the
@@ -29,6 +31,9 @@ FF_REF_DIR = REFERENCE_ROOT / "FFKer_cori"
 FF_REF_SRC = FF_REF_DIR / "ffKernel.cpp"
 FF_REF_BIN = REF_OUT / "ffKernel"
 FF_REF_LIB = REF_OUT / "libffref.so"
+REAL_REF_SRC = REFERENCE_ROOT / "gppKer_real.cpp"
+REAL_REF_BIN = REF_OUT / "gppKer_real"
+REAL_REF_LIB = REF_OUT / "libgpprealref.so"
 
 ORACLE_FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 # the timing build of the same file: the reference's own optimisation flags
@@ -88,6 +93,13 @@ def build_reference() -> bool:
         if not _newer(FF_REF_LIB, FF_REF_SRC, ffh):
             _run(["g++", *REF_FLAGS, *inc, "-fPIC", "-shared", "-Dmain=ffker_reference_main",
                   str(FF_REF_SRC), str(ffh), "-o", str(FF_REF_LIB)])
+    if REAL_REF_SRC.exists():
+        if not _newer(REAL_REF_BIN, REAL_REF_SRC):
+            _run(["g++", *REF_FLAGS, str(REAL_REF_SRC), "-o", str(REAL_REF_BIN)])
+        rh = HERE / "ref_real_harness.cpp"
+        if not _newer(REAL_REF_LIB, REAL_REF_SRC, rh):
+            _run(["g++", *REF_FLAGS, "-fPIC", "-shared", "-Dmain=gppreal_reference_main",
+                  str(REAL_REF_SRC), str(rh), "-o", str(REAL_REF_LIB)])
     return True
 
 

@@ -825,3 +825,115 @@ extern "C" int oracle_ff_sigma(int number_bands, int nvband, int ncouls, int ngp
   }
   return kOk;
 }
+
+// ---------------------------------------------------------------------------
+// Real-valued GPP (gppKer_real.cpp:17-155, 302-390): the same loop nest with
+// real arrays, mygpvar1 = aqsm[n1][igp] (no conjugate), the same pole guard,
+// and in the occupied-band solver ssx = Omega2 / wx^2 or
+// -Omega2 cden delw / cden^2 with cden = 4 wtilde^2 (delw + 1/2).  Terms in
+// the reference's operation order, double-double sums.  Where the
+// reference's unoccupied loop leaves scha[ig] from an earlier frequency or
+// block when the guard drops a term (:367-371 writes it only when kept), the
+// oracle adds 0, the value the guard means.
+namespace {
+
+inline void real_occ(double wxt, double wtilde, double ieps, double matngmatmgp, double& ssxa,
+                     double& scha) {
+  const double wtilde2 = wtilde * wtilde;
+  const double Omega2 = wtilde2 * ieps;
+  const double wdiff = wxt - wtilde;
+  double cden = wdiff;
+  double rden = 1 / (cden * cden);
+  const double delw = wtilde * cden * rden;
+  const double delwr = delw * delw;
+  const double wdiffr = wdiff * wdiff;
+  double sch, ssx;
+  if ((wdiffr > kLimitTwo) && (delwr < kLimitOne)) {
+    sch = delw * ieps;
+    cden = wxt * wxt;
+    rden = cden * cden;
+    rden = 1.00 / rden;
+    ssx = Omega2 * cden * rden;
+  } else if (delwr > kTo1) {
+    sch = 0.0;
+    cden = 4.00 * wtilde2 * (delw + 0.50);
+    rden = cden * cden;
+    rden = 1.00 / rden;
+    ssx = -Omega2 * cden * rden * delw;
+  } else {
+    sch = 0.0;
+    ssx = 0.0;
+  }
+  ssxa = matngmatmgp * ssx;
+  scha = matngmatmgp * sch;
+}
+
+}  // namespace
+
+extern "C" int oracle_gpp_real(int number_bands, int nvband, int ncouls, int ngpown,
+                               const int* inv_igp_index, const int* indinv, int indinv_len,
+                               const double* wx, double occ, const double* aqsm,
+                               const double* aqsn, const double* ieps, const double* wt,
+                               const double* vcoul, double* achtemp, double* asxtemp,
+                               double* acht_n1_loc, int nthreads) {
+  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0 || nvband < 0 || nvband > number_bands)
+    return kErrShape;
+  std::vector<int> igp_of(ngpown);
+  for (int g = 0; g < ngpown; ++g) {
+    const int v = map_igp(inv_igp_index, indinv, indinv_len, ncouls, g);
+    if (v == -2) return kErrIndex;
+    igp_of[g] = v;
+  }
+  const size_t nc = static_cast<size_t>(ncouls);
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  // per band: ach[3], asx[3]
+  std::vector<DD> per(static_cast<size_t>(number_bands) * 6);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+  for (int n1 = 0; n1 < number_bands; ++n1) {
+    DD* r = &per[static_cast<size_t>(n1) * 6];
+    const bool flag_occ = n1 < nvband;
+    for (int g = 0; g < ngpown; ++g) {
+      const int igp = igp_of[g];
+      if (igp < 0) continue;
+      const double mygpvar1 = aqsm[n1 * nc + igp];
+      for (int iw = 0; iw < 3; ++iw) {
+        const double wxt = wx[iw];
+        DD scht, ssxt;
+        for (size_t ig = 0; ig < nc; ++ig) {
+          const double w = wt[g * nc + ig], e = ieps[g * nc + ig];
+          if (flag_occ) {
+            double ssxa, scha;
+            real_occ(wxt, w, e, aqsn[n1 * nc + ig] * mygpvar1, ssxa, scha);
+            dd_add(ssxt, ssxa);
+            dd_add(scht, scha);
+          } else {
+            const double wdiff = wxt - w;
+            double cden = wdiff;
+            double rden = cden * cden;
+            rden = 1 / rden;
+            const double delw = w * cden * rden;
+            const double delwr = delw * delw;
+            const double wdiffr = wdiff * wdiff;
+            if ((wdiffr > kLimitTwo) && (delwr < kLimitOne))
+              dd_add(scht, mygpvar1 * aqsn[n1 * nc + ig] * delw * e);
+          }
+        }
+        dd_add(r[iw], dd_mul(dd_mul(scht, 0.5), vcoul[igp]));
+        if (flag_occ) dd_add(r[3 + iw], dd_mul(dd_mul(ssxt, occ), vcoul[igp]));
+      }
+    }
+  }
+  DD ach[3], asx[3];
+  for (int n1 = 0; n1 < number_bands; ++n1) {
+    for (int k = 0; k < 3; ++k) {
+      dd_add(ach[k], per[static_cast<size_t>(n1) * 6 + k]);
+      dd_add(asx[k], per[static_cast<size_t>(n1) * 6 + 3 + k]);
+    }
+    if (acht_n1_loc) acht_n1_loc[n1] = per[static_cast<size_t>(n1) * 6 + 2].hi + per[static_cast<size_t>(n1) * 6 + 2].lo;
+  }
+  for (int k = 0; k < 3; ++k) {
+    achtemp[k] = ach[k].hi + ach[k].lo;
+    asxtemp[k] = asx[k].hi + asx[k].lo;
+  }
+  return kOk;
+}

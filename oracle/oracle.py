@@ -36,6 +36,7 @@ def lib():
         l.oracle_ff_schdt.argtypes = [_I, _I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _I]
         l.oracle_ff_sigma.argtypes = [_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                       _D, _D, _D, _D, _P, _P, _P, _P, _P, _P, _P, _I]
+        l.oracle_gpp_real.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _I]
         l.oracle_gpp_achstemp.argtypes = [_I, _I, _I, _P, _P, _I, _P, _P, _P, _P, _P, _P, _I]
         l.oracle_gpp_abs2.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P,
                                       _I, _I, _I]
@@ -295,4 +296,62 @@ def ff_sigma(prob, schdt=None, nthreads=0):
     if st != 0:
         raise OracleError(f"oracle_ff_sigma status {st}")
     out["achsDtemp"] = out["achsDtemp"][0]
+    return out
+
+
+def gpp_real(prob, nthreads=0):
+    """Real-valued GPP (gppKer_real.cpp semantics): (achtemp[3], asxtemp[3],
+    acht_n1_loc[nb]) float64."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    p = prob
+    inv, ind = i32(p.inv_igp_index), i32(p.indinv)
+    arrs = [f(p.wx_array)]
+    ach, asx, n1 = np.zeros(3), np.zeros(3), np.zeros(p.number_bands)
+    data = [f(p.aqsmtemp), f(p.aqsntemp), f(p.I_eps_array), f(p.wtilde_array), f(p.vcoul)]
+    st = lib().oracle_gpp_real(p.number_bands, p.nvband, p.ncouls, p.ngpown, _p(inv), _p(ind), len(ind),
+                               _p(arrs[0]), p.occ, *[_p(a) for a in data], _p(ach), _p(asx), _p(n1), nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_gpp_real status {st}")
+    return ach, asx, n1
+
+
+_realref = None
+
+
+def reference_real_flagocc_columns(prob, igp_of):
+    """(ssx_array, sch_array) per (band, column, frequency) from the real
+    mini-app's own flagOCC_solver (gppKer_real.cpp:124-155)."""
+    global _realref
+    if _realref is None:
+        if not _build.build_reference() or not _build.REAL_REF_LIB.exists():
+            return None
+        l = C.CDLL(str(_build.REAL_REF_LIB))
+        l.ref_real_flagocc_columns.argtypes = [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]
+        _realref = l
+    nb, ng = prob.number_bands, prob.ngpown
+    arrs = [np.array(a, dtype=np.float64, order="C", copy=True)
+            for a in (prob.aqsmtemp, prob.aqsntemp, prob.I_eps_array, prob.wtilde_array)]
+    ssx = np.zeros((nb, ng, 3))
+    sch = np.zeros((nb, ng, 3))
+    igp = np.ascontiguousarray(igp_of, dtype=np.int32)
+    wx = np.ascontiguousarray(prob.wx_array, dtype=np.float64)
+    _realref.ref_real_flagocc_columns(nb, prob.ncouls, ng, _p(igp), _p(wx), *[_p(a) for a in arrs], _p(ssx),
+                                      _p(sch))
+    return ssx, sch
+
+
+def run_reference_real_binary(number_bands, nvband, ncouls, nodes_per_group, threads=None, timeout=600):
+    """Runs the unmodified gppKer_real.cpp driver (its constant fill); returns achtemp[3]."""
+    if not _build.build_reference() or not _build.REAL_REF_BIN.exists():
+        return None
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    env.setdefault("OMP_STACKSIZE", "64M")
+    r = subprocess.run([str(_build.REAL_REF_BIN), str(number_bands), str(nvband), str(ncouls),
+                        str(nodes_per_group)], capture_output=True, text=True, env=env, timeout=timeout)
+    out = np.zeros(3)
+    for m in re.finditer(r"achtemp\[(\d+)\] = ([-+0-9.eE]+)", r.stdout):
+        out[int(m.group(1))] = float(m.group(2))
     return out

@@ -24,6 +24,11 @@ fixtures it writes are committed so the tests run without it.
       a grid point or outside the grid, where the C++ interval search
       differs.
 
+  gpp_real_reference.json       the unmodified gppKer_real.cpp driver's
+      printed achtemp (15 digits) on its constant fill; gpp_real_flagocc_<case>.npz
+      ssx_array / sch_array per (band, column, frequency) from its own
+      flagOCC_solver on seeded inputs (workload.gpp_real_random).
+
 Run:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -102,6 +107,27 @@ def ff_main():
         "constant_fill": const, "random": rand}, indent=1))
 
 
+REAL_CONST_SHAPES = [(16, 2, 1024, 8), (32, 4, 2048, 16), (9, 1, 999, 9)]
+REAL_FLAGOCC_CASES = {"real_a": (3, 300, 17, 5), "real_b": (2, 777, 33, 6)}
+
+
+def real_main():
+    runs = []
+    for shape in REAL_CONST_SHAPES:
+        ach = O.run_reference_real_binary(*shape, threads=4)
+        runs.append({"shape": list(shape), "achtemp": [float(v) for v in ach]})
+        print(shape, ach)
+    (HERE / "gpp_real_reference.json").write_text(json.dumps({
+        "source": "gppKer_real.cpp, unmodified, g++ -O3 -fopenmp -std=c++11; stdout achtemp (15 digits)",
+        "runs": runs}, indent=1))
+    for name, (nb, nc, ng, seed) in REAL_FLAGOCC_CASES.items():
+        prob = W.gpp_real_random(nb, nb, nc, ng, seed)
+        ssx, sch = O.reference_real_flagocc_columns(prob, igp_map(prob))
+        np.savez_compressed(HERE / f"gpp_real_flagocc_{name}.npz", ssx=ssx, sch=sch,
+                            meta=np.array([nb, nc, ng, seed]))
+        print(name, np.abs(sch).max(), np.abs(ssx).max())
+
+
 def main():
     if O.reference_lib() is None:
         sys.exit("reference checkout not found; set REFERENCE_ROOT")
@@ -132,3 +158,4 @@ def main():
 if __name__ == "__main__":
     main()
     ff_main()
+    real_main()

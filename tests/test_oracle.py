@@ -228,3 +228,31 @@ def test_ff_sigma_oracle_schdt_epilogue_is_linear():
     for k in ("achDtemp_cor", "ach2Dtemp"):
         assert np.abs((b[k] - z[k]) - 2 * (a[k] - z[k])).max() <= 1e-12 * np.abs(a[k] - z[k]).max()
     assert a["achsDtemp"] == z["achsDtemp"] and np.array_equal(a["asxDtemp"], z["asxDtemp"])
+
+
+REAL_REF = json.loads((GOLD / "gpp_real_reference.json").read_text())
+
+
+@pytest.mark.parametrize("run", REAL_REF["runs"], ids=lambda r: "x".join(map(str, r["shape"])))
+def test_real_oracle_matches_reference_driver_constant_fill(run):
+    """The unmodified gppKer_real.cpp driver's printed achtemp (15 digits)."""
+    ach, _, _ = O.gpp_real(W.gpp_real_constant(*run["shape"]))
+    ref = np.array(run["achtemp"])
+    assert np.abs(ach - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["real_a", "real_b"])
+def test_real_oracle_terms_match_reference_flagocc(name):
+    """Per-column sums of the real mini-app's own occupied-band solver; the
+    oracle's band totals must equal their vcoul-weighted sum."""
+    f = np.load(GOLD / f"gpp_real_flagocc_{name}.npz")
+    nb, nc, ng, seed = (int(x) for x in f["meta"])
+    p = W.gpp_real_random(nb, nb, nc, ng, seed)
+    igp = _igp_map(p)
+    ach_ref = (f["sch"] * p.vcoul[igp][None, :, None]).sum(axis=(0, 1))
+    asx_ref = (f["ssx"] * p.vcoul[igp][None, :, None]).sum(axis=(0, 1))
+    ach, asx, _ = O.gpp_real(p)
+    scale = np.abs(f["sch"] * p.vcoul[igp][None, :, None]).sum(axis=(0, 1))
+    assert np.all(np.abs(ach - ach_ref) <= 1e-13 * scale)
+    scale = np.abs(f["ssx"] * p.vcoul[igp][None, :, None]).sum(axis=(0, 1))
+    assert np.all(np.abs(asx - asx_ref) <= 1e-13 * scale)
