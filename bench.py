@@ -471,7 +471,8 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     gs = torch.cuda.Stream()  # graphs are captured on a non-default stream
     gptr = gs.cuda_stream
     torch.cuda.synchronize()
-    for prec, name, steps in ((S.PREC_FP64, "fp64", args.batch_fp64_steps), (S.PREC_MIXED, "mixed", 5)):
+    for prec, name, steps in ((S.PREC_FP64, "fp64", args.batch_fp64_steps), (S.PREC_MIXED, "mixed", 5),
+                              (S.PREC_TENSOR, "tensor", 5)):
         b = S.GppBatch(dicts, precision=prec, tiles=tiles if prec == S.PREC_FP64 else None)
         terms, items, launches = b.info()
         b.launch_graph(gptr)  # capture, and the warm-up replay
@@ -482,17 +483,18 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
                      "ms_per_step": round(ms / steps, 3), "steps": steps, "terms_per_step": terms,
                      "items": items, "kernels_per_step": launches, "status": st}
         b.close()
-    worst, over = 0.0, 0
-    for a, m in zip(outs["fp64"], outs["mixed"]):
-        for k in (0, 1):
-            e = np.abs(m[k] - a[k]) / np.abs(a[k])
-            worst = max(worst, float(e.max()))
-            over += int(np.sum(e > 1e-6))
-    res["mixed"]["max_rel_err_vs_fp64"] = worst
-    res["mixed"]["outputs_over_1e-6"] = over
-    res["mixed"]["outputs"] = 6 * len(xs)
-    res["mixed"]["speedup_vs_fp64_batched"] = round(res["mixed"]["value"] / res["fp64"]["value"], 2)
-    res["mixed"]["speedup_vs_fp64_dropin"] = round(res["mixed"]["value"] / dropin_value, 2)
+    for name in ("mixed", "tensor"):
+        worst, over = 0.0, 0
+        for a, m in zip(outs["fp64"], outs[name]):
+            for k in (0, 1):
+                e = np.abs(m[k] - a[k]) / np.abs(a[k])
+                worst = max(worst, float(e.max()))
+                over += int(np.sum(e > 1e-6))
+        res[name]["max_rel_err_vs_fp64"] = worst
+        res[name]["outputs_over_1e-6"] = over
+        res[name]["outputs"] = 6 * len(xs)
+        res[name]["speedup_vs_fp64_batched"] = round(res[name]["value"] / res["fp64"]["value"], 2)
+        res[name]["speedup_vs_fp64_dropin"] = round(res[name]["value"] / dropin_value, 2)
     del xs, dicts
     torch.cuda.empty_cache()
     return res

@@ -53,7 +53,7 @@ namespace sigma {
 // Plan over an already validated column map (igp_of[my_igp], -1 = column
 // left out).  Shared by the FF contraction and the static remainders.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
-                  const std::vector<int>& igp_of, int mode) {
+                  const std::vector<int>& igp_of, int mode, void* shared_tiles) {
   *out = nullptr;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -109,7 +109,8 @@ int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, 
   const size_t b_cnt = 256;
   const size_t b_part = up256(sizeof(double2) * (size_t)w.n_items * kFfCols);
   size_t b_oz = 0;
-  if (mode == SIGMA_FF_OZAKI_BF16) b_oz = ozaki_prep_bytes(p->oz);
+  if (mode == SIGMA_FF_OZAKI_BF16)
+    b_oz = shared_tiles ? ozaki_partial_bytes(p->oz) : ozaki_prep_bytes(p->oz);
   cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_part + b_oz);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -122,7 +123,12 @@ int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, 
   w.counter = reinterpret_cast<int*>(base + b_igp);
   w.status = w.counter + 1;
   w.partial = reinterpret_cast<double2*>(base + b_igp + b_cnt);
-  if (mode == SIGMA_FF_OZAKI_BF16) ozaki_prep_bind(p->oz, base + b_igp + b_cnt + b_part);
+  if (mode == SIGMA_FF_OZAKI_BF16) {
+    if (shared_tiles)
+      ozaki_bind(p->oz, shared_tiles, base + b_igp + b_cnt + b_part);
+    else
+      ozaki_prep_bind(p->oz, base + b_igp + b_cnt + b_part);
+  }
   e = cudaMemcpy(const_cast<int*>(d.igp_of), igp_of.data(), sizeof(int) * ngpown,
                  cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -196,6 +202,23 @@ extern "C" int sigma_ff_plan_timing(sigma_ff_plan plan, int* executions, double*
   plan->recorded = 0;
   return SIGMA_OK;
 }
+
+namespace sigma {
+int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes) {
+  FfDev d{};
+  d.nb = number_bands;
+  d.nc = ncouls;
+  d.ng = ngpown;
+  d.nf = nfreq;
+  OzakiPrep oz{};
+  const int sms = device_sm_count();
+  if (sms <= 0) return SIGMA_ERR_NO_DEVICE;
+  ozaki_size(oz, d, sms);
+  if (oz.max_seg > ozaki_max_segments()) return SIGMA_ERR_UNSUPPORTED;
+  *bytes = ozaki_tile_bytes(oz);
+  return SIGMA_OK;
+}
+}  // namespace sigma
 
 extern "C" int sigma_ff_plan_bands(sigma_ff_plan plan, int* number_bands) {
   if (!plan || !number_bands) return SIGMA_ERR_NULL;

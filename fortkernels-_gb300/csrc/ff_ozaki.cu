@@ -447,19 +447,26 @@ void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid) {
 
 int ozaki_max_segments() { return kMaxSeg; }
 
-size_t ozaki_prep_bytes(const OzakiPrep& oz) {
-  const size_t tiles = ((size_t)oz.n_row_blocks + oz.n_col_blocks) * 2 * oz.kt * kOperandBytes;
-  const size_t part = sizeof(double2) * (size_t)oz.n_items * oz.max_seg * kOzCols;
-  return tiles + part + 2048;
+size_t ozaki_tile_bytes(const OzakiPrep& oz) {
+  return ((size_t)oz.n_row_blocks + oz.n_col_blocks) * 2 * oz.kt * kOperandBytes + 1024;
+}
+
+size_t ozaki_partial_bytes(const OzakiPrep& oz) {
+  return sizeof(double2) * (size_t)oz.n_items * oz.max_seg * kOzCols + 256;
+}
+
+size_t ozaki_prep_bytes(const OzakiPrep& oz) { return ozaki_tile_bytes(oz) + ozaki_partial_bytes(oz); }
+
+void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial) {
+  uintptr_t b = (reinterpret_cast<uintptr_t>(tiles) + 1023) & ~uintptr_t(1023);
+  oz.a_tiles = reinterpret_cast<unsigned char*>(b);
+  oz.b_tiles = oz.a_tiles + (size_t)oz.n_row_blocks * 2 * oz.kt * kOperandBytes;
+  uintptr_t pp = (reinterpret_cast<uintptr_t>(partial) + 255) & ~uintptr_t(255);
+  oz.partial = reinterpret_cast<double2*>(pp);
 }
 
 void ozaki_prep_bind(OzakiPrep& oz, void* base) {
-  uintptr_t b = (reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023);
-  oz.a_tiles = reinterpret_cast<unsigned char*>(b);
-  oz.b_tiles = oz.a_tiles + (size_t)oz.n_row_blocks * 2 * oz.kt * kOperandBytes;
-  uintptr_t pp = reinterpret_cast<uintptr_t>(oz.b_tiles + (size_t)oz.n_col_blocks * 2 * oz.kt * kOperandBytes);
-  pp = (pp + 255) & ~uintptr_t(255);
-  oz.partial = reinterpret_cast<double2*>(pp);
+  ozaki_bind(oz, base, static_cast<char*>(base) + ozaki_tile_bytes(oz));
 }
 
 cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s) {

@@ -32,8 +32,13 @@ struct OzakiPrep {
 // Work sizing and buffers of the split-BF16 form (partials + slices).
 void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid);
 int ozaki_max_segments();
-size_t ozaki_prep_bytes(const OzakiPrep& oz);
+size_t ozaki_prep_bytes(const OzakiPrep& oz);  // slice images + partials
+size_t ozaki_tile_bytes(const OzakiPrep& oz);   // slice images (1024-aligned inside)
+size_t ozaki_partial_bytes(const OzakiPrep& oz);
 void ozaki_prep_bind(OzakiPrep& oz, void* base);
+// Slice images and partials in separate buffers (images may be a workspace
+// shared by plans that run one after another on one stream).
+void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial);
 cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s);
 cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& oz, int grid,
                               cudaStream_t s);

@@ -9,8 +9,12 @@ namespace sigma {
 
 // Plan over an already validated column map (igp_of[my_igp] in [0, ncouls),
 // or -1 for a column left out of every sum).
+// shared_tiles (split-BF16 form only): a workspace of at least
+// ff_plan_tile_bytes() holding the slice images instead of the plan's own
+// allocation, for plans that run one after another on one stream.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
-                  const std::vector<int>& igp_of, int mode);
+                  const std::vector<int>& igp_of, int mode, void* shared_tiles = nullptr);
+int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes);
 
 // sigma_ff_execute with the column weight vfac * vcoul[igp] (vcoul a device
 // array, or nullptr for weight 1).

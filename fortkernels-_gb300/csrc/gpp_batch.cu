@@ -7,6 +7,12 @@
 // the concatenation of every instance's work items; per-instance pre-passes
 // (mixed form) and the fixed-order reductions run around them, and the whole
 // sequence is captured once in a CUDA graph and replayed.
+//
+// The tensor form (SIGMA_PREC_TENSOR) runs each instance's band sum as its
+// own split-BF16 contraction (frequency factors, slicing, tcgen05 GEMM) in
+// stream order, the instances sharing one factor buffer and one slice
+// workspace sized for the largest; the occupied-band pass and the
+// reductions stay batched.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -14,6 +20,7 @@
 #include "sigma_gpp.h"
 #include "sigma_internal.cuh"
 #include "gpp_batch.cuh"
+#include "ff_plan.h"
 #include "runtime.h"
 
 namespace sigma {
@@ -36,6 +43,11 @@ struct sigma_gpp_batch_s {
   int* counters = nullptr;  // [0] main pass, [1] occupied-band pass, [2] status
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // tensor form
+  std::vector<sigma_ff_plan> ff;   // per instance (3 slabs, GPP column map)
+  void* tensor_ws = nullptr;       // shared: factors Y[3][ng][nc] then the slice images
+  double2* yfac = nullptr;
+  void* tiles = nullptr;
 };
 
 namespace sigma {
@@ -85,10 +97,13 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   if (!out || !inst) return SIGMA_ERR_NULL;
   *out = nullptr;
   if (n_instances <= 0) return SIGMA_ERR_INVALID_SHAPE;
-  if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED) return SIGMA_ERR_UNSUPPORTED;
-  const bool mixed = precision == SIGMA_PREC_MIXED;
+  if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED && precision != SIGMA_PREC_TENSOR)
+    return SIGMA_ERR_UNSUPPORTED;
+  const bool tensor = precision == SIGMA_PREC_TENSOR;
+  const bool mixed = precision == SIGMA_PREC_MIXED || tensor;  // the tensor form keeps the mixed pre-pass
   bool all_shared = true;
   for (int i = 0; i < n_instances; ++i) all_shared = all_shared && inst[i].wx_band_stride == 0;
+  if (tensor && !all_shared) return SIGMA_ERR_UNSUPPORTED;  // needs one frequency set per instance
   std::vector<std::vector<int>> igp(n_instances);
   long long terms = 0;
   for (int i = 0; i < n_instances; ++i) {
@@ -271,6 +286,40 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   if (b->sch_grid > v.total) b->sch_grid = std::max(1, v.total);
   if (b->ssx_grid > b->ssx_view.total) b->ssx_grid = std::max(1, b->ssx_view.total);
   b->launches = (mixed ? 2 * n_instances : 0) + 1 + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
+  if (tensor) {
+    // one factor buffer and one slice workspace, each sized for the largest instance
+    size_t ybytes = 0, tbytes = 0;
+    for (int i = 0; i < n_instances; ++i) {
+      ybytes = std::max(ybytes, sizeof(double2) * 3 * (size_t)inst[i].ngpown * inst[i].ncouls);
+      size_t tb = 0;
+      int st = ff_plan_tile_bytes(inst[i].number_bands, inst[i].ncouls, inst[i].ngpown, kNW, &tb);
+      if (st != SIGMA_OK) {
+        sigma_gpp_batch_destroy(b);
+        return st;
+      }
+      tbytes = std::max(tbytes, tb);
+    }
+    cudaError_t e2 = cudaMalloc(&b->tensor_ws, up256(ybytes) + tbytes);
+    if (e2 != cudaSuccess) {
+      cudaGetLastError();
+      set_last_cuda_error(e2, "cudaMalloc(batch tensor workspace)", __LINE__);
+      sigma_gpp_batch_destroy(b);
+      return SIGMA_ERR_ALLOC;
+    }
+    b->yfac = static_cast<double2*>(b->tensor_ws);
+    b->tiles = static_cast<char*>(b->tensor_ws) + up256(ybytes);
+    b->ff.assign(n_instances, nullptr);
+    for (int i = 0; i < n_instances; ++i) {
+      int st = ff_plan_build(&b->ff[i], inst[i].number_bands, inst[i].ncouls, inst[i].ngpown, kNW, igp[i],
+                             SIGMA_FF_OZAKI_BF16, b->tiles);
+      if (st != SIGMA_OK) {
+        sigma_gpp_batch_destroy(b);
+        return st;
+      }
+    }
+    // per instance: pre-pass (2), factors, slicing (2), GEMM, its reduction; then ssx and reductions
+    b->launches = 7 * n_instances + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
+  }
   *out = b;
   return SIGMA_OK;
 }
@@ -282,23 +331,36 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   SIGMA_CUDA_TRY(cudaGetDevice(&dev));
   if (dev != b->device) return SIGMA_ERR_UNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const bool mixed = b->precision == SIGMA_PREC_MIXED;
+  const bool tensor = b->precision == SIGMA_PREC_TENSOR;
+  const bool mixed = b->precision == SIGMA_PREC_MIXED || tensor;
   SIGMA_CUDA_TRY(cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), s));
   if (mixed)
     for (int i = 0; i < b->n; ++i)
-      if (b->sch[i].n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->sch[i], b->prep[i], s));
-  if (b->sch_view.total > 0)
+      if (b->sch[i].n_items > 0 && (!tensor || b->ssx[i].n_items > 0))
+        SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->sch[i], b->prep[i], s));
+  if (tensor) {
+    for (int i = 0; i < b->n; ++i) {
+      SIGMA_CUDA_TRY(launch_gpp_y_factor(b->dev[i], b->yfac, s));
+      const int st = ff_execute_weighted(b->ff[i], reinterpret_cast<const sigma_complex128*>(b->yfac),
+                                         b->inst[i].aqsntemp, b->inst[i].aqsmtemp, b->inst[i].vcoul, 0.5,
+                                         reinterpret_cast<sigma_complex128*>(b->acht_n1[i]), stream);
+      if (st != SIGMA_OK) return st;
+    }
+  } else if (b->sch_view.total > 0)
     SIGMA_CUDA_TRY(mixed ? launch_sch_mixed_batch(b->sch_view, b->sch_grid, s)
                          : (b->all_shared_wx ? launch_sch_fp64y_batch(b->sch_view, b->sch_grid, s)
                                              : launch_sch_fp64_batch(b->sch_view, b->sch_grid, s)));
   if (b->ssx_view.total > 0)
     SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed_batch(b->ssx_view, b->ssx_grid, b->all_shared_wx, s)
                          : launch_ssx_fp64_batch(b->ssx_view, b->ssx_grid, s));
-  for (int i = 0; i < b->n; ++i)
-    SIGMA_CUDA_TRY(launch_gpp_reduce(b->sch[i], b->ssx[i], b->dev[i].nb, b->acht_n1[i],
+  for (int i = 0; i < b->n; ++i) {
+    GppWork main = b->sch[i];
+    if (tensor) main.partial = nullptr;  // band sums already in acht_n1
+    SIGMA_CUDA_TRY(launch_gpp_reduce(main, b->ssx[i], b->dev[i].nb, b->acht_n1[i],
                                      reinterpret_cast<double2*>(b->inst[i].achtemp),
                                      reinterpret_cast<double2*>(b->inst[i].asxtemp),
                                      reinterpret_cast<double2*>(b->inst[i].acht_n1_loc), s));
+  }
   return SIGMA_OK;
 }
 
@@ -341,6 +403,8 @@ extern "C" int sigma_gpp_batch_status(sigma_gpp_batch b, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   SIGMA_CUDA_TRY(cudaMemcpyAsync(&st, b->counters + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
   SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+  for (sigma_ff_plan f : b->ff)
+    if (st == SIGMA_OK) st = sigma_ff_plan_status(f, stream);
   return st;
 }
 
@@ -351,6 +415,9 @@ extern "C" int sigma_gpp_batch_destroy(sigma_gpp_batch b) {
   cudaSetDevice(b->device);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
+  for (sigma_ff_plan f : b->ff)
+    if (f) sigma_ff_plan_destroy(f);
+  if (b->tensor_ws) cudaFree(b->tensor_ws);
   if (b->block) cudaFree(b->block);
   cudaSetDevice(cur);
   delete b;

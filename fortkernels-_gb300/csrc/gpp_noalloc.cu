@@ -127,9 +127,10 @@ extern "C" int sigma_gpp_fp64_noalloc(int number_bands, int nvband, int ncouls, 
   if (sms <= 0) return SIGMA_ERR_NO_DEVICE;
 
   GppWork sch{}, ssx{};
-  int sch_grid = sms * sch_blocks_per_sm_fp64();
+  // wx_array is one frequency set for every band: the shared-factor main pass
+  int sch_grid = sms * sch_blocks_per_sm_fp64y();
   int ssx_grid = sms * ssx_blocks_per_sm_fp64();
-  size_pass(sch, number_bands, kBN, kBP, ncouls, ngpown, sch_grid, kNoAllocItemsPerSlot);
+  size_pass(sch, number_bands, kBNY, kBPY, ncouls, ngpown, sch_grid, kNoAllocItemsPerSlot);
   size_pass(ssx, nvband, kSsxBN, kSsxColumns, ncouls, ngpown, ssx_grid, 8);
   if (sch.n_items < sch_grid) sch_grid = sch.n_items;
   if (ssx.n_items < ssx_grid) ssx_grid = ssx.n_items;
@@ -139,7 +140,7 @@ extern "C" int sigma_gpp_fp64_noalloc(int number_bands, int nvband, int ncouls, 
   const size_t o_igp = 256;
   const size_t o_n1 = o_igp + up256(sizeof(int) * ngpown);
   const size_t o_sch = o_n1 + up256(sizeof(double2) * (size_t)(number_bands + nvband) * kNW);
-  const size_t o_ssx = o_sch + up256(sizeof(double2) * (size_t)sch.n_items * kBN * kNW);
+  const size_t o_ssx = o_sch + up256(sizeof(double2) * (size_t)sch.n_items * kBNY * kNW);
   const size_t need = o_ssx + up256(sizeof(double2) * (size_t)ssx.n_items * kSsxBN * kNW);
   if (need > kNoAllocScratchBytes) {
     set_last_error_text("sigma_gpp_fp64_noalloc: problem needs more than the 32 MiB static scratch");
@@ -177,7 +178,7 @@ extern "C" int sigma_gpp_fp64_noalloc(int number_bands, int nvband, int ncouls, 
   p.wx = wx_array;
   p.igp_of = reinterpret_cast<const int*>(base + o_igp);
 
-  if (sch.n_items > 0) SIGMA_CUDA_TRY(launch_sch_fp64(p, sch, sch_grid, s));
+  if (sch.n_items > 0) SIGMA_CUDA_TRY(launch_sch_fp64y(p, sch, sch_grid, s));
   if (ssx.n_items > 0) SIGMA_CUDA_TRY(launch_ssx_fp64(p, ssx, ssx_grid, s));
   SIGMA_CUDA_TRY(launch_gpp_reduce(sch, ssx, number_bands, acht_n1,
                                    reinterpret_cast<double2*>(achtemp),

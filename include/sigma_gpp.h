@@ -162,7 +162,11 @@ typedef struct sigma_gpp_batch_s* sigma_gpp_batch;
  * 5 = 32 x 32; otherwise the per-band kernel: 0 = 32 x 32, 1 = 16 x 64,
  * 2 = 64 x 16.  A tile of the other family is SIGMA_ERR_UNSUPPORTED.  The
  * tuning table of fortkernels-_gb300/autotune.py chooses per shape class.
- * The mixed form has one tile shape. */
+ * The mixed form has one tile shape.  precision SIGMA_PREC_TENSOR needs one
+ * frequency set per instance and ngpown >= ~18 (SIGMA_ERR_UNSUPPORTED
+ * otherwise): each instance's band sum runs as its own split-BF16
+ * contraction in stream order, sharing one workspace sized for the largest
+ * instance; the occupied-band pass and reductions stay batched. */
 int sigma_gpp_batch_create(sigma_gpp_batch* batch, int n_instances, const sigma_gpp_instance* inst,
                            int precision, const int* tile_shape);
 

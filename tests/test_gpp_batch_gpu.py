@@ -157,6 +157,31 @@ def test_batch_shared_frequency_tiles_match_oracle(sigma_lib, small_set, tile):
     assert e.value.status == -8
 
 
+def test_batch_tensor_matches_oracle(sigma_lib, small_set):
+    """Tensor form: the shared-frequency instances with enough columns for
+    the contraction tiles; same error model as the FP32 path."""
+    xs, oracles, abs2 = small_set
+    keep = [k for k, x in enumerate(xs) if x.wx_stride == 0 and x.prob.ngpown >= 20]
+    b = sigma_lib.GppBatch([xs[k].as_dict() for k in keep], precision=sigma_lib.PREC_TENSOR)
+    s = torch.cuda.Stream()
+    b.launch_graph(s.cuda_stream)
+    s.synchronize()
+    assert b.status(s.cuda_stream) == 0
+    first = [xs[k].outputs() for k in keep]
+    for k, g in zip(keep, first):
+        _check(g, oracles[k], 1, abs2[k])
+    b.launch_graph(s.cuda_stream)   # replay: bit-identical
+    s.synchronize()
+    for k, g in zip(keep, first):
+        for u, v in zip(xs[k].outputs(), g):
+            assert np.array_equal(u, v)
+    b.close()
+    small = [k for k, x in enumerate(xs) if x.prob.ngpown < 18]
+    with pytest.raises(sigma_lib.SigmaError) as e:
+        sigma_lib.GppBatch([xs[k].as_dict() for k in small], precision=sigma_lib.PREC_TENSOR)
+    assert e.value.status == -8
+
+
 def test_batch_mixed_tiles_in_one_queue(sigma_lib, small_set):
     xs, oracles, _ = small_set
     tiles = [k % 3 for k in range(len(xs))]
@@ -259,14 +284,15 @@ def test_batch48_fp64_equals_single_plans_and_oracle(sigma_lib, batch48):
     b.close()
 
 
-def test_batch48_mixed_within_bar_of_fp64(sigma_lib, batch48):
+@pytest.mark.parametrize("prec", [1, 2], ids=["mixed", "tensor"])
+def test_batch48_within_bar_of_fp64(sigma_lib, batch48, prec):
     xs = batch48
     b64 = sigma_lib.GppBatch([x.as_dict() for x in xs], precision=0)
     b64.execute()
     assert b64.status() == 0
     g64 = [x.outputs() for x in xs]
     b64.close()
-    bmx = sigma_lib.GppBatch([x.as_dict() for x in xs], precision=1)
+    bmx = sigma_lib.GppBatch([x.as_dict() for x in xs], precision=prec)
     bmx.execute()
     assert bmx.status() == 0
     gmx = [x.outputs() for x in xs]

@@ -169,7 +169,8 @@ def test_batch_validation_precedes_device_work(libpath):
     assert create([good, dict(good, ngpown=65, inv_igp_index=np.arange(65, dtype=np.int32))]) == -1
     assert create([good, dict(good, inv_igp_index=np.array([16, 32, 65, 64], np.int32))]) == -2
     assert create([good, dict(good, aqsntemp=None)]) == -6
-    assert create([good], prec=2) == -8
+    assert create([good], prec=3) == -8
+    assert create([good, dict(good, wx_band_stride=3)], prec=2) == -8   # tensor needs shared frequencies
     assert create([good, good], tiles=[0, 5]) == -8
     assert create([dict(good, wx_band_stride=2)]) == -1
     assert create([good, good], tiles=[1, -1]) == -8   # per-band-kernel tile, shared frequencies
