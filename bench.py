@@ -257,9 +257,8 @@ def timed(torch, dist, world, fn, steps, stream):
         dist.barrier()
     ms = e0.elapsed_time(e1)
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        import replicas
+        ms = replicas.max_over_ranks(ms, dist)
     return ms
 
 
@@ -519,8 +518,14 @@ def run_ours(args, rank, world, local_rank):
         if rank == 0:
             print(json.dumps({"batched": res}), flush=True)
         return 0
+    if args.only_ff:
+        res = run_ff(S, W, torch, dist, world, stream, sptr, args)
+        if rank == 0:
+            print(json.dumps({"ff": res}), flush=True)
+        return 0
     fp64_peak, fp32_peak = S.measure_fma_peaks(sptr)
-    inst = Instance(S, W, torch, seed=1 + rank)
+    import replicas
+    inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
     plan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_FP64)
     valid, terms = plan.info()
 
@@ -729,6 +734,10 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-static", action="store_true")
     ap.add_argument("--no-real", action="store_true")
+    ap.add_argument("--ff-shape", default=None,
+                    help="number_bands,ncouls,ngpown,nfreq of the FF runs (default the production "
+                         "512,16384,820,15; smaller only for profiling captures)")
+    ap.add_argument("--only-ff", action="store_true", help="run the FF contraction alone (profiling)")
     ap.add_argument("--batch-instances", type=int, default=48,
                     help="leading instances of the 48-instance batched set (fewer only for profiling)")
     ap.add_argument("--batch-fp64-steps", type=int, default=2)
@@ -739,6 +748,9 @@ def main():
                          "for profiling captures)")
     args = ap.parse_args()
     set_bands(args.bands)
+    if args.ff_shape:
+        global FF_SHAPE
+        FF_SHAPE = tuple(int(x) for x in args.ff_shape.split(","))
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
