@@ -416,6 +416,37 @@ def run_real(S, W, torch, dist, world, stream, sptr, args):
     return res
 
 
+def run_halfsum(S, W, torch, dist, world, stream, sptr, args, inst):
+    """gppsum = 1 half sum (gppKerSeq.cpp) on the production instance's device
+    arrays, FP64: Gterms/s of the band sums (terms = bands x sum over valid
+    columns of igp x 3, the (n1, my_igp, ig < igp, iw) iterations of the
+    reference's loop), and the step time with the static remainder."""
+    f64 = dict(dtype=torch.float64, device="cuda")
+    igp = np.array([NC - 1 if i == NC else int(inst.indinv[i]) for i in inst.inv])
+    igp = igp[igp >= 0]
+    terms = NB * int(igp.sum()) * 3
+    ach, asx, n1, st = (torch.zeros(6, **f64), torch.zeros(6, **f64), torch.zeros(2 * NB, **f64),
+                        torch.zeros(2, **f64))
+    res = {"workload": f"gppsum=1 half sum, {NB} bands x {NG} columns x g-vectors below igp "
+                       f"(of {NC}) x 3 frequencies, FP64, band-major device arrays",
+           "unit": UNIT, "terms_per_step": terms}
+    for flags, key in ((0, "sums"), (S.HALFSUM_STATIC, "with_static")):
+        plan = S.GppHalfSumPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, flags=flags)
+        run = lambda: plan.execute(inst.wx, inst.aqsm, inst.aqsn, inst.ieps, inst.wt, inst.vcoul, ach, asx,
+                                   n1, st if flags else None, stream=sptr)
+        for _ in range(max(1, min(args.warmup, 2))):
+            run()
+        steps = 3
+        ms = timed(torch, dist, world, run, steps, stream)
+        plan.close()
+        if key == "sums":
+            res["value"] = round(terms * world / (ms / steps * 1e-3) / 1e9, 4)
+            res["ms_per_step"] = round(ms / steps, 3)
+        else:
+            res["with_static_ms_per_step"] = round(ms / steps, 3)
+    return res
+
+
 def run_static(S, W, torch, dist, world, stream, sptr, inst):
     """Static remainder (sigma_gpp_static_execute) on the production
     instance's device arrays: both contraction forms, FP64-equivalent TF/s
@@ -610,6 +641,7 @@ def run_ours(args, rank, world, local_rank):
                   "acht_n1_loc_normwise": float(np.linalg.norm(tensor_out[2] - fp64_out[2]) /
                                                 np.linalg.norm(fp64_out[2]))}
     static = None if args.no_static else run_static(S, W, torch, dist, world, stream, sptr, inst)
+    half = None if args.no_halfsum else run_halfsum(S, W, torch, dist, world, stream, sptr, args, inst)
     cpu_prob = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # host copy of the instance for the CPU baseline: trailing bands + all columns
@@ -706,6 +738,7 @@ def run_ours(args, rank, world, local_rank):
         "batched": batch,
         "static_remainder": static,
         "real": real,
+        "halfsum": half,
         "peaks_measured": {"fp64_fma_probe_tflops": round(fp64_peak, 4),
                            "fp32_fma_probe_tflops": round(fp32_peak, 3),
                            "fp64_pipe_tflops_at_clock": round(fp64_pipe_peak, 4),
@@ -734,6 +767,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-static", action="store_true")
     ap.add_argument("--no-real", action="store_true")
+    ap.add_argument("--no-halfsum", action="store_true")
     ap.add_argument("--ff-shape", default=None,
                     help="number_bands,ncouls,ngpown,nfreq of the FF runs (default the production "
                          "512,16384,820,15; smaller only for profiling captures)")

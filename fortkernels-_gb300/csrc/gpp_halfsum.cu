@@ -1,0 +1,768 @@
+// gppsum = 1 ("half sum") GPP variant of gppKerSeq.cpp, FP64.
+//
+// For column my_igp (igp = its mapped g-vector) and band n1 the reference
+// sums over g-vectors ig < igp only, pairing each term with its Hermitian
+// partner:
+//   term = conj(aqsm[n1][igp]) aqsn[n1][ig] Z + v_p conj(aqsm[n1][ig]) conj(Z)
+// so with T = sum aqsn[n1][ig] Z and U = sum aqsm[n1][ig] Z over the column's
+// g-vector set,  scht = conj(aqsm[n1][igp]) T + v_p conj(U).
+//
+//   non-occupied bands (noflagOCC_solver, gppKerSeq.cpp:206-242, driven in
+//     512-wide blocks at :457-470): Z = delw I_eps with delw = wtilde / wdiff,
+//     kept where |wdiff|^2 < 0.25 or |delw|^2 > limitone (the complement of
+//     the gppsum = 0 guard), v_p = aqsm[n1][igp].  The block loop visits
+//     g-vectors ig < igp - 1 with ig mod 512 != 511, plus ig = igp alone
+//     (no partner term) when igp is a positive multiple of 512.
+//   static remainder (reduce_achstemp, gppKerSeq.cpp:13-72): Z = -I_eps over
+//     ig < igp, v_p = aqsn[n1][igp], plus ig = igp alone when |I_eps| > to1.
+//   occupied bands (flagOCC_solver, gppKerSeq.cpp:90-139): per g-vector
+//     sch = G / (wx - wtilde) unless |wx - wtilde| < 0.5 or |delw|^2 < to1
+//     (delw = (wx - wtilde) / (2 wtilde)), ssx = Omega2 / (wx^2 - wtilde^2) or
+//     -G / (2 (wx + wtilde)) (= -Omega2 / (4 wtilde^2 (1 + delw))); the loop
+//     stops at the first g-vector with |Omega2| < to1; the term at
+//     ig = igp - 1 has no partner.
+//
+// Z does not depend on the band (one frequency set for every band), so the
+// non-occupied pass and the static remainder are two complex FP64 GEMMs over
+// a triangular g-vector range: items of 32 bands x 32 columns x a g-vector
+// split stage Z once per 16-g-vector chunk for all 32 bands; each thread
+// keeps 2 bands x 2 columns x NF frequencies of T and U (8 DFMA per term).
+// Items past a column block's range write zero partials.  Occupied bands run
+// one CTA per (column, frequency).  All partials have fixed slots and are
+// summed in a fixed order with compensation: results are identical run to
+// run.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "sigma_gpp.h"
+#include "sigma_internal.cuh"
+#include "runtime.h"
+
+namespace sigma {
+namespace {
+
+constexpr int kHBN = 32, kHBP = 32;  // bands x columns per item
+constexpr int kHCK = 16;             // g-vectors per staged chunk
+constexpr int kHTB = kHBN / 16, kHTC = kHBP / 16;
+constexpr int kOccBands = 4;         // occupied bands per accumulation pass
+constexpr int kIgBlk = 512;          // g-vector block of the reference's loop
+
+struct HalfDev {
+  int nb, nvband, nc, ng;
+  double occ;
+  const double2 *aqsm, *aqsn, *ieps, *wt;  // [nb][nc], [nb][nc], [ng][nc], [ng][nc]
+  const double* vcoul;                     // [nc]
+  const double* wx;                        // [3]
+  const int* igp_of;                       // [ng], -1 = skipped column
+  const int* brk;                          // [ng] occupied-band cut
+};
+
+template <int NF>
+struct HalfSmem {
+  double2 z[kHCK][NF][kHBP];
+  double2 n[kHCK][kHBN];
+  double2 m[kHCK][kHBN];
+};
+
+__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
+  acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+
+// End of the (non-diagonal) g-vector range of a column: [0, lim).
+template <int NF>
+__device__ __forceinline__ int column_limit(int igp) {
+  if (igp < 0) return 0;
+  return NF == 1 ? igp : max(igp - 1, 0);
+}
+
+// Z of the non-occupied half sum at one (column, g-vector) for the three
+// frequencies: G (c + i b) / (c^2 + b^2), G = I_eps wtilde, c = wx - Re wtilde,
+// b = Im wtilde (= delw I_eps), kept where |wdiff|^2 is below the threshold.
+__device__ __forceinline__ void half_factor(double2 wt, double2 ie, const double* wx,
+                                            double2 (&z)[3]) {
+  const double a = wt.x, b = wt.y;
+  const double b2 = guard_b2(b);
+  const double thr = guard_thr(a, b2);
+  const double2 g = cmul(ie, wt);
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    const double c = __dsub_rn(wx[f], a);
+    const double wv = fma(c, c, b2);
+    const double r = rcp_f64_seed32(wv);
+    const double2 y = make_double2(fma(g.x, c, -g.y * b) * r, fma(g.x, b, g.y * c) * r);
+    z[f] = gt_nonneg(thr, wv) ? y : make_double2(0.0, 0.0);
+  }
+}
+
+template <int NF>
+__global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWork w) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  HalfSmem<NF>& sm = *reinterpret_cast<HalfSmem<NF>*>(smem_raw);
+  __shared__ int s_item, s_kmax;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const double wx[3] = {p.wx[0], p.wx[1], p.wx[2]};
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(w.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= w.n_items) break;
+    const ItemCoord ic = decode_item(w, item);
+    const int n1_0 = w.band_begin + ic.bb * kHBN, p0 = ic.cb * kHBP;
+    if (tid < 32) {
+      const int col = p0 + tid;
+      const int lim = column_limit<NF>(col < p.ng ? p.igp_of[col] : -1);
+      const int mx = __reduce_max_sync(0xffffffffu, lim);
+      if (tid == 0) s_kmax = mx;
+    }
+    __syncthreads();
+    const int ig_begin = ic.s * w.split_len;
+    const int ig_end = min(min(ig_begin + w.split_len, p.nc), s_kmax);
+
+    double2 T[kHTB][kHTC][NF], U[kHTB][kHTC][NF];
+#pragma unroll
+    for (int i = 0; i < kHTB; ++i)
+#pragma unroll
+      for (int j = 0; j < kHTC; ++j)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) T[i][j][f] = U[i][j][f] = make_double2(0.0, 0.0);
+
+    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kHCK) {
+      __syncthreads();
+      for (int e = tid; e < kHCK * kHBP; e += kThreads) {
+        const int k = e % kHCK, pl = e / kHCK;
+        const int ig = ig0 + k, col = p0 + pl;
+        const int lim = column_limit<NF>(col < p.ng ? p.igp_of[col] : -1);
+        bool in = ig < ig_end && ig < lim;
+        if (NF == 3) in = in && (ig % kIgBlk) != kIgBlk - 1;
+        double2 z[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+        if (in) {
+          const size_t off = (size_t)col * p.nc + ig;
+          const double2 ie = p.ieps[off];
+          if (NF == 1)
+            z[0] = make_double2(-ie.x, -ie.y);
+          else
+            half_factor(p.wt[off], ie, wx, z);
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f) sm.z[k][f][pl] = z[f];
+      }
+      for (int e = tid; e < kHCK * kHBN; e += kThreads) {
+        const int k = e % kHCK, bl = e / kHCK;
+        const int ig = ig0 + k, n1 = n1_0 + bl;
+        const bool in = ig < ig_end && n1 < p.nb;
+        const size_t off = (size_t)n1 * p.nc + ig;
+        sm.n[k][bl] = in ? p.aqsn[off] : make_double2(0.0, 0.0);
+        sm.m[k][bl] = in ? p.aqsm[off] : make_double2(0.0, 0.0);
+      }
+      __syncthreads();
+#pragma unroll 2
+      for (int k = 0; k < kHCK; ++k) {
+        double2 nn[kHTB], mm[kHTB], z[kHTC][NF];
+#pragma unroll
+        for (int i = 0; i < kHTB; ++i) {
+          nn[i] = sm.n[k][ty + 16 * i];
+          mm[i] = sm.m[k][ty + 16 * i];
+        }
+#pragma unroll
+        for (int j = 0; j < kHTC; ++j)
+#pragma unroll
+          for (int f = 0; f < NF; ++f) z[j][f] = sm.z[k][f][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < kHTB; ++i)
+#pragma unroll
+          for (int j = 0; j < kHTC; ++j)
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+              cfma(T[i][j][f], nn[i], z[j][f]);
+              cfma(U[i][j][f], mm[i], z[j][f]);
+            }
+      }
+    }
+    // epilogue: 0.5 vcoul (conj(aqsm_p) T + v_p conj(U)) [+ the diagonal term
+    // in the first split], half-warp butterfly over the columns
+#pragma unroll
+    for (int i = 0; i < kHTB; ++i) {
+      const int bl = ty + 16 * i, n1 = n1_0 + bl;
+      double2 part[NF];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) part[f] = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int j = 0; j < kHTC; ++j) {
+        const int col = p0 + tx + 16 * j;
+        const int igp = col < p.ng ? p.igp_of[col] : -1;
+        if (n1 < p.nb && igp >= 0) {
+          const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+          const double2 an = p.aqsn[(size_t)n1 * p.nc + igp];
+          const double2 vp = NF == 1 ? an : am;
+          const double wgt = 0.5 * p.vcoul[igp];
+          double2 val[NF];
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            val[f] = cmul(cconj(am), T[i][j][f]);
+            cfma(val[f], vp, cconj(U[i][j][f]));
+          }
+          if (ic.s == 0) {
+            const size_t off = (size_t)col * p.nc + igp;
+            const double2 d = cmul(cconj(am), an);
+            if (NF == 1) {
+              const double2 ie = p.ieps[off];
+              if (fma(ie.x, ie.x, ie.y * ie.y) > kTo1 * kTo1)
+                cfma(val[0], d, make_double2(-ie.x, -ie.y));
+            } else if (igp > 0 && igp % kIgBlk == 0) {
+              double2 z[3];
+              half_factor(p.wt[off], p.ieps[off], wx, z);
+#pragma unroll
+              for (int f = 0; f < NF; ++f) cfma(val[f], d, z[f]);
+            }
+          }
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            part[f].x = fma(wgt, val[f].x, part[f].x);
+            part[f].y = fma(wgt, val[f].y, part[f].y);
+          }
+        }
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+          part[f].x += __shfl_xor_sync(0xffffffffu, part[f].x, o);
+          part[f].y += __shfl_xor_sync(0xffffffffu, part[f].y, o);
+        }
+      if (tx == 0)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) w.partial[ic.pidx * kHBN * NF + bl * NF + f] = part[f];
+    }
+  }
+}
+
+// First g-vector of each column with |Omega2| < to1 (ncouls if none): the
+// occupied-band loop of the reference stops there (gppKerSeq.cpp:96).
+__global__ void __launch_bounds__(kThreads) half_brk_kernel(HalfDev p, int* brk) {
+  __shared__ int s_min;
+  const int col = blockIdx.x;
+  if (threadIdx.x == 0) s_min = p.nc;
+  __syncthreads();
+  int first = p.nc;
+  for (int ig = threadIdx.x; ig < p.nc; ig += kThreads) {
+    const size_t off = (size_t)col * p.nc + ig;
+    const double2 wt = p.wt[off];
+    const double2 w2 = make_double2(fma(wt.x, wt.x, -wt.y * wt.y), 2.0 * wt.x * wt.y);
+    const double2 om = cmul(w2, p.ieps[off]);
+    if (fma(om.x, om.x, om.y * om.y) < kTo1 * kTo1) {
+      first = ig;
+      break;
+    }
+  }
+  if (first < p.nc) atomicMin(&s_min, first);
+  __syncthreads();
+  if (threadIdx.x == 0) brk[col] = s_min;
+}
+
+// Occupied bands: one CTA per (column, frequency), threads over g-vectors,
+// kOccBands bands per pass.  Writes the column's contributions
+// 0.5 vcoul scht (achtemp) and occ vcoul ssxt (asxtemp) per band.
+__global__ void __launch_bounds__(kThreads) half_occ_kernel(HalfDev p, double2* occ_ach,
+                                                            double2* occ_asx) {
+  constexpr int kVals = kOccBands * 8;  // per band: T_sch, U_sch, T_ssx, U_ssx (complex)
+  __shared__ double red[kThreads / 32][kVals];
+  __shared__ double tot[kVals];
+  const int col = blockIdx.x, iw = blockIdx.y;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int igp = p.igp_of[col];
+  const double wx = p.wx[iw];
+  const int kend = igp >= 0 ? min(igp, p.brk[col]) : 0;
+  for (int g0 = 0; g0 < p.nvband; g0 += kOccBands) {
+    const int nbl = min(kOccBands, p.nvband - g0);
+    double acc[kVals];
+#pragma unroll
+    for (int v = 0; v < kVals; ++v) acc[v] = 0.0;
+    for (int ig = tid; ig < kend; ig += kThreads) {
+      const size_t off = (size_t)col * p.nc + ig;
+      const double2 wt = p.wt[off], ie = p.ieps[off];
+      const double a = wt.x, b = wt.y;
+      const double b2 = guard_b2(b);
+      const double2 g = cmul(ie, wt);
+      const double c = __dsub_rn(wx, a);
+      const double wv = fma(c, c, b2);
+      double2 sch = make_double2(0.0, 0.0), ssx = make_double2(0.0, 0.0);
+      if (gt_nonneg(guard_thr(a, b2), wv)) {
+        // |wx - wtilde| < gamma or |delw|^2 < to1: sch = 0
+        if (fma(a, a, b2) > kTo1 * kTo1) {
+          const double dr = wx + a;
+          const double r = rcp_f64(fma(dr, dr, b2));
+          // -G / (2 (wx + wtilde)) = -0.5 G conj(d) / |d|^2, d = (wx + a, b)
+          ssx = make_double2(-0.5 * r * fma(g.x, dr, g.y * b), -0.5 * r * fma(g.y, dr, -g.x * b));
+        }
+      } else {
+        const double r = rcp_f64(wv);
+        sch = make_double2(fma(g.x, c, -g.y * b) * r, fma(g.x, b, g.y * c) * r);
+        // Omega2 / (wx^2 - wtilde^2), Omega2 = wtilde^2 I_eps
+        const double2 w2 = make_double2(fma(a, a, -b2), 2.0 * a * b);
+        const double2 om = cmul(w2, ie);
+        const double2 d = make_double2(fma(wx, wx, -w2.x), -w2.y);
+        const double rd = rcp_f64(fma(d.x, d.x, d.y * d.y));
+        ssx = make_double2(fma(om.x, d.x, om.y * d.y) * rd, fma(om.y, d.x, -om.x * d.y) * rd);
+      }
+      const bool pair = ig != igp - 1;
+#pragma unroll
+      for (int q = 0; q < kOccBands; ++q)
+        if (q < nbl) {
+          const size_t bo = (size_t)(g0 + q) * p.nc + ig;
+          const double2 an = p.aqsn[bo];
+          double2 ts = make_double2(acc[8 * q + 0], acc[8 * q + 1]);
+          double2 tx2 = make_double2(acc[8 * q + 4], acc[8 * q + 5]);
+          cfma(ts, an, sch);
+          cfma(tx2, an, ssx);
+          acc[8 * q + 0] = ts.x;
+          acc[8 * q + 1] = ts.y;
+          acc[8 * q + 4] = tx2.x;
+          acc[8 * q + 5] = tx2.y;
+          if (pair) {
+            const double2 am = p.aqsm[bo];
+            double2 us = make_double2(acc[8 * q + 2], acc[8 * q + 3]);
+            double2 ux = make_double2(acc[8 * q + 6], acc[8 * q + 7]);
+            cfma(us, am, sch);
+            cfma(ux, am, ssx);
+            acc[8 * q + 2] = us.x;
+            acc[8 * q + 3] = us.y;
+            acc[8 * q + 6] = ux.x;
+            acc[8 * q + 7] = ux.y;
+          }
+        }
+    }
+    // fixed-order block reduction
+#pragma unroll
+    for (int v = 0; v < kVals; ++v) {
+      double x = acc[v];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0) red[warp][v] = x;
+    }
+    __syncthreads();
+    if (tid < kVals) {
+      double s = 0.0;
+      for (int q = 0; q < kThreads / 32; ++q) s += red[q][tid];
+      tot[tid] = s;
+    }
+    __syncthreads();
+    if (tid < nbl) {
+      const int n1 = g0 + tid;
+      double2 ach = make_double2(0.0, 0.0), asx = make_double2(0.0, 0.0);
+      if (igp >= 0) {
+        const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+        const double* t = tot + 8 * tid;
+        double2 scht = cmul(cconj(am), make_double2(t[0], t[1]));
+        cfma(scht, am, make_double2(t[2], -t[3]));
+        double2 ssxt = cmul(cconj(am), make_double2(t[4], t[5]));
+        cfma(ssxt, am, make_double2(t[6], -t[7]));
+        const double v = p.vcoul[igp];
+        ach = make_double2(0.5 * scht.x * v, 0.5 * scht.y * v);
+        asx = make_double2(ssxt.x * p.occ * v, ssxt.y * p.occ * v);
+      }
+      const size_t o = ((size_t)n1 * p.ng + col) * kNW + iw;
+      occ_ach[o] = ach;
+      occ_asx[o] = asx;
+    }
+    __syncthreads();
+  }
+}
+
+struct HalfReduceArgs {
+  int nb, nvband, ng;
+  const double2* main_part;  // non-occupied bands [nvband, nb), kNW per row
+  int main_count;            // column blocks x splits
+  const double2* stat_part;  // all bands, 1 per row (null without the static remainder)
+  int stat_count;
+  const double2* occ_ach;    // [nvband][ng][3]
+  const double2* occ_asx;
+  double2* acht_n1;  // [nb][3]
+  double2* asx_n1;   // [nvband][3]
+  double2* stat_n1;  // [nb]
+};
+
+// One warp per output row, fixed order, compensated.
+__global__ void half_reduce_bands_kernel(HalfReduceArgs a) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int n_ach = a.nb * kNW, n_asx = a.nvband * kNW, n_stat = a.stat_part ? a.nb : 0;
+  if (warp >= n_ach + n_asx + n_stat) return;
+  Comp sx, sy;
+  double2* dst;
+  if (warp < n_ach) {
+    const int n1 = warp / kNW, iw = warp % kNW;
+    if (n1 >= a.nvband) {
+      const int r = n1 - a.nvband, bb = r / kHBN, bl = r % kHBN;
+      for (int q = lane; q < a.main_count; q += 32) {
+        const double2 v = a.main_part[((size_t)bb * a.main_count + q) * kHBN * kNW + bl * kNW + iw];
+        sx.add(v.x);
+        sy.add(v.y);
+      }
+    } else {
+      for (int c = lane; c < a.ng; c += 32) {
+        const double2 v = a.occ_ach[((size_t)n1 * a.ng + c) * kNW + iw];
+        sx.add(v.x);
+        sy.add(v.y);
+      }
+    }
+    dst = a.acht_n1 + warp;
+  } else if (warp < n_ach + n_asx) {
+    const int e = warp - n_ach, n1 = e / kNW, iw = e % kNW;
+    for (int c = lane; c < a.ng; c += 32) {
+      const double2 v = a.occ_asx[((size_t)n1 * a.ng + c) * kNW + iw];
+      sx.add(v.x);
+      sy.add(v.y);
+    }
+    dst = a.asx_n1 + e;
+  } else {
+    const int n1 = warp - n_ach - n_asx, bb = n1 / kHBN, bl = n1 % kHBN;
+    for (int q = lane; q < a.stat_count; q += 32) {
+      const double2 v = a.stat_part[((size_t)bb * a.stat_count + q) * kHBN + bl];
+      sx.add(v.x);
+      sy.add(v.y);
+    }
+    dst = a.stat_n1 + n1;
+  }
+  const double rx = warp_sum_comp(sx), ry = warp_sum_comp(sy);
+  if (lane == 0) *dst = make_double2(rx, ry);
+}
+
+__global__ void half_reduce_total_kernel(const double2* acht_n1, const double2* asx_n1,
+                                         const double2* stat_n1, int nb, int nvband,
+                                         double2* achtemp, double2* asxtemp, double2* achstemp,
+                                         double2* acht_n1_loc) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < 2 * kNW + 1) {
+    Comp sx, sy;
+    if (warp < 2 * kNW) {
+      const bool ach = warp < kNW;
+      const int iw = ach ? warp : warp - kNW;
+      const double2* src = ach ? acht_n1 : asx_n1;
+      const int n = ach ? nb : nvband;
+      for (int n1 = lane; n1 < n; n1 += 32) {
+        sx.add(src[n1 * kNW + iw].x);
+        sy.add(src[n1 * kNW + iw].y);
+      }
+    } else if (achstemp) {
+      for (int n1 = lane; n1 < nb; n1 += 32) {
+        sx.add(stat_n1[n1].x);
+        sy.add(stat_n1[n1].y);
+      }
+    }
+    const double rx = warp_sum_comp(sx), ry = warp_sum_comp(sy);
+    if (lane == 0) {
+      if (warp < kNW)
+        achtemp[warp] = make_double2(rx, ry);
+      else if (warp < 2 * kNW)
+        asxtemp[warp - kNW] = make_double2(rx, ry);
+      else if (achstemp)
+        achstemp[0] = make_double2(rx, ry);
+    }
+  }
+  if (acht_n1_loc)
+    for (int n1 = threadIdx.x; n1 < nb; n1 += blockDim.x) acht_n1_loc[n1] = acht_n1[n1 * kNW + 2];
+}
+
+// [rows][cols] complex -> [cols][rows], 32 x 32 tiles through shared memory.
+__global__ void transpose_c128_kernel(const double2* __restrict__ src, double2* __restrict__ dst,
+                                      int rows, int cols) {
+  __shared__ double2 tile[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 rows per pass
+  for (int r = ty; r < 32; r += 8) {
+    const int rr = r0 + r, cc = c0 + tx;
+    if (rr < rows && cc < cols) tile[r][tx] = src[(size_t)rr * cols + cc];
+  }
+  __syncthreads();
+  for (int c = ty; c < 32; c += 8) {
+    const int cc = c0 + c, rr = r0 + tx;
+    if (rr < rows && cc < cols) dst[(size_t)cc * rows + rr] = tile[tx][c];
+  }
+}
+
+cudaError_t launch_transpose(const double2* src, double2* dst, int rows, int cols, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  const dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+  transpose_c128_kernel<<<grid, kThreads, 0, s>>>(src, dst, rows, cols);
+  return cudaGetLastError();
+}
+
+size_t up256(size_t v) { return (v + 255) / 256 * 256; }
+
+template <int NF>
+cudaError_t launch_half_main(const HalfDev& p, const GppWork& w, int grid, cudaStream_t s) {
+  constexpr int smem = (int)sizeof(HalfSmem<NF>);
+  cudaError_t e = cudaFuncSetAttribute(half_main_kernel<NF>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  half_main_kernel<NF><<<grid, kThreads, smem, s>>>(p, w);
+  return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace sigma
+
+struct sigma_gpp_halfsum_plan_s {
+  int device = 0, nb = 0, nvband = 0, nc = 0, ng = 0, flags = 0;
+  int main_grid = 0, stat_grid = 0;
+  sigma::GppWork wm{}, ws{};
+  void* block = nullptr;
+  int* igp_of = nullptr;
+  int* brk = nullptr;
+  int* counters = nullptr;
+  double2 *occ_ach = nullptr, *occ_asx = nullptr;
+  double2 *acht_n1 = nullptr, *asx_n1 = nullptr, *stat_n1 = nullptr;
+  double2 *t_aqsm = nullptr, *t_aqsn = nullptr, *t_ieps = nullptr, *t_wt = nullptr;
+};
+
+extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int number_bands,
+                                             int nvband, int ncouls, int ngpown, int nstart,
+                                             int nend, const int* inv_igp_index,
+                                             const int* indinv, int indinv_len, int flags) {
+  using namespace sigma;
+  if (!out || !inv_igp_index || !indinv) return SIGMA_ERR_NULL;
+  *out = nullptr;
+  if (flags & ~(SIGMA_HALFSUM_STATIC | SIGMA_HALFSUM_GVEC_MAJOR)) return SIGMA_ERR_UNSUPPORTED;
+  int st = gpp_check_shape(number_bands, nvband, ncouls, ngpown, nstart, nend);
+  if (st != SIGMA_OK) return st;
+  if (indinv_len < ncouls) return SIGMA_ERR_INVALID_SHAPE;
+  std::vector<int> igp_of;
+  int valid = 0;
+  st = gpp_map_columns(ncouls, ngpown, inv_igp_index, indinv, indinv_len, igp_of, valid);
+  if (st != SIGMA_OK) return st;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return SIGMA_ERR_NO_DEVICE;
+  }
+  const int sms = device_sm_count();
+  if (sms <= 0) return SIGMA_ERR_NO_DEVICE;
+  auto* p = new sigma_gpp_halfsum_plan_s();
+  p->device = dev;
+  p->nb = number_bands;
+  p->nvband = nvband;
+  p->nc = ncouls;
+  p->ng = ngpown;
+  p->flags = flags;
+  p->main_grid = p->stat_grid = sms;
+  // about half of the items fall past their column block's range (triangle)
+  gpp_size_work(p->wm, nvband, number_bands - nvband, kHBN, kHBP, ncouls, ngpown, p->main_grid, 48);
+  if (flags & SIGMA_HALFSUM_STATIC)
+    gpp_size_work(p->ws, 0, number_bands, kHBN, kHBP, ncouls, ngpown, p->stat_grid, 48);
+  if (p->wm.n_items < p->main_grid) p->main_grid = std::max(1, p->wm.n_items);
+  if (p->ws.n_items < p->stat_grid) p->stat_grid = std::max(1, p->ws.n_items);
+  const size_t nbc = (size_t)number_bands * ncouls, ngc = (size_t)ngpown * ncouls;
+  const size_t b_igp = up256(sizeof(int) * ngpown), b_brk = b_igp, b_cnt = 256;
+  const size_t b_occ = up256(sizeof(double2) * (size_t)nvband * ngpown * kNW);
+  const size_t b_n1 = up256(sizeof(double2) * (size_t)number_bands * kNW);
+  const size_t b_asx = up256(sizeof(double2) * (size_t)std::max(nvband, 1) * kNW);
+  const size_t b_st = up256(sizeof(double2) * (size_t)number_bands);
+  const size_t b_pm = up256(sizeof(double2) * (size_t)p->wm.n_items * kHBN * kNW);
+  const size_t b_ps = up256(sizeof(double2) * (size_t)p->ws.n_items * kHBN);
+  const size_t b_tr = (flags & SIGMA_HALFSUM_GVEC_MAJOR) ? up256(sizeof(double2) * nbc) * 2 +
+                                                               up256(sizeof(double2) * ngc) * 2
+                                                         : 0;
+  const size_t total = b_igp + b_brk + b_cnt + 2 * b_occ + b_n1 + b_asx + b_st + b_pm + b_ps + b_tr;
+  cudaError_t e = cudaMalloc(&p->block, total);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_last_cuda_error(e, "cudaMalloc(halfsum plan)", __LINE__);
+    delete p;
+    return SIGMA_ERR_ALLOC;
+  }
+  char* b = static_cast<char*>(p->block);
+  size_t off = 0;
+  auto take = [&](size_t n) {
+    char* r = b + off;
+    off += n;
+    return r;
+  };
+  p->igp_of = reinterpret_cast<int*>(take(b_igp));
+  p->brk = reinterpret_cast<int*>(take(b_brk));
+  p->counters = reinterpret_cast<int*>(take(b_cnt));
+  p->occ_ach = reinterpret_cast<double2*>(take(b_occ));
+  p->occ_asx = reinterpret_cast<double2*>(take(b_occ));
+  p->acht_n1 = reinterpret_cast<double2*>(take(b_n1));
+  p->asx_n1 = reinterpret_cast<double2*>(take(b_asx));
+  p->stat_n1 = reinterpret_cast<double2*>(take(b_st));
+  p->wm.partial = reinterpret_cast<double2*>(take(b_pm));
+  p->ws.partial = (flags & SIGMA_HALFSUM_STATIC) ? reinterpret_cast<double2*>(take(b_ps)) : nullptr;
+  if (flags & SIGMA_HALFSUM_GVEC_MAJOR) {
+    p->t_aqsm = reinterpret_cast<double2*>(take(up256(sizeof(double2) * nbc)));
+    p->t_aqsn = reinterpret_cast<double2*>(take(up256(sizeof(double2) * nbc)));
+    p->t_ieps = reinterpret_cast<double2*>(take(up256(sizeof(double2) * ngc)));
+    p->t_wt = reinterpret_cast<double2*>(take(up256(sizeof(double2) * ngc)));
+  }
+  p->wm.counter = p->counters;
+  p->ws.counter = p->counters + 1;
+  e = cudaMemcpy(p->igp_of, igp_of.data(), sizeof(int) * ngpown, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "cudaMemcpy(halfsum igp_of)", __LINE__);
+    cudaFree(p->block);
+    delete p;
+    return SIGMA_ERR_CUDA;
+  }
+  *out = p;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_halfsum_plan_destroy(sigma_gpp_halfsum_plan p) {
+  if (!p) return SIGMA_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(p->device);
+  if (p->block) cudaFree(p->block);
+  cudaSetDevice(cur);
+  delete p;
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const double* wx_array,
+                                         double occ, const sigma_complex128* aqsmtemp,
+                                         const sigma_complex128* aqsntemp,
+                                         const sigma_complex128* I_eps_array,
+                                         const sigma_complex128* wtilde_array,
+                                         const double* vcoul, sigma_complex128* achtemp,
+                                         sigma_complex128* asxtemp, sigma_complex128* acht_n1_loc,
+                                         sigma_complex128* achstemp, void* stream) {
+  using namespace sigma;
+  if (!plan) return SIGMA_ERR_NULL;
+  if (!wx_array || !aqsmtemp || !aqsntemp || !I_eps_array || !wtilde_array || !vcoul || !achtemp ||
+      !asxtemp)
+    return SIGMA_ERR_NULL;
+  if (achstemp && !(plan->flags & SIGMA_HALFSUM_STATIC)) return SIGMA_ERR_UNSUPPORTED;
+  int dev = 0;
+  SIGMA_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != plan->device) return SIGMA_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const double2* aqsm = reinterpret_cast<const double2*>(aqsmtemp);
+  const double2* aqsn = reinterpret_cast<const double2*>(aqsntemp);
+  const double2* ieps = reinterpret_cast<const double2*>(I_eps_array);
+  const double2* wt = reinterpret_cast<const double2*>(wtilde_array);
+  if (plan->flags & SIGMA_HALFSUM_GVEC_MAJOR) {
+    // gppKerSeq.cpp's layout: aqsmtemp[ncouls][number_bands], I_eps_array[ncouls][ngpown]
+    SIGMA_CUDA_TRY(launch_transpose(aqsm, plan->t_aqsm, plan->nc, plan->nb, s));
+    SIGMA_CUDA_TRY(launch_transpose(aqsn, plan->t_aqsn, plan->nc, plan->nb, s));
+    SIGMA_CUDA_TRY(launch_transpose(ieps, plan->t_ieps, plan->nc, plan->ng, s));
+    SIGMA_CUDA_TRY(launch_transpose(wt, plan->t_wt, plan->nc, plan->ng, s));
+    aqsm = plan->t_aqsm;
+    aqsn = plan->t_aqsn;
+    ieps = plan->t_ieps;
+    wt = plan->t_wt;
+  }
+  HalfDev p{plan->nb, plan->nvband, plan->nc, plan->ng, occ, aqsm, aqsn, ieps, wt,
+            vcoul, wx_array, plan->igp_of, plan->brk};
+  SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 2 * sizeof(int), s));
+  if (plan->nvband > 0) {
+    half_brk_kernel<<<plan->ng, kThreads, 0, s>>>(p, plan->brk);
+    SIGMA_CUDA_TRY(cudaGetLastError());
+    half_occ_kernel<<<dim3(plan->ng, kNW), kThreads, 0, s>>>(p, plan->occ_ach, plan->occ_asx);
+    SIGMA_CUDA_TRY(cudaGetLastError());
+  }
+  if (plan->wm.n_items > 0) SIGMA_CUDA_TRY(launch_half_main<3>(p, plan->wm, plan->main_grid, s));
+  const bool stat = plan->ws.partial && achstemp;
+  if (stat && plan->ws.n_items > 0) SIGMA_CUDA_TRY(launch_half_main<1>(p, plan->ws, plan->stat_grid, s));
+  HalfReduceArgs a;
+  a.nb = plan->nb;
+  a.nvband = plan->nvband;
+  a.ng = plan->ng;
+  a.main_part = plan->wm.partial;
+  a.main_count = plan->wm.n_col_blocks * plan->wm.n_splits;
+  a.stat_part = stat ? plan->ws.partial : nullptr;
+  a.stat_count = plan->ws.n_col_blocks * plan->ws.n_splits;
+  a.occ_ach = plan->occ_ach;
+  a.occ_asx = plan->occ_asx;
+  a.acht_n1 = plan->acht_n1;
+  a.asx_n1 = plan->asx_n1;
+  a.stat_n1 = plan->stat_n1;
+  const int warps = plan->nb * kNW + plan->nvband * kNW + (stat ? plan->nb : 0);
+  half_reduce_bands_kernel<<<(warps * 32 + 255) / 256, 256, 0, s>>>(a);
+  SIGMA_CUDA_TRY(cudaGetLastError());
+  half_reduce_total_kernel<<<1, 256, 0, s>>>(plan->acht_n1, plan->asx_n1, plan->stat_n1, plan->nb,
+                                             plan->nvband, reinterpret_cast<double2*>(achtemp),
+                                             reinterpret_cast<double2*>(asxtemp),
+                                             stat ? reinterpret_cast<double2*>(achstemp) : nullptr,
+                                             reinterpret_cast<double2*>(acht_n1_loc));
+  SIGMA_CUDA_TRY(cudaGetLastError());
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, int ngpown,
+                                      int nstart, int nend, const int* inv_igp_index,
+                                      const int* indinv, const double* wx_array, double occ,
+                                      const sigma_complex128* aqsmtemp,
+                                      const sigma_complex128* aqsntemp,
+                                      const sigma_complex128* I_eps_array,
+                                      const sigma_complex128* wtilde_array, const double* vcoul,
+                                      sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                                      sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
+                                      void* stream) {
+  using namespace sigma;
+  if (!inv_igp_index || !indinv || !wx_array || !aqsmtemp || !aqsntemp || !I_eps_array ||
+      !wtilde_array || !vcoul || !achtemp || !asxtemp)
+    return SIGMA_ERR_NULL;
+  int st = gpp_check_shape(number_bands, nvband, ncouls, ngpown, nstart, nend);
+  if (st != SIGMA_OK) return st;
+  std::lock_guard<std::mutex> lk(api_mutex());
+  sigma_gpp_halfsum_plan plan = nullptr;
+  const int flags = SIGMA_HALFSUM_GVEC_MAJOR | (achstemp ? SIGMA_HALFSUM_STATIC : 0);
+  st = sigma_gpp_halfsum_plan_create(&plan, number_bands, nvband, ncouls, ngpown, nstart, nend,
+                                     inv_igp_index, indinv, ncouls, flags);
+  if (st != SIGMA_OK) return st;
+  const size_t bb = sizeof(sigma_complex128) * (size_t)number_bands * ncouls;
+  const size_t cb = sizeof(sigma_complex128) * (size_t)ngpown * ncouls;
+  size_t off = 0;
+  auto take = [&](size_t n) {
+    const size_t o = off;
+    off += up256(n);
+    return o;
+  };
+  const size_t o_m = take(bb), o_n = take(bb), o_e = take(cb), o_w = take(cb),
+               o_v = take(sizeof(double) * ncouls), o_x = take(sizeof(double) * kNW),
+               o_out = take(sizeof(sigma_complex128) * (2 * kNW + 1 + (size_t)number_bands));
+  void* arena = nullptr;
+  st = arena_get(kArenaMisc, off, &arena);
+  if (st != SIGMA_OK) {
+    sigma_gpp_halfsum_plan_destroy(plan);
+    return st;
+  }
+  char* a = static_cast<char*>(arena);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  auto C = [&](size_t o) { return reinterpret_cast<sigma_complex128*>(a + o); };
+  sigma_complex128* out = C(o_out);  // achtemp[3], asxtemp[3], achstemp[1], acht_n1_loc[nb]
+  auto run = [&]() -> int {
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_m, aqsmtemp, bb, cudaMemcpyHostToDevice, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_n, aqsntemp, bb, cudaMemcpyHostToDevice, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_e, I_eps_array, cb, cudaMemcpyHostToDevice, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_w, wtilde_array, cb, cudaMemcpyHostToDevice, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_v, vcoul, sizeof(double) * ncouls, cudaMemcpyHostToDevice, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + o_x, wx_array, sizeof(double) * kNW, cudaMemcpyHostToDevice, s));
+    int r = sigma_gpp_halfsum_execute(plan, reinterpret_cast<const double*>(a + o_x), occ, C(o_m),
+                                      C(o_n), C(o_e), C(o_w), reinterpret_cast<const double*>(a + o_v),
+                                      out, out + kNW, acht_n1_loc ? out + 2 * kNW + 1 : nullptr,
+                                      achstemp ? out + 2 * kNW : nullptr, stream);
+    if (r != SIGMA_OK) return r;
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(achtemp, out, sizeof(sigma_complex128) * kNW, cudaMemcpyDeviceToHost, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(asxtemp, out + kNW, sizeof(sigma_complex128) * kNW,
+                                   cudaMemcpyDeviceToHost, s));
+    if (achstemp)
+      SIGMA_CUDA_TRY(cudaMemcpyAsync(achstemp, out + 2 * kNW, sizeof(sigma_complex128),
+                                     cudaMemcpyDeviceToHost, s));
+    if (acht_n1_loc)
+      SIGMA_CUDA_TRY(cudaMemcpyAsync(acht_n1_loc, out + 2 * kNW + 1,
+                                     sizeof(sigma_complex128) * number_bands, cudaMemcpyDeviceToHost, s));
+    SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+    return SIGMA_OK;
+  };
+  const int rc = run();
+  sigma_gpp_halfsum_plan_destroy(plan);
+  return rc;
+}

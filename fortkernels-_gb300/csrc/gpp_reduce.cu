@@ -12,21 +12,6 @@ namespace sigma {
 namespace {
 
 
-// Butterfly combine of compensated pairs; every lane ends with the same value
-// (TwoSum's error term is exact, so a+b and b+a agree bit for bit).
-__device__ __forceinline__ double warp_sum_comp(Comp c) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const double s2 = __shfl_xor_sync(0xffffffffu, c.s, o);
-    const double c2 = __shfl_xor_sync(0xffffffffu, c.c, o);
-    double t, e;
-    two_sum_d(c.s, s2, t, e);
-    c.s = t;
-    c.c = __dadd_rn(__dadd_rn(c.c, c2), e);
-  }
-  return c.value();
-}
-
 struct ReduceArgs {
   int sch_rows;       // bands whose sums come from sch partials (0: acht_n1 already holds them)
   const double2* sch_partial;

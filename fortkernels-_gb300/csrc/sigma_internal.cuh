@@ -148,7 +148,7 @@ cudaError_t launch_gpp_reduce(const GppWork& sch, const GppWork& ssx, int nb, do
 
 // ---------------------------------------------------------------- device helpers
 __device__ __forceinline__ double rcp_f64(double w) {
-  // Hardware approximation of the high word (MUFU.RCP64H), then one cubic
+  // Hardware approximation of the reciprocal's leading bits, then one cubic
   // Newton-Raphson step r = r0 (1 + e + e^2), e = 1 - w r0: the relative error
   // goes from ~2^-20 to below the FP64 rounding unit.
   double r0;
@@ -181,7 +181,7 @@ __device__ __forceinline__ double rcp_f64_seed32(double w) {
 }
 
 __device__ __forceinline__ float rcp_f32(float w) {
-  // MUFU.RCP plus one Newton-Raphson step r = r0 (2 - w r0).
+  // rcp.approx.f32 plus one Newton-Raphson step r = r0 (2 - w r0).
   float r0;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(w));
   float e = fmaf(-w, r0, 1.0f);
@@ -245,5 +245,20 @@ struct Comp {
   }
   __device__ __forceinline__ double value() const { return __dadd_rn(s, c); }
 };
+
+// Butterfly combine of compensated pairs; every lane ends with the same value
+// (TwoSum's error term is exact, so a+b and b+a agree bit for bit).
+__device__ __forceinline__ double warp_sum_comp(Comp c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double s2 = __shfl_xor_sync(0xffffffffu, c.s, o);
+    const double c2 = __shfl_xor_sync(0xffffffffu, c.c, o);
+    double t, e;
+    two_sum_d(c.s, s2, t, e);
+    c.s = t;
+    c.c = __dadd_rn(__dadd_rn(c.c, c2), e);
+  }
+  return c.value();
+}
 
 }  // namespace sigma

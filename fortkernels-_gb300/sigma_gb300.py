@@ -72,6 +72,11 @@ SIGNATURES = {
     "sigma_gpp_real_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I], _I),
     "sigma_gpp_real_execute": ([_P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_real_plan_destroy": ([_P], _I),
+    "sigma_gpp_halfsum_fp64": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+                               _I),
+    "sigma_gpp_halfsum_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I, _I], _I),
+    "sigma_gpp_halfsum_execute": ([_P, _P, _D] + [_P] * 10, _I),
+    "sigma_gpp_halfsum_plan_destroy": ([_P], _I),
     "sigma_gpp_achstemp": ([_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "sigma_gpp_static_plan_create": ([_P, _I, _I, _I, _P, _P, _I], _I),
     "sigma_gpp_static_execute": ([_P, _P, _P, _P, _P, _P, _P, _P], _I),
@@ -181,6 +186,65 @@ def gpp_real_host(prob, stream: int = 0, want_n1: bool = True):
                                  *[_ptr(a) for a in arrs[1:]], _ptr(ach), _ptr(asx), _ptr(n1), stream)
     _check(st, "sigma_gpp_real_fp64")
     return ach, asx, n1
+
+
+HALFSUM_STATIC, HALFSUM_GVEC_MAJOR = 1, 2
+
+
+def gpp_halfsum_host(prob, stream: int = 0, want_n1: bool = True, want_static: bool = True):
+    """gppsum = 1 host drop-in (sigma_gpp_halfsum_fp64) on a workload.GppProblem
+    held band-major; the arrays are handed over in gppKerSeq.cpp's
+    g-vector-major layout, as that driver stores them.  Returns (achtemp[3],
+    asxtemp[3], acht_n1_loc[nb] or None, achstemp or None) complex128."""
+    lib = load()
+    inv = np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, dtype=np.int32)
+    wx = np.ascontiguousarray(prob.wx_array[:3], dtype=np.float64)
+    arrs = [_c128(np.asarray(a).T) for a in (prob.aqsmtemp, prob.aqsntemp, prob.I_eps_array, prob.wtilde_array)]
+    vcoul = np.ascontiguousarray(prob.vcoul, dtype=np.float64)
+    ach, asx = np.zeros(3, np.complex128), np.zeros(3, np.complex128)
+    n1 = np.zeros(prob.number_bands, np.complex128) if want_n1 else None
+    stat = np.zeros(1, np.complex128) if want_static else None
+    st = lib.sigma_gpp_halfsum_fp64(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart,
+                                    prob.nend, _ptr(inv), _ptr(indinv), _ptr(wx), prob.occ,
+                                    *[_ptr(a) for a in arrs], _ptr(vcoul), _ptr(ach), _ptr(asx), _ptr(n1),
+                                    _ptr(stat), stream)
+    _check(st, "sigma_gpp_halfsum_fp64")
+    return ach, asx, n1, (stat[0] if want_static else None)
+
+
+class GppHalfSumPlan:
+    """Device-resident gppsum = 1 GPP (sigma_gpp_halfsum_plan_create / execute).
+    flags: HALFSUM_STATIC (also achstemp), HALFSUM_GVEC_MAJOR (inputs in
+    gppKerSeq.cpp's [ncouls][...] layout)."""
+
+    def __init__(self, number_bands, nvband, ncouls, ngpown, inv_igp_index, indinv, flags=HALFSUM_STATIC):
+        self.lib = load()
+        self.inv = np.ascontiguousarray(inv_igp_index, dtype=np.int32)
+        self.indinv = np.ascontiguousarray(indinv, dtype=np.int32)
+        h = C.c_void_p()
+        _check(self.lib.sigma_gpp_halfsum_plan_create(C.byref(h), number_bands, nvband, ncouls, ngpown, 0, 3,
+                                                      _ptr(self.inv), _ptr(self.indinv), len(self.indinv),
+                                                      flags), "sigma_gpp_halfsum_plan_create")
+        self.handle = h
+
+    def execute(self, wx, aqsm, aqsn, ieps, wt, vcoul, achtemp, asxtemp, acht_n1_loc=None, achstemp=None,
+                occ=1.0, stream=0):
+        _check(self.lib.sigma_gpp_halfsum_execute(
+            self.handle, _dptr(wx), occ,
+            *[_dptr(a) for a in (aqsm, aqsn, ieps, wt, vcoul, achtemp, asxtemp)],
+            _dptr(acht_n1_loc), _dptr(achstemp), stream), "sigma_gpp_halfsum_execute")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sigma_gpp_halfsum_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class GppRealPlan:

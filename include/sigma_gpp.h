@@ -292,6 +292,61 @@ int sigma_gpp_real_execute(sigma_gpp_real_plan plan, const double* wx_array, dou
                            double* asxtemp, double* acht_n1_loc, void* stream);
 int sigma_gpp_real_plan_destroy(sigma_gpp_real_plan plan);
 
+/* ---------------------------------------------------------------------------
+ * gppsum = 1 ("half sum") GPP (gppKerSeq.cpp, the reference's sequential
+ * driver, run as `gppKerSeq nb nvband ncouls npg 1`), FP64.  Replaces its
+ * band loop :407-492 with the solvers it drives: noflagOCC_solver :193-261
+ * (non-occupied bands, in 512-wide g-vector blocks :457-470),
+ * flagOCC_solver :76-191 (occupied bands) and reduce_achstemp :13-72 (the
+ * static remainder `achstemp`, which the reference computes and never
+ * prints).  Each column my_igp sums g-vectors below its igp with the
+ * Hermitian partner term; the reference's own conventions are kept: its
+ * inverted pole test for the non-occupied bands (a term is kept where
+ * |wdiff|^2 < 0.25 or |delw|^2 > limitone), the g-vectors its block loop
+ * skips (ig mod 512 == 511 and ig == igp - 1; ig == igp alone when igp is a
+ * positive multiple of 512), the occupied loop's stop at the first
+ * |Omega2| < to1, and the unpaired term at ig == igp - 1.  Exact poles give
+ * non-finite results, as in the reference.
+ *
+ * sigma_gpp_halfsum_fp64 takes host arrays in gppKerSeq.cpp's own
+ * g-vector-major layout: aqsmtemp / aqsntemp [ncouls][number_bands],
+ * I_eps_array / wtilde_array [ncouls][ngpown] (the reference's row-pointer
+ * arrays, stored contiguously), vcoul [ncouls], wx_array [3].  Outputs are
+ * overwritten: achtemp[3], asxtemp[3], acht_n1_loc[number_bands] (may be
+ * NULL), achstemp[1] (may be NULL: the static remainder is then not run).
+ * ------------------------------------------------------------------------- */
+enum {
+  SIGMA_HALFSUM_STATIC = 1,    /* plan also evaluates the static remainder achstemp */
+  SIGMA_HALFSUM_GVEC_MAJOR = 2 /* execute takes gppKerSeq.cpp's [ncouls][...] layout */
+};
+int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
+                           int nend, const int* inv_igp_index, const int* indinv,
+                           const double* wx_array, double occ, const sigma_complex128* aqsmtemp,
+                           const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                           const sigma_complex128* wtilde_array, const double* vcoul,
+                           sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                           sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
+                           void* stream);
+
+/* Device-resident form.  Without SIGMA_HALFSUM_GVEC_MAJOR execute takes the
+ * library's band-major layout (aqsmtemp / aqsntemp [number_bands][ncouls],
+ * I_eps_array / wtilde_array [ngpown][ncouls], as gppKer.cpp); with it, the
+ * layout above, transposed on the device into plan-owned buffers.  achstemp
+ * needs SIGMA_HALFSUM_STATIC (else SIGMA_ERR_UNSUPPORTED). */
+typedef struct sigma_gpp_halfsum_plan_s* sigma_gpp_halfsum_plan;
+int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* plan, int number_bands, int nvband,
+                                  int ncouls, int ngpown, int nstart, int nend,
+                                  const int* inv_igp_index, const int* indinv, int indinv_len,
+                                  int flags);
+int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const double* wx_array, double occ,
+                              const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
+                              const sigma_complex128* I_eps_array,
+                              const sigma_complex128* wtilde_array, const double* vcoul,
+                              sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                              sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
+                              void* stream);
+int sigma_gpp_halfsum_plan_destroy(sigma_gpp_halfsum_plan plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,14 +1,17 @@
 """Build recipe of the CPU oracle (test infrastructure only).
 
-  oracle/_build/liboracle.so  <- oracle/gpp_oracle.cpp (the C++ restatement)
+  oracle/_build/liboracle.so  <- oracle/gpp_oracle.cpp + oracle/gpp_halfsum_oracle.cpp
+                                 (the C++ restatements)
   oracle/_ref/gppKer          <- BGW-Kernels/gppKer.cpp of the reference, unmodified
   oracle/_ref/libgppref.so    <- the same file (main renamed by -D) + oracle/ref_harness.cpp
   oracle/_ref/ffKernel        <- FFKer_cori/ffKernel.cpp of the reference, unmodified
   oracle/_ref/libffref.so     <- the same file (main renamed by -D) + oracle/ff_ref_harness.cpp
   oracle/_ref/gppKer_real     <- gppKer_real.cpp of the reference, unmodified
   oracle/_ref/libgpprealref.so <- the same file (main renamed by -D) + oracle/ref_real_harness.cpp
+  oracle/_ref/gppKerSeq       <- gppKerSeq.cpp of the reference, unmodified (the gppsum = 1 driver)
+  oracle/_ref/libgppseqref.so <- the same file (main renamed by -D) + oracle/ref_seq_harness.cpp
 
-The two oracle/_ref products are built only where the reference checkout is
+The oracle/_ref products are built only where the reference checkout is
 present (REFERENCE_ROOT, default /root/reference); they are compiled from the
 reference's own source file in place and nothing of it is copied.
 """
@@ -34,11 +37,17 @@ FF_REF_LIB = REF_OUT / "libffref.so"
 REAL_REF_SRC = REFERENCE_ROOT / "gppKer_real.cpp"
 REAL_REF_BIN = REF_OUT / "gppKer_real"
 REAL_REF_LIB = REF_OUT / "libgpprealref.so"
+SEQ_REF_SRC = REFERENCE_ROOT / "gppKerSeq.cpp"
+SEQ_REF_BIN = REF_OUT / "gppKerSeq"
+SEQ_REF_LIB = REF_OUT / "libgppseqref.so"
+ORACLE_SRCS = ("gpp_oracle.cpp", "gpp_halfsum_oracle.cpp")
 
 ORACLE_FLAGS = ["-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 # the timing build of the same file: the reference's own optimisation flags
 PORT_FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared"]
 REF_FLAGS = ["-O3", "-std=c++11", "-fopenmp"]
+# gppKerSeq.cpp writes `0.0 + 0.0i` (:121), a C++14 complex literal
+SEQ_REF_FLAGS = ["-O3", "-std=c++14", "-fopenmp"]
 
 
 def _run(cmd):
@@ -52,21 +61,21 @@ def _newer(target: pathlib.Path, *deps: pathlib.Path) -> bool:
 
 
 def build_oracle() -> pathlib.Path:
-    src = HERE / "gpp_oracle.cpp"
-    if _newer(ORACLE_LIB, src):
+    srcs = [HERE / f for f in ORACLE_SRCS]
+    if _newer(ORACLE_LIB, *srcs):
         return ORACLE_LIB
     BUILD.mkdir(exist_ok=True)
-    _run(["g++", *ORACLE_FLAGS, str(src), "-o", str(ORACLE_LIB)])
+    _run(["g++", *ORACLE_FLAGS, *map(str, srcs), "-o", str(ORACLE_LIB)])
     return ORACLE_LIB
 
 
 def build_port() -> pathlib.Path:
-    """oracle/gpp_oracle.cpp built with -O3 like the reference, for CPU timing."""
-    src = HERE / "gpp_oracle.cpp"
-    if _newer(PORT_LIB, src):
+    """The oracle sources built with -O3 like the reference, for CPU timing."""
+    srcs = [HERE / f for f in ORACLE_SRCS]
+    if _newer(PORT_LIB, *srcs):
         return PORT_LIB
     BUILD.mkdir(exist_ok=True)
-    _run(["g++", *PORT_FLAGS, str(src), "-o", str(PORT_LIB)])
+    _run(["g++", *PORT_FLAGS, *map(str, srcs), "-o", str(PORT_LIB)])
     return PORT_LIB
 
 
@@ -100,6 +109,13 @@ def build_reference() -> bool:
         if not _newer(REAL_REF_LIB, REAL_REF_SRC, rh):
             _run(["g++", *REF_FLAGS, "-fPIC", "-shared", "-Dmain=gppreal_reference_main",
                   str(REAL_REF_SRC), str(rh), "-o", str(REAL_REF_LIB)])
+    if SEQ_REF_SRC.exists():
+        if not _newer(SEQ_REF_BIN, SEQ_REF_SRC):
+            _run(["g++", *SEQ_REF_FLAGS, str(SEQ_REF_SRC), "-o", str(SEQ_REF_BIN)])
+        sh = HERE / "ref_seq_harness.cpp"
+        if not _newer(SEQ_REF_LIB, SEQ_REF_SRC, sh):
+            _run(["g++", *SEQ_REF_FLAGS, "-fPIC", "-shared", "-Dmain=gppseq_reference_main",
+                  str(SEQ_REF_SRC), str(sh), "-o", str(SEQ_REF_LIB)])
     return True
 
 

@@ -355,3 +355,97 @@ def run_reference_real_binary(number_bands, nvband, ncouls, nodes_per_group, thr
     for m in re.finditer(r"achtemp\[(\d+)\] = ([-+0-9.eE]+)", r.stdout):
         out[int(m.group(1))] = float(m.group(2))
     return out
+
+
+def gpp_halfsum(prob, nthreads=0, columns=False):
+    """gppsum = 1 ("half sum") GPP of gppKerSeq.cpp on a GppProblem in
+    band-major layout.  Returns (achtemp[3], asxtemp[3], acht_n1_loc[nb],
+    achstemp) complex128, plus (col_sch, col_ssx) [nb][ng][3] with
+    columns=True."""
+    l = lib()
+    if not hasattr(l, "_halfsum_ready"):
+        l.oracle_gpp_halfsum.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P,
+                                         _P, _P, _P, _P, _I]
+        l._halfsum_ready = True
+    inv, indinv, wx, aqsm, aqsn, ieps, wt, vcoul = _prep(prob)
+    nb, ng = prob.number_bands, prob.ngpown
+    ach, asx = np.zeros(3, np.complex128), np.zeros(3, np.complex128)
+    n1, stat = np.zeros(nb, np.complex128), np.zeros(1, np.complex128)
+    cs = np.zeros((nb, ng, 3), np.complex128) if columns else None
+    cx = np.zeros((nb, ng, 3), np.complex128) if columns else None
+    st = l.oracle_gpp_halfsum(nb, prob.nvband, prob.ncouls, ng, _p(inv), _p(indinv), len(indinv), _p(wx[:3]),
+                              float(getattr(prob, "occ", 1.0)), _p(aqsm), _p(aqsn), _p(ieps), _p(wt),
+                              _p(vcoul), _p(ach), _p(asx), _p(n1), _p(stat), _p(cs), _p(cx), nthreads)
+    if st != 0:
+        raise OracleError(f"oracle_gpp_halfsum status {st}")
+    out = (ach, asx, n1, stat[0])
+    return out + (cs, cx) if columns else out
+
+
+_seqref = None
+
+
+def reference_seq_lib():
+    """gppKerSeq.cpp's own solvers through oracle/ref_seq_harness.cpp (None
+    when the reference checkout is absent)."""
+    global _seqref
+    if _seqref is None:
+        if not _build.build_reference() or not _build.SEQ_REF_LIB.exists():
+            return None
+        l = C.CDLL(str(_build.SEQ_REF_LIB))
+        l.ref_seq_columns.argtypes = [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]
+        l.ref_seq_achstemp.argtypes = [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P]
+        l.ref_seq_main.argtypes = [_I, _I, _I, _I, _I]
+        _seqref = l
+    return _seqref
+
+
+def reference_seq_columns(prob, igp_of):
+    """(sch_array, ssx_array) per (band, column, frequency) from gppKerSeq.cpp's
+    own gppsum = 1 solvers, driven as its main loop drives them."""
+    l = reference_seq_lib()
+    if l is None:
+        return None
+    nb, ng = prob.number_bands, prob.ngpown
+    _, _, wx, aqsm, aqsn, ieps, wt, _ = _prep(prob)
+    sch = np.zeros((nb, ng, 3), np.complex128)
+    ssx = np.zeros((nb, ng, 3), np.complex128)
+    igp = np.ascontiguousarray(igp_of, dtype=np.int32)
+    l.ref_seq_columns(nb, prob.nvband, prob.ncouls, ng, _p(igp), _p(wx[:3]), _p(aqsm), _p(aqsn), _p(ieps),
+                      _p(wt), _p(sch), _p(ssx))
+    return sch, ssx
+
+
+def reference_seq_achstemp(prob):
+    """achstemp after gppKerSeq.cpp's own reduce_achstemp (gppsum = 1) over every band."""
+    l = reference_seq_lib()
+    if l is None:
+        return None
+    inv, indinv, _, aqsm, aqsn, ieps, _, vcoul = _prep(prob)
+    inv, indinv, vcoul = inv.copy(), indinv.copy(), vcoul.copy()
+    out = np.zeros(1, np.complex128)
+    l.ref_seq_achstemp(prob.number_bands, prob.ncouls, prob.ngpown, _p(inv), _p(indinv), _p(aqsm), _p(aqsn),
+                       _p(ieps), _p(vcoul), _p(out))
+    return out[0]
+
+
+def run_reference_seq_binary(number_bands, nvband, ncouls, nodes_per_group, gppsum=1, timeout=900):
+    """Runs the unmodified gppKerSeq.cpp driver (its constant fill); returns
+    (achtemp[3], seconds, stdout)."""
+    if not _build.build_reference() or not _build.SEQ_REF_BIN.exists():
+        return None
+
+    def _unlimit_stack():
+        try:
+            resource.setrlimit(resource.RLIMIT_STACK, (resource.RLIM_INFINITY, resource.RLIM_INFINITY))
+        except (ValueError, OSError):
+            pass
+
+    r = subprocess.run([str(_build.SEQ_REF_BIN), str(number_bands), str(nvband), str(ncouls),
+                        str(nodes_per_group), str(gppsum)], capture_output=True, text=True,
+                       timeout=timeout, preexec_fn=_unlimit_stack)
+    ach = np.zeros(3, np.complex128)
+    for m in _ACH.finditer(r.stdout):
+        ach[int(m.group(1))] = complex(float(m.group(2)), float(m.group(3)))
+    t = re.search(r"Time Taken \*+= ([0-9.eE+-]+)", r.stdout)
+    return ach, (float(t.group(1)) if t else float("nan")), r.stdout

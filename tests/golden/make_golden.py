@@ -29,6 +29,15 @@ fixtures it writes are committed so the tests run without it.
       ssx_array / sch_array per (band, column, frequency) from its own
       flagOCC_solver on seeded inputs (workload.gpp_real_random).
 
+  gpp_halfsum_reference.json    the unmodified gppKerSeq.cpp driver (the
+      reference's one buildable statement of gppsum = 1) run with gppsum = 1:
+      its printed achtemp (15 digits) on its constant fill.
+      gpp_halfsum_<case>.npz sch_array / ssx_array per (band, column,
+      frequency) from its own flagOCC_solver / noflagOCC_solver, driven in
+      the 512-wide g-vector blocks of its main loop (oracle/ref_seq_harness.cpp),
+      and achstemp from its own reduce_achstemp, on seeded inputs
+      (workload.gpp_random).
+
 Run:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -128,6 +137,36 @@ def real_main():
         print(name, np.abs(sch).max(), np.abs(ssx).max())
 
 
+HALF_CONST_SHAPES = [(16, 2, 512, 4), (16, 0, 512, 4), (8, 8, 1024, 8), (24, 3, 1536, 3),
+                     (32, 2, 2048, 16), (64, 4, 4096, 8)]
+HALF_CASES = {
+    # name: (number_bands, nvband, ncouls, ngpown, seed, stress); ncouls 1536 with
+    # ngpown 33 puts igp on 512 and 1024 (the unpaired igp term of the blocked loop)
+    "half_a": (6, 2, 1100, 40, 7, False),
+    "half_b": (5, 3, 1536, 33, 8, False),
+    "half_c": (4, 1, 1536, 33, 9, True),
+}
+
+
+def half_main():
+    runs = []
+    for shape in HALF_CONST_SHAPES:
+        ach, secs, _ = O.run_reference_seq_binary(*shape, gppsum=1)
+        runs.append({"shape": list(shape), "gppsum": 1, "achtemp": [[z.real, z.imag] for z in ach]})
+        print(shape, ach, f"{secs:.2f}s")
+    (HERE / "gpp_halfsum_reference.json").write_text(json.dumps({
+        "source": "gppKerSeq.cpp, unmodified, g++ -O3 -fopenmp -std=c++14, argv gppsum = 1; "
+                  "stdout achtemp (15 digits)",
+        "runs": runs}, indent=1))
+    for name, (nb, nvb, nc, ng, seed, stress) in HALF_CASES.items():
+        prob = W.gpp_random(nb, nvb, nc, ng, seed, stress=stress)
+        sch, ssx = O.reference_seq_columns(prob, igp_map(prob))
+        stat = O.reference_seq_achstemp(prob)
+        np.savez_compressed(HERE / f"gpp_halfsum_{name}.npz", sch=sch, ssx=ssx,
+                            achstemp=np.array([stat]), meta=np.array([nb, nvb, nc, ng, seed, int(stress)]))
+        print(name, np.abs(sch).max(), np.abs(ssx).max(), stat)
+
+
 def main():
     if O.reference_lib() is None:
         sys.exit("reference checkout not found; set REFERENCE_ROOT")
@@ -159,3 +198,4 @@ if __name__ == "__main__":
     main()
     ff_main()
     real_main()
+    half_main()

@@ -256,3 +256,67 @@ def test_real_oracle_terms_match_reference_flagocc(name):
     assert np.all(np.abs(ach - ach_ref) <= 1e-13 * scale)
     scale = np.abs(f["ssx"] * p.vcoul[igp][None, :, None]).sum(axis=(0, 1))
     assert np.all(np.abs(asx - asx_ref) <= 1e-13 * scale)
+
+
+# ---- gppsum = 1 ("half sum"), gppKerSeq.cpp ----
+HALF_REF = json.loads((GOLD / "gpp_halfsum_reference.json").read_text())
+
+
+def _half_closed_form(nb, nvb, nc, npg):
+    """Constant fill (every complex 0.5+0.5i, vcoul 1) of the half sum.  The
+    non-occupied bands contribute nothing (|wdiff|^2 >= 6.5 fails the
+    inverted test); an occupied band adds, per column, (igp - 1) paired
+    terms Re(s) and one unpaired s/2 with s = wtilde I_eps / (wx - wtilde)
+    (and x = Omega2 / (wx^2 - wtilde^2) for asxtemp); the static remainder
+    adds, per band and column, igp paired terms -2 |a|^2 Re(a) = -0.5 and the
+    diagonal -|a|^2 a = -a/2, times 0.5 vcoul."""
+    p = W.gpp_constant(nb, nvb, nc, npg)
+    a = 0.5 + 0.5j
+    wx = W.wx_frequencies()
+    igp = _igp_map(p)
+    igp = igp[igp >= 0]
+    s = a * a / (wx - a)
+    x = (a * a * a) / (wx ** 2 - a * a)
+    pos = igp[igp >= 1]
+    ach = nvb * 0.5 * ((pos - 1).sum() * s.real + 0.5 * len(pos) * s)
+    asx = nvb * ((pos - 1).sum() * x.real + 0.5 * len(pos) * x)
+    stat = nb * 0.5 * (-0.5 * igp.sum() + len(igp) * (-0.5 * a))
+    return ach, asx, stat
+
+
+@pytest.mark.parametrize("run", HALF_REF["runs"], ids=lambda r: "x".join(map(str, r["shape"])))
+def test_halfsum_oracle_matches_reference_driver_constant_fill(run):
+    """gppKerSeq.cpp run with gppsum = 1: its printed achtemp (15 digits); the
+    oracle also sits on the closed form of the fill."""
+    nb, nvb, nc, npg = run["shape"]
+    ach, asx, _, stat = O.gpp_halfsum(W.gpp_constant(nb, nvb, nc, npg))
+    ref = np.array([complex(*z) for z in run["achtemp"]])
+    ex_ach, ex_asx, ex_stat = _half_closed_form(nb, nvb, nc, npg)
+    if nvb == 0:
+        assert np.all(ref == 0) and np.all(ach == 0)
+    else:
+        assert rel_err(ach, ref).max() < 1e-12
+        assert rel_err(ach, ex_ach).max() < 1e-14
+        assert rel_err(asx, ex_asx).max() < 1e-14
+    assert abs(stat - ex_stat) <= 1e-14 * abs(ex_stat)
+
+
+@pytest.mark.parametrize("name", ["half_a", "half_b", "half_c"])
+def test_halfsum_oracle_matches_reference_solvers(name):
+    """Per-(band, column, frequency) sch_array / ssx_array of gppKerSeq.cpp's own
+    gppsum = 1 solvers (driven in its 512-wide g-vector blocks), and achstemp of
+    its own reduce_achstemp, against the oracle's."""
+    f = np.load(GOLD / f"gpp_halfsum_{name}.npz")
+    nb, nvb, nc, ng, seed, stress = (int(x) for x in f["meta"])
+    p = W.gpp_random(nb, nvb, nc, ng, seed, stress=bool(stress))
+    ach, asx, n1, stat, cs, cx = O.gpp_halfsum(p, columns=True)
+    assert np.abs(cs - f["sch"]).max() <= 1e-13 * np.abs(f["sch"]).max()
+    assert np.abs(cx - f["ssx"]).max() <= 1e-13 * np.abs(f["ssx"]).max()
+    assert abs(stat - f["achstemp"][0]) <= 1e-13 * abs(f["achstemp"][0])
+    igp = _igp_map(p)
+    v = p.vcoul[igp][None, :, None]
+    ach_ref = (f["sch"] * v).sum(axis=(0, 1))
+    assert np.all(np.abs(ach - ach_ref) <= 1e-13 * np.abs(f["sch"] * v).sum(axis=(0, 1)))
+    asx_ref = (f["ssx"] * v).sum(axis=(0, 1))
+    assert np.all(np.abs(asx - asx_ref) <= 1e-13 * np.abs(f["ssx"] * v).sum(axis=(0, 1)))
+    assert np.abs(n1 - (f["sch"][:, :, 2] * v[:, :, 0]).sum(axis=1)).max() <= 1e-13 * np.abs(n1).max()

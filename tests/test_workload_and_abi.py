@@ -80,6 +80,28 @@ def test_library_exports_every_declared_symbol(libpath):
     assert set(declared) <= set(sigma_gb300.exported_symbols())
 
 
+def _declared_arity():
+    """Parameter count of every sigma_* prototype in include/*.h."""
+    out = {}
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:int|const char\*|size_t|void)\s+(sigma_\w+)\s*\(([^;{]*?)\)\s*;",
+                             text, flags=re.M | re.S):
+            params = m.group(2).strip()
+            out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_binding_argument_counts_match_headers():
+    """Every ctypes binding takes exactly the parameters its C prototype declares."""
+    import sigma_gb300
+    arity = _declared_arity()
+    bad = {n: (len(a), arity[n]) for n, (a, _) in sigma_gb300.SIGNATURES.items()
+           if n in arity and len(a) != arity[n]}
+    assert not bad, bad
+    assert len(set(arity) & set(sigma_gb300.SIGNATURES)) >= 30
+
+
 def test_status_strings(libpath):
     lib = C.CDLL(str(libpath))
     lib.sigma_status_string.restype = C.c_char_p
