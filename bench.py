@@ -554,6 +554,13 @@ def run_ours(args, rank, world, local_rank):
         if rank == 0:
             print(json.dumps({"ff": res}), flush=True)
         return 0
+    if args.only_halfsum:
+        import replicas
+        inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
+        res = run_halfsum(S, W, torch, dist, world, stream, sptr, args, inst)
+        if rank == 0:
+            print(json.dumps({"halfsum": res}), flush=True)
+        return 0
     fp64_peak, fp32_peak = S.measure_fma_peaks(sptr)
     import replicas
     inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
@@ -768,6 +775,8 @@ def main():
     ap.add_argument("--no-static", action="store_true")
     ap.add_argument("--no-real", action="store_true")
     ap.add_argument("--no-halfsum", action="store_true")
+    ap.add_argument("--only-halfsum", action="store_true",
+                    help="run the gppsum=1 half-sum measurement alone (profiling captures)")
     ap.add_argument("--ff-shape", default=None,
                     help="number_bands,ncouls,ngpown,nfreq of the FF runs (default the production "
                          "512,16384,820,15; smaller only for profiling captures)")
