@@ -18,12 +18,15 @@
 // tensor cores fill one, four drain warps read the other (tcgen05.ld) into
 // round-to-nearest FP32 running sums held in registers.
 //
-// Roles (160 threads): warp 4 lane 0 streams 96 KB K-tiles (three A and three
-// B slices, one bulk copy each) into a two-stage shared ring and issues 24
-// tcgen05.mma (M=128, N=128, K=16) per tile; warps 0-3 drain TMEM and run the
-// epilogue, which multiplies tempz by conj(aqsm[n1][igp(my_igp)]) and sums
-// the tile's rows per frequency (:408-418) with a reduce-scatter butterfly.
-// Items are (row block, band block, K split), scheduled statically.
+// Roles (192 threads): warp 4 lane 0 streams 48 KB K-tiles (three A and three
+// B slices of 32 K values in the 64-byte swizzle, one bulk copy per operand)
+// into a four-stage shared ring, up to three tiles ahead of the tensor
+// cores; warp 5 lane 0 issues 12 tcgen05.mma (M=128, N=128, K=16) per tile
+// and releases each stage with tcgen05.commit; warps 0-3 drain TMEM and run
+// the epilogue, which multiplies tempz by conj(aqsm[n1][igp(my_igp)]) and
+// sums the tile's rows per frequency (:408-418) with a reduce-scatter
+// butterfly.  Items are (row block, band block, K split), scheduled
+// statically.
 #include <cuda_bf16.h>
 
 #include "ff_ozaki.cuh"
@@ -34,14 +37,17 @@ namespace {
 
 using namespace tma;
 
-constexpr int kOzThreads = 160;
+constexpr int kOzThreads = 192;
 constexpr int kDrainThreads = 128;
-constexpr uint32_t kSliceBytes = 128 * 64 * 2;          // 16 KB
-constexpr uint32_t kOperandBytes = 3 * kSliceBytes;     // 48 KB
-constexpr uint32_t kStageBytes = 2 * kOperandBytes;     // 96 KB
-constexpr uint32_t kSmemBytes = 2 * kStageBytes + 1024; // + alignment slack
+constexpr int kTmaWarp = 4, kMmaWarp = 5;
+constexpr int kChunksPerRow = kOzKTile / 8;                      // 16-byte chunks per tile row
+constexpr uint32_t kSliceBytes = 128 * kOzKTile * 2;             // 8 KB
+constexpr uint32_t kOperandBytes = 3 * kSliceBytes;              // 24 KB
+constexpr uint32_t kStageBytes = 2 * kOperandBytes;              // 48 KB
+constexpr int kStages = 4;
+constexpr uint32_t kSmemBytes = kStages * kStageBytes + 2048;    // + alignment slack and 1 KB past the ring
 constexpr uint32_t kTmemCols = 512;                     // 2 x (leading + correction) accumulators
-constexpr int kChunkStages = 2;                         // K tiles per accumulator lifetime
+constexpr int kChunkStages = 4;                         // K tiles per accumulator lifetime (8 K-steps)
 constexpr int kMaxSeg = 8;                              // frequencies per row block (host checks)
 constexpr uint32_t kIdesc = idesc_bf16_f32(128, 128);
 
@@ -59,7 +65,7 @@ __device__ __forceinline__ void split3(double v, unsigned short& a, unsigned sho
 }
 
 // Slices of 8 consecutive K values of one row, written as three 16-byte
-// chunks (one per slice tile) of a 48 KB block.
+// chunks (one per slice tile) of a 24 KB block.
 __device__ __forceinline__ void put_row_chunk(unsigned char* blk, int r, int ch, const double (&v)[8]) {
   unsigned short sl[3][8];
 #pragma unroll
@@ -71,20 +77,20 @@ __device__ __forceinline__ void put_row_chunk(unsigned char* blk, int r, int ch,
     q.y = sl[s][2] | ((uint32_t)sl[s][3] << 16);
     q.z = sl[s][4] | ((uint32_t)sl[s][5] << 16);
     q.w = sl[s][6] | ((uint32_t)sl[s][7] << 16);
-    *reinterpret_cast<uint4*>(blk + s * kSliceBytes + sw128_offset(r, ch * 8)) = q;
+    *reinterpret_cast<uint4*>(blk + s * kSliceBytes + sw64_offset(r, ch * 8)) = q;
   }
 }
 
 // A' = [Re | Im] of I_epsR rows.  Thread = (row block, K tile, row, 8-K chunk);
 // it writes the real-part tile kt and the imaginary-part tile kt + oz.kt.
 __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz) {
-  const long long total = (long long)oz.n_row_blocks * oz.kt * 128 * 8;
+  const long long total = (long long)oz.n_row_blocks * oz.kt * 128 * kChunksPerRow;
   const int rows = p.nf * p.ng;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int ch = (int)(t & 7);
-    const int r = (int)((t >> 3) & 127);
-    const long long rest = t >> 10;
+    const int ch = (int)(t % kChunksPerRow);
+    const int r = (int)((t / kChunksPerRow) & 127);
+    const long long rest = t / (kChunksPerRow * 128);
     const int kt = (int)(rest % oz.kt);
     const int rb = (int)(rest / oz.kt);
     const int R = rb * kOzRows + r;
@@ -105,12 +111,12 @@ __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz
 
 // B' rows: [Re | -Im] (real part of the product) and [Im | Re] (imaginary part).
 __global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz) {
-  const long long total = (long long)oz.n_col_blocks * oz.kt * 64 * 8;
+  const long long total = (long long)oz.n_col_blocks * oz.kt * 64 * kChunksPerRow;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int ch = (int)(t & 7);
-    const int nl = (int)((t >> 3) & 63);
-    const long long rest = t >> 9;
+    const int ch = (int)(t % kChunksPerRow);
+    const int nl = (int)((t / kChunksPerRow) & 63);
+    const long long rest = t / (kChunksPerRow * 64);
     const int kt = (int)(rest % oz.kt);
     const int cb = (int)(rest / oz.kt);
     const int n = cb * kOzCols + nl;
@@ -157,22 +163,23 @@ __device__ __forceinline__ void drain_barrier() {
 
 __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWork w, OzakiPrep oz) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) unsigned long long bars[8];  // full[2], empty[2], accf[2], acce[2]
+  // full[kStages], empty[kStages], accf[2], acce[2]
+  __shared__ __align__(8) unsigned long long bars[2 * kStages + 4];
   __shared__ uint32_t tmem_slot;
   __shared__ float2 s_red[4][kMaxSeg][kOzCols];
 
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t sbase = (raw + 1023u) & ~1023u;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]);
-  const uint32_t accf0 = smem_u32(&bars[4]), acce0 = smem_u32(&bars[6]);
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[kStages]);
+  const uint32_t accf0 = smem_u32(&bars[2 * kStages]), acce0 = smem_u32(&bars[2 * kStages + 2]);
   const int two_kt = 2 * oz.kt;
 
   if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), kTmemCols);
   if (tid == 0) {
-    for (int i = 0; i < 6; ++i) mbar_init(smem_u32(&bars[i]), 1);
-    mbar_init(smem_u32(&bars[6]), 4);
-    mbar_init(smem_u32(&bars[7]), 4);
+    for (int i = 0; i < 2 * kStages + 2; ++i) mbar_init(smem_u32(&bars[i]), 1);
+    mbar_init(acce0, 4);
+    mbar_init(acce0 + 8u, 4);
     fence_mbar_init();
   }
   tc_fence_before();
@@ -180,31 +187,44 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  if (warp == 4) {
-    // ------------------------------------------------ producer: TMA + MMA issue
+  if (warp == kTmaWarp) {
+    // ------------------------------------------------ bulk copies into the stage ring
     if (lane == 0) {
-      uint32_t ph_full0 = 0, ph_full1 = 0, ph_empty0 = 0, ph_empty1 = 0, ph_acce0 = 0, ph_acce1 = 0;
-      bool pend0 = false, pend1 = false, used0 = false, used1 = false;
-      uint32_t gc = 0;  // chunks issued by this CTA
+      uint32_t g = 0;  // tiles issued by this CTA
       for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
         const OzItem it = oz_decode(oz, item);
         const int kt_begin = it.s * oz.split_tiles;
         const int nst = min(oz.split_tiles, two_kt - kt_begin);
         const unsigned char* a_src = oz.a_tiles + ((size_t)it.rb * two_kt + kt_begin) * kOperandBytes;
         const unsigned char* b_src = oz.b_tiles + ((size_t)it.cb * two_kt + kt_begin) * kOperandBytes;
-        auto issue = [&](int s, int buf) {
-          const uint32_t bar = full0 + 8u * buf;
-          const uint32_t dst = sbase + (uint32_t)buf * kStageBytes;
+        for (int s = 0; s < nst; ++s, ++g) {
+          const uint32_t b = g % kStages, use = g / kStages;
+          // stage b is free once the MMAs of its previous tile have completed
+          if (use > 0) mbar_wait(empty0 + 8u * b, (use - 1) & 1u, w.status);
+          const uint32_t bar = full0 + 8u * b;
+          const uint32_t dst = sbase + b * kStageBytes;
           mbar_expect_tx(bar, kStageBytes);
           bulk_load(dst, a_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
           bulk_load(dst + kOperandBytes, b_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
-        };
-        issue(0, 0);
-        for (int s = 0; s < nst; ++s) {
-          const int buf = s & 1;
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == kMmaWarp) {
+    // ------------------------------------------------ tensor-core issue
+    if (lane == 0) {
+      uint32_t ph_acce0 = 0, ph_acce1 = 0;
+      bool used0 = false, used1 = false;
+      uint32_t g = 0;   // tiles consumed by this CTA
+      uint32_t gc = 0;  // accumulator lifetimes started
+      for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
+        const OzItem it = oz_decode(oz, item);
+        const int kt_begin = it.s * oz.split_tiles;
+        const int nst = min(oz.split_tiles, two_kt - kt_begin);
+        for (int s = 0; s < nst; ++s, ++g) {
           const int cs = s % kChunkStages;
           const uint32_t tb = gc & 1u;
-          if (cs == 0) {  // first tile of an accumulator lifetime: buffer tb must be drained
+          if (cs == 0) {  // first tile of an accumulator lifetime: pair tb must be drained
             if (tb == 0 && used0) {
               mbar_wait(acce0, ph_acce0, w.status);
               ph_acce0 ^= 1u;
@@ -214,27 +234,21 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
               ph_acce1 ^= 1u;
             }
             if (tb == 0) used0 = true; else used1 = true;
-            tc_fence_after();
           }
-          if (buf == 0) {
-            mbar_wait(full0, ph_full0, w.status);
-            ph_full0 ^= 1u;
-          } else {
-            mbar_wait(full0 + 8u, ph_full1, w.status);
-            ph_full1 ^= 1u;
-          }
+          const uint32_t b = g % kStages;
+          mbar_wait(full0 + 8u * b, (g / kStages) & 1u, w.status);
           tc_fence_after();
-          const uint32_t a_addr = sbase + (uint32_t)buf * kStageBytes;
+          const uint32_t a_addr = sbase + b * kStageBytes;
           const uint32_t b_addr = a_addr + kOperandBytes;
           const uint32_t d_big = tmem + tb * 256u, d_small = d_big + 128u;
 #pragma unroll
           for (int kk = 0; kk < kOzKTile / 16; ++kk) {
-            const uint64_t a1 = sw128_desc(a_addr + kk * 32);
-            const uint64_t a2 = sw128_desc(a_addr + kSliceBytes + kk * 32);
-            const uint64_t a3 = sw128_desc(a_addr + 2 * kSliceBytes + kk * 32);
-            const uint64_t b1 = sw128_desc(b_addr + kk * 32);
-            const uint64_t b2 = sw128_desc(b_addr + kSliceBytes + kk * 32);
-            const uint64_t b3 = sw128_desc(b_addr + 2 * kSliceBytes + kk * 32);
+            const uint64_t a1 = sw64_desc(a_addr + kk * 32);
+            const uint64_t a2 = sw64_desc(a_addr + kSliceBytes + kk * 32);
+            const uint64_t a3 = sw64_desc(a_addr + 2 * kSliceBytes + kk * 32);
+            const uint64_t b1 = sw64_desc(b_addr + kk * 32);
+            const uint64_t b2 = sw64_desc(b_addr + kSliceBytes + kk * 32);
+            const uint64_t b3 = sw64_desc(b_addr + 2 * kSliceBytes + kk * 32);
             const uint32_t acc = (cs > 0 || kk > 0) ? 1u : 0u;
             mma_f16(d_big, a1, b1, kIdesc, acc);
             mma_f16(d_small, a1, b2, kIdesc, acc);
@@ -243,36 +257,11 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
             mma_f16(d_small, a2, b2, kIdesc, 1u);
             mma_f16(d_small, a3, b1, kIdesc, 1u);
           }
-          mma_commit(empty0 + 8u * buf);
-          if (buf == 0) pend0 = true; else pend1 = true;
+          mma_commit(empty0 + 8u * b);  // stage b free once these MMAs complete
           if (cs == kChunkStages - 1 || s == nst - 1) {
             mma_commit(accf0 + 8u * tb);  // accumulator pair tb complete
             ++gc;
           }
-          if (s + 1 < nst) {
-            const int nb = buf ^ 1;
-            if (nb == 0 && pend0) {
-              mbar_wait(empty0, ph_empty0, w.status);
-              ph_empty0 ^= 1u;
-              pend0 = false;
-            }
-            if (nb == 1 && pend1) {
-              mbar_wait(empty0 + 8u, ph_empty1, w.status);
-              ph_empty1 ^= 1u;
-              pend1 = false;
-            }
-            issue(s + 1, nb);
-          }
-        }
-        if (pend0) {
-          mbar_wait(empty0, ph_empty0, w.status);
-          ph_empty0 ^= 1u;
-          pend0 = false;
-        }
-        if (pend1) {
-          mbar_wait(empty0 + 8u, ph_empty1, w.status);
-          ph_empty1 ^= 1u;
-          pend1 = false;
         }
       }
       // wait until the drain warps released every accumulator pair in use

@@ -5,7 +5,7 @@
 
 namespace sigma {
 
-constexpr int kOzKTile = 64;    // K elements per staged tile (one 128-byte swizzle row)
+constexpr int kOzKTile = 32;    // K elements per staged tile (one 64-byte swizzle row)
 constexpr int kOzRows = 128;    // complex rows (ifreq, my_igp) per tile, frequencies flattened
 constexpr int kOzCols = 64;     // complex bands per tile
 
@@ -16,11 +16,11 @@ constexpr int kOzCols = 64;     // complex bands per tile
 //   B'[n][k']   = Re aqsn[n][k], -Im ...   (rows 0..63: real part of the product)
 //   B'[64+n][k']= Im aqsn[n][k],  Re ...   (rows 64..127: imaginary part)
 // so C'[R][n] = Re tempz and C'[R][64+n] = Im tempz sit in one TMEM lane.
-// One 48 KB block per (row block, K' tile) holds three 16 KB BF16 slices.
+// One 24 KB block per (row block, K' tile) holds three 8 KB BF16 slices.
 struct OzakiPrep {
-  unsigned char* a_tiles;   // [n_row_blocks][2*kt][3][128][64] bf16
-  unsigned char* b_tiles;   // [n_col_blocks][2*kt][3][128][64] bf16
-  int kt;                   // K tiles per real/imaginary half (ncouls padded to 64)
+  unsigned char* a_tiles;   // [n_row_blocks][2*kt][3][128][32] bf16
+  unsigned char* b_tiles;   // [n_col_blocks][2*kt][3][128][32] bf16
+  int kt;                   // K tiles per real/imaginary half (ncouls padded to 32)
   int n_row_blocks;         // ceil(nfreq * ngpown / 128)
   int n_col_blocks;         // ceil(number_bands / 64)
   int n_splits, split_tiles;  // K' split into n_splits ranges of split_tiles tiles

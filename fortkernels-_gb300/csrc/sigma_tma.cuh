@@ -123,6 +123,19 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t smem_addr) {
   return d;
 }
 
+// The same for the 64-byte swizzle: rows of 32 elements (64 B), 8-row groups
+// of 512 B, 16-byte chunk c of row r stored at chunk (c ^ ((r / 2) % 4))
+// (layout code 4 in bits 61-63).
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t smem_addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((smem_addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)(512u >> 4) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)4u << 61;
+  return d;
+}
+
 // Instruction descriptor of tcgen05.mma.kind::f16: FP32 accumulator, BF16 A
 // and B, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n) {
@@ -133,6 +146,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n) {
 // of 64-element rows (16-bit elements).
 __host__ __device__ __forceinline__ uint32_t sw128_offset(int r, int k) {
   return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 3) ^ (r & 7)) & 7) << 4) + (k & 7) * 2);
+}
+
+// Byte offset of element (row r, k) inside a K-major 64-byte-swizzled tile of
+// 32-element rows (16-bit elements).
+__host__ __device__ __forceinline__ uint32_t sw64_offset(int r, int k) {
+  return (uint32_t)((r >> 3) * 512 + (r & 7) * 64 + ((((k >> 3) ^ (r >> 1)) & 3) << 4) + (k & 7) * 2);
 }
 
 }  // namespace tma
