@@ -144,12 +144,17 @@ struct OzItem {
   int rb, cb, s;
   size_t pidx;
 };
+// Items run band block fastest, then row block, with the K split slowest:
+// the CTAs running at one time share A tiles (8 band blocks read each) and
+// touch only one K split of the B operand, which then stays in L2 (the whole
+// B operand is 200 MB at the production shape, one split a quarter of it).
+// pidx, the partial-sum slot, does not depend on the order.
 __device__ __forceinline__ OzItem oz_decode(const OzakiPrep& oz, int item) {
   OzItem t;
   t.cb = item % oz.n_col_blocks;
   const int r = item / oz.n_col_blocks;
-  t.s = r % oz.n_splits;
-  t.rb = r / oz.n_splits;
+  t.rb = r % oz.n_row_blocks;
+  t.s = r / oz.n_row_blocks;
   t.pidx = ((size_t)t.rb * oz.n_col_blocks + t.cb) * oz.n_splits + t.s;
   return t;
 }
