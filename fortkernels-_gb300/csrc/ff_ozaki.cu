@@ -140,6 +140,24 @@ __global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz
   }
 }
 
+// wtab[g][n] = aqsm[n][igp(g)] * weight(g), rounded to FP32 from the FP64
+// product (the value the epilogue used to form per lane from global loads).
+__global__ void __launch_bounds__(256) ozaki_weights_kernel(FfDev p, OzakiPrep oz) {
+  const long long total = (long long)oz.ng * oz.nb_pad;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(t / oz.nb_pad), n = (int)(t % oz.nb_pad);
+    const int igp = p.igp_of[g];
+    float2 v = make_float2(0.f, 0.f);
+    if (igp >= 0 && n < p.nb) {
+      const double wgt = ff_column_weight(p, igp);
+      const double2 md = p.aqsm[(size_t)n * p.nc + igp];
+      v = make_float2(__double2float_rn(md.x * wgt), __double2float_rn(md.y * wgt));
+    }
+    oz.wtab[t] = v;
+  }
+}
+
 struct OzItem {
   int rb, cb, s;
   size_t pidx;
@@ -312,30 +330,32 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
         ++gc;
       }
 
-      // epilogue: row R of this lane, 64 bands; tempz * conj(aqsm[n1][igp])
+      // epilogue: row R of this lane, 64 bands; tempz * weight * conj(aqsm[n1][igp])
       const int R = it.rb * kOzRows + warp * 32 + lane;
       const bool row_ok = R < rows;
       const int f = row_ok ? R / p.ng : 0;
       const int g = row_ok ? R % p.ng : 0;
       const int f_first = (it.rb * kOzRows) / p.ng;
       const int f_last = (min(it.rb * kOzRows + kOzRows, rows) - 1) / p.ng;
-      const int igp_raw = row_ok ? p.igp_of[g] : -1;
-      const bool col_ok = igp_raw >= 0;
-      const int igp = col_ok ? igp_raw : 0;
-      const double wgt = ff_column_weight(p, igp_raw);
-      // acc[n] <- Re, acc[64 + n] <- Im of tempz * weight * conj(aqsm[n1][igp])
+      // the row's 64 factors: 32 contiguous 16-byte loads in four batches
+      const float4* wrow =
+          reinterpret_cast<const float4*>(oz.wtab + (size_t)g * oz.nb_pad + (size_t)it.cb * kOzCols);
 #pragma unroll
-      for (int n = 0; n < 64; ++n) {
-        const int nn = it.cb * kOzCols + n;
-        float mr = 0.f, mi = 0.f;
-        if (col_ok && nn < p.nb) {
-          const double2 md = p.aqsm[(size_t)nn * p.nc + igp];
-          mr = __double2float_rn(md.x * wgt);
-          mi = __double2float_rn(md.y * wgt);
+      for (int n0 = 0; n0 < 64; n0 += 16) {
+        float4 wv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) wv[j] = row_ok ? __ldg(wrow + n0 / 2 + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int n = n0 + 2 * j + h;
+            const float mr = h ? wv[j].z : wv[j].x, mi = h ? wv[j].w : wv[j].y;
+            const float cr = acc[n], ci = acc[64 + n];
+            acc[n] = fmaf(cr, mr, ci * mi);
+            acc[64 + n] = fmaf(ci, mr, -cr * mi);
+          }
         }
-        const float cr = acc[n], ci = acc[64 + n];
-        acc[n] = fmaf(cr, mr, ci * mi);
-        acc[64 + n] = fmaf(ci, mr, -cr * mi);
       }
       for (int seg = 0; seg <= f_last - f_first; ++seg) {
         const bool mine = row_ok && (f - f_first) == seg;
@@ -437,6 +457,8 @@ void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid) {
   oz.split_tiles = (int)((two_kt + s - 1) / s);
   oz.n_splits = (two_kt + oz.split_tiles - 1) / oz.split_tiles;
   oz.n_items = (int)(base * oz.n_splits);
+  oz.ng = d.ng;
+  oz.nb_pad = oz.n_col_blocks * kOzCols;
 }
 
 int ozaki_max_segments() { return kMaxSeg; }
@@ -445,8 +467,12 @@ size_t ozaki_tile_bytes(const OzakiPrep& oz) {
   return ((size_t)oz.n_row_blocks + oz.n_col_blocks) * 2 * oz.kt * kOperandBytes + 1024;
 }
 
+static size_t ozaki_partial_only_bytes(const OzakiPrep& oz) {
+  return (sizeof(double2) * (size_t)oz.n_items * oz.max_seg * kOzCols + 255) / 256 * 256;
+}
+
 size_t ozaki_partial_bytes(const OzakiPrep& oz) {
-  return sizeof(double2) * (size_t)oz.n_items * oz.max_seg * kOzCols + 256;
+  return ozaki_partial_only_bytes(oz) + sizeof(float2) * (size_t)oz.ng * oz.nb_pad + 256;
 }
 
 size_t ozaki_prep_bytes(const OzakiPrep& oz) { return ozaki_tile_bytes(oz) + ozaki_partial_bytes(oz); }
@@ -457,6 +483,7 @@ void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial) {
   oz.b_tiles = oz.a_tiles + (size_t)oz.n_row_blocks * 2 * oz.kt * kOperandBytes;
   uintptr_t pp = (reinterpret_cast<uintptr_t>(partial) + 255) & ~uintptr_t(255);
   oz.partial = reinterpret_cast<double2*>(pp);
+  oz.wtab = reinterpret_cast<float2*>(pp + ozaki_partial_only_bytes(oz));
 }
 
 void ozaki_prep_bind(OzakiPrep& oz, void* base) {
@@ -468,6 +495,9 @@ cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t 
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   ozaki_prep_b_kernel<<<152 * 4, 256, 0, s>>>(d, oz);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  ozaki_weights_kernel<<<152 * 2, 256, 0, s>>>(d, oz);
   return cudaGetLastError();
 }
 

@@ -27,6 +27,11 @@ struct OzakiPrep {
   int n_items;
   int max_seg;              // frequencies one row block can touch
   double2* partial;         // [row block][col block][split][max_seg][64]
+  // Epilogue factors, formed per execution: wtab[g][n] = aqsm[n][igp(g)] *
+  // column weight, in FP32 (0 for a skipped column or a padded band), so a
+  // drain lane reads its row's 64 factors as contiguous 16-byte loads.
+  float2* wtab;             // [ng][nb_pad]
+  int ng, nb_pad;
 };
 
 // Work sizing and buffers of the split-BF16 form (partials + slices).
