@@ -378,9 +378,49 @@ namespace {
 
 sigma_gpp_plan g_cached_plan = nullptr;
 
+// Copy stream and gate words of the FP64 host drop-in, whose host-to-device
+// copies run beside the sum (one per process, guarded by api_mutex()).
+constexpr int kGateChunks = 8;
+struct CopyLane {
+  int device = -1;
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_s = nullptr, ev_done = nullptr;
+  unsigned* host_words = nullptr;  // pinned, kGateChunks
+  unsigned epoch = 0;
+};
+CopyLane g_lane;
+
+void drop_lane() {
+  if (g_lane.device < 0) return;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(g_lane.device);
+  if (g_lane.cs) cudaStreamDestroy(g_lane.cs);
+  if (g_lane.ev_s) cudaEventDestroy(g_lane.ev_s);
+  if (g_lane.ev_done) cudaEventDestroy(g_lane.ev_done);
+  if (g_lane.host_words) cudaFreeHost(g_lane.host_words);
+  cudaSetDevice(cur);
+  g_lane = CopyLane();
+}
+
+int lane_for(int dev, CopyLane** out) {
+  if (g_lane.device != dev) {
+    drop_lane();
+    g_lane.device = dev;
+    SIGMA_CUDA_TRY(cudaStreamCreateWithFlags(&g_lane.cs, cudaStreamNonBlocking));
+    SIGMA_CUDA_TRY(cudaEventCreateWithFlags(&g_lane.ev_s, cudaEventDisableTiming));
+    SIGMA_CUDA_TRY(cudaEventCreateWithFlags(&g_lane.ev_done, cudaEventDisableTiming));
+    SIGMA_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&g_lane.host_words),
+                                 sizeof(unsigned) * kGateChunks, cudaHostAllocDefault));
+  }
+  *out = &g_lane;
+  return SIGMA_OK;
+}
+
 void drop_cached_plan() {
   if (g_cached_plan) sigma_gpp_plan_destroy(g_cached_plan);
   g_cached_plan = nullptr;
+  drop_lane();
 }
 
 struct HookOnce {
@@ -431,12 +471,13 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
 
   const size_t band_bytes = sizeof(sigma_complex128) * (size_t)nb * nc;
   const size_t col_bytes = sizeof(sigma_complex128) * (size_t)ng * nc;
-  size_t off[9];
+  size_t off[10];
   size_t total = 0;
-  const size_t sizes[9] = {band_bytes, band_bytes, col_bytes, col_bytes, sizeof(double) * (size_t)nc,
-                           sizeof(double) * kNW, sizeof(sigma_complex128) * kNW,
-                           sizeof(sigma_complex128) * kNW, sizeof(sigma_complex128) * (size_t)nb};
-  for (int i = 0; i < 9; ++i) {
+  const size_t sizes[10] = {band_bytes, band_bytes, col_bytes, col_bytes, sizeof(double) * (size_t)nc,
+                            sizeof(double) * kNW, sizeof(sigma_complex128) * kNW,
+                            sizeof(sigma_complex128) * kNW, sizeof(sigma_complex128) * (size_t)nb,
+                            sizeof(unsigned) * kGateChunks};
+  for (int i = 0; i < 10; ++i) {
     off[i] = total;
     total += align_up(sizes[i], 256);
   }
@@ -445,6 +486,84 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
   if (st != SIGMA_OK) return st;
   char* a = static_cast<char*>(arena);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (precision == SIGMA_PREC_FP64 && plan->schy.n_items > 0) {
+    // FP64 with the shared-frequency pass: the column inputs travel in
+    // kGateChunks pieces on a copy stream while the sum runs; each piece is
+    // followed by its gate word, which the pass's items wait for.
+    CopyLane* lane = nullptr;
+    st = lane_for(dev, &lane);
+    if (st != SIGMA_OK) return st;
+    const int ncb = plan->schy.n_col_blocks;
+    const int per = (ncb + kGateChunks - 1) / kGateChunks;  // column blocks per piece
+    const int pieces = (ncb + per - 1) / per;
+    unsigned epoch = ++lane->epoch;
+    if (epoch == 0) epoch = ++lane->epoch;
+    for (int c = 0; c < pieces; ++c) lane->host_words[c] = epoch;
+    unsigned* gate = reinterpret_cast<unsigned*>(a + off[9]);
+    // gate words cleared and counters zeroed on the caller's stream; the
+    // copies start after that and after the work already queued there (no
+    // operation of the copy stream needs a multiprocessor, so the sum,
+    // which holds them all while it waits, cannot block a copy)
+    SIGMA_CUDA_TRY(cudaMemsetAsync(gate, 0, sizes[9], s));
+    SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
+    SIGMA_CUDA_TRY(cudaEventRecord(lane->ev_s, s));
+    SIGMA_CUDA_TRY(cudaStreamWaitEvent(lane->cs, lane->ev_s, 0));
+    const void* base_src[4] = {aqsm, aqsn, vcoul, wx};
+    const int base_idx[4] = {0, 1, 4, 5};
+    for (int i = 0; i < 4; ++i)
+      SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[base_idx[i]], base_src[i], sizes[base_idx[i]],
+                                     cudaMemcpyHostToDevice, lane->cs));
+    const size_t row_bytes = sizeof(sigma_complex128) * (size_t)nc;
+    for (int c = 0; c < pieces; ++c) {
+      const int g0 = c * per * kBPY, g1 = std::min((c + 1) * per * kBPY, ng);
+      if (g1 > g0) {
+        const size_t o = row_bytes * (size_t)g0, n = row_bytes * (size_t)(g1 - g0);
+        SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[2] + o, reinterpret_cast<const char*>(ieps) + o, n,
+                                       cudaMemcpyHostToDevice, lane->cs));
+        SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[3] + o, reinterpret_cast<const char*>(wt) + o, n,
+                                       cudaMemcpyHostToDevice, lane->cs));
+      }
+      SIGMA_CUDA_TRY(cudaMemcpyAsync(gate + c, lane->host_words + c, sizeof(unsigned),
+                                     cudaMemcpyHostToDevice, lane->cs));
+    }
+    SIGMA_CUDA_TRY(cudaEventRecord(lane->ev_done, lane->cs));
+
+    GppDev p;
+    p.nb = nb;
+    p.nvband = nvband;
+    p.nc = nc;
+    p.ng = ng;
+    p.wx_stride = 0;
+    p.occ = occ;
+    p.aqsm = reinterpret_cast<const double2*>(a + off[0]);
+    p.aqsn = reinterpret_cast<const double2*>(a + off[1]);
+    p.ieps = reinterpret_cast<const double2*>(a + off[2]);
+    p.wt = reinterpret_cast<const double2*>(a + off[3]);
+    p.vcoul = reinterpret_cast<const double*>(a + off[4]);
+    p.wx = reinterpret_cast<const double*>(a + off[5]);
+    p.igp_of = plan->igp_of;
+    GppWork w = plan->schy;
+    w.ready = gate;
+    w.epoch = epoch;
+    w.ready_cb = per;
+    w.ready_status = plan->prep.status;
+    SIGMA_CUDA_TRY(launch_sch_fp64y(p, w, plan->schy_grid, s));
+    SIGMA_CUDA_TRY(cudaStreamWaitEvent(s, lane->ev_done, 0));
+    if (plan->ssx.n_items > 0) SIGMA_CUDA_TRY(launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
+    auto* d_ach = reinterpret_cast<double2*>(a + off[6]);
+    auto* d_asx = reinterpret_cast<double2*>(a + off[7]);
+    auto* d_n1 = reinterpret_cast<double2*>(a + off[8]);
+    SIGMA_CUDA_TRY(launch_gpp_reduce(plan->schy, plan->ssx, nb, plan->acht_n1, d_ach, d_asx,
+                                     acht_n1_loc ? d_n1 : nullptr, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(achtemp, d_ach, sizes[6], cudaMemcpyDeviceToHost, s));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(asxtemp, d_asx, sizes[7], cudaMemcpyDeviceToHost, s));
+    if (acht_n1_loc)
+      SIGMA_CUDA_TRY(cudaMemcpyAsync(acht_n1_loc, d_n1, sizes[8], cudaMemcpyDeviceToHost, s));
+    int dev_status = 0;
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(&dev_status, plan->prep.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+    return dev_status == 0 ? SIGMA_OK : dev_status;
+  }
   const void* src[6] = {aqsm, aqsn, ieps, wt, vcoul, wx};
   for (int i = 0; i < 6; ++i)
     SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[i], src[i], sizes[i], cudaMemcpyHostToDevice, s));

@@ -216,9 +216,25 @@ struct SchYSmem {
   double2 n[kCKY][BN];
 };
 
+// Bounded wait for a gate word written by a host-to-device copy (about 1 s).
+__device__ __forceinline__ void wait_ready(const unsigned* flag, unsigned epoch, int* status) {
+  if (*reinterpret_cast<volatile int*>(status) != 0) return;  // an earlier wait gave up
+  for (int i = 0; i < (1 << 22); ++i) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+    if (v == epoch) return;
+    __nanosleep(256);
+  }
+  atomicExch(status, (int)SIGMA_ERR_TIMEOUT);
+}
+
 template <int BN, int BP>
 __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w, int item,
                                                unsigned char* smem_raw, int tid) {
+  if (w.ready) {  // inputs of this column block copied yet?
+    if (tid == 0) wait_ready(w.ready + decode_item(w, item).cb / w.ready_cb, w.epoch, w.ready_status);
+    __syncthreads();
+  }
   constexpr int TB = BN / 16, TC = BP / 16;
   SchYSmem<BN, BP>& sm = *reinterpret_cast<SchYSmem<BN, BP>*>(smem_raw);
   const int tx = tid & 15, ty = tid >> 4;

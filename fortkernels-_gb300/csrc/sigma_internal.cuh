@@ -59,6 +59,14 @@ struct GppWork {
   int n_items;
   int* counter;                // dynamic item counter (zeroed before launch)
   double2* partial;            // [n_band_blocks][n_col_blocks][n_splits][BN][3]
+  // Optional gate of the FP64 shared-frequency pass: the items of column
+  // block cb first wait (bounded) until ready[cb / ready_cb] == epoch, a word
+  // the host copies to the device after that column range's inputs, so host
+  // copies overlap the sum; a wait that gives up records SIGMA_ERR_TIMEOUT.
+  const unsigned* ready = nullptr;
+  unsigned epoch = 0;
+  int ready_cb = 1;
+  int* ready_status = nullptr;
 };
 
 // Tile shapes.  Every pass uses kBN-band blocks (partial-sum layout of the
