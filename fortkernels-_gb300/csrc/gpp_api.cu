@@ -20,9 +20,11 @@ struct sigma_gpp_plan_s {
   int device = 0;
   int nb = 0, nvband = 0, nc = 0, ng = 0, precision = 0;
   int valid_columns = 0;
-  int sch_grid = 0, ssx_grid = 0, schy_grid = 0;
+  int sch_grid = 0, ssx_grid = 0, schy_grid = 0, schmy_grid = 0;
   sigma::GppWork sch{}, ssx{};
   sigma::GppWork schy{};      // FP64 main pass for shared frequencies (shares sch's buffers)
+  sigma::GppWork schmy{};     // mixed main pass for shared frequencies (shares sch's buffers)
+  sigma::GppWork prepw{};     // pre-pass blocks: sch's, rounded up to even counts
   sigma_ff_plan ff = nullptr; // tensor form: the contraction plan (3 slabs = 3 frequencies)
   double2* yfac = nullptr;    // tensor form: frequency factors Y[3][ng][nc]
   sigma::MixedPrep prep{};    // FP32 operands of the mixed path (unused for FP64)
@@ -108,6 +110,7 @@ namespace {
 constexpr int kItemsPerSlot = 48;       // work items per resident CTA (load balance of the tail)
 constexpr int kItemsPerSlotMixed = 12;  // mixed items are 64x cheaper: fewer, longer items
 constexpr int kItemsPerSlotY = 24;      // shared-frequency FP64 items (64 x 32 tiles, 1 CTA per SM)
+constexpr int kItemsPerSlotMY = 12;     // shared-frequency mixed items (64 x 32 tiles, 1 CTA per SM)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -162,16 +165,27 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
     gpp_size_work(p->schy, 0, number_bands, kBNY, kBPY, ncouls, ngpown, p->schy_grid, kItemsPerSlotY);
     if (p->schy.n_items < p->schy_grid) p->schy_grid = p->schy.n_items;
   }
+  if (mixed && !tensor) {
+    p->schmy_grid = sms * sch_blocks_per_sm_mixedy();
+    gpp_size_work(p->schmy, 0, number_bands, 2 * kBN, 2 * kBPM, ncouls, ngpown, p->schmy_grid,
+                  kItemsPerSlotMY);
+    if (p->schmy.n_items < p->schmy_grid) p->schmy_grid = p->schmy.n_items;
+  }
+  p->prepw = p->sch;
+  p->prepw.n_col_blocks = (p->sch.n_col_blocks + 1) / 2 * 2;
+  p->prepw.n_band_blocks = (p->sch.n_band_blocks + 1) / 2 * 2;
 
   const size_t b_igp = align_up(sizeof(int) * ngpown, 256);
   const size_t b_cnt = 256;
   const size_t b_n1 = align_up(sizeof(double2) * (size_t)(number_bands + nvband) * kNW, 256);
-  const size_t b_sch = align_up(sizeof(double2) * std::max((size_t)p->sch.n_items * kBN,
-                                                           (size_t)p->schy.n_items * kBNY) * kNW, 256);
+  const size_t b_sch = align_up(sizeof(double2) * std::max({(size_t)p->sch.n_items * kBN,
+                                                            (size_t)p->schy.n_items * kBNY,
+                                                            (size_t)p->schmy.n_items * 2 * kBN}) * kNW,
+                                256);
   const size_t b_ssx = align_up(sizeof(double2) * (size_t)p->ssx.n_items * kSsxBN * kNW, 256);
   const int nc_pad = (ncouls + kCK - 1) / kCK * kCK;
-  const size_t col_elems = mixed ? (size_t)p->sch.n_col_blocks * kBPM * nc_pad : 0;
-  const size_t band_elems = mixed ? (size_t)p->sch.n_band_blocks * kBN * nc_pad : 0;
+  const size_t col_elems = mixed ? (size_t)p->prepw.n_col_blocks * kBPM * nc_pad : 0;
+  const size_t band_elems = mixed ? (size_t)p->prepw.n_band_blocks * kBN * nc_pad : 0;
   const size_t b_colA = align_up(sizeof(float4) * col_elems, 256);
   const size_t b_colB = align_up(sizeof(float2) * col_elems, 256);
   const size_t b_band = align_up(sizeof(float2) * band_elems, 256);
@@ -203,6 +217,8 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   p->ssx.counter = p->counters + 1;
   p->schy.partial = p->sch.partial;
   p->schy.counter = p->counters;
+  p->schmy.partial = p->sch.partial;
+  p->schmy.counter = p->counters;
   {
     char* q = base + b_igp + b_cnt + b_n1 + b_sch + b_ssx;
     p->prep.colA = mixed ? reinterpret_cast<float4*>(q) : nullptr;
@@ -342,10 +358,11 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
   const bool mixed = plan->precision == SIGMA_PREC_MIXED;
   if ((mixed || (tensor && plan->ssx.n_items > 0)) && plan->sch.n_items > 0)
-    SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->sch, plan->prep, s));
-  // FP64 with one frequency set for every band: the shared-factor kernel
-  const bool ypath = !mixed && wx_band_stride == 0 && plan->schy.n_items > 0;
-  GppWork main = ypath ? plan->schy : plan->sch;
+    SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->prepw, plan->prep, s));
+  // one frequency set for every band: the shared-factor kernels
+  const bool ypath = !mixed && !tensor && wx_band_stride == 0 && plan->schy.n_items > 0;
+  const bool mypath = mixed && wx_band_stride == 0 && plan->schmy.n_items > 0;
+  GppWork main = ypath ? plan->schy : (mypath ? plan->schmy : plan->sch);
   if (tensor) main.partial = nullptr;  // band sums land in acht_n1 directly
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
   if (tensor) {
@@ -356,6 +373,8 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
     if (st != SIGMA_OK) return st;
   } else if (ypath)
     SIGMA_CUDA_TRY(launch_sch_fp64y(p, plan->schy, plan->schy_grid, s));
+  else if (mypath)
+    SIGMA_CUDA_TRY(launch_sch_mixedy(p, plan->schmy, plan->prep, plan->schmy_grid, s));
   else if (plan->sch.n_items > 0)
     SIGMA_CUDA_TRY(mixed ? launch_sch_mixed(p, plan->sch, plan->prep, plan->sch_grid, s)
                          : launch_sch_fp64(p, plan->sch, plan->sch_grid, s));

@@ -486,6 +486,234 @@ __global__ void __launch_bounds__(kThreads, 3) sch_mixed_batch_kernel(GppBatchVi
 
 }  // namespace
 
+namespace {
+
+// ---------------------------------------------------------------- shared-frequency main pass
+// With one frequency set for every band the factor Y_iw = G (c + i b) r of a
+// (column, g-vector) is the same for every band (the FP64 path's
+// sch_fp64y_kernel uses the same algebra).  sch_mixedy forms Y once per
+// staged chunk in FP32 from the pre-pass operands and the exact keep masks,
+// and the band sum becomes an FP32 complex GEMM: items of 64 bands x 32
+// columns (two pre-pass blocks each way), 16 x 16 threads with 4 bands x 2
+// columns x 3 frequencies each, runs of kRun g-vectors folded into
+// float-float accumulators as in the per-band kernel.
+constexpr int kYBN = 2 * kBN, kYBP = 2 * kBPM;  // 64 bands x 32 columns
+constexpr uint32_t kYChunkBytes = 2 * kChunkBytes;
+
+struct __align__(16) StageY {
+  float4 a[2][kCK][kBPM];
+  float2 b[2][kCK][kBPM];
+  float2 n[2][kCK][kBN];
+};
+struct __align__(16) SchSmemY {
+  StageY st[2];
+  float2 y[kCK][kNW][kYBP];
+  unsigned long long bar[2];
+};
+static_assert(sizeof(StageY) == kYChunkBytes, "six bulk copies per chunk");
+
+__device__ __forceinline__ void issue_chunk_y(const MixedPrep& m, int cb, int bb, int ig0, StageY& st,
+                                              unsigned long long* bar) {
+  mbar_expect_tx(bar, kYChunkBytes);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const size_t col_off = ((size_t)(2 * cb + h) * m.nc_pad + ig0) * kBPM;
+    const size_t band_off = ((size_t)(2 * bb + h) * m.nc_pad + ig0) * kBN;
+    bulk_load(&st.a[h][0][0], m.colA + col_off, sizeof(st.a[h]), bar);
+    bulk_load(&st.b[h][0][0], m.colB + col_off, sizeof(st.b[h]), bar);
+    bulk_load(&st.n[h][0][0], m.band + band_off, sizeof(st.n[h]), bar);
+  }
+}
+
+__device__ __forceinline__ void sch_mixedy_item(const GppDev& p, const GppWork& w, const MixedPrep& m,
+                                                int item, SchSmemY& sm, int tid, uint32_t& phase0,
+                                                uint32_t& phase1) {
+  constexpr int TB = 4, TC = 2;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int band_end = w.band_begin + w.band_count;
+  const ItemCoord ic = decode_item(w, item);
+  const int n1_0 = w.band_begin + ic.bb * kYBN;
+  const int p0 = ic.cb * kYBP;
+  const int ig_begin = ic.s * w.split_len;
+  const int ig_end = min(ig_begin + w.split_len, p.nc);
+  const int n_chunks = (ig_end - ig_begin + kCK - 1) / kCK;
+  float wxh[kNW], wxl[kNW];
+#pragma unroll
+  for (int iw = 0; iw < kNW; ++iw) split_f(p.wx[iw], wxh[iw], wxl[iw]);
+
+  float2 acc[TB][TC][kNW], hi[TB][TC][kNW], lo[TB][TC][kNW];
+#pragma unroll
+  for (int i = 0; i < TB; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        acc[i][j][iw] = make_float2(0.f, 0.f);
+        hi[i][j][iw] = make_float2(0.f, 0.f);
+        lo[i][j][iw] = make_float2(0.f, 0.f);
+      }
+  // this thread's bands: 4 consecutive of one pre-pass band block
+  const int nb_blk = ty >> 3, nb_off = (ty & 7) * TB;
+
+  if (tid == 0) issue_chunk_y(m, ic.cb, ic.bb, ig_begin, sm.st[0], &sm.bar[0]);
+  for (int c = 0; c < n_chunks; ++c) {
+    const int buf = c & 1;
+    const int ig0 = ig_begin + c * kCK;
+    if (tid == 0 && c + 1 < n_chunks)
+      issue_chunk_y(m, ic.cb, ic.bb, ig0 + kCK, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
+    if (buf == 0) {
+      mbar_wait(&sm.bar[0], phase0, m.status);
+      phase0 ^= 1;
+    } else {
+      mbar_wait(&sm.bar[1], phase1, m.status);
+      phase1 ^= 1;
+    }
+    const StageY& st = sm.st[buf];
+    // frequency factors of the chunk; g-vectors past the split's end and
+    // padding columns carry a zero mask
+    for (int e = tid; e < kCK * kYBP; e += kThreads) {
+      const int k = e / kYBP, col = e % kYBP;
+      const int h = col / kBPM, pl = col % kBPM;
+      const float4 a = st.a[h][k][pl];
+      const float2 g = st.b[h][k][pl];
+      const unsigned mask = (ig0 + k < ig_end) ? __float_as_uint(a.w) : 0u;
+      const float b2 = a.z * a.z;
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        const float cc = (wxh[iw] - a.x) + (wxl[iw] - a.y);
+        const float r = rcp_f32(fmaf(cc, cc, b2));
+        const float rm = (mask & (1u << iw)) ? r : 0.f;
+        sm.y[k][iw][col] = make_float2(fmaf(g.x, cc, -g.y * a.z) * rm, fmaf(g.x, a.z, g.y * cc) * rm);
+      }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int kr = 0; kr < kCK; kr += kRun) {
+#pragma unroll 2
+      for (int k = kr; k < kr + kRun; ++k) {
+        const float4 n01 = *reinterpret_cast<const float4*>(&st.n[nb_blk][k][nb_off]);
+        const float4 n23 = *reinterpret_cast<const float4*>(&st.n[nb_blk][k][nb_off + 2]);
+        const float2 nn[TB] = {make_float2(n01.x, n01.y), make_float2(n01.z, n01.w),
+                               make_float2(n23.x, n23.y), make_float2(n23.z, n23.w)};
+        float2 yv[TC][kNW];
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          const float4 y2 = *reinterpret_cast<const float4*>(&sm.y[k][iw][2 * tx]);
+          yv[0][iw] = make_float2(y2.x, y2.y);
+          yv[1][iw] = make_float2(y2.z, y2.w);
+        }
+#pragma unroll
+        for (int i = 0; i < TB; ++i)
+#pragma unroll
+          for (int j = 0; j < TC; ++j)
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              float2& a = acc[i][j][iw];
+              a.x = fmaf(nn[i].x, yv[j][iw].x, a.x);
+              a.x = fmaf(-nn[i].y, yv[j][iw].y, a.x);
+              a.y = fmaf(nn[i].x, yv[j][iw].y, a.y);
+              a.y = fmaf(nn[i].y, yv[j][iw].x, a.y);
+            }
+      }
+#pragma unroll
+      for (int i = 0; i < TB; ++i)
+#pragma unroll
+        for (int j = 0; j < TC; ++j)
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            float sum, err;
+            two_sum_f(hi[i][j][iw].x, acc[i][j][iw].x, sum, err);
+            hi[i][j][iw].x = sum;
+            lo[i][j][iw].x += err;
+            two_sum_f(hi[i][j][iw].y, acc[i][j][iw].y, sum, err);
+            hi[i][j][iw].y = sum;
+            lo[i][j][iw].y += err;
+            acc[i][j][iw] = make_float2(0.f, 0.f);
+          }
+    }
+    __syncthreads();  // stage and factors consumed before they are refilled
+  }
+
+  // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp] in FP64; the 16 lanes
+  // of a half-warp hold the item's 32 columns for the same 4 bands and sum
+  // them with a fixed butterfly
+#pragma unroll
+  for (int i = 0; i < TB; ++i) {
+    const int bl = nb_blk * kBN + nb_off + i;  // band within the item
+    const int n1 = n1_0 + bl;
+    double2 part[kNW];
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) part[iw] = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int j = 0; j < TC; ++j) {
+      const int my_igp = p0 + 2 * tx + j;
+      const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
+      if (n1 < band_end && igp >= 0) {
+        const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+        const double2 mm = make_double2(am.x, -am.y);
+        const double f = 0.5 * p.vcoul[igp];
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          const double2 sv = make_double2((double)hi[i][j][iw].x + (double)lo[i][j][iw].x,
+                                          (double)hi[i][j][iw].y + (double)lo[i][j][iw].y);
+          const double2 v = cmul(sv, mm);
+          part[iw].x = fma(v.x, f, part[iw].x);
+          part[iw].y = fma(v.y, f, part[iw].y);
+        }
+      }
+    }
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw)
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) {
+        part[iw].x += __shfl_xor_sync(0xffffffffu, part[iw].x, o);
+        part[iw].y += __shfl_xor_sync(0xffffffffu, part[iw].y, o);
+      }
+    if (tx == 0)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) w.partial[ic.pidx * kYBN * kNW + bl * kNW + iw] = part[iw];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) sch_mixedy_kernel(GppDev p, GppWork w, MixedPrep m) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SchSmemY& sm = *reinterpret_cast<SchSmemY*>(smem_raw);
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_fence_init();
+  }
+  uint32_t phase0 = 0, phase1 = 0;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(w.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= w.n_items) break;
+    sch_mixedy_item(p, w, m, item, sm, tid, phase0, phase1);
+  }
+}
+
+}  // namespace
+
+int sch_blocks_per_sm_mixedy() {
+  int n = 0;
+  cudaFuncSetAttribute(sch_mixedy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SchSmemY));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sch_mixedy_kernel, kThreads, sizeof(SchSmemY));
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_sch_mixedy(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
+                              cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(sch_mixedy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       sizeof(SchSmemY));
+  if (e != cudaSuccess) return e;
+  sch_mixedy_kernel<<<grid, kThreads, sizeof(SchSmemY), s>>>(p, w, m);
+  return cudaGetLastError();
+}
+
 int sch_blocks_per_sm_mixed() {
   int n = 0;
   cudaFuncSetAttribute(sch_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SchSmemM));

@@ -137,6 +137,12 @@ int sch_blocks_per_sm_fp64y();
 cudaError_t launch_sch_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
                              cudaStream_t s);
 cudaError_t launch_prep_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, cudaStream_t s);
+// Mixed main pass for one frequency set shared by every band: items of
+// 2*kBN bands x 2*kBPM columns; the pre-pass must cover an even number of
+// band and column blocks.
+cudaError_t launch_sch_mixedy(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
+                              cudaStream_t s);
+int sch_blocks_per_sm_mixedy();
 // The pre-pass (launch_prep_mixed) must have run for the same execution.
 cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, int grid,
                              cudaStream_t s);
