@@ -168,8 +168,8 @@ def cpu_baseline(prob, target_s=15.0):
             "sample": f"bands {NB - bands}..{NB - 1} of the production instance (all 1638 columns, "
                       f"32768 g-vectors, 3 frequencies; {bands * NG * NC * 3:.3e} terms, {dt:.1f} s); "
                       "oracle port of BGW-Kernels/gppKer.cpp:303-439 with its OpenMP dynamic schedule, "
-                      "g++ -O2 -fopenmp; the reference's own binary needs its source checkout, absent "
-                      "on this host"}
+                      "g++ -O3 -fopenmp as the reference builds; the unmodified reference driver only "
+                      "runs its constant fill"}
 
 
 # ------------------------------------------------------------------ reference arm
@@ -199,8 +199,9 @@ def run_reference(args, rank):
                    "ngpown": NG, "sample_bands_per_step": bands},
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{bands} non-occupied bands per step, all columns and g-vectors; "
-                                   "the reference's own binary needs the reference checkout, absent "
-                                   "on this host, so the oracle port of its loop nest runs"},
+                                   "the unmodified reference driver only runs its constant fill, so the "
+                                   "oracle port of its loop nest (BGW-Kernels/gppKer.cpp:303-439, OpenMP "
+                                   "dynamic schedule) runs on the same seeded inputs"},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
