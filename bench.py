@@ -431,20 +431,33 @@ def run_halfsum(S, W, torch, dist, world, stream, sptr, args, inst):
     res = {"workload": f"gppsum=1 half sum, {NB} bands x {NG} columns x g-vectors below igp "
                        f"(of {NC}) x 3 frequencies, FP64, band-major device arrays",
            "unit": UNIT, "terms_per_step": terms}
-    for flags, key in ((0, "sums"), (S.HALFSUM_STATIC, "with_static")):
+    outs = {}
+    for flags, key, steps in ((0, "sums", 3), (S.HALFSUM_STATIC, "with_static", 3),
+                              (S.HALFSUM_STATIC | S.HALFSUM_TENSOR, "tensor", 10)):
         plan = S.GppHalfSumPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, flags=flags)
         run = lambda: plan.execute(inst.wx, inst.aqsm, inst.aqsn, inst.ieps, inst.wt, inst.vcoul, ach, asx,
                                    n1, st if flags else None, stream=sptr)
         for _ in range(max(1, min(args.warmup, 2))):
             run()
-        steps = 3
         ms = timed(torch, dist, world, run, steps, stream)
         plan.close()
+        outs[key] = [t.cpu().numpy().view(np.complex128).copy() for t in (ach, asx, n1, st)]
         if key == "sums":
             res["value"] = round(terms * world / (ms / steps * 1e-3) / 1e9, 4)
             res["ms_per_step"] = round(ms / steps, 3)
-        else:
+        elif key == "with_static":
             res["with_static_ms_per_step"] = round(ms / steps, 3)
+        else:
+            a, b = outs["tensor"], outs["with_static"]
+            res["tensor"] = {
+                "value": round(terms * world / (ms / steps * 1e-3) / 1e9, 4), "unit": UNIT,
+                "ms_per_step_with_static": round(ms / steps, 3),
+                "rel_err_vs_fp64": {"achtemp": rel(a[0], b[0]), "achstemp": float(abs(a[3][0] - b[3][0]) /
+                                                                                    abs(b[3][0])),
+                                    "acht_n1_loc_normwise": float(np.linalg.norm(a[2] - b[2]) /
+                                                                  np.linalg.norm(b[2]))},
+                "path": "band sums as four split-BF16 tcgen05 contractions (T, U, static T and U); "
+                        "occupied bands and unpaired igp terms in FP64"}
     return res
 
 

@@ -38,6 +38,7 @@
 
 #include "sigma_gpp.h"
 #include "sigma_internal.cuh"
+#include "ff_plan.h"
 #include "runtime.h"
 
 namespace sigma {
@@ -495,6 +496,115 @@ cudaError_t launch_transpose(const double2* src, double2* dst, int rows, int col
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- tensor-core form
+// The non-occupied sums T and U and the static remainder's are weighted FF
+// contractions (ff_ozaki.cu) of band-independent factor slabs:
+//   sum_col 0.5 vcoul conj(aqsm_p) T = FF(Z, B = aqsn, M = aqsm)
+//   sum_col 0.5 vcoul aqsm_p conj(U) = conj(FF(Z, B = aqsm, M = aqsm))
+// and for the static remainder (v_p = aqsn_p) FF(Zs, aqsn, aqsm) +
+// conj(FF(Zs, B = aqsm, M = aqsn)).  Z[iw][col][ig] is the masked factor over
+// the reference's g-vector set, Zs = -I_eps below igp; the unpaired igp terms
+// and the occupied bands run in FP64.
+
+// Z slabs [3][ng][nc] of the non-occupied half sum.
+__global__ void __launch_bounds__(256) half_z_kernel(HalfDev p, double2* z) {
+  const long long total = (long long)p.ng * p.nc;
+  const double wx[3] = {p.wx[0], p.wx[1], p.wx[2]};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int col = (int)(t / p.nc), ig = (int)(t % p.nc);
+    const int lim = column_limit<3>(p.igp_of[col]);
+    double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    if (ig < lim && (ig % kIgBlk) != kIgBlk - 1) half_factor(p.wt[t], p.ieps[t], wx, v);
+    z[t] = v[0];
+    z[total + t] = v[1];
+    z[2 * total + t] = v[2];
+  }
+}
+
+// Zs [ng][nc] of the static remainder: -I_eps below igp.
+__global__ void __launch_bounds__(256) half_zs_kernel(HalfDev p, double2* z) {
+  const long long total = (long long)p.ng * p.nc;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int col = (int)(t / p.nc), ig = (int)(t % p.nc);
+    const int lim = column_limit<1>(p.igp_of[col]);
+    const double2 e = p.ieps[t];
+    z[t] = ig < lim ? make_double2(-e.x, -e.y) : make_double2(0.0, 0.0);
+  }
+}
+
+// Band rows of the tensor form: one warp per band, compensated sums over the
+// columns of the unpaired igp terms (and of the occupied-band partials), then
+//   acht_n1[n1][iw] = T + conj(U) + unpaired       (n1 >= nvband)
+//                   = sum_col occ_ach                (n1 <  nvband)
+//   asx_n1[n1][iw]  = sum_col occ_asx                (n1 <  nvband)
+//   stat_n1[n1]     = Ts + conj(Us) + unpaired       (static remainder)
+__global__ void half_tensor_rows_kernel(HalfDev p, const double2* t3, const double2* u3,
+                                        const double2* ts, const double2* us, const double2* occ_ach,
+                                        const double2* occ_asx, double2* acht_n1, double2* asx_n1,
+                                        double2* stat_n1) {
+  const int n1 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (n1 >= p.nb) return;
+  const bool occ = n1 < p.nvband;
+  const double wx[3] = {p.wx[0], p.wx[1], p.wx[2]};
+  Comp ax[3], ay[3], sx[3], sy[3], qx, qy;
+  for (int col = lane; col < p.ng; col += 32) {
+    const int igp = p.igp_of[col];
+    if (igp < 0) continue;
+    const size_t off = (size_t)col * p.nc + igp;
+    const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+    const double2 an = p.aqsn[(size_t)n1 * p.nc + igp];
+    const double w = 0.5 * p.vcoul[igp];
+    const double2 d = cmul(cconj(am), an);
+    if (ts) {  // static remainder's unpaired igp term
+      const double2 e = p.ieps[off];
+      if (fma(e.x, e.x, e.y * e.y) > kTo1 * kTo1) {
+        const double2 v = cmul(d, make_double2(-e.x, -e.y));
+        qx.add(w * v.x);
+        qy.add(w * v.y);
+      }
+    }
+    if (occ) {
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        const double2 a = occ_ach[((size_t)n1 * p.ng + col) * kNW + iw];
+        const double2 x = occ_asx[((size_t)n1 * p.ng + col) * kNW + iw];
+        ax[iw].add(a.x);
+        ay[iw].add(a.y);
+        sx[iw].add(x.x);
+        sy[iw].add(x.y);
+      }
+    } else if (igp > 0 && igp % kIgBlk == 0) {
+      double2 z[3];
+      half_factor(p.wt[off], p.ieps[off], wx, z);
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        const double2 v = cmul(d, z[iw]);
+        ax[iw].add(w * v.x);
+        ay[iw].add(w * v.y);
+      }
+    }
+  }
+#pragma unroll
+  for (int iw = 0; iw < kNW; ++iw) {
+    const double rx = warp_sum_comp(ax[iw]), ry = warp_sum_comp(ay[iw]);
+    const double ux = warp_sum_comp(sx[iw]), uy = warp_sum_comp(sy[iw]);
+    if (lane == 0) {
+      if (occ) {
+        acht_n1[n1 * kNW + iw] = make_double2(rx, ry);
+        asx_n1[n1 * kNW + iw] = make_double2(ux, uy);
+      } else {
+        const double2 a = t3[(size_t)n1 * kNW + iw], b = u3[(size_t)n1 * kNW + iw];
+        acht_n1[n1 * kNW + iw] = make_double2(rx + a.x + b.x, ry + a.y - b.y);
+      }
+    }
+  }
+  const double vx = warp_sum_comp(qx), vy = warp_sum_comp(qy);
+  if (ts && lane == 0) stat_n1[n1] = make_double2(vx + ts[n1].x + us[n1].x, vy + ts[n1].y - us[n1].y);
+}
+
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 
 template <int NF>
@@ -521,6 +631,12 @@ struct sigma_gpp_halfsum_plan_s {
   double2 *occ_ach = nullptr, *occ_asx = nullptr;
   double2 *acht_n1 = nullptr, *asx_n1 = nullptr, *stat_n1 = nullptr;
   double2 *t_aqsm = nullptr, *t_aqsn = nullptr, *t_ieps = nullptr, *t_wt = nullptr;
+  // tensor-core form: contraction plans over a shared slice workspace, the
+  // factor slabs and the four contraction results
+  sigma_ff_plan ff3 = nullptr, ff1 = nullptr;
+  void* tblock = nullptr;
+  double2* z = nullptr;                                          // [3][ng][nc]
+  double2 *t3 = nullptr, *u3 = nullptr, *ts = nullptr, *us = nullptr;  // [nb][3], [nb][1]
 };
 
 extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int number_bands,
@@ -530,7 +646,9 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
   using namespace sigma;
   if (!out || !inv_igp_index || !indinv) return SIGMA_ERR_NULL;
   *out = nullptr;
-  if (flags & ~(SIGMA_HALFSUM_STATIC | SIGMA_HALFSUM_GVEC_MAJOR)) return SIGMA_ERR_UNSUPPORTED;
+  if (flags & ~(SIGMA_HALFSUM_STATIC | SIGMA_HALFSUM_GVEC_MAJOR | SIGMA_HALFSUM_TENSOR))
+    return SIGMA_ERR_UNSUPPORTED;
+  const bool tensor = (flags & SIGMA_HALFSUM_TENSOR) != 0;
   int st = gpp_check_shape(number_bands, nvband, ncouls, ngpown, nstart, nend);
   if (st != SIGMA_OK) return st;
   if (indinv_len < ncouls) return SIGMA_ERR_INVALID_SHAPE;
@@ -554,9 +672,11 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
   p->flags = flags;
   p->main_grid = p->stat_grid = sms;
   // about half of the items fall past their column block's range (triangle)
-  gpp_size_work(p->wm, nvband, number_bands - nvband, kHBN, kHBP, ncouls, ngpown, p->main_grid, 48);
-  if (flags & SIGMA_HALFSUM_STATIC)
-    gpp_size_work(p->ws, 0, number_bands, kHBN, kHBP, ncouls, ngpown, p->stat_grid, 48);
+  if (!tensor) {
+    gpp_size_work(p->wm, nvband, number_bands - nvband, kHBN, kHBP, ncouls, ngpown, p->main_grid, 48);
+    if (flags & SIGMA_HALFSUM_STATIC)
+      gpp_size_work(p->ws, 0, number_bands, kHBN, kHBP, ncouls, ngpown, p->stat_grid, 48);
+  }
   if (p->wm.n_items < p->main_grid) p->main_grid = std::max(1, p->wm.n_items);
   if (p->ws.n_items < p->stat_grid) p->stat_grid = std::max(1, p->ws.n_items);
   const size_t nbc = (size_t)number_bands * ncouls, ngc = (size_t)ngpown * ncouls;
@@ -594,7 +714,8 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
   p->asx_n1 = reinterpret_cast<double2*>(take(b_asx));
   p->stat_n1 = reinterpret_cast<double2*>(take(b_st));
   p->wm.partial = reinterpret_cast<double2*>(take(b_pm));
-  p->ws.partial = (flags & SIGMA_HALFSUM_STATIC) ? reinterpret_cast<double2*>(take(b_ps)) : nullptr;
+  p->ws.partial = (flags & SIGMA_HALFSUM_STATIC) && !tensor ? reinterpret_cast<double2*>(take(b_ps))
+                                                            : nullptr;
   if (flags & SIGMA_HALFSUM_GVEC_MAJOR) {
     p->t_aqsm = reinterpret_cast<double2*>(take(up256(sizeof(double2) * nbc)));
     p->t_aqsn = reinterpret_cast<double2*>(take(up256(sizeof(double2) * nbc)));
@@ -610,6 +731,41 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
     delete p;
     return SIGMA_ERR_CUDA;
   }
+  if (tensor) {
+    size_t b3 = 0, b1 = 0;
+    st = ff_plan_tile_bytes(number_bands, ncouls, ngpown, 3, &b3);
+    if (st == SIGMA_OK && (flags & SIGMA_HALFSUM_STATIC))
+      st = ff_plan_tile_bytes(number_bands, ncouls, ngpown, 1, &b1);
+    const size_t b_tiles = up256(std::max(b3, b1));
+    const size_t b_z = up256(sizeof(double2) * 3 * ngc);
+    const size_t b_r3 = up256(sizeof(double2) * (size_t)number_bands * kNW);
+    const size_t b_r1 = up256(sizeof(double2) * (size_t)number_bands);
+    if (st == SIGMA_OK) {
+      e = cudaMalloc(&p->tblock, b_tiles + b_z + 2 * b_r3 + 2 * b_r1);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_last_cuda_error(e, "cudaMalloc(halfsum tensor)", __LINE__);
+        st = SIGMA_ERR_ALLOC;
+      }
+    }
+    if (st == SIGMA_OK) {
+      char* t = static_cast<char*>(p->tblock);
+      p->z = reinterpret_cast<double2*>(t + b_tiles);
+      p->t3 = reinterpret_cast<double2*>(t + b_tiles + b_z);
+      p->u3 = reinterpret_cast<double2*>(t + b_tiles + b_z + b_r3);
+      p->ts = reinterpret_cast<double2*>(t + b_tiles + b_z + 2 * b_r3);
+      p->us = reinterpret_cast<double2*>(t + b_tiles + b_z + 2 * b_r3 + b_r1);
+      st = ff_plan_build(&p->ff3, number_bands, ncouls, ngpown, kNW, igp_of, SIGMA_FF_OZAKI_BF16,
+                         p->tblock);
+      if (st == SIGMA_OK && (flags & SIGMA_HALFSUM_STATIC))
+        st = ff_plan_build(&p->ff1, number_bands, ncouls, ngpown, 1, igp_of, SIGMA_FF_OZAKI_BF16,
+                           p->tblock);
+    }
+    if (st != SIGMA_OK) {
+      sigma_gpp_halfsum_plan_destroy(p);
+      return st;
+    }
+  }
   *out = p;
   return SIGMA_OK;
 }
@@ -620,6 +776,9 @@ extern "C" int sigma_gpp_halfsum_plan_destroy(sigma_gpp_halfsum_plan p) {
   cudaGetDevice(&cur);
   cudaSetDevice(p->device);
   if (p->block) cudaFree(p->block);
+  if (p->ff3) sigma_ff_plan_destroy(p->ff3);
+  if (p->ff1) sigma_ff_plan_destroy(p->ff1);
+  if (p->tblock) cudaFree(p->tblock);
   cudaSetDevice(cur);
   delete p;
   return SIGMA_OK;
@@ -667,6 +826,35 @@ extern "C" int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const doub
     half_occ_kernel<<<dim3(plan->ng, kNW), kThreads, 0, s>>>(p, plan->occ_ach, plan->occ_asx);
     SIGMA_CUDA_TRY(cudaGetLastError());
   }
+  if (plan->ff3) {
+    const bool stat = plan->ff1 && achstemp;
+    auto C = [](const double2* x) { return reinterpret_cast<const sigma_complex128*>(x); };
+    auto M = [](double2* x) { return reinterpret_cast<sigma_complex128*>(x); };
+    half_z_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
+    SIGMA_CUDA_TRY(cudaGetLastError());
+    int st = ff_execute_weighted(plan->ff3, C(plan->z), C(aqsn), C(aqsm), vcoul, 0.5, M(plan->t3), stream);
+    if (st == SIGMA_OK)
+      st = ff_execute_weighted(plan->ff3, C(plan->z), C(aqsm), C(aqsm), vcoul, 0.5, M(plan->u3), stream);
+    if (st == SIGMA_OK && stat) {
+      half_zs_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
+      SIGMA_CUDA_TRY(cudaGetLastError());
+      st = ff_execute_weighted(plan->ff1, C(plan->z), C(aqsn), C(aqsm), vcoul, 0.5, M(plan->ts), stream);
+      if (st == SIGMA_OK)
+        st = ff_execute_weighted(plan->ff1, C(plan->z), C(aqsm), C(aqsn), vcoul, 0.5, M(plan->us), stream);
+    }
+    if (st != SIGMA_OK) return st;
+    half_tensor_rows_kernel<<<(plan->nb * 32 + 255) / 256, 256, 0, s>>>(
+        p, plan->t3, plan->u3, stat ? plan->ts : nullptr, plan->us, plan->occ_ach, plan->occ_asx,
+        plan->acht_n1, plan->asx_n1, plan->stat_n1);
+    SIGMA_CUDA_TRY(cudaGetLastError());
+    half_reduce_total_kernel<<<1, 256, 0, s>>>(plan->acht_n1, plan->asx_n1, plan->stat_n1, plan->nb,
+                                               plan->nvband, reinterpret_cast<double2*>(achtemp),
+                                               reinterpret_cast<double2*>(asxtemp),
+                                               stat ? reinterpret_cast<double2*>(achstemp) : nullptr,
+                                               reinterpret_cast<double2*>(acht_n1_loc));
+    SIGMA_CUDA_TRY(cudaGetLastError());
+    return SIGMA_OK;
+  }
   if (plan->wm.n_items > 0) SIGMA_CUDA_TRY(launch_half_main<3>(p, plan->wm, plan->main_grid, s));
   const bool stat = plan->ws.partial && achstemp;
   if (stat && plan->ws.n_items > 0) SIGMA_CUDA_TRY(launch_half_main<1>(p, plan->ws, plan->stat_grid, s));
@@ -695,16 +883,14 @@ extern "C" int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const doub
   return SIGMA_OK;
 }
 
-extern "C" int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, int ngpown,
-                                      int nstart, int nend, const int* inv_igp_index,
-                                      const int* indinv, const double* wx_array, double occ,
-                                      const sigma_complex128* aqsmtemp,
-                                      const sigma_complex128* aqsntemp,
-                                      const sigma_complex128* I_eps_array,
-                                      const sigma_complex128* wtilde_array, const double* vcoul,
-                                      sigma_complex128* achtemp, sigma_complex128* asxtemp,
-                                      sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
-                                      void* stream) {
+namespace {
+
+int halfsum_host(bool tensor, int number_bands, int nvband, int ncouls, int ngpown, int nstart,
+                 int nend, const int* inv_igp_index, const int* indinv, const double* wx_array,
+                 double occ, const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
+                 const sigma_complex128* I_eps_array, const sigma_complex128* wtilde_array,
+                 const double* vcoul, sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                 sigma_complex128* acht_n1_loc, sigma_complex128* achstemp, void* stream) {
   using namespace sigma;
   if (!inv_igp_index || !indinv || !wx_array || !aqsmtemp || !aqsntemp || !I_eps_array ||
       !wtilde_array || !vcoul || !achtemp || !asxtemp)
@@ -713,7 +899,8 @@ extern "C" int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, 
   if (st != SIGMA_OK) return st;
   std::lock_guard<std::mutex> lk(api_mutex());
   sigma_gpp_halfsum_plan plan = nullptr;
-  const int flags = SIGMA_HALFSUM_GVEC_MAJOR | (achstemp ? SIGMA_HALFSUM_STATIC : 0);
+  const int flags = SIGMA_HALFSUM_GVEC_MAJOR | (achstemp ? SIGMA_HALFSUM_STATIC : 0) |
+                    (tensor ? SIGMA_HALFSUM_TENSOR : 0);
   st = sigma_gpp_halfsum_plan_create(&plan, number_bands, nvband, ncouls, ngpown, nstart, nend,
                                      inv_igp_index, indinv, ncouls, flags);
   if (st != SIGMA_OK) return st;
@@ -765,4 +952,36 @@ extern "C" int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, 
   const int rc = run();
   sigma_gpp_halfsum_plan_destroy(plan);
   return rc;
+}
+
+}  // namespace
+
+extern "C" int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, int ngpown,
+                                      int nstart, int nend, const int* inv_igp_index,
+                                      const int* indinv, const double* wx_array, double occ,
+                                      const sigma_complex128* aqsmtemp,
+                                      const sigma_complex128* aqsntemp,
+                                      const sigma_complex128* I_eps_array,
+                                      const sigma_complex128* wtilde_array, const double* vcoul,
+                                      sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                                      sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
+                                      void* stream) {
+  return halfsum_host(false, number_bands, nvband, ncouls, ngpown, nstart, nend, inv_igp_index,
+                      indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul,
+                      achtemp, asxtemp, acht_n1_loc, achstemp, stream);
+}
+
+extern "C" int sigma_gpp_halfsum_tensor(int number_bands, int nvband, int ncouls, int ngpown,
+                                        int nstart, int nend, const int* inv_igp_index,
+                                        const int* indinv, const double* wx_array, double occ,
+                                        const sigma_complex128* aqsmtemp,
+                                        const sigma_complex128* aqsntemp,
+                                        const sigma_complex128* I_eps_array,
+                                        const sigma_complex128* wtilde_array, const double* vcoul,
+                                        sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                                        sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
+                                        void* stream) {
+  return halfsum_host(true, number_bands, nvband, ncouls, ngpown, nstart, nend, inv_igp_index,
+                      indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul,
+                      achtemp, asxtemp, acht_n1_loc, achstemp, stream);
 }

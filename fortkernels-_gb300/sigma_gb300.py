@@ -74,6 +74,8 @@ SIGNATURES = {
     "sigma_gpp_real_plan_destroy": ([_P], _I),
     "sigma_gpp_halfsum_fp64": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
                                _I),
+    "sigma_gpp_halfsum_tensor": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+                                 _I),
     "sigma_gpp_halfsum_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I, _I], _I),
     "sigma_gpp_halfsum_execute": ([_P, _P, _D] + [_P] * 10, _I),
     "sigma_gpp_halfsum_plan_destroy": ([_P], _I),
@@ -188,14 +190,16 @@ def gpp_real_host(prob, stream: int = 0, want_n1: bool = True):
     return ach, asx, n1
 
 
-HALFSUM_STATIC, HALFSUM_GVEC_MAJOR = 1, 2
+HALFSUM_STATIC, HALFSUM_GVEC_MAJOR, HALFSUM_TENSOR = 1, 2, 4
 
 
-def gpp_halfsum_host(prob, stream: int = 0, want_n1: bool = True, want_static: bool = True):
-    """gppsum = 1 host drop-in (sigma_gpp_halfsum_fp64) on a workload.GppProblem
-    held band-major; the arrays are handed over in gppKerSeq.cpp's
-    g-vector-major layout, as that driver stores them.  Returns (achtemp[3],
-    asxtemp[3], acht_n1_loc[nb] or None, achstemp or None) complex128."""
+def gpp_halfsum_host(prob, stream: int = 0, want_n1: bool = True, want_static: bool = True,
+                     tensor: bool = False):
+    """gppsum = 1 host drop-in (sigma_gpp_halfsum_fp64, or with tensor=True
+    sigma_gpp_halfsum_tensor) on a workload.GppProblem held band-major; the
+    arrays are handed over in gppKerSeq.cpp's g-vector-major layout, as that
+    driver stores them.  Returns (achtemp[3], asxtemp[3], acht_n1_loc[nb] or
+    None, achstemp or None) complex128."""
     lib = load()
     inv = np.ascontiguousarray(prob.inv_igp_index, dtype=np.int32)
     indinv = np.ascontiguousarray(prob.indinv, dtype=np.int32)
@@ -205,11 +209,12 @@ def gpp_halfsum_host(prob, stream: int = 0, want_n1: bool = True, want_static: b
     ach, asx = np.zeros(3, np.complex128), np.zeros(3, np.complex128)
     n1 = np.zeros(prob.number_bands, np.complex128) if want_n1 else None
     stat = np.zeros(1, np.complex128) if want_static else None
-    st = lib.sigma_gpp_halfsum_fp64(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart,
-                                    prob.nend, _ptr(inv), _ptr(indinv), _ptr(wx), prob.occ,
-                                    *[_ptr(a) for a in arrs], _ptr(vcoul), _ptr(ach), _ptr(asx), _ptr(n1),
-                                    _ptr(stat), stream)
-    _check(st, "sigma_gpp_halfsum_fp64")
+    fn = lib.sigma_gpp_halfsum_tensor if tensor else lib.sigma_gpp_halfsum_fp64
+    st = fn(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, prob.nstart,
+            prob.nend, _ptr(inv), _ptr(indinv), _ptr(wx), prob.occ,
+            *[_ptr(a) for a in arrs], _ptr(vcoul), _ptr(ach), _ptr(asx), _ptr(n1),
+            _ptr(stat), stream)
+    _check(st, fn.__name__)
     return ach, asx, n1, (stat[0] if want_static else None)
 
 

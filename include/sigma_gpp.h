@@ -316,8 +316,10 @@ int sigma_gpp_real_plan_destroy(sigma_gpp_real_plan plan);
  * NULL), achstemp[1] (may be NULL: the static remainder is then not run).
  * ------------------------------------------------------------------------- */
 enum {
-  SIGMA_HALFSUM_STATIC = 1,    /* plan also evaluates the static remainder achstemp */
-  SIGMA_HALFSUM_GVEC_MAJOR = 2 /* execute takes gppKerSeq.cpp's [ncouls][...] layout */
+  SIGMA_HALFSUM_STATIC = 1,     /* plan also evaluates the static remainder achstemp */
+  SIGMA_HALFSUM_GVEC_MAJOR = 2, /* execute takes gppKerSeq.cpp's [ncouls][...] layout */
+  SIGMA_HALFSUM_TENSOR = 4      /* the band sums as split-BF16 tcgen05 contractions (FP32-class
+                                   error, ~1e-7 relative); occupied bands stay FP64 */
 };
 int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
                            int nend, const int* inv_igp_index, const int* indinv,
@@ -327,6 +329,16 @@ int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, int ngpown,
                            sigma_complex128* achtemp, sigma_complex128* asxtemp,
                            sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
                            void* stream);
+
+/* The same with the band sums on the tensor cores (SIGMA_HALFSUM_TENSOR). */
+int sigma_gpp_halfsum_tensor(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
+                             int nend, const int* inv_igp_index, const int* indinv,
+                             const double* wx_array, double occ, const sigma_complex128* aqsmtemp,
+                             const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                             const sigma_complex128* wtilde_array, const double* vcoul,
+                             sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                             sigma_complex128* acht_n1_loc, sigma_complex128* achstemp,
+                             void* stream);
 
 /* Device-resident form.  Without SIGMA_HALFSUM_GVEC_MAJOR execute takes the
  * library's band-major layout (aqsmtemp / aqsntemp [number_bands][ncouls],

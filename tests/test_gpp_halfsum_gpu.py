@@ -128,3 +128,26 @@ def test_halfsum_config0_shape_random(sigma_lib):
     p = W.gpp_random(128, 2, 8192, 409, 80)
     o = O.gpp_halfsum(p)
     _check(sigma_lib.gpp_halfsum_host(p), o, 2)
+
+
+# ---- tensor-core form (SIGMA_HALFSUM_TENSOR): band sums as split-BF16
+# contractions, FP32-class error; against the FP64 form (itself pinned above)
+TENSOR_CASES = [
+    (40, 3, 2048, 100, 81, False),
+    (37, 2, 1536, 33, 82, True),      # unpaired igp terms, near-pole wtilde
+    (70, 0, 4096, 130, 83, False),    # no occupied band
+]
+
+
+@pytest.mark.parametrize("case", TENSOR_CASES, ids=lambda c: "x".join(map(str, c[:4])) + ("s" if c[5] else ""))
+def test_halfsum_tensor_matches_fp64(sigma_lib, case):
+    nb, nvb, nc, ng, seed, stress = case
+    p = W.gpp_random(nb, nvb, nc, ng, seed, stress=stress)
+    f = sigma_lib.gpp_halfsum_host(p)
+    t = sigma_lib.gpp_halfsum_host(p, tensor=True)
+    rel = lambda a, b: np.abs(a - b) / np.abs(b)
+    assert np.all(rel(t[0], f[0]) <= 2e-6), rel(t[0], f[0])
+    if nvb:
+        assert np.all(rel(t[1], f[1]) <= 1e-12)     # occupied bands run in FP64 in both forms
+    assert rel(t[3], f[3]) <= 2e-6
+    assert np.linalg.norm(t[2] - f[2]) <= 1e-6 * np.linalg.norm(f[2])
