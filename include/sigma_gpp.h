@@ -319,7 +319,8 @@ enum {
   SIGMA_HALFSUM_STATIC = 1,     /* plan also evaluates the static remainder achstemp */
   SIGMA_HALFSUM_GVEC_MAJOR = 2, /* execute takes gppKerSeq.cpp's [ncouls][...] layout */
   SIGMA_HALFSUM_TENSOR = 4      /* the band sums as split-BF16 tcgen05 contractions (FP32-class
-                                   error, ~1e-7 relative); occupied bands stay FP64 */
+                                   error, ~1e-7 relative); occupied bands stay FP64; needs
+                                   ngpown of at least ~18, as sigma_gpp_tensor */
 };
 int sigma_gpp_halfsum_fp64(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
                            int nend, const int* inv_igp_index, const int* indinv,
