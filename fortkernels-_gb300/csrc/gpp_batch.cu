@@ -32,12 +32,14 @@ struct sigma_gpp_batch_s {
   std::vector<sigma::GppDev> dev;
   std::vector<sigma::GppWork> sch, ssx;
   std::vector<sigma::MixedPrep> prep;
+  std::vector<sigma::GppWork> prepw;  // pre-pass block counts per instance
   std::vector<int> tile, sch_off, ssx_off;
   std::vector<double2*> acht_n1;
   std::vector<sigma_gpp_instance> inst;
   long long terms = 0;
   int sch_grid = 0, ssx_grid = 0, launches = 0;
   bool all_shared_wx = true;  // every instance has one frequency set for all bands
+  bool mixedy = false;        // mixed main pass on the shared-factor kernel
   void* block = nullptr;
   sigma::GppBatchView sch_view{}, ssx_view{};
   int* counters = nullptr;  // [0] main pass, [1] occupied-band pass, [2] status
@@ -137,13 +139,19 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   b->terms = terms;
   b->inst.assign(inst, inst + n_instances);
   for (int i = 0; i < n_instances; ++i) b->all_shared_wx = b->all_shared_wx && inst[i].wx_band_stride == 0;
-  b->sch_grid = sms * (mixed ? sch_batch_blocks_per_sm_mixed()
-                             : (all_shared ? sch_batch_blocks_per_sm_fp64y() : sch_batch_blocks_per_sm_fp64()));
+  // mixed with one frequency set per instance: the shared-factor kernel
+  const bool mixedy = precision == SIGMA_PREC_MIXED && all_shared;
+  b->mixedy = mixedy;
+  b->sch_grid = sms * (mixedy ? sch_batch_blocks_per_sm_mixedy()
+                              : mixed ? sch_batch_blocks_per_sm_mixed()
+                                      : (all_shared ? sch_batch_blocks_per_sm_fp64y()
+                                                    : sch_batch_blocks_per_sm_fp64()));
   b->ssx_grid = sms * (mixed ? ssx_batch_blocks_per_sm_mixed() : ssx_batch_blocks_per_sm_fp64());
   b->dev.resize(n_instances);
   b->sch.resize(n_instances);
   b->ssx.resize(n_instances);
   b->prep.resize(n_instances);
+  b->prepw.resize(n_instances);
   b->tile.resize(n_instances);
   b->acht_n1.resize(n_instances);
   b->sch_off.assign(n_instances + 1, 0);
@@ -167,7 +175,8 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
                                ? tile_shape[i]
                                : least_padding_tile(q.number_bands, q.ngpown, all_shared));
     b->tile[i] = t;
-    const int bn = mixed ? kBN : tile_bn(t), bp = mixed ? kBPM : tile_bp(t);
+    const int bn = mixedy ? 2 * kBN : (mixed ? kBN : tile_bn(t));
+    const int bp = mixedy ? 2 * kBPM : (mixed ? kBPM : tile_bp(t));
     size_instance(b->sch[i], q.number_bands, bn, bp, q.ncouls, q.ngpown, target);
     size_instance(b->ssx[i], q.nvband, kSsxBN, kSsxBP, q.ncouls, q.ngpown, ssx_target);
     b->sch_off[i + 1] = b->sch_off[i] + b->sch[i].n_items;
@@ -181,9 +190,17 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
     total += up256(sizeof(double2) * (size_t)b->sch[i].n_items * bn * kNW);
     o_ssx[i] = total;
     total += up256(sizeof(double2) * (size_t)b->ssx[i].n_items * kSsxBN * kNW);
+    // pre-pass blocks (kBN bands, kBPM columns): twice the items' with the
+    // shared-factor kernel, whose items span two of each
+    GppWork& pw = b->prepw[i];
+    pw = b->sch[i];
+    if (mixedy) {
+      pw.n_col_blocks = 2 * b->sch[i].n_col_blocks;
+      pw.n_band_blocks = 2 * b->sch[i].n_band_blocks;
+    }
     if (mixed) {
-      const size_t col = (size_t)b->sch[i].n_col_blocks * kBPM * nc_pad;
-      const size_t band = (size_t)b->sch[i].n_band_blocks * kBN * nc_pad;
+      const size_t col = (size_t)pw.n_col_blocks * kBPM * nc_pad;
+      const size_t band = (size_t)pw.n_band_blocks * kBN * nc_pad;
       o_a[i] = total;
       total += up256(sizeof(float4) * col);
       o_b[i] = total;
@@ -337,7 +354,7 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   if (mixed)
     for (int i = 0; i < b->n; ++i)
       if (b->sch[i].n_items > 0 && (!tensor || b->ssx[i].n_items > 0))
-        SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->sch[i], b->prep[i], s));
+        SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->prepw[i], b->prep[i], s));
   if (tensor) {
     for (int i = 0; i < b->n; ++i) {
       SIGMA_CUDA_TRY(launch_gpp_y_factor(b->dev[i], b->yfac, s));
@@ -347,7 +364,8 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
       if (st != SIGMA_OK) return st;
     }
   } else if (b->sch_view.total > 0)
-    SIGMA_CUDA_TRY(mixed ? launch_sch_mixed_batch(b->sch_view, b->sch_grid, s)
+    SIGMA_CUDA_TRY(b->mixedy ? launch_sch_mixedy_batch(b->sch_view, b->sch_grid, s)
+                   : mixed ? launch_sch_mixed_batch(b->sch_view, b->sch_grid, s)
                          : (b->all_shared_wx ? launch_sch_fp64y_batch(b->sch_view, b->sch_grid, s)
                                              : launch_sch_fp64_batch(b->sch_view, b->sch_grid, s)));
   if (b->ssx_view.total > 0)

@@ -48,6 +48,10 @@ cudaError_t launch_ssx_fp64_batch(const GppBatchView& b, int grid, cudaStream_t 
 cudaError_t launch_sch_mixed_batch(const GppBatchView& b, int grid, cudaStream_t s);
 cudaError_t launch_ssx_mixed_batch(const GppBatchView& b, int grid, bool all_shared_wx, cudaStream_t s);
 cudaError_t launch_sch_fp64y_batch(const GppBatchView& b, int grid, cudaStream_t s);
+// Mixed main pass with one frequency set per instance: items of 2*kBN bands x
+// 2*kBPM columns (the pre-pass must cover twice the items' block counts).
+cudaError_t launch_sch_mixedy_batch(const GppBatchView& b, int grid, cudaStream_t s);
+int sch_batch_blocks_per_sm_mixedy();
 int sch_batch_blocks_per_sm_fp64();
 int sch_batch_blocks_per_sm_fp64y();
 int ssx_batch_blocks_per_sm_fp64();
