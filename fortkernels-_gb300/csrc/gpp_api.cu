@@ -298,9 +298,12 @@ extern "C" int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, doubl
   if (other_ms) *other_ms = tr;
   if (launches_per_execution) {
     const bool mixed = plan->precision == SIGMA_PREC_MIXED;
-    if (plan->precision == SIGMA_PREC_TENSOR)  // pre-pass (2), factors, slicing (2), GEMM, its reduction
-      *launches_per_execution = 7 + (plan->ssx.n_items > 0 ? 1 : 0) + 2;
-    else
+    if (plan->precision == SIGMA_PREC_TENSOR) {
+      // factors (+ band operands with occupied bands), slicing and epilogue
+      // factors (3), GEMM, its reduction; the occupied-band pass; 2 reductions
+      const bool occ = plan->ssx.n_items > 0;
+      *launches_per_execution = (occ ? 2 : 1) + 3 + 2 + (occ ? 1 : 0) + 2;
+    } else
       *launches_per_execution = (plan->sch.n_items > 0 ? (mixed ? 3 : 1) : 0) +
                                 (plan->ssx.n_items > 0 ? 1 : 0) + 2;
   }
@@ -357,8 +360,7 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (tensor && wx_band_stride != 0) return SIGMA_ERR_UNSUPPORTED;  // needs one frequency set
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
   const bool mixed = plan->precision == SIGMA_PREC_MIXED;
-  if ((mixed || (tensor && plan->ssx.n_items > 0)) && plan->sch.n_items > 0)
-    SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->prepw, plan->prep, s));
+  if (mixed && plan->sch.n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->prepw, plan->prep, s));
   // one frequency set for every band: the shared-factor kernels
   const bool ypath = !mixed && !tensor && wx_band_stride == 0 && plan->schy.n_items > 0;
   const bool mypath = mixed && wx_band_stride == 0 && plan->schmy.n_items > 0;
@@ -366,7 +368,9 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (tensor) main.partial = nullptr;  // band sums land in acht_n1 directly
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
   if (tensor) {
-    SIGMA_CUDA_TRY(launch_gpp_y_factor(p, plan->yfac, s));
+    // factors, and the occupied-band operands from the same pass
+    SIGMA_CUDA_TRY(launch_tensor_factors(p, plan->yfac, plan->prepw,
+                                         plan->ssx.n_items > 0 ? &plan->prep : nullptr, s));
     const int st = ff_execute_weighted(plan->ff, reinterpret_cast<const sigma_complex128*>(plan->yfac),
                                        aqsntemp, aqsmtemp, vcoul, 0.5,
                                        reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream);

@@ -334,8 +334,11 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
         return st;
       }
     }
-    // per instance: pre-pass (2), factors, slicing (2), GEMM, its reduction; then ssx and reductions
-    b->launches = 7 * n_instances + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
+    // per instance: factors (+ band operands with occupied bands), slicing and
+    // epilogue factors (3), GEMM, its reduction; then ssx and the reductions
+    int per = 0;
+    for (int i = 0; i < n_instances; ++i) per += (b->ssx[i].n_items > 0 ? 2 : 1) + 3 + 2;
+    b->launches = per + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
   }
   *out = b;
   return SIGMA_OK;
@@ -351,13 +354,14 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   const bool tensor = b->precision == SIGMA_PREC_TENSOR;
   const bool mixed = b->precision == SIGMA_PREC_MIXED || tensor;
   SIGMA_CUDA_TRY(cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), s));
-  if (mixed)
+  if (mixed && !tensor)
     for (int i = 0; i < b->n; ++i)
-      if (b->sch[i].n_items > 0 && (!tensor || b->ssx[i].n_items > 0))
-        SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->prepw[i], b->prep[i], s));
+      if (b->sch[i].n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->prepw[i], b->prep[i], s));
   if (tensor) {
     for (int i = 0; i < b->n; ++i) {
-      SIGMA_CUDA_TRY(launch_gpp_y_factor(b->dev[i], b->yfac, s));
+      // factors, and the occupied-band operands from the same pass
+      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], b->yfac, b->prepw[i],
+                                           b->ssx[i].n_items > 0 ? &b->prep[i] : nullptr, s));
       const int st = ff_execute_weighted(b->ff[i], reinterpret_cast<const sigma_complex128*>(b->yfac),
                                          b->inst[i].aqsntemp, b->inst[i].aqsmtemp, b->inst[i].vcoul, 0.5,
                                          reinterpret_cast<sigma_complex128*>(b->acht_n1[i]), stream);

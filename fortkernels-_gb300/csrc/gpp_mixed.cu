@@ -216,6 +216,79 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
   }
 }
 
+// Tensor form with one frequency set: the frequency factors
+//   y[iw][my_igp][ig] = G (c + i b) / (c^2 + b^2)   (0 when the guard drops it)
+// in FP64 with the FP64 path's decisions, and in the same pass (same inputs,
+// same G and threshold) the pre-pass operands of the occupied-band kernel
+// (colA with the exact keep and second-branch bits, colB = G, colC =
+// Omega2) when m.colA is set.  Tiles of kBPM columns x 32 g-vectors: factor
+// writes run along g-vectors, operand writes go through shared memory.
+__global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, double2* y, MixedPrep m,
+                                                             int n_col_blocks) {
+  __shared__ float4 ta[32][kBPM + 1];
+  __shared__ float2 tb[32][kBPM + 1];
+  __shared__ float2 tc[32][kBPM + 1];
+  const int tid = threadIdx.x;
+  const size_t plane = (size_t)p.ng * p.nc;
+  const double wx[kNW] = {p.wx[0], p.wx[1], p.wx[2]};
+  const bool ops = m.colA != nullptr;
+  const long long tiles = (long long)n_col_blocks * (m.nc_pad / 32);
+  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int cb = (int)(t / (m.nc_pad / 32));
+    const int ig0 = (int)(t % (m.nc_pad / 32)) * 32;
+    __syncthreads();
+    for (int e = tid; e < 32 * kBPM; e += 256) {
+      const int pl = e / 32, k = e % 32;  // reads and factor writes run along g-vectors
+      const int my_igp = cb * kBPM + pl, ig = ig0 + k;
+      float4 a = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
+      float2 g32 = make_float2(0.f, 0.f), om = make_float2(0.f, 0.f);
+      if (my_igp < p.ng && ig < p.nc) {
+        const size_t off = (size_t)my_igp * p.nc + ig;
+        const double2 wt = p.wt[off];
+        const double2 ie = p.ieps[off];
+        const double2 g = cmul(ie, wt);
+        const double b = wt.y, b2 = guard_b2(b);
+        const double thr = guard_thr(wt.x, b2);
+        const double thr2 = p.nvband > 0 ? guard_thr2(wt.x, b2) : 0.0;
+        unsigned mask = 0u;
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          const double c = __dsub_rn(wx[iw], wt.x);
+          const double wv = fma(c, c, b2);
+          const bool keep = gt_nonneg(wv, thr);
+          const double r = keep ? rcp_f64_seed32(wv) : 0.0;
+          const double zr = c * r, zi = b * r;
+          y[(size_t)iw * plane + off] = make_double2(fma(g.x, zr, -g.y * zi), fma(g.x, zi, g.y * zr));
+          mask |= keep ? (1u << iw) : 0u;
+          if (!keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv)) mask |= 8u << iw;
+        }
+        if (ops) {
+          split_f(wt.x, a.x, a.y);
+          a.z = __double2float_rn(wt.y);
+          a.w = __uint_as_float(mask);
+          g32 = make_float2(__double2float_rn(g.x), __double2float_rn(g.y));
+          if (m.colC) {
+            const double2 o2 = cmul(wt, g);  // Omega2 = wtilde^2 I_eps
+            om = make_float2(__double2float_rn(o2.x), __double2float_rn(o2.y));
+          }
+        }
+      }
+      ta[k][pl] = a;
+      tb[k][pl] = g32;
+      tc[k][pl] = om;
+    }
+    if (!ops) continue;
+    __syncthreads();
+    for (int e = tid; e < 32 * kBPM; e += 256) {
+      const int k = e / kBPM, pl = e % kBPM;  // operand writes run along columns
+      const size_t o = ((size_t)cb * m.nc_pad + ig0 + k) * kBPM + pl;
+      m.colA[o] = ta[k][pl];
+      m.colB[o] = tb[k][pl];
+      if (m.colC) m.colC[o] = tc[k][pl];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) prep_bands_kernel(GppDev p, MixedPrep m, int band_begin,
                                                          int band_count, int n_band_blocks) {
   __shared__ float2 tn[32][kBN + 1];
@@ -769,6 +842,23 @@ int sch_blocks_per_sm_mixed() {
   cudaFuncSetAttribute(sch_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(SchSmemM));
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sch_mixed_kernel, kThreads, sizeof(SchSmemM));
   return n > 0 ? n : 1;
+}
+
+cudaError_t launch_tensor_factors(const GppDev& p, double2* y, const GppWork& w, const MixedPrep* m,
+                                  cudaStream_t s) {
+  const int sms = 152;
+  MixedPrep mm{};
+  if (m) {
+    mm = *m;
+    prep_bands_kernel<<<sms * 4, 256, 0, s>>>(p, mm, w.band_begin, w.band_count, w.n_band_blocks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  } else {
+    mm.nc_pad = (p.nc + 31) / 32 * 32;  // tiles over the factor slabs alone
+  }
+  const int ncb = m ? w.n_col_blocks : (p.ng + kBPM - 1) / kBPM;
+  tensor_factors_kernel<<<sms * 8, 256, 0, s>>>(p, y, mm, ncb);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_prep_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, cudaStream_t s) {

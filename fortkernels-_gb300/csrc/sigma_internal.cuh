@@ -152,6 +152,10 @@ int ssx_blocks_per_sm(int precision);
 // Tensor form: frequency factors y[iw][my_igp][ig] of one shared frequency
 // set (gpp_tensor.cu).
 cudaError_t launch_gpp_y_factor(const GppDev& p, double2* y, cudaStream_t s);
+// The same factors together with the occupied-band kernel's pre-pass
+// operands (w: the pre-pass blocks; m null: factors only).
+cudaError_t launch_tensor_factors(const GppDev& p, double2* y, const GppWork& w, const MixedPrep* m,
+                                  cudaStream_t s);
 
 // Sums the partials of the sch and ssx passes in a fixed order into
 // acht_n1[nb][3] (workspace), achtemp[3], asxtemp[3] and acht_n1_loc[nb].
