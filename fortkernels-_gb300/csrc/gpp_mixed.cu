@@ -216,7 +216,12 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
   }
 }
 
-// Tensor form with one frequency set: the frequency factors
+// Tensor form (precision SIGMA_PREC_TENSOR).  With one frequency set for
+// every band a term factors as
+//   scha = conj(aqsm[n1][igp]) * aqsn[n1][ig] * Y_iw[my_igp][ig],
+// so the band sum is the FF contraction (ff_ozaki.cu) with the three
+// frequencies as slabs and the column weight 0.5 vcoul[igp].  This kernel
+// forms the frequency factors
 //   y[iw][my_igp][ig] = G (c + i b) / (c^2 + b^2)   (0 when the guard drops it)
 // in FP64 with the FP64 path's decisions, and in the same pass (same inputs,
 // same G and threshold) the pre-pass operands of the occupied-band kernel

@@ -150,10 +150,8 @@ int sch_blocks_per_sm(int precision);
 int ssx_blocks_per_sm(int precision);
 
 // Tensor form: frequency factors y[iw][my_igp][ig] of one shared frequency
-// set (gpp_tensor.cu).
-cudaError_t launch_gpp_y_factor(const GppDev& p, double2* y, cudaStream_t s);
-// The same factors together with the occupied-band kernel's pre-pass
-// operands (w: the pre-pass blocks; m null: factors only).
+// set, together with the occupied-band kernel's pre-pass operands
+// (w: the pre-pass blocks; m null: factors only).
 cudaError_t launch_tensor_factors(const GppDev& p, double2* y, const GppWork& w, const MixedPrep* m,
                                   cudaStream_t s);
 
