@@ -208,12 +208,22 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
 // g-vectors is then a complex GEMM (bands x g-vectors times g-vectors x
 // (column, frequency)) on the FP64 pipe, 16 x 16 threads with a
 // (BN/16 bands x BP/16 columns x 3 frequencies) register tile each.
+//
+// The complex multiply-accumulate runs with three real products per term
+// instead of four: with the chunk's sums n.x + n.y (per band) and
+// Y.x + Y.y (per column and frequency) staged beside the operands,
+//   P1 = sum n.x Y.x,  P2 = sum n.y Y.y,  P3 = sum (n.x + n.y)(Y.x + Y.y),
+//   sum n Y = (P1 - P2) + i (P3 - P1 - P2),
+// 3 DFMA per term.  In FP64 the extra roundings (the two sums and the final
+// subtractions) stay near 1e-16 of the partial sums.
 constexpr int kCKY = 16;  // g-vectors per staged chunk
 
 template <int BN, int BP>
 struct SchYSmem {
   double2 y[kCKY][kNW][BP];
+  double ys[kCKY][kNW][BP];  // Y.x + Y.y
   double2 n[kCKY][BN];
+  double ns[kCKY][BN];       // n.x + n.y
 };
 
 // Bounded wait for a gate word written by a host-to-device copy (about 1 s).
@@ -246,13 +256,13 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const int ig_end = min(ig_begin + w.split_len, p.nc);
   const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
 
-  double2 acc[TB][TC][kNW];
+  double p1[TB][TC][kNW], p2[TB][TC][kNW], p3[TB][TC][kNW];
 #pragma unroll
   for (int i = 0; i < TB; ++i)
 #pragma unroll
     for (int j = 0; j < TC; ++j)
 #pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = make_double2(0.0, 0.0);
+      for (int iw = 0; iw < kNW; ++iw) p1[i][j][iw] = p2[i][j][iw] = p3[i][j][iw] = 0.0;
 
   for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCKY) {
     __syncthreads();
@@ -282,6 +292,9 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       sm.y[k][0][pl] = y0;
       sm.y[k][1][pl] = y1;
       sm.y[k][2][pl] = y2;
+      sm.ys[k][0][pl] = __dadd_rn(y0.x, y0.y);
+      sm.ys[k][1][pl] = __dadd_rn(y1.x, y1.y);
+      sm.ys[k][2][pl] = __dadd_rn(y2.x, y2.y);
     }
     for (int e = tid; e < kCKY * BN; e += kThreads) {
       const int k = e % kCKY, bl = e / kCKY;
@@ -289,29 +302,35 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
       sm.n[k][bl] = v;
+      sm.ns[k][bl] = __dadd_rn(v.x, v.y);
     }
     __syncthreads();
 
 #pragma unroll 2
     for (int k = 0; k < kCKY; ++k) {
       double2 nn[TB], y[TC][kNW];
+      double nsum[TB], ysum[TC][kNW];
 #pragma unroll
-      for (int i = 0; i < TB; ++i) nn[i] = sm.n[k][ty + 16 * i];
+      for (int i = 0; i < TB; ++i) {
+        nn[i] = sm.n[k][ty + 16 * i];
+        nsum[i] = sm.ns[k][ty + 16 * i];
+      }
 #pragma unroll
       for (int j = 0; j < TC; ++j)
 #pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) y[j][iw] = sm.y[k][iw][tx + 16 * j];
+        for (int iw = 0; iw < kNW; ++iw) {
+          y[j][iw] = sm.y[k][iw][tx + 16 * j];
+          ysum[j][iw] = sm.ys[k][iw][tx + 16 * j];
+        }
 #pragma unroll
       for (int i = 0; i < TB; ++i)
 #pragma unroll
         for (int j = 0; j < TC; ++j)
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            double2& a = acc[i][j][iw];
-            a.x = fma(nn[i].x, y[j][iw].x, a.x);
-            a.x = fma(-nn[i].y, y[j][iw].y, a.x);
-            a.y = fma(nn[i].x, y[j][iw].y, a.y);
-            a.y = fma(nn[i].y, y[j][iw].x, a.y);
+            p1[i][j][iw] = fma(nn[i].x, y[j][iw].x, p1[i][j][iw]);
+            p2[i][j][iw] = fma(nn[i].y, y[j][iw].y, p2[i][j][iw]);
+            p3[i][j][iw] = fma(nsum[i], ysum[j][iw], p3[i][j][iw]);
           }
     }
   }
@@ -335,7 +354,9 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         const double f = 0.5 * p.vcoul[igp];
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          const double2 v = cmul(acc[i][j][iw], m);
+          const double re = __dsub_rn(p1[i][j][iw], p2[i][j][iw]);
+          const double im = __dsub_rn(__dsub_rn(p3[i][j][iw], p1[i][j][iw]), p2[i][j][iw]);
+          const double2 v = cmul(make_double2(re, im), m);
           part[iw].x = fma(v.x, f, part[iw].x);
           part[iw].y = fma(v.y, f, part[iw].y);
         }
