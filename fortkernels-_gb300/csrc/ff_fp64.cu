@@ -6,8 +6,12 @@
 // writes it as zgemm('t','n', ...) (ffkernel.deslippe.best.f90:404).  Here a
 // persistent grid takes (row block, band block, K split) items; each CTA
 // stages 16-wide K chunks of both operands through shared memory and every
-// thread keeps a 4 x 4 complex register tile (4 DFMA per complex
-// multiply-add, the FP64 pipe's natural unit).  The epilogue fuses the second
+// thread keeps a 4 x 4 complex register tile.  Each complex multiply-add is
+// three real products: with the chunk's sums a.x + a.y and b.x + b.y staged
+// beside the operands, P1 = sum a.x b.x, P2 = sum a.y b.y,
+// P3 = sum (a.x + a.y)(b.x + b.y) and sum a b = (P1 - P2) + i (P3 - P1 - P2):
+// 3 DFMA instead of 4 (FP64 roundings of the sums stay near 1e-16 of the
+// partial sums).  The epilogue fuses the second
 // half of the source loop (:408-418): each tile multiplies its tempz values
 // by conj(aqsm[n1][igp(my_igp)]) and sums its rows, so tempz never reaches
 // memory.
@@ -22,10 +26,12 @@ constexpr int kFfThreads = 256;   // 16 x 16 threads, 4 x 4 complex per thread
 struct FfSmem {
   double2 a[kK][kFfRows + 1];
   double2 b[kK][kFfCols + 1];
+  double as[kK][kFfRows + 1];  // a.x + a.y
+  double bs[kK][kFfCols + 1];  // b.x + b.y
   double2 red[16][kFfCols];
 };
 
-__global__ void __launch_bounds__(kFfThreads, 2) ff_fp64_kernel(FfDev p, FfWork w) {
+__global__ void __launch_bounds__(kFfThreads, 1) ff_fp64_kernel(FfDev p, FfWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FfSmem& sm = *reinterpret_cast<FfSmem*>(smem_raw);
   __shared__ int s_item;
@@ -45,11 +51,11 @@ __global__ void __launch_bounds__(kFfThreads, 2) ff_fp64_kernel(FfDev p, FfWork 
     const int k_begin = it.s * w.split_len;
     const int k_end = min(k_begin + w.split_len, p.nc);
 
-    double2 acc[4][4];
+    double p1[4][4], p2[4][4], p3[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+      for (int j = 0; j < 4; ++j) p1[i][j] = p2[i][j] = p3[i][j] = 0.0;
 
     for (int k0 = k_begin; k0 < k_end; k0 += kK) {
       __syncthreads();
@@ -59,6 +65,7 @@ __global__ void __launch_bounds__(kFfThreads, 2) ff_fp64_kernel(FfDev p, FfWork 
         double2 v = make_double2(0.0, 0.0);
         if (g < p.ng && kk < k_end) v = p.epsr[((size_t)f * p.ng + g) * p.nc + kk];
         sm.a[k][r] = v;
+        sm.as[k][r] = __dadd_rn(v.x, v.y);
       }
       for (int e = tid; e < kK * kFfCols; e += kFfThreads) {
         const int c = e / kK, k = e % kK;
@@ -66,23 +73,30 @@ __global__ void __launch_bounds__(kFfThreads, 2) ff_fp64_kernel(FfDev p, FfWork 
         double2 v = make_double2(0.0, 0.0);
         if (n < p.nb && kk < k_end) v = p.aqsn[(size_t)n * p.nc + kk];
         sm.b[k][c] = v;
+        sm.bs[k][c] = __dadd_rn(v.x, v.y);
       }
       __syncthreads();
 #pragma unroll 4
       for (int k = 0; k < kK; ++k) {
         double2 a[4], b[4];
+        double asum[4], bsum[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = sm.a[k][tr + 16 * i];
+        for (int i = 0; i < 4; ++i) {
+          a[i] = sm.a[k][tr + 16 * i];
+          asum[i] = sm.as[k][tr + 16 * i];
+        }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = sm.b[k][tc + 16 * j];
+        for (int j = 0; j < 4; ++j) {
+          b[j] = sm.b[k][tc + 16 * j];
+          bsum[j] = sm.bs[k][tc + 16 * j];
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
-            acc[i][j].x = fma(-a[i].y, b[j].y, acc[i][j].x);
-            acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
-            acc[i][j].y = fma(a[i].y, b[j].x, acc[i][j].y);
+            p1[i][j] = fma(a[i].x, b[j].x, p1[i][j]);
+            p2[i][j] = fma(a[i].y, b[j].y, p2[i][j]);
+            p3[i][j] = fma(asum[i], bsum[j], p3[i][j]);
           }
       }
     }
@@ -105,8 +119,10 @@ __global__ void __launch_bounds__(kFfThreads, 2) ff_fp64_kernel(FfDev p, FfWork 
         double2 m = p.aqsm[(size_t)n * p.nc + igp];  // conj(m) applied below
         m.x *= wgt;
         m.y *= wgt;
-        part[j].x += acc[i][j].x * m.x + acc[i][j].y * m.y;
-        part[j].y += acc[i][j].y * m.x - acc[i][j].x * m.y;
+        const double tre = __dsub_rn(p1[i][j], p2[i][j]);
+        const double tim = __dsub_rn(__dsub_rn(p3[i][j], p1[i][j]), p2[i][j]);
+        part[j].x += tre * m.x + tim * m.y;
+        part[j].y += tim * m.x - tre * m.y;
       }
     }
 #pragma unroll

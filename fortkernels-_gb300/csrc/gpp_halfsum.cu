@@ -26,7 +26,11 @@
 // non-occupied pass and the static remainder are two complex FP64 GEMMs over
 // a triangular g-vector range: items of 32 bands x 32 columns x a g-vector
 // split stage Z once per 16-g-vector chunk for all 32 bands; each thread
-// keeps 2 bands x 2 columns x NF frequencies of T and U (8 DFMA per term).
+// keeps 2 bands x 2 columns x NF frequencies of T and U, each complex
+// multiply-add as three real products (the chunk's sums x.x + x.y staged
+// beside the operands: P1 = sum x.x z.x, P2 = sum x.y z.y, P3 = sum
+// (x.x + x.y)(z.x + z.y), sum x z = (P1 - P2) + i (P3 - P1 - P2)), 6 DFMA per
+// term.
 // Items past a column block's range write zero partials.  Occupied bands run
 // one CTA per (column, frequency).  All partials have fixed slots and are
 // summed in a fixed order with compensation: results are identical run to
@@ -65,6 +69,9 @@ struct HalfSmem {
   double2 z[kHCK][NF][kHBP];
   double2 n[kHCK][kHBN];
   double2 m[kHCK][kHBN];
+  double zs[kHCK][NF][kHBP];  // z.x + z.y
+  double ns[kHCK][kHBN];
+  double ms[kHCK][kHBN];
 };
 
 __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
@@ -127,13 +134,16 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
     const int ig_begin = ic.s * w.split_len;
     const int ig_end = min(min(ig_begin + w.split_len, p.nc), s_kmax);
 
-    double2 T[kHTB][kHTC][NF], U[kHTB][kHTC][NF];
+    // three real sums per complex sum: T from (t1, t2, t3), U from (u1, u2, u3)
+    double t1[kHTB][kHTC][NF], t2[kHTB][kHTC][NF], t3[kHTB][kHTC][NF];
+    double u1[kHTB][kHTC][NF], u2[kHTB][kHTC][NF], u3[kHTB][kHTC][NF];
 #pragma unroll
     for (int i = 0; i < kHTB; ++i)
 #pragma unroll
       for (int j = 0; j < kHTC; ++j)
 #pragma unroll
-        for (int f = 0; f < NF; ++f) T[i][j][f] = U[i][j][f] = make_double2(0.0, 0.0);
+        for (int f = 0; f < NF; ++f)
+          t1[i][j][f] = t2[i][j][f] = t3[i][j][f] = u1[i][j][f] = u2[i][j][f] = u3[i][j][f] = 0.0;
 
     for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kHCK) {
       __syncthreads();
@@ -153,37 +163,54 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
             half_factor(p.wt[off], ie, wx, z);
         }
 #pragma unroll
-        for (int f = 0; f < NF; ++f) sm.z[k][f][pl] = z[f];
+        for (int f = 0; f < NF; ++f) {
+          sm.z[k][f][pl] = z[f];
+          sm.zs[k][f][pl] = __dadd_rn(z[f].x, z[f].y);
+        }
       }
       for (int e = tid; e < kHCK * kHBN; e += kThreads) {
         const int k = e % kHCK, bl = e / kHCK;
         const int ig = ig0 + k, n1 = n1_0 + bl;
         const bool in = ig < ig_end && n1 < p.nb;
         const size_t off = (size_t)n1 * p.nc + ig;
-        sm.n[k][bl] = in ? p.aqsn[off] : make_double2(0.0, 0.0);
-        sm.m[k][bl] = in ? p.aqsm[off] : make_double2(0.0, 0.0);
+        const double2 nv = in ? p.aqsn[off] : make_double2(0.0, 0.0);
+        const double2 mv = in ? p.aqsm[off] : make_double2(0.0, 0.0);
+        sm.n[k][bl] = nv;
+        sm.m[k][bl] = mv;
+        sm.ns[k][bl] = __dadd_rn(nv.x, nv.y);
+        sm.ms[k][bl] = __dadd_rn(mv.x, mv.y);
       }
       __syncthreads();
 #pragma unroll 2
       for (int k = 0; k < kHCK; ++k) {
         double2 nn[kHTB], mm[kHTB], z[kHTC][NF];
+        double nsum[kHTB], msum[kHTB], zsum[kHTC][NF];
 #pragma unroll
         for (int i = 0; i < kHTB; ++i) {
           nn[i] = sm.n[k][ty + 16 * i];
           mm[i] = sm.m[k][ty + 16 * i];
+          nsum[i] = sm.ns[k][ty + 16 * i];
+          msum[i] = sm.ms[k][ty + 16 * i];
         }
 #pragma unroll
         for (int j = 0; j < kHTC; ++j)
 #pragma unroll
-          for (int f = 0; f < NF; ++f) z[j][f] = sm.z[k][f][tx + 16 * j];
+          for (int f = 0; f < NF; ++f) {
+            z[j][f] = sm.z[k][f][tx + 16 * j];
+            zsum[j][f] = sm.zs[k][f][tx + 16 * j];
+          }
 #pragma unroll
         for (int i = 0; i < kHTB; ++i)
 #pragma unroll
           for (int j = 0; j < kHTC; ++j)
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-              cfma(T[i][j][f], nn[i], z[j][f]);
-              cfma(U[i][j][f], mm[i], z[j][f]);
+              t1[i][j][f] = fma(nn[i].x, z[j][f].x, t1[i][j][f]);
+              t2[i][j][f] = fma(nn[i].y, z[j][f].y, t2[i][j][f]);
+              t3[i][j][f] = fma(nsum[i], zsum[j][f], t3[i][j][f]);
+              u1[i][j][f] = fma(mm[i].x, z[j][f].x, u1[i][j][f]);
+              u2[i][j][f] = fma(mm[i].y, z[j][f].y, u2[i][j][f]);
+              u3[i][j][f] = fma(msum[i], zsum[j][f], u3[i][j][f]);
             }
       }
     }
@@ -207,8 +234,12 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
           double2 val[NF];
 #pragma unroll
           for (int f = 0; f < NF; ++f) {
-            val[f] = cmul(cconj(am), T[i][j][f]);
-            cfma(val[f], vp, cconj(U[i][j][f]));
+            const double2 T = make_double2(__dsub_rn(t1[i][j][f], t2[i][j][f]),
+                                           __dsub_rn(__dsub_rn(t3[i][j][f], t1[i][j][f]), t2[i][j][f]));
+            const double2 U = make_double2(__dsub_rn(u1[i][j][f], u2[i][j][f]),
+                                           __dsub_rn(__dsub_rn(u3[i][j][f], u1[i][j][f]), u2[i][j][f]));
+            val[f] = cmul(cconj(am), T);
+            cfma(val[f], vp, cconj(U));
           }
           if (ic.s == 0) {
             const size_t off = (size_t)col * p.nc + igp;
