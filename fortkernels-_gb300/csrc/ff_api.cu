@@ -240,9 +240,10 @@ namespace sigma {
 int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
                         const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
                         const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
-                        void* stream) {
+                        void* stream, const float2* epsr32) {
   if (!plan) return SIGMA_ERR_NULL;
-  if (!I_epsR || !aqsntemp || !aqsmtemp || !schDt_matrix) return SIGMA_ERR_NULL;
+  if ((!I_epsR && !epsr32) || !aqsntemp || !aqsmtemp || !schDt_matrix) return SIGMA_ERR_NULL;
+  if (epsr32 && plan->mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
   int dev = 0;
   SIGMA_CUDA_TRY(cudaGetDevice(&dev));
   if (dev != plan->device) return SIGMA_ERR_UNSUPPORTED;
@@ -253,6 +254,7 @@ int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
   d.aqsm = reinterpret_cast<const double2*>(aqsmtemp);
   d.vcoul = vcoul;
   d.vfac = vfac;
+  d.epsr32 = epsr32;
   cudaEvent_t* ev = nullptr;
   if (plan->timing && plan->recorded < kFfMaxTimed) ev = &plan->events[3 * plan->recorded++];
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->work.counter, 0, 2 * sizeof(int), s));

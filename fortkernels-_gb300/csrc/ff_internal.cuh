@@ -23,6 +23,9 @@ struct FfDev {
   // remainders), by conj(aqsm[n1][igp]) alone otherwise (schDt).
   const double* vcoul;
   double vfac;
+  // Optional FP32 operand [nf][ng][nc] used instead of epsr (the tensor-core
+  // form rounds its operand to FP32 before slicing it)
+  const float2* epsr32 = nullptr;
 };
 
 // Column weight of the contraction epilogue (0 for a column left out).

@@ -51,9 +51,8 @@ constexpr int kChunkStages = 4;                         // K tiles per accumulat
 constexpr int kMaxSeg = 8;                              // frequencies per row block (host checks)
 constexpr uint32_t kIdesc = idesc_bf16_f32(128, 128);
 
-__device__ __forceinline__ void split3(double v, unsigned short& a, unsigned short& b,
+__device__ __forceinline__ void split3(float x, unsigned short& a, unsigned short& b,
                                        unsigned short& c) {
-  const float x = __double2float_rn(v);
   const __nv_bfloat16 s1 = __float2bfloat16_rn(x);
   const float t1 = x - __bfloat162float(s1);
   const __nv_bfloat16 s2 = __float2bfloat16_rn(t1);
@@ -66,7 +65,7 @@ __device__ __forceinline__ void split3(double v, unsigned short& a, unsigned sho
 
 // Slices of 8 consecutive K values of one row, written as three 16-byte
 // chunks (one per slice tile) of a 24 KB block.
-__device__ __forceinline__ void put_row_chunk(unsigned char* blk, int r, int ch, const double (&v)[8]) {
+__device__ __forceinline__ void put_row_chunk(unsigned char* blk, int r, int ch, const float (&v)[8]) {
   unsigned short sl[3][8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) split3(v[j], sl[0][j], sl[1][j], sl[2][j]);
@@ -95,11 +94,19 @@ __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz
     const int rb = (int)(rest / oz.kt);
     const int R = rb * kOzRows + r;
     const int k0 = kt * kOzKTile + ch * 8;
-    double re[8], im[8];
+    float re[8], im[8];  // each value rounded to FP32 before it is sliced
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int k = k0 + j;
-      const double2 v = (R < rows && k < p.nc) ? p.epsr[(size_t)R * p.nc + k] : make_double2(0.0, 0.0);
+      float2 v = make_float2(0.f, 0.f);
+      if (R < rows && k < p.nc) {
+        if (p.epsr32) {
+          v = p.epsr32[(size_t)R * p.nc + k];
+        } else {
+          const double2 d = p.epsr[(size_t)R * p.nc + k];
+          v = make_float2(__double2float_rn(d.x), __double2float_rn(d.y));
+        }
+      }
       re[j] = v.x;
       im[j] = v.y;
     }
@@ -121,14 +128,14 @@ __global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz
     const int cb = (int)(rest / oz.kt);
     const int n = cb * kOzCols + nl;
     const int k0 = kt * kOzKTile + ch * 8;
-    double re[8], im[8], nim[8];
+    float re[8], im[8], nim[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int k = k0 + j;
       const double2 v = (n < p.nb && k < p.nc) ? p.aqsn[(size_t)n * p.nc + k] : make_double2(0.0, 0.0);
-      re[j] = v.x;
-      im[j] = v.y;
-      nim[j] = -v.y;
+      re[j] = __double2float_rn(v.x);
+      im[j] = __double2float_rn(v.y);
+      nim[j] = -im[j];
     }
     unsigned char* base = oz.b_tiles + (size_t)cb * 2 * oz.kt * kOperandBytes;
     unsigned char* lo = base + (size_t)kt * kOperandBytes;            // K' < K: real parts of aqsn

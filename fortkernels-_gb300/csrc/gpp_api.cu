@@ -26,7 +26,7 @@ struct sigma_gpp_plan_s {
   sigma::GppWork schmy{};     // mixed main pass for shared frequencies (shares sch's buffers)
   sigma::GppWork prepw{};     // pre-pass blocks: sch's, rounded up to even counts
   sigma_ff_plan ff = nullptr; // tensor form: the contraction plan (3 slabs = 3 frequencies)
-  double2* yfac = nullptr;    // tensor form: frequency factors Y[3][ng][nc]
+  double2* yfac = nullptr;    // tensor form: frequency factors Y[3][ng][nc] (FP32 complex)
   sigma::MixedPrep prep{};    // FP32 operands of the mixed path (unused for FP64)
   void* block = nullptr;      // one device allocation for everything below
   int* igp_of = nullptr;      // [ng]
@@ -190,7 +190,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   const size_t b_colB = align_up(sizeof(float2) * col_elems, 256);
   const size_t b_band = align_up(sizeof(float2) * band_elems, 256);
   const size_t b_colC = nvband > 0 ? b_colB : 0;
-  const size_t b_y = tensor ? align_up(sizeof(double2) * 3 * (size_t)ngpown * ncouls, 256) : 0;
+  const size_t b_y = tensor ? align_up(sizeof(float2) * 3 * (size_t)ngpown * ncouls, 256) : 0;
   if (tensor) {
     int st2 = ff_plan_build(&p->ff, number_bands, ncouls, ngpown, kNW, igp_of, SIGMA_FF_OZAKI_BF16);
     if (st2 != SIGMA_OK) {
@@ -369,11 +369,11 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
   if (tensor) {
     // factors, and the occupied-band operands from the same pass
-    SIGMA_CUDA_TRY(launch_tensor_factors(p, plan->yfac, plan->prepw,
+    float2* y32 = reinterpret_cast<float2*>(plan->yfac);
+    SIGMA_CUDA_TRY(launch_tensor_factors(p, y32, plan->prepw,
                                          plan->ssx.n_items > 0 ? &plan->prep : nullptr, s));
-    const int st = ff_execute_weighted(plan->ff, reinterpret_cast<const sigma_complex128*>(plan->yfac),
-                                       aqsntemp, aqsmtemp, vcoul, 0.5,
-                                       reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream);
+    const int st = ff_execute_weighted(plan->ff, nullptr, aqsntemp, aqsmtemp, vcoul, 0.5,
+                                       reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream, y32);
     if (st != SIGMA_OK) return st;
   } else if (ypath)
     SIGMA_CUDA_TRY(launch_sch_fp64y(p, plan->schy, plan->schy_grid, s));

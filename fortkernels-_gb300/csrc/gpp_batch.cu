@@ -307,7 +307,7 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
     // one factor buffer and one slice workspace, each sized for the largest instance
     size_t ybytes = 0, tbytes = 0;
     for (int i = 0; i < n_instances; ++i) {
-      ybytes = std::max(ybytes, sizeof(double2) * 3 * (size_t)inst[i].ngpown * inst[i].ncouls);
+      ybytes = std::max(ybytes, sizeof(float2) * 3 * (size_t)inst[i].ngpown * inst[i].ncouls);
       size_t tb = 0;
       int st = ff_plan_tile_bytes(inst[i].number_bands, inst[i].ncouls, inst[i].ngpown, kNW, &tb);
       if (st != SIGMA_OK) {
@@ -360,11 +360,12 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   if (tensor) {
     for (int i = 0; i < b->n; ++i) {
       // factors, and the occupied-band operands from the same pass
-      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], b->yfac, b->prepw[i],
+      float2* y32 = reinterpret_cast<float2*>(b->yfac);
+      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], y32, b->prepw[i],
                                            b->ssx[i].n_items > 0 ? &b->prep[i] : nullptr, s));
-      const int st = ff_execute_weighted(b->ff[i], reinterpret_cast<const sigma_complex128*>(b->yfac),
-                                         b->inst[i].aqsntemp, b->inst[i].aqsmtemp, b->inst[i].vcoul, 0.5,
-                                         reinterpret_cast<sigma_complex128*>(b->acht_n1[i]), stream);
+      const int st = ff_execute_weighted(b->ff[i], nullptr, b->inst[i].aqsntemp, b->inst[i].aqsmtemp,
+                                         b->inst[i].vcoul, 0.5,
+                                         reinterpret_cast<sigma_complex128*>(b->acht_n1[i]), stream, y32);
       if (st != SIGMA_OK) return st;
     }
   } else if (b->sch_view.total > 0)

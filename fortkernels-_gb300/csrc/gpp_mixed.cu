@@ -220,23 +220,84 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
 // every band a term factors as
 //   scha = conj(aqsm[n1][igp]) * aqsn[n1][ig] * Y_iw[my_igp][ig],
 // so the band sum is the FF contraction (ff_ozaki.cu) with the three
-// frequencies as slabs and the column weight 0.5 vcoul[igp].  This kernel
-// forms the frequency factors
+// frequencies as slabs and the column weight 0.5 vcoul[igp].  The contraction
+// rounds its operand to FP32 before splitting it into BF16 slices, so this
+// pass delivers the factors
 //   y[iw][my_igp][ig] = G (c + i b) / (c^2 + b^2)   (0 when the guard drops it)
-// in FP64 with the FP64 path's decisions, and in the same pass (same inputs,
-// same G and threshold) the pre-pass operands of the occupied-band kernel
-// (colA with the exact keep and second-branch bits, colB = G, colC =
-// Omega2) when m.colA is set.  Tiles of kBPM columns x 32 g-vectors: factor
-// writes run along g-vectors, operand writes go through shared memory.
-__global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, double2* y, MixedPrep m,
+// already rounded to FP32, computed in float-float arithmetic (pairs of FP32
+// values, ~2^-44 relative) from exact splits of the FP64 inputs: the same
+// FP32 values as rounding FP64 factors, on the FP32 pipe instead of GB300's
+// 1/64-rate FP64 pipe.  Keep and second-branch decisions are taken in
+// float-float and re-taken with the FP64 path's own expressions within 2^-30
+// of a threshold.  In the same pass (same inputs) it writes the pre-pass
+// operands of the occupied-band kernel (colA with the exact keep and
+// second-branch bits, colB = G, colC = Omega2) when m.colA is set.  Tiles of
+// kBPM columns x 32 g-vectors: factor writes run along g-vectors, operand
+// writes go through shared memory.
+
+// x = hi + lo: hi is x truncated to 24 significant bits (exact in FP32), lo
+// the rest rounded to FP32; integer operations and one exact conversion only.
+__device__ __forceinline__ void split_exact(double x, float& hi, float& lo) {
+  const long long bits = __double_as_longlong(x);
+  constexpr long long kLow = (1LL << 29) - 1;
+  hi = __double2float_rn(__longlong_as_double(bits & ~kLow));
+  const int e = (int)((bits >> 52) & 0x7FF);
+  const float m = __ll2float_rn(bits & kLow);  // low 29 mantissa bits, < 2^29
+  const float scale = e > 948 ? __int_as_float((e - 948) << 23) : 0.f;  // 2^(e - 1075)
+  lo = (bits < 0) ? -(m * scale) : m * scale;
+}
+
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_of(double x) {
+  FF r;
+  split_exact(x, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ FF ff_norm(float s, float e) {
+  const float h = s + e;
+  return FF{h, e - (h - s)};
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+  float s, e;
+  two_sum_f(x.hi, y.hi, s, e);
+  return ff_norm(s, e + (x.lo + y.lo));
+}
+__device__ __forceinline__ FF ff_neg(FF x) { return FF{-x.hi, -x.lo}; }
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+  const float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
+  return ff_norm(p, e);
+}
+// 1/x for x > 0: FP32 reciprocal, one float-float correction
+__device__ __forceinline__ FF ff_rcp(FF x) {
+  const float r0 = rcp_f32(x.hi);
+  const float e = fmaf(-x.hi, r0, 1.0f) - x.lo * r0;
+  return ff_norm(r0, r0 * e);
+}
+__device__ __forceinline__ float ff_round(FF x) { return x.hi + x.lo; }
+// x > y for non-negative float-float values, with `near` set when they are
+// within 2^-30 (relative) of each other
+__device__ __forceinline__ bool ff_gt(FF x, FF y, bool& near) {
+  const float d = (x.hi - y.hi) + (x.lo - y.lo);
+  near = fabsf(d) <= 9.3132257e-10f * fmaxf(x.hi, y.hi);  // 2^-30
+  return d > 0.f;
+}
+
+__global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y, MixedPrep m,
                                                              int n_col_blocks) {
   __shared__ float4 ta[32][kBPM + 1];
   __shared__ float2 tb[32][kBPM + 1];
   __shared__ float2 tc[32][kBPM + 1];
   const int tid = threadIdx.x;
   const size_t plane = (size_t)p.ng * p.nc;
-  const double wx[kNW] = {p.wx[0], p.wx[1], p.wx[2]};
+  FF wx[kNW];
+#pragma unroll
+  for (int iw = 0; iw < kNW; ++iw) wx[iw] = ff_of(p.wx[iw]);
   const bool ops = m.colA != nullptr;
+  const FF quarter{0.25f, 0.f};
   const long long tiles = (long long)n_col_blocks * (m.nc_pad / 32);
   for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int cb = (int)(t / (m.nc_pad / 32));
@@ -245,40 +306,64 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, double2* 
     for (int e = tid; e < 32 * kBPM; e += 256) {
       const int pl = e / 32, k = e % 32;  // reads and factor writes run along g-vectors
       const int my_igp = cb * kBPM + pl, ig = ig0 + k;
-      float4 a = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
+      float4 av = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
       float2 g32 = make_float2(0.f, 0.f), om = make_float2(0.f, 0.f);
       if (my_igp < p.ng && ig < p.nc) {
         const size_t off = (size_t)my_igp * p.nc + ig;
         const double2 wt = p.wt[off];
         const double2 ie = p.ieps[off];
-        const double2 g = cmul(ie, wt);
-        const double b = wt.y, b2 = guard_b2(b);
-        const double thr = guard_thr(wt.x, b2);
-        const double thr2 = p.nvband > 0 ? guard_thr2(wt.x, b2) : 0.0;
+        const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
+        const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));
+        const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
+        const FF b2 = ff_mul(b, b);
+        const FF s2 = ff_add(ff_mul(a, a), b2);            // |wtilde|^2
+        const FF s_big = ff_mul(s2, FF{1e6f, 0.f});        // |wtilde|^2 / to1 (1e6 exact)
         unsigned mask = 0u;
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          const double c = __dsub_rn(wx[iw], wt.x);
-          const double wv = fma(c, c, b2);
-          const bool keep = gt_nonneg(wv, thr);
-          const double r = keep ? rcp_f64_seed32(wv) : 0.0;
-          const double zr = c * r, zi = b * r;
-          y[(size_t)iw * plane + off] = make_double2(fma(g.x, zr, -g.y * zi), fma(g.x, zi, g.y * zr));
+          const FF c = ff_add(wx[iw], ff_neg(a));
+          const FF wv = ff_add(ff_mul(c, c), b2);
+          // keep: |wdiff|^2 > max(0.25, |wtilde|^2 * 4e-6), i.e. both
+          // wv > 0.25 and wv * 250000 > |wtilde|^2 (250000 exact in FP32)
+          bool n1, n2;
+          const bool k1 = ff_gt(wv, quarter, n1);
+          const bool k2 = ff_gt(ff_mul(wv, FF{250000.f, 0.f}), s2, n2);
+          bool keep = k1 && k2;
+          if (n1 || n2) {  // within 2^-30 of a threshold: the FP64 path's decision
+            const double b2d = guard_b2(wt.y);
+            keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2d), guard_thr(wt.x, b2d));
+          }
+          float2 yv = make_float2(0.f, 0.f);
+          if (keep) {
+            const FF r = ff_rcp(wv);
+            const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
+            yv = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
+                             ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
+          }
+          y[(size_t)iw * plane + off] = yv;
           mask |= keep ? (1u << iw) : 0u;
-          if (!keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv)) mask |= 8u << iw;
+          if (ops && p.nvband > 0 && !keep) {
+            // second branch: 0 < |wdiff|^2 < |wtilde|^2 / to1
+            bool n3;
+            bool second = wv.hi > 0.f && ff_gt(s_big, wv, n3);
+            if (n3 || wv.hi < 1e-30f) {
+              const double b2d = guard_b2(wt.y);
+              const double w64 = guard_w(p.wx[iw], wt.x, b2d);
+              second = gt_nonneg(w64, 0.0) && gt_nonneg(guard_thr2(wt.x, b2d), w64);
+            }
+            mask |= second ? (8u << iw) : 0u;
+          }
         }
         if (ops) {
-          split_f(wt.x, a.x, a.y);
-          a.z = __double2float_rn(wt.y);
-          a.w = __uint_as_float(mask);
-          g32 = make_float2(__double2float_rn(g.x), __double2float_rn(g.y));
-          if (m.colC) {
-            const double2 o2 = cmul(wt, g);  // Omega2 = wtilde^2 I_eps
-            om = make_float2(__double2float_rn(o2.x), __double2float_rn(o2.y));
+          av = make_float4(a.hi, a.lo, ff_round(b), __uint_as_float(mask));
+          g32 = make_float2(ff_round(gx), ff_round(gy));
+          if (m.colC) {  // Omega2 = wtilde G
+            om = make_float2(ff_round(ff_add(ff_mul(a, gx), ff_neg(ff_mul(b, gy)))),
+                             ff_round(ff_add(ff_mul(a, gy), ff_mul(b, gx))));
           }
         }
       }
-      ta[k][pl] = a;
+      ta[k][pl] = av;
       tb[k][pl] = g32;
       tc[k][pl] = om;
     }
@@ -849,7 +934,7 @@ int sch_blocks_per_sm_mixed() {
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_tensor_factors(const GppDev& p, double2* y, const GppWork& w, const MixedPrep* m,
+cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, const MixedPrep* m,
                                   cudaStream_t s) {
   const int sms = 152;
   MixedPrep mm{};

@@ -150,9 +150,9 @@ int sch_blocks_per_sm(int precision);
 int ssx_blocks_per_sm(int precision);
 
 // Tensor form: frequency factors y[iw][my_igp][ig] of one shared frequency
-// set, together with the occupied-band kernel's pre-pass operands
+// set, rounded to FP32, together with the occupied-band kernel's pre-pass operands
 // (w: the pre-pass blocks; m null: factors only).
-cudaError_t launch_tensor_factors(const GppDev& p, double2* y, const GppWork& w, const MixedPrep* m,
+cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, const MixedPrep* m,
                                   cudaStream_t s);
 
 // Sums the partials of the sch and ssx passes in a fixed order into
