@@ -360,10 +360,13 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (tensor && wx_band_stride != 0) return SIGMA_ERR_UNSUPPORTED;  // needs one frequency set
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
   const bool mixed = plan->precision == SIGMA_PREC_MIXED;
-  if (mixed && plan->sch.n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->prepw, plan->prep, s));
   // one frequency set for every band: the shared-factor kernels
   const bool ypath = !mixed && !tensor && wx_band_stride == 0 && plan->schy.n_items > 0;
   const bool mypath = mixed && wx_band_stride == 0 && plan->schmy.n_items > 0;
+  if (mypath)  // pre-pass in float-float arithmetic (the tensor form's operand pass)
+    SIGMA_CUDA_TRY(launch_tensor_factors(p, nullptr, plan->prepw, &plan->prep, s));
+  else if (mixed && plan->sch.n_items > 0)
+    SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->prepw, plan->prep, s));
   GppWork main = ypath ? plan->schy : (mypath ? plan->schmy : plan->sch);
   if (tensor) main.partial = nullptr;  // band sums land in acht_n1 directly
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));

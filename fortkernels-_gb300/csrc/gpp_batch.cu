@@ -356,7 +356,9 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   SIGMA_CUDA_TRY(cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), s));
   if (mixed && !tensor)
     for (int i = 0; i < b->n; ++i)
-      if (b->sch[i].n_items > 0) SIGMA_CUDA_TRY(launch_prep_mixed(b->dev[i], b->prepw[i], b->prep[i], s));
+      if (b->sch[i].n_items > 0)
+        SIGMA_CUDA_TRY(b->mixedy ? launch_tensor_factors(b->dev[i], nullptr, b->prepw[i], &b->prep[i], s)
+                                 : launch_prep_mixed(b->dev[i], b->prepw[i], b->prep[i], s));
   if (tensor) {
     for (int i = 0; i < b->n; ++i) {
       // factors, and the occupied-band operands from the same pass

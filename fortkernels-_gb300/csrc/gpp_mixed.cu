@@ -231,7 +231,9 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
 // float-float and re-taken with the FP64 path's own expressions within 2^-30
 // of a threshold.  In the same pass (same inputs) it writes the pre-pass
 // operands of the occupied-band kernel (colA with the exact keep and
-// second-branch bits, colB = G, colC = Omega2) when m.colA is set.  Tiles of
+// second-branch bits, colB = G, colC = Omega2) when m.colA is set; with y
+// null it writes those operands alone (the mixed form's pre-pass for one
+// frequency set).  Tiles of
 // kBPM columns x 32 g-vectors: factor writes run along g-vectors, operand
 // writes go through shared memory.
 
@@ -333,14 +335,16 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
             const double b2d = guard_b2(wt.y);
             keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2d), guard_thr(wt.x, b2d));
           }
-          float2 yv = make_float2(0.f, 0.f);
-          if (keep) {
-            const FF r = ff_rcp(wv);
-            const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
-            yv = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
-                             ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
+          if (y) {
+            float2 yv = make_float2(0.f, 0.f);
+            if (keep) {
+              const FF r = ff_rcp(wv);
+              const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
+              yv = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
+                               ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
+            }
+            y[(size_t)iw * plane + off] = yv;
           }
-          y[(size_t)iw * plane + off] = yv;
           mask |= keep ? (1u << iw) : 0u;
           if (ops && p.nvband > 0 && !keep) {
             // second branch: 0 < |wdiff|^2 < |wtilde|^2 / to1

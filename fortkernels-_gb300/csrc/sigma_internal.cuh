@@ -151,7 +151,8 @@ int ssx_blocks_per_sm(int precision);
 
 // Tensor form: frequency factors y[iw][my_igp][ig] of one shared frequency
 // set, rounded to FP32, together with the occupied-band kernel's pre-pass operands
-// (w: the pre-pass blocks; m null: factors only).
+// (w: the pre-pass blocks; m null: factors only; y null: the operands alone,
+// which is the mixed form's pre-pass for one frequency set).
 cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, const MixedPrep* m,
                                   cudaStream_t s);
 
