@@ -154,19 +154,21 @@ extern "C" {
 // achtemp[3], asxtemp[3]; acht_n1_loc[nb], achstemp[1] (the static remainder
 // summed over every band and column, gppKerSeq.cpp:412 accumulates it over
 // the band loop), col_sch/col_ssx [nb][ng][3] (sch_array and ssx_array of
-// every (n1, my_igp), before vcoul) are optional.  Returns 0 or a negative
-// error code.
+// every (n1, my_igp), before vcoul) are optional.  Only bands [band_begin,
+// band_end) are summed (acht_n1_loc and the column arrays are written for
+// those bands).  Returns 0 or a negative error code.
 int oracle_gpp_halfsum(int number_bands, int nvband, int ncouls, int ngpown,
                        const int* inv_igp_index, const int* indinv, int indinv_len,
                        const double* wx, double occ, const double* aqsmtemp,
                        const double* aqsntemp, const double* I_eps_array,
                        const double* wtilde_array, const double* vcoul, double* achtemp,
                        double* asxtemp, double* acht_n1_loc, double* achstemp, double* col_sch,
-                       double* col_ssx, int nthreads) {
+                       double* col_ssx, int nthreads, int band_begin, int band_end) {
   if (!inv_igp_index || !indinv || !wx || !aqsmtemp || !aqsntemp || !I_eps_array ||
       !wtilde_array || !vcoul || !achtemp || !asxtemp)
     return -6;
-  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0 || nvband < 0 || nvband > number_bands)
+  if (number_bands <= 0 || ncouls <= 0 || ngpown <= 0 || nvband < 0 || nvband > number_bands ||
+      band_begin < 0 || band_end > number_bands || band_begin > band_end)
     return -1;
   std::vector<int> igp_of(ngpown);
   for (int g = 0; g < ngpown; ++g) {
@@ -183,7 +185,7 @@ int oracle_gpp_halfsum(int number_bands, int nvband, int ncouls, int ngpown,
   CDD ach_total[3], asx_total[3], stat_total;
   std::vector<CDD> sch_c(static_cast<size_t>(ngpown) * 3), ssx_c(static_cast<size_t>(ngpown) * 3);
   std::vector<CDD> stat_c(ngpown);
-  for (int n1 = 0; n1 < number_bands; ++n1) {
+  for (int n1 = band_begin; n1 < band_end; ++n1) {
     const bool flag_occ = n1 < nvband;
     const cd* nrow = aqsn + n1 * nc;
     const cd* mrow = aqsm + n1 * nc;

@@ -357,16 +357,17 @@ def run_reference_real_binary(number_bands, nvband, ncouls, nodes_per_group, thr
     return out
 
 
-def gpp_halfsum(prob, nthreads=0, columns=False):
+def gpp_halfsum(prob, nthreads=0, columns=False, band_begin=0, band_end=None):
     """gppsum = 1 ("half sum") GPP of gppKerSeq.cpp on a GppProblem in
     band-major layout.  Returns (achtemp[3], asxtemp[3], acht_n1_loc[nb],
     achstemp) complex128, plus (col_sch, col_ssx) [nb][ng][3] with
-    columns=True."""
+    columns=True; sums over bands [band_begin, band_end) (all by default)."""
     l = lib()
     if not hasattr(l, "_halfsum_ready"):
         l.oracle_gpp_halfsum.argtypes = [_I, _I, _I, _I, _P, _P, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P,
-                                         _P, _P, _P, _P, _I]
+                                         _P, _P, _P, _P, _I, _I, _I]
         l._halfsum_ready = True
+    band_end = prob.number_bands if band_end is None else band_end
     inv, indinv, wx, aqsm, aqsn, ieps, wt, vcoul = _prep(prob)
     nb, ng = prob.number_bands, prob.ngpown
     ach, asx = np.zeros(3, np.complex128), np.zeros(3, np.complex128)
@@ -375,7 +376,8 @@ def gpp_halfsum(prob, nthreads=0, columns=False):
     cx = np.zeros((nb, ng, 3), np.complex128) if columns else None
     st = l.oracle_gpp_halfsum(nb, prob.nvband, prob.ncouls, ng, _p(inv), _p(indinv), len(indinv), _p(wx[:3]),
                               float(getattr(prob, "occ", 1.0)), _p(aqsm), _p(aqsn), _p(ieps), _p(wt),
-                              _p(vcoul), _p(ach), _p(asx), _p(n1), _p(stat), _p(cs), _p(cx), nthreads)
+                              _p(vcoul), _p(ach), _p(asx), _p(n1), _p(stat), _p(cs), _p(cx), nthreads,
+                              band_begin, band_end)
     if st != 0:
         raise OracleError(f"oracle_gpp_halfsum status {st}")
     out = (ach, asx, n1, stat[0])

@@ -151,3 +151,56 @@ def test_halfsum_tensor_matches_fp64(sigma_lib, case):
         assert np.all(rel(t[1], f[1]) <= 1e-12)     # occupied bands run in FP64 in both forms
     assert rel(t[3], f[3]) <= 2e-6
     assert np.linalg.norm(t[2] - f[2]) <= 1e-6 * np.linalg.norm(f[2])
+
+
+# ---- production shape: 512 bands, nvband 2, ncouls 32768, ngpown 1638
+@pytest.fixture(scope="module")
+def production_half(sigma_lib):
+    nb, nvb, nc = 512, 2, 32768
+    ng = nc // 20
+    seed = W.GPP_PRODUCTION_SEED
+    f64 = dict(dtype=torch.float64, device="cuda")
+    d = dict(aqsm=torch.empty(2 * nb * nc, **f64), aqsn=torch.empty(2 * nb * nc, **f64),
+             ieps=torch.empty(2 * ng * nc, **f64), wt=torch.empty(2 * ng * nc, **f64),
+             vcoul=torch.empty(nc, **f64), wx=torch.tensor(W.wx_frequencies(), **f64))
+    sigma_lib.fill_complex_device(d["aqsm"].data_ptr(), nb * nc, seed, W.AID_AQSM, (-1, 1), (-1, 1))
+    sigma_lib.fill_complex_device(d["aqsn"].data_ptr(), nb * nc, seed, W.AID_AQSN, (-1, 1), (-1, 1))
+    sigma_lib.fill_complex_device(d["ieps"].data_ptr(), ng * nc, seed, W.AID_IEPS, (-1, 1), (-1, 1))
+    sigma_lib.fill_complex_device(d["wt"].data_ptr(), ng * nc, seed, W.AID_WTILDE, (0.5, 5.0), (-0.1, 0.1))
+    sigma_lib.fill_real_device(d["vcoul"].data_ptr(), nc, seed, W.AID_VCOUL, 0.1, 10.0)
+    inv, indinv = W.gpp_index_maps(nc, ng)
+    outs = {}
+    for name, flags in (("fp64", sigma_lib.HALFSUM_STATIC),
+                        ("tensor", sigma_lib.HALFSUM_STATIC | sigma_lib.HALFSUM_TENSOR)):
+        plan = sigma_lib.GppHalfSumPlan(nb, nvb, nc, ng, inv, indinv, flags=flags)
+        z = lambda n: torch.zeros(n, **f64)
+        ach, asx, n1, st = z(6), z(6), z(2 * nb), z(2)
+        plan.execute(d["wx"], d["aqsm"], d["aqsn"], d["ieps"], d["wt"], d["vcoul"], ach, asx, n1, st)
+        torch.cuda.synchronize()
+        plan.close()
+        outs[name] = [t.cpu().numpy().view(np.complex128).copy() for t in (ach, asx, n1, st)]
+    c = lambda t, r: t.cpu().numpy().view(np.complex128).reshape(r, nc)
+    prob = W.GppProblem(nb, nvb, nc, ng, inv, indinv, W.wx_frequencies(), c(d["aqsm"], nb), c(d["aqsn"], nb),
+                        c(d["ieps"], ng), c(d["wt"], ng), d["vcoul"].cpu().numpy())
+    del d
+    torch.cuda.empty_cache()
+    return outs, prob
+
+
+def test_halfsum_production_sampled_bands_match_oracle(production_half):
+    outs, prob = production_half
+    g = outs["fp64"]
+    for band in (0, 1, 300, 511):  # two occupied, two not
+        _, _, on1, _ = O.gpp_halfsum(prob, band_begin=band, band_end=band + 1)
+        assert abs(g[2][band] - on1[band]) <= TOL * abs(on1[band])
+    assert abs(g[2].sum() - g[0][2]) <= 1e-13 * np.abs(g[2]).sum()   # acht_n1_loc sums to achtemp[2]
+
+
+def test_halfsum_production_tensor_within_bar_of_fp64(production_half):
+    outs, _ = production_half
+    f, t = outs["fp64"], outs["tensor"]
+    rel = lambda a, b: np.abs(a - b) / np.abs(b)
+    assert np.all(rel(t[0], f[0]) <= 2e-6)
+    assert np.all(rel(t[1], f[1]) <= 1e-12)       # occupied bands in FP64 in both forms
+    assert rel(t[3], f[3]) <= 2e-6
+    assert np.linalg.norm(t[2] - f[2]) <= 1e-6 * np.linalg.norm(f[2])
