@@ -22,6 +22,7 @@
 // ranges), so the re-check runs in a warp-uniform fix-up after each
 // g-vector step.
 #include "sigma_internal.cuh"
+#include "floatfloat.cuh"
 #include "gpp_batch.cuh"
 
 namespace sigma {
@@ -236,57 +237,6 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
 // frequency set).  Tiles of
 // kBPM columns x 32 g-vectors: factor writes run along g-vectors, operand
 // writes go through shared memory.
-
-// x = hi + lo: hi is x truncated to 24 significant bits (exact in FP32), lo
-// the rest rounded to FP32; integer operations and one exact conversion only.
-__device__ __forceinline__ void split_exact(double x, float& hi, float& lo) {
-  const long long bits = __double_as_longlong(x);
-  constexpr long long kLow = (1LL << 29) - 1;
-  hi = __double2float_rn(__longlong_as_double(bits & ~kLow));
-  const int e = (int)((bits >> 52) & 0x7FF);
-  const float m = __ll2float_rn(bits & kLow);  // low 29 mantissa bits, < 2^29
-  const float scale = e > 948 ? __int_as_float((e - 948) << 23) : 0.f;  // 2^(e - 1075)
-  lo = (bits < 0) ? -(m * scale) : m * scale;
-}
-
-struct FF {
-  float hi, lo;
-};
-__device__ __forceinline__ FF ff_of(double x) {
-  FF r;
-  split_exact(x, r.hi, r.lo);
-  return r;
-}
-__device__ __forceinline__ FF ff_norm(float s, float e) {
-  const float h = s + e;
-  return FF{h, e - (h - s)};
-}
-__device__ __forceinline__ FF ff_add(FF x, FF y) {
-  float s, e;
-  two_sum_f(x.hi, y.hi, s, e);
-  return ff_norm(s, e + (x.lo + y.lo));
-}
-__device__ __forceinline__ FF ff_neg(FF x) { return FF{-x.hi, -x.lo}; }
-__device__ __forceinline__ FF ff_mul(FF x, FF y) {
-  const float p = x.hi * y.hi;
-  float e = fmaf(x.hi, y.hi, -p);
-  e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
-  return ff_norm(p, e);
-}
-// 1/x for x > 0: FP32 reciprocal, one float-float correction
-__device__ __forceinline__ FF ff_rcp(FF x) {
-  const float r0 = rcp_f32(x.hi);
-  const float e = fmaf(-x.hi, r0, 1.0f) - x.lo * r0;
-  return ff_norm(r0, r0 * e);
-}
-__device__ __forceinline__ float ff_round(FF x) { return x.hi + x.lo; }
-// x > y for non-negative float-float values, with `near` set when they are
-// within 2^-30 (relative) of each other
-__device__ __forceinline__ bool ff_gt(FF x, FF y, bool& near) {
-  const float d = (x.hi - y.hi) + (x.lo - y.lo);
-  near = fabsf(d) <= 9.3132257e-10f * fmaxf(x.hi, y.hi);  // 2^-30
-  return d > 0.f;
-}
 
 __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y, MixedPrep m,
                                                              int n_col_blocks) {
