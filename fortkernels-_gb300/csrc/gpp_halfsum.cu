@@ -42,6 +42,7 @@
 
 #include "sigma_gpp.h"
 #include "sigma_internal.cuh"
+#include "floatfloat.cuh"
 #include "ff_plan.h"
 #include "runtime.h"
 
@@ -51,7 +52,8 @@ namespace {
 constexpr int kHBN = 32, kHBP = 32;  // bands x columns per item
 constexpr int kHCK = 16;             // g-vectors per staged chunk
 constexpr int kHTB = kHBN / 16, kHTC = kHBP / 16;
-constexpr int kOccBands = 4;         // occupied bands per accumulation pass
+constexpr int kOccBands = 4;         // occupied bands per accumulation pass (FP64)
+constexpr int kOccBandsF = 2;        // the same for the float-float form
 constexpr int kIgBlk = 512;          // g-vector block of the reference's loop
 
 struct HalfDev {
@@ -276,19 +278,29 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
   }
 }
 
-// First g-vector of each column with |Omega2| < to1 (ncouls if none): the
-// occupied-band loop of the reference stops there (gppKerSeq.cpp:96).
+// First g-vector below igp of each column with |Omega2| < to1 (ncouls if
+// none): the occupied-band loop of the reference stops there
+// (gppKerSeq.cpp:96) and never passes igp.  |Omega2|^2 = |wtilde|^4 |I_eps|^2
+// is screened in FP32 (relative error below 2^-20); values not clearly above
+// to1^2 take the FP64 expression, so the cut is the FP64 one.
 __global__ void __launch_bounds__(kThreads) half_brk_kernel(HalfDev p, int* brk) {
   __shared__ int s_min;
   const int col = blockIdx.x;
   if (threadIdx.x == 0) s_min = p.nc;
   __syncthreads();
   int first = p.nc;
-  for (int ig = threadIdx.x; ig < p.nc; ig += kThreads) {
+  const int igp = p.igp_of[col];
+  const int lim = igp >= 0 ? igp : 0;
+  constexpr float kAbove = 1.0000153e-12f;  // to1^2 (1 + 2^-16)
+  for (int ig = threadIdx.x; ig < lim; ig += kThreads) {
     const size_t off = (size_t)col * p.nc + ig;
-    const double2 wt = p.wt[off];
+    const double2 wt = p.wt[off], ie = p.ieps[off];
+    const float a = __double2float_rn(wt.x), b = __double2float_rn(wt.y);
+    const float ex = __double2float_rn(ie.x), ey = __double2float_rn(ie.y);
+    const float s2 = fmaf(a, a, b * b);
+    if (s2 * s2 * fmaf(ex, ex, ey * ey) > kAbove) continue;
     const double2 w2 = make_double2(fma(wt.x, wt.x, -wt.y * wt.y), 2.0 * wt.x * wt.y);
-    const double2 om = cmul(w2, p.ieps[off]);
+    const double2 om = cmul(w2, ie);
     if (fma(om.x, om.x, om.y * om.y) < kTo1 * kTo1) {
       first = ig;
       break;
@@ -299,16 +311,60 @@ __global__ void __launch_bounds__(kThreads) half_brk_kernel(HalfDev p, int* brk)
   if (threadIdx.x == 0) brk[col] = s_min;
 }
 
+// Fixed-order block reduction of the occupied-band sums of kVals / 8 bands
+// (per band T_sch, U_sch, T_ssx, U_ssx, complex), then the column's
+// contributions 0.5 vcoul scht (achtemp) and occ vcoul ssxt (asxtemp) per band:
+// scht = conj(aqsm_p) T_sch + aqsm_p conj(U_sch), likewise ssxt.
+template <int kVals>
+__device__ __forceinline__ void occ_finish(const HalfDev& p, const double (&acc)[kVals],
+                                           double (*red)[kVals], double* tot, int g0, int nbl,
+                                           int col, int igp, int iw, double2* occ_ach,
+                                           double2* occ_asx) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int v = 0; v < kVals; ++v) {
+    double x = acc[v];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][v] = x;
+  }
+  __syncthreads();
+  if (tid < kVals) {
+    double s = 0.0;
+    for (int q = 0; q < kThreads / 32; ++q) s += red[q][tid];
+    tot[tid] = s;
+  }
+  __syncthreads();
+  if (tid < nbl) {
+    const int n1 = g0 + tid;
+    double2 ach = make_double2(0.0, 0.0), asx = make_double2(0.0, 0.0);
+    if (igp >= 0) {
+      const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+      const double* t = tot + 8 * tid;
+      double2 scht = cmul(cconj(am), make_double2(t[0], t[1]));
+      cfma(scht, am, make_double2(t[2], -t[3]));
+      double2 ssxt = cmul(cconj(am), make_double2(t[4], t[5]));
+      cfma(ssxt, am, make_double2(t[6], -t[7]));
+      const double v = p.vcoul[igp];
+      ach = make_double2(0.5 * scht.x * v, 0.5 * scht.y * v);
+      asx = make_double2(ssxt.x * p.occ * v, ssxt.y * p.occ * v);
+    }
+    const size_t o = ((size_t)n1 * p.ng + col) * kNW + iw;
+    occ_ach[o] = ach;
+    occ_asx[o] = asx;
+  }
+  __syncthreads();
+}
+
 // Occupied bands: one CTA per (column, frequency), threads over g-vectors,
-// kOccBands bands per pass.  Writes the column's contributions
-// 0.5 vcoul scht (achtemp) and occ vcoul ssxt (asxtemp) per band.
+// kOccBands bands per pass.
 __global__ void __launch_bounds__(kThreads) half_occ_kernel(HalfDev p, double2* occ_ach,
                                                             double2* occ_asx) {
   constexpr int kVals = kOccBands * 8;  // per band: T_sch, U_sch, T_ssx, U_ssx (complex)
   __shared__ double red[kThreads / 32][kVals];
   __shared__ double tot[kVals];
   const int col = blockIdx.x, iw = blockIdx.y;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int igp = p.igp_of[col];
   const double wx = p.wx[iw];
   const int kend = igp >= 0 ? min(igp, p.brk[col]) : 0;
@@ -371,40 +427,136 @@ __global__ void __launch_bounds__(kThreads) half_occ_kernel(HalfDev p, double2* 
           }
         }
     }
-    // fixed-order block reduction
+    occ_finish<kVals>(p, acc, red, tot, g0, nbl, col, igp, iw, occ_ach, occ_asx);
+  }
+}
+
+// Occupied bands of the tensor-core form.  The factors sch and ssx of
+// half_occ_kernel in float-float arithmetic on the FP32 pipe (~2^-44 before
+// the one rounding to FP32); decisions within 2^-30 of a threshold take the
+// FP64 expressions of half_occ_kernel.  The band sums are FP32 products over
+// FP32 copies of the occupied bands' aqsm / aqsn rows (m32, n32: [nvband][nc]),
+// folded into float-float accumulators every 8 g-vectors.  The three
+// frequency CTAs of a column are adjacent in the grid, so the column's
+// wtilde and I_eps rows are read from DRAM once.
+__global__ void __launch_bounds__(kThreads) half_occ_ff_kernel(HalfDev p, const float2* m32,
+                                                               const float2* n32, double2* occ_ach,
+                                                               double2* occ_asx) {
+  constexpr int kVals = kOccBandsF * 8;
+  __shared__ double red[kThreads / 32][kVals];
+  __shared__ double tot[kVals];
+  const int iw = blockIdx.x, col = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int igp = p.igp_of[col];
+  const double wxd = p.wx[iw];
+  const FF wx = ff_of(wxd);
+  const FF wx2 = ff_mul(wx, wx);
+  const double to2 = kTo1 * kTo1;
+  const FF to2f = ff_of(to2);
+  const int kend = igp >= 0 ? min(igp, p.brk[col]) : 0;
+  for (int g0 = 0; g0 < p.nvband; g0 += kOccBandsF) {
+    const int nbl = min(kOccBandsF, p.nvband - g0);
+    float acc[kVals], hi[kVals], lo[kVals];
+#pragma unroll
+    for (int v = 0; v < kVals; ++v) acc[v] = hi[v] = lo[v] = 0.f;
+    int run = 0;
+    for (int ig = tid; ig < kend; ig += kThreads) {
+      const size_t off = (size_t)col * p.nc + ig;
+      const double2 wt = p.wt[off], ie = p.ieps[off];
+      const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
+      const FF b2 = ff_mul(b, b);
+      const FF s2 = ff_add(ff_mul(a, a), b2);  // |wtilde|^2
+      const FF c = ff_add(wx, ff_neg(a));
+      const FF wv = ff_add(ff_mul(c, c), b2);  // |wdiff|^2
+      const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));  // G = I_eps wtilde
+      const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
+      // sch = 0 where |wdiff|^2 < max(0.25, 4e-6 |wtilde|^2): wv < 0.25 or
+      // 250000 wv < |wtilde|^2 (250000 exact in FP32)
+      bool n1, n2;
+      const bool z1 = ff_gt(FF{0.25f, 0.f}, wv, n1);
+      const bool z2 = ff_gt(s2, ff_mul(wv, FF{250000.f, 0.f}), n2);
+      bool zero = z1 || z2;
+      if (n1 || n2) {
+        const double b2d = guard_b2(wt.y);
+        zero = gt_nonneg(guard_thr(wt.x, b2d), guard_w(wxd, wt.x, b2d));
+      }
+      float2 sch = make_float2(0.f, 0.f), ssx = make_float2(0.f, 0.f);
+      if (!zero) {
+        // sch = G (c + i b) / wv
+        const FF r = ff_rcp(wv);
+        const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
+        sch = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
+                          ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
+        // ssx = Omega2 conj(D) / |D|^2, Omega2 = wtilde^2 I_eps, D = wx^2 - wtilde^2
+        const FF w2x = ff_add(ff_mul(a, a), ff_neg(b2));
+        const FF ab = ff_mul(a, b);
+        const FF w2y{2.f * ab.hi, 2.f * ab.lo};
+        const FF omx = ff_add(ff_mul(w2x, er), ff_neg(ff_mul(w2y, ei)));
+        const FF omy = ff_add(ff_mul(w2x, ei), ff_mul(w2y, er));
+        const FF dx = ff_add(wx2, ff_neg(w2x));
+        const FF rd = ff_rcp(ff_add(ff_mul(dx, dx), ff_mul(w2y, w2y)));
+        // D = (dx, -w2y): Omega2 conj(D) = (omx dx - omy w2y, omy dx + omx w2y)
+        ssx = make_float2(ff_round(ff_mul(ff_add(ff_mul(omx, dx), ff_neg(ff_mul(omy, w2y))), rd)),
+                          ff_round(ff_mul(ff_add(ff_mul(omy, dx), ff_mul(omx, w2y)), rd)));
+      } else {
+        bool n3;
+        bool big = ff_gt(s2, to2f, n3);  // |wtilde|^2 > to1^2
+        if (n3) big = fma(wt.x, wt.x, guard_b2(wt.y)) > to2;
+        if (big) {
+          // -G / (2 (wx + wtilde)) = -0.5 G conj(d) / |d|^2, d = (wx + a, b)
+          const FF dr = ff_add(wx, a);
+          const FF r = ff_rcp(ff_add(ff_mul(dr, dr), b2));
+          const FF hr{-0.5f * r.hi, -0.5f * r.lo};
+          ssx = make_float2(ff_round(ff_mul(ff_add(ff_mul(gx, dr), ff_mul(gy, b)), hr)),
+                            ff_round(ff_mul(ff_add(ff_mul(gy, dr), ff_neg(ff_mul(gx, b))), hr)));
+        }
+      }
+      const bool pair = ig != igp - 1;
+#pragma unroll
+      for (int q = 0; q < kOccBandsF; ++q)
+        if (q < nbl) {
+          const size_t bo = (size_t)(g0 + q) * p.nc + ig;
+          const float2 an = n32[bo];
+          float* t = acc + 8 * q;
+          t[0] = fmaf(an.x, sch.x, fmaf(-an.y, sch.y, t[0]));
+          t[1] = fmaf(an.x, sch.y, fmaf(an.y, sch.x, t[1]));
+          t[4] = fmaf(an.x, ssx.x, fmaf(-an.y, ssx.y, t[4]));
+          t[5] = fmaf(an.x, ssx.y, fmaf(an.y, ssx.x, t[5]));
+          if (pair) {
+            const float2 am = m32[bo];
+            t[2] = fmaf(am.x, sch.x, fmaf(-am.y, sch.y, t[2]));
+            t[3] = fmaf(am.x, sch.y, fmaf(am.y, sch.x, t[3]));
+            t[6] = fmaf(am.x, ssx.x, fmaf(-am.y, ssx.y, t[6]));
+            t[7] = fmaf(am.x, ssx.y, fmaf(am.y, ssx.x, t[7]));
+          }
+        }
+      if (++run == 8) {
+#pragma unroll
+        for (int v = 0; v < kVals; ++v) {
+          ff_add(hi[v], lo[v], acc[v]);
+          acc[v] = 0.f;
+        }
+        run = 0;
+      }
+    }
+    double sum[kVals];
 #pragma unroll
     for (int v = 0; v < kVals; ++v) {
-      double x = acc[v];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      if (lane == 0) red[warp][v] = x;
+      ff_add(hi[v], lo[v], acc[v]);
+      sum[v] = (double)hi[v] + (double)lo[v];
     }
-    __syncthreads();
-    if (tid < kVals) {
-      double s = 0.0;
-      for (int q = 0; q < kThreads / 32; ++q) s += red[q][tid];
-      tot[tid] = s;
-    }
-    __syncthreads();
-    if (tid < nbl) {
-      const int n1 = g0 + tid;
-      double2 ach = make_double2(0.0, 0.0), asx = make_double2(0.0, 0.0);
-      if (igp >= 0) {
-        const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
-        const double* t = tot + 8 * tid;
-        double2 scht = cmul(cconj(am), make_double2(t[0], t[1]));
-        cfma(scht, am, make_double2(t[2], -t[3]));
-        double2 ssxt = cmul(cconj(am), make_double2(t[4], t[5]));
-        cfma(ssxt, am, make_double2(t[6], -t[7]));
-        const double v = p.vcoul[igp];
-        ach = make_double2(0.5 * scht.x * v, 0.5 * scht.y * v);
-        asx = make_double2(ssxt.x * p.occ * v, ssxt.y * p.occ * v);
-      }
-      const size_t o = ((size_t)n1 * p.ng + col) * kNW + iw;
-      occ_ach[o] = ach;
-      occ_asx[o] = asx;
-    }
-    __syncthreads();
+    occ_finish<kVals>(p, sum, red, tot, g0, nbl, col, igp, iw, occ_ach, occ_asx);
+  }
+}
+
+// FP32 copies of the occupied bands' aqsm and aqsn rows.
+__global__ void __launch_bounds__(256) half_occ_rows32_kernel(HalfDev p, float2* m32, float2* n32) {
+  const long long total = (long long)p.nvband * p.nc;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double2 m = p.aqsm[t], n = p.aqsn[t];
+    m32[t] = make_float2(__double2float_rn(m.x), __double2float_rn(m.y));
+    n32[t] = make_float2(__double2float_rn(n.x), __double2float_rn(n.y));
   }
 }
 
@@ -537,31 +689,67 @@ cudaError_t launch_transpose(const double2* src, double2* dst, int rows, int col
 // the reference's g-vector set, Zs = -I_eps below igp; the unpaired igp terms
 // and the occupied bands run in FP64.
 
-// Z slabs [3][ng][nc] of the non-occupied half sum.
-__global__ void __launch_bounds__(256) half_z_kernel(HalfDev p, double2* z) {
+// Z slabs [3][ng][nc] of the non-occupied half sum in FP32, the contraction's
+// input precision: the factor of half_factor in float-float arithmetic on the
+// FP32 pipe (~2^-44 before the one rounding), with the threshold decision of
+// half_factor taken in FP64 within 2^-30 of the threshold.
+__global__ void __launch_bounds__(256) half_z32_kernel(HalfDev p, float2* z) {
   const long long total = (long long)p.ng * p.nc;
-  const double wx[3] = {p.wx[0], p.wx[1], p.wx[2]};
+  FF wx[3];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) wx[f] = ff_of(p.wx[f]);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int col = (int)(t / p.nc), ig = (int)(t % p.nc);
     const int lim = column_limit<3>(p.igp_of[col]);
-    double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
-    if (ig < lim && (ig % kIgBlk) != kIgBlk - 1) half_factor(p.wt[t], p.ieps[t], wx, v);
+    float2 v[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    if (ig < lim && (ig % kIgBlk) != kIgBlk - 1) {
+      const double2 wt = p.wt[t], ie = p.ieps[t];
+      const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
+      const FF b2 = ff_mul(b, b);
+      const FF s2 = ff_add(ff_mul(a, a), b2);
+      const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));
+      const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        const FF c = ff_add(wx[f], ff_neg(a));
+        const FF wv = ff_add(ff_mul(c, c), b2);
+        // kept where wv < max(0.25, 4e-6 |wtilde|^2)
+        bool n1, n2;
+        const bool k1 = ff_gt(FF{0.25f, 0.f}, wv, n1);
+        const bool k2 = ff_gt(s2, ff_mul(wv, FF{250000.f, 0.f}), n2);
+        bool keep = k1 || k2;
+        if (n1 || n2) {
+          const double b2d = guard_b2(wt.y);
+          keep = gt_nonneg(guard_thr(wt.x, b2d), guard_w(p.wx[f], wt.x, b2d));
+        }
+        if (keep) {
+          const FF r = ff_rcp(wv);
+          const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
+          v[f] = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
+                             ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
+        }
+      }
+    }
     z[t] = v[0];
     z[total + t] = v[1];
     z[2 * total + t] = v[2];
   }
 }
 
-// Zs [ng][nc] of the static remainder: -I_eps below igp.
-__global__ void __launch_bounds__(256) half_zs_kernel(HalfDev p, double2* z) {
+// Zs [ng][nc] of the static remainder in FP32: -I_eps below igp.
+__global__ void __launch_bounds__(256) half_zs32_kernel(HalfDev p, float2* z) {
   const long long total = (long long)p.ng * p.nc;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int col = (int)(t / p.nc), ig = (int)(t % p.nc);
     const int lim = column_limit<1>(p.igp_of[col]);
-    const double2 e = p.ieps[t];
-    z[t] = ig < lim ? make_double2(-e.x, -e.y) : make_double2(0.0, 0.0);
+    float2 v = make_float2(0.f, 0.f);
+    if (ig < lim) {
+      const double2 e = p.ieps[t];
+      v = make_float2(-__double2float_rn(e.x), -__double2float_rn(e.y));
+    }
+    z[t] = v;
   }
 }
 
@@ -666,7 +854,8 @@ struct sigma_gpp_halfsum_plan_s {
   // factor slabs and the four contraction results
   sigma_ff_plan ff3 = nullptr, ff1 = nullptr;
   void* tblock = nullptr;
-  double2* z = nullptr;                                          // [3][ng][nc]
+  float2* z = nullptr;                                           // [3][ng][nc], FP32
+  float2 *m32 = nullptr, *n32 = nullptr;  // occupied bands' aqsm / aqsn rows in FP32
   double2 *t3 = nullptr, *u3 = nullptr, *ts = nullptr, *us = nullptr;  // [nb][3], [nb][1]
 };
 
@@ -768,11 +957,12 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
     if (st == SIGMA_OK && (flags & SIGMA_HALFSUM_STATIC))
       st = ff_plan_tile_bytes(number_bands, ncouls, ngpown, 1, &b1);
     const size_t b_tiles = up256(std::max(b3, b1));
-    const size_t b_z = up256(sizeof(double2) * 3 * ngc);
+    const size_t b_z = up256(sizeof(float2) * 3 * ngc);
     const size_t b_r3 = up256(sizeof(double2) * (size_t)number_bands * kNW);
     const size_t b_r1 = up256(sizeof(double2) * (size_t)number_bands);
+    const size_t b_o = up256(sizeof(float2) * (size_t)std::max(nvband, 1) * ncouls);
     if (st == SIGMA_OK) {
-      e = cudaMalloc(&p->tblock, b_tiles + b_z + 2 * b_r3 + 2 * b_r1);
+      e = cudaMalloc(&p->tblock, b_tiles + b_z + 2 * b_r3 + 2 * b_r1 + 2 * b_o);
       if (e != cudaSuccess) {
         cudaGetLastError();
         set_last_cuda_error(e, "cudaMalloc(halfsum tensor)", __LINE__);
@@ -781,11 +971,13 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
     }
     if (st == SIGMA_OK) {
       char* t = static_cast<char*>(p->tblock);
-      p->z = reinterpret_cast<double2*>(t + b_tiles);
+      p->z = reinterpret_cast<float2*>(t + b_tiles);
       p->t3 = reinterpret_cast<double2*>(t + b_tiles + b_z);
       p->u3 = reinterpret_cast<double2*>(t + b_tiles + b_z + b_r3);
       p->ts = reinterpret_cast<double2*>(t + b_tiles + b_z + 2 * b_r3);
       p->us = reinterpret_cast<double2*>(t + b_tiles + b_z + 2 * b_r3 + b_r1);
+      p->m32 = reinterpret_cast<float2*>(t + b_tiles + b_z + 2 * b_r3 + 2 * b_r1);
+      p->n32 = reinterpret_cast<float2*>(t + b_tiles + b_z + 2 * b_r3 + 2 * b_r1 + b_o);
       st = ff_plan_build(&p->ff3, number_bands, ncouls, ngpown, kNW, igp_of, SIGMA_FF_OZAKI_BF16,
                          p->tblock);
       if (st == SIGMA_OK && (flags & SIGMA_HALFSUM_STATIC))
@@ -854,24 +1046,32 @@ extern "C" int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const doub
   if (plan->nvband > 0) {
     half_brk_kernel<<<plan->ng, kThreads, 0, s>>>(p, plan->brk);
     SIGMA_CUDA_TRY(cudaGetLastError());
-    half_occ_kernel<<<dim3(plan->ng, kNW), kThreads, 0, s>>>(p, plan->occ_ach, plan->occ_asx);
+    if (plan->ff3) {
+      half_occ_rows32_kernel<<<152, 256, 0, s>>>(p, plan->m32, plan->n32);
+      SIGMA_CUDA_TRY(cudaGetLastError());
+      half_occ_ff_kernel<<<dim3(kNW, plan->ng), kThreads, 0, s>>>(p, plan->m32, plan->n32,
+                                                                  plan->occ_ach, plan->occ_asx);
+    } else {
+      half_occ_kernel<<<dim3(plan->ng, kNW), kThreads, 0, s>>>(p, plan->occ_ach, plan->occ_asx);
+    }
     SIGMA_CUDA_TRY(cudaGetLastError());
   }
   if (plan->ff3) {
     const bool stat = plan->ff1 && achstemp;
     auto C = [](const double2* x) { return reinterpret_cast<const sigma_complex128*>(x); };
     auto M = [](double2* x) { return reinterpret_cast<sigma_complex128*>(x); };
-    half_z_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
+    half_z32_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
     SIGMA_CUDA_TRY(cudaGetLastError());
-    int st = ff_execute_weighted(plan->ff3, C(plan->z), C(aqsn), C(aqsm), vcoul, 0.5, M(plan->t3), stream);
+    const float2* z = plan->z;
+    int st = ff_execute_weighted(plan->ff3, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->t3), stream, z);
     if (st == SIGMA_OK)
-      st = ff_execute_weighted(plan->ff3, C(plan->z), C(aqsm), C(aqsm), vcoul, 0.5, M(plan->u3), stream);
+      st = ff_execute_weighted(plan->ff3, nullptr, C(aqsm), C(aqsm), vcoul, 0.5, M(plan->u3), stream, z);
     if (st == SIGMA_OK && stat) {
-      half_zs_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
+      half_zs32_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
       SIGMA_CUDA_TRY(cudaGetLastError());
-      st = ff_execute_weighted(plan->ff1, C(plan->z), C(aqsn), C(aqsm), vcoul, 0.5, M(plan->ts), stream);
+      st = ff_execute_weighted(plan->ff1, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->ts), stream, z);
       if (st == SIGMA_OK)
-        st = ff_execute_weighted(plan->ff1, C(plan->z), C(aqsm), C(aqsn), vcoul, 0.5, M(plan->us), stream);
+        st = ff_execute_weighted(plan->ff1, nullptr, C(aqsm), C(aqsn), vcoul, 0.5, M(plan->us), stream, z);
     }
     if (st != SIGMA_OK) return st;
     half_tensor_rows_kernel<<<(plan->nb * 32 + 255) / 256, 256, 0, s>>>(
