@@ -1,4 +1,5 @@
 // C ABI of the FF schDt contraction: plans, device execution, host drop-in.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -53,7 +54,8 @@ namespace sigma {
 // Plan over an already validated column map (igp_of[my_igp], -1 = column
 // left out).  Shared by the FF contraction and the static remainders.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
-                  const std::vector<int>& igp_of, int mode, void* shared_tiles) {
+                  const std::vector<int>& igp_of, int mode, void* shared_tiles,
+                  const int* row_kend) {
   *out = nullptr;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -82,13 +84,14 @@ int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, 
   const int ktile = 16;
   const int per_sm = mode == SIGMA_FF_FP64 ? ff_fp64_blocks_per_sm() : 1;
   p->grid = sms * per_sm;
+  OzakiTables tables;
   if (mode == SIGMA_FF_OZAKI_BF16) {
-    ozaki_size(p->oz, d, p->grid);
+    ozaki_size(p->oz, d, p->grid, row_kend, &tables);
     if (p->oz.max_seg > ozaki_max_segments()) {  // ngpown below ~18: too many frequencies per tile
       delete p;
       return SIGMA_ERR_UNSUPPORTED;
     }
-    if (p->oz.n_items < p->grid) p->grid = p->oz.n_items;
+    if (p->oz.n_items < p->grid) p->grid = std::max(1, p->oz.n_items);
     w.n_splits = 1;
     w.split_len = ncouls;
     w.n_items = 0;
@@ -131,6 +134,7 @@ int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, 
   }
   e = cudaMemcpy(const_cast<int*>(d.igp_of), igp_of.data(), sizeof(int) * ngpown,
                  cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && mode == SIGMA_FF_OZAKI_BF16) e = ozaki_upload_tables(p->oz, tables);
   if (e != cudaSuccess) {
     set_last_cuda_error(e, "cudaMemcpy(ff igp_of)", __LINE__);
     cudaFree(p->block);

@@ -27,6 +27,8 @@
 // sums the tile's rows per frequency (:408-418) with a reduce-scatter
 // butterfly.  Items are (row block, band block, K split), scheduled
 // statically.
+#include <algorithm>
+
 #include <cuda_bf16.h>
 
 #include "ff_ozaki.cuh"
@@ -92,6 +94,7 @@ __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz
     const long long rest = t / (kChunksPerRow * 128);
     const int kt = (int)(rest % oz.kt);
     const int rb = (int)(rest / oz.kt);
+    if (kt >= oz.kt_lim[rb]) continue;  // zero tile, not read by the contraction
     const int R = rb * kOzRows + r;
     const int k0 = kt * kOzKTile + ch * 8;
     float re[8], im[8];  // each value rounded to FP32 before it is sliced
@@ -166,21 +169,23 @@ __global__ void __launch_bounds__(256) ozaki_weights_kernel(FfDev p, OzakiPrep o
 }
 
 struct OzItem {
-  int rb, cb, s;
+  int rb, cb, t0, nst;  // row block, band block, first K' tile, tiles
   size_t pidx;
 };
-// Items run band block fastest, then row block, with the K split slowest:
-// the CTAs running at one time share A tiles (8 band blocks read each) and
-// touch only one K split of the B operand, which then stays in L2 (the whole
-// B operand is 200 MB at the production shape, one split a quarter of it).
-// pidx, the partial-sum slot, does not depend on the order.
+// Items run band block fastest, then the work entries (row block, then the
+// K split slowest): the CTAs running at one time share A tiles (8 band
+// blocks read each) and touch only one K split of the B operand, which then
+// stays in L2 (the whole B operand is 200 MB at the production shape, one
+// split a quarter of it).  pidx, the partial-sum slot, does not depend on
+// the order.
 __device__ __forceinline__ OzItem oz_decode(const OzakiPrep& oz, int item) {
   OzItem t;
   t.cb = item % oz.n_col_blocks;
-  const int r = item / oz.n_col_blocks;
-  t.rb = r % oz.n_row_blocks;
-  t.s = r / oz.n_row_blocks;
-  t.pidx = ((size_t)t.rb * oz.n_col_blocks + t.cb) * oz.n_splits + t.s;
+  const int4 e = oz.entries[item / oz.n_col_blocks];
+  t.rb = e.x;
+  t.t0 = e.z;
+  t.nst = e.w;
+  t.pidx = ((size_t)t.rb * oz.n_col_blocks + t.cb) * oz.max_pieces + e.y;
   return t;
 }
 
@@ -223,10 +228,9 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
       uint32_t g = 0;  // tiles issued by this CTA
       for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
         const OzItem it = oz_decode(oz, item);
-        const int kt_begin = it.s * oz.split_tiles;
-        const int nst = min(oz.split_tiles, two_kt - kt_begin);
-        const unsigned char* a_src = oz.a_tiles + ((size_t)it.rb * two_kt + kt_begin) * kOperandBytes;
-        const unsigned char* b_src = oz.b_tiles + ((size_t)it.cb * two_kt + kt_begin) * kOperandBytes;
+        const int nst = it.nst;
+        const unsigned char* a_src = oz.a_tiles + ((size_t)it.rb * two_kt + it.t0) * kOperandBytes;
+        const unsigned char* b_src = oz.b_tiles + ((size_t)it.cb * two_kt + it.t0) * kOperandBytes;
         for (int s = 0; s < nst; ++s, ++g) {
           const uint32_t b = g % kStages, use = g / kStages;
           // stage b is free once the MMAs of its previous tile have completed
@@ -248,9 +252,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
       uint32_t g = 0;   // tiles consumed by this CTA
       uint32_t gc = 0;  // accumulator lifetimes started
       for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
-        const OzItem it = oz_decode(oz, item);
-        const int kt_begin = it.s * oz.split_tiles;
-        const int nst = min(oz.split_tiles, two_kt - kt_begin);
+        const int nst = oz_decode(oz, item).nst;
         for (int s = 0; s < nst; ++s, ++g) {
           const int cs = s % kChunkStages;
           const uint32_t tb = gc & 1u;
@@ -307,9 +309,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
     const int rows = p.nf * p.ng;
     for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
       const OzItem it = oz_decode(oz, item);
-      const int kt_begin = it.s * oz.split_tiles;
-      const int nst = min(oz.split_tiles, two_kt - kt_begin);
-      const int nchunks = (nst + kChunkStages - 1) / kChunkStages;
+      const int nchunks = (it.nst + kChunkStages - 1) / kChunkStages;
       float acc[128];
 #pragma unroll
       for (int i = 0; i < 128; ++i) acc[i] = 0.f;
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
 }
 
 // schDt[n1][ifreq]: one warp per entry, fixed-order compensated sum over the
-// row blocks that hold frequency ifreq and over the K splits.
+// row blocks that hold frequency ifreq and over their work entries.
 __global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, double2* schdt) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -423,15 +423,18 @@ __global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, double2* schdt) {
   const int n = warp / p.nf, f = warp % p.nf;
   const int cb = n / kOzCols, c = n % kOzCols;
   const int rb_lo = (f * p.ng) / kOzRows, rb_hi = ((f + 1) * p.ng - 1) / kOzRows;
-  const int count = (rb_hi - rb_lo + 1) * oz.n_splits;
   Comp sx, sy;
-  for (int q = lane; q < count; q += 32) {
-    const int rb = rb_lo + q / oz.n_splits, s = q % oz.n_splits;
+  int q0 = 0;  // entries of the row blocks before rb, lanes take every 32nd
+  for (int rb = rb_lo; rb <= rb_hi; ++rb) {
+    const int np = oz.pieces[rb];
     const int seg = f - (rb * kOzRows) / p.ng;
-    const size_t pidx = ((size_t)rb * oz.n_col_blocks + cb) * oz.n_splits + s;
-    const double2 v = oz.partial[(pidx * oz.max_seg + seg) * kOzCols + c];
-    sx.add(v.x);
-    sy.add(v.y);
+    for (int j = (lane - q0 % 32 + 32) % 32; j < np; j += 32) {
+      const size_t pidx = ((size_t)rb * oz.n_col_blocks + cb) * oz.max_pieces + j;
+      const double2 v = oz.partial[(pidx * oz.max_seg + seg) * kOzCols + c];
+      sx.add(v.x);
+      sy.add(v.y);
+    }
+    q0 += np;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -450,22 +453,65 @@ __global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, double2* schdt) {
 
 }  // namespace
 
-void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid) {
+void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend, OzakiTables* tables) {
   oz.kt = (d.nc + kOzKTile - 1) / kOzKTile;
   const int rows = d.nf * d.ng;
   oz.n_row_blocks = (rows + kOzRows - 1) / kOzRows;
   oz.n_col_blocks = (d.nb + kOzCols - 1) / kOzCols;
   oz.max_seg = (kOzRows + d.ng - 2) / d.ng + 1;
-  const long long base = (long long)oz.n_row_blocks * oz.n_col_blocks;
   const int two_kt = 2 * oz.kt;
-  long long s = (20LL * grid + base - 1) / base;
+  std::vector<int> kl(oz.n_row_blocks, oz.kt);
+  long long active = 0;  // K' tiles over all row blocks that can be nonzero
+  for (int rb = 0; rb < oz.n_row_blocks; ++rb) {
+    if (row_kend) {
+      int k = 0;
+      for (int r = rb * kOzRows; r < std::min(rows, rb * kOzRows + kOzRows); ++r)
+        k = std::max(k, std::min(row_kend[r], d.nc));
+      kl[rb] = (k + kOzKTile - 1) / kOzKTile;
+    }
+    active += 2LL * kl[rb];
+  }
+  // about 20 items per CTA: as many K splits as the active tiles need
+  const long long want = 20LL * grid * two_kt;
+  const long long have = std::max(1LL, active * oz.n_col_blocks);
+  long long s = (want + have - 1) / have;
   if (s < 1) s = 1;
   if (s > two_kt) s = two_kt;
   oz.split_tiles = (int)((two_kt + s - 1) / s);
   oz.n_splits = (two_kt + oz.split_tiles - 1) / oz.split_tiles;
-  oz.n_items = (int)(base * oz.n_splits);
+  // entries: per split, per row block, the split's tiles within [0, kl) and
+  // [kt, kt + kl) (one run when they touch)
+  std::vector<int4> ent;
+  std::vector<int> pieces(oz.n_row_blocks, 0);
+  for (int sp = 0; sp < oz.n_splits; ++sp) {
+    const int a = sp * oz.split_tiles, b = std::min(two_kt, a + oz.split_tiles);
+    for (int rb = 0; rb < oz.n_row_blocks; ++rb) {
+      const int runs[2][2] = {{0, kl[rb]}, {oz.kt, oz.kt + kl[rb]}};
+      int lo[2], hi[2], n = 0;
+      for (const auto& run : runs) {
+        const int x = std::max(a, run[0]), y = std::min(b, run[1]);
+        if (x >= y) continue;
+        if (n > 0 && hi[n - 1] == x) {
+          hi[n - 1] = y;
+        } else {
+          lo[n] = x;
+          hi[n] = y;
+          ++n;
+        }
+      }
+      for (int i = 0; i < n; ++i) ent.push_back(make_int4(rb, pieces[rb]++, lo[i], hi[i] - lo[i]));
+    }
+  }
+  oz.n_entries = (int)ent.size();
+  oz.n_items = oz.n_entries * oz.n_col_blocks;
+  oz.max_pieces = std::max(1, *std::max_element(pieces.begin(), pieces.end()));
   oz.ng = d.ng;
   oz.nb_pad = oz.n_col_blocks * kOzCols;
+  if (tables) {
+    tables->entries = std::move(ent);
+    tables->pieces = std::move(pieces);
+    tables->kt_lim = std::move(kl);
+  }
 }
 
 int ozaki_max_segments() { return kMaxSeg; }
@@ -474,12 +520,20 @@ size_t ozaki_tile_bytes(const OzakiPrep& oz) {
   return ((size_t)oz.n_row_blocks + oz.n_col_blocks) * 2 * oz.kt * kOperandBytes + 1024;
 }
 
+static size_t up256(size_t v) { return (v + 255) / 256 * 256; }
+
 static size_t ozaki_partial_only_bytes(const OzakiPrep& oz) {
-  return (sizeof(double2) * (size_t)oz.n_items * oz.max_seg * kOzCols + 255) / 256 * 256;
+  return up256(sizeof(double2) * (size_t)oz.n_row_blocks * oz.n_col_blocks * oz.max_pieces *
+               oz.max_seg * kOzCols);
+}
+static size_t ozaki_wtab_bytes(const OzakiPrep& oz) {
+  return up256(sizeof(float2) * (size_t)oz.ng * oz.nb_pad);
 }
 
 size_t ozaki_partial_bytes(const OzakiPrep& oz) {
-  return ozaki_partial_only_bytes(oz) + sizeof(float2) * (size_t)oz.ng * oz.nb_pad + 256;
+  return ozaki_partial_only_bytes(oz) + ozaki_wtab_bytes(oz) +
+         up256(sizeof(int4) * (size_t)std::max(oz.n_entries, 1)) +
+         2 * up256(sizeof(int) * (size_t)oz.n_row_blocks) + 256;
 }
 
 size_t ozaki_prep_bytes(const OzakiPrep& oz) { return ozaki_tile_bytes(oz) + ozaki_partial_bytes(oz); }
@@ -490,11 +544,32 @@ void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial) {
   oz.b_tiles = oz.a_tiles + (size_t)oz.n_row_blocks * 2 * oz.kt * kOperandBytes;
   uintptr_t pp = (reinterpret_cast<uintptr_t>(partial) + 255) & ~uintptr_t(255);
   oz.partial = reinterpret_cast<double2*>(pp);
-  oz.wtab = reinterpret_cast<float2*>(pp + ozaki_partial_only_bytes(oz));
+  pp += ozaki_partial_only_bytes(oz);
+  oz.wtab = reinterpret_cast<float2*>(pp);
+  pp += ozaki_wtab_bytes(oz);
+  oz.entries = reinterpret_cast<const int4*>(pp);
+  pp += up256(sizeof(int4) * (size_t)std::max(oz.n_entries, 1));
+  oz.pieces = reinterpret_cast<const int*>(pp);
+  pp += up256(sizeof(int) * (size_t)oz.n_row_blocks);
+  oz.kt_lim = reinterpret_cast<const int*>(pp);
 }
 
 void ozaki_prep_bind(OzakiPrep& oz, void* base) {
   ozaki_bind(oz, base, static_cast<char*>(base) + ozaki_tile_bytes(oz));
+}
+
+cudaError_t ozaki_upload_tables(const OzakiPrep& oz, const OzakiTables& t) {
+  cudaError_t e = cudaSuccess;
+  if (!t.entries.empty())
+    e = cudaMemcpy(const_cast<int4*>(oz.entries), t.entries.data(), sizeof(int4) * t.entries.size(),
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(const_cast<int*>(oz.pieces), t.pieces.data(), sizeof(int) * t.pieces.size(),
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(const_cast<int*>(oz.kt_lim), t.kt_lim.data(), sizeof(int) * t.kt_lim.size(),
+                   cudaMemcpyHostToDevice);
+  return e;
 }
 
 cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s) {

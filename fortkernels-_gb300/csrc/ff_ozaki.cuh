@@ -1,6 +1,8 @@
 // FF schDt contraction on tcgen05 tensor cores with split BF16 operands.
 #pragma once
 
+#include <vector>
+
 #include "ff_internal.cuh"
 
 namespace sigma {
@@ -24,9 +26,16 @@ struct OzakiPrep {
   int n_row_blocks;         // ceil(nfreq * ngpown / 128)
   int n_col_blocks;         // ceil(number_bands / 64)
   int n_splits, split_tiles;  // K' split into n_splits ranges of split_tiles tiles
-  int n_items;
+  // Work entries, the K split slowest: each is one row block's tiles within
+  // one split that can hold nonzero A values (row blocks whose rows are zero
+  // past some K have fewer); items are entries x band blocks.
+  int n_entries, n_items;
+  int max_pieces;           // entries per row block at most (partial slots)
+  const int4* entries;      // [n_entries]: row block, piece, first K' tile, tiles
+  const int* pieces;        // [n_row_blocks]: entries of each row block
+  const int* kt_lim;        // [n_row_blocks]: K tiles (per half) that can be nonzero
   int max_seg;              // frequencies one row block can touch
-  double2* partial;         // [row block][col block][split][max_seg][64]
+  double2* partial;         // [row block][col block][piece][max_seg][64]
   // Epilogue factors, formed per execution: wtab[g][n] = aqsm[n][igp(g)] *
   // column weight, in FP32 (0 for a skipped column or a padded band), so a
   // drain lane reads its row's 64 factors as contiguous 16-byte loads.
@@ -35,7 +44,16 @@ struct OzakiPrep {
 };
 
 // Work sizing and buffers of the split-BF16 form (partials + slices).
-void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid);
+// row_kend (nullable, [nfreq * ngpown]): the A row's entries at K >= row_kend
+// are zero, so the tiles past its row block's largest value are skipped.
+// The entry tables (host copies) are uploaded by ozaki_upload_tables.
+struct OzakiTables {
+  std::vector<int4> entries;
+  std::vector<int> pieces, kt_lim;
+};
+void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend = nullptr,
+                OzakiTables* tables = nullptr);
+cudaError_t ozaki_upload_tables(const OzakiPrep& oz, const OzakiTables& t);
 int ozaki_max_segments();
 size_t ozaki_prep_bytes(const OzakiPrep& oz);  // slice images + partials
 size_t ozaki_tile_bytes(const OzakiPrep& oz);   // slice images (1024-aligned inside)

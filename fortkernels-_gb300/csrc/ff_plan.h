@@ -14,8 +14,12 @@ namespace sigma {
 // shared_tiles (split-BF16 form only): a workspace of at least
 // ff_plan_tile_bytes() holding the slice images instead of the plan's own
 // allocation, for plans that run one after another on one stream.
+// row_kend (split-BF16 form only, nullable): per I_epsR row (ifreq * ngpown
+// + my_igp) the K from which the row is zero in every execution; the
+// contraction skips those K tiles.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
-                  const std::vector<int>& igp_of, int mode, void* shared_tiles = nullptr);
+                  const std::vector<int>& igp_of, int mode, void* shared_tiles = nullptr,
+                  const int* row_kend = nullptr);
 int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes);
 
 // sigma_ff_execute with the column weight vfac * vcoul[igp] (vcoul a device

@@ -978,11 +978,18 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
       p->us = reinterpret_cast<double2*>(t + b_tiles + b_z + 2 * b_r3 + b_r1);
       p->m32 = reinterpret_cast<float2*>(t + b_tiles + b_z + 2 * b_r3 + 2 * b_r1);
       p->n32 = reinterpret_cast<float2*>(t + b_tiles + b_z + 2 * b_r3 + 2 * b_r1 + b_o);
+      // Z rows (iw, col) are zero from the column's g-vector limit on
+      std::vector<int> kend3((size_t)kNW * ngpown), kend1(ngpown);
+      for (int g = 0; g < ngpown; ++g) {
+        const int igp = igp_of[g];
+        kend1[g] = igp < 0 ? 0 : igp;
+        for (int f = 0; f < kNW; ++f) kend3[(size_t)f * ngpown + g] = igp < 0 ? 0 : std::max(igp - 1, 0);
+      }
       st = ff_plan_build(&p->ff3, number_bands, ncouls, ngpown, kNW, igp_of, SIGMA_FF_OZAKI_BF16,
-                         p->tblock);
+                         p->tblock, kend3.data());
       if (st == SIGMA_OK && (flags & SIGMA_HALFSUM_STATIC))
         st = ff_plan_build(&p->ff1, number_bands, ncouls, ngpown, 1, igp_of, SIGMA_FF_OZAKI_BF16,
-                           p->tblock);
+                           p->tblock, kend1.data());
     }
     if (st != SIGMA_OK) {
       sigma_gpp_halfsum_plan_destroy(p);
