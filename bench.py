@@ -760,8 +760,9 @@ def run_ours(args, rank, world, local_rank):
                    "rel_err_vs_fp64": tensor_err, "stress_rel_err_vs_fp64": tensor_stress_err,
                    "max_rel_err": max(max(tensor_err["achtemp"]), max(tensor_err["asxtemp"]),
                                       max(tensor_stress_err["achtemp"]), max(tensor_stress_err["asxtemp"])),
-                   "path": "frequency factors in FP64, band sum as split-BF16 tcgen05 GEMM (FF kernel), "
-                           "occupied bands as in the mixed form"},
+                   "path": "frequency factors in float-float arithmetic on the FP32 pipe, rounded to FP32; "
+                           "band sum as split-BF16 tcgen05 GEMM (FF kernel); occupied bands as in the "
+                           "mixed form"},
         "ff": ff,
         "ff_sigma": ffs,
         "batched": batch,

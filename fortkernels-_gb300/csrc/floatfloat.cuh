@@ -9,8 +9,22 @@
 namespace sigma {
 
 // x = hi + lo: hi is x truncated to 24 significant bits (exact in FP32), lo
-// the rest rounded to FP32; integer operations and one exact conversion only.
+// the remaining 29 bits rounded to FP32 (|x - hi - lo| <= 2^-48 |x|).  For
+// exponents where both are normal FP32 values, hi is assembled from the
+// bits and lo is one 32-bit integer conversion scaled by a power of two; no
+// instruction on the FP64 pipe (conversions from FP64 run there at the FP64
+// rate).
 __device__ __forceinline__ void split_exact(double x, float& hi, float& lo) {
+  const unsigned int whi = (unsigned int)__double2hiint(x), wlo = (unsigned int)__double2loint(x);
+  const int ex = (int)((whi >> 20) & 0x7FFu);
+  if (ex >= 949 && ex <= 1150) {  // 2^-74 <= |x| < 2^128
+    hi = __uint_as_float((whi & 0x80000000u) | ((unsigned int)(ex - 896) << 23) |
+                         ((whi & 0xFFFFFu) << 3) | (wlo >> 29));
+    const float m = __uint2float_rn(wlo & 0x1FFFFFFFu);    // < 2^29
+    const float scale = __uint_as_float((unsigned int)(ex - 948) << 23);  // 2^(ex - 1075)
+    lo = (whi >> 31) ? -(m * scale) : m * scale;
+    return;
+  }
   const long long bits = __double_as_longlong(x);
   constexpr long long kLow = (1LL << 29) - 1;
   hi = __double2float_rn(__longlong_as_double(bits & ~kLow));

@@ -460,9 +460,31 @@ __global__ void __launch_bounds__(kThreads) half_occ_ff_kernel(HalfDev p, const 
 #pragma unroll
     for (int v = 0; v < kVals; ++v) acc[v] = hi[v] = lo[v] = 0.f;
     int run = 0;
+    // operands of the next g-vector are loaded one iteration ahead
+    const double2* wt_row = p.wt + (size_t)col * p.nc;
+    const double2* ie_row = p.ieps + (size_t)col * p.nc;
+    double2 wt_n = make_double2(0.0, 0.0), ie_n = make_double2(0.0, 0.0);
+    float2 an_n[kOccBandsF], am_n[kOccBandsF];
+    auto fetch = [&](int ig) {
+      wt_n = wt_row[ig];
+      ie_n = ie_row[ig];
+#pragma unroll
+      for (int q = 0; q < kOccBandsF; ++q) {
+        const size_t bo = (size_t)(g0 + min(q, nbl - 1)) * p.nc + ig;
+        an_n[q] = n32[bo];
+        am_n[q] = m32[bo];
+      }
+    };
+    if (tid < kend) fetch(tid);
     for (int ig = tid; ig < kend; ig += kThreads) {
-      const size_t off = (size_t)col * p.nc + ig;
-      const double2 wt = p.wt[off], ie = p.ieps[off];
+      const double2 wt = wt_n, ie = ie_n;
+      float2 an_c[kOccBandsF], am_c[kOccBandsF];
+#pragma unroll
+      for (int q = 0; q < kOccBandsF; ++q) {
+        an_c[q] = an_n[q];
+        am_c[q] = am_n[q];
+      }
+      if (ig + kThreads < kend) fetch(ig + kThreads);
       const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
       const FF b2 = ff_mul(b, b);
       const FF s2 = ff_add(ff_mul(a, a), b2);  // |wtilde|^2
@@ -515,15 +537,14 @@ __global__ void __launch_bounds__(kThreads) half_occ_ff_kernel(HalfDev p, const 
 #pragma unroll
       for (int q = 0; q < kOccBandsF; ++q)
         if (q < nbl) {
-          const size_t bo = (size_t)(g0 + q) * p.nc + ig;
-          const float2 an = n32[bo];
+          const float2 an = an_c[q];
           float* t = acc + 8 * q;
           t[0] = fmaf(an.x, sch.x, fmaf(-an.y, sch.y, t[0]));
           t[1] = fmaf(an.x, sch.y, fmaf(an.y, sch.x, t[1]));
           t[4] = fmaf(an.x, ssx.x, fmaf(-an.y, ssx.y, t[4]));
           t[5] = fmaf(an.x, ssx.y, fmaf(an.y, ssx.x, t[5]));
           if (pair) {
-            const float2 am = m32[bo];
+            const float2 am = am_c[q];
             t[2] = fmaf(am.x, sch.x, fmaf(-am.y, sch.y, t[2]));
             t[3] = fmaf(am.x, sch.y, fmaf(am.y, sch.x, t[3]));
             t[6] = fmaf(am.x, ssx.x, fmaf(-am.y, ssx.y, t[6]));
