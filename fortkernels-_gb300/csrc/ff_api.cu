@@ -244,10 +244,10 @@ namespace sigma {
 int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
                         const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
                         const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
-                        void* stream, const float2* epsr32) {
+                        void* stream, const float2* epsr32, bool reuse_a) {
   if (!plan) return SIGMA_ERR_NULL;
-  if ((!I_epsR && !epsr32) || !aqsntemp || !aqsmtemp || !schDt_matrix) return SIGMA_ERR_NULL;
-  if (epsr32 && plan->mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
+  if ((!I_epsR && !epsr32 && !reuse_a) || !aqsntemp || !aqsmtemp || !schDt_matrix) return SIGMA_ERR_NULL;
+  if ((epsr32 || reuse_a) && plan->mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
   int dev = 0;
   SIGMA_CUDA_TRY(cudaGetDevice(&dev));
   if (dev != plan->device) return SIGMA_ERR_UNSUPPORTED;
@@ -268,7 +268,7 @@ int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
     SIGMA_CUDA_TRY(launch_ff_reduce(d, plan->work, reinterpret_cast<double2*>(schDt_matrix), s));
   } else {
-    SIGMA_CUDA_TRY(launch_ozaki_prep(d, plan->oz, s));
+    SIGMA_CUDA_TRY(launch_ozaki_prep(d, plan->oz, s, !reuse_a));
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
     SIGMA_CUDA_TRY(launch_ozaki_gemm(d, plan->work, plan->oz, plan->grid, s));
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));

@@ -572,10 +572,13 @@ cudaError_t ozaki_upload_tables(const OzakiPrep& oz, const OzakiTables& t) {
   return e;
 }
 
-cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s) {
-  ozaki_prep_a_kernel<<<152 * 16, 256, 0, s>>>(d, oz);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s, bool with_a) {
+  cudaError_t e;
+  if (with_a) {
+    ozaki_prep_a_kernel<<<152 * 16, 256, 0, s>>>(d, oz);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   ozaki_prep_b_kernel<<<152 * 4, 256, 0, s>>>(d, oz);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -62,7 +62,8 @@ void ozaki_prep_bind(OzakiPrep& oz, void* base);
 // Slice images and partials in separate buffers (images may be a workspace
 // shared by plans that run one after another on one stream).
 void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial);
-cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s);
+// with_a = false keeps the A slices already in the workspace
+cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s, bool with_a = true);
 cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& oz, int grid,
                               cudaStream_t s);
 cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s);

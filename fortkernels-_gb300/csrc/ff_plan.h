@@ -25,10 +25,14 @@ int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size
 // sigma_ff_execute with the column weight vfac * vcoul[igp] (vcoul a device
 // array, or nullptr for weight 1).
 // With epsr32 set (split-BF16 form only) the contraction reads that FP32
-// operand [nf][ng][nc] instead of I_epsR (which may then be NULL).
+// operand [nf][ng][nc] instead of I_epsR (which may then be NULL).  With
+// reuse_a (split-BF16 form only) it contracts the operand slices the
+// previous execution left in the plan's slice workspace (the same operand
+// again, no other plan on that workspace in between); I_epsR and epsr32 are
+// then not read.
 int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
                         const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
                         const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
-                        void* stream, const float2* epsr32 = nullptr);
+                        void* stream, const float2* epsr32 = nullptr, bool reuse_a = false);
 
 }  // namespace sigma

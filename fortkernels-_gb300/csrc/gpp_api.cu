@@ -406,12 +406,13 @@ sigma_gpp_plan g_cached_plan = nullptr;
 
 // Copy stream and gate words of the FP64 host drop-in, whose host-to-device
 // copies run beside the sum (one per process, guarded by api_mutex()).
-constexpr int kGateChunks = 8;
+constexpr int kGateChunks = 8;               // words for the K splits after the first
+constexpr int kGateWords = kGateChunks + 3;  // + two for split 0 + one for aqsm
 struct CopyLane {
   int device = -1;
   cudaStream_t cs = nullptr;
   cudaEvent_t ev_s = nullptr, ev_done = nullptr;
-  unsigned* host_words = nullptr;  // pinned, kGateChunks
+  unsigned* host_words = nullptr;  // pinned, kGateWords
   unsigned epoch = 0;
 };
 CopyLane g_lane;
@@ -437,7 +438,7 @@ int lane_for(int dev, CopyLane** out) {
     SIGMA_CUDA_TRY(cudaEventCreateWithFlags(&g_lane.ev_s, cudaEventDisableTiming));
     SIGMA_CUDA_TRY(cudaEventCreateWithFlags(&g_lane.ev_done, cudaEventDisableTiming));
     SIGMA_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&g_lane.host_words),
-                                 sizeof(unsigned) * kGateChunks, cudaHostAllocDefault));
+                                 sizeof(unsigned) * kGateWords, cudaHostAllocDefault));
   }
   *out = &g_lane;
   return SIGMA_OK;
@@ -502,7 +503,7 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
   const size_t sizes[10] = {band_bytes, band_bytes, col_bytes, col_bytes, sizeof(double) * (size_t)nc,
                             sizeof(double) * kNW, sizeof(sigma_complex128) * kNW,
                             sizeof(sigma_complex128) * kNW, sizeof(sigma_complex128) * (size_t)nb,
-                            sizeof(unsigned) * kGateChunks};
+                            sizeof(unsigned) * kGateWords};
   for (int i = 0; i < 10; ++i) {
     off[i] = total;
     total += align_up(sizes[i], 256);
@@ -513,18 +514,24 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
   char* a = static_cast<char*>(arena);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (precision == SIGMA_PREC_FP64 && plan->schy.n_items > 0) {
-    // FP64 with the shared-frequency pass: the column inputs travel in
-    // kGateChunks pieces on a copy stream while the sum runs; each piece is
-    // followed by its gate word, which the pass's items wait for.
+    // FP64 with the shared-frequency pass: the inputs travel on a copy
+    // stream while the sum runs, each piece followed by a gate word the
+    // pass's items wait for.  The items run with the K split slowest, and
+    // the pieces follow them: split 0 of aqsn and of the columns the first
+    // wave of items takes, aqsm (read only in the items' epilogues), split 0
+    // of the other columns, then groups of splits of aqsn and all columns.
     CopyLane* lane = nullptr;
     st = lane_for(dev, &lane);
     if (st != SIGMA_OK) return st;
-    const int ncb = plan->schy.n_col_blocks;
-    const int per = (ncb + kGateChunks - 1) / kGateChunks;  // column blocks per piece
-    const int pieces = (ncb + per - 1) / per;
+    const GppWork& y = plan->schy;
+    const int ncb = y.n_col_blocks, nsp = y.n_splits;
+    const int first = std::min(ncb, (plan->schy_grid + y.n_band_blocks - 1) / y.n_band_blocks);
+    const int gs = std::max(1, (nsp - 1 + kGateChunks - 1) / kGateChunks);  // splits per later word
+    const int groups = (nsp - 1 + gs - 1) / gs;
+    const int m_word = 2 + groups;
     unsigned epoch = ++lane->epoch;
     if (epoch == 0) epoch = ++lane->epoch;
-    for (int c = 0; c < pieces; ++c) lane->host_words[c] = epoch;
+    for (int c = 0; c <= m_word; ++c) lane->host_words[c] = epoch;
     unsigned* gate = reinterpret_cast<unsigned*>(a + off[9]);
     // gate words cleared and counters zeroed on the caller's stream; the
     // copies start after that and after the work already queued there (no
@@ -534,24 +541,46 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
     SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 4 * sizeof(int), s));
     SIGMA_CUDA_TRY(cudaEventRecord(lane->ev_s, s));
     SIGMA_CUDA_TRY(cudaStreamWaitEvent(lane->cs, lane->ev_s, 0));
-    const void* base_src[4] = {aqsm, aqsn, vcoul, wx};
-    const int base_idx[4] = {0, 1, 4, 5};
-    for (int i = 0; i < 4; ++i)
-      SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[base_idx[i]], base_src[i], sizes[base_idx[i]],
-                                     cudaMemcpyHostToDevice, lane->cs));
-    const size_t row_bytes = sizeof(sigma_complex128) * (size_t)nc;
-    for (int c = 0; c < pieces; ++c) {
-      const int g0 = c * per * kBPY, g1 = std::min((c + 1) * per * kBPY, ng);
-      if (g1 > g0) {
-        const size_t o = row_bytes * (size_t)g0, n = row_bytes * (size_t)(g1 - g0);
-        SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[2] + o, reinterpret_cast<const char*>(ieps) + o, n,
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[4], vcoul, sizes[4], cudaMemcpyHostToDevice, lane->cs));
+    SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[5], wx, sizes[5], cudaMemcpyHostToDevice, lane->cs));
+    const size_t pitch = sizeof(sigma_complex128) * (size_t)nc;
+    // rows [r0, r1) x g-vectors [k0, k1) of a [rows][nc] array
+    auto block = [&](int dst, const sigma_complex128* src, int r0, int r1, int k0, int k1) -> int {
+      if (r1 <= r0 || k1 <= k0) return SIGMA_OK;
+      const size_t o = pitch * (size_t)r0 + sizeof(sigma_complex128) * (size_t)k0;
+      SIGMA_CUDA_TRY(cudaMemcpy2DAsync(a + off[dst] + o, pitch, reinterpret_cast<const char*>(src) + o,
+                                       pitch, sizeof(sigma_complex128) * (size_t)(k1 - k0), r1 - r0,
                                        cudaMemcpyHostToDevice, lane->cs));
-        SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[3] + o, reinterpret_cast<const char*>(wt) + o, n,
-                                       cudaMemcpyHostToDevice, lane->cs));
-      }
+      return SIGMA_OK;
+    };
+    auto word = [&](int c) -> int {
       SIGMA_CUDA_TRY(cudaMemcpyAsync(gate + c, lane->host_words + c, sizeof(unsigned),
                                      cudaMemcpyHostToDevice, lane->cs));
+      return SIGMA_OK;
+    };
+    const int k_split0 = std::min(y.split_len, nc);
+    const int g_first = std::min(first * kBPY, ng);
+    int r = SIGMA_OK;
+    if (r == SIGMA_OK) r = block(1, aqsn, 0, nb, 0, k_split0);
+    if (r == SIGMA_OK) r = block(2, ieps, 0, g_first, 0, k_split0);
+    if (r == SIGMA_OK) r = block(3, wt, 0, g_first, 0, k_split0);
+    if (r == SIGMA_OK) r = word(0);
+    if (r == SIGMA_OK) {
+      SIGMA_CUDA_TRY(cudaMemcpyAsync(a + off[0], aqsm, sizes[0], cudaMemcpyHostToDevice, lane->cs));
+      r = word(m_word);
     }
+    if (r == SIGMA_OK) r = block(2, ieps, g_first, ng, 0, k_split0);
+    if (r == SIGMA_OK) r = block(3, wt, g_first, ng, 0, k_split0);
+    if (r == SIGMA_OK) r = word(1);
+    for (int g = 0; g < groups && r == SIGMA_OK; ++g) {
+      const int k0 = std::min(nc, (1 + g * gs) * y.split_len);
+      const int k1 = std::min(nc, (1 + (g + 1) * gs) * y.split_len);
+      r = block(1, aqsn, 0, nb, k0, k1);
+      if (r == SIGMA_OK) r = block(2, ieps, 0, ng, k0, k1);
+      if (r == SIGMA_OK) r = block(3, wt, 0, ng, k0, k1);
+      if (r == SIGMA_OK) r = word(2 + g);
+    }
+    if (r != SIGMA_OK) return r;
     SIGMA_CUDA_TRY(cudaEventRecord(lane->ev_done, lane->cs));
 
     GppDev p;
@@ -569,9 +598,12 @@ int gpp_host(int precision, int nb, int nvband, int nc, int ng, int nstart, int 
     p.wx = reinterpret_cast<const double*>(a + off[5]);
     p.igp_of = plan->igp_of;
     GppWork w = plan->schy;
+    w.order_ks = 1;
     w.ready = gate;
     w.epoch = epoch;
-    w.ready_cb = per;
+    w.ready_first = first;
+    w.ready_gs = gs;
+    w.ready_m = gate + m_word;
     w.ready_status = plan->prep.status;
     SIGMA_CUDA_TRY(launch_sch_fp64y(p, w, plan->schy_grid, s));
     SIGMA_CUDA_TRY(cudaStreamWaitEvent(s, lane->ev_done, 0));

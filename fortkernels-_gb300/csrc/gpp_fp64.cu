@@ -241,8 +241,11 @@ __device__ __forceinline__ void wait_ready(const unsigned* flag, unsigned epoch,
 template <int BN, int BP>
 __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w, int item,
                                                unsigned char* smem_raw, int tid) {
-  if (w.ready) {  // inputs of this column block copied yet?
-    if (tid == 0) wait_ready(w.ready + decode_item(w, item).cb / w.ready_cb, w.epoch, w.ready_status);
+  if (w.ready) {  // inputs of this item copied yet?
+    if (tid == 0) {
+      const ItemCoord g = decode_item(w, item);
+      wait_ready(w.ready + gate_word(w, g.cb, g.s), w.epoch, w.ready_status);
+    }
     __syncthreads();
   }
   constexpr int TB = BN / 16, TC = BP / 16;
@@ -338,6 +341,10 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp]; the 16 lanes of a
   // half-warp hold the item's columns for the same bands and sum them with
   // a fixed butterfly
+  if (w.ready_m) {  // aqsm copied yet?
+    if (tid == 0) wait_ready(w.ready_m, w.epoch, w.ready_status);
+    __syncthreads();
+  }
 #pragma unroll
   for (int i = 0; i < TB; ++i) {
     const int bl = ty + 16 * i, n1 = n1_0 + bl;

@@ -1091,15 +1091,18 @@ extern "C" int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const doub
     half_z32_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
     SIGMA_CUDA_TRY(cudaGetLastError());
     const float2* z = plan->z;
+    // T and U contract the same slab: U reuses the slices T cut
     int st = ff_execute_weighted(plan->ff3, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->t3), stream, z);
     if (st == SIGMA_OK)
-      st = ff_execute_weighted(plan->ff3, nullptr, C(aqsm), C(aqsm), vcoul, 0.5, M(plan->u3), stream, z);
+      st = ff_execute_weighted(plan->ff3, nullptr, C(aqsm), C(aqsm), vcoul, 0.5, M(plan->u3), stream,
+                               nullptr, true);
     if (st == SIGMA_OK && stat) {
       half_zs32_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
       SIGMA_CUDA_TRY(cudaGetLastError());
       st = ff_execute_weighted(plan->ff1, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->ts), stream, z);
       if (st == SIGMA_OK)
-        st = ff_execute_weighted(plan->ff1, nullptr, C(aqsm), C(aqsn), vcoul, 0.5, M(plan->us), stream, z);
+        st = ff_execute_weighted(plan->ff1, nullptr, C(aqsm), C(aqsn), vcoul, 0.5, M(plan->us), stream,
+                                 nullptr, true);
     }
     if (st != SIGMA_OK) return st;
     half_tensor_rows_kernel<<<(plan->nb * 32 + 255) / 256, 256, 0, s>>>(

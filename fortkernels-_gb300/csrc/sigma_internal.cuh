@@ -59,15 +59,26 @@ struct GppWork {
   int n_items;
   int* counter;                // dynamic item counter (zeroed before launch)
   double2* partial;            // [n_band_blocks][n_col_blocks][n_splits][BN][3]
-  // Optional gate of the FP64 shared-frequency pass: the items of column
-  // block cb first wait (bounded) until ready[cb / ready_cb] == epoch, a word
-  // the host copies to the device after that column range's inputs, so host
-  // copies overlap the sum; a wait that gives up records SIGMA_ERR_TIMEOUT.
+  // Items run band block fastest, then the K split, then the column block;
+  // with order_ks set, band block, column block, K split (the split slowest).
+  int order_ks = 0;
+  // Optional gate of the FP64 shared-frequency pass (with order_ks): an item
+  // first waits (bounded) until the word of its inputs' piece equals epoch,
+  // a word the host copies to the device after that piece, so host copies
+  // overlap the sum; a wait that gives up records SIGMA_ERR_TIMEOUT.  Pieces:
+  // K split 0 of the first ready_first column blocks (word 0), split 0 of
+  // the others (word 1), then ready_gs splits per word.  An item's epilogue
+  // (the aqsm reads) waits for ready_m.
   const unsigned* ready = nullptr;
   unsigned epoch = 0;
-  int ready_cb = 1;
+  int ready_first = 0, ready_gs = 1;
+  const unsigned* ready_m = nullptr;
   int* ready_status = nullptr;
 };
+
+__host__ __device__ __forceinline__ int gate_word(const GppWork& w, int cb, int s) {
+  return s == 0 ? (cb < w.ready_first ? 0 : 1) : 2 + (s - 1) / w.ready_gs;
+}
 
 // Tile shapes.  Every pass uses kBN-band blocks (partial-sum layout of the
 // reduction); the column block width differs per precision.
@@ -93,8 +104,13 @@ __device__ __forceinline__ ItemCoord decode_item(const GppWork& w, int item) {
   ItemCoord c;
   c.bb = item % w.n_band_blocks;
   const int r = item / w.n_band_blocks;
-  c.s = r % w.n_splits;
-  c.cb = r / w.n_splits;
+  if (w.order_ks) {
+    c.cb = r % w.n_col_blocks;
+    c.s = r / w.n_col_blocks;
+  } else {
+    c.s = r % w.n_splits;
+    c.cb = r / w.n_splits;
+  }
   c.pidx = ((size_t)c.bb * w.n_col_blocks + c.cb) * w.n_splits + c.s;
   return c;
 }
