@@ -355,7 +355,8 @@ def run_ff_sigma(S, W, torch, dist, world, stream, sptr):
     inv, indinv = W.ff_index_maps(nc, ng)
     flops = 3 * 8.0 * nf * ng * nb * nc  # three contractions per step
     res = {"workload": f"FF sigma band loop: {nb} bands x {nf}x{ng} rows x {nc} g-vectors, "
-                       f"nfreqeval {ne}, nvband {nv}; 3 contractions + band algebra per step",
+                       f"nfreqeval {ne}, nvband {nv}; 3 contraction outputs (schDt, C_R, C_A) + band "
+                       f"algebra per step (the tensor form takes schDt and C_R from one pass)",
            "unit": "TFLOP/s (FP64-equivalent, contractions)"}
     outs = {}
     for mode, name, steps in ((1, "ozaki_bf16", 10), (0, "fp64", 1)):

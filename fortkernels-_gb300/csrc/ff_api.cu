@@ -244,10 +244,18 @@ namespace sigma {
 int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
                         const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
                         const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
-                        void* stream, const float2* epsr32, bool reuse_a) {
+                        void* stream, const float2* epsr32, bool reuse_a, const double* vcoul2,
+                        double vfac2, sigma_complex128* out2) {
   if (!plan) return SIGMA_ERR_NULL;
   if ((!I_epsR && !epsr32 && !reuse_a) || !aqsntemp || !aqsmtemp || !schDt_matrix) return SIGMA_ERR_NULL;
   if ((epsr32 || reuse_a) && plan->mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
+  if ((out2 != nullptr) != (vcoul2 != nullptr) || (out2 && vcoul)) return SIGMA_ERR_UNSUPPORTED;
+  if (out2 && plan->mode == SIGMA_FF_FP64) {
+    // the FP64 form contracts twice
+    const int r = ff_execute_weighted(plan, I_epsR, aqsntemp, aqsmtemp, nullptr, vfac, schDt_matrix, stream);
+    if (r != SIGMA_OK) return r;
+    return ff_execute_weighted(plan, I_epsR, aqsntemp, aqsmtemp, vcoul2, vfac * vfac2, out2, stream);
+  }
   int dev = 0;
   SIGMA_CUDA_TRY(cudaGetDevice(&dev));
   if (dev != plan->device) return SIGMA_ERR_UNSUPPORTED;
@@ -259,6 +267,10 @@ int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
   d.vcoul = vcoul;
   d.vfac = vfac;
   d.epsr32 = epsr32;
+  d.vcoul2 = vcoul2;
+  d.vfac2 = vfac2;
+  OzakiPrep oz = plan->oz;
+  oz.stab = vcoul2 ? oz.stab_buf : nullptr;
   cudaEvent_t* ev = nullptr;
   if (plan->timing && plan->recorded < kFfMaxTimed) ev = &plan->events[3 * plan->recorded++];
   SIGMA_CUDA_TRY(cudaMemsetAsync(plan->work.counter, 0, 2 * sizeof(int), s));
@@ -268,11 +280,12 @@ int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
     SIGMA_CUDA_TRY(launch_ff_reduce(d, plan->work, reinterpret_cast<double2*>(schDt_matrix), s));
   } else {
-    SIGMA_CUDA_TRY(launch_ozaki_prep(d, plan->oz, s, !reuse_a));
+    SIGMA_CUDA_TRY(launch_ozaki_prep(d, oz, s, !reuse_a));
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
-    SIGMA_CUDA_TRY(launch_ozaki_gemm(d, plan->work, plan->oz, plan->grid, s));
+    SIGMA_CUDA_TRY(launch_ozaki_gemm(d, plan->work, oz, plan->grid, s));
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
-    SIGMA_CUDA_TRY(launch_ozaki_reduce(d, plan->oz, reinterpret_cast<double2*>(schDt_matrix), s));
+    SIGMA_CUDA_TRY(launch_ozaki_reduce(d, oz, reinterpret_cast<double2*>(schDt_matrix), s,
+                                       reinterpret_cast<double2*>(out2)));
   }
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[2], s));
   return SIGMA_OK;

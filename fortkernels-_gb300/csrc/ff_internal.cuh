@@ -26,6 +26,10 @@ struct FfDev {
   // Optional FP32 operand [nf][ng][nc] used instead of epsr (the tensor-core
   // form rounds its operand to FP32 before slicing it)
   const float2* epsr32 = nullptr;
+  // Optional second output of the split-BF16 form: the same sum with the
+  // extra column factor vfac2 * vcoul2[igp]
+  const double* vcoul2 = nullptr;
+  double vfac2 = 1.0;
 };
 
 // Column weight of the contraction epilogue (0 for a column left out).

@@ -165,6 +165,7 @@ __global__ void __launch_bounds__(256) ozaki_weights_kernel(FfDev p, OzakiPrep o
       v = make_float2(__double2float_rn(md.x * wgt), __double2float_rn(md.y * wgt));
     }
     oz.wtab[t] = v;
+    if (oz.stab && n == 0) oz.stab[g] = igp >= 0 ? (float)(p.vfac2 * p.vcoul2[igp]) : 0.f;
   }
 }
 
@@ -201,7 +202,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
   // full[kStages], empty[kStages], accf[2], acce[2]
   __shared__ __align__(8) unsigned long long bars[2 * kStages + 4];
   __shared__ uint32_t tmem_slot;
-  __shared__ float2 s_red[4][kMaxSeg][kOzCols];
+  __shared__ float2 s_red[2][4][kMaxSeg][kOzCols];
 
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t sbase = (raw + 1023u) & ~1023u;
@@ -364,46 +365,55 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
           }
         }
       }
+      // one or two outputs: the second's rows carry the extra column factor stab
+      const bool two = oz.stab != nullptr;
+      const float sc = (two && row_ok) ? oz.stab[g] : 0.f;
       for (int seg = 0; seg <= f_last - f_first; ++seg) {
         const bool mine = row_ok && (f - f_first) == seg;
         // 16 bands at a time: a reduce-scatter butterfly over the warp leaves
         // lanes 2j and 2j+1 with the sum of band j of the batch
 #pragma unroll
         for (int b0 = 0; b0 < 64; b0 += 16) {
-          float xr[16], xi[16];
+#pragma unroll 1
+          for (int out = 0; out < 2; ++out) {
+            if (out == 1 && !two) break;
+            const float m = out == 0 ? 1.f : sc;
+            float xr[16], xi[16];
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            xr[i] = mine ? acc[b0 + i] : 0.f;
-            xi[i] = mine ? acc[64 + b0 + i] : 0.f;
-          }
-#pragma unroll
-          for (int o = 16, h = 8; o >= 2; o >>= 1, h >>= 1) {
-            const bool up = (lane & o) != 0;
-#pragma unroll
-            for (int i = 0; i < h; ++i) {
-              const float sr = up ? xr[i] : xr[i + h];
-              const float si = up ? xi[i] : xi[i + h];
-              const float rr = __shfl_xor_sync(0xffffffffu, sr, o);
-              const float ri = __shfl_xor_sync(0xffffffffu, si, o);
-              xr[i] = (up ? xr[i + h] : xr[i]) + rr;
-              xi[i] = (up ? xi[i + h] : xi[i]) + ri;
+            for (int i = 0; i < 16; ++i) {
+              xr[i] = mine ? acc[b0 + i] * m : 0.f;
+              xi[i] = mine ? acc[64 + b0 + i] * m : 0.f;
             }
+#pragma unroll
+            for (int o = 16, h = 8; o >= 2; o >>= 1, h >>= 1) {
+              const bool up = (lane & o) != 0;
+#pragma unroll
+              for (int i = 0; i < h; ++i) {
+                const float sr = up ? xr[i] : xr[i + h];
+                const float si = up ? xi[i] : xi[i + h];
+                const float rr = __shfl_xor_sync(0xffffffffu, sr, o);
+                const float ri = __shfl_xor_sync(0xffffffffu, si, o);
+                xr[i] = (up ? xr[i + h] : xr[i]) + rr;
+                xi[i] = (up ? xi[i + h] : xi[i]) + ri;
+              }
+            }
+            xr[0] += __shfl_xor_sync(0xffffffffu, xr[0], 1);
+            xi[0] += __shfl_xor_sync(0xffffffffu, xi[0], 1);
+            if ((lane & 1) == 0) s_red[out][warp][seg][b0 + (lane >> 1)] = make_float2(xr[0], xi[0]);
           }
-          xr[0] += __shfl_xor_sync(0xffffffffu, xr[0], 1);
-          xi[0] += __shfl_xor_sync(0xffffffffu, xi[0], 1);
-          if ((lane & 1) == 0) s_red[warp][seg][b0 + (lane >> 1)] = make_float2(xr[0], xi[0]);
         }
       }
       drain_barrier();
       const int nseg = f_last - f_first + 1;
-      for (int e = tid; e < nseg * kOzCols; e += kDrainThreads) {
-        const int seg = e / kOzCols, n = e % kOzCols;
+      for (int e = tid; e < (two ? 2 : 1) * nseg * kOzCols; e += kDrainThreads) {
+        const int out = e / (nseg * kOzCols), r = e % (nseg * kOzCols);
+        const int seg = r / kOzCols, n = r % kOzCols;
         double sr = 0.0, si = 0.0;
         for (int q = 0; q < 4; ++q) {
-          sr += (double)s_red[q][seg][n].x;
-          si += (double)s_red[q][seg][n].y;
+          sr += (double)s_red[out][q][seg][n].x;
+          si += (double)s_red[out][q][seg][n].y;
         }
-        oz.partial[(it.pidx * oz.max_seg + seg) * kOzCols + n] = make_double2(sr, si);
+        (out ? oz.partial2 : oz.partial)[(it.pidx * oz.max_seg + seg) * kOzCols + n] = make_double2(sr, si);
       }
       drain_barrier();
     }
@@ -416,7 +426,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
 
 // schDt[n1][ifreq]: one warp per entry, fixed-order compensated sum over the
 // row blocks that hold frequency ifreq and over their work entries.
-__global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, double2* schdt) {
+__global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, const double2* partial, double2* schdt) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= p.nb * p.nf) return;
@@ -430,7 +440,7 @@ __global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, double2* schdt) {
     const int seg = f - (rb * kOzRows) / p.ng;
     for (int j = (lane - q0 % 32 + 32) % 32; j < np; j += 32) {
       const size_t pidx = ((size_t)rb * oz.n_col_blocks + cb) * oz.max_pieces + j;
-      const double2 v = oz.partial[(pidx * oz.max_seg + seg) * kOzCols + c];
+      const double2 v = partial[(pidx * oz.max_seg + seg) * kOzCols + c];
       sx.add(v.x);
       sy.add(v.y);
     }
@@ -531,7 +541,7 @@ static size_t ozaki_wtab_bytes(const OzakiPrep& oz) {
 }
 
 size_t ozaki_partial_bytes(const OzakiPrep& oz) {
-  return ozaki_partial_only_bytes(oz) + ozaki_wtab_bytes(oz) +
+  return 2 * ozaki_partial_only_bytes(oz) + ozaki_wtab_bytes(oz) + up256(sizeof(float) * (size_t)oz.ng) +
          up256(sizeof(int4) * (size_t)std::max(oz.n_entries, 1)) +
          2 * up256(sizeof(int) * (size_t)oz.n_row_blocks) + 256;
 }
@@ -545,8 +555,13 @@ void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial) {
   uintptr_t pp = (reinterpret_cast<uintptr_t>(partial) + 255) & ~uintptr_t(255);
   oz.partial = reinterpret_cast<double2*>(pp);
   pp += ozaki_partial_only_bytes(oz);
+  oz.partial2 = reinterpret_cast<double2*>(pp);
+  pp += ozaki_partial_only_bytes(oz);
   oz.wtab = reinterpret_cast<float2*>(pp);
   pp += ozaki_wtab_bytes(oz);
+  oz.stab_buf = reinterpret_cast<float*>(pp);
+  oz.stab = nullptr;
+  pp += up256(sizeof(float) * (size_t)oz.ng);
   oz.entries = reinterpret_cast<const int4*>(pp);
   pp += up256(sizeof(int4) * (size_t)std::max(oz.n_entries, 1));
   oz.pieces = reinterpret_cast<const int*>(pp);
@@ -595,10 +610,14 @@ cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& 
   return cudaGetLastError();
 }
 
-cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s) {
+cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s,
+                                double2* schdt2) {
   const int warps = d.nb * d.nf;
   const int blocks = (warps * 32 + 255) / 256;
-  ozaki_reduce_kernel<<<blocks, 256, 0, s>>>(d, oz, schdt);
+  ozaki_reduce_kernel<<<blocks, 256, 0, s>>>(d, oz, oz.partial, schdt);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !schdt2) return e;
+  ozaki_reduce_kernel<<<blocks, 256, 0, s>>>(d, oz, oz.partial2, schdt2);
   return cudaGetLastError();
 }
 

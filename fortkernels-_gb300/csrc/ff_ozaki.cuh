@@ -41,6 +41,12 @@ struct OzakiPrep {
   // drain lane reads its row's 64 factors as contiguous 16-byte loads.
   float2* wtab;             // [ng][nb_pad]
   int ng, nb_pad;
+  // Optional second output (FfDev::vcoul2 set): the same contraction with
+  // the extra column factor stab[g] = vfac2 * vcoul2[igp(g)] in FP32, summed
+  // into partial2 by the same epilogue.  stab points at stab_buf then.
+  float* stab;
+  float* stab_buf;          // [ng]
+  double2* partial2;
 };
 
 // Work sizing and buffers of the split-BF16 form (partials + slices).
@@ -66,6 +72,7 @@ void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial);
 cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s, bool with_a = true);
 cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& oz, int grid,
                               cudaStream_t s);
-cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s);
+cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s,
+                                double2* schdt2 = nullptr);
 
 }  // namespace sigma

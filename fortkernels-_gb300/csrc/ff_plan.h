@@ -30,9 +30,15 @@ int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size
 // previous execution left in the plan's slice workspace (the same operand
 // again, no other plan on that workspace in between); I_epsR and epsr32 are
 // then not read.
+// With out2 and vcoul2 set (vcoul then NULL) the same contraction also
+// yields out2, the sum with the extra column factor vfac2 * vcoul2[igp]: one
+// tensor-core pass with a second epilogue reduction (the FP64 form
+// contracts twice).
 int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
                         const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
                         const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
-                        void* stream, const float2* epsr32 = nullptr, bool reuse_a = false);
+                        void* stream, const float2* epsr32 = nullptr, bool reuse_a = false,
+                        const double* vcoul2 = nullptr, double vfac2 = 1.0,
+                        sigma_complex128* out2 = nullptr);
 
 }  // namespace sigma

@@ -283,16 +283,20 @@ extern "C" int sigma_ff_sigma_execute(sigma_ff_sigma_plan p, const sigma_complex
     return SIGMA_ERR_NULL;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   auto C = [](double2* x) { return reinterpret_cast<sigma_complex128*>(x); };
-  int r = ff_execute_weighted(p->ff, I_epsR, aqsntemp, aqsmtemp, vcoul, 1.0, C(p->cr), stream);
+  // schDt (weight 1) and C_R (weight vcoul) are one contraction of I_epsR
+  // with two epilogue sums when schDt is not given
+  const double2* sd = reinterpret_cast<const double2*>(schDt_matrix);
+  int r;
+  if (!schDt_matrix) {
+    r = ff_execute_weighted(p->ff, I_epsR, aqsntemp, aqsmtemp, nullptr, 1.0, C(p->sd), stream,
+                            nullptr, false, vcoul, 1.0, C(p->cr));
+    sd = p->sd;
+  } else {
+    r = ff_execute_weighted(p->ff, I_epsR, aqsntemp, aqsmtemp, vcoul, 1.0, C(p->cr), stream);
+  }
   if (r != SIGMA_OK) return r;
   r = ff_execute_weighted(p->ff, I_epsA, aqsntemp, aqsmtemp, vcoul, 1.0, C(p->ca), stream);
   if (r != SIGMA_OK) return r;
-  const double2* sd = reinterpret_cast<const double2*>(schDt_matrix);
-  if (!schDt_matrix) {
-    r = ff_execute_weighted(p->ff, I_epsR, aqsntemp, aqsmtemp, nullptr, 1.0, C(p->sd), stream);
-    if (r != SIGMA_OK) return r;
-    sd = p->sd;
-  }
   FfSigmaArgs g;
   g.nb = p->nb;
   g.nvband = p->nvband;
