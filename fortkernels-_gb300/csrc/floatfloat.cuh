@@ -11,9 +11,9 @@ namespace sigma {
 // x = hi + lo: hi is x truncated to 24 significant bits (exact in FP32), lo
 // the remaining 29 bits rounded to FP32 (|x - hi - lo| <= 2^-48 |x|).  For
 // exponents where both are normal FP32 values, hi is assembled from the
-// bits and lo is one 32-bit integer conversion scaled by a power of two; no
-// instruction on the FP64 pipe (conversions from FP64 run there at the FP64
-// rate).
+// bits and lo is one 32-bit integer conversion scaled by a power of two: no
+// conversion from a 64-bit operand (with those, an FP32 kernel kept GB300's
+// FP64 pipe half busy).
 __device__ __forceinline__ void split_exact(double x, float& hi, float& lo) {
   const unsigned int whi = (unsigned int)__double2hiint(x), wlo = (unsigned int)__double2loint(x);
   const int ex = (int)((whi >> 20) & 0x7FFu);
