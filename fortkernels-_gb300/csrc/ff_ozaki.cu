@@ -43,6 +43,7 @@ using namespace tma;
 constexpr int kOzThreads = 224;
 constexpr int kDrainThreads = 128;
 constexpr int kTmaWarp = 4, kMmaWarp = 5, kGateWarp = 6;
+constexpr int kGateTiles = 2;  // tiles per release of the MMA warp
 constexpr int kChunksPerRow = kOzKTile / 8;                      // 16-byte chunks per tile row
 constexpr uint32_t kSliceBytes = 128 * kOzKTile * 2;             // 8 KB
 constexpr uint32_t kOperandBytes = 3 * kSliceBytes;              // 24 KB
@@ -253,8 +254,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
   } else if (warp == kGateWarp) {
     // ------------------------------------------------ release of the MMA warp
     // Waits for each tile's stage (and, at an accumulator lifetime's first
-    // tile, for the drain of that accumulator pair), then meets the MMA warp
-    // at a named barrier.  The issuing thread itself never polls shared
+    // tile, for the drain of that accumulator pair), and meets the MMA warp
+    // at a named barrier once per kGateTiles tiles.  The issuing thread itself never polls shared
     // memory: a poll between its MMAs stalls the tensor pipe (measured: 89
     // instead of 64 cycles per MMA).
     uint32_t ph_acce0 = 0, ph_acce1 = 0;
@@ -283,8 +284,10 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
           if (tb == 0) used0 = true; else used1 = true;
         }
         if (cs == kChunkStages - 1 || s == nst - 1) ++gc;
-        __syncwarp();
-        mma_gate_sync();
+        if (s % kGateTiles == kGateTiles - 1 || s == nst - 1) {
+          __syncwarp();
+          mma_gate_sync();
+        }
       }
     }
     // every accumulator pair in use drained
@@ -302,7 +305,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
       for (int s = 0; s < nst; ++s, ++g) {
         const int cs = s % kChunkStages;
         const uint32_t tb = gc & 1u;
-        mma_gate_sync();  // stage full, accumulator pair free
+        if (s % kGateTiles == 0) mma_gate_sync();  // stages full, accumulator pair free
         if (lane == 0) {
           tc_fence_after();
           const uint32_t b = g % kStages;
