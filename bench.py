@@ -285,6 +285,17 @@ def profile_traffic_per_term():
 FF_SHAPE = (512, 16384, 820, 15)  # number_bands, ncouls, ngpown, nfreq
 
 
+def bf16_peak():
+    """Dense BF16 peak for the tensor-core roofline: the measured cuBLAS burst
+    figure of this GPU pool (MEASURED_PEAKS.json beside this file), else the
+    stated fallback."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 burst; of measured)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback 1.9 PFLOP/s bf16 burst (no measured peak file; of fallback)"
+
+
 def run_ff(S, W, torch, dist, world, stream, sptr, args):
     """FF schDt contraction at its production shape: FP64 form and the
     split-BF16 tensor-core form, TF/s = 8 * (nfreq*ngpown) * number_bands *
@@ -321,6 +332,13 @@ def run_ff(S, W, torch, dist, world, stream, sptr, args):
         "normwise": float(np.linalg.norm(d) / np.linalg.norm(outs["fp64"])),
         "max_abs_over_max": float(np.abs(d).max() / np.abs(outs["fp64"]).max())}
     res["ozaki_bf16"]["tensor_tflops"] = round(6 * flops / (res["ozaki_bf16"]["kernel_ms_per_launch"] * 1e-3) / 1e12, 1)
+    peak, src = bf16_peak()
+    res["ozaki_bf16"]["roofline"] = {
+        "bound": "tensor", "kernel": "ozaki_gemm_kernel", "achieved": res["ozaki_bf16"]["tensor_tflops"],
+        "peak": peak, "unit": "TFLOP/s", "frac": round(res["ozaki_bf16"]["tensor_tflops"] / peak, 4),
+        "peak_source": src,
+        "note": "achieved = BF16 tensor work (6 slice products of the complex-as-real GEMM, 48 M N K flop) "
+                "over the GEMM launch's CUDA-event time; profiles/ozaki_gemm_ff_4096.md"}
     res["speedup_ozaki_vs_fp64"] = round(res["ozaki_bf16"]["value"] / res["fp64"]["value"], 1)
     del epsr, aqsn, aqsm
     torch.cuda.empty_cache()
