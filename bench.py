@@ -594,6 +594,19 @@ def run_ours(args, rank, world, local_rank):
         if rank == 0:
             print(json.dumps({"ff": res}), flush=True)
         return 0
+    if args.only_gpp_tensor:
+        import replicas
+        inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
+        tplan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_TENSOR)
+        _, terms = tplan.info()
+        for _ in range(args.warmup):
+            inst.run(tplan, sptr)
+        ms = timed(torch, dist, world, lambda: inst.run(tplan, sptr), args.steps, stream)
+        tplan.close()
+        if rank == 0:
+            print(json.dumps({"tensor": {"value": round(terms * world / (ms / args.steps * 1e-3) / 1e9, 4),
+                                         "unit": UNIT, "ms_per_step": round(ms / args.steps, 3)}}), flush=True)
+        return 0
     if args.only_halfsum:
         import replicas
         inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
@@ -817,6 +830,8 @@ def main():
     ap.add_argument("--no-static", action="store_true")
     ap.add_argument("--no-real", action="store_true")
     ap.add_argument("--no-halfsum", action="store_true")
+    ap.add_argument("--only-gpp-tensor", action="store_true",
+                    help="run the tensor-core GPP measurement alone (profiling captures)")
     ap.add_argument("--only-halfsum", action="store_true",
                     help="run the gppsum=1 half-sum measurement alone (profiling captures)")
     ap.add_argument("--halfsum-forms", default="sums,with_static,tensor",

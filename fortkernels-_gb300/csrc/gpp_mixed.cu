@@ -1158,14 +1158,23 @@ __device__ __forceinline__ void ssx_masked_item(const GppDev& p, const GppWork& 
     split_f(p.wx[iw], wxh[iw], wxl[iw]);
     iwx2[iw] = __double2float_rn(rcp_f64(p.wx[iw] * p.wx[iw]));
   }
-  float2 acc[kSsxBN][kNW], accl[kSsxBN][kNW];
+  // per (band, frequency): FP32 sums of kU = 2 terms folded into
+  // float-float sums (hi, lo)
+  float2 acc[kSsxBN][kNW], hi[kSsxBN][kNW], lo[kSsxBN][kNW];
 #pragma unroll
   for (int i = 0; i < kSsxBN; ++i)
 #pragma unroll
-    for (int iw = 0; iw < kNW; ++iw) {
-      acc[i][iw] = make_float2(0.f, 0.f);
-      accl[i][iw] = make_float2(0.f, 0.f);
-    }
+    for (int iw = 0; iw < kNW; ++iw) acc[i][iw] = hi[i][iw] = lo[i][iw] = make_float2(0.f, 0.f);
+  auto fold = [&]() {
+#pragma unroll
+    for (int i = 0; i < kSsxBN; ++i)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        ff_add(hi[i][iw].x, lo[i][iw].x, acc[i][iw].x);
+        ff_add(hi[i][iw].y, lo[i][iw].y, acc[i][iw].y);
+        acc[i][iw] = make_float2(0.f, 0.f);
+      }
+  };
 
   if (col_in) {
     const size_t cbase = (size_t)(my_igp / kBPM) * m.nc_pad * kBPM + (my_igp % kBPM);
@@ -1178,71 +1187,74 @@ __device__ __forceinline__ void ssx_masked_item(const GppDev& p, const GppWork& 
       const int n1 = min(n1_0 + i, band_end - 1);
       bands[i] = m.band + ((size_t)(n1 / kBN) * m.nc_pad) * kBN + (n1 % kBN);
     }
-#pragma unroll 4
-    for (int ig = ig_begin; ig < ig_end; ++ig) {
-      {
-        const float4 a = ca[(size_t)ig * kBPM];
-        const unsigned mask = __float_as_uint(a.w);
-        if ((mask & 0x3Fu) == 0u) continue;
-        const float2 g = cg[(size_t)ig * kBPM];
-        const float2 om = co[(size_t)ig * kBPM];
-        const float b = a.z;
-        const float omx = om.x, omy = om.y;
+    constexpr int kU = 2;  // g-vectors whose operands are loaded together
+    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kU) {
+      float4 a[kU];
+      float2 g[kU], om[kU], an[kU][kSsxBN];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const size_t ig = (size_t)min(ig0 + u, ig_end - 1);
+        a[u] = ca[ig * kBPM];
+        g[u] = cg[ig * kBPM];
+        om[u] = co[ig * kBPM];
+#pragma unroll
+        for (int i = 0; i < kSsxBN; ++i) an[u][i] = i < nbl ? bands[i][ig * kBN] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        // mask bits: keep (1 << iw), second branch (8 << iw); a tail g-vector past ig_end adds 0
+        const unsigned mask = ig0 + u < ig_end ? __float_as_uint(a[u].w) : 0u;
+        const float b = a[u].z;
         float2 sv[kNW];
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          const float zr = (wxh[iw] + a.x) + (wxl[iw] + a.y);
+          const float zr = (wxh[iw] + a[u].x) + (wxl[iw] + a[u].y);
           const float q = -0.5f * rcp_f32(fmaf(zr, zr, b * b));
-          const float2 s2 = make_float2(fmaf(g.x, zr, g.y * b) * q, fmaf(g.y, zr, -g.x * b) * q);
-          const float2 s1 = make_float2(omx * iwx2[iw], omy * iwx2[iw]);
+          const float2 s2 = make_float2(fmaf(g[u].x, zr, g[u].y * b) * q, fmaf(g[u].y, zr, -g[u].x * b) * q);
+          const float2 s1 = make_float2(om[u].x * iwx2[iw], om[u].y * iwx2[iw]);
           sv[iw] = (mask & (1u << iw)) ? s1 : ((mask & (8u << iw)) ? s2 : make_float2(0.f, 0.f));
         }
+        // each product formed before it is added: one rounding of the pair sum
 #pragma unroll
-        for (int i = 0; i < kSsxBN; ++i) {
-          if (i < nbl) {
-            const float2 an = bands[i][(size_t)ig * kBN];
+        for (int i = 0; i < kSsxBN; ++i)
 #pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) {
-              const float tx = fmaf(an.x, sv[iw].x, -an.y * sv[iw].y);
-              const float ty = fmaf(an.x, sv[iw].y, an.y * sv[iw].x);
-              float t, e;
-              two_sum_f(acc[i][iw].x, tx, t, e);
-              acc[i][iw].x = t;
-              accl[i][iw].x += e;
-              two_sum_f(acc[i][iw].y, ty, t, e);
-              acc[i][iw].y = t;
-              accl[i][iw].y += e;
-            }
+          for (int iw = 0; iw < kNW; ++iw) {
+            acc[i][iw].x += fmaf(an[u][i].x, sv[iw].x, -an[u][i].y * sv[iw].y);
+            acc[i][iw].y += fmaf(an[u][i].x, sv[iw].y, an[u][i].y * sv[iw].x);
           }
-        }
       }
+      fold();  // runs of kU terms
     }
   }
 
+  // epilogue: x conj(aqsm[n1][igp]) occ vcoul[igp] in float-float, warp sums
+  // in float-float, block sum in FP64 with compensation
   const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
   const int lane = tid & 31, warp = tid >> 5;
   __syncthreads();  // the previous item's epilogue is done with sh.red
 #pragma unroll
-  for (int i = 0; i < kSsxBN; ++i)
+  for (int i = 0; i < kSsxBN; ++i) {
+    FF fr{0.f, 0.f}, fi{0.f, 0.f};  // conj(aqsm) occ vcoul
+    if (i < nbl && igp >= 0) {
+      const double2 am = p.aqsm[(size_t)(n1_0 + i) * p.nc + igp];
+      const FF f = ff_of(p.occ * p.vcoul[igp]);
+      fr = ff_mul(ff_of(am.x), f);
+      fi = ff_neg(ff_mul(ff_of(am.y), f));
+    }
 #pragma unroll
     for (int iw = 0; iw < kNW; ++iw) {
-      double2 v = make_double2(0.0, 0.0);
-      if (i < nbl && igp >= 0) {
-        const double2 am = p.aqsm[(size_t)(n1_0 + i) * p.nc + igp];
-        const double f = p.occ * p.vcoul[igp];
-        const double2 sum = make_double2((double)acc[i][iw].x + (double)accl[i][iw].x,
-                                         (double)acc[i][iw].y + (double)accl[i][iw].y);
-        v = cmul(sum, make_double2(am.x, -am.y));
-        v.x *= f;
-        v.y *= f;
-      }
+      const FF sx{hi[i][iw].x, lo[i][iw].x}, sy{hi[i][iw].y, lo[i][iw].y};
+      FF vx = ff_add(ff_mul(sx, fr), ff_neg(ff_mul(sy, fi)));
+      FF vy = ff_add(ff_mul(sx, fi), ff_mul(sy, fr));
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        vx = ff_add(vx, FF{__shfl_xor_sync(0xffffffffu, vx.hi, o), __shfl_xor_sync(0xffffffffu, vx.lo, o)});
+        vy = ff_add(vy, FF{__shfl_xor_sync(0xffffffffu, vy.hi, o), __shfl_xor_sync(0xffffffffu, vy.lo, o)});
       }
-      if (lane == 0) sh.red[i][iw][warp] = v;
+      if (lane == 0)
+        sh.red[i][iw][warp] = make_double2((double)vx.hi + (double)vx.lo, (double)vy.hi + (double)vy.lo);
     }
+  }
   __syncthreads();
   if (tid < kSsxBN * kNW) {
     const int i = tid / kNW, iw = tid % kNW;
