@@ -373,7 +373,7 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (tensor) {
     // factors, and the occupied-band operands from the same pass
     float2* y32 = reinterpret_cast<float2*>(plan->yfac);
-    SIGMA_CUDA_TRY(launch_tensor_factors(p, y32, plan->prepw,
+    SIGMA_CUDA_TRY(launch_tensor_factors(p, y32, occupied_bands(plan->prepw, p.nvband),
                                          plan->ssx.n_items > 0 ? &plan->prep : nullptr, s));
     const int st = ff_execute_weighted(plan->ff, nullptr, aqsntemp, aqsmtemp, vcoul, 0.5,
                                        reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream, y32);

@@ -363,7 +363,7 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
     for (int i = 0; i < b->n; ++i) {
       // factors, and the occupied-band operands from the same pass
       float2* y32 = reinterpret_cast<float2*>(b->yfac);
-      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], y32, b->prepw[i],
+      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], y32, occupied_bands(b->prepw[i], b->dev[i].nvband),
                                            b->ssx[i].n_items > 0 ? &b->prep[i] : nullptr, s));
       const int st = ff_execute_weighted(b->ff[i], nullptr, b->inst[i].aqsntemp, b->inst[i].aqsmtemp,
                                          b->inst[i].vcoul, 0.5,

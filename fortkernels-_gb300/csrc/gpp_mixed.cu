@@ -255,6 +255,7 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
     const int cb = (int)(t / (m.nc_pad / 32));
     const int ig0 = (int)(t % (m.nc_pad / 32)) * 32;
     __syncthreads();
+#pragma unroll 2
     for (int e = tid; e < 32 * kBPM; e += 256) {
       const int pl = e / 32, k = e % 32;  // reads and factor writes run along g-vectors
       const int my_igp = cb * kBPM + pl, ig = ig0 + k;

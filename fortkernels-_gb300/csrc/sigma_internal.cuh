@@ -92,6 +92,14 @@ constexpr int kBPY = 32;   // columns per FP64 item when the frequencies are sha
 constexpr int kSsxBN = 4;   // bands per occupied-band item
 constexpr int kSsxBP = 256; // columns per occupied-band item, one per thread
 
+// The pre-pass work of the tensor form: only the occupied bands' FP32 rows
+// are read (by the occupied-band pass); the band sums run on the tensor cores.
+inline GppWork occupied_bands(GppWork w, int nvband) {
+  w.band_count = w.band_begin < nvband ? nvband - w.band_begin : 0;
+  w.n_band_blocks = (w.band_count + kBN - 1) / kBN;
+  return w;
+}
+
 // Item -> (band block, column block, g-vector split).  Band blocks vary
 // fastest so that CTAs running at the same time share column data in L2.
 // pidx is the item's slot in the partial-sum array, ordered
