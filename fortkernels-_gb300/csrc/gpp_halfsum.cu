@@ -450,7 +450,6 @@ __global__ void __launch_bounds__(kThreads) half_occ_ff_kernel(HalfDev p, const 
   const int igp = p.igp_of[col];
   const double wxd = p.wx[iw];
   const FF wx = ff_of(wxd);
-  const FF wx2 = ff_mul(wx, wx);
   const double to2 = kTo1 * kTo1;
   const FF to2f = ff_of(to2);
   const int kend = igp >= 0 ? min(igp, p.brk[col]) : 0;
@@ -502,33 +501,29 @@ __global__ void __launch_bounds__(kThreads) half_occ_ff_kernel(HalfDev p, const 
         const double b2d = guard_b2(wt.y);
         zero = gt_nonneg(guard_thr(wt.x, b2d), guard_w(wxd, wt.x, b2d));
       }
+      // d = wx + wtilde = (wx + a, b), in both branches
+      const FF dr = ff_add(wx, a);
+      const FF rd = ff_rcp(ff_add(ff_mul(dr, dr), b2));  // 1 / |d|^2
       float2 sch = make_float2(0.f, 0.f), ssx = make_float2(0.f, 0.f);
       if (!zero) {
-        // sch = G (c + i b) / wv
+        // sch = G (c + i b) / wv = G / (wx - wtilde)
         const FF r = ff_rcp(wv);
         const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
-        sch = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
-                          ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
-        // ssx = Omega2 conj(D) / |D|^2, Omega2 = wtilde^2 I_eps, D = wx^2 - wtilde^2
-        const FF w2x = ff_add(ff_mul(a, a), ff_neg(b2));
-        const FF ab = ff_mul(a, b);
-        const FF w2y{2.f * ab.hi, 2.f * ab.lo};
-        const FF omx = ff_add(ff_mul(w2x, er), ff_neg(ff_mul(w2y, ei)));
-        const FF omy = ff_add(ff_mul(w2x, ei), ff_mul(w2y, er));
-        const FF dx = ff_add(wx2, ff_neg(w2x));
-        const FF rd = ff_rcp(ff_add(ff_mul(dx, dx), ff_mul(w2y, w2y)));
-        // D = (dx, -w2y): Omega2 conj(D) = (omx dx - omy w2y, omy dx + omx w2y)
-        ssx = make_float2(ff_round(ff_mul(ff_add(ff_mul(omx, dx), ff_neg(ff_mul(omy, w2y))), rd)),
-                          ff_round(ff_mul(ff_add(ff_mul(omy, dx), ff_mul(omx, w2y)), rd)));
+        const FF sx = ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)));
+        const FF sy = ff_add(ff_mul(gx, zi), ff_mul(gy, zr));
+        sch = make_float2(ff_round(sx), ff_round(sy));
+        // ssx = Omega2 / (wx^2 - wtilde^2) = sch wtilde / (wx + wtilde),
+        // wtilde conj(d) = (a (wx + a) + b^2, b wx)
+        const FF qr = ff_mul(ff_add(ff_mul(a, dr), b2), rd), qi = ff_mul(ff_mul(b, wx), rd);
+        ssx = make_float2(ff_round(ff_add(ff_mul(sx, qr), ff_neg(ff_mul(sy, qi)))),
+                          ff_round(ff_add(ff_mul(sx, qi), ff_mul(sy, qr))));
       } else {
         bool n3;
         bool big = ff_gt(s2, to2f, n3);  // |wtilde|^2 > to1^2
         if (n3) big = fma(wt.x, wt.x, guard_b2(wt.y)) > to2;
         if (big) {
-          // -G / (2 (wx + wtilde)) = -0.5 G conj(d) / |d|^2, d = (wx + a, b)
-          const FF dr = ff_add(wx, a);
-          const FF r = ff_rcp(ff_add(ff_mul(dr, dr), b2));
-          const FF hr{-0.5f * r.hi, -0.5f * r.lo};
+          // -G / (2 (wx + wtilde)) = -0.5 G conj(d) / |d|^2
+          const FF hr{-0.5f * rd.hi, -0.5f * rd.lo};
           ssx = make_float2(ff_round(ff_mul(ff_add(ff_mul(gx, dr), ff_mul(gy, b)), hr)),
                             ff_round(ff_mul(ff_add(ff_mul(gy, dr), ff_neg(ff_mul(gx, b))), hr)));
         }
