@@ -45,9 +45,12 @@ extern "C" {
 /* ---------------------------------------------------------------------------
  * Host-pointer drop-in.  Takes the arrays gppKer.cpp builds in main()
  * (BGW-Kernels/gppKer.cpp:222-299) and replaces its loop nest :303-439 with
- * one call.  The library copies the inputs into its cached device buffers on
- * `stream` (NULL: the legacy default stream), runs the kernels and copies
- * the outputs back; it returns after the stream has drained.  indinv has
+ * one call.  The library copies the inputs into its cached device buffers,
+ * runs the kernels on `stream` (NULL: the legacy default stream) and copies
+ * the outputs back; it returns after the stream has drained.  The FP64 form
+ * copies on an internal stream ordered after the work already queued on
+ * `stream`, in pieces that the sum waits for one by one, so the copies
+ * overlap the sum; the other forms copy on `stream` first.  indinv has
  * ncouls entries, as in the reference; wx_array has 3 entries shared by every
  * band.  Host buffers in pinned memory copy fastest.
  * ------------------------------------------------------------------------- */
