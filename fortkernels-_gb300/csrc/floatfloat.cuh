@@ -65,6 +65,11 @@ __device__ __forceinline__ FF ff_rcp(FF x) {
   return ff_norm(r0, r0 * e);
 }
 __device__ __forceinline__ float ff_round(FF x) { return x.hi + x.lo; }
+// x y rounded once to FP32: the cross terms in one FMA, the final FMA exact
+// before its rounding, so the result is within 1/2 ulp + 2^-47 |xy| of xy
+__device__ __forceinline__ float ff_mul_round(FF x, FF y) {
+  return fmaf(x.hi, y.hi, fmaf(x.hi, y.lo, x.lo * y.hi));
+}
 // x > y for non-negative float-float values, with `near` set when they are
 // within 2^-30 (relative) of each other
 __device__ __forceinline__ bool ff_gt(FF x, FF y, bool& near) {

@@ -726,6 +726,8 @@ __global__ void __launch_bounds__(256) half_z32_kernel(HalfDev p, float2* z) {
       const FF s2 = ff_add(ff_mul(a, a), b2);
       const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));
       const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
+      // G (c + i b) = wx G - G conj(wtilde) = wx G - |wtilde|^2 I_eps
+      const FF sex = ff_mul(s2, er), sey = ff_mul(s2, ei);
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
         const FF c = ff_add(wx[f], ff_neg(a));
@@ -741,9 +743,8 @@ __global__ void __launch_bounds__(256) half_z32_kernel(HalfDev p, float2* z) {
         }
         if (keep) {
           const FF r = ff_rcp(wv);
-          const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
-          v[f] = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
-                             ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
+          v[f] = make_float2(ff_mul_round(ff_add(ff_mul(wx[f], gx), ff_neg(sex)), r),
+                             ff_mul_round(ff_add(ff_mul(wx[f], gy), ff_neg(sey)), r));
         }
       }
     }

@@ -271,6 +271,8 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
         const FF b2 = ff_mul(b, b);
         const FF s2 = ff_add(ff_mul(a, a), b2);            // |wtilde|^2
         const FF s_big = ff_mul(s2, FF{1e6f, 0.f});        // |wtilde|^2 / to1 (1e6 exact)
+        // G (c + i b) = wx G - G conj(wtilde) = wx G - |wtilde|^2 I_eps
+        const FF sex = ff_mul(s2, er), sey = ff_mul(s2, ei);
         unsigned mask = 0u;
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
@@ -290,9 +292,8 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
             float2 yv = make_float2(0.f, 0.f);
             if (keep) {
               const FF r = ff_rcp(wv);
-              const FF zr = ff_mul(c, r), zi = ff_mul(b, r);
-              yv = make_float2(ff_round(ff_add(ff_mul(gx, zr), ff_neg(ff_mul(gy, zi)))),
-                               ff_round(ff_add(ff_mul(gx, zi), ff_mul(gy, zr))));
+              yv = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
+                               ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
             }
             y[(size_t)iw * plane + off] = yv;
           }
