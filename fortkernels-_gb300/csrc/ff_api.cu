@@ -208,6 +208,10 @@ extern "C" int sigma_ff_plan_timing(sigma_ff_plan plan, int* executions, double*
 }
 
 namespace sigma {
+const OzakiPrep* ff_plan_ozaki(sigma_ff_plan plan) {
+  return plan && plan->mode == SIGMA_FF_OZAKI_BF16 ? &plan->oz : nullptr;
+}
+
 int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes) {
   FfDev d{};
   d.nb = number_bands;

@@ -45,8 +45,8 @@ constexpr int kDrainThreads = 128;
 constexpr int kTmaWarp = 4, kMmaWarp = 5, kGateWarp = 6;
 constexpr int kGateTiles = 2;  // tiles per release of the MMA warp
 constexpr int kChunksPerRow = kOzKTile / 8;                      // 16-byte chunks per tile row
-constexpr uint32_t kSliceBytes = 128 * kOzKTile * 2;             // 8 KB
-constexpr uint32_t kOperandBytes = 3 * kSliceBytes;              // 24 KB
+constexpr uint32_t kSliceBytes = kOzSliceBytes;                  // 8 KB
+constexpr uint32_t kOperandBytes = kOzOperandBytes;              // 24 KB
 constexpr uint32_t kStageBytes = 2 * kOperandBytes;              // 48 KB
 constexpr int kStages = 4;
 constexpr uint32_t kSmemBytes = kStages * kStageBytes + 2048;    // + alignment slack and 1 KB past the ring
@@ -55,37 +55,6 @@ constexpr int kChunkStages = 4;                         // K tiles per accumulat
 constexpr int kMaxSeg = 8;                              // frequencies per row block (host checks)
 constexpr uint32_t kIdesc = idesc_bf16_f32(128, 128);
 
-__device__ __forceinline__ void split3(float x, unsigned short& a, unsigned short& b,
-                                       unsigned short& c) {
-  const __nv_bfloat16 s1 = __float2bfloat16_rn(x);
-  const float t1 = x - __bfloat162float(s1);
-  const __nv_bfloat16 s2 = __float2bfloat16_rn(t1);
-  const float t2 = t1 - __bfloat162float(s2);
-  const __nv_bfloat16 s3 = __float2bfloat16_rn(t2);
-  a = __bfloat16_as_ushort(s1);
-  b = __bfloat16_as_ushort(s2);
-  c = __bfloat16_as_ushort(s3);
-}
-
-// Slices of 8 consecutive K values of one row, written as three 16-byte
-// chunks (one per slice tile) of a 24 KB block.
-__device__ __forceinline__ void put_row_chunk(unsigned char* blk, int r, int ch, const float (&v)[8]) {
-  unsigned short sl[3][8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) split3(v[j], sl[0][j], sl[1][j], sl[2][j]);
-#pragma unroll
-  for (int s = 0; s < 3; ++s) {
-    uint4 q;
-    q.x = sl[s][0] | ((uint32_t)sl[s][1] << 16);
-    q.y = sl[s][2] | ((uint32_t)sl[s][3] << 16);
-    q.z = sl[s][4] | ((uint32_t)sl[s][5] << 16);
-    q.w = sl[s][6] | ((uint32_t)sl[s][7] << 16);
-    *reinterpret_cast<uint4*>(blk + s * kSliceBytes + sw64_offset(r, ch * 8)) = q;
-  }
-}
-
-// A' = [Re | Im] of I_epsR rows.  Thread = (row block, K tile, row, 8-K chunk);
-// it writes the real-part tile kt and the imaginary-part tile kt + oz.kt.
 __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz) {
   const long long total = (long long)oz.n_row_blocks * oz.kt * 128 * kChunksPerRow;
   const int rows = p.nf * p.ng;
@@ -116,8 +85,8 @@ __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz
       im[j] = v.y;
     }
     unsigned char* base = oz.a_tiles + (size_t)rb * 2 * oz.kt * kOperandBytes;
-    put_row_chunk(base + (size_t)kt * kOperandBytes, r, ch, re);
-    put_row_chunk(base + (size_t)(oz.kt + kt) * kOperandBytes, r, ch, im);
+    oz_put_row_chunk(base + (size_t)kt * kOperandBytes, r, ch, re);
+    oz_put_row_chunk(base + (size_t)(oz.kt + kt) * kOperandBytes, r, ch, im);
   }
 }
 
@@ -145,10 +114,10 @@ __global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz
     unsigned char* base = oz.b_tiles + (size_t)cb * 2 * oz.kt * kOperandBytes;
     unsigned char* lo = base + (size_t)kt * kOperandBytes;            // K' < K: real parts of aqsn
     unsigned char* hi = base + (size_t)(oz.kt + kt) * kOperandBytes;  // K' >= K: imaginary parts
-    put_row_chunk(lo, nl, ch, re);
-    put_row_chunk(lo, 64 + nl, ch, im);
-    put_row_chunk(hi, nl, ch, nim);
-    put_row_chunk(hi, 64 + nl, ch, re);
+    oz_put_row_chunk(lo, nl, ch, re);
+    oz_put_row_chunk(lo, 64 + nl, ch, im);
+    oz_put_row_chunk(hi, nl, ch, nim);
+    oz_put_row_chunk(hi, 64 + nl, ch, re);
   }
 }
 
@@ -631,6 +600,32 @@ cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t 
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   ozaki_weights_kernel<<<152 * 2, 256, 0, s>>>(d, oz);
+  return cudaGetLastError();
+}
+
+namespace {
+// Zero slices of the A rows in [rows, n_row_blocks * 128) for the K tiles the
+// contraction reads (rows a producer of A rows does not write).
+__global__ void __launch_bounds__(256) ozaki_zero_rows_kernel(OzakiPrep oz, int rows) {
+  const int last = oz.n_row_blocks - 1;
+  const int r0 = rows - last * kOzRows;
+  if (r0 >= kOzRows) return;
+  const long long total = (long long)(kOzRows - r0) * oz.kt * kChunksPerRow;
+  const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int ch = (int)(t % kChunksPerRow);
+    const int kt = (int)((t / kChunksPerRow) % oz.kt);
+    const int r = r0 + (int)(t / ((long long)kChunksPerRow * oz.kt));
+    if (kt >= oz.kt_lim[last]) continue;
+    oz_put_a(oz, last * kOzRows + r, kt * kOzKTile + ch * 8, z, z);
+  }
+}
+}  // namespace
+
+cudaError_t launch_ozaki_zero_rows(const OzakiPrep& oz, int rows, cudaStream_t s) {
+  if (rows >= oz.n_row_blocks * kOzRows) return cudaSuccess;
+  ozaki_zero_rows_kernel<<<152, 256, 0, s>>>(oz, rows);
   return cudaGetLastError();
 }
 

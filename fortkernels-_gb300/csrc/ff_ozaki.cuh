@@ -3,7 +3,10 @@
 
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "ff_internal.cuh"
+#include "sigma_tma.cuh"
 
 namespace sigma {
 
@@ -49,6 +52,45 @@ struct OzakiPrep {
   double2* partial2;
 };
 
+constexpr uint32_t kOzSliceBytes = 128 * kOzKTile * 2;  // one BF16 slice of a 128-row K tile, 8 KB
+constexpr uint32_t kOzOperandBytes = 3 * kOzSliceBytes;  // the three slices, 24 KB
+
+// x = s1 + s2 + s3 exactly, each a BF16 value (8 significant bits).
+__device__ __forceinline__ void oz_split3(float x, unsigned short& a, unsigned short& b,
+                                          unsigned short& c) {
+  const __nv_bfloat16 s1 = __float2bfloat16_rn(x);
+  const float t1 = x - __bfloat162float(s1);
+  const __nv_bfloat16 s2 = __float2bfloat16_rn(t1);
+  const float t2 = t1 - __bfloat162float(s2);
+  const __nv_bfloat16 s3 = __float2bfloat16_rn(t2);
+  a = __bfloat16_as_ushort(s1);
+  b = __bfloat16_as_ushort(s2);
+  c = __bfloat16_as_ushort(s3);
+}
+
+// Slices of 8 consecutive K values of one row, written as three 16-byte
+// chunks (one per slice tile) of a 24 KB block.
+__device__ __forceinline__ void oz_put_row_chunk(unsigned char* blk, int r, int ch, const float (&v)[8]) {
+  unsigned short sl[3][8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) oz_split3(v[j], sl[0][j], sl[1][j], sl[2][j]);
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    uint4 q;
+    q.x = sl[s][0] | ((uint32_t)sl[s][1] << 16);
+    q.y = sl[s][2] | ((uint32_t)sl[s][3] << 16);
+    q.z = sl[s][4] | ((uint32_t)sl[s][5] << 16);
+    q.w = sl[s][6] | ((uint32_t)sl[s][7] << 16);
+    *reinterpret_cast<uint4*>(blk + s * kOzSliceBytes + tma::sw64_offset(r, ch * 8)) = q;
+  }
+}
+
+// The slices of A'[R][k0 .. k0+8): real parts re (K' = k) and imaginary
+// parts im (K' = ncouls_padded + k); k0 a multiple of 8.  A producer of FP32
+// A rows writes these instead of the operand the slicing pre-pass reads.
+__device__ __forceinline__ void oz_put_a(const OzakiPrep& oz, int R, int k0, const float (&re)[8],
+                                         const float (&im)[8]);
+
 // Work sizing and buffers of the split-BF16 form (partials + slices).
 // row_kend (nullable, [nfreq * ngpown]): the A row's entries at K >= row_kend
 // are zero, so the tiles past its row block's largest value are skipped.
@@ -70,9 +112,20 @@ void ozaki_prep_bind(OzakiPrep& oz, void* base);
 void ozaki_bind(OzakiPrep& oz, void* tiles, void* partial);
 // with_a = false keeps the A slices already in the workspace
 cudaError_t launch_ozaki_prep(const FfDev& d, const OzakiPrep& oz, cudaStream_t s, bool with_a = true);
+// Zero slices of A rows [rows, n_row_blocks * 128): the rows past nf * ngpown
+// that a producer of A rows leaves unwritten.
+cudaError_t launch_ozaki_zero_rows(const OzakiPrep& oz, int rows, cudaStream_t s);
 cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& oz, int grid,
                               cudaStream_t s);
 cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s,
                                 double2* schdt2 = nullptr);
+
+__device__ __forceinline__ void oz_put_a(const OzakiPrep& oz, int R, int k0, const float (&re)[8],
+                                         const float (&im)[8]) {
+  const int rb = R / kOzRows, r = R % kOzRows, kt = k0 / kOzKTile, ch = (k0 % kOzKTile) / 8;
+  unsigned char* base = oz.a_tiles + (size_t)rb * 2 * oz.kt * kOzOperandBytes;
+  oz_put_row_chunk(base + (size_t)kt * kOzOperandBytes, r, ch, re);
+  oz_put_row_chunk(base + (size_t)(oz.kt + kt) * kOzOperandBytes, r, ch, im);
+}
 
 }  // namespace sigma

@@ -22,6 +22,12 @@ int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, 
                   const int* row_kend = nullptr);
 int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes);
 
+// The split-BF16 plan's operand layout (slice images, K tiles, row limits),
+// for kernels that write the A slices themselves and then execute with
+// reuse_a; nullptr for an FP64 plan.
+struct OzakiPrep;
+const OzakiPrep* ff_plan_ozaki(sigma_ff_plan plan);
+
 // sigma_ff_execute with the column weight vfac * vcoul[igp] (vcoul a device
 // array, or nullptr for weight 1).
 // With epsr32 set (split-BF16 form only) the contraction reads that FP32

@@ -7,6 +7,7 @@
 #include "sigma_gpp.h"
 #include "sigma_internal.cuh"
 #include "ff_plan.h"
+#include "ff_ozaki.cuh"
 #include "runtime.h"
 
 namespace sigma {
@@ -26,7 +27,7 @@ struct sigma_gpp_plan_s {
   sigma::GppWork schmy{};     // mixed main pass for shared frequencies (shares sch's buffers)
   sigma::GppWork prepw{};     // pre-pass blocks: sch's, rounded up to even counts
   sigma_ff_plan ff = nullptr; // tensor form: the contraction plan (3 slabs = 3 frequencies)
-  double2* yfac = nullptr;    // tensor form: frequency factors Y[3][ng][nc] (FP32 complex)
+
   sigma::MixedPrep prep{};    // FP32 operands of the mixed path (unused for FP64)
   void* block = nullptr;      // one device allocation for everything below
   int* igp_of = nullptr;      // [ng]
@@ -190,7 +191,6 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   const size_t b_colB = align_up(sizeof(float2) * col_elems, 256);
   const size_t b_band = align_up(sizeof(float2) * band_elems, 256);
   const size_t b_colC = nvband > 0 ? b_colB : 0;
-  const size_t b_y = tensor ? align_up(sizeof(float2) * 3 * (size_t)ngpown * ncouls, 256) : 0;
   if (tensor) {
     int st2 = ff_plan_build(&p->ff, number_bands, ncouls, ngpown, kNW, igp_of, SIGMA_FF_OZAKI_BF16);
     if (st2 != SIGMA_OK) {
@@ -199,7 +199,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
     }
   }
   cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx + b_colA + b_colB + b_band +
-                                            b_colC + b_y);
+                                            b_colC);
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_last_cuda_error(e, "cudaMalloc(plan)", __LINE__);
@@ -225,7 +225,6 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
     p->prep.colB = mixed ? reinterpret_cast<float2*>(q + b_colA) : nullptr;
     p->prep.band = mixed ? reinterpret_cast<float2*>(q + b_colA + b_colB) : nullptr;
     p->prep.colC = mixed && nvband > 0 ? reinterpret_cast<float2*>(q + b_colA + b_colB + b_band) : nullptr;
-    p->yfac = tensor ? reinterpret_cast<double2*>(q + b_colA + b_colB + b_band + b_colC) : nullptr;
     p->prep.nc_pad = nc_pad;
     p->prep.status = p->counters + 2;
   }
@@ -299,10 +298,13 @@ extern "C" int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, doubl
   if (launches_per_execution) {
     const bool mixed = plan->precision == SIGMA_PREC_MIXED;
     if (plan->precision == SIGMA_PREC_TENSOR) {
-      // factors (+ band operands with occupied bands), slicing and epilogue
-      // factors (3), GEMM, its reduction; the occupied-band pass; 2 reductions
+      // factors written as A slices (+ band operands with occupied bands),
+      // zeroed padding rows, B slices and epilogue factors (2), GEMM, its
+      // reduction; the occupied-band pass; 2 reductions
       const bool occ = plan->ssx.n_items > 0;
-      *launches_per_execution = (occ ? 2 : 1) + 3 + 2 + (occ ? 1 : 0) + 2;
+      const sigma::OzakiPrep* oz = sigma::ff_plan_ozaki(plan->ff);
+      const int pad = oz && oz->n_row_blocks * sigma::kOzRows > sigma::kNW * plan->ng ? 1 : 0;
+      *launches_per_execution = (occ ? 2 : 1) + pad + 2 + 2 + (occ ? 1 : 0) + 2;
     } else
       *launches_per_execution = (plan->sch.n_items > 0 ? (mixed ? 3 : 1) : 0) +
                                 (plan->ssx.n_items > 0 ? 1 : 0) + 2;
@@ -372,11 +374,13 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
   if (tensor) {
     // factors, and the occupied-band operands from the same pass
-    float2* y32 = reinterpret_cast<float2*>(plan->yfac);
-    SIGMA_CUDA_TRY(launch_tensor_factors(p, y32, occupied_bands(plan->prepw, p.nvband),
-                                         plan->ssx.n_items > 0 ? &plan->prep : nullptr, s));
+    // the factors land directly as the contraction's A slices
+    SIGMA_CUDA_TRY(launch_tensor_factors(p, nullptr, occupied_bands(plan->prepw, p.nvband),
+                                         plan->ssx.n_items > 0 ? &plan->prep : nullptr, s,
+                                         ff_plan_ozaki(plan->ff)));
     const int st = ff_execute_weighted(plan->ff, nullptr, aqsntemp, aqsmtemp, vcoul, 0.5,
-                                       reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream, y32);
+                                       reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream, nullptr,
+                                       true);
     if (st != SIGMA_OK) return st;
   } else if (ypath)
     SIGMA_CUDA_TRY(launch_sch_fp64y(p, plan->schy, plan->schy_grid, s));

@@ -21,6 +21,7 @@
 #include "sigma_internal.cuh"
 #include "gpp_batch.cuh"
 #include "ff_plan.h"
+#include "ff_ozaki.cuh"
 #include "runtime.h"
 
 namespace sigma {
@@ -48,7 +49,6 @@ struct sigma_gpp_batch_s {
   // tensor form
   std::vector<sigma_ff_plan> ff;   // per instance (3 slabs, GPP column map)
   void* tensor_ws = nullptr;       // shared: factors Y[3][ng][nc] then the slice images
-  double2* yfac = nullptr;
   void* tiles = nullptr;
 };
 
@@ -305,9 +305,8 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   b->launches = (mixed ? 2 * n_instances : 0) + 1 + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
   if (tensor) {
     // one factor buffer and one slice workspace, each sized for the largest instance
-    size_t ybytes = 0, tbytes = 0;
+    size_t tbytes = 0;  // one slice workspace, sized for the largest instance
     for (int i = 0; i < n_instances; ++i) {
-      ybytes = std::max(ybytes, sizeof(float2) * 3 * (size_t)inst[i].ngpown * inst[i].ncouls);
       size_t tb = 0;
       int st = ff_plan_tile_bytes(inst[i].number_bands, inst[i].ncouls, inst[i].ngpown, kNW, &tb);
       if (st != SIGMA_OK) {
@@ -316,15 +315,14 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
       }
       tbytes = std::max(tbytes, tb);
     }
-    cudaError_t e2 = cudaMalloc(&b->tensor_ws, up256(ybytes) + tbytes);
+    cudaError_t e2 = cudaMalloc(&b->tensor_ws, tbytes);
     if (e2 != cudaSuccess) {
       cudaGetLastError();
       set_last_cuda_error(e2, "cudaMalloc(batch tensor workspace)", __LINE__);
       sigma_gpp_batch_destroy(b);
       return SIGMA_ERR_ALLOC;
     }
-    b->yfac = static_cast<double2*>(b->tensor_ws);
-    b->tiles = static_cast<char*>(b->tensor_ws) + up256(ybytes);
+    b->tiles = static_cast<char*>(b->tensor_ws);
     b->ff.assign(n_instances, nullptr);
     for (int i = 0; i < n_instances; ++i) {
       int st = ff_plan_build(&b->ff[i], inst[i].number_bands, inst[i].ncouls, inst[i].ngpown, kNW, igp[i],
@@ -334,10 +332,15 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
         return st;
       }
     }
-    // per instance: factors (+ band operands with occupied bands), slicing and
-    // epilogue factors (3), GEMM, its reduction; then ssx and the reductions
+    // per instance: factors written as A slices (+ band operands with
+    // occupied bands), zeroed padding rows, B slices and epilogue factors (2),
+    // GEMM, its reduction; then ssx and the reductions
     int per = 0;
-    for (int i = 0; i < n_instances; ++i) per += (b->ssx[i].n_items > 0 ? 2 : 1) + 3 + 2;
+    for (int i = 0; i < n_instances; ++i) {
+      const OzakiPrep* oz = ff_plan_ozaki(b->ff[i]);
+      const int pad = oz->n_row_blocks * kOzRows > kNW * inst[i].ngpown ? 1 : 0;
+      per += (b->ssx[i].n_items > 0 ? 2 : 1) + pad + 2 + 2;
+    }
     b->launches = per + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
   }
   *out = b;
@@ -362,12 +365,14 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   if (tensor) {
     for (int i = 0; i < b->n; ++i) {
       // factors, and the occupied-band operands from the same pass
-      float2* y32 = reinterpret_cast<float2*>(b->yfac);
-      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], y32, occupied_bands(b->prepw[i], b->dev[i].nvband),
-                                           b->ssx[i].n_items > 0 ? &b->prep[i] : nullptr, s));
+      // the factors land directly as the contraction's A slices
+      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], nullptr, occupied_bands(b->prepw[i], b->dev[i].nvband),
+                                           b->ssx[i].n_items > 0 ? &b->prep[i] : nullptr, s,
+                                           ff_plan_ozaki(b->ff[i])));
       const int st = ff_execute_weighted(b->ff[i], nullptr, b->inst[i].aqsntemp, b->inst[i].aqsmtemp,
                                          b->inst[i].vcoul, 0.5,
-                                         reinterpret_cast<sigma_complex128*>(b->acht_n1[i]), stream, y32);
+                                         reinterpret_cast<sigma_complex128*>(b->acht_n1[i]), stream, nullptr,
+                                         true);
       if (st != SIGMA_OK) return st;
     }
   } else if (b->sch_view.total > 0)

@@ -44,6 +44,7 @@
 #include "sigma_internal.cuh"
 #include "floatfloat.cuh"
 #include "ff_plan.h"
+#include "ff_ozaki.cuh"
 #include "runtime.h"
 
 namespace sigma {
@@ -705,68 +706,111 @@ cudaError_t launch_transpose(const double2* src, double2* dst, int rows, int col
 // the reference's g-vector set, Zs = -I_eps below igp; the unpaired igp terms
 // and the occupied bands run in FP64.
 
-// Z slabs [3][ng][nc] of the non-occupied half sum in FP32, the contraction's
-// input precision: the factor of half_factor in float-float arithmetic on the
-// FP32 pipe (~2^-44 before the one rounding), with the threshold decision of
-// half_factor taken in FP64 within 2^-30 of the threshold.
-__global__ void __launch_bounds__(256) half_z32_kernel(HalfDev p, float2* z) {
-  const long long total = (long long)p.ng * p.nc;
-  FF wx[3];
+// Tiles of 32 g-vectors x kZCols columns: the factors are formed into shared
+// memory, then written as the split-BF16 contraction's A slices (rows
+// f * ngpown + column, 8 g-vectors per 16-byte chunk; consecutive threads fill
+// one 8-row group), skipping the K tiles past a row block's limit.
+constexpr int kZCols = 16;
+
+template <int NF>
+__device__ __forceinline__ void put_z_tile(const HalfDev& p, const OzakiPrep& oz, int c0, int ig0,
+                                           float2 (*tz)[kZCols][33]) {
+  for (int c = threadIdx.x; c < NF * kZCols * 4; c += blockDim.x) {
+    const int ch = c % 4, pl = (c / 4) % kZCols, f = c / (4 * kZCols);
+    const int col = c0 + pl;
+    if (col >= p.ng) continue;
+    const int R = f * p.ng + col;
+    if (ig0 / kOzKTile >= oz.kt_lim[R / kOzRows]) continue;
+    float re[8], im[8];
 #pragma unroll
-  for (int f = 0; f < 3; ++f) wx[f] = ff_of(p.wx[f]);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int col = (int)(t / p.nc), ig = (int)(t % p.nc);
-    const int lim = column_limit<3>(p.igp_of[col]);
-    float2 v[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-    if (ig < lim && (ig % kIgBlk) != kIgBlk - 1) {
-      const double2 wt = p.wt[t], ie = p.ieps[t];
-      const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
-      const FF b2 = ff_mul(b, b);
-      const FF s2 = ff_add(ff_mul(a, a), b2);
-      const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));
-      const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
-      // G (c + i b) = wx G - G conj(wtilde) = wx G - |wtilde|^2 I_eps
-      const FF sex = ff_mul(s2, er), sey = ff_mul(s2, ei);
-#pragma unroll
-      for (int f = 0; f < 3; ++f) {
-        const FF c = ff_add(wx[f], ff_neg(a));
-        const FF wv = ff_add(ff_mul(c, c), b2);
-        // kept where wv < max(0.25, 4e-6 |wtilde|^2)
-        bool n1, n2;
-        const bool k1 = ff_gt(FF{0.25f, 0.f}, wv, n1);
-        const bool k2 = ff_gt(s2, ff_mul(wv, FF{250000.f, 0.f}), n2);
-        bool keep = k1 || k2;
-        if (n1 || n2) {
-          const double b2d = guard_b2(wt.y);
-          keep = gt_nonneg(guard_thr(wt.x, b2d), guard_w(p.wx[f], wt.x, b2d));
-        }
-        if (keep) {
-          const FF r = ff_rcp(wv);
-          v[f] = make_float2(ff_mul_round(ff_add(ff_mul(wx[f], gx), ff_neg(sex)), r),
-                             ff_mul_round(ff_add(ff_mul(wx[f], gy), ff_neg(sey)), r));
-        }
-      }
+    for (int j = 0; j < 8; ++j) {
+      const float2 v = tz[f][pl][ch * 8 + j];
+      re[j] = v.x;
+      im[j] = v.y;
     }
-    z[t] = v[0];
-    z[total + t] = v[1];
-    z[2 * total + t] = v[2];
+    oz_put_a(oz, R, ig0 + ch * 8, re, im);
   }
 }
 
-// Zs [ng][nc] of the static remainder in FP32: -I_eps below igp.
-__global__ void __launch_bounds__(256) half_zs32_kernel(HalfDev p, float2* z) {
-  const long long total = (long long)p.ng * p.nc;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int col = (int)(t / p.nc), ig = (int)(t % p.nc);
-    const int lim = column_limit<1>(p.igp_of[col]);
-    float2 v = make_float2(0.f, 0.f);
-    if (ig < lim) {
-      const double2 e = p.ieps[t];
-      v = make_float2(-__double2float_rn(e.x), -__double2float_rn(e.y));
+// Z slabs of the non-occupied half sum, [3][ng][nc] as contraction rows: the
+// factor of half_factor in float-float arithmetic on the FP32 pipe (~2^-44
+// before the one rounding to FP32, the contraction's input precision), with
+// the threshold decision of half_factor taken in FP64 within 2^-30 of the
+// threshold.
+__global__ void __launch_bounds__(256) half_z_slices_kernel(HalfDev p, OzakiPrep oz) {
+  __shared__ float2 tz[3][kZCols][33];
+  FF wx[3];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) wx[f] = ff_of(p.wx[f]);
+  const int kt_all = (p.nc + kOzKTile - 1) / kOzKTile;
+  const long long tiles = (long long)((p.ng + kZCols - 1) / kZCols) * kt_all;
+  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int c0 = (int)(t / kt_all) * kZCols, ig0 = (int)(t % kt_all) * kOzKTile;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * kZCols; e += blockDim.x) {
+      const int pl = e / 32, k = e % 32;  // reads run along g-vectors
+      const int col = c0 + pl, ig = ig0 + k;
+      float2 v[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      const int lim = col < p.ng ? column_limit<3>(p.igp_of[col]) : 0;
+      if (ig < lim && (ig % kIgBlk) != kIgBlk - 1) {
+        const size_t off = (size_t)col * p.nc + ig;
+        const double2 wt = p.wt[off], ie = p.ieps[off];
+        const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
+        const FF b2 = ff_mul(b, b);
+        const FF s2 = ff_add(ff_mul(a, a), b2);
+        const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));
+        const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
+        // G (c + i b) = wx G - G conj(wtilde) = wx G - |wtilde|^2 I_eps
+        const FF sex = ff_mul(s2, er), sey = ff_mul(s2, ei);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const FF c = ff_add(wx[f], ff_neg(a));
+          const FF wv = ff_add(ff_mul(c, c), b2);
+          // kept where wv < max(0.25, 4e-6 |wtilde|^2)
+          bool n1, n2;
+          const bool k1 = ff_gt(FF{0.25f, 0.f}, wv, n1);
+          const bool k2 = ff_gt(s2, ff_mul(wv, FF{250000.f, 0.f}), n2);
+          bool keep = k1 || k2;
+          if (n1 || n2) {
+            const double b2d = guard_b2(wt.y);
+            keep = gt_nonneg(guard_thr(wt.x, b2d), guard_w(p.wx[f], wt.x, b2d));
+          }
+          if (keep) {
+            const FF r = ff_rcp(wv);
+            v[f] = make_float2(ff_mul_round(ff_add(ff_mul(wx[f], gx), ff_neg(sex)), r),
+                               ff_mul_round(ff_add(ff_mul(wx[f], gy), ff_neg(sey)), r));
+          }
+        }
+      }
+#pragma unroll
+      for (int f = 0; f < 3; ++f) tz[f][pl][k] = v[f];
     }
-    z[t] = v;
+    __syncthreads();
+    put_z_tile<3>(p, oz, c0, ig0, tz);
+  }
+}
+
+// Zs of the static remainder as contraction rows: -I_eps below igp, in FP32.
+__global__ void __launch_bounds__(256) half_zs_slices_kernel(HalfDev p, OzakiPrep oz) {
+  __shared__ float2 tz[1][kZCols][33];
+  const int kt_all = (p.nc + kOzKTile - 1) / kOzKTile;
+  const long long tiles = (long long)((p.ng + kZCols - 1) / kZCols) * kt_all;
+  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int c0 = (int)(t / kt_all) * kZCols, ig0 = (int)(t % kt_all) * kOzKTile;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * kZCols; e += blockDim.x) {
+      const int pl = e / 32, k = e % 32;
+      const int col = c0 + pl, ig = ig0 + k;
+      const int lim = col < p.ng ? column_limit<1>(p.igp_of[col]) : 0;
+      float2 v = make_float2(0.f, 0.f);
+      if (ig < lim) {
+        const double2 e2 = p.ieps[(size_t)col * p.nc + ig];
+        v = make_float2(-__double2float_rn(e2.x), -__double2float_rn(e2.y));
+      }
+      tz[0][pl][k] = v;
+    }
+    __syncthreads();
+    put_z_tile<1>(p, oz, c0, ig0, tz);
   }
 }
 
@@ -871,7 +915,6 @@ struct sigma_gpp_halfsum_plan_s {
   // factor slabs and the four contraction results
   sigma_ff_plan ff3 = nullptr, ff1 = nullptr;
   void* tblock = nullptr;
-  float2* z = nullptr;                                           // [3][ng][nc], FP32
   float2 *m32 = nullptr, *n32 = nullptr;  // occupied bands' aqsm / aqsn rows in FP32
   double2 *t3 = nullptr, *u3 = nullptr, *ts = nullptr, *us = nullptr;  // [nb][3], [nb][1]
 };
@@ -974,12 +1017,11 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
     if (st == SIGMA_OK && (flags & SIGMA_HALFSUM_STATIC))
       st = ff_plan_tile_bytes(number_bands, ncouls, ngpown, 1, &b1);
     const size_t b_tiles = up256(std::max(b3, b1));
-    const size_t b_z = up256(sizeof(float2) * 3 * ngc);
     const size_t b_r3 = up256(sizeof(double2) * (size_t)number_bands * kNW);
     const size_t b_r1 = up256(sizeof(double2) * (size_t)number_bands);
     const size_t b_o = up256(sizeof(float2) * (size_t)std::max(nvband, 1) * ncouls);
     if (st == SIGMA_OK) {
-      e = cudaMalloc(&p->tblock, b_tiles + b_z + 2 * b_r3 + 2 * b_r1 + 2 * b_o);
+      e = cudaMalloc(&p->tblock, b_tiles + 2 * b_r3 + 2 * b_r1 + 2 * b_o);
       if (e != cudaSuccess) {
         cudaGetLastError();
         set_last_cuda_error(e, "cudaMalloc(halfsum tensor)", __LINE__);
@@ -988,13 +1030,12 @@ extern "C" int sigma_gpp_halfsum_plan_create(sigma_gpp_halfsum_plan* out, int nu
     }
     if (st == SIGMA_OK) {
       char* t = static_cast<char*>(p->tblock);
-      p->z = reinterpret_cast<float2*>(t + b_tiles);
-      p->t3 = reinterpret_cast<double2*>(t + b_tiles + b_z);
-      p->u3 = reinterpret_cast<double2*>(t + b_tiles + b_z + b_r3);
-      p->ts = reinterpret_cast<double2*>(t + b_tiles + b_z + 2 * b_r3);
-      p->us = reinterpret_cast<double2*>(t + b_tiles + b_z + 2 * b_r3 + b_r1);
-      p->m32 = reinterpret_cast<float2*>(t + b_tiles + b_z + 2 * b_r3 + 2 * b_r1);
-      p->n32 = reinterpret_cast<float2*>(t + b_tiles + b_z + 2 * b_r3 + 2 * b_r1 + b_o);
+      p->t3 = reinterpret_cast<double2*>(t + b_tiles);
+      p->u3 = reinterpret_cast<double2*>(t + b_tiles + b_r3);
+      p->ts = reinterpret_cast<double2*>(t + b_tiles + 2 * b_r3);
+      p->us = reinterpret_cast<double2*>(t + b_tiles + 2 * b_r3 + b_r1);
+      p->m32 = reinterpret_cast<float2*>(t + b_tiles + 2 * b_r3 + 2 * b_r1);
+      p->n32 = reinterpret_cast<float2*>(t + b_tiles + 2 * b_r3 + 2 * b_r1 + b_o);
       // Z rows (iw, col) are zero from the column's g-vector limit on
       std::vector<int> kend3((size_t)kNW * ngpown), kend1(ngpown);
       for (int g = 0; g < ngpown; ++g) {
@@ -1084,18 +1125,24 @@ extern "C" int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const doub
     const bool stat = plan->ff1 && achstemp;
     auto C = [](const double2* x) { return reinterpret_cast<const sigma_complex128*>(x); };
     auto M = [](double2* x) { return reinterpret_cast<sigma_complex128*>(x); };
-    half_z32_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
+    // the slabs are written directly as the contractions' A slices; T and U
+    // (and the static pair) contract the same slices
+    const OzakiPrep& oz3 = *ff_plan_ozaki(plan->ff3);
+    half_z_slices_kernel<<<152 * 8, 256, 0, s>>>(p, oz3);
     SIGMA_CUDA_TRY(cudaGetLastError());
-    const float2* z = plan->z;
-    // T and U contract the same slab: U reuses the slices T cut
-    int st = ff_execute_weighted(plan->ff3, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->t3), stream, z);
+    SIGMA_CUDA_TRY(launch_ozaki_zero_rows(oz3, kNW * plan->ng, s));
+    int st = ff_execute_weighted(plan->ff3, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->t3), stream,
+                                 nullptr, true);
     if (st == SIGMA_OK)
       st = ff_execute_weighted(plan->ff3, nullptr, C(aqsm), C(aqsm), vcoul, 0.5, M(plan->u3), stream,
                                nullptr, true);
     if (st == SIGMA_OK && stat) {
-      half_zs32_kernel<<<152 * 8, 256, 0, s>>>(p, plan->z);
+      const OzakiPrep& oz1 = *ff_plan_ozaki(plan->ff1);
+      half_zs_slices_kernel<<<152 * 8, 256, 0, s>>>(p, oz1);
       SIGMA_CUDA_TRY(cudaGetLastError());
-      st = ff_execute_weighted(plan->ff1, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->ts), stream, z);
+      SIGMA_CUDA_TRY(launch_ozaki_zero_rows(oz1, plan->ng, s));
+      st = ff_execute_weighted(plan->ff1, nullptr, C(aqsn), C(aqsm), vcoul, 0.5, M(plan->ts), stream,
+                               nullptr, true);
       if (st == SIGMA_OK)
         st = ff_execute_weighted(plan->ff1, nullptr, C(aqsm), C(aqsn), vcoul, 0.5, M(plan->us), stream,
                                  nullptr, true);

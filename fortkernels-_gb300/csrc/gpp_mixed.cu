@@ -23,6 +23,7 @@
 // g-vector step.
 #include "sigma_internal.cuh"
 #include "floatfloat.cuh"
+#include "ff_ozaki.cuh"
 #include "gpp_batch.cuh"
 
 namespace sigma {
@@ -239,10 +240,12 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
 // writes go through shared memory.
 
 __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y, MixedPrep m,
-                                                             int n_col_blocks) {
+                                                             int n_col_blocks, OzakiPrep oz) {
   __shared__ float4 ta[32][kBPM + 1];
   __shared__ float2 tb[32][kBPM + 1];
   __shared__ float2 tc[32][kBPM + 1];
+  __shared__ float2 ty[kNW][kBPM][33];  // the tile's factors for the slice writes
+  const bool slices = oz.a_tiles != nullptr;
   const int tid = threadIdx.x;
   const size_t plane = (size_t)p.ng * p.nc;
   FF wx[kNW];
@@ -261,6 +264,7 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
       const int my_igp = cb * kBPM + pl, ig = ig0 + k;
       float4 av = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
       float2 g32 = make_float2(0.f, 0.f), om = make_float2(0.f, 0.f);
+      float2 yt[kNW] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
       if (my_igp < p.ng && ig < p.nc) {
         const size_t off = (size_t)my_igp * p.nc + ig;
         const double2 wt = p.wt[off];
@@ -288,14 +292,15 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
             const double b2d = guard_b2(wt.y);
             keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2d), guard_thr(wt.x, b2d));
           }
-          if (y) {
+          if (y || slices) {
             float2 yv = make_float2(0.f, 0.f);
             if (keep) {
               const FF r = ff_rcp(wv);
               yv = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
                                ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
             }
-            y[(size_t)iw * plane + off] = yv;
+            if (y) y[(size_t)iw * plane + off] = yv;
+            yt[iw] = yv;
           }
           mask |= keep ? (1u << iw) : 0u;
           if (ops && p.nvband > 0 && !keep) {
@@ -322,15 +327,38 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
       ta[k][pl] = av;
       tb[k][pl] = g32;
       tc[k][pl] = om;
+      if (slices) {
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) ty[iw][pl][k] = yt[iw];
+      }
     }
-    if (!ops) continue;
+    if (!ops && !slices) continue;
     __syncthreads();
-    for (int e = tid; e < 32 * kBPM; e += 256) {
-      const int k = e / kBPM, pl = e % kBPM;  // operand writes run along columns
-      const size_t o = ((size_t)cb * m.nc_pad + ig0 + k) * kBPM + pl;
-      m.colA[o] = ta[k][pl];
-      m.colB[o] = tb[k][pl];
-      if (m.colC) m.colC[o] = tc[k][pl];
+    if (ops) {
+      for (int e = tid; e < 32 * kBPM; e += 256) {
+        const int k = e / kBPM, pl = e % kBPM;  // operand writes run along columns
+        const size_t o = ((size_t)cb * m.nc_pad + ig0 + k) * kBPM + pl;
+        m.colA[o] = ta[k][pl];
+        m.colB[o] = tb[k][pl];
+        if (m.colC) m.colC[o] = tc[k][pl];
+      }
+    }
+    if (slices) {
+      // split-BF16 slices of the contraction's A rows (iw, column), 8
+      // g-vectors per chunk; consecutive threads fill one 8-row group
+      for (int c = tid; c < kNW * kBPM * 4; c += 256) {
+        const int ch = c % 4, pl = (c / 4) % kBPM, iw = c / (4 * kBPM);
+        const int col = cb * kBPM + pl;
+        if (col >= p.ng) continue;
+        float re[8], im[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float2 v = ty[iw][pl][ch * 8 + j];
+          re[j] = v.x;
+          im[j] = v.y;
+        }
+        oz_put_a(oz, iw * p.ng + col, ig0 + ch * 8, re, im);
+      }
     }
   }
 }
@@ -891,7 +919,7 @@ int sch_blocks_per_sm_mixed() {
 }
 
 cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, const MixedPrep* m,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, const OzakiPrep* oz) {
   const int sms = 152;
   MixedPrep mm{};
   if (m) {
@@ -903,8 +931,12 @@ cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, 
     mm.nc_pad = (p.nc + 31) / 32 * 32;  // tiles over the factor slabs alone
   }
   const int ncb = m ? w.n_col_blocks : (p.ng + kBPM - 1) / kBPM;
-  tensor_factors_kernel<<<sms * 8, 256, 0, s>>>(p, y, mm, ncb);
-  return cudaGetLastError();
+  OzakiPrep o{};
+  if (oz) o = *oz;
+  tensor_factors_kernel<<<sms * 8, 256, 0, s>>>(p, y, mm, ncb, o);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !oz) return e;
+  return launch_ozaki_zero_rows(*oz, kNW * p.ng, s);
 }
 
 cudaError_t launch_prep_mixed(const GppDev& p, const GppWork& w, const MixedPrep& m, cudaStream_t s) {
