@@ -158,7 +158,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
   p->ssx_grid = sms * (mixed ? ssx_blocks_per_sm_mixed() : ssx_blocks_per_sm_fp64());
   gpp_size_work(p->sch, 0, number_bands, kBN, mixed ? kBPM : kBP, ncouls, ngpown, p->sch_grid,
             mixed ? kItemsPerSlotMixed : kItemsPerSlot);
-  gpp_size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
+  gpp_size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 2);
   if (p->sch.n_items < p->sch_grid) p->sch_grid = p->sch.n_items;
   if (p->ssx.n_items < p->ssx_grid) p->ssx_grid = p->ssx.n_items;
   if (!mixed) {
