@@ -814,23 +814,25 @@ __global__ void __launch_bounds__(256) half_zs_slices_kernel(HalfDev p, OzakiPre
   }
 }
 
-// Band rows of the tensor form: one warp per band, compensated sums over the
-// columns of the unpaired igp terms (and of the occupied-band partials), then
+// Band rows of the tensor form: one CTA per band, its 8 warps over the
+// columns, compensated sums of the unpaired igp terms (and of the
+// occupied-band partials) combined in a fixed order, then
 //   acht_n1[n1][iw] = T + conj(U) + unpaired       (n1 >= nvband)
 //                   = sum_col occ_ach                (n1 <  nvband)
 //   asx_n1[n1][iw]  = sum_col occ_asx                (n1 <  nvband)
 //   stat_n1[n1]     = Ts + conj(Us) + unpaired       (static remainder)
-__global__ void half_tensor_rows_kernel(HalfDev p, const double2* t3, const double2* u3,
-                                        const double2* ts, const double2* us, const double2* occ_ach,
-                                        const double2* occ_asx, double2* acht_n1, double2* asx_n1,
-                                        double2* stat_n1) {
-  const int n1 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (n1 >= p.nb) return;
+constexpr int kRowWarps = 8;
+__global__ void __launch_bounds__(kRowWarps * 32) half_tensor_rows_kernel(
+    HalfDev p, const double2* t3, const double2* u3, const double2* ts, const double2* us,
+    const double2* occ_ach, const double2* occ_asx, double2* acht_n1, double2* asx_n1, double2* stat_n1) {
+  constexpr int kVals = 4 * kNW + 2;  // ax, ay, sx, sy per frequency; qx, qy
+  __shared__ double part[kRowWarps][kVals];
+  const int n1 = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool occ = n1 < p.nvband;
   const double wx[3] = {p.wx[0], p.wx[1], p.wx[2]};
   Comp ax[3], ay[3], sx[3], sy[3], qx, qy;
-  for (int col = lane; col < p.ng; col += 32) {
+  for (int col = warp * 32 + lane; col < p.ng; col += kRowWarps * 32) {
     const int igp = p.igp_of[col];
     if (igp < 0) continue;
     const size_t off = (size_t)col * p.nc + igp;
@@ -869,20 +871,40 @@ __global__ void half_tensor_rows_kernel(HalfDev p, const double2* t3, const doub
   }
 #pragma unroll
   for (int iw = 0; iw < kNW; ++iw) {
-    const double rx = warp_sum_comp(ax[iw]), ry = warp_sum_comp(ay[iw]);
-    const double ux = warp_sum_comp(sx[iw]), uy = warp_sum_comp(sy[iw]);
+    const double v0 = warp_sum_comp(ax[iw]), v1 = warp_sum_comp(ay[iw]);
+    const double v2 = warp_sum_comp(sx[iw]), v3 = warp_sum_comp(sy[iw]);
     if (lane == 0) {
-      if (occ) {
-        acht_n1[n1 * kNW + iw] = make_double2(rx, ry);
-        asx_n1[n1 * kNW + iw] = make_double2(ux, uy);
-      } else {
-        const double2 a = t3[(size_t)n1 * kNW + iw], b = u3[(size_t)n1 * kNW + iw];
-        acht_n1[n1 * kNW + iw] = make_double2(rx + a.x + b.x, ry + a.y - b.y);
-      }
+      part[warp][4 * iw + 0] = v0;
+      part[warp][4 * iw + 1] = v1;
+      part[warp][4 * iw + 2] = v2;
+      part[warp][4 * iw + 3] = v3;
     }
   }
-  const double vx = warp_sum_comp(qx), vy = warp_sum_comp(qy);
-  if (ts && lane == 0) stat_n1[n1] = make_double2(vx + ts[n1].x + us[n1].x, vy + ts[n1].y - us[n1].y);
+  const double q0 = warp_sum_comp(qx), q1 = warp_sum_comp(qy);
+  if (lane == 0) {
+    part[warp][4 * kNW] = q0;
+    part[warp][4 * kNW + 1] = q1;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double tot[kVals];
+  for (int v = 0; v < kVals; ++v) {
+    Comp c;
+    for (int q = 0; q < kRowWarps; ++q) c.add(part[q][v]);
+    tot[v] = c.value();
+  }
+#pragma unroll
+  for (int iw = 0; iw < kNW; ++iw) {
+    const double rx = tot[4 * iw], ry = tot[4 * iw + 1], ux = tot[4 * iw + 2], uy = tot[4 * iw + 3];
+    if (occ) {
+      acht_n1[n1 * kNW + iw] = make_double2(rx, ry);
+      asx_n1[n1 * kNW + iw] = make_double2(ux, uy);
+    } else {
+      const double2 a = t3[(size_t)n1 * kNW + iw], b = u3[(size_t)n1 * kNW + iw];
+      acht_n1[n1 * kNW + iw] = make_double2(rx + a.x + b.x, ry + a.y - b.y);
+    }
+  }
+  if (ts) stat_n1[n1] = make_double2(tot[4 * kNW] + ts[n1].x + us[n1].x, tot[4 * kNW + 1] + ts[n1].y - us[n1].y);
 }
 
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
@@ -1148,7 +1170,7 @@ extern "C" int sigma_gpp_halfsum_execute(sigma_gpp_halfsum_plan plan, const doub
                                  nullptr, true);
     }
     if (st != SIGMA_OK) return st;
-    half_tensor_rows_kernel<<<(plan->nb * 32 + 255) / 256, 256, 0, s>>>(
+    half_tensor_rows_kernel<<<plan->nb, kRowWarps * 32, 0, s>>>(
         p, plan->t3, plan->u3, stat ? plan->ts : nullptr, plan->us, plan->occ_ach, plan->occ_asx,
         plan->acht_n1, plan->asx_n1, plan->stat_n1);
     SIGMA_CUDA_TRY(cudaGetLastError());
