@@ -293,7 +293,10 @@ def test_production_stress_mixed_within_bar(sigma_lib):
 
 
 # ------------------------------------------------------------ tensor-core form
-TENSOR_CASES = [c for c in RANDOM_CASES if c[3] >= 20]
+TENSOR_CASES = [c for c in RANDOM_CASES if c[3] >= 20] + [
+    (50, 2, 2080, 128, 31, False),      # 3 x 128 contraction rows: no padding rows to zero
+    (24, 0, 1000, 128, 32, True),       # the same with a ragged last K tile and no occupied band
+]
 
 
 @pytest.mark.parametrize("case", TENSOR_CASES, ids=lambda c: f"nb{c[0]}-nv{c[1]}-nc{c[2]}-ng{c[3]}{'-stress' if c[5] else ''}")

@@ -136,6 +136,8 @@ TENSOR_CASES = [
     (40, 3, 2048, 100, 81, False),
     (37, 2, 1536, 33, 82, True),      # unpaired igp terms, near-pole wtilde
     (70, 0, 4096, 130, 83, False),    # no occupied band
+    (30, 2, 1000, 128, 84, False),    # contraction rows a multiple of 128 (no padding), ragged K
+    (45, 5, 2048, 64, 85, True),      # three occupied-band groups, 192 slab rows
 ]
 
 
