@@ -1192,8 +1192,8 @@ __device__ __forceinline__ void ssx_masked_item(const GppDev& p, const GppWork& 
     split_f(p.wx[iw], wxh[iw], wxl[iw]);
     iwx2[iw] = __double2float_rn(rcp_f64(p.wx[iw] * p.wx[iw]));
   }
-  // per (band, frequency): FP32 sums of kU = 2 terms folded into
-  // float-float sums (hi, lo)
+  // per (band, frequency): FP32 sums of 2 terms folded into float-float
+  // sums (hi, lo)
   float2 acc[kSsxBN][kNW], hi[kSsxBN][kNW], lo[kSsxBN][kNW];
 #pragma unroll
   for (int i = 0; i < kSsxBN; ++i)
@@ -1221,7 +1221,7 @@ __device__ __forceinline__ void ssx_masked_item(const GppDev& p, const GppWork& 
       const int n1 = min(n1_0 + i, band_end - 1);
       bands[i] = m.band + ((size_t)(n1 / kBN) * m.nc_pad) * kBN + (n1 % kBN);
     }
-    constexpr int kU = 2;  // g-vectors whose operands are loaded together
+    constexpr int kU = 4;  // g-vectors whose operands are loaded together
     for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kU) {
       float4 a[kU];
       float2 g[kU], om[kU], an[kU][kSsxBN];
@@ -1256,8 +1256,8 @@ __device__ __forceinline__ void ssx_masked_item(const GppDev& p, const GppWork& 
             acc[i][iw].x += fmaf(an[u][i].x, sv[iw].x, -an[u][i].y * sv[iw].y);
             acc[i][iw].y += fmaf(an[u][i].x, sv[iw].y, an[u][i].y * sv[iw].x);
           }
+        if (u & 1) fold();  // pair sums
       }
-      fold();  // runs of kU terms
     }
   }
 
