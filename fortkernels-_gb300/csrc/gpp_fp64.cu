@@ -500,26 +500,48 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       const double2 g = sm.g[k][tid], om = sm.om[k][tid];
       const double b2 = guard_b2(b);
       const double thr = guard_thr(a, b2), thr2 = guard_thr2(a, b2);
+      // ssx factor of band i and frequency iw (band-independent when the
+      // frequencies are shared)
+      auto factor = [&](int i, int iw) {
+        const double wx = sh.wx[i][iw];
+        const double wv = guard_w(wx, a, b2);
+        const bool keep = gt_nonneg(wv, thr);
+        const bool br2 = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
+        // branch 1: Omega2 / wx^2
+        const double iwx2 = sh.iwx2[i][iw];
+        const double2 s1 = make_double2(om.x * iwx2, om.y * iwx2);
+        // branch 2: -G conj(z) / (2 |z|^2), z = wtilde + wx
+        const double zr = a + wx;
+        const double q = -0.5 * rcp_f64(fma(zr, zr, b2));
+        const double2 s2 = make_double2(fma(g.x, zr, g.y * b) * q, fma(g.y, zr, -g.x * b) * q);
+        return keep ? s1 : (br2 ? s2 : make_double2(0.0, 0.0));
+      };
+      if (p.wx_stride == 0) {
+        double2 sv[kNW];
 #pragma unroll
-      for (int i = 0; i < kSsxBN; ++i) {
-        if (i < nbl) {
-          const double2 an = sm.n[k][i];
+        for (int iw = 0; iw < kNW; ++iw) sv[iw] = factor(0, iw);
 #pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) {
-            const double wx = sh.wx[i][iw];
-            const double wv = guard_w(wx, a, b2);
-            const bool keep = gt_nonneg(wv, thr);
-            const bool br2 = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
-            // branch 1: Omega2 / wx^2
-            const double iwx2 = sh.iwx2[i][iw];
-            const double2 s1 = make_double2(om.x * iwx2, om.y * iwx2);
-            // branch 2: -G conj(z) / (2 |z|^2), z = wtilde + wx
-            const double zr = a + wx;
-            const double q = -0.5 * rcp_f64(fma(zr, zr, b2));
-            const double2 s2 = make_double2(fma(g.x, zr, g.y * b) * q, fma(g.y, zr, -g.x * b) * q);
-            const double2 s = keep ? s1 : (br2 ? s2 : make_double2(0.0, 0.0));
-            acc[i][iw].x = fma(an.x, s.x, fma(-an.y, s.y, acc[i][iw].x));
-            acc[i][iw].y = fma(an.x, s.y, fma(an.y, s.x, acc[i][iw].y));
+        for (int i = 0; i < kSsxBN; ++i) {
+          if (i < nbl) {
+            const double2 an = sm.n[k][i];
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              acc[i][iw].x = fma(an.x, sv[iw].x, fma(-an.y, sv[iw].y, acc[i][iw].x));
+              acc[i][iw].y = fma(an.x, sv[iw].y, fma(an.y, sv[iw].x, acc[i][iw].y));
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < kSsxBN; ++i) {
+          if (i < nbl) {
+            const double2 an = sm.n[k][i];
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const double2 s = factor(i, iw);
+              acc[i][iw].x = fma(an.x, s.x, fma(-an.y, s.y, acc[i][iw].x));
+              acc[i][iw].y = fma(an.x, s.y, fma(an.y, s.x, acc[i][iw].y));
+            }
           }
         }
       }
