@@ -366,7 +366,7 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   const bool ypath = !mixed && !tensor && wx_band_stride == 0 && plan->schy.n_items > 0;
   const bool mypath = mixed && wx_band_stride == 0 && plan->schmy.n_items > 0;
   if (mypath)  // pre-pass in float-float arithmetic (the tensor form's operand pass)
-    SIGMA_CUDA_TRY(launch_tensor_factors(p, nullptr, plan->prepw, &plan->prep, s));
+    SIGMA_CUDA_TRY(launch_tensor_factors(p, plan->prepw, &plan->prep, s));
   else if (mixed && plan->sch.n_items > 0)
     SIGMA_CUDA_TRY(launch_prep_mixed(p, plan->prepw, plan->prep, s));
   GppWork main = ypath ? plan->schy : (mypath ? plan->schmy : plan->sch);
@@ -375,7 +375,7 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (tensor) {
     // factors, and the occupied-band operands from the same pass
     // the factors land directly as the contraction's A slices
-    SIGMA_CUDA_TRY(launch_tensor_factors(p, nullptr, occupied_bands(plan->prepw, p.nvband),
+    SIGMA_CUDA_TRY(launch_tensor_factors(p, occupied_bands(plan->prepw, p.nvband),
                                          plan->ssx.n_items > 0 ? &plan->prep : nullptr, s,
                                          ff_plan_ozaki(plan->ff)));
     const int st = ff_execute_weighted(plan->ff, nullptr, aqsntemp, aqsmtemp, vcoul, 0.5,

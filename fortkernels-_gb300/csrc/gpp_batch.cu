@@ -360,13 +360,13 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   if (mixed && !tensor)
     for (int i = 0; i < b->n; ++i)
       if (b->sch[i].n_items > 0)
-        SIGMA_CUDA_TRY(b->mixedy ? launch_tensor_factors(b->dev[i], nullptr, b->prepw[i], &b->prep[i], s)
+        SIGMA_CUDA_TRY(b->mixedy ? launch_tensor_factors(b->dev[i], b->prepw[i], &b->prep[i], s)
                                  : launch_prep_mixed(b->dev[i], b->prepw[i], b->prep[i], s));
   if (tensor) {
     for (int i = 0; i < b->n; ++i) {
       // factors, and the occupied-band operands from the same pass
       // the factors land directly as the contraction's A slices
-      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], nullptr, occupied_bands(b->prepw[i], b->dev[i].nvband),
+      SIGMA_CUDA_TRY(launch_tensor_factors(b->dev[i], occupied_bands(b->prepw[i], b->dev[i].nvband),
                                            b->ssx[i].n_items > 0 ? &b->prep[i] : nullptr, s,
                                            ff_plan_ozaki(b->ff[i])));
       const int st = ff_execute_weighted(b->ff[i], nullptr, b->inst[i].aqsntemp, b->inst[i].aqsmtemp,

@@ -224,30 +224,29 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
 // so the band sum is the FF contraction (ff_ozaki.cu) with the three
 // frequencies as slabs and the column weight 0.5 vcoul[igp].  The contraction
 // rounds its operand to FP32 before splitting it into BF16 slices, so this
-// pass delivers the factors
-//   y[iw][my_igp][ig] = G (c + i b) / (c^2 + b^2)   (0 when the guard drops it)
-// already rounded to FP32, computed in float-float arithmetic (pairs of FP32
-// values, ~2^-44 relative) from exact splits of the FP64 inputs: the same
-// FP32 values as rounding FP64 factors, on the FP32 pipe instead of GB300's
-// 1/64-rate FP64 pipe.  Keep and second-branch decisions are taken in
-// float-float and re-taken with the FP64 path's own expressions within 2^-30
-// of a threshold.  In the same pass (same inputs) it writes the pre-pass
-// operands of the occupied-band kernel (colA with the exact keep and
-// second-branch bits, colB = G, colC = Omega2) when m.colA is set; with y
-// null it writes those operands alone (the mixed form's pre-pass for one
-// frequency set).  Tiles of
-// kBPM columns x 32 g-vectors: factor writes run along g-vectors, operand
-// writes go through shared memory.
+// pass forms the factors
+//   Y[iw][my_igp][ig] = G (c + i b) / (c^2 + b^2)   (0 when the guard drops it)
+//                     = (wx G - |wtilde|^2 I_eps) / (c^2 + b^2)
+// rounded to FP32, computed in float-float arithmetic (pairs of FP32 values,
+// ~2^-44 relative) from exact splits of the FP64 inputs, on the FP32 pipe
+// instead of GB300's 1/64-rate FP64 pipe, and writes them directly as the
+// contraction's A slices (oz.a_tiles set).  Keep and second-branch decisions
+// are taken in float-float and re-taken with the FP64 path's own expressions
+// within 2^-30 of a threshold.  In the same pass (same inputs) it writes the
+// pre-pass operands of the occupied-band kernel (colA with the exact keep
+// and second-branch bits, colB = G, colC = Omega2) when m.colA is set; with
+// no slices it writes those operands alone (the mixed form's pre-pass for
+// one frequency set).  Tiles of kBPM columns x 32 g-vectors staged in shared
+// memory, from which the operand and slice writes run.
 
-__global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y, MixedPrep m,
-                                                             int n_col_blocks, OzakiPrep oz) {
+__global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, MixedPrep m, int n_col_blocks,
+                                                             OzakiPrep oz) {
   __shared__ float4 ta[32][kBPM + 1];
   __shared__ float2 tb[32][kBPM + 1];
   __shared__ float2 tc[32][kBPM + 1];
   __shared__ float2 ty[kNW][kBPM][33];  // the tile's factors for the slice writes
   const bool slices = oz.a_tiles != nullptr;
   const int tid = threadIdx.x;
-  const size_t plane = (size_t)p.ng * p.nc;
   FF wx[kNW];
 #pragma unroll
   for (int iw = 0; iw < kNW; ++iw) wx[iw] = ff_of(p.wx[iw]);
@@ -292,14 +291,13 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, float2* y
             const double b2d = guard_b2(wt.y);
             keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2d), guard_thr(wt.x, b2d));
           }
-          if (y || slices) {
+          if (slices) {
             float2 yv = make_float2(0.f, 0.f);
             if (keep) {
               const FF r = ff_rcp(wv);
               yv = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
                                ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
             }
-            if (y) y[(size_t)iw * plane + off] = yv;
             yt[iw] = yv;
           }
           mask |= keep ? (1u << iw) : 0u;
@@ -918,8 +916,8 @@ int sch_blocks_per_sm_mixed() {
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, const MixedPrep* m,
-                                  cudaStream_t s, const OzakiPrep* oz) {
+cudaError_t launch_tensor_factors(const GppDev& p, const GppWork& w, const MixedPrep* m, cudaStream_t s,
+                                  const OzakiPrep* oz) {
   const int sms = 152;
   MixedPrep mm{};
   if (m) {
@@ -933,7 +931,7 @@ cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, 
   const int ncb = m ? w.n_col_blocks : (p.ng + kBPM - 1) / kBPM;
   OzakiPrep o{};
   if (oz) o = *oz;
-  tensor_factors_kernel<<<sms * 8, 256, 0, s>>>(p, y, mm, ncb, o);
+  tensor_factors_kernel<<<sms * 8, 256, 0, s>>>(p, mm, ncb, o);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || !oz) return e;
   return launch_ozaki_zero_rows(*oz, kNW * p.ng, s);

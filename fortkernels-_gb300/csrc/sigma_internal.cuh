@@ -173,16 +173,16 @@ cudaError_t launch_ssx_mixed(const GppDev& p, const GppWork& w, const MixedPrep&
 int sch_blocks_per_sm(int precision);
 int ssx_blocks_per_sm(int precision);
 
-// Tensor form: frequency factors y[iw][my_igp][ig] of one shared frequency
-// set, rounded to FP32, together with the occupied-band kernel's pre-pass operands
-// (w: the pre-pass blocks; m null: factors only; y null: the operands alone,
-// which is the mixed form's pre-pass for one frequency set).  With oz set
-// the factors are also written as the split-BF16 contraction's A slices
-// (rows iw * ngpown + my_igp), padding rows zeroed, for an execution with
-// reuse_a.
+// The float-float pass over (column, g-vector) of one shared frequency set:
+// the FP32 pre-pass operands of the occupied-band and mixed kernels (m; null:
+// none; w: the pre-pass blocks) and, with oz set, the tensor form's
+// frequency factors Y[iw][my_igp][ig] rounded to FP32 and written as the
+// split-BF16 contraction's A slices (rows iw * ngpown + my_igp, padding rows
+// zeroed) for an execution with reuse_a.  With m set and oz null it is the
+// mixed form's pre-pass.
 struct OzakiPrep;
-cudaError_t launch_tensor_factors(const GppDev& p, float2* y, const GppWork& w, const MixedPrep* m,
-                                  cudaStream_t s, const OzakiPrep* oz = nullptr);
+cudaError_t launch_tensor_factors(const GppDev& p, const GppWork& w, const MixedPrep* m, cudaStream_t s,
+                                  const OzakiPrep* oz = nullptr);
 
 // Sums the partials of the sch and ssx passes in a fixed order into
 // acht_n1[nb][3] (workspace), achtemp[3], asxtemp[3] and acht_n1_loc[nb].
