@@ -29,7 +29,7 @@
 namespace sigma {
 namespace {
 
-constexpr int kRBN = 64, kRBP = 64;  // bands x columns per main-pass item
+constexpr int kRBN = 128, kRBP = 32;  // bands x columns per main-pass item
 constexpr int kRCK = 32;             // g-vectors per staged chunk
 
 struct GppRealDev {
