@@ -263,10 +263,11 @@ def timed(torch, dist, world, fn, steps, stream):
     return ms
 
 
-FP64_PROFILE = ROOT / "profiles" / "gpp_sch_fp64y_64bands.md"
+FP64_PROFILE = ROOT / "profiles" / "gpp_sch_fp64y_128bands.md"
 # 3 DFMA (three-product complex multiply-add) + the shared factor and staged
-# sums (~42 FP64 operations per column and g-vector / 192 terms)
-FP64_PIPE_OPS_PER_TERM = 3.22
+# sums (~41 FP64 operations per column and g-vector / 384 terms, one band sum
+# per band and g-vector / 48 terms)
+FP64_PIPE_OPS_PER_TERM = 3.13
 
 
 def profile_value(key):
@@ -773,7 +774,7 @@ def run_ours(args, rank, world, local_rank):
                              "so frac exceeds 1; pipe_ops_frac is "
                              "the FP64 pipe occupancy those operations imply and "
                              "fp64_pipe_utilisation_ncu the measured one "
-                             "(profiles/gpp_sch_fp64y_64bands.md)"},
+                             "(profiles/gpp_sch_fp64y_128bands.md)"},
         "mixed": {"value": round(mixed_value, 4), "unit": UNIT,
                   "speedup_vs_fp64": round(mixed_value / value, 3),
                   "ms_per_step": round(ms_mixed / msteps, 3),

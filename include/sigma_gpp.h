@@ -206,7 +206,7 @@ int sigma_gpp_batched(int n_instances, const sigma_gpp_instance* inst, int preci
  * every GPU that loads the library until the process exits; the call makes
  * no cudaMalloc, cudaFree or other allocation.
  *   - Limits: ngpown <= 65536, and the partial sums of the problem must fit
- *     the 32 MiB (the production shape 512 x 1638 x 32768 uses ~9 MB);
+ *     the 32 MiB (the production shape 512 x 1638 x 32768 uses ~17 MB);
  *     larger problems return SIGMA_ERR_WORKSPACE with a message in
  *     sigma_last_error_message().
  *   - The first call on a device looks up the array's device address
