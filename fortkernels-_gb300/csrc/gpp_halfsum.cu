@@ -50,7 +50,8 @@
 namespace sigma {
 namespace {
 
-constexpr int kHBN = 32, kHBP = 32;  // bands x columns per item
+constexpr int kHBN = 64, kHBP = 16;  // bands x columns per item
+static_assert(kHBP <= 32, "one warp finds the item's g-vector limit");
 constexpr int kHCK = 16;             // g-vectors per staged chunk
 constexpr int kHTB = kHBN / 16, kHTC = kHBP / 16;
 constexpr int kOccBands = 4;         // occupied bands per accumulation pass (FP64)
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
     const int n1_0 = w.band_begin + ic.bb * kHBN, p0 = ic.cb * kHBP;
     if (tid < 32) {
       const int col = p0 + tid;
-      const int lim = column_limit<NF>(col < p.ng ? p.igp_of[col] : -1);
+      const int lim = column_limit<NF>(tid < kHBP && col < p.ng ? p.igp_of[col] : -1);
       const int mx = __reduce_max_sync(0xffffffffu, lim);
       if (tid == 0) s_kmax = mx;
     }
