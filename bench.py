@@ -15,9 +15,15 @@ device.  One step = one full evaluation of achtemp / asxtemp / acht_n1_loc.
   mixed      the mixed-precision path on the same inputs, its Gterms/s and
              the relative error of every achtemp / asxtemp output against the
              FP64 path (and on the stress fill with 5% near-pole wtilde)
-  roofline   the main FP64 kernel: 27 flop per term (algorithmic count of the
-             reference's term) over its CUDA-event time, against the FP64 FMA
-             peak measured on this device at start-up
+  roofline   the main FP64 kernel (sch_fp64y_kernel): the FP64 pipe work its
+             algorithm issues per term (3.13 operations: three real products
+             per complex multiply-add plus the shared frequency factor) over
+             its CUDA-event time, against the FP64 pipe peak (2 DFMA / clk / SM
+             at the SM clock sampled during the timed region); the reference's
+             27 flop per term is reported beside it as a rate
+  rel_err_vs_oracle  every achtemp / asxtemp output (and acht_n1_loc) of each
+             form against the CPU oracle's full outputs of the same seeded
+             inputs (tests/golden/config_*.npz)
   cpu_baseline  the reference algorithm (oracle port with the reference's
              loop nest and OpenMP schedule) on a bounded band sample, all host
              cores
@@ -36,7 +42,6 @@ import argparse
 import json
 import os
 import pathlib
-import re
 import statistics
 import subprocess
 import sys
@@ -57,12 +62,37 @@ FLOP_PER_TERM = 27  # algorithmic count of one (n1, igp, ig, iw) term of the ref
 CPU_MAX_BANDS = 256
 NB, NVB, NC, NPG = 512, 2, 32768, 20
 NG = NC // NPG
+PRODUCTION = (NB, NVB, NC, NPG)
+GOLDEN = ROOT / "tests" / "golden"
 
 
-def set_bands(nb):
-    global NB, WORKLOAD
-    NB = nb
-    WORKLOAD = f"GPP sigma sum, FP64 drop-in, {NB} bands x 1638 columns x 32768 g-vectors x 3 frequencies"
+def set_shape(nb, nvb, nc, npg):
+    """GPP instance shape of the run (the production 512 2 32768 20 by default;
+    smaller shapes only for profiling captures)."""
+    global NB, NVB, NC, NPG, NG, WORKLOAD
+    NB, NVB, NC, NPG = nb, nvb, nc, npg
+    NG = NC // NPG
+    WORKLOAD = (f"GPP sigma sum, FP64 drop-in, {NB} bands x {NG} columns x {NC} g-vectors x 3 frequencies")
+
+
+def golden(name):
+    """Full oracle outputs of a production workload (None when the fixture is absent)."""
+    f = GOLDEN / name
+    if not f.exists():
+        return None
+    with np.load(f) as z:
+        return {k: z[k] for k in z.files}
+
+
+def err_vs_oracle(out, ref):
+    """Relative error of every achtemp / asxtemp output, and acht_n1_loc
+    normwise, against the oracle's outputs."""
+    ach, asx, n1 = out
+    e = {"achtemp": rel(ach, ref["achtemp"]), "asxtemp": rel(asx, ref["asxtemp"]),
+         "acht_n1_loc_normwise": float(np.linalg.norm(n1 - ref["acht_n1_loc"]) /
+                                       np.linalg.norm(ref["acht_n1_loc"]))}
+    e["max"] = max(max(e["achtemp"]), max(e["asxtemp"]))
+    return e
 
 
 def log(*a):
@@ -263,27 +293,64 @@ def timed(torch, dist, world, fn, steps, stream):
     return ms
 
 
-FP64_PROFILE = ROOT / "profiles" / "gpp_sch_fp64y_128bands.md"
-# 3 DFMA (three-product complex multiply-add) + the shared factor and staged
-# sums (~41 FP64 operations per column and g-vector / 384 terms, one band sum
-# per band and g-vector / 48 terms)
-FP64_PIPE_OPS_PER_TERM = 3.13
-
-
-def profile_value(key):
-    """A figure of the main FP64 kernel's committed ncu summary (None when absent)."""
-    if not FP64_PROFILE.exists():
-        return None
-    m = re.search(key + r":\s*([0-9.eE+-]+)", FP64_PROFILE.read_text())
-    return float(m.group(1)) if m else None
-
-
-def profile_traffic_per_term():
-    """DRAM bytes per term of the main FP64 kernel from the committed ncu summary."""
-    return profile_value("dram_bytes_per_term")
+# FP64 pipe operations of sch_fp64y_kernel per term, counted from its
+# algorithm: 3 DFMA (three-product complex multiply-add) + the shared
+# frequency factor and staged sums (~41 FP64 operations per column and
+# g-vector over 128 bands x 3 frequencies = 384 terms) + one band sum per
+# band and g-vector (over 16 columns x 3 frequencies = 48 terms).
+FP64_PIPE_OPS_PER_TERM = 3.0 + 41.0 / 384 + 1.0 / 48
+# ncu, sch_fp64y_kernel, 128-band capture of the production instance
+# (--set full): dram__bytes_read.sum + dram__bytes_write.sum per term, and
+# sm__pipe_fp64_cycles_active over elapsed cycles.  Traffic scales with the
+# band blocks, so the per-term figure carries to the 512-band launch.
+FP64_DRAM_BYTES_PER_TERM = 0.1644
+FP64_PIPE_ACTIVE_NCU = 0.945
+# FP32 pipe operations of sch_mixedy_kernel per term: 4 FFMA (complex
+# multiply-add) + the float-float fold of each accumulator every 8 g-vectors
+# (2 x 7 operations / 8) + the shared frequency factor (~10 per column,
+# g-vector and frequency over 64 bands).
+MIXED_FP32_OPS_PER_TERM = 4.0 + 14.0 / 8 + 10.0 / 64
 
 
 FF_SHAPE = (512, 16384, 820, 15)  # number_bands, ncouls, ngpown, nfreq
+
+
+def library_tensor_rates(torch, n=8192, reps=10):
+    """Dense tensor-core rates of this GPU through the vendor library, for
+    the choice of slice type of the split contraction: BF16 (torch.matmul)
+    and INT8 with INT32 accumulation (torch._int_mm), n^3 GEMMs, best of
+    `reps` (CUDA events).  An INT8 split needs about twice the products of
+    the BF16 split for the same accuracy (7-bit signed slices against 8-bit
+    significands), so it pays only where INT8 runs at more than twice the
+    BF16 rate."""
+    out = {"n": n}
+    for name, make, fn in (
+            ("bf16_tflops", lambda: torch.randn(n, n, device="cuda", dtype=torch.bfloat16), torch.matmul),
+            ("int8_tops", lambda: torch.randint(-64, 64, (n, n), device="cuda", dtype=torch.int8),
+             getattr(torch, "_int_mm", None))):
+        if fn is None:
+            out[name] = None
+            continue
+        try:
+            a, b = make(), make()
+            fn(a, b)
+            best = float("inf")
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn(a, b)
+                e1.record()
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            out[name] = round(2.0 * n ** 3 / (best * 1e-3) / 1e12, 1)
+            del a, b
+        except RuntimeError as exc:  # no INT8 GEMM for this device in the library
+            out[name] = None
+            out[name + "_error"] = str(exc).splitlines()[0][:200]
+    torch.cuda.empty_cache()
+    if out.get("bf16_tflops") and out.get("int8_tops"):
+        out["int8_over_bf16"] = round(out["int8_tops"] / out["bf16_tflops"], 3)
+    return out
 
 
 def bf16_peak():
@@ -328,6 +395,14 @@ def run_ff(S, W, torch, dist, world, stream, sptr, args):
                      "status": plan.status(sptr)}
         outs[name] = out.cpu().numpy().view(np.complex128)
         plan.close()
+    ref = golden("config_ff_schdt.npz") if FF_SHAPE == (512, 16384, 820, 15) else None
+    if ref is not None:
+        o = ref["schdt"].reshape(-1)
+        for name in outs:
+            d = outs[name] - o
+            res[name]["rel_err_vs_oracle"] = {
+                "normwise": float(np.linalg.norm(d) / np.linalg.norm(o)),
+                "max_elementwise": float((np.abs(d) / np.abs(o)).max())}
     d = outs["ozaki_bf16"] - outs["fp64"]
     res["ozaki_bf16"]["rel_err_vs_fp64"] = {
         "normwise": float(np.linalg.norm(d) / np.linalg.norm(outs["fp64"])),
@@ -339,7 +414,7 @@ def run_ff(S, W, torch, dist, world, stream, sptr, args):
         "peak": peak, "unit": "TFLOP/s", "frac": round(res["ozaki_bf16"]["tensor_tflops"] / peak, 4),
         "peak_source": src,
         "note": "achieved = BF16 tensor work (6 slice products of the complex-as-real GEMM, 48 M N K flop) "
-                "over the GEMM launch's CUDA-event time; profiles/ozaki_gemm_ff_4096.md"}
+                "over the GEMM launch's CUDA-event time"}
     res["speedup_ozaki_vs_fp64"] = round(res["ozaki_bf16"]["value"] / res["fp64"]["value"], 1)
     del epsr, aqsn, aqsm
     torch.cuda.empty_cache()
@@ -554,6 +629,22 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
                      "ms_per_step": round(ms / steps, 3), "steps": steps, "terms_per_step": terms,
                      "items": items, "kernels_per_step": launches, "status": st}
         b.close()
+    ref = golden("config_gpp_batched.npz")
+    if ref is not None:
+        off = ref["n1_offsets"]
+        for name in outs:
+            worst, over, n1_worst = 0.0, 0, 0.0
+            for i, o in enumerate(outs[name]):
+                for k, key in ((0, "achtemp"), (1, "asxtemp")):
+                    e = np.abs(o[k] - ref[key][i]) / np.abs(ref[key][i])
+                    worst = max(worst, float(e.max()))
+                    over += int(np.sum(e > (1e-12 if name == "fp64" else 1e-6)))
+                r1 = ref["acht_n1_loc"][off[i]:off[i + 1]]
+                n1_worst = max(n1_worst, float(np.linalg.norm(o[2] - r1) / np.linalg.norm(r1)))
+            res[name]["rel_err_vs_oracle"] = {"max": worst, "outputs_over_bar": over,
+                                              "bar": 1e-12 if name == "fp64" else 1e-6,
+                                              "outputs": 6 * len(outs[name]),
+                                              "acht_n1_loc_normwise_max": n1_worst}
     for name in ("mixed", "tensor"):
         worst, over = 0.0, 0
         for a, m in zip(outs["fp64"], outs[name]):
@@ -616,6 +707,7 @@ def run_ours(args, rank, world, local_rank):
             print(json.dumps({"halfsum": res}), flush=True)
         return 0
     fp64_peak, fp32_peak = S.measure_fma_peaks(sptr)
+    lib_rates = None if args.no_ff else library_tensor_rates(torch)
     import replicas
     inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
     plan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_FP64)
@@ -635,8 +727,11 @@ def run_ours(args, rank, world, local_rank):
     ms_step = ms / args.steps
     value = terms * world / (ms_step * 1e-3) / 1e9
     main_s = kt["main_ms"] / max(1, kt["executions"]) * 1e-3
-    achieved = FLOP_PER_TERM * terms / main_s / 1e12
-    tpt = profile_traffic_per_term()
+    algorithmic_tflops = FLOP_PER_TERM * terms / main_s / 1e12
+    pipe_tflops = 2 * FP64_PIPE_OPS_PER_TERM * terms / main_s / 1e12
+    production = (NB, NVB, NC, NPG) == PRODUCTION
+    ref_prod = golden("config_gpp_production.npz") if production else None
+    ref_stress = golden("config_gpp_stress.npz") if production else None
 
     # ---- end to end through the host C ABI (pinned host buffers)
     host = {k: torch.empty(getattr(inst, k).numel(), dtype=torch.float64, pin_memory=True)
@@ -687,6 +782,7 @@ def run_ours(args, rank, world, local_rank):
                  "acht_n1_loc_normwise": float(np.linalg.norm(mixed_out[2] - fp64_out[2]) /
                                                np.linalg.norm(fp64_out[2]))}
     mixed_main_s = mkt["main_ms"] / max(1, mkt["executions"]) * 1e-3
+    mixed_pipe = 2 * MIXED_FP32_OPS_PER_TERM * terms / mixed_main_s / 1e12
 
     # ---- tensor-core form on the same inputs
     tplan = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=S.PREC_TENSOR)
@@ -725,6 +821,15 @@ def run_ours(args, rank, world, local_rank):
     sinst.run(tplan, sptr)
     stc = sinst.outputs()
     tensor_stress_err = {"achtemp": rel(stc[0], s64[0]), "asxtemp": rel(stc[1], s64[1])}
+    oracle = None
+    if ref_prod is not None and ref_stress is not None:
+        forms = {"fp64": (fp64_out, s64), "mixed": (mixed_out, smx), "tensor": (tensor_out, stc)}
+        oracle = {k: {"production": err_vs_oracle(a, ref_prod), "stress": err_vs_oracle(b, ref_stress)}
+                  for k, (a, b) in forms.items()}
+        for k, v in oracle.items():
+            v["max"] = max(v["production"]["max"], v["stress"]["max"])
+            v["bar"] = 1e-12 if k == "fp64" else 1e-6
+            v["within_bar"] = v["max"] <= v["bar"]
     tplan.close()
     del sinst
     plan.close()
@@ -755,42 +860,44 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": (round(e2e_value, 4) if e2e_steps else None), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                 "path": "sigma_gpp_fp64 host C ABI, pinned buffers", "matches_device_path": e2e_match},
-        "roofline": {"bound": "fp64", "kernel": "sch_fp64y_kernel",
-                     "achieved": round(achieved, 4), "peak": round(fp64_pipe_peak, 4), "unit": "TFLOP/s",
-                     "frac": round(achieved / fp64_pipe_peak, 4),
-                     "traffic": (round(tpt * terms) if tpt else None),
-                     "flop_per_term": FLOP_PER_TERM,
+        "roofline": {"bound": "fp64_pipe", "kernel": "sch_fp64y_kernel",
+                     "achieved": round(pipe_tflops, 4), "peak": round(fp64_pipe_peak, 4), "unit": "TFLOP/s",
+                     "frac": round(pipe_tflops / fp64_pipe_peak, 4),
+                     "traffic": round(FP64_DRAM_BYTES_PER_TERM * terms),
                      "kernel_ms_per_launch": round(main_s * 1e3, 3),
+                     "fp64_pipe_ops_per_term": round(FP64_PIPE_OPS_PER_TERM, 4),
                      "peak_source": f"FP64 pipe 2 DFMA/clk/SM x {sms} SMs x {clock_mhz:.0f} MHz "
-                                    "(SM clock sampled during the timed region); the driver's peak file "
-                                    "has no FP64 figure; dependent-FMA probe on this device: "
+                                    "(SM clock sampled during the timed region; the measured-peaks file "
+                                    "has no FP64 figure); dependent-FMA probe on this device: "
                                     f"{fp64_peak:.3f} TFLOP/s",
-                     "fp64_pipe_utilisation_ncu": profile_value("fp64_pipe_utilisation"),
-                     "fp64_pipe_ops_per_term": FP64_PIPE_OPS_PER_TERM,
-                     "pipe_ops_frac": round(FP64_PIPE_OPS_PER_TERM * terms / main_s / (fp64_pipe_peak / 2 * 1e12), 4),
-                     "note": "achieved counts the reference's 27 flop per term; with one frequency set "
-                             "for all bands the kernel forms the frequency factor once per column and "
-                             "g-vector and spends 3 DFMA per term (three-product complex multiply-add), "
-                             "so frac exceeds 1; pipe_ops_frac is "
-                             "the FP64 pipe occupancy those operations imply and "
-                             "fp64_pipe_utilisation_ncu the measured one "
-                             "(profiles/gpp_sch_fp64y_128bands.md)"},
+                     "ncu_fp64_pipe_active": FP64_PIPE_ACTIVE_NCU,
+                     "algorithmic": {"flop_per_term": FLOP_PER_TERM,
+                                     "tflops": round(algorithmic_tflops, 4),
+                                     "note": "the reference's 27 flop per term (its own formulation, which "
+                                             "rebuilds the frequency factor for every band) at the measured "
+                                             "term rate: a rate, not a pipe fraction"},
+                     "note": "achieved = FP64 pipe work (2 flop per DFMA) of the kernel's own algorithm: "
+                             "with one frequency set for all bands the frequency factor is formed once per "
+                             "column and g-vector, and every term is one complex multiply-add as three "
+                             "real products; traffic = ncu DRAM bytes per term x terms"},
+        "rel_err_vs_oracle": oracle,
         "mixed": {"value": round(mixed_value, 4), "unit": UNIT,
                   "speedup_vs_fp64": round(mixed_value / value, 3),
                   "ms_per_step": round(ms_mixed / msteps, 3),
                   "kernel_ms_per_launch": round(mixed_main_s * 1e3, 3),
                   "rel_err_vs_fp64": mixed_err, "stress_rel_err_vs_fp64": stress_err,
                   "max_rel_err": worst, "within_1e-6": worst <= 1e-6,
-                  "roofline": {"bound": "fp32", "kernel": "sch_mixedy_kernel",
-                               "achieved": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12, 3),
+                  "roofline": {"bound": "fp32_pipe", "kernel": "sch_mixedy_kernel",
+                               "achieved": round(mixed_pipe, 3),
                                "peak": round(fp32_pipe_peak, 3), "unit": "TFLOP/s",
-                               "frac": round(FLOP_PER_TERM * terms / mixed_main_s / 1e12 / fp32_pipe_peak, 4),
+                               "frac": round(mixed_pipe / fp32_pipe_peak, 4),
+                               "fp32_pipe_ops_per_term": round(MIXED_FP32_OPS_PER_TERM, 4),
+                               "algorithmic_tflops_27_flop_per_term":
+                                   round(FLOP_PER_TERM * terms / mixed_main_s / 1e12, 3),
                                "peak_source": "FP32 pipe 128 FFMA/clk/SM at the sampled SM clock",
-                               "note": "achieved counts the reference's 27 flop per term; with one "
-                                       "frequency set for all bands the kernel forms the frequency "
-                                       "factor once per column and g-vector and spends 4 FFMA per term "
-                                       "on the band sum, so frac exceeds 1 "
-                                       "(profiles/gpp_sch_mixedy_64bands.md)"}},
+                               "note": "achieved = FP32 pipe work (2 flop per FFMA) of the kernel's own "
+                                       "algorithm: 4 FFMA per term for the complex multiply-add, the "
+                                       "float-float fold every 8 g-vectors and the shared frequency factor"}},
         "tensor": {"value": round(tensor_value, 4), "unit": UNIT,
                    "speedup_vs_fp64": round(tensor_value / value, 3),
                    "ms_per_step": round(ms_tensor / tsteps, 3),
@@ -810,7 +917,8 @@ def run_ours(args, rank, world, local_rank):
         "peaks_measured": {"fp64_fma_probe_tflops": round(fp64_peak, 4),
                            "fp32_fma_probe_tflops": round(fp32_peak, 3),
                            "fp64_pipe_tflops_at_clock": round(fp64_pipe_peak, 4),
-                           "fp32_pipe_tflops_at_clock": round(fp32_pipe_peak, 3)},
+                           "fp32_pipe_tflops_at_clock": round(fp32_pipe_peak, 3),
+                           "library_tensor_rates": lib_rates},
         "clocks": clk,
         "gpu_launches": int(kt["launches"]) * args.steps,
     }
@@ -852,11 +960,12 @@ def main():
     ap.add_argument("--batch-fp64-steps", type=int, default=2)
     ap.add_argument("--only-batched", action="store_true",
                     help="run the batched measurement alone (profiling captures)")
-    ap.add_argument("--bands", type=int, default=NB,
-                    help="number_bands of the instance (512 = the production shape; smaller only "
-                         "for profiling captures)")
+    ap.add_argument("--gpp-shape", default=None,
+                    help="number_bands,nvband,ncouls,nodes_per_group of the GPP instance (default the "
+                         "production 512,2,32768,20; smaller only for profiling captures)")
     args = ap.parse_args()
-    set_bands(args.bands)
+    if args.gpp_shape:
+        set_shape(*(int(x) for x in args.gpp_shape.split(",")))
     if args.ff_shape:
         global FF_SHAPE
         FF_SHAPE = tuple(int(x) for x in args.ff_shape.split(","))
