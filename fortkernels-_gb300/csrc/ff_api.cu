@@ -55,7 +55,7 @@ namespace sigma {
 // left out).  Shared by the FF contraction and the static remainders.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
                   const std::vector<int>& igp_of, int mode, void* shared_tiles,
-                  const int* row_kend) {
+                  const int* row_kend, int split_tiles_hint) {
   *out = nullptr;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -86,7 +86,7 @@ int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, 
   p->grid = sms * per_sm;
   OzakiTables tables;
   if (mode == SIGMA_FF_OZAKI_BF16) {
-    ozaki_size(p->oz, d, p->grid, row_kend, &tables);
+    ozaki_size(p->oz, d, p->grid, row_kend, &tables, split_tiles_hint);
     if (p->oz.max_seg > ozaki_max_segments()) {  // ngpown below ~18: too many frequencies per tile
       delete p;
       return SIGMA_ERR_UNSUPPORTED;
@@ -211,6 +211,7 @@ namespace sigma {
 const OzakiPrep* ff_plan_ozaki(sigma_ff_plan plan) {
   return plan && plan->mode == SIGMA_FF_OZAKI_BF16 ? &plan->oz : nullptr;
 }
+const FfDev* ff_plan_dev(sigma_ff_plan plan) { return plan ? &plan->dev : nullptr; }
 
 int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes) {
   FfDev d{};

@@ -90,11 +90,10 @@ __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz
   }
 }
 
-// B' rows: [Re | -Im] (real part of the product) and [Im | Re] (imaginary part).
-__global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz) {
-  const long long total = (long long)oz.n_col_blocks * oz.kt * 64 * kChunksPerRow;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
+// B' rows: [Re | -Im] (real part of the product) and [Im | Re] (imaginary part);
+// element t of n_col_blocks * kt * 64 * kChunksPerRow.
+__device__ __forceinline__ void prep_b_elem(const FfDev& p, const OzakiPrep& oz, long long t) {
+  {
     const int ch = (int)(t % kChunksPerRow);
     const int nl = (int)((t / kChunksPerRow) & 63);
     const long long rest = t / (kChunksPerRow * 64);
@@ -120,13 +119,20 @@ __global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz
     oz_put_row_chunk(hi, 64 + nl, ch, re);
   }
 }
+__device__ __forceinline__ long long prep_b_count(const OzakiPrep& oz) {
+  return (long long)oz.n_col_blocks * oz.kt * 64 * kChunksPerRow;
+}
+__global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz) {
+  const long long total = prep_b_count(oz);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x)
+    prep_b_elem(p, oz, t);
+}
 
 // wtab[g][n] = aqsm[n][igp(g)] * weight(g), rounded to FP32 from the FP64
 // product (the value the epilogue used to form per lane from global loads).
-__global__ void __launch_bounds__(256) ozaki_weights_kernel(FfDev p, OzakiPrep oz) {
-  const long long total = (long long)oz.ng * oz.nb_pad;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void weights_elem(const FfDev& p, const OzakiPrep& oz, long long t) {
+  {
     const int g = (int)(t / oz.nb_pad), n = (int)(t % oz.nb_pad);
     const int igp = p.igp_of[g];
     float2 v = make_float2(0.f, 0.f);
@@ -138,6 +144,38 @@ __global__ void __launch_bounds__(256) ozaki_weights_kernel(FfDev p, OzakiPrep o
     oz.wtab[t] = v;
     if (oz.stab && n == 0) oz.stab[g] = igp >= 0 ? (float)(p.vfac2 * p.vcoul2[igp]) : 0.f;
   }
+}
+__global__ void __launch_bounds__(256) ozaki_weights_kernel(FfDev p, OzakiPrep oz) {
+  const long long total = (long long)oz.ng * oz.nb_pad;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x)
+    weights_elem(p, oz, t);
+}
+
+// Group forms: each job owns a contiguous range of blocks (found once per
+// block), its threads stride over the job's elements.
+__device__ __forceinline__ int group_job_of_block(const OzGroup& g, int b, bool weights) {
+  int lo = 0, hi = g.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const int off = weights ? g.jobs[mid].w_blk_off : g.jobs[mid].b_blk_off;
+    if (off <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__global__ void __launch_bounds__(256) ozaki_group_prep_b_kernel(OzGroup g) {
+  const OzGroupJob& J = g.jobs[group_job_of_block(g, blockIdx.x, false)];
+  const long long total = prep_b_count(J.oz);
+  for (long long t = (long long)(blockIdx.x - J.b_blk_off) * blockDim.x + threadIdx.x; t < total;
+       t += (long long)J.b_blks * blockDim.x)
+    prep_b_elem(J.d, J.oz, t);
+}
+__global__ void __launch_bounds__(256) ozaki_group_weights_kernel(OzGroup g) {
+  const OzGroupJob& J = g.jobs[group_job_of_block(g, blockIdx.x, true)];
+  const long long total = (long long)J.oz.ng * J.oz.nb_pad;
+  for (long long t = (long long)(blockIdx.x - J.w_blk_off) * blockDim.x + threadIdx.x; t < total;
+       t += (long long)J.w_blks * blockDim.x)
+    weights_elem(J.d, J.oz, t);
 }
 
 struct OzItem {
@@ -167,15 +205,45 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 __device__ __forceinline__ void drain_barrier() {
   asm volatile("bar.sync 1, 128;" ::: "memory");
 }
-// the MMA warp and the gate warp meet once per tile
-__device__ __forceinline__ void mma_gate_sync() {
-  asm volatile("bar.sync 2, 64;" ::: "memory");
+// The MMA warp and the gate warp meet once per kGateTiles tiles; the
+// barrier's OR reduction carries the gate warp's failure flag to the MMA
+// warp (a shared-memory flag read by the issuing thread between its MMAs
+// would stall the tensor pipe).
+__device__ __forceinline__ bool mma_gate_sync(bool flag) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, 2, 64, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)flag)
+      : "memory");
+  return r != 0;
 }
 
-__global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWork w, OzakiPrep oz) {
+// One item of a group's table (kGroup): its job, tile run and partial slot.
+__device__ __forceinline__ OzItem oz_group_item(const OzGroup& g, int item, int& job) {
+  const int4 e = g.items[item];
+  job = e.x;
+  const OzakiPrep& oz = g.jobs[e.x].oz;
+  OzItem t;
+  t.rb = e.y >> 16;
+  t.cb = e.y & 0xFFFF;
+  t.t0 = e.z;
+  t.nst = e.w & 0xFFFF;
+  t.pidx = ((size_t)t.rb * oz.n_col_blocks + t.cb) * oz.max_pieces + (e.w >> 16);
+  return t;
+}
+
+// kGroup: the items of every job of the group `g` (one table, one static
+// schedule), each item with its own job's operands and epilogue; else the
+// one contraction (p, oz).  The roles and their waits are the same.
+template <bool kGroup>
+__global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWork w, OzakiPrep oz, OzGroup grp) {
   extern __shared__ unsigned char smem_raw[];
-  // full[kStages], empty[kStages], accf[2], acce[2]
-  __shared__ __align__(8) unsigned long long bars[2 * kStages + 4];
+  // full[kStages], empty[kStages], accf[2], acce[2], done
+  __shared__ __align__(8) unsigned long long bars[2 * kStages + 5];
   __shared__ uint32_t tmem_slot;
   __shared__ float2 s_red[2][4][kMaxSeg][kOzCols];
 
@@ -184,13 +252,16 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[kStages]);
   const uint32_t accf0 = smem_u32(&bars[2 * kStages]), acce0 = smem_u32(&bars[2 * kStages + 2]);
-  const int two_kt = 2 * oz.kt;
+  const int n_items = kGroup ? grp.total : oz.n_items;
+  int* const status = kGroup ? grp.status : w.status;
 
   if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), kTmemCols);
+  const uint32_t done0 = smem_u32(&bars[2 * kStages + 4]);
   if (tid == 0) {
     for (int i = 0; i < 2 * kStages + 2; ++i) mbar_init(smem_u32(&bars[i]), 1);
     mbar_init(acce0, 4);
     mbar_init(acce0 + 8u, 4);
+    mbar_init(done0, 1);
     fence_mbar_init();
   }
   tc_fence_before();
@@ -202,15 +273,23 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
     // ------------------------------------------------ bulk copies into the stage ring
     if (lane == 0) {
       uint32_t g = 0;  // tiles issued by this CTA
-      for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
-        const OzItem it = oz_decode(oz, item);
+      bool ok = true;
+      for (int item = blockIdx.x; ok && item < n_items; item += gridDim.x) {
+        int job = 0;
+        const OzItem it = kGroup ? oz_group_item(grp, item, job) : oz_decode(oz, item);
         const int nst = it.nst;
-        const unsigned char* a_src = oz.a_tiles + ((size_t)it.rb * two_kt + it.t0) * kOperandBytes;
-        const unsigned char* b_src = oz.b_tiles + ((size_t)it.cb * two_kt + it.t0) * kOperandBytes;
+        const unsigned char* at = kGroup ? grp.jobs[job].oz.a_tiles : oz.a_tiles;
+        const unsigned char* bt = kGroup ? grp.jobs[job].oz.b_tiles : oz.b_tiles;
+        const int two_kt = 2 * (kGroup ? grp.jobs[job].oz.kt : oz.kt);
+        const unsigned char* a_src = at + ((size_t)it.rb * two_kt + it.t0) * kOperandBytes;
+        const unsigned char* b_src = bt + ((size_t)it.cb * two_kt + it.t0) * kOperandBytes;
         for (int s = 0; s < nst; ++s, ++g) {
           const uint32_t b = g % kStages, use = g / kStages;
           // stage b is free once the MMAs of its previous tile have completed
-          if (use > 0) mbar_wait(empty0 + 8u * b, (use - 1) & 1u, w.status);
+          if (use > 0 && !mbar_wait(empty0 + 8u * b, (use - 1) & 1u, status)) {
+            ok = false;  // no further copies
+            break;
+          }
           const uint32_t bar = full0 + 8u * b;
           const uint32_t dst = sbase + b * kStageBytes;
           mbar_expect_tx(bar, kStageBytes);
@@ -218,6 +297,11 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
           bulk_load(dst + kOperandBytes, b_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
         }
       }
+      // after a failure: the copies of the last (up to kStages) tiles may
+      // still be landing; wait for them before the CTA releases its ring
+      if (!ok)
+        for (uint32_t t = g > (uint32_t)kStages ? g - kStages : 0u; t < g; ++t)
+          mbar_wait_own(full0 + 8u * (t % kStages), (t / kStages) & 1u);
     }
     __syncwarp();
   } else if (warp == kGateWarp) {
@@ -227,27 +311,30 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
     // at a named barrier once per kGateTiles tiles.  The issuing thread itself never polls shared
     // memory: a poll between its MMAs stalls the tensor pipe (measured: 89
     // instead of 64 cycles per MMA).
+    // After a wait gives up it keeps meeting the MMA warp at the same named
+    // barriers (whose count must match) without waiting, and passes the
+    // failure on through them so the MMA warp issues nothing more.
     uint32_t ph_acce0 = 0, ph_acce1 = 0;
-    bool used0 = false, used1 = false;
+    bool used0 = false, used1 = false, failed = false;
     uint32_t g = 0, gc = 0;
-    for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
-      const int nst = oz_decode(oz, item).nst;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+      const int nst = kGroup ? (grp.items[item].w & 0xFFFF) : oz_decode(oz, item).nst;
       for (int s = 0; s < nst; ++s, ++g) {
         const int cs = s % kChunkStages;
         const uint32_t tb = gc & 1u;
-        if (lane == 0) {
+        if (lane == 0 && !failed) {
           if (cs == 0) {  // first tile of an accumulator lifetime: pair tb must be drained
             if (tb == 0 && used0) {
-              mbar_wait(acce0, ph_acce0, w.status);
+              failed = !mbar_wait(acce0, ph_acce0, status);
               ph_acce0 ^= 1u;
             }
             if (tb == 1 && used1) {
-              mbar_wait(acce0 + 8u, ph_acce1, w.status);
+              failed = failed || !mbar_wait(acce0 + 8u, ph_acce1, status);
               ph_acce1 ^= 1u;
             }
           }
           const uint32_t b = g % kStages;
-          mbar_wait(full0 + 8u * b, (g / kStages) & 1u, w.status);
+          failed = failed || !mbar_wait(full0 + 8u * b, (g / kStages) & 1u, status);
         }
         if (cs == 0) {
           if (tb == 0) used0 = true; else used1 = true;
@@ -255,27 +342,29 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
         if (cs == kChunkStages - 1 || s == nst - 1) ++gc;
         if (s % kGateTiles == kGateTiles - 1 || s == nst - 1) {
           __syncwarp();
-          mma_gate_sync();
+          mma_gate_sync(failed);
         }
       }
     }
     // every accumulator pair in use drained
-    if (lane == 0) {
-      if (used0) mbar_wait(acce0, ph_acce0, w.status);
-      if (used1) mbar_wait(acce0 + 8u, ph_acce1, w.status);
+    if (lane == 0 && !failed) {
+      if (used0) mbar_wait(acce0, ph_acce0, status);
+      if (used1) mbar_wait(acce0 + 8u, ph_acce1, status);
     }
     __syncwarp();
   } else if (warp == kMmaWarp) {
     // ------------------------------------------------ tensor-core issue (lane 0)
     uint32_t g = 0;   // tiles consumed by this CTA
     uint32_t gc = 0;  // accumulator lifetimes started
-    for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
-      const int nst = oz_decode(oz, item).nst;
+    bool failed = false;
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+      const int nst = kGroup ? (grp.items[item].w & 0xFFFF) : oz_decode(oz, item).nst;
       for (int s = 0; s < nst; ++s, ++g) {
         const int cs = s % kChunkStages;
         const uint32_t tb = gc & 1u;
-        if (s % kGateTiles == 0) mma_gate_sync();  // stages full, accumulator pair free
-        if (lane == 0) {
+        // stages full, accumulator pair free (or the gate warp gave up)
+        if (s % kGateTiles == 0) failed = mma_gate_sync(false) || failed;
+        if (lane == 0 && !failed) {
           tc_fence_after();
           const uint32_t b = g % kStages;
           const uint32_t a_addr = sbase + b * kStageBytes;
@@ -304,14 +393,24 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
         __syncwarp();
       }
     }
+    // after a failure: the MMAs already issued complete before the tensor
+    // memory is released
+    if (lane == 0 && failed) {
+      mma_commit(done0);
+      mbar_wait_own(done0, 0);
+    }
+    __syncwarp();
   } else {
     // ------------------------------------------------ drain + epilogue (warps 0-3)
     uint32_t ph_accf0 = 0, ph_accf1 = 0;
     uint32_t gc = 0;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    const int rows = p.nf * p.ng;
-    for (int item = blockIdx.x; item < oz.n_items; item += gridDim.x) {
-      const OzItem it = oz_decode(oz, item);
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+      int job = 0;
+      const OzItem it = kGroup ? oz_group_item(grp, item, job) : oz_decode(oz, item);
+      // the item's contraction: its shape, epilogue factors and partial slots
+      const int e_nf = kGroup ? grp.jobs[job].d.nf : p.nf, e_ng = kGroup ? grp.jobs[job].d.ng : p.ng;
+      const int rows = e_nf * e_ng;
       const int nchunks = (it.nst + kChunkStages - 1) / kChunkStages;
       float acc[128];
 #pragma unroll
@@ -319,10 +418,10 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
       for (int c = 0; c < nchunks; ++c) {
         const uint32_t tb = gc & 1u;
         if (tb == 0) {
-          mbar_wait(accf0, ph_accf0, w.status);
+          mbar_wait(accf0, ph_accf0, status);
           ph_accf0 ^= 1u;
         } else {
-          mbar_wait(accf0 + 8u, ph_accf1, w.status);
+          mbar_wait(accf0 + 8u, ph_accf1, status);
           ph_accf1 ^= 1u;
         }
         tc_fence_after();
@@ -343,13 +442,16 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
       // epilogue: row R of this lane, 64 bands; tempz * weight * conj(aqsm[n1][igp])
       const int R = it.rb * kOzRows + warp * 32 + lane;
       const bool row_ok = R < rows;
-      const int f = row_ok ? R / p.ng : 0;
-      const int g = row_ok ? R % p.ng : 0;
-      const int f_first = (it.rb * kOzRows) / p.ng;
-      const int f_last = (min(it.rb * kOzRows + kOzRows, rows) - 1) / p.ng;
+      const int f = row_ok ? R / e_ng : 0;
+      const int g = row_ok ? R % e_ng : 0;
+      const int f_first = (it.rb * kOzRows) / e_ng;
+      const int f_last = (min(it.rb * kOzRows + kOzRows, rows) - 1) / e_ng;
+      const float2* e_wtab = kGroup ? grp.jobs[job].oz.wtab : oz.wtab;
+      const int e_nbpad = kGroup ? grp.jobs[job].oz.nb_pad : oz.nb_pad;
+      const float* e_stab = kGroup ? grp.jobs[job].oz.stab : oz.stab;
       // the row's 64 factors: 32 contiguous 16-byte loads in four batches
       const float4* wrow =
-          reinterpret_cast<const float4*>(oz.wtab + (size_t)g * oz.nb_pad + (size_t)it.cb * kOzCols);
+          reinterpret_cast<const float4*>(e_wtab + (size_t)g * e_nbpad + (size_t)it.cb * kOzCols);
 #pragma unroll
       for (int n0 = 0; n0 < 64; n0 += 16) {
         float4 wv[8];
@@ -368,8 +470,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
         }
       }
       // one or two outputs: the second's rows carry the extra column factor stab
-      const bool two = oz.stab != nullptr;
-      const float sc = (two && row_ok) ? oz.stab[g] : 0.f;
+      const bool two = e_stab != nullptr;
+      const float sc = (two && row_ok) ? e_stab[g] : 0.f;
       for (int seg = 0; seg <= f_last - f_first; ++seg) {
         const bool mine = row_ok && (f - f_first) == seg;
         // 16 bands at a time: a reduce-scatter butterfly over the warp leaves
@@ -415,7 +517,10 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
           sr += (double)s_red[out][q][seg][n].x;
           si += (double)s_red[out][q][seg][n].y;
         }
-        (out ? oz.partial2 : oz.partial)[(it.pidx * oz.max_seg + seg) * kOzCols + n] = make_double2(sr, si);
+        double2* part = kGroup ? (out ? grp.jobs[job].oz.partial2 : grp.jobs[job].oz.partial)
+                               : (out ? oz.partial2 : oz.partial);
+        const int max_seg = kGroup ? grp.jobs[job].oz.max_seg : oz.max_seg;
+        part[(it.pidx * max_seg + seg) * kOzCols + n] = make_double2(sr, si);
       }
       drain_barrier();
     }
@@ -428,10 +533,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
 
 // schDt[n1][ifreq]: one warp per entry, fixed-order compensated sum over the
 // row blocks that hold frequency ifreq and over their work entries.
-__global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, const double2* partial, double2* schdt) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= p.nb * p.nf) return;
+__device__ __forceinline__ void reduce_entry(const FfDev& p, const OzakiPrep& oz, const double2* partial,
+                                             double2* schdt, int warp, int lane) {
   const int n = warp / p.nf, f = warp % p.nf;
   const int cb = n / kOzCols, c = n % kOzCols;
   const int rb_lo = (f * p.ng) / kOzRows, rb_hi = ((f + 1) * p.ng - 1) / kOzRows;
@@ -463,9 +566,29 @@ __global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, const double2* partia
   if (lane == 0) schdt[(size_t)n * p.nf + f] = make_double2(sx.value(), sy.value());
 }
 
+__global__ void ozaki_reduce_kernel(FfDev p, OzakiPrep oz, const double2* partial, double2* schdt) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= p.nb * p.nf) return;
+  reduce_entry(p, oz, partial, schdt, warp, threadIdx.x & 31);
+}
+
+// Group form: warps r_warp_off .. + nb * nf of each job reduce its entries.
+__global__ void ozaki_group_reduce_kernel(OzGroup g) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= g.r_warps) return;
+  int lo = 0, hi = g.n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.jobs[mid].r_warp_off <= warp) lo = mid; else hi = mid - 1;
+  }
+  const OzGroupJob& J = g.jobs[lo];
+  reduce_entry(J.d, J.oz, J.oz.partial, J.out, warp - J.r_warp_off, threadIdx.x & 31);
+}
+
 }  // namespace
 
-void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend, OzakiTables* tables) {
+void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend, OzakiTables* tables,
+                int split_tiles_hint) {
   oz.kt = (d.nc + kOzKTile - 1) / kOzKTile;
   const int rows = d.nf * d.ng;
   oz.n_row_blocks = (rows + kOzRows - 1) / kOzRows;
@@ -487,6 +610,7 @@ void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend, Oz
   const long long want = 20LL * grid * two_kt;
   const long long have = std::max(1LL, active * oz.n_col_blocks);
   long long s = (want + have - 1) / have;
+  if (split_tiles_hint > 0) s = (two_kt + split_tiles_hint - 1) / split_tiles_hint;
   if (s < 1) s = 1;
   if (s > two_kt) s = two_kt;
   oz.split_tiles = (int)((two_kt + s - 1) / s);
@@ -632,9 +756,43 @@ cudaError_t launch_ozaki_zero_rows(const OzakiPrep& oz, int rows, cudaStream_t s
 cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& oz, int grid,
                               cudaStream_t s) {
   cudaError_t e =
-      cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+      cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
   if (e != cudaSuccess) return e;
-  ozaki_gemm_kernel<<<grid, kOzThreads, kSmemBytes, s>>>(d, w, oz);
+  ozaki_gemm_kernel<false><<<grid, kOzThreads, kSmemBytes, s>>>(d, w, oz, OzGroup{});
+  return cudaGetLastError();
+}
+
+void ozaki_group_items(int job, const OzakiPrep& oz, const OzakiTables& t, std::vector<int4>& items) {
+  for (int it = 0; it < oz.n_items; ++it) {
+    const int4 e = t.entries[it / oz.n_col_blocks];
+    const int cb = it % oz.n_col_blocks;
+    items.push_back(make_int4(job, (e.x << 16) | cb, e.z, e.w | (e.y << 16)));
+  }
+}
+
+cudaError_t launch_ozaki_group_prep(const OzGroup& g, cudaStream_t s) {
+  if (g.b_blocks > 0) {
+    ozaki_group_prep_b_kernel<<<g.b_blocks, 256, 0, s>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (g.w_blocks > 0) ozaki_group_weights_kernel<<<g.w_blocks, 256, 0, s>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ozaki_group_gemm(const OzGroup& g, int grid, cudaStream_t s) {
+  if (g.total <= 0) return cudaSuccess;
+  cudaError_t e =
+      cudaFuncSetAttribute(ozaki_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  if (e != cudaSuccess) return e;
+  ozaki_gemm_kernel<true><<<std::min(grid, g.total), kOzThreads, kSmemBytes, s>>>(FfDev{}, FfWork{}, OzakiPrep{},
+                                                                                  g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ozaki_group_reduce(const OzGroup& g, cudaStream_t s) {
+  if (g.r_warps <= 0) return cudaSuccess;
+  ozaki_group_reduce_kernel<<<(g.r_warps * 32 + 255) / 256, 256, 0, s>>>(g);
   return cudaGetLastError();
 }
 

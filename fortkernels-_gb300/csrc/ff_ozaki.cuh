@@ -99,8 +99,10 @@ struct OzakiTables {
   std::vector<int4> entries;
   std::vector<int> pieces, kt_lim;
 };
+// split_tiles_hint > 0 sets the K' tiles per split (a group sizes every
+// job's items alike); otherwise about 20 items per CTA of `grid`.
 void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend = nullptr,
-                OzakiTables* tables = nullptr);
+                OzakiTables* tables = nullptr, int split_tiles_hint = 0);
 cudaError_t ozaki_upload_tables(const OzakiPrep& oz, const OzakiTables& t);
 int ozaki_max_segments();
 size_t ozaki_prep_bytes(const OzakiPrep& oz);  // slice images + partials
@@ -119,6 +121,33 @@ cudaError_t launch_ozaki_gemm(const FfDev& d, const FfWork& w, const OzakiPrep& 
                               cudaStream_t s);
 cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* schdt, cudaStream_t s,
                                 double2* schdt2 = nullptr);
+
+// A group of contractions run as one launch per stage (the batched tensor
+// form): each job is one contraction with its own operands, layout and
+// partial buffers; the GEMM's items of every job are listed in one table,
+// the other stages split their blocks among the jobs.
+struct OzGroupJob {
+  FfDev d;
+  OzakiPrep oz;
+  double2* out;            // [nb][nf] (reduction output)
+  int b_blk_off, b_blks;   // blocks of the B-slice stage
+  int w_blk_off, w_blks;   // blocks of the epilogue-factor stage
+  int r_warp_off;          // first warp of the reduction stage (nb * nf warps)
+};
+struct OzGroup {
+  const OzGroupJob* jobs;  // device array
+  int n_jobs;
+  const int4* items;       // [total]: job, row block << 16 | band block, first K' tile, tiles | piece << 16
+  int total;
+  int b_blocks, w_blocks, r_warps;
+  int* status;
+};
+// Host side of a group: the item table of job `job` appended to `items`
+// (its entries in the order of ozaki_size, band blocks fastest).
+void ozaki_group_items(int job, const OzakiPrep& oz, const OzakiTables& t, std::vector<int4>& items);
+cudaError_t launch_ozaki_group_prep(const OzGroup& g, cudaStream_t s);
+cudaError_t launch_ozaki_group_gemm(const OzGroup& g, int grid, cudaStream_t s);
+cudaError_t launch_ozaki_group_reduce(const OzGroup& g, cudaStream_t s);
 
 __device__ __forceinline__ void oz_put_a(const OzakiPrep& oz, int R, int k0, const float (&re)[8],
                                          const float (&im)[8]) {

@@ -17,9 +17,11 @@ namespace sigma {
 // row_kend (split-BF16 form only, nullable): per I_epsR row (ifreq * ngpown
 // + my_igp) the K from which the row is zero in every execution; the
 // contraction skips those K tiles.
+// split_tiles_hint (split-BF16 form, > 0): K' tiles per work split, so
+// that the plans of a group have items of about the same size.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
                   const std::vector<int>& igp_of, int mode, void* shared_tiles = nullptr,
-                  const int* row_kend = nullptr);
+                  const int* row_kend = nullptr, int split_tiles_hint = 0);
 int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes);
 
 // The split-BF16 plan's operand layout (slice images, K tiles, row limits),
@@ -27,6 +29,9 @@ int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size
 // reuse_a; nullptr for an FP64 plan.
 struct OzakiPrep;
 const OzakiPrep* ff_plan_ozaki(sigma_ff_plan plan);
+// The plan's device view (shape, column map; operand pointers unset).
+struct FfDev;
+const FfDev* ff_plan_dev(sigma_ff_plan plan);
 
 // sigma_ff_execute with the column weight vfac * vcoul[igp] (vcoul a device
 // array, or nullptr for weight 1).

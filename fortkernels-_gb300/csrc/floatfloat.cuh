@@ -9,29 +9,34 @@
 namespace sigma {
 
 // x = hi + lo: hi is x truncated to 24 significant bits (exact in FP32), lo
-// the remaining 29 bits rounded to FP32 (|x - hi - lo| <= 2^-48 |x|).  For
-// exponents where both are normal FP32 values, hi is assembled from the
-// bits and lo is one 32-bit integer conversion scaled by a power of two: no
-// conversion from a 64-bit operand (with those, an FP32 kernel kept GB300's
-// FP64 pipe half busy).
+// the remaining 29 bits rounded to FP32 (|x - hi - lo| <= 2^-48 |x|), for
+// 2^-74 <= |x| < 2^128.  Integer operations only (hi assembled from the bits,
+// lo one 32-bit integer conversion scaled by a power of two): a conversion
+// from a 64-bit operand runs on GB300's FP64 pipe, at 1/64 of the FP32 rate,
+// and so would a slow path the compiler evaluates predicated off for every
+// value.  Outside that range: 2^-126 <= |x| < 2^-74 keeps hi with lo = 0
+// (error below 2^-23 |x|, far below any value that matters next to the FP32
+// forms' range); smaller magnitudes give a signed zero; |x| >= 2^128 gives
+// an infinite hi (NaN for a NaN), so such inputs show up as non-finite
+// outputs of the FP32 forms instead of wrong finite values.
 __device__ __forceinline__ void split_exact(double x, float& hi, float& lo) {
   const unsigned int whi = (unsigned int)__double2hiint(x), wlo = (unsigned int)__double2loint(x);
+  const unsigned int sign = whi & 0x80000000u;
   const int ex = (int)((whi >> 20) & 0x7FFu);
-  if (ex >= 949 && ex <= 1150) {  // 2^-74 <= |x| < 2^128
-    hi = __uint_as_float((whi & 0x80000000u) | ((unsigned int)(ex - 896) << 23) |
-                         ((whi & 0xFFFFFu) << 3) | (wlo >> 29));
-    const float m = __uint2float_rn(wlo & 0x1FFFFFFFu);    // < 2^29
-    const float scale = __uint_as_float((unsigned int)(ex - 948) << 23);  // 2^(ex - 1075)
-    lo = (whi >> 31) ? -(m * scale) : m * scale;
-    return;
+  const unsigned int mant = ((whi & 0xFFFFFu) << 3) | (wlo >> 29);  // leading 23 fraction bits
+  unsigned int hb;
+  if (ex > 1150) {
+    hb = sign | 0x7F800000u | ((ex == 2047 && ((whi & 0xFFFFFu) | wlo)) ? 0x400000u : 0u);
+  } else if (ex >= 897) {
+    hb = sign | ((unsigned int)(ex - 896) << 23) | mant;
+  } else {
+    hb = sign;
   }
-  const long long bits = __double_as_longlong(x);
-  constexpr long long kLow = (1LL << 29) - 1;
-  hi = __double2float_rn(__longlong_as_double(bits & ~kLow));
-  const int e = (int)((bits >> 52) & 0x7FF);
-  const float m = __ll2float_rn(bits & kLow);  // low 29 mantissa bits, < 2^29
-  const float scale = e > 948 ? __int_as_float((e - 948) << 23) : 0.f;  // 2^(e - 1075)
-  lo = (bits < 0) ? -(m * scale) : m * scale;
+  hi = __uint_as_float(hb);
+  const float m = __uint2float_rn(wlo & 0x1FFFFFFFu);                        // < 2^29
+  const float scale = __uint_as_float((unsigned int)max(ex - 948, 0) << 23);  // 2^(ex - 1075), or 0
+  const float l = (ex >= 949 && ex <= 1150) ? m * scale : 0.f;
+  lo = sign ? -l : l;
 }
 
 struct FF {
@@ -76,6 +81,34 @@ __device__ __forceinline__ bool ff_gt(FF x, FF y, bool& near) {
   const float d = (x.hi - y.hi) + (x.lo - y.lo);
   near = fabsf(d) <= 9.3132257e-10f * fmaxf(x.hi, y.hi);  // 2^-30
   return d > 0.f;
+}
+
+// x > y for non-negative normalised float-float values, taken on the hi
+// parts when they differ by more than 2^-21 of the larger (|lo| <= 2^-24
+// |hi| and one rounding of the difference cannot flip the sign then), else
+// with the full compare; `near` as ff_gt.  Same result as ff_gt.
+__device__ __forceinline__ bool ff_gt_fast(FF x, FF y, bool& near) {
+  const float d = x.hi - y.hi;
+  if (fabsf(d) > 4.76837158e-07f * fmaxf(x.hi, y.hi)) {  // 2^-21
+    near = false;
+    return d > 0.f;
+  }
+  return ff_gt(x, y, near);
+}
+
+// The pole-guard decisions of the FP64 path (guard_w / guard_thr /
+// guard_thr2), for the float-float kernels' rare values near a threshold.
+// Out of line so that those kernels branch to them instead of running their
+// FP64 instructions predicated off for every value.
+static __device__ __noinline__ bool keep_fp64(double wx, double a, double b) {
+  const double b2 = guard_b2(b);
+  return keep_nonneg(guard_w(wx, a, b2), guard_thr(a, b2));
+}
+// second occupied-band branch: 0 < |wdiff|^2 < |wtilde|^2 / to1
+static __device__ __noinline__ bool second_fp64(double wx, double a, double b) {
+  const double b2 = guard_b2(b);
+  const double w = guard_w(wx, a, b2);
+  return gt_nonneg(w, 0.0) && gt_nonneg(guard_thr2(a, b2), w);
 }
 
 }  // namespace sigma

@@ -1,6 +1,7 @@
 // C ABI of the GPP path: plans, device-resident execution and the
 // host-pointer drop-in for BGW-Kernels/gppKer.cpp:303-439.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -8,6 +9,7 @@
 #include "sigma_internal.cuh"
 #include "ff_plan.h"
 #include "ff_ozaki.cuh"
+#include "gpp_tensor.cuh"
 #include "runtime.h"
 
 namespace sigma {
@@ -27,6 +29,11 @@ struct sigma_gpp_plan_s {
   sigma::GppWork schmy{};     // mixed main pass for shared frequencies (shares sch's buffers)
   sigma::GppWork prepw{};     // pre-pass blocks: sch's, rounded up to even counts
   sigma_ff_plan ff = nullptr; // tensor form: the contraction plan (3 slabs = 3 frequencies)
+  // tensor form with nvband <= kFusedBands: the factor pass that also sums
+  // the occupied bands (its ssx partials in the plan's block)
+  bool fused = false;
+  sigma::FactorJob fac{};
+  int fac_grid = 0;
 
   sigma::MixedPrep prep{};    // FP32 operands of the mixed path (unused for FP64)
   void* block = nullptr;      // one device allocation for everything below
@@ -185,21 +192,38 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
                                 256);
   const size_t b_ssx = align_up(sizeof(double2) * (size_t)p->ssx.n_items * kSsxBN * kNW, 256);
   const int nc_pad = (ncouls + kCK - 1) / kCK * kCK;
-  const size_t col_elems = mixed ? (size_t)p->prepw.n_col_blocks * kBPM * nc_pad : 0;
-  const size_t band_elems = mixed ? (size_t)p->prepw.n_band_blocks * kBN * nc_pad : 0;
+  // the fused tensor factor pass needs none of the mixed form's FP32 operands
+  const bool fused = tensor && factor_fuses_ssx(nvband);
+  const size_t col_elems = mixed && !fused ? (size_t)p->prepw.n_col_blocks * kBPM * nc_pad : 0;
+  const size_t band_elems = mixed && !fused ? (size_t)p->prepw.n_band_blocks * kBN * nc_pad : 0;
   const size_t b_colA = align_up(sizeof(float4) * col_elems, 256);
   const size_t b_colB = align_up(sizeof(float2) * col_elems, 256);
   const size_t b_band = align_up(sizeof(float2) * band_elems, 256);
   const size_t b_colC = nvband > 0 ? b_colB : 0;
+  size_t b_fssx = 0;
   if (tensor) {
     int st2 = ff_plan_build(&p->ff, number_bands, ncouls, ngpown, kNW, igp_of, SIGMA_FF_OZAKI_BF16);
     if (st2 != SIGMA_OK) {
       delete p;
       return st2;
     }
+    if (fused) {
+      const OzakiPrep* oz = ff_plan_ozaki(p->ff);
+      GppDev d{};
+      d.nb = number_bands;
+      d.nvband = nvband;
+      d.nc = ncouls;
+      d.ng = ngpown;
+      p->fused = true;
+      p->fac_grid = sms * factor_blocks_per_sm();
+      factor_job_size(p->fac, d, oz->kt, p->fac_grid, 1.0);
+      p->fac.a_tiles = oz->a_tiles;
+      p->fac.item_off = 0;
+      b_fssx = align_up(factor_ssx_partial_bytes(p->fac), 256);
+    }
   }
   cudaError_t e = cudaMalloc(&p->block, b_igp + b_cnt + b_n1 + b_sch + b_ssx + b_colA + b_colB + b_band +
-                                            b_colC);
+                                            b_colC + b_fssx);
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_last_cuda_error(e, "cudaMalloc(plan)", __LINE__);
@@ -227,6 +251,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
     p->prep.colC = mixed && nvband > 0 ? reinterpret_cast<float2*>(q + b_colA + b_colB + b_band) : nullptr;
     p->prep.nc_pad = nc_pad;
     p->prep.status = p->counters + 2;
+    p->fac.ssx.partial = b_fssx ? reinterpret_cast<double2*>(q + b_colA + b_colB + b_band + b_colC) : nullptr;
   }
   e = cudaMemcpy(p->igp_of, igp_of.data(), sizeof(int) * ngpown, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -304,7 +329,9 @@ extern "C" int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, doubl
       const bool occ = plan->ssx.n_items > 0;
       const sigma::OzakiPrep* oz = sigma::ff_plan_ozaki(plan->ff);
       const int pad = oz && oz->n_row_blocks * sigma::kOzRows > sigma::kNW * plan->ng ? 1 : 0;
-      *launches_per_execution = (occ ? 2 : 1) + pad + 2 + 2 + (occ ? 1 : 0) + 2;
+      // fused: the factor pass (padding rows and occupied bands included),
+      // B slices and epilogue factors (2), GEMM, its reduction, 2 reductions
+      *launches_per_execution = plan->fused ? 1 + 2 + 2 + 2 : (occ ? 2 : 1) + pad + 2 + 2 + (occ ? 1 : 0) + 2;
     } else
       *launches_per_execution = (plan->sch.n_items > 0 ? (mixed ? 3 : 1) : 0) +
                                 (plan->ssx.n_items > 0 ? 1 : 0) + 2;
@@ -372,7 +399,17 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   GppWork main = ypath ? plan->schy : (mypath ? plan->schmy : plan->sch);
   if (tensor) main.partial = nullptr;  // band sums land in acht_n1 directly
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
-  if (tensor) {
+  if (tensor && plan->fused) {
+    // factors written as the contraction's A slices, occupied bands summed
+    // in the same pass
+    FactorJob j = plan->fac;
+    j.p = p;
+    SIGMA_CUDA_TRY(launch_factor_pass(j, plan->fac_grid, s));
+    const int st = ff_execute_weighted(plan->ff, nullptr, aqsntemp, aqsmtemp, vcoul, 0.5,
+                                       reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream, nullptr,
+                                       true);
+    if (st != SIGMA_OK) return st;
+  } else if (tensor) {
     // factors, and the occupied-band operands from the same pass
     // the factors land directly as the contraction's A slices
     SIGMA_CUDA_TRY(launch_tensor_factors(p, occupied_bands(plan->prepw, p.nvband),
@@ -390,16 +427,65 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
     SIGMA_CUDA_TRY(mixed ? launch_sch_mixed(p, plan->sch, plan->prep, plan->sch_grid, s)
                          : launch_sch_fp64(p, plan->sch, plan->sch_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
-  if (plan->ssx.n_items > 0)
+  if (plan->ssx.n_items > 0 && !plan->fused)
     SIGMA_CUDA_TRY((mixed || tensor) ? launch_ssx_mixed(p, plan->ssx, plan->prep, plan->ssx_grid, s)
                                      : launch_ssx_fp64(p, plan->ssx, plan->ssx_grid, s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[2], s));
-  SIGMA_CUDA_TRY(launch_gpp_reduce(main, plan->ssx, plan->nb, plan->acht_n1,
+  SIGMA_CUDA_TRY(launch_gpp_reduce(main, plan->fused ? plan->fac.ssx : plan->ssx, plan->nb, plan->acht_n1,
                                    reinterpret_cast<double2*>(achtemp),
                                    reinterpret_cast<double2*>(asxtemp),
                                    reinterpret_cast<double2*>(acht_n1_loc), s));
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[3], s));
   return SIGMA_OK;
+}
+
+extern "C" int sigma_gpp_selftest_gate_timeout(sigma_gpp_plan plan, const double* wx_array,
+                                               const sigma_complex128* aqsmtemp,
+                                               const sigma_complex128* aqsntemp,
+                                               const sigma_complex128* I_eps_array,
+                                               const sigma_complex128* wtilde_array, const double* vcoul,
+                                               int wait_polls, void* stream) {
+  using namespace sigma;
+  if (!plan || !wx_array || !aqsmtemp || !aqsntemp || !I_eps_array || !wtilde_array || !vcoul)
+    return SIGMA_ERR_NULL;
+  if (plan->precision != SIGMA_PREC_FP64 || plan->schy.n_items == 0) return SIGMA_ERR_UNSUPPORTED;
+  if (wait_polls < 1) return SIGMA_ERR_INVALID_SHAPE;
+  int dev = 0;
+  SIGMA_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != plan->device) return SIGMA_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  GppDev p;
+  p.nb = plan->nb;
+  p.nvband = plan->nvband;
+  p.nc = plan->nc;
+  p.ng = plan->ng;
+  p.wx_stride = 0;
+  p.occ = 1.0;
+  p.aqsm = reinterpret_cast<const double2*>(aqsmtemp);
+  p.aqsn = reinterpret_cast<const double2*>(aqsntemp);
+  p.ieps = reinterpret_cast<const double2*>(I_eps_array);
+  p.wt = reinterpret_cast<const double2*>(wtilde_array);
+  p.vcoul = vcoul;
+  p.wx = wx_array;
+  p.igp_of = plan->igp_of;
+  // counters, status and four gate words (ints 16-19 of the 256-byte
+  // counter block) cleared; no copy ever sets a gate word to the epoch
+  SIGMA_CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 256, s));
+  unsigned* gate = reinterpret_cast<unsigned*>(plan->counters + 16);
+  GppWork w = plan->schy;
+  w.order_ks = 1;
+  w.ready = gate;
+  w.epoch = 1;
+  w.ready_first = 1;
+  w.ready_gs = std::max(1, w.n_splits);  // every later split on word 2
+  w.ready_m = gate + 3;
+  w.ready_status = plan->prep.status;
+  w.ready_polls = wait_polls;
+  SIGMA_CUDA_TRY(launch_sch_fp64y(p, w, plan->schy_grid, s));
+  int dev_status = 0;
+  SIGMA_CUDA_TRY(cudaMemcpyAsync(&dev_status, plan->prep.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SIGMA_CUDA_TRY(cudaStreamSynchronize(s));
+  return dev_status;
 }
 
 // ---------------------------------------------------------------- host drop-in
@@ -678,6 +764,34 @@ extern "C" int sigma_gpp_mixed(int number_bands, int nvband, int ncouls, int ngp
   return sigma::gpp_host(SIGMA_PREC_MIXED, number_bands, nvband, ncouls, ngpown, nstart, nend,
                          inv_igp_index, indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array,
                          wtilde_array, vcoul, achtemp, asxtemp, acht_n1_loc, stream);
+}
+
+extern "C" int sigma_gpp_mixed_checked(int number_bands, int nvband, int ncouls, int ngpown, int nstart,
+                                       int nend, const int* inv_igp_index, const int* indinv,
+                                       const double* wx_array, double occ,
+                                       const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
+                                       const sigma_complex128* I_eps_array,
+                                       const sigma_complex128* wtilde_array, const double* vcoul,
+                                       sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                                       sigma_complex128* acht_n1_loc, void* stream, double* rel_err_out) {
+  int st = sigma::gpp_host(SIGMA_PREC_MIXED, number_bands, nvband, ncouls, ngpown, nstart, nend,
+                           inv_igp_index, indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array,
+                           wtilde_array, vcoul, achtemp, asxtemp, acht_n1_loc, stream);
+  if (st != SIGMA_OK || !rel_err_out) return st;
+  sigma_complex128 a64[sigma::kNW], x64[sigma::kNW];
+  st = sigma::gpp_host(SIGMA_PREC_FP64, number_bands, nvband, ncouls, ngpown, nstart, nend, inv_igp_index,
+                       indinv, wx_array, occ, aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul, a64,
+                       x64, nullptr, stream);
+  if (st != SIGMA_OK) return st;
+  auto rel = [](sigma_complex128 x, sigma_complex128 r) {
+    const double d = std::hypot(x.re - r.re, x.im - r.im), m = std::hypot(r.re, r.im);
+    return m > 0.0 ? d / m : (d > 0.0 ? HUGE_VAL : 0.0);
+  };
+  for (int iw = 0; iw < sigma::kNW; ++iw) {
+    rel_err_out[iw] = rel(achtemp[iw], a64[iw]);
+    rel_err_out[sigma::kNW + iw] = rel(asxtemp[iw], x64[iw]);
+  }
+  return SIGMA_OK;
 }
 
 extern "C" int sigma_gpp_tensor(int number_bands, int nvband, int ncouls, int ngpown, int nstart,

@@ -8,11 +8,20 @@
 // (mixed form) and the fixed-order reductions run around them, and the whole
 // sequence is captured once in a CUDA graph and replayed.
 //
-// The tensor form (SIGMA_PREC_TENSOR) runs each instance's band sum as its
-// own split-BF16 contraction (frequency factors, slicing, tcgen05 GEMM) in
-// stream order, the instances sharing one factor buffer and one slice
-// workspace sized for the largest; the occupied-band pass and the
-// reductions stay batched.
+// The tensor form (SIGMA_PREC_TENSOR) runs every stage once for all
+// instances: one factor pass (frequency factors written as each instance's
+// contraction A slices, occupied bands summed in the same pass), one pass
+// for the B slices and one for the epilogue factors, ONE split-BF16 tcgen05
+// GEMM whose work table lists the items of every instance's contraction, one
+// contraction reduction and the two fixed-order GPP reductions: seven
+// launches per execution whatever the number of instances.  Every instance
+// keeps its own slice images (about 36 B per column and g-vector plus 24 B
+// per band and g-vector).  Instances with more than kFusedBands occupied
+// bands take the earlier form instead: per-instance contractions in stream
+// order over one shared slice workspace, occupied bands in a separate pass.
+//
+// The FP64 and mixed forms reduce all instances with the grouped reduction
+// (two launches).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -22,6 +31,7 @@
 #include "gpp_batch.cuh"
 #include "ff_plan.h"
 #include "ff_ozaki.cuh"
+#include "gpp_tensor.cuh"
 #include "runtime.h"
 
 namespace sigma {
@@ -48,8 +58,18 @@ struct sigma_gpp_batch_s {
   cudaGraphExec_t exec = nullptr;
   // tensor form
   std::vector<sigma_ff_plan> ff;   // per instance (3 slabs, GPP column map)
-  void* tensor_ws = nullptr;       // shared: factors Y[3][ng][nc] then the slice images
+  void* tensor_ws = nullptr;       // slice images: one region per instance (grouped) or one shared
   void* tiles = nullptr;
+  bool grouped = false;            // every stage one launch for all instances
+  void* group_block = nullptr;     // descriptors, item table, ssx partials
+  const sigma::FactorJob* d_fac = nullptr;
+  int fac_total = 0, fac_grid = 0;
+  sigma::OzGroup grp{};
+  // grouped reductions (every form)
+  const sigma::ReduceJob* d_red = nullptr;
+  int red_warps = 0;
+  void* red_block = nullptr;
+  std::vector<sigma::GppWork> fssx;  // grouped tensor form: the factor pass's ssx partials per instance
 };
 
 namespace sigma {
@@ -87,6 +107,157 @@ void size_instance(GppWork& w, int band_count, int bn, int bp, int nc, int ng, d
   w.split_len = len;
   w.n_splits = (nc + len - 1) / len;
   w.n_items = w.n_band_blocks * w.n_col_blocks * w.n_splits;
+}
+
+// The grouped tensor form: every instance's contraction plan over its own
+// slice images (items of about the same number of K tiles in every plan),
+// the factor-pass jobs, the contraction jobs and the GEMM's item table in
+// one device block.
+int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
+                       const std::vector<std::vector<int>>& igp, int sms) {
+  const int n = b->n;
+  std::vector<size_t> toff(n);
+  size_t tbytes = 0;
+  long long tiles = 0;  // K' tiles x band blocks of every contraction
+  double elems = 0.0;   // (column, g-vector) pairs of every instance
+  for (int i = 0; i < n; ++i) {
+    const sigma_gpp_instance& q = inst[i];
+    size_t tb = 0;
+    const int st = ff_plan_tile_bytes(q.number_bands, q.ncouls, q.ngpown, kNW, &tb);
+    if (st != SIGMA_OK) return st;
+    toff[i] = tbytes;
+    tbytes += (tb + 1023) / 1024 * 1024;
+    const long long nrb = (kNW * q.ngpown + kOzRows - 1) / kOzRows, kt = (q.ncouls + kOzKTile - 1) / kOzKTile;
+    tiles += nrb * 2 * kt * ((q.number_bands + kOzCols - 1) / kOzCols);
+    elems += (double)q.ngpown * q.ncouls;
+  }
+  cudaError_t e = cudaMalloc(&b->tensor_ws, tbytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_last_cuda_error(e, "cudaMalloc(batch slice images)", __LINE__);
+    return SIGMA_ERR_ALLOC;
+  }
+  // about 20 GEMM items per CTA over the whole group (one CTA per SM), at
+  // most 256 K' tiles per item: the drain warps carry an item's sum in FP32
+  // registers across its accumulator lifetimes (4 K' tiles each), and the
+  // rounding error of that running sum grows with their number
+  const int hint = (int)std::min(256LL, std::max(8LL, tiles / (20LL * sms)));
+  b->ff.assign(n, nullptr);
+  b->fac_grid = sms * factor_blocks_per_sm();
+  std::vector<FactorJob> fac(n);
+  std::vector<OzGroupJob> jobs(n);
+  std::vector<int4> items;
+  std::vector<size_t> ssx_off(n);
+  size_t ssx_bytes = 0;
+  int bblk = 0, wblk = 0, rwarps = 0;
+  b->fac_total = 0;
+  for (int i = 0; i < n; ++i) {
+    const sigma_gpp_instance& q = inst[i];
+    int st = ff_plan_build(&b->ff[i], q.number_bands, q.ncouls, q.ngpown, kNW, igp[i], SIGMA_FF_OZAKI_BF16,
+                           static_cast<char*>(b->tensor_ws) + toff[i], nullptr, hint);
+    if (st != SIGMA_OK) return st;
+    const OzakiPrep& oz = *ff_plan_ozaki(b->ff[i]);
+    // the plan's work entries, for the group's item table (with a split
+    // size given, they depend on the shape and the split size only)
+    OzakiTables t;
+    OzakiPrep again{};
+    ozaki_size(again, *ff_plan_dev(b->ff[i]), sms, nullptr, &t, hint);
+    if (again.n_items != oz.n_items || again.n_entries != oz.n_entries) return SIGMA_ERR_UNSUPPORTED;
+    ozaki_group_items(i, oz, t, items);
+
+    FactorJob& fj = fac[i];
+    factor_job_size(fj, b->dev[i], oz.kt, b->fac_grid, (double)q.ngpown * q.ncouls / elems);
+    fj.a_tiles = oz.a_tiles;
+    fj.item_off = b->fac_total;
+    b->fac_total += factor_job_items(fj);
+    ssx_off[i] = ssx_bytes;
+    ssx_bytes += up256(factor_ssx_partial_bytes(fj));
+
+    OzGroupJob& J = jobs[i];
+    J.d = *ff_plan_dev(b->ff[i]);
+    J.d.epsr = nullptr;
+    J.d.aqsn = reinterpret_cast<const double2*>(q.aqsntemp);
+    J.d.aqsm = reinterpret_cast<const double2*>(q.aqsmtemp);
+    J.d.vcoul = q.vcoul;  // column weight 0.5 vcoul[igp]
+    J.d.vfac = 0.5;
+    J.oz = oz;
+    J.oz.stab = nullptr;
+    J.out = b->acht_n1[i];
+    const long long b_cnt = (long long)oz.n_col_blocks * oz.kt * 64 * 4, w_cnt = (long long)oz.ng * oz.nb_pad;
+    J.b_blks = (int)std::max(1LL, (b_cnt + 2047) / 2048);  // ~8 elements per thread
+    J.b_blk_off = bblk;
+    bblk += J.b_blks;
+    J.w_blks = (int)std::max(1LL, (w_cnt + 2047) / 2048);
+    J.w_blk_off = wblk;
+    wblk += J.w_blks;
+    J.r_warp_off = rwarps;
+    rwarps += q.number_bands * kNW;
+  }
+  const size_t o_fac = 0;
+  const size_t o_jobs = o_fac + up256(sizeof(FactorJob) * n);
+  const size_t o_items = o_jobs + up256(sizeof(OzGroupJob) * n);
+  const size_t o_ssx = o_items + up256(sizeof(int4) * std::max<size_t>(1, items.size()));
+  e = cudaMalloc(&b->group_block, o_ssx + ssx_bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_last_cuda_error(e, "cudaMalloc(batch group)", __LINE__);
+    return SIGMA_ERR_ALLOC;
+  }
+  char* base = static_cast<char*>(b->group_block);
+  b->fssx.resize(n);
+  for (int i = 0; i < n; ++i) {
+    fac[i].ssx.partial = reinterpret_cast<double2*>(base + o_ssx + ssx_off[i]);
+    b->fssx[i] = fac[i].ssx;
+  }
+  e = cudaMemcpy(base + o_fac, fac.data(), sizeof(FactorJob) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(base + o_jobs, jobs.data(), sizeof(OzGroupJob) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !items.empty())
+    e = cudaMemcpy(base + o_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "cudaMemcpy(batch group)", __LINE__);
+    return SIGMA_ERR_CUDA;
+  }
+  b->d_fac = reinterpret_cast<const FactorJob*>(base + o_fac);
+  OzGroup& g = b->grp;
+  g.jobs = reinterpret_cast<const OzGroupJob*>(base + o_jobs);
+  g.n_jobs = n;
+  g.items = reinterpret_cast<const int4*>(base + o_items);
+  g.total = (int)items.size();
+  g.b_blocks = bblk;
+  g.w_blocks = wblk;
+  g.r_warps = rwarps;
+  g.status = b->counters + 2;
+  return SIGMA_OK;
+}
+
+// The grouped reductions of every form: one job per instance.
+int build_reductions(sigma_gpp_batch_s* b) {
+  const bool tensor = b->precision == SIGMA_PREC_TENSOR;
+  std::vector<ReduceJob> r(b->n);
+  int warps = 0;
+  for (int i = 0; i < b->n; ++i) {
+    GppWork main = b->sch[i];
+    if (tensor) main.partial = nullptr;  // band sums already in acht_n1
+    const GppWork& ssx = (tensor && b->grouped) ? b->fssx[i] : b->ssx[i];
+    r[i] = gpp_reduce_job(main, ssx, b->dev[i].nb, b->acht_n1[i], reinterpret_cast<double2*>(b->inst[i].achtemp),
+                          reinterpret_cast<double2*>(b->inst[i].asxtemp),
+                          reinterpret_cast<double2*>(b->inst[i].acht_n1_loc), warps);
+    warps += gpp_reduce_job_rows(r[i]);
+  }
+  cudaError_t e = cudaMalloc(&b->red_block, sizeof(ReduceJob) * b->n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_last_cuda_error(e, "cudaMalloc(batch reductions)", __LINE__);
+    return SIGMA_ERR_ALLOC;
+  }
+  e = cudaMemcpy(b->red_block, r.data(), sizeof(ReduceJob) * b->n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e, "cudaMemcpy(batch reductions)", __LINE__);
+    return SIGMA_ERR_CUDA;
+  }
+  b->d_red = static_cast<const ReduceJob*>(b->red_block);
+  b->red_warps = warps;
+  return SIGMA_OK;
 }
 
 }  // namespace
@@ -132,8 +303,15 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   const int sms = device_sm_count();
   if (sms <= 0) return SIGMA_ERR_NO_DEVICE;
 
+  // tensor form: every stage grouped when every instance's occupied bands
+  // fit the fused factor pass; the mixed form's FP32 operands are then unused
+  bool grouped = tensor;
+  for (int i = 0; i < n_instances; ++i) grouped = grouped && factor_fuses_ssx(inst[i].nvband);
+  const bool mixed_ops = mixed && !grouped;
+
   auto* b = new sigma_gpp_batch_s();
   b->device = dev;
+  b->grouped = grouped;
   b->n = n_instances;
   b->precision = precision;
   b->terms = terms;
@@ -198,7 +376,7 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
       pw.n_col_blocks = 2 * b->sch[i].n_col_blocks;
       pw.n_band_blocks = 2 * b->sch[i].n_band_blocks;
     }
-    if (mixed) {
+    if (mixed_ops) {
       const size_t col = (size_t)pw.n_col_blocks * kBPM * nc_pad;
       const size_t band = (size_t)pw.n_band_blocks * kBN * nc_pad;
       o_a[i] = total;
@@ -259,10 +437,10 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
     MixedPrep& m = b->prep[i];
     m.nc_pad = (q.ncouls + kCK - 1) / kCK * kCK;
     m.status = b->counters + 2;
-    m.colA = mixed ? reinterpret_cast<float4*>(base + o_a[i]) : nullptr;
-    m.colB = mixed ? reinterpret_cast<float2*>(base + o_b[i]) : nullptr;
-    m.colC = mixed && q.nvband > 0 ? reinterpret_cast<float2*>(base + o_c[i]) : nullptr;
-    m.band = mixed ? reinterpret_cast<float2*>(base + o_band[i]) : nullptr;
+    m.colA = mixed_ops ? reinterpret_cast<float4*>(base + o_a[i]) : nullptr;
+    m.colB = mixed_ops ? reinterpret_cast<float2*>(base + o_b[i]) : nullptr;
+    m.colC = mixed_ops && q.nvband > 0 ? reinterpret_cast<float2*>(base + o_c[i]) : nullptr;
+    m.band = mixed_ops ? reinterpret_cast<float2*>(base + o_band[i]) : nullptr;
   }
   int rc = SIGMA_OK;
   auto up = [&](size_t off, const void* src, size_t bytes) {
@@ -302,10 +480,18 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   b->ssx_view.counter = b->counters + 1;
   if (b->sch_grid > v.total) b->sch_grid = std::max(1, v.total);
   if (b->ssx_grid > b->ssx_view.total) b->ssx_grid = std::max(1, b->ssx_view.total);
-  b->launches = (mixed ? 2 * n_instances : 0) + 1 + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
-  if (tensor) {
-    // one factor buffer and one slice workspace, each sized for the largest instance
-    size_t tbytes = 0;  // one slice workspace, sized for the largest instance
+  // every form: the two fixed-order reductions for all instances
+  b->launches = (mixed ? 2 * n_instances : 0) + 1 + (b->ssx_view.total > 0 ? 1 : 0) + 2;
+  if (tensor && grouped) {
+    int st = build_tensor_group(b, inst, igp, sms);
+    if (st != SIGMA_OK) {
+      sigma_gpp_batch_destroy(b);
+      return st;
+    }
+    b->launches = 7;  // factors, B slices, epilogue factors, GEMM, its reduction, 2 reductions
+  } else if (tensor) {
+    // one slice workspace, sized for the largest instance
+    size_t tbytes = 0;
     for (int i = 0; i < n_instances; ++i) {
       size_t tb = 0;
       int st = ff_plan_tile_bytes(inst[i].number_bands, inst[i].ncouls, inst[i].ngpown, kNW, &tb);
@@ -341,7 +527,12 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
       const int pad = oz->n_row_blocks * kOzRows > kNW * inst[i].ngpown ? 1 : 0;
       per += (b->ssx[i].n_items > 0 ? 2 : 1) + pad + 2 + 2;
     }
-    b->launches = per + (b->ssx_view.total > 0 ? 1 : 0) + 2 * n_instances;
+    b->launches = per + (b->ssx_view.total > 0 ? 1 : 0) + 2;
+  }
+  int st = build_reductions(b);
+  if (st != SIGMA_OK) {
+    sigma_gpp_batch_destroy(b);
+    return st;
   }
   *out = b;
   return SIGMA_OK;
@@ -357,6 +548,17 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   const bool tensor = b->precision == SIGMA_PREC_TENSOR;
   const bool mixed = b->precision == SIGMA_PREC_MIXED || tensor;
   SIGMA_CUDA_TRY(cudaMemsetAsync(b->counters, 0, 4 * sizeof(int), s));
+  if (tensor && b->grouped) {
+    // every instance in each launch: factors (A slices, occupied bands),
+    // B slices and epilogue factors, the GEMM over the group's item table,
+    // its reduction
+    SIGMA_CUDA_TRY(launch_factor_pass(b->d_fac, b->n, b->fac_total, b->fac_grid, s));
+    SIGMA_CUDA_TRY(launch_ozaki_group_prep(b->grp, s));
+    SIGMA_CUDA_TRY(launch_ozaki_group_gemm(b->grp, device_sm_count(), s));
+    SIGMA_CUDA_TRY(launch_ozaki_group_reduce(b->grp, s));
+    SIGMA_CUDA_TRY(launch_gpp_reduce_group(b->d_red, b->n, b->red_warps, s));
+    return SIGMA_OK;
+  }
   if (mixed && !tensor)
     for (int i = 0; i < b->n; ++i)
       if (b->sch[i].n_items > 0)
@@ -383,14 +585,7 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   if (b->ssx_view.total > 0)
     SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed_batch(b->ssx_view, b->ssx_grid, b->all_shared_wx, s)
                          : launch_ssx_fp64_batch(b->ssx_view, b->ssx_grid, s));
-  for (int i = 0; i < b->n; ++i) {
-    GppWork main = b->sch[i];
-    if (tensor) main.partial = nullptr;  // band sums already in acht_n1
-    SIGMA_CUDA_TRY(launch_gpp_reduce(main, b->ssx[i], b->dev[i].nb, b->acht_n1[i],
-                                     reinterpret_cast<double2*>(b->inst[i].achtemp),
-                                     reinterpret_cast<double2*>(b->inst[i].asxtemp),
-                                     reinterpret_cast<double2*>(b->inst[i].acht_n1_loc), s));
-  }
+  SIGMA_CUDA_TRY(launch_gpp_reduce_group(b->d_red, b->n, b->red_warps, s));
   return SIGMA_OK;
 }
 
@@ -448,6 +643,8 @@ extern "C" int sigma_gpp_batch_destroy(sigma_gpp_batch b) {
   for (sigma_ff_plan f : b->ff)
     if (f) sigma_ff_plan_destroy(f);
   if (b->tensor_ws) cudaFree(b->tensor_ws);
+  if (b->group_block) cudaFree(b->group_block);
+  if (b->red_block) cudaFree(b->red_block);
   if (b->block) cudaFree(b->block);
   cudaSetDevice(cur);
   delete b;

@@ -6,17 +6,20 @@
 namespace sigma {
 
 // Tile shapes of the FP64 main pass (bands x columns per item).  Tiles 0-2
-// belong to the per-band-frequency kernel, tiles 3-5 to the shared-frequency
-// kernel (sch_fp64y_item); a batch runs one kernel for all its instances.
+// belong to the per-band-frequency kernel, tiles 3-6 to the shared-frequency
+// kernel (sch_fp64y_item; 128 x 16 is the single-instance plan's item); a
+// batch runs one kernel for all its instances.
 enum GppTile {
   kTile32x32 = 0, kTile16x64 = 1, kTile64x16 = 2,
-  kTileY64x32 = 3, kTileY32x64 = 4, kTileY32x32 = 5, kTileCount = 6
+  kTileY64x32 = 3, kTileY32x64 = 4, kTileY32x32 = 5, kTileY128x16 = 6, kTileCount = 7
 };
 __host__ __device__ constexpr int tile_bn(int t) {
-  return (t == kTile16x64) ? 16 : ((t == kTile64x16 || t == kTileY64x32) ? 64 : 32);
+  return (t == kTile16x64) ? 16
+         : (t == kTileY128x16) ? 128
+                               : ((t == kTile64x16 || t == kTileY64x32) ? 64 : 32);
 }
 __host__ __device__ constexpr int tile_bp(int t) {
-  return (t == kTile16x64 || t == kTileY32x64) ? 64 : (t == kTile64x16 ? 16 : 32);
+  return (t == kTile16x64 || t == kTileY32x64) ? 64 : ((t == kTile64x16 || t == kTileY128x16) ? 16 : 32);
 }
 __host__ __device__ constexpr bool tile_shared(int t) { return t >= kTileY64x32; }
 

@@ -133,7 +133,7 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
             const double c = __dsub_rn(wxr[i][iw], a[j]);
             const double wv = fma(c, c, b2[j]);
             double r = rcp_f64_seed32(wv);
-            r = gt_nonneg(wv, thr[j]) ? r : 0.0;
+            r = keep_nonneg(wv, thr[j]) ? r : 0.0;
             const double ure = fma(R.x, c, -bRim);
             const double uim = fma(R.y, c, bRre);
             acc[i][j][iw].x = fma(ure, r, acc[i][j][iw].x);
@@ -226,27 +226,30 @@ struct SchYSmem {
   double ns[kCKY][BN];       // n.x + n.y
 };
 
-// Bounded wait for a gate word written by a host-to-device copy (about 1 s).
-__device__ __forceinline__ void wait_ready(const unsigned* flag, unsigned epoch, int* status) {
-  if (*reinterpret_cast<volatile int*>(status) != 0) return;  // an earlier wait gave up
-  for (int i = 0; i < (1 << 22); ++i) {
+// Bounded wait for a gate word written by a host-to-device copy (`polls`
+// polls 256 ns apart: about 1 s with the default bound).  False when it gave
+// up (SIGMA_ERR_TIMEOUT recorded) or an earlier wait of the launch had; the
+// item is then dropped and the CTA takes no further item.
+__device__ __forceinline__ bool wait_ready(const unsigned* flag, unsigned epoch, int* status, int polls) {
+  if (*reinterpret_cast<volatile int*>(status) != 0) return false;  // an earlier wait gave up
+  for (int i = 0; i < polls; ++i) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
-    if (v == epoch) return;
+    if (v == epoch) return true;
     __nanosleep(256);
   }
-  atomicExch(status, (int)SIGMA_ERR_TIMEOUT);
+  atomicCAS(status, 0, (int)SIGMA_ERR_TIMEOUT);
+  return false;
 }
 
 template <int BN, int BP>
 __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w, int item,
                                                unsigned char* smem_raw, int tid) {
   if (w.ready) {  // inputs of this item copied yet?
-    if (tid == 0) {
-      const ItemCoord g = decode_item(w, item);
-      wait_ready(w.ready + gate_word(w, g.cb, g.s), w.epoch, w.ready_status);
-    }
-    __syncthreads();
+    const ItemCoord g = decode_item(w, item);
+    if (!__syncthreads_and(tid != 0 ||
+                           wait_ready(w.ready + gate_word(w, g.cb, g.s), w.epoch, w.ready_status, w.ready_polls)))
+      return;
   }
   constexpr int TB = BN / 16, TC = BP / 16;
   SchYSmem<BN, BP>& sm = *reinterpret_cast<SchYSmem<BN, BP>*>(smem_raw);
@@ -284,7 +287,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         auto factor = [&](double wx) {
           const double c = __dsub_rn(wx, wt.x);
           const double wv = fma(c, c, b2);
-          const double r = gt_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
+          const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
           const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
           return make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
         };
@@ -342,8 +345,8 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   // half-warp hold the item's columns for the same bands and sum them with
   // a fixed butterfly
   if (w.ready_m) {  // aqsm copied yet?
-    if (tid == 0) wait_ready(w.ready_m, w.epoch, w.ready_status);
-    __syncthreads();
+    if (!__syncthreads_and(tid != 0 || wait_ready(w.ready_m, w.epoch, w.ready_status, w.ready_polls)))
+      return;
   }
 #pragma unroll
   for (int i = 0; i < TB; ++i) {
@@ -390,7 +393,10 @@ __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_kernel(GppDev p, GppWor
   const int tid = threadIdx.x;
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_item = atomicAdd(w.counter, 1);
+    // gated launch: no further items once a wait gave up
+    if (tid == 0)
+      s_item = (w.ready && *reinterpret_cast<volatile int*>(w.ready_status) != 0) ? w.n_items
+                                                                                  : atomicAdd(w.counter, 1);
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
@@ -398,8 +404,9 @@ __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_kernel(GppDev p, GppWor
   }
 }
 
+constexpr size_t smax(size_t a, size_t b) { return a > b ? a : b; }
 constexpr size_t kSchYBatchSmem =
-    sizeof(SchYSmem<64, 32>) > sizeof(SchYSmem<32, 64>) ? sizeof(SchYSmem<64, 32>) : sizeof(SchYSmem<32, 64>);
+    smax(smax(sizeof(SchYSmem<64, 32>), sizeof(SchYSmem<32, 64>)), sizeof(SchYSmem<128, 16>));
 
 __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchView b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -418,6 +425,7 @@ __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchVi
     switch (b.tile[inst]) {
       case kTileY32x64: sch_fp64y_item<32, 64>(p, w, local, smem_raw, tid); break;
       case kTileY32x32: sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid); break;
+      case kTileY128x16: sch_fp64y_item<128, 16>(p, w, local, smem_raw, tid); break;
       default: sch_fp64y_item<64, 32>(p, w, local, smem_raw, tid); break;
     }
   }
@@ -505,7 +513,7 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       auto factor = [&](int i, int iw) {
         const double wx = sh.wx[i][iw];
         const double wv = guard_w(wx, a, b2);
-        const bool keep = gt_nonneg(wv, thr);
+        const bool keep = keep_nonneg(wv, thr);
         const bool br2 = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
         // branch 1: Omega2 / wx^2
         const double iwx2 = sh.iwx2[i][iw];

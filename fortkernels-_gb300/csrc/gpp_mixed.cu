@@ -33,7 +33,6 @@ constexpr int kTN = 2;    // bands per thread (one column per thread)
 constexpr int kRun = 8;   // g-vectors summed in FP32 before the float-float fold
 constexpr uint32_t kChunkBytes =
     kCK * kBPM * sizeof(float4) + kCK * kBPM * sizeof(float2) + kCK * kBN * sizeof(float2);
-constexpr int kWaitSpins = 1 << 22;  // bound on mbarrier polls before reporting a timeout
 
 struct __align__(16) Stage {
   float4 a[kCK][kBPM];
@@ -83,26 +82,24 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
+// Bounded waits (sigma_tma.cuh): mbar_wait gives up once the launch's status
+// word is set or after its poll bound (recording SIGMA_ERR_TIMEOUT);
+// mbar_wait_own waits for a copy this CTA issued itself, whatever the status.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity, int* status) {
+  return tma::mbar_wait(smem_u32(bar), parity, status);
 }
-// Bounded wait: after kWaitSpins polls it records SIGMA_ERR_TIMEOUT and keeps
-// waiting once more with the same bound (a bulk copy from valid global memory
-// always lands; the bound only keeps a fault elsewhere from becoming a hang).
-__device__ __forceinline__ void mbar_wait(unsigned long long* bar, uint32_t parity, int* status) {
-  for (int i = 0; i < kWaitSpins; ++i)
-    if (mbar_try_wait(bar, parity)) return;
-  atomicExch(status, (int)SIGMA_ERR_TIMEOUT);
-  for (int i = 0; i < kWaitSpins; ++i)
-    if (mbar_try_wait(bar, parity)) return;
+__device__ __forceinline__ void mbar_wait_own(unsigned long long* bar, uint32_t parity) {
+  tma::mbar_wait_own(smem_u32(bar), parity);
+}
+
+// After a failed wait at chunk c: the copies of chunk c (parity `pc` on
+// bar[c & 1]) and, when issued, of chunk c + 1 (parity `pn` on the other
+// barrier) may still be landing; the issuing thread waits for both before
+// the CTA leaves, so no copy writes shared memory after it is released.
+__device__ __forceinline__ void drain_chunks(unsigned long long* bar, int c, int n_chunks, uint32_t pc,
+                                             uint32_t pn) {
+  mbar_wait_own(&bar[c & 1], pc);
+  if (c + 1 < n_chunks) mbar_wait_own(&bar[(c + 1) & 1], pn);
 }
 
 // Issues the three bulk copies of chunk (cb, bb, ig0) into stage `st`.
@@ -120,7 +117,7 @@ __device__ __forceinline__ void issue_chunk(const MixedPrep& m, int cb, int bb, 
 __device__ __forceinline__ bool keep_exact(const GppDev& p, int my_igp, int ig, double wx) {
   const double2 wt = p.wt[(size_t)my_igp * p.nc + ig];
   const double b2 = guard_b2(wt.y);
-  return gt_nonneg(guard_w(wx, wt.x, b2), guard_thr(wt.x, b2));
+  return keep_nonneg(guard_w(wx, wt.x, b2), guard_thr(wt.x, b2));
 }
 
 // ---- pre-pass: FP32 operands in tile-interleaved layouts
@@ -177,7 +174,7 @@ __global__ void __launch_bounds__(256) prep_cols_kernel(GppDev p, MixedPrep m, i
             else if (wv <= t32 * (1.0f - kGuardBand))
               keep = false;
             else
-              keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2), thr);
+              keep = keep_nonneg(guard_w(p.wx[iw], wt.x, b2), thr);
             mask |= keep ? (1u << iw) : 0u;
             if (p.nvband > 0 && !keep) {
               bool second;
@@ -284,13 +281,10 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, MixedPrep
           // keep: |wdiff|^2 > max(0.25, |wtilde|^2 * 4e-6), i.e. both
           // wv > 0.25 and wv * 250000 > |wtilde|^2 (250000 exact in FP32)
           bool n1, n2;
-          const bool k1 = ff_gt(wv, quarter, n1);
-          const bool k2 = ff_gt(ff_mul(wv, FF{250000.f, 0.f}), s2, n2);
+          const bool k1 = ff_gt_fast(wv, quarter, n1);
+          const bool k2 = ff_gt_fast(ff_mul(wv, FF{250000.f, 0.f}), s2, n2);
           bool keep = k1 && k2;
-          if (n1 || n2) {  // within 2^-30 of a threshold: the FP64 path's decision
-            const double b2d = guard_b2(wt.y);
-            keep = gt_nonneg(guard_w(p.wx[iw], wt.x, b2d), guard_thr(wt.x, b2d));
-          }
+          if (n1 || n2) keep = keep_fp64(p.wx[iw], wt.x, wt.y);  // within 2^-30 of a threshold
           if (slices) {
             float2 yv = make_float2(0.f, 0.f);
             if (keep) {
@@ -304,12 +298,8 @@ __global__ void __launch_bounds__(256) tensor_factors_kernel(GppDev p, MixedPrep
           if (ops && p.nvband > 0 && !keep) {
             // second branch: 0 < |wdiff|^2 < |wtilde|^2 / to1
             bool n3;
-            bool second = wv.hi > 0.f && ff_gt(s_big, wv, n3);
-            if (n3 || wv.hi < 1e-30f) {
-              const double b2d = guard_b2(wt.y);
-              const double w64 = guard_w(p.wx[iw], wt.x, b2d);
-              second = gt_nonneg(w64, 0.0) && gt_nonneg(guard_thr2(wt.x, b2d), w64);
-            }
+            bool second = wv.hi > 0.f && ff_gt_fast(s_big, wv, n3);
+            if (n3 || wv.hi < 1e-30f) second = second_fp64(p.wx[iw], wt.x, wt.y);
             mask |= second ? (8u << iw) : 0u;
           }
         }
@@ -488,8 +478,9 @@ __device__ __forceinline__ void chunk_terms(const Stage& st, int pl, int ty, con
 }
 
 // One work item of the main pass (TMA ring barriers and their phases persist
-// across the items a CTA takes).
-__device__ __forceinline__ void sch_mixed_item(const GppDev& p, const GppWork& w, const MixedPrep& m,
+// across the items a CTA takes).  False (the same in every thread) when a
+// copy wait gave up; the CTA then takes no further item.
+__device__ __forceinline__ bool sch_mixed_item(const GppDev& p, const GppWork& w, const MixedPrep& m,
                                                int item, SchSmemM& sm, int tid, uint32_t& phase0,
                                                uint32_t& phase1) {
   const int tx = tid & 15, ty = tid >> 4;
@@ -532,13 +523,9 @@ __device__ __forceinline__ void sch_mixed_item(const GppDev& p, const GppWork& w
     const int ig0 = ig_begin + c * kCK;
     if (tid == 0 && c + 1 < n_chunks)
       issue_chunk(m, ic.cb, ic.bb, ig0 + kCK, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
-    if (buf == 0) {
-      mbar_wait(&sm.bar[0], phase0, m.status);
-      phase0 ^= 1;
-    } else {
-      mbar_wait(&sm.bar[1], phase1, m.status);
-      phase1 ^= 1;
-    }
+    const uint32_t pc = buf ? phase1 : phase0, pn = buf ? phase0 : phase1;
+    const bool ok = mbar_wait(&sm.bar[buf], pc, m.status);
+    if (buf == 0) phase0 ^= 1; else phase1 ^= 1;
     const Stage& st = sm.st[buf];
     if (shared_wx) {
       if (wx_exact)
@@ -548,7 +535,11 @@ __device__ __forceinline__ void sch_mixed_item(const GppDev& p, const GppWork& w
     } else {
       chunk_terms<false, true>(st, pl, ty, wxh, wxl, acc, hi, lo, p, n1_0, my_igp, ig0, ig_end, band_end);
     }
-    __syncthreads();  // every thread is done with this stage before it is refilled
+    // every thread is done with this stage before it is refilled
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) drain_chunks(sm.bar, c, n_chunks, pc, pn);
+      return false;
+    }
   }
 
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp] in FP64, then a
@@ -584,6 +575,7 @@ __device__ __forceinline__ void sch_mixed_item(const GppDev& p, const GppWork& w
     }
     w.partial[ic.pidx * kBN * kNW + bl * kNW + iw] = make_double2(sx.value(), sy.value());
   }
+  return true;
 }
 
 __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWork w, MixedPrep m) {
@@ -599,11 +591,12 @@ __global__ void __launch_bounds__(kThreads, 3) sch_mixed_kernel(GppDev p, GppWor
   uint32_t phase0 = 0, phase1 = 0;
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_item = atomicAdd(w.counter, 1);
+    // no further items once a wait of this launch gave up
+    if (tid == 0) s_item = tma::status_set(m.status) ? w.n_items : atomicAdd(w.counter, 1);
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    sch_mixed_item(p, w, m, item, sm, tid, phase0, phase1);
+    if (!sch_mixed_item(p, w, m, item, sm, tid, phase0, phase1)) break;
   }
 }
 
@@ -620,12 +613,15 @@ __global__ void __launch_bounds__(kThreads, 3) sch_mixed_batch_kernel(GppBatchVi
   uint32_t phase0 = 0, phase1 = 0;
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_item = atomicAdd(b.counter, 1);
+    // no further items once a wait of this launch gave up (one status word per batch)
+    if (tid == 0) s_item = tma::status_set(b.prep[0].status) ? b.total : atomicAdd(b.counter, 1);
     __syncthreads();
     const int g = s_item;
     if (g >= b.total) break;
     const int inst = batch_owner(b.item_off, b.n_inst, g);
-    sch_mixed_item(b.dev[inst], b.work[inst], b.prep[inst], g - b.item_off[inst], sm, tid, phase0, phase1);
+    if (!sch_mixed_item(b.dev[inst], b.work[inst], b.prep[inst], g - b.item_off[inst], sm, tid, phase0,
+                        phase1))
+      break;
   }
 }
 
@@ -674,7 +670,7 @@ __device__ __forceinline__ void issue_chunk_y(const MixedPrep& m, int cb, int bb
 // the running sum per component and term instead of two, 50 % more FP32
 // operations), which brings the error to the per-band kernel's.
 template <bool kExact>
-__device__ __forceinline__ void sch_mixedy_item(const GppDev& p, const GppWork& w, const MixedPrep& m,
+__device__ __forceinline__ bool sch_mixedy_item(const GppDev& p, const GppWork& w, const MixedPrep& m,
                                                 int item, SchSmemY& sm, int tid, uint32_t& phase0,
                                                 uint32_t& phase1) {
   constexpr int TB = 4, TC = 2;
@@ -710,13 +706,9 @@ __device__ __forceinline__ void sch_mixedy_item(const GppDev& p, const GppWork& 
     const int ig0 = ig_begin + c * kCK;
     if (tid == 0 && c + 1 < n_chunks)
       issue_chunk_y(m, ic.cb, ic.bb, ig0 + kCK, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
-    if (buf == 0) {
-      mbar_wait(&sm.bar[0], phase0, m.status);
-      phase0 ^= 1;
-    } else {
-      mbar_wait(&sm.bar[1], phase1, m.status);
-      phase1 ^= 1;
-    }
+    const uint32_t pc = buf ? phase1 : phase0, pn = buf ? phase0 : phase1;
+    const bool ok = mbar_wait(&sm.bar[buf], pc, m.status);
+    if (buf == 0) phase0 ^= 1; else phase1 ^= 1;
     const StageY& st = sm.st[buf];
     // frequency factors of the chunk; g-vectors past the split's end and
     // padding columns carry a zero mask
@@ -785,7 +777,11 @@ __device__ __forceinline__ void sch_mixedy_item(const GppDev& p, const GppWork& 
             acc[i][j][iw] = make_float2(0.f, 0.f);
           }
     }
-    __syncthreads();  // stage and factors consumed before they are refilled
+    // stage and factors consumed before they are refilled
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) drain_chunks(sm.bar, c, n_chunks, pc, pn);
+      return false;
+    }
   }
 
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp] in FP64; the 16 lanes
@@ -827,6 +823,7 @@ __device__ __forceinline__ void sch_mixedy_item(const GppDev& p, const GppWork& 
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) w.partial[ic.pidx * kYBN * kNW + bl * kNW + iw] = part[iw];
   }
+  return true;
 }
 
 __global__ void __launch_bounds__(kThreads, 1) sch_mixedy_kernel(GppDev p, GppWork w, MixedPrep m) {
@@ -842,11 +839,12 @@ __global__ void __launch_bounds__(kThreads, 1) sch_mixedy_kernel(GppDev p, GppWo
   uint32_t phase0 = 0, phase1 = 0;
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_item = atomicAdd(w.counter, 1);
+    // no further items once a wait of this launch gave up
+    if (tid == 0) s_item = tma::status_set(m.status) ? w.n_items : atomicAdd(w.counter, 1);
     __syncthreads();
     const int item = s_item;
     if (item >= w.n_items) break;
-    sch_mixedy_item<false>(p, w, m, item, sm, tid, phase0, phase1);
+    if (!sch_mixedy_item<false>(p, w, m, item, sm, tid, phase0, phase1)) break;
   }
 }
 
@@ -865,13 +863,15 @@ __global__ void __launch_bounds__(kThreads, 1) sch_mixedy_batch_kernel(GppBatchV
   uint32_t phase0 = 0, phase1 = 0;
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_item = atomicAdd(b.counter, 1);
+    // no further items once a wait of this launch gave up (one status word per batch)
+    if (tid == 0) s_item = tma::status_set(b.prep[0].status) ? b.total : atomicAdd(b.counter, 1);
     __syncthreads();
     const int g = s_item;
     if (g >= b.total) break;
     const int inst = batch_owner(b.item_off, b.n_inst, g);
-    sch_mixedy_item<true>(b.dev[inst], b.work[inst], b.prep[inst], g - b.item_off[inst], sm, tid, phase0,
-                          phase1);
+    if (!sch_mixedy_item<true>(b.dev[inst], b.work[inst], b.prep[inst], g - b.item_off[inst], sm, tid,
+                               phase0, phase1))
+      break;
   }
 }
 
@@ -980,7 +980,7 @@ __device__ __forceinline__ int ssx_branch_exact(const GppDev& p, int my_igp, int
   const double2 wt = p.wt[(size_t)my_igp * p.nc + ig];
   const double b2 = guard_b2(wt.y);
   const double wv = guard_w(wx, wt.x, b2);
-  if (gt_nonneg(wv, guard_thr(wt.x, b2))) return 1;
+  if (keep_nonneg(wv, guard_thr(wt.x, b2))) return 1;
   if (gt_nonneg(wv, 0.0) && gt_nonneg(guard_thr2(wt.x, b2), wv)) return 2;
   return 0;
 }

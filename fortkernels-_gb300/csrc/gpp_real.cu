@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kThreads, 1) sch_real_kernel(GppRealDev p, Gpp
           auto factor = [&](double wx) {
             const double c = __dsub_rn(wx, wt);
             const double wv = __dmul_rn(c, c);
-            const double r = gt_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
+            const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
             return g * (c * r);
           };
           y0 = factor(wx0);
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(kThreads) ssx_real_kernel(GppRealDev p, GppWor
         for (int iw = 0; iw < kNW; ++iw) {
           const double c = __dsub_rn(p.wx[iw], wt);
           const double wv = __dmul_rn(c, c);
-          const bool keep = gt_nonneg(wv, thr);
+          const bool keep = keep_nonneg(wv, thr);
           const bool br2 = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
           const double s2 = -0.5 * g / (p.wx[iw] + wt);
           sv[iw] = keep ? om * iwx2[iw] : (br2 ? s2 : 0.0);

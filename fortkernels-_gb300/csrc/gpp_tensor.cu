@@ -1,0 +1,352 @@
+// Factor pass of the tensor-core GPP form, with the occupied bands' ssx sums
+// fused in; one instance or a batch of instances per launch.
+//
+// With one frequency set for every band the band sum is a contraction of the
+// band-independent factors
+//   Y[iw][my_igp][ig] = G (c + i b) / (c^2 + b^2)        (0 when the guard drops it)
+//                     = (wx G - |wtilde|^2 I_eps) / (c^2 + b^2),
+// G = I_eps wtilde, c = wx - Re wtilde, b = Im wtilde (BGW-Kernels/gppKer.cpp
+// :394-404 with conj(aqsm) and vcoul moved to the contraction's epilogue).
+// This pass forms Y in float-float arithmetic (FP32 pairs, ~2^-44 relative)
+// from exact splits of the FP64 inputs, rounds it once to FP32 and writes it
+// straight into the contraction's A operand as split-BF16 slices.  Keep and
+// second-branch decisions are re-taken with the FP64 path's expressions
+// within 2^-30 of a threshold.
+//
+// The occupied bands (n1 < nvband, flagOCC_solver :130-159 with
+// ssxt_scht_solver :19-65) need, for the same (column, g-vector), the ssx
+// factor of each frequency,
+//   kept:          ssx = Omega2 / wx^2,          Omega2 = wtilde G
+//   second branch: ssx = -G / (2 (wtilde + wx))  (0 < |wdiff|^2 < |wtilde|^2 / to1)
+//   otherwise      0,
+// summed over g-vectors with aqsn[n1][ig].  The pass forms them from the
+// values it already holds and stages them in shared memory; one thread per
+// (band, frequency, column) then sums the tile's 32 g-vectors (FP32 runs of
+// 8 folded into float-float accumulators).  At the end of an item each
+// column's sums are multiplied by conj(aqsm[n1][igp]) occ vcoul[igp] in FP64
+// and summed over the item's columns in a fixed order.  The inputs are read
+// once for both, and no intermediate operand is written.
+//
+// Items are (g-vector segment, column block of 16 columns), plus, per
+// instance, a few items that zero the A slices' padding rows; a batch
+// concatenates the items of every instance (one static schedule).
+#include <algorithm>
+
+#include "gpp_tensor.cuh"
+#include "floatfloat.cuh"
+
+namespace sigma {
+namespace {
+
+constexpr int kFacThreads = 256;
+constexpr int kZeroTiles = 64;  // K tiles per padding-row item
+
+struct FactorSmem {
+  float2 y[kNW][kFacCols][kFacK + 1];          // the tile's factors for the slice writes
+  float2 x[kFacCols][kNW][kFacK + 1];          // the tile's ssx factors
+  float2 an[kFusedBands][kFacK];               // occupied bands' aqsn over the tile's g-vectors
+  double2 red[kFusedBands][kNW][kFacCols];     // item epilogue: per-column ssx sums
+};
+// ssx sums a thread owns: outputs o = tid + 256 r, (band, frequency, column)
+constexpr int kSsxOwn = (kFusedBands * kNW * kFacCols + 255) / 256;
+
+__device__ __forceinline__ int find_job(const FactorJob* jobs, int n, int item) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].item_off <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int padding_rows(const FactorJob& j) {
+  const int rows = kNW * j.p.ng;
+  return (rows + kOzRows - 1) / kOzRows * kOzRows - rows;
+}
+
+// Slices of A row R, K values [k0, k0 + 8): real parts in the first half of
+// the K' tiles, imaginary parts in the second (the OzakiPrep layout).
+__device__ __forceinline__ void put_a(unsigned char* a_tiles, int kt, int R, int k0, const float (&re)[8],
+                                      const float (&im)[8]) {
+  const int rb = R / kOzRows, r = R % kOzRows, t = k0 / kOzKTile, ch = (k0 % kOzKTile) / 8;
+  unsigned char* base = a_tiles + (size_t)rb * 2 * kt * kOzOperandBytes;
+  oz_put_row_chunk(base + (size_t)t * kOzOperandBytes, r, ch, re);
+  oz_put_row_chunk(base + (size_t)(kt + t) * kOzOperandBytes, r, ch, im);
+}
+
+// x * conj-free product of float-float values rounded once to FP32 with
+// the products' errors carried: (a.hi + a.lo)(g.hi + g.lo) - (b.hi + b.lo)(h.hi + h.lo)
+// within ~1 ulp of the result (the one rounding of the hi difference plus
+// the dropped lo * lo terms, 2^-48 of the products).
+__device__ __forceinline__ float ff_dot2_round(FF a, FF g, FF b, FF h) {
+  const float p1 = a.hi * g.hi, p2 = b.hi * h.hi;
+  const float e1 = fmaf(a.hi, g.hi, -p1), e2 = fmaf(b.hi, h.hi, -p2);
+  const float t = fmaf(a.hi, g.lo, fmaf(a.lo, g.hi, e1)) - fmaf(b.hi, h.lo, fmaf(b.lo, h.hi, e2));
+  return (p1 - p2) + t;
+}
+
+// kGroup: the jobs of a batch from a device array; else the one job `single`
+// (a kernel parameter, so that an execution can be captured in a graph).
+template <bool kGroup>
+__global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob single,
+                                                                 const FactorJob* __restrict__ jobs, int n_jobs,
+                                                                 int total) {
+  __shared__ FactorSmem sm;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const FF quarter{0.25f, 0.f};
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    const FactorJob& J = kGroup ? jobs[find_job(jobs, n_jobs, item)] : single;
+    const GppDev& p = J.p;
+    const int local = item - J.item_off;
+    const int main_items = J.ncb * J.n_seg;
+    __syncthreads();  // the previous item is done with shared memory
+    if (local >= main_items) {
+      // zero the A slices of the padding rows for kZeroTiles K tiles
+      const int rows = kNW * p.ng, pad = padding_rows(J);
+      const int t0 = (local - main_items) * kZeroTiles, t1 = min(J.kt, t0 + kZeroTiles);
+      const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int e = tid; e < (t1 - t0) * pad * 4; e += kFacThreads) {
+        const int ch = e % 4, r = (e / 4) % pad, t = t0 + e / (4 * pad);
+        put_a(J.a_tiles, J.kt, rows + r, t * kOzKTile + ch * 8, z, z);
+      }
+      continue;
+    }
+    const int s = local / J.ncb, cb = local % J.ncb;
+    const int t_begin = s * J.seg_tiles, t_end = min(J.kt, t_begin + J.seg_tiles);
+    const int nvb = p.nvband <= kFusedBands ? p.nvband : 0;
+    const int outputs = nvb * kNW * kFacCols;  // ssx sums: (band, frequency, column)
+    FF wx[kNW];
+    float wxh[kNW], wxl[kNW], iwx2[kNW];
+#pragma unroll
+    for (int iw = 0; iw < kNW; ++iw) {
+      wx[iw] = ff_of(p.wx[iw]);
+      wxh[iw] = __double2float_rn(p.wx[iw]);
+      wxl[iw] = __double2float_rn(p.wx[iw] - (double)wxh[iw]);
+      iwx2[iw] = __double2float_rn(rcp_f64(p.wx[iw] * p.wx[iw]));
+    }
+    // float-float accumulators of the ssx sums this thread owns
+    float2 ahi[kSsxOwn], alo[kSsxOwn];
+#pragma unroll
+    for (int r = 0; r < kSsxOwn; ++r) ahi[r] = alo[r] = make_float2(0.f, 0.f);
+
+    for (int t = t_begin; t < t_end; ++t) {
+      const int ig0 = t * kFacK;
+      for (int e = tid; e < nvb * kFacK; e += kFacThreads) {
+        const int n1 = e / kFacK, k = e % kFacK, ig = ig0 + k;
+        float2 v = make_float2(0.f, 0.f);
+        if (ig < p.nc) {
+          const double2 d = p.aqsn[(size_t)n1 * p.nc + ig];
+          v = make_float2(__double2float_rn(d.x), __double2float_rn(d.y));
+        }
+        sm.an[n1][k] = v;
+      }
+#pragma unroll 1
+      for (int j = 0; j < 2; ++j) {
+        const int pl = warp + 8 * j, my_igp = cb * kFacCols + pl, ig = ig0 + lane;
+        float2 yt[kNW] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        float2 sv[kNW] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        if (my_igp < p.ng && ig < p.nc) {
+          const size_t off = (size_t)my_igp * p.nc + ig;
+          const double2 wt = p.wt[off];
+          const double2 ie = p.ieps[off];
+          const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
+          const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));
+          const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
+          const FF b2 = ff_mul(b, b);
+          const FF s2 = ff_add(ff_mul(a, a), b2);      // |wtilde|^2
+          // G (c + i b) = wx G - G conj(wtilde) = wx G - |wtilde|^2 I_eps
+          const FF sex = ff_mul(s2, er), sey = ff_mul(s2, ei);
+          // |wtilde|^2 * 4e-6 >= 0.25 only for |wtilde|^2 >= 62500; below,
+          // |wdiff|^2 > 0.25 implies the guard's second condition
+          const bool thr2_binds = s2.hi >= 62000.f;
+          // |wtilde|^2 / to1 > 1 >= |wdiff|^2 of a dropped term: its second
+          // occupied-band branch is then the exact-pole test alone
+          const bool big_s = s2.hi > 1.01e-6f;
+          unsigned mask = 0u;
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            const FF c = ff_add(wx[iw], ff_neg(a));
+            const FF wv = ff_add(ff_mul(c, c), b2);
+            // keep: |wdiff|^2 > max(0.25, |wtilde|^2 * 4e-6), i.e. both
+            // wv > 0.25 and wv * 250000 > |wtilde|^2 (250000 exact in FP32)
+            bool near;
+            bool keep = ff_gt_fast(wv, quarter, near);
+            if (thr2_binds) {
+              bool n2;
+              keep = keep && ff_gt(ff_mul(wv, FF{250000.f, 0.f}), s2, n2);
+              near = near || n2;
+            }
+            if (near) keep = keep_fp64(p.wx[iw], wt.x, wt.y);  // within 2^-30 of a threshold
+            if (keep) {
+              const FF r = ff_rcp(wv);
+              yt[iw] = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
+                                   ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
+            }
+            mask |= keep ? (1u << iw) : 0u;
+            if (nvb > 0 && !keep) {
+              // second branch: 0 < |wdiff|^2 < |wtilde|^2 / to1
+              bool second;
+              if (big_s && wv.hi >= 1e-30f) {
+                second = true;
+              } else {
+                bool n3;
+                const FF s_big = ff_mul(s2, FF{1e6f, 0.f});  // |wtilde|^2 / to1 (1e6 exact)
+                second = wv.hi > 0.f && ff_gt_fast(s_big, wv, n3);
+                if (n3 || wv.hi < 1e-30f) second = second_fp64(p.wx[iw], wt.x, wt.y);
+              }
+              mask |= second ? (8u << iw) : 0u;
+            }
+          }
+          if (nvb > 0 && mask != 0u) {
+            const float2 g32 = make_float2(ff_round(gx), ff_round(gy));
+            const float bb = ff_round(b);
+            // Omega2 = wtilde G
+            const float2 om = make_float2(ff_dot2_round(a, gx, b, gy), ff_dot2_round(a, gy, ff_neg(b), gx));
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              if (mask & (1u << iw)) {
+                sv[iw] = make_float2(om.x * iwx2[iw], om.y * iwx2[iw]);
+              } else if (mask & (8u << iw)) {
+                const float zr = (wxh[iw] + a.hi) + (wxl[iw] + a.lo);
+                const float q = -0.5f * rcp_f32(fmaf(zr, zr, bb * bb));
+                sv[iw] = make_float2(fmaf(g32.x, zr, g32.y * bb) * q, fmaf(g32.y, zr, -g32.x * bb) * q);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          sm.y[iw][pl][lane] = yt[iw];
+          sm.x[pl][iw][lane] = sv[iw];
+        }
+      }
+      __syncthreads();
+      // split-BF16 slices of the A rows (iw, column): 8 g-vectors per chunk,
+      // consecutive threads fill one 8-row group
+      for (int c = tid; c < kNW * kFacCols * 4; c += kFacThreads) {
+        const int ch = c % 4, pl = (c / 4) % kFacCols, iw = c / (4 * kFacCols);
+        const int col = cb * kFacCols + pl;
+        if (col >= p.ng) continue;
+        float re[8], im[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float2 v = sm.y[iw][pl][ch * 8 + q];
+          re[q] = v.x;
+          im[q] = v.y;
+        }
+        put_a(J.a_tiles, J.kt, iw * p.ng + col, ig0 + ch * 8, re, im);
+      }
+      // the tile's ssx products: output o = (band n1, frequency iw, column pl),
+      // FP32 runs of 8 g-vectors folded into float-float
+#pragma unroll
+      for (int r = 0; r < kSsxOwn; ++r) {
+        const int o = tid + r * kFacThreads;
+        if (o < outputs) {
+          const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
+#pragma unroll
+          for (int k0 = 0; k0 < kFacK; k0 += 8) {
+            float2 run = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = k0; k < k0 + 8; ++k) {
+              const float2 an = sm.an[n1][k], x = sm.x[pl][iw][k];
+              run.x += fmaf(an.x, x.x, -an.y * x.y);
+              run.y += fmaf(an.x, x.y, an.y * x.x);
+            }
+            ff_add(ahi[r].x, alo[r].x, run.x);
+            ff_add(ahi[r].y, alo[r].y, run.y);
+          }
+        }
+      }
+      __syncthreads();  // sm.an, sm.x and sm.y are refilled by the next tile
+    }
+
+    if (nvb > 0) {
+      // each column's sums x conj(aqsm[n1][igp]) occ vcoul[igp] in FP64
+#pragma unroll
+      for (int r = 0; r < kSsxOwn; ++r) {
+        const int o = tid + r * kFacThreads;
+        if (o < outputs) {
+          const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
+          const int my_igp = cb * kFacCols + pl;
+          const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
+          double2 v = make_double2(0.0, 0.0);
+          if (igp >= 0) {
+            const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
+            const double f = p.occ * p.vcoul[igp];
+            const double sx = (double)ahi[r].x + (double)alo[r].x;
+            const double sy = (double)ahi[r].y + (double)alo[r].y;
+            // (sx + i sy) conj(am) f
+            v = make_double2(fma(sx, am.x, sy * am.y) * f, fma(sy, am.x, -sx * am.y) * f);
+          }
+          sm.red[n1][iw][pl] = v;
+        }
+      }
+      __syncthreads();
+      if (tid < nvb * kNW) {
+        const int n1 = tid / kNW, iw = tid % kNW;
+        Comp sx, sy;
+        for (int q = 0; q < kFacCols; ++q) {
+          sx.add(sm.red[n1][iw][q].x);
+          sy.add(sm.red[n1][iw][q].y);
+        }
+        const GppWork& w = J.ssx;
+        const size_t pidx = ((size_t)(n1 / kSsxBN) * w.n_col_blocks + cb) * w.n_splits + s;
+        w.partial[pidx * kSsxBN * kNW + (n1 % kSsxBN) * kNW + iw] = make_double2(sx.value(), sy.value());
+      }
+    }
+  }
+}
+
+}  // namespace
+
+void factor_job_size(FactorJob& j, const GppDev& p, int kt, int grid, double share) {
+  j.p = p;
+  j.kt = kt;
+  j.ncb = (p.ng + kFacCols - 1) / kFacCols;
+  // about 12 items per CTA over this instance's share of the launch
+  const double want = std::max(1.0, 12.0 * grid * share);
+  int seg = (int)std::max(1.0, std::min((double)kt, want / j.ncb + 0.5));
+  j.seg_tiles = (kt + seg - 1) / seg;
+  j.n_seg = (kt + j.seg_tiles - 1) / j.seg_tiles;
+  GppWork& w = j.ssx;
+  w = GppWork{};
+  w.band_begin = 0;
+  w.band_count = factor_fuses_ssx(p.nvband) ? p.nvband : 0;
+  w.bn = kSsxBN;
+  w.n_band_blocks = (w.band_count + kSsxBN - 1) / kSsxBN;
+  w.n_col_blocks = j.ncb;
+  w.n_splits = j.n_seg;
+  w.split_len = j.seg_tiles * kFacK;
+  w.n_items = w.n_band_blocks * j.ncb * j.n_seg;
+}
+
+size_t factor_ssx_partial_bytes(const FactorJob& j) {
+  return sizeof(double2) * (size_t)j.ssx.n_band_blocks * j.ncb * j.n_seg * kSsxBN * kNW;
+}
+
+int factor_job_items(const FactorJob& j) {
+  const int rows = kNW * j.p.ng;
+  const int pad = (rows + kOzRows - 1) / kOzRows * kOzRows - rows;
+  return j.ncb * j.n_seg + (pad > 0 ? (j.kt + kZeroTiles - 1) / kZeroTiles : 0);
+}
+
+int factor_blocks_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, factor_kernel<true>, kFacThreads, 0);
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_factor_pass(const FactorJob* jobs, int n_jobs, int total, int grid, cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  factor_kernel<true><<<std::min(grid, total), kFacThreads, 0, s>>>(FactorJob{}, jobs, n_jobs, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_factor_pass(const FactorJob& job, int grid, cudaStream_t s) {
+  const int total = factor_job_items(job);
+  if (total <= 0) return cudaSuccess;
+  factor_kernel<false><<<std::min(grid, total), kFacThreads, 0, s>>>(job, nullptr, 1, total);
+  return cudaGetLastError();
+}
+
+}  // namespace sigma

@@ -1,0 +1,48 @@
+// Tensor-core GPP form (SIGMA_PREC_TENSOR): the factor pass and the batched
+// (grouped) contraction of many instances.
+#pragma once
+
+#include "sigma_internal.cuh"
+#include "ff_ozaki.cuh"
+
+namespace sigma {
+
+constexpr int kFacCols = 16;        // columns (my_igp) per factor tile
+constexpr int kFacK = 32;           // g-vectors per factor tile (one K tile of the contraction)
+constexpr int kFusedBands = 8;      // occupied bands whose ssx sums the factor pass takes
+
+// One instance of the factor pass.  Items are (g-vector segment, column
+// block); an item writes the contraction's A slices of its tiles and, for
+// the occupied bands, the ssx partial sums of its columns over its
+// g-vectors into ssx.partial in the reduction's layout (band block, column
+// block, segment).
+struct FactorJob {
+  GppDev p;
+  unsigned char* a_tiles;  // OzakiPrep::a_tiles of the instance's contraction
+  int kt;                  // K tiles per real / imaginary half
+  int ncb;                 // column blocks of kFacCols columns
+  int n_seg, seg_tiles;    // g-vector segments per column block, K tiles per segment
+  int item_off;            // first global item of the job
+  GppWork ssx;             // ssx partial layout (bn kSsxBN, n_col_blocks ncb, n_splits n_seg)
+};
+
+// Sizes the factor items of one instance whose share of a launch over
+// `grid` CTAs is `share` (its fraction of the launch's (column, g-vector)
+// elements; about 12 items per CTA over the launch) and fills the ssx work
+// layout (partial pointer and item_off left to the caller).
+void factor_job_size(FactorJob& j, const GppDev& p, int kt, int grid, double share);
+size_t factor_ssx_partial_bytes(const FactorJob& j);
+// Items of the job: the (segment, column block) items and those that zero
+// the padding rows of the last row block.
+int factor_job_items(const FactorJob& j);
+int factor_blocks_per_sm();
+// Whether the fused pass covers the occupied bands of this instance.
+inline bool factor_fuses_ssx(int nvband) { return nvband <= kFusedBands; }
+
+// The factor pass over jobs[0 .. n_jobs) (device array; job i's items are
+// [item_off, item_off + factor_job_items)), `total` items in all.
+cudaError_t launch_factor_pass(const FactorJob* jobs, int n_jobs, int total, int grid, cudaStream_t s);
+// One instance, the job passed by value (item_off 0).
+cudaError_t launch_factor_pass(const FactorJob& job, int grid, cudaStream_t s);
+
+}  // namespace sigma

@@ -74,6 +74,7 @@ struct GppWork {
   int ready_first = 0, ready_gs = 1;
   const unsigned* ready_m = nullptr;
   int* ready_status = nullptr;
+  int ready_polls = 1 << 22;   // polls of a gate word (256 ns apart) before a wait gives up
 };
 
 __host__ __device__ __forceinline__ int gate_word(const GppWork& w, int cb, int s) {
@@ -184,6 +185,29 @@ struct OzakiPrep;
 cudaError_t launch_tensor_factors(const GppDev& p, const GppWork& w, const MixedPrep* m, cudaStream_t s,
                                   const OzakiPrep* oz = nullptr);
 
+// Arguments of the fixed-order reduction of one instance.
+struct ReduceArgs {
+  int sch_rows;       // bands whose sums come from sch partials (0: acht_n1 already holds them)
+  const double2* sch_partial;
+  int sch_ncb, sch_splits, sch_bn;
+  const double2* ssx_partial;
+  int ssx_ncb, ssx_splits;
+  int nb, nvband;
+  double2* acht_n1;  // [nb][3]
+  double2* asx_n1;   // [nvband][3]
+};
+// One instance of a grouped reduction (many instances per launch).
+struct ReduceJob {
+  ReduceArgs a;
+  double2 *achtemp, *asxtemp, *acht_n1_loc;
+  int row_off;  // first row (block) of this instance in the band-sum stage
+};
+ReduceJob gpp_reduce_job(const GppWork& sch, const GppWork& ssx, int nb, double2* acht_n1, double2* achtemp,
+                         double2* asxtemp, double2* acht_n1_loc, int row_off);
+int gpp_reduce_job_rows(const ReduceJob& j);
+// The reductions of jobs[0 .. n) (device array): two launches for all.
+cudaError_t launch_gpp_reduce_group(const ReduceJob* jobs, int n, int total_rows, cudaStream_t s);
+
 // Sums the partials of the sch and ssx passes in a fixed order into
 // acht_n1[nb][3] (workspace), achtemp[3], asxtemp[3] and acht_n1_loc[nb].
 // With sch.partial null, acht_n1's first nb rows already hold the band sums.
@@ -256,6 +280,16 @@ __device__ __forceinline__ double guard_thr2(double a, double b2) {
 // FP64 pipe for arithmetic).
 __device__ __forceinline__ bool gt_nonneg(double x, double y) {
   return __double_as_longlong(x) > __double_as_longlong(y);
+}
+
+// Keep decision of the pole guard, wv = |wdiff|^2 > thr, on the integer pipe,
+// with wv finite: an |wdiff|^2 that overflowed to inf drops the term, as in
+// the reference, where rden = 1/inf = 0 makes delw NaN (an overflowing
+// product times 0) and the guard's delwr < limitone test fails
+// (BGW-Kernels/gppKer.cpp:396-404).
+__device__ __forceinline__ bool keep_nonneg(double wv, double thr) {
+  const long long w = __double_as_longlong(wv);
+  return w > __double_as_longlong(thr) && w < 0x7FF0000000000000LL;
 }
 
 // Error-free sum (Knuth TwoSum).

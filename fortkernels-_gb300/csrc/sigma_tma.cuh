@@ -45,12 +45,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: after kWaitSpins polls it records SIGMA_ERR_TIMEOUT in
-// *status and polls once more with the same bound, then gives up.
+__device__ __forceinline__ bool status_set(const int* status) {
+  return *reinterpret_cast<const volatile int*>(status) != 0;
+}
+// Bounded wait on one phase of an mbarrier; true once the phase completed.
+// False when the launch's status word is nonzero (checked every 1024 polls
+// once the first poll fails, so after one wait of a launch has given up every
+// later wait ends within microseconds), or after kWaitSpins polls, which
+// record SIGMA_ERR_TIMEOUT.  A caller that gets false issues no further
+// copies or tensor-core work and leaves its loops.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* status) {
-  for (int i = 0; i < kWaitSpins; ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  for (int i = 1; i <= kWaitSpins; ++i) {
+    if ((i & 1023) == 0 && status_set(status)) return false;
     if (mbar_try_wait(bar, parity)) return true;
-  atomicExch(status, (int)SIGMA_ERR_TIMEOUT);
+  }
+  atomicCAS(status, 0, (int)SIGMA_ERR_TIMEOUT);
+  return false;
+}
+// Bounded wait that ignores the status word, for a CTA that stops after a
+// failure: it waits for the bulk copies or tensor-core operations it issued
+// itself, so that none of them still writes its shared memory or tensor
+// memory when the CTA releases them.
+__device__ __forceinline__ bool mbar_wait_own(uint32_t bar, uint32_t parity) {
   for (int i = 0; i < kWaitSpins; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;

@@ -134,3 +134,28 @@ extern "C" int sigma_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops,
   if (fp32_tflops) *fp32_tflops = res[1];
   return SIGMA_OK;
 }
+
+namespace sigma {
+namespace {
+__global__ void reciprocals_kernel(const double* w, double* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double x = w[i];
+    out[3 * i] = rcp_f64(x);
+    out[3 * i + 1] = rcp_f64_seed32(x);
+    out[3 * i + 2] = __drcp_rn(x);  // IEEE 1/x, correctly rounded
+  }
+}
+}  // namespace
+}  // namespace sigma
+
+extern "C" int sigma_eval_reciprocals(const double* w, double* out, long long n, void* stream) {
+  using namespace sigma;
+  if (!w || !out) return SIGMA_ERR_NULL;
+  if (n <= 0) return SIGMA_ERR_INVALID_SHAPE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  reciprocals_kernel<<<(int)blocks, 256, 0, s>>>(w, out, n);
+  SIGMA_CUDA_TRY(cudaGetLastError());
+  return SIGMA_OK;
+}

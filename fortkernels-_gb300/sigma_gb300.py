@@ -53,11 +53,14 @@ SIGNATURES = {
     "sigma_gpp_fp64": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_mixed": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_tensor": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+    "sigma_gpp_mixed_checked": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                 _P], _I),
     "sigma_gpp_plan_create": ([_P, _I, _I, _I, _I, _I, _I, _P, _P, _I, _I], _I),
     "sigma_gpp_execute": ([_P, _P, _I, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_plan_destroy": ([_P], _I),
     "sigma_gpp_plan_info": ([_P, _P, _P], _I),
     "sigma_gpp_plan_status": ([_P, _P], _I),
+    "sigma_gpp_selftest_gate_timeout": ([_P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "sigma_gpp_plan_set_timing": ([_P, _I], _I),
     "sigma_gpp_plan_timing": ([_P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_fp64_noalloc": ([_I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
@@ -100,6 +103,7 @@ SIGNATURES = {
     "sigma_fill_uniform": ([_P, _LL, _LL, _ULL, _ULL, _LL, _LL, _D, _D, _P], _I),
     "sigma_fill_stress": ([_P, _LL, _ULL, _ULL, _P, _I, _D, _D, _P], _I),
     "sigma_measure_fma_peaks": ([_P, _P, _P], _I),
+    "sigma_eval_reciprocals": ([_P, _P, _LL, _P], _I),
 }
 
 
@@ -333,6 +337,13 @@ class GppPlan:
     def status(self, stream=0):
         """Device status of the last execution (0, or -5 after a bounded wait gave up)."""
         return self.lib.sigma_gpp_plan_status(self.handle, stream)
+
+    def selftest_gate_timeout(self, wx, aqsm, aqsn, ieps, wt, vcoul, wait_polls, stream=0):
+        """sigma_gpp_selftest_gate_timeout: the gated FP64 main pass with gate
+        words nothing writes; returns the device status (-5 expected)."""
+        return self.lib.sigma_gpp_selftest_gate_timeout(
+            self.handle, *[a if isinstance(a, int) else _ptr(a) for a in (wx, aqsm, aqsn, ieps, wt, vcoul)],
+            wait_polls, stream)
 
     def close(self):
         if getattr(self, "handle", None):

@@ -73,6 +73,23 @@ int sigma_gpp_mixed(int number_bands, int nvband, int ncouls, int ngpown, int ns
                     sigma_complex128* achtemp, sigma_complex128* asxtemp,
                     sigma_complex128* acht_n1_loc, void* stream);
 
+/* sigma_gpp_mixed with its error reported: when rel_err_out (double[6]) is
+ * not NULL, the FP64 form also runs on the same inputs and
+ *   rel_err_out[iw]     = |achtemp[iw] - achtemp_fp64[iw]| / |achtemp_fp64[iw]|
+ *   rel_err_out[3 + iw] = the same for asxtemp (0 where both are 0),
+ * the mixed outputs being the ones returned.  The check costs one FP64
+ * evaluation (about 90 times the mixed one at the production shape), so it
+ * is a validation mode.  sigma_gpp_mixed keeps the argument list of
+ * sigma_gpp_fp64 (no extra argument) so that the two are interchangeable
+ * where the reference's loop is replaced (BGW-Kernels/gppKer.cpp:303-439). */
+int sigma_gpp_mixed_checked(int number_bands, int nvband, int ncouls, int ngpown, int nstart, int nend,
+                            const int* inv_igp_index, const int* indinv, const double* wx_array,
+                            double occ, const sigma_complex128* aqsmtemp,
+                            const sigma_complex128* aqsntemp, const sigma_complex128* I_eps_array,
+                            const sigma_complex128* wtilde_array, const double* vcoul,
+                            sigma_complex128* achtemp, sigma_complex128* asxtemp,
+                            sigma_complex128* acht_n1_loc, void* stream, double* rel_err_out);
+
 /* Same contract, tensor-core form (SIGMA_PREC_TENSOR): one frequency set for
  * every band (wx_array[3]); the band sum runs as a complex GEMM on tcgen05
  * tensor cores with split-BF16 operands.  ngpown must be at least ~18 (the
@@ -113,6 +130,22 @@ int sigma_gpp_plan_destroy(sigma_gpp_plan plan);
  * execution: SIGMA_OK, or SIGMA_ERR_TIMEOUT when a bounded wait inside a
  * kernel gave up (results of that execution are then not valid). */
 int sigma_gpp_plan_status(sigma_gpp_plan plan, void* stream);
+
+/* Self-test of the device-side bounded wait (no counterpart in the
+ * reference, whose loops never wait on the device).  Runs the FP64 plan's
+ * shared-frequency main pass on the given device arrays the way the host
+ * drop-in runs it beside its copies, but with gate words that nothing ever
+ * writes and each wait bounded by `wait_polls` polls (256 ns apart), then
+ * waits for `stream` and returns the device status: SIGMA_ERR_TIMEOUT when
+ * the waits gave up as designed (the kernel drops its items and returns; the
+ * CUDA context stays usable).  The next sigma_gpp_execute of the plan, or the
+ * next host drop-in call, starts from a cleared status.  FP64 plans with one
+ * frequency set only (SIGMA_ERR_UNSUPPORTED otherwise). */
+int sigma_gpp_selftest_gate_timeout(sigma_gpp_plan plan, const double* wx_array,
+                                    const sigma_complex128* aqsmtemp, const sigma_complex128* aqsntemp,
+                                    const sigma_complex128* I_eps_array,
+                                    const sigma_complex128* wtilde_array, const double* vcoul,
+                                    int wait_polls, void* stream);
 
 /* Per-launch timing, the device-side counterpart of the reference's chrono
  * timer around its band loop (BGW-Kernels/gppKer.cpp:301, 441).  While
@@ -162,14 +195,18 @@ typedef struct sigma_gpp_batch_s* sigma_gpp_batch;
  * for the library's choice (least padding).  A batch whose instances all
  * share one frequency set per instance (wx_band_stride 0) runs the
  * shared-frequency kernel: tiles 3 = 64 bands x 32 columns, 4 = 32 x 64,
- * 5 = 32 x 32; otherwise the per-band kernel: 0 = 32 x 32, 1 = 16 x 64,
- * 2 = 64 x 16.  A tile of the other family is SIGMA_ERR_UNSUPPORTED.  The
- * tuning table of fortkernels-_gb300/autotune.py chooses per shape class.
- * The mixed form has one tile shape.  precision SIGMA_PREC_TENSOR needs one
- * frequency set per instance and ngpown >= ~18 (SIGMA_ERR_UNSUPPORTED
- * otherwise): each instance's band sum runs as its own split-BF16
- * contraction in stream order, sharing one workspace sized for the largest
- * instance; the occupied-band pass and reductions stay batched. */
+ * 5 = 32 x 32, 6 = 128 x 16; otherwise the per-band kernel: 0 = 32 x 32,
+ * 1 = 16 x 64, 2 = 64 x 16.  A tile of the other family is
+ * SIGMA_ERR_UNSUPPORTED.  The tuning table of fortkernels-_gb300/autotune.py
+ * chooses per shape class.  The mixed form has one tile shape.  precision
+ * SIGMA_PREC_TENSOR needs one frequency set per instance and ngpown >= ~18
+ * (SIGMA_ERR_UNSUPPORTED otherwise); with at most 8 occupied bands per
+ * instance every stage is one launch for all instances (the split-BF16
+ * GEMM over one work table listing every instance's items), each instance
+ * keeping its own slice images (about 36 B per column and g-vector plus
+ * 24 B per band and g-vector of device memory); otherwise each instance's
+ * contraction runs in stream order over one shared workspace.  Every form
+ * reduces all instances with two launches. */
 int sigma_gpp_batch_create(sigma_gpp_batch* batch, int n_instances, const sigma_gpp_instance* inst,
                            int precision, const int* tile_shape);
 

@@ -37,6 +37,15 @@ int sigma_fill_stress(double* wtilde, long long count, unsigned long long seed,
  * milliseconds of kernels on `stream` and synchronises it. */
 int sigma_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops, void* stream);
 
+/* The library's two FP64 reciprocal routines on n positive device values w
+ * (a check of their error bounds; no counterpart in the reference):
+ * out[3i] = rcp_f64(w[i]) (hardware seed, cubic Newton step; within the FP64
+ * rounding unit), out[3i+1] = rcp_f64_seed32(w[i]) (FP32 seed, one Newton
+ * step; within 2^-44.8 relative, from below, for normal w whose reciprocal
+ * is normal), out[3i+2] = the correctly rounded IEEE 1/w.  out is a device
+ * array of 3n doubles.  Asynchronous on `stream`. */
+int sigma_eval_reciprocals(const double* w, double* out, long long n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,69 @@
+"""Device arithmetic the FP64 path's accuracy claim rests on.
+
+rcp_f64_seed32 forms 1/|wdiff|^2 for every kept term of the FP64 kernels
+(the reference divides: BGW-Kernels/gppKer.cpp:397-398): an FP32 seed of the
+leading 23 mantissa bits, the exponent rebuilt on the integer pipe, one FP64
+Newton step; stated within 2^-44.8 relative for normal w whose reciprocal is
+normal.  rcp_f64 (hardware FP64 seed, cubic step) is stated within the FP64
+rounding unit.  Both are checked against the correctly rounded IEEE 1/w.
+"""
+import numpy as np
+import pytest
+import torch
+
+import workload as W
+from conftest import rel_err
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SEED32_BOUND = 2.0 ** -44.8
+RCP64_BOUND = 2.0 ** -52
+
+
+def _sample_w(n, seed):
+    """Normal doubles over exponents -1000..1000 (reciprocals normal), random
+    mantissas, plus the edges of the seed: mantissas 1.0 and all ones, the
+    23-bit truncation boundary, and the pole-guard range [0.25, 1e7]."""
+    rng = np.random.default_rng(seed)
+    mant = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    ex = rng.integers(1023 - 1000, 1023 + 1000, n, dtype=np.uint64)
+    w = (ex << np.uint64(52) | mant).view(np.float64)
+    edges = []
+    for e in (-1000, -300, -1, 0, 1, 2, 300, 1000):
+        for m in (0, (1 << 52) - 1, (1 << 29) - 1, 1 << 29, ((1 << 23) - 1) << 29, (((1 << 23) - 1) << 29) | 1):
+            edges.append(((e + 1023) << 52) | m)
+    edges = np.array(edges, dtype=np.uint64).view(np.float64)
+    guard = np.exp(rng.uniform(np.log(0.25), np.log(1e7), n // 4))
+    return np.concatenate([w, edges, guard])
+
+
+def test_fp64_reciprocals_within_stated_bounds(sigma_lib):
+    w = _sample_w(1 << 20, 5)
+    dw = torch.from_numpy(w).cuda()
+    out = torch.empty(3 * len(w), dtype=torch.float64, device="cuda")
+    st = sigma_lib.load().sigma_eval_reciprocals(dw.data_ptr(), out.data_ptr(), len(w), None)
+    assert st == 0
+    torch.cuda.synchronize()
+    o = out.cpu().numpy().reshape(-1, 3)
+    exact = o[:, 2]
+    assert np.array_equal(exact, 1.0 / w)  # the device's IEEE 1/w is numpy's
+    e_seed = (o[:, 1] - exact) / exact
+    e_rcp = (o[:, 0] - exact) / exact
+    assert np.abs(e_seed).max() <= SEED32_BOUND, np.abs(e_seed).max()
+    assert np.abs(e_rcp).max() <= RCP64_BOUND, np.abs(e_rcp).max()
+    # the Newton step approaches 1/w from below (up to the final rounding)
+    assert np.all(e_seed <= 2.0 ** -53)
+
+
+def test_overflowing_wdiff_drops_the_term(sigma_lib):
+    """A frequency so large that |wdiff|^2 overflows: the reference's rden is
+    1/inf = 0, so every term of that frequency is 0; the FP64 path drops
+    them (no garbage reciprocal of inf)."""
+    prob = W.gpp_random(20, 0, 1024, 40, 43)
+    prob.wx_array = np.array([3.0, 4.0, 1e200])
+    ach, asx, _ = O.gpp(prob)
+    assert ach[2] == 0 and np.all(asx == 0)
+    g = sigma_lib.gpp_host(prob, sigma_lib.PREC_FP64)
+    assert g[0][2] == 0
+    assert rel_err(g[0][:2], ach[:2]).max() <= 1e-12

@@ -333,3 +333,29 @@ def test_production_tensor_within_bar_of_fp64(production):
     assert rel_err(gtc[0], g64[0]).max() <= MIXED_TOL
     assert rel_err(gtc[1], g64[1]).max() <= MIXED_TOL
     assert normwise_err(gtc[2], g64[2]) <= MIXED_TOL
+
+
+def test_mixed_checked_reports_its_error(sigma_lib):
+    """sigma_gpp_mixed_checked: the mixed outputs plus rel_err_out[6], the
+    relative error of each achtemp / asxtemp against the FP64 form."""
+    prob = W.gpp_random(40, 3, 2048, 100, 44, stress=True)
+    lib = sigma_lib.load()
+    inv = np.ascontiguousarray(prob.inv_igp_index, np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, np.int32)
+    c = lambda a: np.ascontiguousarray(a, np.complex128)
+    ins = [c(prob.aqsmtemp), c(prob.aqsntemp), c(prob.I_eps_array), c(prob.wtilde_array)]
+    vc = np.ascontiguousarray(prob.vcoul, np.float64)
+    wx = np.ascontiguousarray(prob.wx_array, np.float64)
+    ach, asx = np.zeros(3, np.complex128), np.zeros(3, np.complex128)
+    err = np.full(6, -1.0)
+    st = lib.sigma_gpp_mixed_checked(prob.number_bands, prob.nvband, prob.ncouls, prob.ngpown, 0, 3,
+                                     inv.ctypes.data, indinv.ctypes.data, wx.ctypes.data, 1.0,
+                                     *[a.ctypes.data for a in ins], vc.ctypes.data, ach.ctypes.data,
+                                     asx.ctypes.data, None, None, err.ctypes.data)
+    assert st == 0
+    g64 = sigma_lib.gpp_host(prob, sigma_lib.PREC_FP64)
+    gmx = sigma_lib.gpp_host(prob, sigma_lib.PREC_MIXED)
+    assert np.array_equal(ach, gmx[0]) and np.array_equal(asx, gmx[1])
+    expect = np.concatenate([rel_err(gmx[0], g64[0]), rel_err(gmx[1], g64[1])])
+    assert np.allclose(err, expect, rtol=1e-12, atol=0)
+    assert err.max() <= MIXED_TOL
