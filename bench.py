@@ -595,6 +595,27 @@ def run_static(S, W, torch, dist, world, stream, sptr, inst):
     return res
 
 
+def time_single_plans(S, torch, dist, world, xs, prec, stream):
+    """The same instances as one device-resident plan each, executed back to
+    back on one stream (plans created and warmed up outside the timed
+    region): ms for one pass over all of them."""
+    f64 = dict(dtype=torch.float64, device="cuda")
+    plans = [S.GppPlan(x.nb, x.nvb, x.nc, x.ng, x.inv, x.indinv, precision=prec) for x in xs]
+    outs = [(torch.zeros(6, **f64), torch.zeros(6, **f64), torch.zeros(2 * x.nb, **f64)) for x in xs]
+    sp = stream.cuda_stream
+
+    def one_pass():
+        for x, pl, o in zip(xs, plans, outs):
+            pl.execute(x.wx, x.aqsm, x.aqsn, x.ieps, x.wt, x.vcoul, *o, stream=sp)
+
+    one_pass()
+    ms = timed(torch, dist, world, one_pass, 1, stream)
+    for pl in plans:
+        pl.close()
+    torch.cuda.empty_cache()
+    return ms
+
+
 def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     """48 uneven GPP instances (workload.batched_shapes) through the batched
     API, one CUDA-graph replay per step, FP64 (tiles from the tuning table)
@@ -629,6 +650,11 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
                      "ms_per_step": round(ms / steps, 3), "steps": steps, "terms_per_step": terms,
                      "items": items, "kernels_per_step": launches, "status": st}
         b.close()
+        torch.cuda.empty_cache()
+        if not args.no_batch_singles:
+            single_ms = time_single_plans(S, torch, dist, world, xs, prec, gs)
+            res[name]["single_plans_ms_per_step"] = round(single_ms, 3)
+            res[name]["batch_over_single_plans_time"] = round((ms / steps) / single_ms, 4)
     ref = golden("config_gpp_batched.npz")
     if ref is not None:
         off = ref["n1_offsets"]
@@ -646,13 +672,15 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
                                               "outputs": 6 * len(outs[name]),
                                               "acht_n1_loc_normwise_max": n1_worst}
     for name in ("mixed", "tensor"):
-        worst, over = 0.0, 0
+        worst, over, by = 0.0, 0, {"achtemp": 0.0, "asxtemp": 0.0}
         for a, m in zip(outs["fp64"], outs[name]):
-            for k in (0, 1):
+            for k, key in ((0, "achtemp"), (1, "asxtemp")):
                 e = np.abs(m[k] - a[k]) / np.abs(a[k])
                 worst = max(worst, float(e.max()))
+                by[key] = max(by[key], float(e.max()))
                 over += int(np.sum(e > 1e-6))
         res[name]["max_rel_err_vs_fp64"] = worst
+        res[name]["max_rel_err_vs_fp64_by_output"] = by
         res[name]["outputs_over_1e-6"] = over
         res[name]["outputs"] = 6 * len(xs)
         res[name]["speedup_vs_fp64_batched"] = round(res[name]["value"] / res["fp64"]["value"], 2)
@@ -685,6 +713,11 @@ def run_ours(args, rank, world, local_rank):
         res = run_ff(S, W, torch, dist, world, stream, sptr, args)
         if rank == 0:
             print(json.dumps({"ff": res}), flush=True)
+        return 0
+    if args.only_ff_sigma:
+        res = run_ff_sigma(S, W, torch, dist, world, stream, sptr)
+        if rank == 0:
+            print(json.dumps({"ff_sigma": res}), flush=True)
         return 0
     if args.only_gpp_tensor:
         import replicas
@@ -955,9 +988,13 @@ def main():
                     help="number_bands,ncouls,ngpown,nfreq of the FF runs (default the production "
                          "512,16384,820,15; smaller only for profiling captures)")
     ap.add_argument("--only-ff", action="store_true", help="run the FF contraction alone (profiling)")
+    ap.add_argument("--only-ff-sigma", action="store_true",
+                    help="run the FF band loop alone at --ff-shape (profiling)")
     ap.add_argument("--batch-instances", type=int, default=48,
                     help="leading instances of the 48-instance batched set (fewer only for profiling)")
     ap.add_argument("--batch-fp64-steps", type=int, default=2)
+    ap.add_argument("--no-batch-singles", action="store_true",
+                    help="skip timing the batched instances as single plans back to back")
     ap.add_argument("--only-batched", action="store_true",
                     help="run the batched measurement alone (profiling captures)")
     ap.add_argument("--gpp-shape", default=None,

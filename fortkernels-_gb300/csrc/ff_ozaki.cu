@@ -317,8 +317,16 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
     uint32_t ph_acce0 = 0, ph_acce1 = 0;
     bool used0 = false, used1 = false, failed = false;
     uint32_t g = 0, gc = 0;
+    // group: the next item's tile count is loaded one item ahead
+    int nst_next = kGroup && blockIdx.x < n_items ? (grp.items[blockIdx.x].w & 0xFFFF) : 0;
     for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
-      const int nst = kGroup ? (grp.items[item].w & 0xFFFF) : oz_decode(oz, item).nst;
+      int nst;
+      if (kGroup) {
+        nst = nst_next;
+        if (item + (int)gridDim.x < n_items) nst_next = grp.items[item + gridDim.x].w & 0xFFFF;
+      } else {
+        nst = oz_decode(oz, item).nst;
+      }
       for (int s = 0; s < nst; ++s, ++g) {
         const int cs = s % kChunkStages;
         const uint32_t tb = gc & 1u;
@@ -357,8 +365,16 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWo
     uint32_t g = 0;   // tiles consumed by this CTA
     uint32_t gc = 0;  // accumulator lifetimes started
     bool failed = false;
+    // group: the next item's tile count is loaded one item ahead
+    int nst_next = kGroup && blockIdx.x < n_items ? (grp.items[blockIdx.x].w & 0xFFFF) : 0;
     for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
-      const int nst = kGroup ? (grp.items[item].w & 0xFFFF) : oz_decode(oz, item).nst;
+      int nst;
+      if (kGroup) {
+        nst = nst_next;
+        if (item + (int)gridDim.x < n_items) nst_next = grp.items[item + gridDim.x].w & 0xFFFF;
+      } else {
+        nst = oz_decode(oz, item).nst;
+      }
       for (int s = 0; s < nst; ++s, ++g) {
         const int cs = s % kChunkStages;
         const uint32_t tb = gc & 1u;

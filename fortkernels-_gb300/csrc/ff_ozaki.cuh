@@ -69,20 +69,27 @@ __device__ __forceinline__ void oz_split3(float x, unsigned short& a, unsigned s
 }
 
 // Slices of 8 consecutive K values of one row, written as three 16-byte
-// chunks (one per slice tile) of a 24 KB block.
+// chunks (one per slice tile) of a 24 KB block.  Two values per paired
+// conversion (cvt.rn.bf16x2.f32 rounds each as __float2bfloat16_rn does, so
+// the slices are those of oz_split3), the pairs already packed.
 __device__ __forceinline__ void oz_put_row_chunk(unsigned char* blk, int r, int ch, const float (&v)[8]) {
-  unsigned short sl[3][8];
+  uint32_t sl[3][4];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) oz_split3(v[j], sl[0][j], sl[1][j], sl[2][j]);
-#pragma unroll
-  for (int s = 0; s < 3; ++s) {
-    uint4 q;
-    q.x = sl[s][0] | ((uint32_t)sl[s][1] << 16);
-    q.y = sl[s][2] | ((uint32_t)sl[s][3] << 16);
-    q.z = sl[s][4] | ((uint32_t)sl[s][5] << 16);
-    q.w = sl[s][6] | ((uint32_t)sl[s][7] << 16);
-    *reinterpret_cast<uint4*>(blk + s * kOzSliceBytes + tma::sw64_offset(r, ch * 8)) = q;
+  for (int j = 0; j < 4; ++j) {
+    const __nv_bfloat162 h1 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+    const float2 f1 = __bfloat1622float2(h1);
+    const float r0 = v[2 * j] - f1.x, r1 = v[2 * j + 1] - f1.y;  // exact
+    const __nv_bfloat162 h2 = __floats2bfloat162_rn(r0, r1);
+    const float2 f2 = __bfloat1622float2(h2);
+    const __nv_bfloat162 h3 = __floats2bfloat162_rn(r0 - f2.x, r1 - f2.y);
+    sl[0][j] = *reinterpret_cast<const uint32_t*>(&h1);
+    sl[1][j] = *reinterpret_cast<const uint32_t*>(&h2);
+    sl[2][j] = *reinterpret_cast<const uint32_t*>(&h3);
   }
+#pragma unroll
+  for (int s = 0; s < 3; ++s)
+    *reinterpret_cast<uint4*>(blk + s * kOzSliceBytes + tma::sw64_offset(r, ch * 8)) =
+        make_uint4(sl[s][0], sl[s][1], sl[s][2], sl[s][3]);
 }
 
 // The slices of A'[R][k0 .. k0+8): real parts re (K' = k) and imaginary

@@ -22,21 +22,26 @@ namespace sigma {
 __device__ __forceinline__ void split_exact(double x, float& hi, float& lo) {
   const unsigned int whi = (unsigned int)__double2hiint(x), wlo = (unsigned int)__double2loint(x);
   const unsigned int sign = whi & 0x80000000u;
-  const int ex = (int)((whi >> 20) & 0x7FFu);
-  const unsigned int mant = ((whi & 0xFFFFFu) << 3) | (wlo >> 29);  // leading 23 fraction bits
+  const unsigned int ex = (whi >> 20) & 0x7FFu;
+  if (ex - 949u <= 201u) {  // 949 <= ex <= 1150: hi and lo normal FP32 values
+    // (whi << 3 | wlo >> 29) holds the exponent's low 8 bits and the leading
+    // 23 fraction bits; ex - 896 = (ex mod 256) + 128 modulo 256 in this range
+    const unsigned int f = __funnelshift_l(wlo, whi, 3);
+    hi = __uint_as_float(((f + 0x40000000u) & 0x7FFFFFFFu) | sign);
+    const float l = __uint2float_rn(wlo & 0x1FFFFFFFu) * __uint_as_float((ex - 948u) << 23);  // x 2^(ex - 1075)
+    lo = __uint_as_float(__float_as_uint(l) ^ sign);
+    return;
+  }
   unsigned int hb;
-  if (ex > 1150) {
-    hb = sign | 0x7F800000u | ((ex == 2047 && ((whi & 0xFFFFFu) | wlo)) ? 0x400000u : 0u);
-  } else if (ex >= 897) {
-    hb = sign | ((unsigned int)(ex - 896) << 23) | mant;
+  if (ex > 1150u) {
+    hb = sign | 0x7F800000u | ((ex == 2047u && ((whi & 0xFFFFFu) | wlo)) ? 0x400000u : 0u);
+  } else if (ex >= 897u) {
+    hb = sign | ((ex - 896u) << 23) | ((whi & 0xFFFFFu) << 3) | (wlo >> 29);
   } else {
     hb = sign;
   }
   hi = __uint_as_float(hb);
-  const float m = __uint2float_rn(wlo & 0x1FFFFFFFu);                        // < 2^29
-  const float scale = __uint_as_float((unsigned int)max(ex - 948, 0) << 23);  // 2^(ex - 1075), or 0
-  const float l = (ex >= 949 && ex <= 1150) ? m * scale : 0.f;
-  lo = sign ? -l : l;
+  lo = 0.f;
 }
 
 struct FF {

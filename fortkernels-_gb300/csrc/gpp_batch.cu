@@ -137,11 +137,14 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
     set_last_cuda_error(e, "cudaMalloc(batch slice images)", __LINE__);
     return SIGMA_ERR_ALLOC;
   }
-  // about 20 GEMM items per CTA over the whole group (one CTA per SM), at
-  // most 256 K' tiles per item: the drain warps carry an item's sum in FP32
+  // 32 K' tiles per GEMM item: the drain warps carry an item's sum in FP32
   // registers across its accumulator lifetimes (4 K' tiles each), and the
-  // rounding error of that running sum grows with their number
-  const int hint = (int)std::min(256LL, std::max(8LL, tiles / (20LL * sms)));
+  // rounding error of that running sum grows with their number (items of
+  // 256 tiles put 4 of the 48-instance set's 288 outputs above 1e-6).  An
+  // item's epilogue takes less time than one accumulator lifetime of the
+  // tensor cores, which meanwhile fill the other TMEM accumulator pair.
+  (void)tiles;
+  const int hint = 32;
   b->ff.assign(n, nullptr);
   b->fac_grid = sms * factor_blocks_per_sm();
   std::vector<FactorJob> fac(n);

@@ -20,9 +20,10 @@
 //   second branch: ssx = -G / (2 (wtilde + wx))  (0 < |wdiff|^2 < |wtilde|^2 / to1)
 //   otherwise      0,
 // summed over g-vectors with aqsn[n1][ig].  The pass forms them from the
-// values it already holds and stages them in shared memory; one thread per
-// (band, frequency, column) then sums the tile's 32 g-vectors (FP32 runs of
-// 8 folded into float-float accumulators).  At the end of an item each
+// values it already holds and stages them in shared memory; four lanes per
+// (band, frequency, column) then sum the tile's 32 g-vectors as a pairwise
+// tree in FP32 (8 products per lane, then two butterfly steps across the
+// four lanes) folded into a float-float accumulator.  At the end of an item each
 // column's sums are multiplied by conj(aqsm[n1][igp]) occ vcoul[igp] in FP64
 // and summed over the item's columns in a fixed order.  The inputs are read
 // once for both, and no intermediate operand is written.
@@ -46,9 +47,13 @@ struct FactorSmem {
   float2 x[kFacCols][kNW][kFacK + 1];          // the tile's ssx factors
   float2 an[kFusedBands][kFacK];               // occupied bands' aqsn over the tile's g-vectors
   double2 red[kFusedBands][kNW][kFacCols];     // item epilogue: per-column ssx sums
+  float4 acc[kFusedBands * kNW * kFacCols];    // ssx float-float accumulators (hi.x, hi.y, lo.x, lo.y),
+                                               // each read and written by its owning lane only
 };
-// ssx sums a thread owns: outputs o = tid + 256 r, (band, frequency, column)
-constexpr int kSsxOwn = (kFusedBands * kNW * kFacCols + 255) / 256;
+// ssx sums: output o = r * 64 + 8 * warp + lane / 4 is computed by the four
+// lanes 4 (lane / 4) + q (q = 0..3, 8 g-vectors each) in round r, so every
+// warp takes part; the lane with q = 0 owns the output's accumulator
+constexpr int kSsxRounds = (kFusedBands * kNW * kFacCols * 4 + 255) / 256;
 
 __device__ __forceinline__ int find_job(const FactorJob* jobs, int n, int item) {
   int lo = 0, hi = n - 1;
@@ -74,21 +79,50 @@ __device__ __forceinline__ void put_a(unsigned char* a_tiles, int kt, int R, int
   oz_put_row_chunk(base + (size_t)(kt + t) * kOzOperandBytes, r, ch, im);
 }
 
-// x * conj-free product of float-float values rounded once to FP32 with
-// the products' errors carried: (a.hi + a.lo)(g.hi + g.lo) - (b.hi + b.lo)(h.hi + h.lo)
-// within ~1 ulp of the result (the one rounding of the hi difference plus
-// the dropped lo * lo terms, 2^-48 of the products).
+// x - y as an unnormalised pair (TwoSum of the hi parts plus the lo
+// parts): exact to ~2^-46 of the operands, for a product or square next.
+__device__ __forceinline__ FF ff_sub_raw(FF x, FF y) {
+  float s, e;
+  two_sum_f(x.hi, -y.hi, s, e);
+  return FF{s, e + (x.lo - y.lo)};
+}
+// c^2 + b2 (b2 normalised), normalised: the square's exact error by FMA.
+__device__ __forceinline__ FF ff_sq_add(FF c, FF b2) {
+  const float p = c.hi * c.hi;
+  const float e = fmaf(2.f * c.hi, c.lo, fmaf(c.hi, c.hi, -p));
+  float s, t;
+  two_sum_f(p, b2.hi, s, t);
+  return ff_norm(s, t + (e + b2.lo));
+}
+// (w g - se) r rounded once to FP32, for an FP32-exact w (w.lo == 0): w g
+// as an exact product pair, the difference by TwoSum, no normalisation
+// before the final rounding (same accuracy as the general form).
+__device__ __forceinline__ float ff_factor_round(float w, FF g, FF se, FF r) {
+  const float p = w * g.hi;
+  const float e = fmaf(w, g.lo, fmaf(w, g.hi, -p));
+  float s, t;
+  two_sum_f(p, -se.hi, s, t);
+  t += e - se.lo;
+  return fmaf(s, r.hi, fmaf(s, r.lo, t * r.hi));
+}
+
+// a g - b h of float-float values rounded once to FP32: the products' exact
+// errors by FMA, the difference of the hi products by TwoSum, so the result
+// is within 1/2 ulp plus ~2^-46 of the products' magnitude (lo * lo terms
+// dropped).
 __device__ __forceinline__ float ff_dot2_round(FF a, FF g, FF b, FF h) {
   const float p1 = a.hi * g.hi, p2 = b.hi * h.hi;
   const float e1 = fmaf(a.hi, g.hi, -p1), e2 = fmaf(b.hi, h.hi, -p2);
   const float t = fmaf(a.hi, g.lo, fmaf(a.lo, g.hi, e1)) - fmaf(b.hi, h.lo, fmaf(b.lo, h.hi, e2));
-  return (p1 - p2) + t;
+  float s, es;
+  two_sum_f(p1, -p2, s, es);  // the difference exact: one rounding at the end
+  return s + (es + t);
 }
 
 // kGroup: the jobs of a batch from a device array; else the one job `single`
 // (a kernel parameter, so that an execution can be captured in a graph).
 template <bool kGroup>
-__global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob single,
+__global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob single,
                                                                  const FactorJob* __restrict__ jobs, int n_jobs,
                                                                  int total) {
   __shared__ FactorSmem sm;
@@ -117,17 +151,20 @@ __global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob 
     const int outputs = nvb * kNW * kFacCols;  // ssx sums: (band, frequency, column)
     FF wx[kNW];
     float wxh[kNW], wxl[kNW], iwx2[kNW];
+    bool wx32 = true;  // every frequency exact in FP32 (the mini-app's 3, 4, 5)
 #pragma unroll
     for (int iw = 0; iw < kNW; ++iw) {
       wx[iw] = ff_of(p.wx[iw]);
+      wx32 = wx32 && wx[iw].lo == 0.f;
       wxh[iw] = __double2float_rn(p.wx[iw]);
       wxl[iw] = __double2float_rn(p.wx[iw] - (double)wxh[iw]);
       iwx2[iw] = __double2float_rn(rcp_f64(p.wx[iw] * p.wx[iw]));
     }
     // float-float accumulators of the ssx sums this thread owns
-    float2 ahi[kSsxOwn], alo[kSsxOwn];
-#pragma unroll
-    for (int r = 0; r < kSsxOwn; ++r) ahi[r] = alo[r] = make_float2(0.f, 0.f);
+    for (int r = 0; r < kSsxRounds; ++r) {
+      const int o = r * (kFacThreads / 4) + warp * 8 + (lane >> 2);
+      if ((lane & 3) == 0 && o < outputs) sm.acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 
     for (int t = t_begin; t < t_end; ++t) {
       const int ig0 = t * kFacK;
@@ -165,8 +202,7 @@ __global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob 
           unsigned mask = 0u;
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            const FF c = ff_add(wx[iw], ff_neg(a));
-            const FF wv = ff_add(ff_mul(c, c), b2);
+            const FF wv = ff_sq_add(ff_sub_raw(wx[iw], a), b2);  // |wdiff|^2
             // keep: |wdiff|^2 > max(0.25, |wtilde|^2 * 4e-6), i.e. both
             // wv > 0.25 and wv * 250000 > |wtilde|^2 (250000 exact in FP32)
             bool near;
@@ -179,8 +215,12 @@ __global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob 
             if (near) keep = keep_fp64(p.wx[iw], wt.x, wt.y);  // within 2^-30 of a threshold
             if (keep) {
               const FF r = ff_rcp(wv);
-              yt[iw] = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
-                                   ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
+              if (wx32)
+                yt[iw] = make_float2(ff_factor_round(wx[iw].hi, gx, sex, r),
+                                     ff_factor_round(wx[iw].hi, gy, sey, r));
+              else
+                yt[iw] = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
+                                     ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
             }
             mask |= keep ? (1u << iw) : 0u;
             if (nvb > 0 && !keep) {
@@ -236,24 +276,38 @@ __global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob 
         }
         put_a(J.a_tiles, J.kt, iw * p.ng + col, ig0 + ch * 8, re, im);
       }
-      // the tile's ssx products: output o = (band n1, frequency iw, column pl),
-      // FP32 runs of 8 g-vectors folded into float-float
+      // the tile's ssx products: output o = (band n1, frequency iw, column
+      // pl); lane quarter q sums g-vectors 8q .. 8q+7 in FP32, two butterfly
+      // steps add the quarters, lane q = 0 folds the tile sum into
+      // float-float
+#pragma unroll 1
+      for (int r = 0; r < kSsxRounds; ++r) {
+        const int o = r * (kFacThreads / 4) + warp * 8 + (lane >> 2), q = lane & 3;
+        if (r * (kFacThreads / 4) < outputs) {  // warp-uniform
+          float2 run = make_float2(0.f, 0.f);
+          if (o < outputs) {
+            const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
+            float2 t[8];
 #pragma unroll
-      for (int r = 0; r < kSsxOwn; ++r) {
-        const int o = tid + r * kFacThreads;
-        if (o < outputs) {
-          const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
-#pragma unroll
-          for (int k0 = 0; k0 < kFacK; k0 += 8) {
-            float2 run = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int k = k0; k < k0 + 8; ++k) {
-              const float2 an = sm.an[n1][k], x = sm.x[pl][iw][k];
-              run.x += fmaf(an.x, x.x, -an.y * x.y);
-              run.y += fmaf(an.x, x.y, an.y * x.x);
+            for (int k = 0; k < 8; ++k) {
+              const float2 an = sm.an[n1][8 * q + k], x = sm.x[pl][iw][8 * q + k];
+              t[k] = make_float2(fmaf(an.x, x.x, -an.y * x.y), fmaf(an.x, x.y, an.y * x.x));
             }
-            ff_add(ahi[r].x, alo[r].x, run.x);
-            ff_add(ahi[r].y, alo[r].y, run.y);
+#pragma unroll
+            for (int h = 4; h >= 1; h >>= 1)
+#pragma unroll
+              for (int k = 0; k < h; ++k) t[k] = make_float2(t[k].x + t[k + h].x, t[k].y + t[k + h].y);
+            run = t[0];
+          }
+          run.x += __shfl_xor_sync(0xffffffffu, run.x, 1);
+          run.y += __shfl_xor_sync(0xffffffffu, run.y, 1);
+          run.x += __shfl_xor_sync(0xffffffffu, run.x, 2);
+          run.y += __shfl_xor_sync(0xffffffffu, run.y, 2);
+          if (q == 0 && o < outputs) {
+            float4 a = sm.acc[o];
+            ff_add(a.x, a.z, run.x);
+            ff_add(a.y, a.w, run.y);
+            sm.acc[o] = a;
           }
         }
       }
@@ -262,10 +316,9 @@ __global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob 
 
     if (nvb > 0) {
       // each column's sums x conj(aqsm[n1][igp]) occ vcoul[igp] in FP64
-#pragma unroll
-      for (int r = 0; r < kSsxOwn; ++r) {
-        const int o = tid + r * kFacThreads;
-        if (o < outputs) {
+      for (int r = 0; r < kSsxRounds; ++r) {
+        const int o = r * (kFacThreads / 4) + warp * 8 + (lane >> 2);
+        if ((lane & 3) == 0 && o < outputs) {
           const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
           const int my_igp = cb * kFacCols + pl;
           const int igp = my_igp < p.ng ? p.igp_of[my_igp] : -1;
@@ -273,8 +326,9 @@ __global__ void __launch_bounds__(kFacThreads, 3) factor_kernel(const FactorJob 
           if (igp >= 0) {
             const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
             const double f = p.occ * p.vcoul[igp];
-            const double sx = (double)ahi[r].x + (double)alo[r].x;
-            const double sy = (double)ahi[r].y + (double)alo[r].y;
+            const float4 a = sm.acc[o];
+            const double sx = (double)a.x + (double)a.z;
+            const double sy = (double)a.y + (double)a.w;
             // (sx + i sy) conj(am) f
             v = make_double2(fma(sx, am.x, sy * am.y) * f, fma(sy, am.x, -sx * am.y) * f);
           }

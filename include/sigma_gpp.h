@@ -53,6 +53,17 @@ extern "C" {
  * overlap the sum; the other forms copy on `stream` first.  indinv has
  * ncouls entries, as in the reference; wx_array has 3 entries shared by every
  * band.  Host buffers in pinned memory copy fastest.
+ *
+ * State: the drop-ins keep ONE cached plan (the last shape, index maps and
+ * form), one input arena and one copy stream with its gate words per
+ * process, for the device that was current at the last call.  Calls are
+ * serialised by a library mutex.  A call on another device, or with another
+ * shape or form, drops that state and builds it anew (a plan costs a few
+ * milliseconds and device allocations), so a process that alternates
+ * between devices or shapes re-plans on every call: use one process per
+ * device (the replica layout), or the plan API (sigma_gpp_plan_create /
+ * sigma_gpp_execute), which keeps one plan per shape and device.
+ * sigma_shutdown() frees the cached state.
  * ------------------------------------------------------------------------- */
 int sigma_gpp_fp64(int number_bands, int nvband, int ncouls, int ngpown, int nstart, int nend,
                    const int* inv_igp_index, const int* indinv, const double* wx_array,

@@ -1,6 +1,7 @@
 """Regenerates the golden fixtures from the reference itself.
 
-Needs the reference checkout (REFERENCE_ROOT, default /root/reference); the
+Needs the reference checkout (REFERENCE_ROOT; oracle/build.py, the build
+recipe that reads it, gives the default location); the
 fixtures it writes are committed so the tests run without it.
 
   gpp_reference_constfill.json  achtemp printed by the unmodified
