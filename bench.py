@@ -63,6 +63,7 @@ CPU_MAX_BANDS = 256
 NB, NVB, NC, NPG = 512, 2, 32768, 20
 NG = NC // NPG
 PRODUCTION = (NB, NVB, NC, NPG)
+PER_BAND_WX = False
 GOLDEN = ROOT / "tests" / "golden"
 
 
@@ -254,7 +255,11 @@ class Instance:
         if stress:
             S.fill_stress_device(self.wt.data_ptr(), NG * NC, seed, W.AID_STRESS, W.wx_frequencies())
         S.fill_real_device(self.vcoul.data_ptr(), NC, seed, W.AID_VCOUL, 0.1, 10.0)
-        self.wx = torch.tensor(W.wx_frequencies(), dtype=torch.float64, device=d)
+        # PER_BAND_WX: the three frequencies stored once per band (stride 3),
+        # which selects the per-band-frequency kernels (profiling captures)
+        wx = W.wx_frequencies()
+        self.wx_stride = 3 if PER_BAND_WX else 0
+        self.wx = torch.tensor(np.tile(wx, NB) if PER_BAND_WX else wx, dtype=torch.float64, device=d)
         self.inv, self.indinv = W.gpp_index_maps(NC, NG)
         self.ach = torch.zeros(6, dtype=torch.float64, device=d)
         self.asx = torch.zeros(6, dtype=torch.float64, device=d)
@@ -262,7 +267,7 @@ class Instance:
 
     def run(self, plan, stream):
         plan.execute(self.wx, self.aqsm, self.aqsn, self.ieps, self.wt, self.vcoul, self.ach,
-                     self.asx, self.n1, stream=stream)
+                     self.asx, self.n1, wx_band_stride=self.wx_stride, stream=stream)
 
     def outputs(self):
         return tuple(t.cpu().numpy().view(np.complex128).copy() for t in (self.ach, self.asx, self.n1))
@@ -719,6 +724,23 @@ def run_ours(args, rank, world, local_rank):
         if rank == 0:
             print(json.dumps({"ff_sigma": res}), flush=True)
         return 0
+    if args.only_gpp_forms:
+        import replicas
+        inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
+        res = {}
+        for name in args.only_gpp_forms.split(","):
+            prec = {"fp64": S.PREC_FP64, "mixed": S.PREC_MIXED, "tensor": S.PREC_TENSOR}[name]
+            pl = S.GppPlan(NB, NVB, NC, NG, inst.inv, inst.indinv, precision=prec)
+            _, terms = pl.info()
+            for _ in range(args.warmup):
+                inst.run(pl, sptr)
+            ms = timed(torch, dist, world, lambda: inst.run(pl, sptr), args.steps, stream)
+            pl.close()
+            res[name] = {"value": round(terms * world / (ms / args.steps * 1e-3) / 1e9, 4), "unit": UNIT,
+                         "ms_per_step": round(ms / args.steps, 3)}
+        if rank == 0:
+            print(json.dumps({"gpp_forms": res, "per_band_wx": PER_BAND_WX}), flush=True)
+        return 0
     if args.only_gpp_tensor:
         import replicas
         inst = Instance(S, W, torch, seed=replicas.rank_seed(W.GPP_PRODUCTION_SEED, rank))
@@ -997,12 +1019,20 @@ def main():
                     help="skip timing the batched instances as single plans back to back")
     ap.add_argument("--only-batched", action="store_true",
                     help="run the batched measurement alone (profiling captures)")
+    ap.add_argument("--per-band-wx", action="store_true",
+                    help="frequencies stored per band (the per-band-frequency kernels; FP64 and mixed "
+                         "only, for profiling captures)")
+    ap.add_argument("--only-gpp-forms", default=None,
+                    help="comma list of fp64,mixed,tensor: run those plans alone on the instance "
+                         "(profiling captures)")
     ap.add_argument("--gpp-shape", default=None,
                     help="number_bands,nvband,ncouls,nodes_per_group of the GPP instance (default the "
                          "production 512,2,32768,20; smaller only for profiling captures)")
     args = ap.parse_args()
     if args.gpp_shape:
         set_shape(*(int(x) for x in args.gpp_shape.split(",")))
+    global PER_BAND_WX
+    PER_BAND_WX = args.per_band_wx
     if args.ff_shape:
         global FF_SHAPE
         FF_SHAPE = tuple(int(x) for x in args.ff_shape.split(","))

@@ -91,14 +91,14 @@ __device__ __forceinline__ bool ff_gt(FF x, FF y, bool& near) {
 // x > y for non-negative normalised float-float values, taken on the hi
 // parts when they differ by more than 2^-21 of the larger (|lo| <= 2^-24
 // |hi| and one rounding of the difference cannot flip the sign then), else
-// with the full compare; `near` as ff_gt.  Same result as ff_gt.
+// with the full compare; `near` as ff_gt.  Same result as ff_gt, without a
+// branch.
 __device__ __forceinline__ bool ff_gt_fast(FF x, FF y, bool& near) {
-  const float d = x.hi - y.hi;
-  if (fabsf(d) > 4.76837158e-07f * fmaxf(x.hi, y.hi)) {  // 2^-21
-    near = false;
-    return d > 0.f;
-  }
-  return ff_gt(x, y, near);
+  const float d = x.hi - y.hi, m = fmaxf(x.hi, y.hi);
+  const bool clear = fabsf(d) > 4.76837158e-07f * m;  // 2^-21
+  const float full = d + (x.lo - y.lo);
+  near = !clear && fabsf(full) <= 9.3132257e-10f * m;  // 2^-30
+  return clear ? d > 0.f : full > 0.f;
 }
 
 // The pole-guard decisions of the FP64 path (guard_w / guard_thr /

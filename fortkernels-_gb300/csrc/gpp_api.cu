@@ -215,7 +215,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
       d.nc = ncouls;
       d.ng = ngpown;
       p->fused = true;
-      p->fac_grid = sms * factor_blocks_per_sm();
+      p->fac_grid = sms * factor_blocks_per_sm(nvband);
       factor_job_size(p->fac, d, oz->kt, p->fac_grid, 1.0);
       p->fac.a_tiles = oz->a_tiles;
       p->fac.item_off = 0;

@@ -63,7 +63,7 @@ struct sigma_gpp_batch_s {
   bool grouped = false;            // every stage one launch for all instances
   void* group_block = nullptr;     // descriptors, item table, ssx partials
   const sigma::FactorJob* d_fac = nullptr;
-  int fac_total = 0, fac_grid = 0;
+  int fac_total = 0, fac_grid = 0, fac_nvband = 0;
   sigma::OzGroup grp{};
   // grouped reductions (every form)
   const sigma::ReduceJob* d_red = nullptr;
@@ -137,16 +137,17 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
     set_last_cuda_error(e, "cudaMalloc(batch slice images)", __LINE__);
     return SIGMA_ERR_ALLOC;
   }
-  // 32 K' tiles per GEMM item: the drain warps carry an item's sum in FP32
-  // registers across its accumulator lifetimes (4 K' tiles each), and the
-  // rounding error of that running sum grows with their number (items of
-  // 256 tiles put 4 of the 48-instance set's 288 outputs above 1e-6).  An
-  // item's epilogue takes less time than one accumulator lifetime of the
-  // tensor cores, which meanwhile fill the other TMEM accumulator pair.
+  // each instance's GEMM items sized as its single-instance plan sizes them
+  // (about 20 per CTA of the instance's own contraction): the tensor form's
+  // errors depend on where the K splits fall (the drain warps' FP32 sums
+  // span an item's accumulator lifetimes), and this sizing keeps them at the
+  // single plans' level on the 48-instance set
   (void)tiles;
-  const int hint = 32;
+  const int hint = 0;
   b->ff.assign(n, nullptr);
-  b->fac_grid = sms * factor_blocks_per_sm();
+  b->fac_nvband = 0;
+  for (int i = 0; i < n; ++i) b->fac_nvband = std::max(b->fac_nvband, inst[i].nvband);
+  b->fac_grid = sms * factor_blocks_per_sm(b->fac_nvband);
   std::vector<FactorJob> fac(n);
   std::vector<OzGroupJob> jobs(n);
   std::vector<int4> items;
@@ -555,7 +556,7 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
     // every instance in each launch: factors (A slices, occupied bands),
     // B slices and epilogue factors, the GEMM over the group's item table,
     // its reduction
-    SIGMA_CUDA_TRY(launch_factor_pass(b->d_fac, b->n, b->fac_total, b->fac_grid, s));
+    SIGMA_CUDA_TRY(launch_factor_pass(b->d_fac, b->n, b->fac_total, b->fac_grid, b->fac_nvband, s));
     SIGMA_CUDA_TRY(launch_ozaki_group_prep(b->grp, s));
     SIGMA_CUDA_TRY(launch_ozaki_group_gemm(b->grp, device_sm_count(), s));
     SIGMA_CUDA_TRY(launch_ozaki_group_reduce(b->grp, s));

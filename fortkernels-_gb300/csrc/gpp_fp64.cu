@@ -256,7 +256,9 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const int tx = tid & 15, ty = tid >> 4;
   const int band_end = w.band_begin + w.band_count;
   const ItemCoord ic = decode_item(w, item);
-  const int n1_0 = w.band_begin + ic.bb * BN;
+  // block origin and partial-slot stride from the pass's layout (w.bn): a
+  // ragged last band block may run a shorter item (BN < w.bn)
+  const int n1_0 = w.band_begin + ic.bb * w.bn;
   const int p0 = ic.cb * BP;
   const int ig_begin = ic.s * w.split_len;
   const int ig_end = min(ig_begin + w.split_len, p.nc);
@@ -381,7 +383,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       }
     if (tx == 0) {
 #pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) w.partial[ic.pidx * BN * kNW + bl * kNW + iw] = part[iw];
+      for (int iw = 0; iw < kNW; ++iw) w.partial[ic.pidx * w.bn * kNW + bl * kNW + iw] = part[iw];
     }
   }
 }
@@ -408,6 +410,33 @@ constexpr size_t smax(size_t a, size_t b) { return a > b ? a : b; }
 constexpr size_t kSchYBatchSmem =
     smax(smax(sizeof(SchYSmem<64, 32>), sizeof(SchYSmem<32, 64>)), sizeof(SchYSmem<128, 16>));
 
+// Item of an instance's shared-frequency pass with tile t: the last band
+// block runs the half-height item when its remaining bands fit (less
+// padded work; the slot layout stays the tile's).
+__device__ __forceinline__ void sch_fp64y_batch_item(const GppDev& p, const GppWork& w, int tile, int local,
+                                                     unsigned char* smem_raw, int tid) {
+  const ItemCoord ic = decode_item(w, local);
+  const bool half = w.band_count - ic.bb * w.bn <= w.bn / 2;  // bands of this item's block
+  switch (tile) {
+    case kTileY32x64:
+      if (half) sch_fp64y_item<16, 64>(p, w, local, smem_raw, tid);
+      else sch_fp64y_item<32, 64>(p, w, local, smem_raw, tid);
+      break;
+    case kTileY32x32:
+      if (half) sch_fp64y_item<16, 32>(p, w, local, smem_raw, tid);
+      else sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid);
+      break;
+    case kTileY128x16:
+      if (half) sch_fp64y_item<64, 16>(p, w, local, smem_raw, tid);
+      else sch_fp64y_item<128, 16>(p, w, local, smem_raw, tid);
+      break;
+    default:
+      if (half) sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid);
+      else sch_fp64y_item<64, 32>(p, w, local, smem_raw, tid);
+      break;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchView b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
@@ -422,12 +451,7 @@ __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchVi
     const GppDev p = b.dev[inst];
     const GppWork w = b.work[inst];
     const int local = g - b.item_off[inst];
-    switch (b.tile[inst]) {
-      case kTileY32x64: sch_fp64y_item<32, 64>(p, w, local, smem_raw, tid); break;
-      case kTileY32x32: sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid); break;
-      case kTileY128x16: sch_fp64y_item<128, 16>(p, w, local, smem_raw, tid); break;
-      default: sch_fp64y_item<64, 32>(p, w, local, smem_raw, tid); break;
-    }
+    sch_fp64y_batch_item(p, w, b.tile[inst], local, smem_raw, tid);
   }
 }
 

@@ -120,6 +120,20 @@ extern "C" int sigma_gpp_fp64_noalloc(int number_bands, int nvband, int ncouls, 
     cudaGetLastError();
     return SIGMA_ERR_NO_DEVICE;
   }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // The column map comes from a reused host buffer and the scratch from one
+  // shared array: a captured call would replay stale contents, so capture is
+  // refused before anything is queued.
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &capturing) != cudaSuccess) {
+    cudaGetLastError();
+    return SIGMA_ERR_CUDA;
+  }
+  if (capturing != cudaStreamCaptureStatusNone) {
+    set_last_error_text("sigma_gpp_fp64_noalloc: the stream is being captured; this entry point "
+                        "does not run inside a CUDA graph");
+    return SIGMA_ERR_UNSUPPORTED;
+  }
   void* scratch = nullptr;
   int st = scratch_address(dev, &scratch);
   if (st != SIGMA_OK) return st;
@@ -154,7 +168,6 @@ extern "C" int sigma_gpp_fp64_noalloc(int number_bands, int nvband, int ncouls, 
   ssx.partial = reinterpret_cast<double2*>(base + o_ssx);
   double2* acht_n1 = reinterpret_cast<double2*>(base + o_n1);
 
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   // The array keeps the previous call's contents: the item counters must
   // start at zero; every other byte the kernels read is written first.  The
   // column map is copied from pageable host memory, which the runtime stages

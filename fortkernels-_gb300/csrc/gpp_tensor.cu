@@ -21,9 +21,9 @@
 //   otherwise      0,
 // summed over g-vectors with aqsn[n1][ig].  The pass forms them from the
 // values it already holds and stages them in shared memory; four lanes per
-// (band, frequency, column) then sum the tile's 32 g-vectors as a pairwise
-// tree in FP32 (8 products per lane, then two butterfly steps across the
-// four lanes) folded into a float-float accumulator.  At the end of an item each
+// (band, frequency, column) then take 8 g-vectors of a tile each and fold
+// each 4-term FP32 tree sum into the lane's own float-float accumulator;
+// the four accumulators are added at the end of the item.  At the end of an item each
 // column's sums are multiplied by conj(aqsm[n1][igp]) occ vcoul[igp] in FP64
 // and summed over the item's columns in a fixed order.  The inputs are read
 // once for both, and no intermediate operand is written.
@@ -44,15 +44,21 @@ constexpr int kZeroTiles = 64;  // K tiles per padding-row item
 
 struct FactorSmem {
   float2 y[kNW][kFacCols][kFacK + 1];          // the tile's factors for the slice writes
-  float2 x[kFacCols][kNW][kFacK + 1];          // the tile's ssx factors
+  union {
+    float2 x[kFacCols][kNW][kFacK + 1];        // the tile's ssx factors
+    double2 red[kFusedBands][kNW][kFacCols];   // item epilogue: per-column ssx sums
+  };
   float2 an[kFusedBands][kFacK];               // occupied bands' aqsn over the tile's g-vectors
-  double2 red[kFusedBands][kNW][kFacCols];     // item epilogue: per-column ssx sums
-  float4 acc[kFusedBands * kNW * kFacCols];    // ssx float-float accumulators (hi.x, hi.y, lo.x, lo.y),
-                                               // each read and written by its owning lane only
 };
+// Dynamic shared memory: ssx float-float accumulators (hi.x, hi.y, lo.x,
+// lo.y) per (output, lane quarter), each read and written by its own lane
+// only; sized for the launch's largest occupied-band count.
+__host__ __device__ constexpr size_t factor_acc_bytes(int nvband) {
+  return sizeof(float4) * (size_t)(nvband < kFusedBands ? nvband : kFusedBands) * kNW * kFacCols * 4;
+}
 // ssx sums: output o = r * 64 + 8 * warp + lane / 4 is computed by the four
 // lanes 4 (lane / 4) + q (q = 0..3, 8 g-vectors each) in round r, so every
-// warp takes part; the lane with q = 0 owns the output's accumulator
+// warp takes part; each lane owns the accumulator acc[4 o + q]
 constexpr int kSsxRounds = (kFusedBands * kNW * kFacCols * 4 + 255) / 256;
 
 __device__ __forceinline__ int find_job(const FactorJob* jobs, int n, int item) {
@@ -126,6 +132,7 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
                                                                  const FactorJob* __restrict__ jobs, int n_jobs,
                                                                  int total) {
   __shared__ FactorSmem sm;
+  extern __shared__ float4 acc_dyn[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const FF quarter{0.25f, 0.f};
   for (int item = blockIdx.x; item < total; item += gridDim.x) {
@@ -163,7 +170,7 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
     // float-float accumulators of the ssx sums this thread owns
     for (int r = 0; r < kSsxRounds; ++r) {
       const int o = r * (kFacThreads / 4) + warp * 8 + (lane >> 2);
-      if ((lane & 3) == 0 && o < outputs) sm.acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (o < outputs) acc_dyn[4 * o + (lane & 3)] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 
     for (int t = t_begin; t < t_end; ++t) {
@@ -213,44 +220,43 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
               near = near || n2;
             }
             if (near) keep = keep_fp64(p.wx[iw], wt.x, wt.y);  // within 2^-30 of a threshold
-            if (keep) {
-              const FF r = ff_rcp(wv);
-              if (wx32)
-                yt[iw] = make_float2(ff_factor_round(wx[iw].hi, gx, sex, r),
-                                     ff_factor_round(wx[iw].hi, gy, sey, r));
-              else
-                yt[iw] = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
-                                     ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
+            // the factor of every term (the warp's lanes almost always
+            // disagree on keep), zero where the guard drops it
+            const FF r = ff_rcp(wv);
+            float yx, yy;
+            if (wx32) {
+              yx = ff_factor_round(wx[iw].hi, gx, sex, r);
+              yy = ff_factor_round(wx[iw].hi, gy, sey, r);
+            } else {
+              yx = ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r);
+              yy = ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r);
             }
+            yt[iw] = keep ? make_float2(yx, yy) : make_float2(0.f, 0.f);
             mask |= keep ? (1u << iw) : 0u;
-            if (nvb > 0 && !keep) {
-              // second branch: 0 < |wdiff|^2 < |wtilde|^2 / to1
-              bool second;
-              if (big_s && wv.hi >= 1e-30f) {
-                second = true;
-              } else {
-                bool n3;
-                const FF s_big = ff_mul(s2, FF{1e6f, 0.f});  // |wtilde|^2 / to1 (1e6 exact)
-                second = wv.hi > 0.f && ff_gt_fast(s_big, wv, n3);
-                if (n3 || wv.hi < 1e-30f) second = second_fp64(p.wx[iw], wt.x, wt.y);
-              }
-              mask |= second ? (8u << iw) : 0u;
+            // second occupied-band branch: 0 < |wdiff|^2 < |wtilde|^2 / to1,
+            // which for |wtilde|^2 > 1e-6 and a dropped term is |wdiff|^2 > 0
+            const bool plain = big_s && wv.hi >= 1e-30f;
+            bool second = !keep && plain;
+            if (nvb > 0 && !keep && !plain) {  // rare
+              bool n3;
+              const FF s_big = ff_mul(s2, FF{1e6f, 0.f});  // |wtilde|^2 / to1 (1e6 exact)
+              second = wv.hi > 0.f && ff_gt_fast(s_big, wv, n3);
+              if (n3 || wv.hi < 1e-30f) second = second_fp64(p.wx[iw], wt.x, wt.y);
             }
+            mask |= (nvb > 0 && second) ? (8u << iw) : 0u;
           }
-          if (nvb > 0 && mask != 0u) {
+          if (nvb > 0) {
             const float2 g32 = make_float2(ff_round(gx), ff_round(gy));
             const float bb = ff_round(b);
             // Omega2 = wtilde G
             const float2 om = make_float2(ff_dot2_round(a, gx, b, gy), ff_dot2_round(a, gy, ff_neg(b), gx));
 #pragma unroll
             for (int iw = 0; iw < kNW; ++iw) {
-              if (mask & (1u << iw)) {
-                sv[iw] = make_float2(om.x * iwx2[iw], om.y * iwx2[iw]);
-              } else if (mask & (8u << iw)) {
-                const float zr = (wxh[iw] + a.hi) + (wxl[iw] + a.lo);
-                const float q = -0.5f * rcp_f32(fmaf(zr, zr, bb * bb));
-                sv[iw] = make_float2(fmaf(g32.x, zr, g32.y * bb) * q, fmaf(g32.y, zr, -g32.x * bb) * q);
-              }
+              const float zr = (wxh[iw] + a.hi) + (wxl[iw] + a.lo);
+              const float q = -0.5f * rcp_f32(fmaf(zr, zr, bb * bb));
+              const float2 s1 = make_float2(om.x * iwx2[iw], om.y * iwx2[iw]);
+              const float2 s2v = make_float2(fmaf(g32.x, zr, g32.y * bb) * q, fmaf(g32.y, zr, -g32.x * bb) * q);
+              sv[iw] = (mask & (1u << iw)) ? s1 : ((mask & (8u << iw)) ? s2v : make_float2(0.f, 0.f));
             }
           }
         }
@@ -277,38 +283,27 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
         put_a(J.a_tiles, J.kt, iw * p.ng + col, ig0 + ch * 8, re, im);
       }
       // the tile's ssx products: output o = (band n1, frequency iw, column
-      // pl); lane quarter q sums g-vectors 8q .. 8q+7 in FP32, two butterfly
-      // steps add the quarters, lane q = 0 folds the tile sum into
-      // float-float
+      // pl); lane quarter q takes g-vectors 8q .. 8q+7 and folds two 4-term
+      // FP32 tree sums into its float-float accumulator
 #pragma unroll 1
       for (int r = 0; r < kSsxRounds; ++r) {
         const int o = r * (kFacThreads / 4) + warp * 8 + (lane >> 2), q = lane & 3;
-        if (r * (kFacThreads / 4) < outputs) {  // warp-uniform
-          float2 run = make_float2(0.f, 0.f);
-          if (o < outputs) {
-            const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
-            float2 t[8];
+        if (o < outputs) {
+          const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
+          float4 a = acc_dyn[4 * o + q];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-              const float2 an = sm.an[n1][8 * q + k], x = sm.x[pl][iw][8 * q + k];
+          for (int half = 0; half < 2; ++half) {
+            float2 t[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int kk = 8 * q + 4 * half + k;
+              const float2 an = sm.an[n1][kk], x = sm.x[pl][iw][kk];
               t[k] = make_float2(fmaf(an.x, x.x, -an.y * x.y), fmaf(an.x, x.y, an.y * x.x));
             }
-#pragma unroll
-            for (int h = 4; h >= 1; h >>= 1)
-#pragma unroll
-              for (int k = 0; k < h; ++k) t[k] = make_float2(t[k].x + t[k + h].x, t[k].y + t[k + h].y);
-            run = t[0];
+            ff_add(a.x, a.z, (t[0].x + t[1].x) + (t[2].x + t[3].x));
+            ff_add(a.y, a.w, (t[0].y + t[1].y) + (t[2].y + t[3].y));
           }
-          run.x += __shfl_xor_sync(0xffffffffu, run.x, 1);
-          run.y += __shfl_xor_sync(0xffffffffu, run.y, 1);
-          run.x += __shfl_xor_sync(0xffffffffu, run.x, 2);
-          run.y += __shfl_xor_sync(0xffffffffu, run.y, 2);
-          if (q == 0 && o < outputs) {
-            float4 a = sm.acc[o];
-            ff_add(a.x, a.z, run.x);
-            ff_add(a.y, a.w, run.y);
-            sm.acc[o] = a;
-          }
+          acc_dyn[4 * o + q] = a;
         }
       }
       __syncthreads();  // sm.an, sm.x and sm.y are refilled by the next tile
@@ -316,6 +311,8 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
 
     if (nvb > 0) {
       // each column's sums x conj(aqsm[n1][igp]) occ vcoul[igp] in FP64
+      // (sm.red aliases sm.x, whose last reads precede the tile loop's
+      // final barrier)
       for (int r = 0; r < kSsxRounds; ++r) {
         const int o = r * (kFacThreads / 4) + warp * 8 + (lane >> 2);
         if ((lane & 3) == 0 && o < outputs) {
@@ -326,9 +323,13 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
           if (igp >= 0) {
             const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
             const double f = p.occ * p.vcoul[igp];
-            const float4 a = sm.acc[o];
-            const double sx = (double)a.x + (double)a.z;
-            const double sy = (double)a.y + (double)a.w;
+            double sx = 0.0, sy = 0.0;  // the four quarters' float-float sums, in FP64
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const float4 a = acc_dyn[4 * o + q];
+              sx += (double)a.x + (double)a.z;
+              sy += (double)a.y + (double)a.w;
+            }
             // (sx + i sy) conj(am) f
             v = make_double2(fma(sx, am.x, sy * am.y) * f, fma(sy, am.x, -sx * am.y) * f);
           }
@@ -384,22 +385,38 @@ int factor_job_items(const FactorJob& j) {
   return j.ncb * j.n_seg + (pad > 0 ? (j.kt + kZeroTiles - 1) / kZeroTiles : 0);
 }
 
-int factor_blocks_per_sm() {
+// Dynamic shared memory above the default 48 KB per block needs the opt-in.
+template <bool kGroup>
+cudaError_t factor_smem_attr() {
+  return cudaFuncSetAttribute(factor_kernel<kGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)factor_acc_bytes(kFusedBands));
+}
+
+int factor_blocks_per_sm(int max_nvband) {
+  factor_smem_attr<true>();
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, factor_kernel<true>, kFacThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, factor_kernel<true>, kFacThreads,
+                                                factor_acc_bytes(max_nvband));
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_factor_pass(const FactorJob* jobs, int n_jobs, int total, int grid, cudaStream_t s) {
+cudaError_t launch_factor_pass(const FactorJob* jobs, int n_jobs, int total, int grid, int max_nvband,
+                               cudaStream_t s) {
   if (total <= 0) return cudaSuccess;
-  factor_kernel<true><<<std::min(grid, total), kFacThreads, 0, s>>>(FactorJob{}, jobs, n_jobs, total);
+  cudaError_t e = factor_smem_attr<true>();
+  if (e != cudaSuccess) return e;
+  factor_kernel<true><<<std::min(grid, total), kFacThreads, factor_acc_bytes(max_nvband), s>>>(
+      FactorJob{}, jobs, n_jobs, total);
   return cudaGetLastError();
 }
 
 cudaError_t launch_factor_pass(const FactorJob& job, int grid, cudaStream_t s) {
   const int total = factor_job_items(job);
   if (total <= 0) return cudaSuccess;
-  factor_kernel<false><<<std::min(grid, total), kFacThreads, 0, s>>>(job, nullptr, 1, total);
+  cudaError_t e = factor_smem_attr<false>();
+  if (e != cudaSuccess) return e;
+  factor_kernel<false><<<std::min(grid, total), kFacThreads, factor_acc_bytes(job.p.nvband), s>>>(
+      job, nullptr, 1, total);
   return cudaGetLastError();
 }
 

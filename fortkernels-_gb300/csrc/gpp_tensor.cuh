@@ -35,13 +35,16 @@ size_t factor_ssx_partial_bytes(const FactorJob& j);
 // Items of the job: the (segment, column block) items and those that zero
 // the padding rows of the last row block.
 int factor_job_items(const FactorJob& j);
-int factor_blocks_per_sm();
+// resident blocks per SM for a launch whose instances have at most
+// max_nvband occupied bands (its shared memory grows with them)
+int factor_blocks_per_sm(int max_nvband);
 // Whether the fused pass covers the occupied bands of this instance.
 inline bool factor_fuses_ssx(int nvband) { return nvband <= kFusedBands; }
 
 // The factor pass over jobs[0 .. n_jobs) (device array; job i's items are
 // [item_off, item_off + factor_job_items)), `total` items in all.
-cudaError_t launch_factor_pass(const FactorJob* jobs, int n_jobs, int total, int grid, cudaStream_t s);
+cudaError_t launch_factor_pass(const FactorJob* jobs, int n_jobs, int total, int grid, int max_nvband,
+                               cudaStream_t s);
 // One instance, the job passed by value (item_off 0).
 cudaError_t launch_factor_pass(const FactorJob& job, int grid, cudaStream_t s);
 

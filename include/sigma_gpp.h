@@ -258,7 +258,11 @@ int sigma_gpp_batched(int n_instances, const sigma_gpp_instance* inst, int preci
  *     larger problems return SIGMA_ERR_WORKSPACE with a message in
  *     sigma_last_error_message().
  *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *     (cudaGetSymbolAddress).
+ *   - A call on a stream that is being captured into a CUDA graph returns
+ *     SIGMA_ERR_UNSUPPORTED and queues nothing: the column map is copied
+ *     from a reused host buffer and the scratch is shared, so a captured
+ *     call could not be replayed.
  *   - Every call shares the one array.  Calls that overlap on the GPU (on
  *     different streams, or from threads that do not wait for each other's
  *     stream) race on it and give wrong results; serialise them.

@@ -12,7 +12,8 @@
   oracle/_ref/libgppseqref.so <- the same file (main renamed by -D) + oracle/ref_seq_harness.cpp
 
 The oracle/_ref products are built only where the reference checkout is
-present (REFERENCE_ROOT, default /root/reference); they are compiled from the
+present (REFERENCE_ROOT, default: a checkout named `reference` beside this
+repository); they are compiled from the
 reference's own source file in place and nothing of it is copied.
 """
 from __future__ import annotations
@@ -28,7 +29,7 @@ ORACLE_LIB = BUILD / "liboracle.so"
 PORT_LIB = BUILD / "libport.so"
 REF_BIN = REF_OUT / "gppKer"
 REF_LIB = REF_OUT / "libgppref.so"
-REFERENCE_ROOT = pathlib.Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
+REFERENCE_ROOT = pathlib.Path(os.environ.get("REFERENCE_ROOT", HERE.parents[1] / "reference"))
 REF_SRC = REFERENCE_ROOT / "BGW-Kernels" / "gppKer.cpp"
 FF_REF_DIR = REFERENCE_ROOT / "FFKer_cori"
 FF_REF_SRC = FF_REF_DIR / "ffKernel.cpp"

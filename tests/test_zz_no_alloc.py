@@ -24,6 +24,7 @@ import torch
 
 import workload as W
 from conftest import rel_err
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -157,3 +158,36 @@ def test_noalloc_rejects_problems_beyond_its_scratch(sigma_lib):
                                     p, p, p, p, p, p, p, p, None)
     assert st == -9
     assert b"32 MiB" in lib.sigma_last_error_message()
+
+
+def test_noalloc_refuses_a_capturing_stream(sigma_lib):
+    """A call on a stream under graph capture returns SIGMA_ERR_UNSUPPORTED
+    and queues nothing; the next plain call on the same stream succeeds."""
+    S = sigma_lib
+    lib = S.load()
+    prob = W.gpp_random(40, 2, 1024, 40, 35)
+    d = [_dev(x) for x in (prob.aqsmtemp, prob.aqsntemp, prob.I_eps_array, prob.wtilde_array,
+                           prob.vcoul)]
+    wx = _dev(prob.wx_array)
+    inv = np.ascontiguousarray(prob.inv_igp_index, np.int32)
+    indinv = np.ascontiguousarray(prob.indinv, np.int32)
+    out = _outputs(40)
+    args = (40, 2, 1024, 40, inv.ctypes.data, indinv.ctypes.data, wx.data_ptr(), 1.0,
+            *[t.data_ptr() for t in d], *[t.data_ptr() for t in out])
+    side = torch.zeros(4, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        g.capture_begin()
+        side.add_(1.0)
+        st = lib.sigma_gpp_fp64_noalloc(*args, C.c_void_p(s.cuda_stream))
+        g.capture_end()
+    assert st == -8  # SIGMA_ERR_UNSUPPORTED
+    assert b"captured" in lib.sigma_last_error_message()
+    assert torch.count_nonzero(out[0]) == 0
+    st = lib.sigma_gpp_fp64_noalloc(*args, C.c_void_p(s.cuda_stream))
+    assert st == 0
+    s.synchronize()
+    ach, _, _ = O.gpp(prob)
+    assert rel_err(_host(out)[0], ach).max() <= FP64_TOL
