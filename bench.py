@@ -638,14 +638,19 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
            "instances": len(xs), "input_bytes": int(sum(x.input_bytes for x in xs)),
            "tiles": {"table": autotune.load_table() is not None,
                      "counts": {autotune.TILES[t] if t >= 0 else "library": tiles.count(t)
-                                for t in sorted(set(tiles))}}}
+                                for t in sorted(set(tiles))},
+                     "items_per_cta": {f: autotune.sizing_for(f) for f in ("fp64", "mixed", "tensor")}}}
     outs = {}
     gs = torch.cuda.Stream()  # graphs are captured on a non-default stream
     gptr = gs.cuda_stream
     torch.cuda.synchronize()
-    for prec, name, steps in ((S.PREC_FP64, "fp64", args.batch_fp64_steps), (S.PREC_MIXED, "mixed", 5),
-                              (S.PREC_TENSOR, "tensor", 5)):
-        b = S.GppBatch(dicts, precision=prec, tiles=tiles if prec == S.PREC_FP64 else None)
+    forms = [(S.PREC_FP64, "fp64", args.batch_fp64_steps), (S.PREC_MIXED, "mixed", 5),
+             (S.PREC_TENSOR, "tensor", 5)]
+    forms = [f for f in forms if f[1] in args.batch_forms.split(",")]
+    for prec, name, steps in forms:
+        b = S.GppBatch(dicts, precision=prec, tiles=tiles if prec == S.PREC_FP64 else None,
+                       items_per_cta=autotune.sizing_for(name) if name != "tensor" else 0,
+                       tensor_items_per_cta=autotune.sizing_for("tensor") if name == "tensor" else 0)
         terms, items, launches = b.info()
         b.launch_graph(gptr)  # capture, and the warm-up replay
         ms = timed(torch, dist, world, lambda: b.launch_graph(gptr), steps, gs)
@@ -677,6 +682,8 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
                                               "outputs": 6 * len(outs[name]),
                                               "acht_n1_loc_normwise_max": n1_worst}
     for name in ("mixed", "tensor"):
+        if name not in outs or "fp64" not in outs:
+            continue
         worst, over, by = 0.0, 0, {"achtemp": 0.0, "asxtemp": 0.0}
         for a, m in zip(outs["fp64"], outs[name]):
             for k, key in ((0, "achtemp"), (1, "asxtemp")):
@@ -1017,6 +1024,8 @@ def main():
     ap.add_argument("--batch-fp64-steps", type=int, default=2)
     ap.add_argument("--no-batch-singles", action="store_true",
                     help="skip timing the batched instances as single plans back to back")
+    ap.add_argument("--batch-forms", default="fp64,mixed,tensor",
+                    help="comma list of the batched forms to time (fewer only for profiling)")
     ap.add_argument("--only-batched", action="store_true",
                     help="run the batched measurement alone (profiling captures)")
     ap.add_argument("--per-band-wx", action="store_true",

@@ -55,7 +55,7 @@ namespace sigma {
 // left out).  Shared by the FF contraction and the static remainders.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
                   const std::vector<int>& igp_of, int mode, void* shared_tiles,
-                  const int* row_kend, int split_tiles_hint) {
+                  const int* row_kend, int split_tiles_hint, int items_per_cta) {
   *out = nullptr;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -86,7 +86,7 @@ int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, 
   p->grid = sms * per_sm;
   OzakiTables tables;
   if (mode == SIGMA_FF_OZAKI_BF16) {
-    ozaki_size(p->oz, d, p->grid, row_kend, &tables, split_tiles_hint);
+    ozaki_size(p->oz, d, p->grid, row_kend, &tables, split_tiles_hint, items_per_cta);
     if (p->oz.max_seg > ozaki_max_segments()) {  // ngpown below ~18: too many frequencies per tile
       delete p;
       return SIGMA_ERR_UNSUPPORTED;
@@ -250,10 +250,11 @@ int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
                         const sigma_complex128* aqsntemp, const sigma_complex128* aqsmtemp,
                         const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
                         void* stream, const float2* epsr32, bool reuse_a, const double* vcoul2,
-                        double vfac2, sigma_complex128* out2) {
+                        double vfac2, sigma_complex128* out2, bool operands_ready) {
   if (!plan) return SIGMA_ERR_NULL;
   if ((!I_epsR && !epsr32 && !reuse_a) || !aqsntemp || !aqsmtemp || !schDt_matrix) return SIGMA_ERR_NULL;
-  if ((epsr32 || reuse_a) && plan->mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
+  if ((epsr32 || reuse_a || operands_ready) && plan->mode != SIGMA_FF_OZAKI_BF16) return SIGMA_ERR_UNSUPPORTED;
+  if (operands_ready && !reuse_a) return SIGMA_ERR_UNSUPPORTED;
   if ((out2 != nullptr) != (vcoul2 != nullptr) || (out2 && vcoul)) return SIGMA_ERR_UNSUPPORTED;
   if (out2 && plan->mode == SIGMA_FF_FP64) {
     // the FP64 form contracts twice
@@ -285,7 +286,9 @@ int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));
     SIGMA_CUDA_TRY(launch_ff_reduce(d, plan->work, reinterpret_cast<double2*>(schDt_matrix), s));
   } else {
-    SIGMA_CUDA_TRY(launch_ozaki_prep(d, oz, s, !reuse_a));
+    // operands_ready: the A and B slices and the epilogue factors were
+    // written by the caller's producer pass
+    if (!operands_ready) SIGMA_CUDA_TRY(launch_ozaki_prep(d, oz, s, !reuse_a));
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
     SIGMA_CUDA_TRY(launch_ozaki_gemm(d, plan->work, oz, plan->grid, s));
     if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[1], s));

@@ -90,92 +90,18 @@ __global__ void __launch_bounds__(256) ozaki_prep_a_kernel(FfDev p, OzakiPrep oz
   }
 }
 
-// B' rows: [Re | -Im] (real part of the product) and [Im | Re] (imaginary part);
-// element t of n_col_blocks * kt * 64 * kChunksPerRow.
-__device__ __forceinline__ void prep_b_elem(const FfDev& p, const OzakiPrep& oz, long long t) {
-  {
-    const int ch = (int)(t % kChunksPerRow);
-    const int nl = (int)((t / kChunksPerRow) & 63);
-    const long long rest = t / (kChunksPerRow * 64);
-    const int kt = (int)(rest % oz.kt);
-    const int cb = (int)(rest / oz.kt);
-    const int n = cb * kOzCols + nl;
-    const int k0 = kt * kOzKTile + ch * 8;
-    float re[8], im[8], nim[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int k = k0 + j;
-      const double2 v = (n < p.nb && k < p.nc) ? p.aqsn[(size_t)n * p.nc + k] : make_double2(0.0, 0.0);
-      re[j] = __double2float_rn(v.x);
-      im[j] = __double2float_rn(v.y);
-      nim[j] = -im[j];
-    }
-    unsigned char* base = oz.b_tiles + (size_t)cb * 2 * oz.kt * kOperandBytes;
-    unsigned char* lo = base + (size_t)kt * kOperandBytes;            // K' < K: real parts of aqsn
-    unsigned char* hi = base + (size_t)(oz.kt + kt) * kOperandBytes;  // K' >= K: imaginary parts
-    oz_put_row_chunk(lo, nl, ch, re);
-    oz_put_row_chunk(lo, 64 + nl, ch, im);
-    oz_put_row_chunk(hi, nl, ch, nim);
-    oz_put_row_chunk(hi, 64 + nl, ch, re);
-  }
-}
-__device__ __forceinline__ long long prep_b_count(const OzakiPrep& oz) {
-  return (long long)oz.n_col_blocks * oz.kt * 64 * kChunksPerRow;
-}
 __global__ void __launch_bounds__(256) ozaki_prep_b_kernel(FfDev p, OzakiPrep oz) {
-  const long long total = prep_b_count(oz);
+  const long long total = oz_prep_b_count(oz);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x)
-    prep_b_elem(p, oz, t);
+    oz_prep_b_elem(p, oz, t);
 }
 
-// wtab[g][n] = aqsm[n][igp(g)] * weight(g), rounded to FP32 from the FP64
-// product (the value the epilogue used to form per lane from global loads).
-__device__ __forceinline__ void weights_elem(const FfDev& p, const OzakiPrep& oz, long long t) {
-  {
-    const int g = (int)(t / oz.nb_pad), n = (int)(t % oz.nb_pad);
-    const int igp = p.igp_of[g];
-    float2 v = make_float2(0.f, 0.f);
-    if (igp >= 0 && n < p.nb) {
-      const double wgt = ff_column_weight(p, igp);
-      const double2 md = p.aqsm[(size_t)n * p.nc + igp];
-      v = make_float2(__double2float_rn(md.x * wgt), __double2float_rn(md.y * wgt));
-    }
-    oz.wtab[t] = v;
-    if (oz.stab && n == 0) oz.stab[g] = igp >= 0 ? (float)(p.vfac2 * p.vcoul2[igp]) : 0.f;
-  }
-}
 __global__ void __launch_bounds__(256) ozaki_weights_kernel(FfDev p, OzakiPrep oz) {
-  const long long total = (long long)oz.ng * oz.nb_pad;
+  const long long total = oz_weights_count(oz);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x)
-    weights_elem(p, oz, t);
-}
-
-// Group forms: each job owns a contiguous range of blocks (found once per
-// block), its threads stride over the job's elements.
-__device__ __forceinline__ int group_job_of_block(const OzGroup& g, int b, bool weights) {
-  int lo = 0, hi = g.n_jobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    const int off = weights ? g.jobs[mid].w_blk_off : g.jobs[mid].b_blk_off;
-    if (off <= b) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-__global__ void __launch_bounds__(256) ozaki_group_prep_b_kernel(OzGroup g) {
-  const OzGroupJob& J = g.jobs[group_job_of_block(g, blockIdx.x, false)];
-  const long long total = prep_b_count(J.oz);
-  for (long long t = (long long)(blockIdx.x - J.b_blk_off) * blockDim.x + threadIdx.x; t < total;
-       t += (long long)J.b_blks * blockDim.x)
-    prep_b_elem(J.d, J.oz, t);
-}
-__global__ void __launch_bounds__(256) ozaki_group_weights_kernel(OzGroup g) {
-  const OzGroupJob& J = g.jobs[group_job_of_block(g, blockIdx.x, true)];
-  const long long total = (long long)J.oz.ng * J.oz.nb_pad;
-  for (long long t = (long long)(blockIdx.x - J.w_blk_off) * blockDim.x + threadIdx.x; t < total;
-       t += (long long)J.w_blks * blockDim.x)
-    weights_elem(J.d, J.oz, t);
+    oz_weights_elem(p, oz, t);
 }
 
 struct OzItem {
@@ -604,7 +530,7 @@ __global__ void ozaki_group_reduce_kernel(OzGroup g) {
 }  // namespace
 
 void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend, OzakiTables* tables,
-                int split_tiles_hint) {
+                int split_tiles_hint, int items_per_cta) {
   oz.kt = (d.nc + kOzKTile - 1) / kOzKTile;
   const int rows = d.nf * d.ng;
   oz.n_row_blocks = (rows + kOzRows - 1) / kOzRows;
@@ -623,7 +549,7 @@ void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend, Oz
     active += 2LL * kl[rb];
   }
   // about 20 items per CTA: as many K splits as the active tiles need
-  const long long want = 20LL * grid * two_kt;
+  const long long want = (long long)(items_per_cta > 0 ? items_per_cta : 20) * grid * two_kt;
   const long long have = std::max(1LL, active * oz.n_col_blocks);
   long long s = (want + have - 1) / have;
   if (split_tiles_hint > 0) s = (two_kt + split_tiles_hint - 1) / split_tiles_hint;
@@ -784,16 +710,6 @@ void ozaki_group_items(int job, const OzakiPrep& oz, const OzakiTables& t, std::
     const int cb = it % oz.n_col_blocks;
     items.push_back(make_int4(job, (e.x << 16) | cb, e.z, e.w | (e.y << 16)));
   }
-}
-
-cudaError_t launch_ozaki_group_prep(const OzGroup& g, cudaStream_t s) {
-  if (g.b_blocks > 0) {
-    ozaki_group_prep_b_kernel<<<g.b_blocks, 256, 0, s>>>(g);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-  }
-  if (g.w_blocks > 0) ozaki_group_weights_kernel<<<g.w_blocks, 256, 0, s>>>(g);
-  return cudaGetLastError();
 }
 
 cudaError_t launch_ozaki_group_gemm(const OzGroup& g, int grid, cudaStream_t s) {

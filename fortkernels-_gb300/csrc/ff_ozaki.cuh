@@ -107,9 +107,10 @@ struct OzakiTables {
   std::vector<int> pieces, kt_lim;
 };
 // split_tiles_hint > 0 sets the K' tiles per split (a group sizes every
-// job's items alike); otherwise about 20 items per CTA of `grid`.
+// job's items alike); otherwise about items_per_cta (0: 20) items per CTA
+// of `grid`.
 void ozaki_size(OzakiPrep& oz, const FfDev& d, int grid, const int* row_kend = nullptr,
-                OzakiTables* tables = nullptr, int split_tiles_hint = 0);
+                OzakiTables* tables = nullptr, int split_tiles_hint = 0, int items_per_cta = 0);
 cudaError_t ozaki_upload_tables(const OzakiPrep& oz, const OzakiTables& t);
 int ozaki_max_segments();
 size_t ozaki_prep_bytes(const OzakiPrep& oz);  // slice images + partials
@@ -132,13 +133,12 @@ cudaError_t launch_ozaki_reduce(const FfDev& d, const OzakiPrep& oz, double2* sc
 // A group of contractions run as one launch per stage (the batched tensor
 // form): each job is one contraction with its own operands, layout and
 // partial buffers; the GEMM's items of every job are listed in one table,
-// the other stages split their blocks among the jobs.
+// the reduction splits its warps among the jobs.  The jobs' operands (A and
+// B slices, epilogue factors) are written by the caller's producer pass.
 struct OzGroupJob {
   FfDev d;
   OzakiPrep oz;
   double2* out;            // [nb][nf] (reduction output)
-  int b_blk_off, b_blks;   // blocks of the B-slice stage
-  int w_blk_off, w_blks;   // blocks of the epilogue-factor stage
   int r_warp_off;          // first warp of the reduction stage (nb * nf warps)
 };
 struct OzGroup {
@@ -146,13 +146,12 @@ struct OzGroup {
   int n_jobs;
   const int4* items;       // [total]: job, row block << 16 | band block, first K' tile, tiles | piece << 16
   int total;
-  int b_blocks, w_blocks, r_warps;
+  int r_warps;
   int* status;
 };
 // Host side of a group: the item table of job `job` appended to `items`
 // (its entries in the order of ozaki_size, band blocks fastest).
 void ozaki_group_items(int job, const OzakiPrep& oz, const OzakiTables& t, std::vector<int4>& items);
-cudaError_t launch_ozaki_group_prep(const OzGroup& g, cudaStream_t s);
 cudaError_t launch_ozaki_group_gemm(const OzGroup& g, int grid, cudaStream_t s);
 cudaError_t launch_ozaki_group_reduce(const OzGroup& g, cudaStream_t s);
 
@@ -162,6 +161,57 @@ __device__ __forceinline__ void oz_put_a(const OzakiPrep& oz, int R, int k0, con
   unsigned char* base = oz.a_tiles + (size_t)rb * 2 * oz.kt * kOzOperandBytes;
   oz_put_row_chunk(base + (size_t)kt * kOzOperandBytes, r, ch, re);
   oz_put_row_chunk(base + (size_t)(oz.kt + kt) * kOzOperandBytes, r, ch, im);
+}
+
+// B' rows: [Re | -Im] (real part of the product) and [Im | Re] (imaginary
+// part); element t of oz_prep_b_count: one (band block, K tile, band, 8-value
+// chunk) of aqsn rounded to FP32 and written as slices.
+__device__ __forceinline__ long long oz_prep_b_count(const OzakiPrep& oz) {
+  return (long long)oz.n_col_blocks * oz.kt * 64 * (kOzKTile / 8);
+}
+__device__ __forceinline__ void oz_prep_b_elem(const FfDev& p, const OzakiPrep& oz, long long t) {
+  constexpr int kChunks = kOzKTile / 8;
+  const int ch = (int)(t % kChunks);
+  const int nl = (int)((t / kChunks) & 63);
+  const long long rest = t / (kChunks * 64);
+  const int kt = (int)(rest % oz.kt);
+  const int cb = (int)(rest / oz.kt);
+  const int n = cb * kOzCols + nl;
+  const int k0 = kt * kOzKTile + ch * 8;
+  float re[8], im[8], nim[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int k = k0 + j;
+    const double2 v = (n < p.nb && k < p.nc) ? p.aqsn[(size_t)n * p.nc + k] : make_double2(0.0, 0.0);
+    re[j] = __double2float_rn(v.x);
+    im[j] = __double2float_rn(v.y);
+    nim[j] = -im[j];
+  }
+  unsigned char* base = oz.b_tiles + (size_t)cb * 2 * oz.kt * kOzOperandBytes;
+  unsigned char* lo = base + (size_t)kt * kOzOperandBytes;            // K' < K: real parts of aqsn
+  unsigned char* hi = base + (size_t)(oz.kt + kt) * kOzOperandBytes;  // K' >= K: imaginary parts
+  oz_put_row_chunk(lo, nl, ch, re);
+  oz_put_row_chunk(lo, 64 + nl, ch, im);
+  oz_put_row_chunk(hi, nl, ch, nim);
+  oz_put_row_chunk(hi, 64 + nl, ch, re);
+}
+
+// Epilogue factors, element t of oz_weights_count: wtab[g][n] = aqsm[n][igp(g)]
+// * weight(g), rounded to FP32 from the FP64 product.
+__device__ __forceinline__ long long oz_weights_count(const OzakiPrep& oz) {
+  return (long long)oz.ng * oz.nb_pad;
+}
+__device__ __forceinline__ void oz_weights_elem(const FfDev& p, const OzakiPrep& oz, long long t) {
+  const int g = (int)(t / oz.nb_pad), n = (int)(t % oz.nb_pad);
+  const int igp = p.igp_of[g];
+  float2 v = make_float2(0.f, 0.f);
+  if (igp >= 0 && n < p.nb) {
+    const double wgt = ff_column_weight(p, igp);
+    const double2 md = p.aqsm[(size_t)n * p.nc + igp];
+    v = make_float2(__double2float_rn(md.x * wgt), __double2float_rn(md.y * wgt));
+  }
+  oz.wtab[t] = v;
+  if (oz.stab && n == 0) oz.stab[g] = igp >= 0 ? (float)(p.vfac2 * p.vcoul2[igp]) : 0.f;
 }
 
 }  // namespace sigma

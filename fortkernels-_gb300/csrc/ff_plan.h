@@ -18,10 +18,11 @@ namespace sigma {
 // + my_igp) the K from which the row is zero in every execution; the
 // contraction skips those K tiles.
 // split_tiles_hint (split-BF16 form, > 0): K' tiles per work split, so
-// that the plans of a group have items of about the same size.
+// that the plans of a group have items of about the same size; otherwise
+// items_per_cta (> 0; default 20) GEMM items per resident CTA.
 int ff_plan_build(sigma_ff_plan* out, int number_bands, int ncouls, int ngpown, int nfreq,
                   const std::vector<int>& igp_of, int mode, void* shared_tiles = nullptr,
-                  const int* row_kend = nullptr, int split_tiles_hint = 0);
+                  const int* row_kend = nullptr, int split_tiles_hint = 0, int items_per_cta = 0);
 int ff_plan_tile_bytes(int number_bands, int ncouls, int ngpown, int nfreq, size_t* bytes);
 
 // The split-BF16 plan's operand layout (slice images, K tiles, row limits),
@@ -50,6 +51,6 @@ int ff_execute_weighted(sigma_ff_plan plan, const sigma_complex128* I_epsR,
                         const double* vcoul, double vfac, sigma_complex128* schDt_matrix,
                         void* stream, const float2* epsr32 = nullptr, bool reuse_a = false,
                         const double* vcoul2 = nullptr, double vfac2 = 1.0,
-                        sigma_complex128* out2 = nullptr);
+                        sigma_complex128* out2 = nullptr, bool operands_ready = false);
 
 }  // namespace sigma

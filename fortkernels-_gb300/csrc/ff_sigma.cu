@@ -314,11 +314,13 @@ extern "C" int sigma_ff_sigma_execute(sigma_ff_sigma_plan p, const sigma_complex
   g.ca = p->ca;
   g.sdt = sd;
   g.per = p->per;
-  const int threads = 256, items = p->nb * p->ne;
+  // one thread per (band, evaluation frequency), FP64-bound: one warp per
+  // block spreads the few thousand threads over every SM
+  const int threads = 32, items = p->nb * p->ne;
   ff_sigma_band_kernel<<<(items + threads - 1) / threads, threads, 0, s>>>(g);
   SIGMA_CUDA_TRY(cudaGetLastError());
   const int warps = 1 + kOut * p->ne;
-  ff_sigma_sum_kernel<<<(warps * 32 + threads - 1) / threads, threads, 0, s>>>(
+  ff_sigma_sum_kernel<<<(warps * 32 + 255) / 256, 256, 0, s>>>(
       p->nb, p->nf, p->ne, p->cr, p->per, reinterpret_cast<double2*>(out));
   SIGMA_CUDA_TRY(cudaGetLastError());
   return SIGMA_OK;

@@ -219,6 +219,7 @@ extern "C" int sigma_gpp_plan_create(sigma_gpp_plan* plan_out, int number_bands,
       factor_job_size(p->fac, d, oz->kt, p->fac_grid, 1.0);
       p->fac.a_tiles = oz->a_tiles;
       p->fac.item_off = 0;
+      factor_job_operands(p->fac, *ff_plan_dev(p->ff), *oz);
       b_fssx = align_up(factor_ssx_partial_bytes(p->fac), 256);
     }
   }
@@ -329,9 +330,9 @@ extern "C" int sigma_gpp_plan_timing(sigma_gpp_plan plan, int* executions, doubl
       const bool occ = plan->ssx.n_items > 0;
       const sigma::OzakiPrep* oz = sigma::ff_plan_ozaki(plan->ff);
       const int pad = oz && oz->n_row_blocks * sigma::kOzRows > sigma::kNW * plan->ng ? 1 : 0;
-      // fused: the factor pass (padding rows and occupied bands included),
-      // B slices and epilogue factors (2), GEMM, its reduction, 2 reductions
-      *launches_per_execution = plan->fused ? 1 + 2 + 2 + 2 : (occ ? 2 : 1) + pad + 2 + 2 + (occ ? 1 : 0) + 2;
+      // fused: the factor pass (padding rows, occupied bands, B slices and
+      // epilogue factors included), GEMM, its reduction, 2 reductions
+      *launches_per_execution = plan->fused ? 1 + 2 + 2 : (occ ? 2 : 1) + pad + 2 + 2 + (occ ? 1 : 0) + 2;
     } else
       *launches_per_execution = (plan->sch.n_items > 0 ? (mixed ? 3 : 1) : 0) +
                                 (plan->ssx.n_items > 0 ? 1 : 0) + 2;
@@ -401,13 +402,17 @@ extern "C" int sigma_gpp_execute(sigma_gpp_plan plan, const double* wx_array, in
   if (ev) SIGMA_CUDA_TRY(cudaEventRecord(ev[0], s));
   if (tensor && plan->fused) {
     // factors written as the contraction's A slices, occupied bands summed
-    // in the same pass
+    // in the same pass, and the B slices and epilogue factors spread through it
     FactorJob j = plan->fac;
     j.p = p;
+    j.d.aqsn = p.aqsn;
+    j.d.aqsm = p.aqsm;
+    j.d.vcoul = vcoul;
+    j.d.vfac = 0.5;
     SIGMA_CUDA_TRY(launch_factor_pass(j, plan->fac_grid, s));
     const int st = ff_execute_weighted(plan->ff, nullptr, aqsntemp, aqsmtemp, vcoul, 0.5,
                                        reinterpret_cast<sigma_complex128*>(plan->acht_n1), stream, nullptr,
-                                       true);
+                                       true, nullptr, 1.0, nullptr, true);
     if (st != SIGMA_OK) return st;
   } else if (tensor) {
     // factors, and the occupied-band operands from the same pass

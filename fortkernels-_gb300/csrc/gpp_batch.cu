@@ -49,6 +49,7 @@ struct sigma_gpp_batch_s {
   std::vector<sigma_gpp_instance> inst;
   long long terms = 0;
   int sch_grid = 0, ssx_grid = 0, launches = 0;
+  int tensor_items_per_cta = 0;  // GEMM items per CTA of each contraction (0: the plans' default)
   bool all_shared_wx = true;  // every instance has one frequency set for all bands
   bool mixedy = false;        // mixed main pass on the shared-factor kernel
   void* block = nullptr;
@@ -78,14 +79,17 @@ namespace {
 constexpr int kBatchItemsPerSlot = 16;
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 
-// Least padded work among the FP64 tile shapes of one kernel family (bands
-// and columns padded up to the tile), ties to the family's first tile.
+// Least padded work among the FP64 tile shapes of one kernel family (columns
+// padded up to the tile; bands up to the tile, or to 16 in the
+// shared-frequency family, whose last band block runs a shorter item), ties
+// to the family's first tile.
 int least_padding_tile(int nb, int ng, bool shared) {
   const int t0 = shared ? kTileY64x32 : kTile32x32, t1 = shared ? kTileCount : kTileY64x32;
   int best = t0;
   double best_cost = 1e300;
   for (int t = t0; t < t1; ++t) {
-    const double cost = (double)((nb + tile_bn(t) - 1) / tile_bn(t) * tile_bn(t)) *
+    const int bq = shared ? 16 : tile_bn(t);
+    const double cost = (double)((nb + bq - 1) / bq * bq) *
                         (double)((ng + tile_bp(t) - 1) / tile_bp(t) * tile_bp(t));
     if (cost < best_cost - 0.5) {
       best_cost = cost;
@@ -143,7 +147,7 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
   // span an item's accumulator lifetimes), and this sizing keeps them at the
   // single plans' level on the 48-instance set
   (void)tiles;
-  const int hint = 0;
+  const int hint = 0, ipc = b->tensor_items_per_cta;
   b->ff.assign(n, nullptr);
   b->fac_nvband = 0;
   for (int i = 0; i < n; ++i) b->fac_nvband = std::max(b->fac_nvband, inst[i].nvband);
@@ -153,19 +157,19 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
   std::vector<int4> items;
   std::vector<size_t> ssx_off(n);
   size_t ssx_bytes = 0;
-  int bblk = 0, wblk = 0, rwarps = 0;
+  int rwarps = 0;
   b->fac_total = 0;
   for (int i = 0; i < n; ++i) {
     const sigma_gpp_instance& q = inst[i];
     int st = ff_plan_build(&b->ff[i], q.number_bands, q.ncouls, q.ngpown, kNW, igp[i], SIGMA_FF_OZAKI_BF16,
-                           static_cast<char*>(b->tensor_ws) + toff[i], nullptr, hint);
+                           static_cast<char*>(b->tensor_ws) + toff[i], nullptr, hint, ipc);
     if (st != SIGMA_OK) return st;
     const OzakiPrep& oz = *ff_plan_ozaki(b->ff[i]);
     // the plan's work entries, for the group's item table (with a split
     // size given, they depend on the shape and the split size only)
     OzakiTables t;
     OzakiPrep again{};
-    ozaki_size(again, *ff_plan_dev(b->ff[i]), sms, nullptr, &t, hint);
+    ozaki_size(again, *ff_plan_dev(b->ff[i]), sms, nullptr, &t, hint, ipc);
     if (again.n_items != oz.n_items || again.n_entries != oz.n_entries) return SIGMA_ERR_UNSUPPORTED;
     ozaki_group_items(i, oz, t, items);
 
@@ -187,15 +191,9 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
     J.oz = oz;
     J.oz.stab = nullptr;
     J.out = b->acht_n1[i];
-    const long long b_cnt = (long long)oz.n_col_blocks * oz.kt * 64 * 4, w_cnt = (long long)oz.ng * oz.nb_pad;
-    J.b_blks = (int)std::max(1LL, (b_cnt + 2047) / 2048);  // ~8 elements per thread
-    J.b_blk_off = bblk;
-    bblk += J.b_blks;
-    J.w_blks = (int)std::max(1LL, (w_cnt + 2047) / 2048);
-    J.w_blk_off = wblk;
-    wblk += J.w_blks;
     J.r_warp_off = rwarps;
     rwarps += q.number_bands * kNW;
+    factor_job_operands(fj, J.d, J.oz);
   }
   const size_t o_fac = 0;
   const size_t o_jobs = o_fac + up256(sizeof(FactorJob) * n);
@@ -227,8 +225,6 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
   g.n_jobs = n;
   g.items = reinterpret_cast<const int4*>(base + o_items);
   g.total = (int)items.size();
-  g.b_blocks = bblk;
-  g.w_blocks = wblk;
   g.r_warps = rwarps;
   g.status = b->counters + 2;
   return SIGMA_OK;
@@ -270,10 +266,17 @@ int build_reductions(sigma_gpp_batch_s* b) {
 extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
                                       const sigma_gpp_instance* inst, int precision,
                                       const int* tile_shape) {
+  return sigma_gpp_batch_create_tuned(out, n_instances, inst, precision, tile_shape, 0, 0);
+}
+
+extern "C" int sigma_gpp_batch_create_tuned(sigma_gpp_batch* out, int n_instances,
+                                            const sigma_gpp_instance* inst, int precision,
+                                            const int* tile_shape, int items_per_cta,
+                                            int tensor_items_per_cta) {
   using namespace sigma;
   if (!out || !inst) return SIGMA_ERR_NULL;
   *out = nullptr;
-  if (n_instances <= 0) return SIGMA_ERR_INVALID_SHAPE;
+  if (n_instances <= 0 || items_per_cta < 0 || tensor_items_per_cta < 0) return SIGMA_ERR_INVALID_SHAPE;
   if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED && precision != SIGMA_PREC_TENSOR)
     return SIGMA_ERR_UNSUPPORTED;
   const bool tensor = precision == SIGMA_PREC_TENSOR;
@@ -316,6 +319,7 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   auto* b = new sigma_gpp_batch_s();
   b->device = dev;
   b->grouped = grouped;
+  b->tensor_items_per_cta = tensor_items_per_cta;
   b->n = n_instances;
   b->precision = precision;
   b->terms = terms;
@@ -339,8 +343,9 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
   b->sch_off.assign(n_instances + 1, 0);
   b->ssx_off.assign(n_instances + 1, 0);
 
-  // item size: the batch's terms spread over ~kBatchItemsPerSlot items per resident CTA
-  const double target = std::max(1.0, (double)terms / ((double)b->sch_grid * kBatchItemsPerSlot));
+  // item size: the batch's terms spread over ~items_per_cta items per resident CTA
+  const int ipc = items_per_cta > 0 ? items_per_cta : kBatchItemsPerSlot;
+  const double target = std::max(1.0, (double)terms / ((double)b->sch_grid * ipc));
   long long ssx_terms = 0;
   for (int i = 0; i < n_instances; ++i)
     ssx_terms += (long long)inst[i].nvband * inst[i].ngpown * inst[i].ncouls * kNW;
@@ -492,7 +497,7 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
       sigma_gpp_batch_destroy(b);
       return st;
     }
-    b->launches = 7;  // factors, B slices, epilogue factors, GEMM, its reduction, 2 reductions
+    b->launches = 5;  // factors (with B slices and epilogue factors), GEMM, its reduction, 2 reductions
   } else if (tensor) {
     // one slice workspace, sized for the largest instance
     size_t tbytes = 0;
@@ -556,8 +561,8 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
     // every instance in each launch: factors (A slices, occupied bands),
     // B slices and epilogue factors, the GEMM over the group's item table,
     // its reduction
+    // the factor pass writes every operand of the contractions
     SIGMA_CUDA_TRY(launch_factor_pass(b->d_fac, b->n, b->fac_total, b->fac_grid, b->fac_nvband, s));
-    SIGMA_CUDA_TRY(launch_ozaki_group_prep(b->grp, s));
     SIGMA_CUDA_TRY(launch_ozaki_group_gemm(b->grp, device_sm_count(), s));
     SIGMA_CUDA_TRY(launch_ozaki_group_reduce(b->grp, s));
     SIGMA_CUDA_TRY(launch_gpp_reduce_group(b->d_red, b->n, b->red_warps, s));

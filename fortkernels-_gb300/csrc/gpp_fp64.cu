@@ -411,28 +411,40 @@ constexpr size_t kSchYBatchSmem =
     smax(smax(sizeof(SchYSmem<64, 32>), sizeof(SchYSmem<32, 64>)), sizeof(SchYSmem<128, 16>));
 
 // Item of an instance's shared-frequency pass with tile t: the last band
-// block runs the half-height item when its remaining bands fit (less
-// padded work; the slot layout stays the tile's).
+// block runs the shortest item (a multiple of 16 bands) that holds its
+// remaining bands (less padded work; the slot layout stays the tile's).
 __device__ __forceinline__ void sch_fp64y_batch_item(const GppDev& p, const GppWork& w, int tile, int local,
                                                      unsigned char* smem_raw, int tid) {
   const ItemCoord ic = decode_item(w, local);
-  const bool half = w.band_count - ic.bb * w.bn <= w.bn / 2;  // bands of this item's block
+  const int slabs = (min(w.band_count - ic.bb * w.bn, w.bn) + 15) / 16;  // 16-band slabs of this block
   switch (tile) {
     case kTileY32x64:
-      if (half) sch_fp64y_item<16, 64>(p, w, local, smem_raw, tid);
+      if (slabs == 1) sch_fp64y_item<16, 64>(p, w, local, smem_raw, tid);
       else sch_fp64y_item<32, 64>(p, w, local, smem_raw, tid);
       break;
     case kTileY32x32:
-      if (half) sch_fp64y_item<16, 32>(p, w, local, smem_raw, tid);
+      if (slabs == 1) sch_fp64y_item<16, 32>(p, w, local, smem_raw, tid);
       else sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid);
       break;
     case kTileY128x16:
-      if (half) sch_fp64y_item<64, 16>(p, w, local, smem_raw, tid);
-      else sch_fp64y_item<128, 16>(p, w, local, smem_raw, tid);
+      switch (slabs) {
+        case 1: sch_fp64y_item<16, 16>(p, w, local, smem_raw, tid); break;
+        case 2: sch_fp64y_item<32, 16>(p, w, local, smem_raw, tid); break;
+        case 3: sch_fp64y_item<48, 16>(p, w, local, smem_raw, tid); break;
+        case 4: sch_fp64y_item<64, 16>(p, w, local, smem_raw, tid); break;
+        case 5: sch_fp64y_item<80, 16>(p, w, local, smem_raw, tid); break;
+        case 6: sch_fp64y_item<96, 16>(p, w, local, smem_raw, tid); break;
+        case 7: sch_fp64y_item<112, 16>(p, w, local, smem_raw, tid); break;
+        default: sch_fp64y_item<128, 16>(p, w, local, smem_raw, tid); break;
+      }
       break;
     default:
-      if (half) sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid);
-      else sch_fp64y_item<64, 32>(p, w, local, smem_raw, tid);
+      switch (slabs) {
+        case 1: sch_fp64y_item<16, 32>(p, w, local, smem_raw, tid); break;
+        case 2: sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid); break;
+        case 3: sch_fp64y_item<48, 32>(p, w, local, smem_raw, tid); break;
+        default: sch_fp64y_item<64, 32>(p, w, local, smem_raw, tid); break;
+      }
       break;
   }
 }

@@ -653,16 +653,18 @@ struct __align__(16) SchSmemY {
 };
 static_assert(sizeof(StageY) == kYChunkBytes, "six bulk copies per chunk");
 
-__device__ __forceinline__ void issue_chunk_y(const MixedPrep& m, int cb, int bb, int ig0, StageY& st,
-                                              unsigned long long* bar) {
-  mbar_expect_tx(bar, kYChunkBytes);
+// band_halves: pre-pass band blocks of the item that hold bands (1 for a
+// last block of at most kBN bands, whose second block is not copied)
+__device__ __forceinline__ void issue_chunk_y(const MixedPrep& m, int cb, int bb, int ig0, int band_halves,
+                                              StageY& st, unsigned long long* bar) {
+  mbar_expect_tx(bar, kYChunkBytes - (uint32_t)(2 - band_halves) * (uint32_t)sizeof(st.n[0]));
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const size_t col_off = ((size_t)(2 * cb + h) * m.nc_pad + ig0) * kBPM;
     const size_t band_off = ((size_t)(2 * bb + h) * m.nc_pad + ig0) * kBN;
     bulk_load(&st.a[h][0][0], m.colA + col_off, sizeof(st.a[h]), bar);
     bulk_load(&st.b[h][0][0], m.colB + col_off, sizeof(st.b[h]), bar);
-    bulk_load(&st.n[h][0][0], m.band + band_off, sizeof(st.n[h]), bar);
+    if (h < band_halves) bulk_load(&st.n[h][0][0], m.band + band_off, sizeof(st.n[h]), bar);
   }
 }
 
@@ -699,13 +701,17 @@ __device__ __forceinline__ bool sch_mixedy_item(const GppDev& p, const GppWork& 
       }
   // this thread's bands: 4 consecutive of one pre-pass band block
   const int nb_blk = ty >> 3, nb_off = (ty & 7) * TB;
+  // a last band block of at most kBN bands sums one pre-pass block: warps
+  // 4-7 (nb_blk 1) form factors but skip the products, their sums stay 0
+  const int band_halves = band_end - n1_0 > kBN ? 2 : 1;
+  const bool sums = nb_blk < band_halves;
 
-  if (tid == 0) issue_chunk_y(m, ic.cb, ic.bb, ig_begin, sm.st[0], &sm.bar[0]);
+  if (tid == 0) issue_chunk_y(m, ic.cb, ic.bb, ig_begin, band_halves, sm.st[0], &sm.bar[0]);
   for (int c = 0; c < n_chunks; ++c) {
     const int buf = c & 1;
     const int ig0 = ig_begin + c * kCK;
     if (tid == 0 && c + 1 < n_chunks)
-      issue_chunk_y(m, ic.cb, ic.bb, ig0 + kCK, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
+      issue_chunk_y(m, ic.cb, ic.bb, ig0 + kCK, band_halves, sm.st[buf ^ 1], &sm.bar[buf ^ 1]);
     const uint32_t pc = buf ? phase1 : phase0, pn = buf ? phase0 : phase1;
     const bool ok = mbar_wait(&sm.bar[buf], pc, m.status);
     if (buf == 0) phase0 ^= 1; else phase1 ^= 1;
@@ -729,7 +735,7 @@ __device__ __forceinline__ bool sch_mixedy_item(const GppDev& p, const GppWork& 
     }
     __syncthreads();
 #pragma unroll 1
-    for (int kr = 0; kr < kCK; kr += kRun) {
+    for (int kr = 0; sums && kr < kCK; kr += kRun) {
 #pragma unroll 2
       for (int k = kr; k < kr + kRun; ++k) {
         const float4 n01 = *reinterpret_cast<const float4*>(&st.n[nb_blk][k][nb_off]);

@@ -49,6 +49,9 @@ struct FactorSmem {
     double2 red[kFusedBands][kNW][kFacCols];   // item epilogue: per-column ssx sums
   };
   float2 an[kFusedBands][kFacK];               // occupied bands' aqsn over the tile's g-vectors
+  // the current job's frequency constants, formed once per CTA and job:
+  // wx as float-float (hi, lo), its FP32 rounding and remainder, 1 / wx^2
+  float wxc[kNW][5];
 };
 // Dynamic shared memory: ssx float-float accumulators (hi.x, hi.y, lo.x,
 // lo.y) per (output, lane quarter), each read and written by its own lane
@@ -125,6 +128,70 @@ __device__ __forceinline__ float ff_dot2_round(FF a, FF g, FF b, FF h) {
   return s + (es + t);
 }
 
+// Unnormalised float-float results (hi, lo) for operands that feed only
+// further products, TwoSums or one final rounding: the pair's value is the
+// same as the normalised one's, its lo may exceed half an ulp of hi.
+// x y: the exact product of the hi parts (FMA) plus the cross terms.
+__device__ __forceinline__ FF ff_mul_raw(FF x, FF y) {
+  const float p = x.hi * y.hi;
+  return FF{p, fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)))};
+}
+// a g - b h: the hi products' difference by TwoSum, their exact errors and
+// the cross terms in lo (lo * lo terms dropped, ~2^-46 of the products).
+__device__ __forceinline__ FF ff_dot2_raw(FF a, FF g, FF b, FF h) {
+  const float p1 = a.hi * g.hi, p2 = b.hi * h.hi;
+  const float e1 = fmaf(a.hi, g.hi, -p1), e2 = fmaf(b.hi, h.hi, -p2);
+  const float t = fmaf(a.hi, g.lo, fmaf(a.lo, g.hi, e1)) - fmaf(b.hi, h.lo, fmaf(b.lo, h.hi, e2));
+  float s, es;
+  two_sum_f(p1, -p2, s, es);
+  return FF{s, es + t};
+}
+// 1 / x for x > 0 (x normalised): FP32 reciprocal and one float-float
+// correction, unnormalised.
+__device__ __forceinline__ FF ff_rcp_raw(FF x) {
+  const float r0 = rcp_f32(x.hi);
+  return FF{r0, r0 * (fmaf(-x.hi, r0, 1.0f) - x.lo * r0)};
+}
+
+// Decisions of one element that the fast path leaves open, out of line so
+// that the common path carries no branch for them: the keep decisions of
+// the frequencies in rare bits 0-2 (within 2^-30 of a threshold, or the
+// guard's second condition binding: |wtilde|^2 >= 62000), and the
+// second-branch tests of dropped terms in bits 3-5 that are not clearly
+// inside it.  Returns the element's mask (keep bits 0-2, second-branch bits
+// 3-5) with those decisions taken as the FP64 path takes them.
+static __device__ __noinline__ unsigned factor_rare(unsigned mask, unsigned rare, const double* wxp,
+                                                    double wtx, double wty, bool thr2_binds, bool big_s) {
+  const FF a = ff_of(wtx), b = ff_of(wty);
+  const FF b2 = ff_mul(b, b);
+  const FF s2 = ff_add(ff_mul(a, a), b2);
+  const FF quarter{0.25f, 0.f};
+  for (int iw = 0; iw < kNW; ++iw) {
+    const FF wv = ff_sq_add(ff_sub_raw(ff_of(wxp[iw]), a), b2);
+    bool keep = (mask >> iw) & 1u;
+    if ((rare >> iw) & 1u) {
+      bool near;
+      keep = ff_gt_fast(wv, quarter, near);
+      if (thr2_binds) {
+        bool n2;
+        keep = keep && ff_gt(ff_mul(wv, FF{250000.f, 0.f}), s2, n2);
+        near = near || n2;
+      }
+      if (near) keep = keep_fp64(wxp[iw], wtx, wty);
+    }
+    const bool plain = big_s && wv.hi >= 1e-30f;
+    bool second = !keep && plain;
+    if ((rare >> (3 + iw)) & 1u || (!keep && !plain)) {
+      bool n3;
+      const FF s_big = ff_mul(s2, FF{1e6f, 0.f});  // |wtilde|^2 / to1 (1e6 exact)
+      second = !keep && wv.hi > 0.f && ff_gt_fast(s_big, wv, n3);
+      if (!keep && (n3 || wv.hi < 1e-30f)) second = second_fp64(wxp[iw], wtx, wty);
+    }
+    mask = (mask & ~((1u << iw) | (8u << iw))) | (keep ? (1u << iw) : 0u) | (second ? (8u << iw) : 0u);
+  }
+  return mask;
+}
+
 // kGroup: the jobs of a batch from a device array; else the one job `single`
 // (a kernel parameter, so that an execution can be captured in a graph).
 template <bool kGroup>
@@ -135,8 +202,10 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
   extern __shared__ float4 acc_dyn[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const FF quarter{0.25f, 0.f};
+  int cached = -1;  // job whose frequency constants sm.wxc holds
   for (int item = blockIdx.x; item < total; item += gridDim.x) {
-    const FactorJob& J = kGroup ? jobs[find_job(jobs, n_jobs, item)] : single;
+    const int ji = kGroup ? find_job(jobs, n_jobs, item) : 0;
+    const FactorJob& J = kGroup ? jobs[ji] : single;
     const GppDev& p = J.p;
     const int local = item - J.item_off;
     const int main_items = J.ncb * J.n_seg;
@@ -152,20 +221,41 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
       }
       continue;
     }
+    {  // this item's share of the B slices and epilogue factors
+      const long long b0 = (long long)local * J.b_per_item, w0 = (long long)local * J.w_per_item;
+      const long long b1 = min(b0 + J.b_per_item, oz_prep_b_count(J.oz));
+      const long long w1 = min(w0 + J.w_per_item, oz_weights_count(J.oz));
+      for (long long e = b0 + tid; e < b1; e += kFacThreads) oz_prep_b_elem(J.d, J.oz, e);
+      for (long long e = w0 + tid; e < w1; e += kFacThreads) oz_weights_elem(J.d, J.oz, e);
+    }
     const int s = local / J.ncb, cb = local % J.ncb;
     const int t_begin = s * J.seg_tiles, t_end = min(J.kt, t_begin + J.seg_tiles);
     const int nvb = p.nvband <= kFusedBands ? p.nvband : 0;
     const int outputs = nvb * kNW * kFacCols;  // ssx sums: (band, frequency, column)
+    if (ji != cached) {  // the same for the whole CTA
+      if (tid < kNW) {
+        const double w = p.wx[tid];
+        const FF f = ff_of(w);
+        const float h = __double2float_rn(w);
+        sm.wxc[tid][0] = f.hi;
+        sm.wxc[tid][1] = f.lo;
+        sm.wxc[tid][2] = h;
+        sm.wxc[tid][3] = __double2float_rn(w - (double)h);
+        sm.wxc[tid][4] = __double2float_rn(rcp_f64(w * w));
+      }
+      __syncthreads();
+      cached = ji;
+    }
     FF wx[kNW];
     float wxh[kNW], wxl[kNW], iwx2[kNW];
     bool wx32 = true;  // every frequency exact in FP32 (the mini-app's 3, 4, 5)
 #pragma unroll
     for (int iw = 0; iw < kNW; ++iw) {
-      wx[iw] = ff_of(p.wx[iw]);
+      wx[iw] = FF{sm.wxc[iw][0], sm.wxc[iw][1]};
       wx32 = wx32 && wx[iw].lo == 0.f;
-      wxh[iw] = __double2float_rn(p.wx[iw]);
-      wxl[iw] = __double2float_rn(p.wx[iw] - (double)wxh[iw]);
-      iwx2[iw] = __double2float_rn(rcp_f64(p.wx[iw] * p.wx[iw]));
+      wxh[iw] = sm.wxc[iw][2];
+      wxl[iw] = sm.wxc[iw][3];
+      iwx2[iw] = sm.wxc[iw][4];
     }
     // float-float accumulators of the ssx sums this thread owns
     for (int r = 0; r < kSsxRounds; ++r) {
@@ -194,57 +284,47 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
           const double2 wt = p.wt[off];
           const double2 ie = p.ieps[off];
           const FF a = ff_of(wt.x), b = ff_of(wt.y), er = ff_of(ie.x), ei = ff_of(ie.y);
-          const FF gx = ff_add(ff_mul(er, a), ff_neg(ff_mul(ei, b)));
-          const FF gy = ff_add(ff_mul(er, b), ff_mul(ei, a));
-          const FF b2 = ff_mul(b, b);
-          const FF s2 = ff_add(ff_mul(a, a), b2);      // |wtilde|^2
+          const FF gx = ff_dot2_raw(er, a, ei, b);           // G = I_eps wtilde
+          const FF gy = ff_dot2_raw(er, b, ff_neg(ei), a);
+          const FF b2 = ff_mul_raw(b, b);
+          const FF s2 = ff_dot2_raw(a, a, b, ff_neg(b));     // |wtilde|^2
           // G (c + i b) = wx G - G conj(wtilde) = wx G - |wtilde|^2 I_eps
-          const FF sex = ff_mul(s2, er), sey = ff_mul(s2, ei);
+          const FF sex = ff_mul_raw(s2, er), sey = ff_mul_raw(s2, ei);
           // |wtilde|^2 * 4e-6 >= 0.25 only for |wtilde|^2 >= 62500; below,
           // |wdiff|^2 > 0.25 implies the guard's second condition
           const bool thr2_binds = s2.hi >= 62000.f;
           // |wtilde|^2 / to1 > 1 >= |wdiff|^2 of a dropped term: its second
           // occupied-band branch is then the exact-pole test alone
           const bool big_s = s2.hi > 1.01e-6f;
-          unsigned mask = 0u;
+          unsigned mask = 0u, rare = thr2_binds ? 7u : 0u;
+          float2 yv[kNW];
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
             const FF wv = ff_sq_add(ff_sub_raw(wx[iw], a), b2);  // |wdiff|^2
             // keep: |wdiff|^2 > max(0.25, |wtilde|^2 * 4e-6), i.e. both
-            // wv > 0.25 and wv * 250000 > |wtilde|^2 (250000 exact in FP32)
+            // wv > 0.25 and wv * 250000 > |wtilde|^2 (250000 exact in FP32);
+            // the second condition only binds for thr2_binds (rare path)
             bool near;
-            bool keep = ff_gt_fast(wv, quarter, near);
-            if (thr2_binds) {
-              bool n2;
-              keep = keep && ff_gt(ff_mul(wv, FF{250000.f, 0.f}), s2, n2);
-              near = near || n2;
-            }
-            if (near) keep = keep_fp64(p.wx[iw], wt.x, wt.y);  // within 2^-30 of a threshold
+            const bool keep = ff_gt_fast(wv, quarter, near);
             // the factor of every term (the warp's lanes almost always
-            // disagree on keep), zero where the guard drops it
-            const FF r = ff_rcp(wv);
-            float yx, yy;
+            // disagree on keep), selected by the final keep bit below
+            const FF r = ff_rcp_raw(wv);
             if (wx32) {
-              yx = ff_factor_round(wx[iw].hi, gx, sex, r);
-              yy = ff_factor_round(wx[iw].hi, gy, sey, r);
+              yv[iw] = make_float2(ff_factor_round(wx[iw].hi, gx, sex, r), ff_factor_round(wx[iw].hi, gy, sey, r));
             } else {
-              yx = ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r);
-              yy = ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r);
+              yv[iw] = make_float2(ff_mul_round(ff_add(ff_mul(wx[iw], gx), ff_neg(sex)), r),
+                                   ff_mul_round(ff_add(ff_mul(wx[iw], gy), ff_neg(sey)), r));
             }
-            yt[iw] = keep ? make_float2(yx, yy) : make_float2(0.f, 0.f);
-            mask |= keep ? (1u << iw) : 0u;
             // second occupied-band branch: 0 < |wdiff|^2 < |wtilde|^2 / to1,
             // which for |wtilde|^2 > 1e-6 and a dropped term is |wdiff|^2 > 0
             const bool plain = big_s && wv.hi >= 1e-30f;
-            bool second = !keep && plain;
-            if (nvb > 0 && !keep && !plain) {  // rare
-              bool n3;
-              const FF s_big = ff_mul(s2, FF{1e6f, 0.f});  // |wtilde|^2 / to1 (1e6 exact)
-              second = wv.hi > 0.f && ff_gt_fast(s_big, wv, n3);
-              if (n3 || wv.hi < 1e-30f) second = second_fp64(p.wx[iw], wt.x, wt.y);
-            }
-            mask |= (nvb > 0 && second) ? (8u << iw) : 0u;
+            mask |= (keep ? (1u << iw) : 0u) | ((!keep && plain) ? (8u << iw) : 0u);
+            rare |= (near ? (1u << iw) : 0u) | ((nvb > 0 && !keep && !plain) ? (8u << iw) : 0u);
           }
+          if (rare) mask = factor_rare(mask, rare, p.wx, wt.x, wt.y, thr2_binds, big_s);
+          if (nvb == 0) mask &= 7u;
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) yt[iw] = (mask & (1u << iw)) ? yv[iw] : make_float2(0.f, 0.f);
           if (nvb > 0) {
             const float2 g32 = make_float2(ff_round(gx), ff_round(gy));
             const float bb = ff_round(b);
@@ -323,13 +403,17 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
           if (igp >= 0) {
             const double2 am = p.aqsm[(size_t)n1 * p.nc + igp];
             const double f = p.occ * p.vcoul[igp];
-            double sx = 0.0, sy = 0.0;  // the four quarters' float-float sums, in FP64
+            // the four quarters' float-float sums added in float-float,
+            // then widened once
+            float4 a = acc_dyn[4 * o];
+            FF fx{a.x, a.z}, fy{a.y, a.w};
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const float4 a = acc_dyn[4 * o + q];
-              sx += (double)a.x + (double)a.z;
-              sy += (double)a.y + (double)a.w;
+            for (int q = 1; q < 4; ++q) {
+              a = acc_dyn[4 * o + q];
+              fx = ff_add(fx, FF{a.x, a.z});
+              fy = ff_add(fy, FF{a.y, a.w});
             }
+            const double sx = (double)fx.hi + (double)fx.lo, sy = (double)fy.hi + (double)fy.lo;
             // (sx + i sy) conj(am) f
             v = make_double2(fma(sx, am.x, sy * am.y) * f, fma(sy, am.x, -sx * am.y) * f);
           }
@@ -373,6 +457,17 @@ void factor_job_size(FactorJob& j, const GppDev& p, int kt, int grid, double sha
   w.n_splits = j.n_seg;
   w.split_len = j.seg_tiles * kFacK;
   w.n_items = w.n_band_blocks * j.ncb * j.n_seg;
+}
+
+void factor_job_operands(FactorJob& j, const FfDev& d, const OzakiPrep& oz) {
+  j.d = d;
+  j.oz = oz;
+  j.oz.stab = nullptr;
+  const long long main_items = std::max(1LL, (long long)j.ncb * j.n_seg);
+  const long long b = (long long)oz.n_col_blocks * oz.kt * 64 * (kOzKTile / 8);
+  const long long w = (long long)oz.ng * oz.nb_pad;
+  j.b_per_item = (b + main_items - 1) / main_items;
+  j.w_per_item = (w + main_items - 1) / main_items;
 }
 
 size_t factor_ssx_partial_bytes(const FactorJob& j) {

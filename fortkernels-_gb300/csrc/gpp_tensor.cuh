@@ -15,7 +15,9 @@ constexpr int kFusedBands = 8;      // occupied bands whose ssx sums the factor 
 // block); an item writes the contraction's A slices of its tiles and, for
 // the occupied bands, the ssx partial sums of its columns over its
 // g-vectors into ssx.partial in the reduction's layout (band block, column
-// block, segment).
+// block, segment).  Each item also writes its share of the contraction's
+// other operands (B slices of aqsn, epilogue factors of aqsm): memory-bound
+// work spread through the compute-bound pass instead of two launches.
 struct FactorJob {
   GppDev p;
   unsigned char* a_tiles;  // OzakiPrep::a_tiles of the instance's contraction
@@ -24,6 +26,9 @@ struct FactorJob {
   int n_seg, seg_tiles;    // g-vector segments per column block, K tiles per segment
   int item_off;            // first global item of the job
   GppWork ssx;             // ssx partial layout (bn kSsxBN, n_col_blocks ncb, n_splits n_seg)
+  FfDev d;                 // the contraction's operands (aqsn, aqsm, column weight)
+  OzakiPrep oz;            // its slice images and epilogue factor table
+  long long b_per_item, w_per_item;  // B-slice / epilogue-factor elements per main item
 };
 
 // Sizes the factor items of one instance whose share of a launch over
@@ -31,6 +36,9 @@ struct FactorJob {
 // elements; about 12 items per CTA over the launch) and fills the ssx work
 // layout (partial pointer and item_off left to the caller).
 void factor_job_size(FactorJob& j, const GppDev& p, int kt, int grid, double share);
+// The contraction's operands of the job (B slices, epilogue factors) as the
+// items' shares; d and oz of the instance's contraction plan.
+void factor_job_operands(FactorJob& j, const FfDev& d, const OzakiPrep& oz);
 size_t factor_ssx_partial_bytes(const FactorJob& j);
 // Items of the job: the (segment, column block) items and those that zero
 // the padding rows of the last row block.

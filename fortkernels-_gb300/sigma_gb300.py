@@ -65,6 +65,7 @@ SIGNATURES = {
     "sigma_gpp_plan_timing": ([_P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_fp64_noalloc": ([_I, _I, _I, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
     "sigma_gpp_batch_create": ([_P, _I, _P, _I, _P], _I),
+    "sigma_gpp_batch_create_tuned": ([_P, _I, _P, _I, _P, _I, _I], _I),
     "sigma_gpp_batch_execute": ([_P, _P], _I),
     "sigma_gpp_batch_launch_graph": ([_P, _P], _I),
     "sigma_gpp_batch_info": ([_P, _P, _P, _P], _I),
@@ -404,9 +405,12 @@ class GppBatch:
     `instances` is a list of dicts with the sigma_gpp_instance fields: host
     index maps as numpy int arrays, every other array a CUDA tensor or a
     device pointer.  `tiles` (optional) gives the FP64 main-pass tile per
-    instance (-1 library choice, 0 = 32x32, 1 = 16x64, 2 = 64x16)."""
+    instance (-1 library choice; per-band frequencies 0 = 32x32, 1 = 16x64,
+    2 = 64x16; one frequency set 3 = 64x32, 4 = 32x64, 5 = 32x32, 6 =
+    128x16).  `items_per_cta` / `tensor_items_per_cta` (0: defaults) size the
+    work items (sigma_gpp_batch_create_tuned)."""
 
-    def __init__(self, instances, precision=PREC_FP64, tiles=None):
+    def __init__(self, instances, precision=PREC_FP64, tiles=None, items_per_cta=0, tensor_items_per_cta=0):
         self.lib = load()
         self._keep = []
         arr = _instance_array(instances, self._keep)
@@ -416,9 +420,10 @@ class GppBatch:
             t = np.ascontiguousarray(tiles, dtype=np.int32)
             self._keep.append(t)
         h = C.c_void_p()
-        st = self.lib.sigma_gpp_batch_create(C.byref(h), len(instances), C.addressof(arr), precision,
-                                             None if t is None else _ptr(t))
-        _check(st, "sigma_gpp_batch_create")
+        st = self.lib.sigma_gpp_batch_create_tuned(C.byref(h), len(instances), C.addressof(arr), precision,
+                                                   None if t is None else _ptr(t), int(items_per_cta),
+                                                   int(tensor_items_per_cta))
+        _check(st, "sigma_gpp_batch_create_tuned")
         self.handle = h
 
     def info(self):

@@ -140,10 +140,12 @@ def test_batch_every_tile_shape_matches_oracle(sigma_lib, small_set, tile):
         _check(x.outputs(), o, 0)
 
 
-@pytest.mark.parametrize("tile", [3, 4, 5], ids=["y64x32", "y32x64", "y32x32"])
+@pytest.mark.parametrize("tile", [3, 4, 5, 6], ids=["y64x32", "y32x64", "y32x32", "y128x16"])
 def test_batch_shared_frequency_tiles_match_oracle(sigma_lib, small_set, tile):
     """Instances that all share one frequency set run the shared-factor
-    kernel (tiles 3-5)."""
+    kernel (tiles 3-6); the last band block of each instance runs the
+    shortest item of 16-band slabs that holds its bands (1 to 8 slabs over
+    the set's 5 to 128 bands)."""
     xs, oracles, _ = small_set
     keep = [k for k, x in enumerate(xs) if x.wx_stride == 0]
     b = sigma_lib.GppBatch([xs[k].as_dict() for k in keep], precision=0, tiles=[tile] * len(keep))

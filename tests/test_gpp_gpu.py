@@ -92,8 +92,11 @@ def test_random_matches_oracle(sigma_lib, case, prec):
     _check(g, o, prec, abs2=O.gpp_abs2(prob) if prec == 1 else None)
 
 
-@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "mixed", "tensor"])
 def test_exact_poles_and_skipped_columns(sigma_lib, prec):
+    """Exact poles, a term exactly on the |wdiff|^2 = 0.25 boundary, a zero
+    wtilde and |wtilde|^2 >= 62000 (the guard's second condition binding):
+    in the tensor form these take the factor pass's out-of-line decisions."""
     prob = W.gpp_random(20, 4, 1024, 30, 21)
     prob.wtilde_array = prob.wtilde_array.copy()
     wx = prob.wx_array
@@ -102,6 +105,7 @@ def test_exact_poles_and_skipped_columns(sigma_lib, prec):
     prob.wtilde_array[5, 11] = complex(wx[2], 0.0)
     prob.wtilde_array[7, 12] = complex(wx[1] + 0.5, 0.0)
     prob.wtilde_array[8, 13] = 0.0
+    prob.wtilde_array[9, 14] = complex(300.0, 0.5)
     # skipped columns: igp < 0 (gppKer.cpp:328)
     prob.indinv = prob.indinv.copy()
     prob.indinv[prob.inv_igp_index[3]] = -1

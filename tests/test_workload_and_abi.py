@@ -197,6 +197,13 @@ def test_batch_validation_precedes_device_work(libpath):
     assert create([dict(good, wx_band_stride=2)]) == -1
     assert create([good, good], tiles=[1, -1]) == -8   # per-band-kernel tile, shared frequencies
     assert create([good, dict(good, wx_band_stride=3)], tiles=[4, 0]) == -8  # mixed families
+    # the tuned entry: negative sizing is an invalid shape, checked first
+    g = lib.sigma_gpp_batch_create_tuned
+    g.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int]
+    keep = []
+    arr = S._instance_array([good], keep)
+    assert g(C.byref(h), 1, C.addressof(arr), 0, None, -1, 0) == -1
+    assert g(C.byref(h), 1, C.addressof(arr), 2, None, 0, -3) == -1
     st = create([good, good], tiles=[4, -1])
     assert st in (0, -7, -4)
     if st == 0:
@@ -222,5 +229,14 @@ def test_tile_table_covers_every_shape_class():
             assert A.TILES[v] == min(ms, key=ms.get)
     assert A.shape_class(16, 16) == "b0c0" and A.shape_class(17, 64) == "b1c3"
     for s in W.batched_shapes():
-        assert A.tile_for(s["number_bands"], s["ngpown"]) in (-1, 3, 4, 5)
+        assert A.tile_for(s["number_bands"], s["ngpown"]) in (-1, 3, 4, 5, 6)
         assert A.tile_for(s["number_bands"], s["ngpown"], shared=False) in (-1, 0, 1, 2)
+    # every form's work sizing: a tuned candidate, the fastest accepted one
+    for form, key in A.SIZING_KEY.items():
+        v = A.sizing_for(form, t)
+        if key not in t:
+            assert v == 0
+            continue
+        assert v in A.SIZING_CANDIDATES[form]
+        ms = {int(k): m for k, m in t["sizing_timings_ms"][form].items() if m is not None}
+        assert v == min(ms, key=ms.get)
