@@ -24,10 +24,10 @@ items each resident CTA takes (sigma_gpp_batch_create_tuned): the FP64 and
 mixed main passes' items per CTA (band block x column block x g-vector
 split), and the tensor form's contraction items per CTA (the K split of
 each instance's 128-row x 64-band blocks).  The tuner times each candidate
-on the first SIZING_INSTANCES instances of the 48-instance set through
-graph replays and keeps the fastest; a tensor candidate is kept only if
-every achtemp / asxtemp of that set stays within 1e-6 of the FP64 form's
-(the tensor form's error depends on where its K splits fall).
+on the 48-instance set through graph replays and keeps the fastest; a
+tensor candidate is kept only if every achtemp / asxtemp of the set stays
+within 1e-6 of the FP64 form's (the tensor form's error depends on where
+its K splits fall, so a subset does not decide it).
 `sizing_for(form)` reads the choice (0 = the library's default).
 
     python fortkernels-_gb300/autotune.py --out <path>
@@ -73,7 +73,7 @@ def tile_for(number_bands: int, ngpown: int, table=None, shared=True) -> int:
     return v if v in FAMILIES["shared" if shared else "per_band"] else -1
 
 
-SIZING_INSTANCES = 12
+SIZING_INSTANCES = 48
 SIZING_CANDIDATES = {"fp64": (8, 16, 32), "mixed": (8, 16, 32), "tensor": (10, 20, 40)}
 SIZING_KEY = {"fp64": "fp64_items_per_cta", "mixed": "mixed_items_per_cta", "tensor": "tensor_items_per_cta"}
 
@@ -107,7 +107,8 @@ def _time_batch(S, torch, dicts, prec, stream, reps, tiles=None, ipc=0, tipc=0):
 
 def tune_sizing(classes, reps=3, log=print):
     """Items per CTA of each batched form on the first SIZING_INSTANCES
-    instances of the 48-instance set (FP64 with its tuned tiles)."""
+    instances of the 48-instance set (all of them; FP64 with its tuned
+    tiles)."""
     import numpy as np
     import torch
 

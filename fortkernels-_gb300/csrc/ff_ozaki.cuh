@@ -147,6 +147,7 @@ struct OzGroup {
   const int4* items;       // [total]: job, row block << 16 | band block, first K' tile, tiles | piece << 16
   int total;
   int r_warps;
+  int outs, segs;          // epilogue staging: outputs per job (1 or 2), max_seg over the jobs
   int* status;
 };
 // Host side of a group: the item table of job `job` appended to `items`

@@ -225,6 +225,9 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
   g.n_jobs = n;
   g.items = reinterpret_cast<const int4*>(base + o_items);
   g.total = (int)items.size();
+  g.outs = 1;
+  g.segs = 1;
+  for (const OzGroupJob& j : jobs) g.segs = std::max(g.segs, j.oz.max_seg);
   g.r_warps = rwarps;
   g.status = b->counters + 2;
   return SIGMA_OK;

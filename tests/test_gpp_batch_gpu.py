@@ -2,13 +2,19 @@
 one work queue per pass, against the oracle and the single-instance plans.
 
 Bars: FP64 <= 1e-12 relative per output against the oracle and against a
-single-instance FP64 plan (same terms, different g-vector splits and tiles).  Mixed (FP32 terms): every achtemp / asxtemp output within
-max(1e-6 |exact|, 8 * 2^-24 * sqrt(sum |term|^2)).  The FP32 path's terms
-carry independent relative errors of about 1.45 * 2^-24 rms, so its error on
-an output is about 1.45 * 2^-24 * sqrt(sum |term|^2); the second bound is
-that model at more than five standard deviations and only exceeds the first
-for outputs whose terms cancel (sqrt(sum |term|^2) / |sum| > 10).  Graph
-replays are bit-identical to one another and to the uncaptured execution.
+single-instance FP64 plan (same terms, different g-vector splits and
+tiles).  Mixed and tensor (FP32-class terms): every achtemp / asxtemp output
+within 1e-6 relative when its condition number kappa = sqrt(sum |term|^2) /
+|sum| is at most 10, else within max(1e-6 |exact|, 8 * 2^-24 * sqrt(sum
+|term|^2)).  The FP32 terms carry independent relative errors of about 1.45
+* 2^-24 rms (the roundings of the operands to FP32, which no compensated
+summation removes), so an output's error is about 1.45 * 2^-24 * sqrt(sum
+|term|^2): 8.6e-8 * kappa relative; the second bound is that model at more
+than five standard deviations.  Two outputs of the small set have kappa >
+10: instance 0's achtemp[1] (kappa 10.8, within 1e-6 all the same) and
+instance 1's achtemp[1] (17 bands, stress fill; kappa 17.2: 1.5e-6 mixed,
+1.75e-6 tensor, 2e-7 * kappa).  Graph replays are bit-identical to one
+another and to the uncaptured execution.
 """
 import numpy as np
 import pytest
@@ -87,8 +93,15 @@ def _small_set():
 
 
 def mixed_bound(exact, abs2):
-    """Allowed |error| of each mixed-path output (see the module docstring)."""
-    return np.maximum(MIXED_TOL * np.abs(exact), FP32_TERM_BOUND * np.sqrt(abs2))
+    """Allowed |error| of each mixed / tensor output: 1e-6 relative for
+    every output whose condition number kappa = sqrt(sum |term|^2) / |sum
+    term| is at most 10; beyond that the FP32 term-rounding model
+    8 * 2^-24 * sqrt(sum |term|^2) (the terms' own FP32 roundings, ~1.5 *
+    2^-24 rms, cannot be compensated by the summation)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kappa = np.sqrt(abs2) / np.abs(exact)
+    model = np.maximum(MIXED_TOL * np.abs(exact), FP32_TERM_BOUND * np.sqrt(abs2))
+    return np.where(kappa <= 10.0, MIXED_TOL * np.abs(exact), model)
 
 
 def _check(g, o, prec, abs2=None):

@@ -3,11 +3,13 @@
 Bars (written in each test): FP64 path <= 1e-12 relative per output, mixed
 path <= 1e-6 relative per achtemp / asxtemp output.  acht_n1_loc is checked
 per band for FP64 and normwise for the mixed path.  On the seeded random
-cases the mixed bar is max(1e-6 |exact|, 8 * 2^-24 * sqrt(sum |term|^2)) per
-output: FP32 terms carry independent errors of ~1.5 * 2^-24 rms, so an
-output whose terms cancel (sqrt(sum |term|^2) / |sum| above ~10) can sit
-above 1e-6 relative while within the method's error; the second bound is
-that model at more than five standard deviations.
+cases the mixed and tensor bar is 1e-6 relative for every output whose
+condition number kappa = sqrt(sum |term|^2) / |sum| is at most 10, else
+max(1e-6 |exact|, 8 * 2^-24 * sqrt(sum |term|^2)): FP32 terms carry
+independent errors of ~1.5 * 2^-24 rms, so an output whose terms cancel can
+sit above 1e-6 relative while within the method's error; the second bound is
+that model at more than five standard deviations.  The largest kappa of
+these cases is 10.06 (nb33-nv1-nc1000-ng37, asxtemp[0]: 5.3e-7 mixed).
 """
 import numpy as np
 import pytest
@@ -25,7 +27,15 @@ FP32_TERM_BOUND = 8 * 2.0 ** -24
 
 
 def _mixed_bound(exact, abs2):
-    return np.maximum(MIXED_TOL * np.abs(exact), FP32_TERM_BOUND * np.sqrt(abs2))
+    """Allowed |error| of each mixed / tensor output: 1e-6 relative for
+    every output whose condition number kappa = sqrt(sum |term|^2) / |sum
+    term| is at most 10; beyond that the FP32 term-rounding model
+    8 * 2^-24 * sqrt(sum |term|^2) (the terms' own FP32 roundings, ~1.5 *
+    2^-24 rms, cannot be compensated by the summation)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kappa = np.sqrt(abs2) / np.abs(exact)
+    model = np.maximum(MIXED_TOL * np.abs(exact), FP32_TERM_BOUND * np.sqrt(abs2))
+    return np.where(kappa <= 10.0, MIXED_TOL * np.abs(exact), model)
 
 
 def _check(g, o, prec, check_n1=True, abs2=None):
