@@ -1,7 +1,5 @@
-// The split-BF16 tcgen05 contraction kernel (roles, ring, TMEM drains and
-// epilogue), shared by the FF / GPP contractions (ff_ozaki.cu) and by the
-// GPP tensor form's fused producer (gpp_tensor.cu), which adds warps of its
-// own to the same CTA.
+// The split-BF16 tcgen05 contraction kernel: roles, stage ring, TMEM drains
+// and epilogue (ff_ozaki.cu launches it for the FF and GPP contractions).
 #pragma once
 
 #include "ff_ozaki.cuh"
@@ -103,38 +101,9 @@ __host__ __device__ constexpr uint32_t oz_smem_bytes(int outs, int segs) {
   return kRingBytes + oz_red_bytes(outs, segs);
 }
 
-// A producer that runs in warps of its own beside the contraction's roles
-// (warps 8 on; warp 7 pads the roles' warpgroup): it shares the SM's issue
-// slots with the tensor-core pipeline and waits on none of its barriers.
-// NoSide adds no warp.  A side sets kWarps (whole warpgroups), kRegs (its
-// per-thread registers after the redistribution below), and run(smem,
-// thread) with its dynamic shared memory after the epilogue staging.
-struct NoSide {
-  static constexpr int kWarps = 0;
-  static constexpr int kRegs = 0;
-  __device__ void run(unsigned char*, int) const {}
-};
-template <class Side>
-__host__ __device__ constexpr int oz_threads() {
-  return Side::kWarps > 0 ? 256 + 32 * Side::kWarps : kOzThreads;
-}
-// With a side the CTA launches at 65536 / threads registers per thread; the
-// roles' warpgroup drops to kRoleRegs (its three working lanes need few)
-// and the drain warpgroup takes kDrainRegs (128 FP32 running sums per lane).
-constexpr int kRoleRegs = 40, kDrainRegs = 232;
-
-template <int kRegs>
-__device__ __forceinline__ void reg_alloc() {
-  asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegs));
-}
-template <int kRegs>
-__device__ __forceinline__ void reg_dealloc() {
-  asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegs));
-}
-
-template <bool kGroup, class Side = NoSide>
-__global__ void __launch_bounds__(oz_threads<Side>(), 1)
-    ozaki_gemm_kernel(FfDev p, FfWork w, OzakiPrep oz, OzGroup grp, OzLaunch L, Side side = Side{}) {
+template <bool kGroup>
+__global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(FfDev p, FfWork w, OzakiPrep oz, OzGroup grp,
+                                                                  OzLaunch L) {
   extern __shared__ unsigned char smem_raw[];
   // full[kStages], empty[kStages], accf[2], acce[2], done
   __shared__ __align__(8) unsigned long long bars[2 * kStages + 5];
@@ -164,167 +133,155 @@ __global__ void __launch_bounds__(oz_threads<Side>(), 1)
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  if (warp >= 8) {
-    // ------------------------------------------------ the side producer
-    if constexpr (Side::kWarps > 0) {
-      if constexpr (Side::kRegs > 65536 / oz_threads<Side>()) reg_alloc<Side::kRegs>();
-      else if constexpr (Side::kRegs < 65536 / oz_threads<Side>()) reg_dealloc<Side::kRegs>();
-      side.run(reinterpret_cast<unsigned char*>(s_red + L.outs * 4 * L.segs * kOzCols), tid - 256);
+  if (warp == kTmaWarp) {
+    // ------------------------------------------------ bulk copies into the stage ring
+    if (lane == 0) {
+      uint32_t g = 0;  // tiles issued by this CTA
+      bool ok = true;
+      for (int item = L.begin + blockIdx.x; ok && item < n_items; item += gridDim.x) {
+        int job = 0;
+        const OzItem it = kGroup ? oz_group_item(grp, item, job) : oz_decode(oz, item);
+        const int nst = it.nst;
+        const unsigned char* at = kGroup ? grp.jobs[job].oz.a_tiles : oz.a_tiles;
+        const unsigned char* bt = kGroup ? grp.jobs[job].oz.b_tiles : oz.b_tiles;
+        const int two_kt = 2 * (kGroup ? grp.jobs[job].oz.kt : oz.kt);
+        const unsigned char* a_src = at + ((size_t)it.rb * two_kt + it.t0) * kOperandBytes;
+        const unsigned char* b_src = bt + ((size_t)it.cb * two_kt + it.t0) * kOperandBytes;
+        for (int s = 0; s < nst; ++s, ++g) {
+          const uint32_t b = g % kStages, use = g / kStages;
+          // stage b is free once the MMAs of its previous tile have completed
+          if (use > 0 && !mbar_wait(empty0 + 8u * b, (use - 1) & 1u, status)) {
+            ok = false;  // no further copies
+            break;
+          }
+          const uint32_t bar = full0 + 8u * b;
+          const uint32_t dst = sbase + b * kStageBytes;
+          mbar_expect_tx(bar, kStageBytes);
+          bulk_load(dst, a_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
+          bulk_load(dst + kOperandBytes, b_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
+        }
+      }
+      // after a failure: the copies of the last (up to kStages) tiles may
+      // still be landing; wait for them before the CTA releases its ring
+      if (!ok)
+        for (uint32_t t = g > (uint32_t)kStages ? g - kStages : 0u; t < g; ++t)
+          mbar_wait_own(full0 + 8u * (t % kStages), (t / kStages) & 1u);
     }
-  } else if (warp >= 4) {
-    // the roles' warpgroup (warp 7 pads it when a side is present)
-    if constexpr (Side::kWarps > 0) reg_dealloc<kRoleRegs>();
-    if (warp == kTmaWarp) {
-      // ------------------------------------------------ bulk copies into the stage ring
-      if (lane == 0) {
-        uint32_t g = 0;  // tiles issued by this CTA
-        bool ok = true;
-        for (int item = L.begin + blockIdx.x; ok && item < n_items; item += gridDim.x) {
-          int job = 0;
-          const OzItem it = kGroup ? oz_group_item(grp, item, job) : oz_decode(oz, item);
-          const int nst = it.nst;
-          const unsigned char* at = kGroup ? grp.jobs[job].oz.a_tiles : oz.a_tiles;
-          const unsigned char* bt = kGroup ? grp.jobs[job].oz.b_tiles : oz.b_tiles;
-          const int two_kt = 2 * (kGroup ? grp.jobs[job].oz.kt : oz.kt);
-          const unsigned char* a_src = at + ((size_t)it.rb * two_kt + it.t0) * kOperandBytes;
-          const unsigned char* b_src = bt + ((size_t)it.cb * two_kt + it.t0) * kOperandBytes;
-          for (int s = 0; s < nst; ++s, ++g) {
-            const uint32_t b = g % kStages, use = g / kStages;
-            // stage b is free once the MMAs of its previous tile have completed
-            if (use > 0 && !mbar_wait(empty0 + 8u * b, (use - 1) & 1u, status)) {
-              ok = false;  // no further copies
-              break;
-            }
-            const uint32_t bar = full0 + 8u * b;
-            const uint32_t dst = sbase + b * kStageBytes;
-            mbar_expect_tx(bar, kStageBytes);
-            bulk_load(dst, a_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
-            bulk_load(dst + kOperandBytes, b_src + (size_t)s * kOperandBytes, kOperandBytes, bar);
-          }
-        }
-        // after a failure: the copies of the last (up to kStages) tiles may
-        // still be landing; wait for them before the CTA releases its ring
-        if (!ok)
-          for (uint32_t t = g > (uint32_t)kStages ? g - kStages : 0u; t < g; ++t)
-            mbar_wait_own(full0 + 8u * (t % kStages), (t / kStages) & 1u);
+    __syncwarp();
+  } else if (warp == kGateWarp) {
+    // ------------------------------------------------ release of the MMA warp
+    // Waits for each tile's stage (and, at an accumulator lifetime's first
+    // tile, for the drain of that accumulator pair), and meets the MMA warp
+    // at a named barrier once per kGateTiles tiles.  The issuing thread itself never polls shared
+    // memory: a poll between its MMAs stalls the tensor pipe (measured: 89
+    // instead of 64 cycles per MMA).
+    // After a wait gives up it keeps meeting the MMA warp at the same named
+    // barriers (whose count must match) without waiting, and passes the
+    // failure on through them so the MMA warp issues nothing more.
+    uint32_t ph_acce0 = 0, ph_acce1 = 0;
+    bool used0 = false, used1 = false, failed = false;
+    uint32_t g = 0, gc = 0;
+    // group: the next item's tile count is loaded one item ahead
+    int nst_next = kGroup && L.begin + (int)blockIdx.x < n_items ? (grp.items[L.begin + blockIdx.x].w & 0xFFFF) : 0;
+    for (int item = L.begin + blockIdx.x; item < n_items; item += gridDim.x) {
+      int nst;
+      if (kGroup) {
+        nst = nst_next;
+        if (item + (int)gridDim.x < n_items) nst_next = grp.items[item + gridDim.x].w & 0xFFFF;
+      } else {
+        nst = oz_decode(oz, item).nst;
       }
-      __syncwarp();
-    } else if (warp == kGateWarp) {
-      // ------------------------------------------------ release of the MMA warp
-      // Waits for each tile's stage (and, at an accumulator lifetime's first
-      // tile, for the drain of that accumulator pair), and meets the MMA warp
-      // at a named barrier once per kGateTiles tiles.  The issuing thread itself never polls shared
-      // memory: a poll between its MMAs stalls the tensor pipe (measured: 89
-      // instead of 64 cycles per MMA).
-      // After a wait gives up it keeps meeting the MMA warp at the same named
-      // barriers (whose count must match) without waiting, and passes the
-      // failure on through them so the MMA warp issues nothing more.
-      uint32_t ph_acce0 = 0, ph_acce1 = 0;
-      bool used0 = false, used1 = false, failed = false;
-      uint32_t g = 0, gc = 0;
-      // group: the next item's tile count is loaded one item ahead
-      int nst_next = kGroup && L.begin + (int)blockIdx.x < n_items ? (grp.items[L.begin + blockIdx.x].w & 0xFFFF) : 0;
-      for (int item = L.begin + blockIdx.x; item < n_items; item += gridDim.x) {
-        int nst;
-        if (kGroup) {
-          nst = nst_next;
-          if (item + (int)gridDim.x < n_items) nst_next = grp.items[item + gridDim.x].w & 0xFFFF;
-        } else {
-          nst = oz_decode(oz, item).nst;
-        }
-        for (int s = 0; s < nst; ++s, ++g) {
-          const int cs = s % kChunkStages;
-          const uint32_t tb = gc & 1u;
-          if (lane == 0 && !failed) {
-            if (cs == 0) {  // first tile of an accumulator lifetime: pair tb must be drained
-              if (tb == 0 && used0) {
-                failed = !mbar_wait(acce0, ph_acce0, status);
-                ph_acce0 ^= 1u;
-              }
-              if (tb == 1 && used1) {
-                failed = failed || !mbar_wait(acce0 + 8u, ph_acce1, status);
-                ph_acce1 ^= 1u;
-              }
+      for (int s = 0; s < nst; ++s, ++g) {
+        const int cs = s % kChunkStages;
+        const uint32_t tb = gc & 1u;
+        if (lane == 0 && !failed) {
+          if (cs == 0) {  // first tile of an accumulator lifetime: pair tb must be drained
+            if (tb == 0 && used0) {
+              failed = !mbar_wait(acce0, ph_acce0, status);
+              ph_acce0 ^= 1u;
             }
-            const uint32_t b = g % kStages;
-            failed = failed || !mbar_wait(full0 + 8u * b, (g / kStages) & 1u, status);
-          }
-          if (cs == 0) {
-            if (tb == 0) used0 = true; else used1 = true;
-          }
-          if (cs == kChunkStages - 1 || s == nst - 1) ++gc;
-          if (s % kGateTiles == kGateTiles - 1 || s == nst - 1) {
-            __syncwarp();
-            mma_gate_sync(failed);
-          }
-        }
-      }
-      // every accumulator pair in use drained
-      if (lane == 0 && !failed) {
-        if (used0) mbar_wait(acce0, ph_acce0, status);
-        if (used1) mbar_wait(acce0 + 8u, ph_acce1, status);
-      }
-      __syncwarp();
-    } else if (warp == kMmaWarp) {
-      // ------------------------------------------------ tensor-core issue (lane 0)
-      uint32_t g = 0;   // tiles consumed by this CTA
-      uint32_t gc = 0;  // accumulator lifetimes started
-      bool failed = false;
-      // group: the next item's tile count is loaded one item ahead
-      int nst_next = kGroup && L.begin + (int)blockIdx.x < n_items ? (grp.items[L.begin + blockIdx.x].w & 0xFFFF) : 0;
-      for (int item = L.begin + blockIdx.x; item < n_items; item += gridDim.x) {
-        int nst;
-        if (kGroup) {
-          nst = nst_next;
-          if (item + (int)gridDim.x < n_items) nst_next = grp.items[item + gridDim.x].w & 0xFFFF;
-        } else {
-          nst = oz_decode(oz, item).nst;
-        }
-        for (int s = 0; s < nst; ++s, ++g) {
-          const int cs = s % kChunkStages;
-          const uint32_t tb = gc & 1u;
-          // stages full, accumulator pair free (or the gate warp gave up)
-          if (s % kGateTiles == 0) failed = mma_gate_sync(false) || failed;
-          if (lane == 0 && !failed) {
-            tc_fence_after();
-            const uint32_t b = g % kStages;
-            const uint32_t a_addr = sbase + b * kStageBytes;
-            const uint32_t b_addr = a_addr + kOperandBytes;
-            const uint32_t d_big = tmem + tb * 256u, d_small = d_big + 128u;
-  #pragma unroll
-            for (int kk = 0; kk < kOzKTile / 16; ++kk) {
-              const uint64_t a1 = sw64_desc(a_addr + kk * 32);
-              const uint64_t a2 = sw64_desc(a_addr + kSliceBytes + kk * 32);
-              const uint64_t a3 = sw64_desc(a_addr + 2 * kSliceBytes + kk * 32);
-              const uint64_t b1 = sw64_desc(b_addr + kk * 32);
-              const uint64_t b2 = sw64_desc(b_addr + kSliceBytes + kk * 32);
-              const uint64_t b3 = sw64_desc(b_addr + 2 * kSliceBytes + kk * 32);
-              const uint32_t acc = (cs > 0 || kk > 0) ? 1u : 0u;
-              mma_f16(d_big, a1, b1, kIdesc, acc);
-              mma_f16(d_small, a1, b2, kIdesc, acc);
-              mma_f16(d_small, a2, b1, kIdesc, 1u);
-              mma_f16(d_small, a1, b3, kIdesc, 1u);
-              mma_f16(d_small, a2, b2, kIdesc, 1u);
-              mma_f16(d_small, a3, b1, kIdesc, 1u);
+            if (tb == 1 && used1) {
+              failed = failed || !mbar_wait(acce0 + 8u, ph_acce1, status);
+              ph_acce1 ^= 1u;
             }
-            mma_commit(empty0 + 8u * b);  // stage b free once these MMAs complete
-            if (cs == kChunkStages - 1 || s == nst - 1) mma_commit(accf0 + 8u * tb);  // pair tb complete
           }
-          if (cs == kChunkStages - 1 || s == nst - 1) ++gc;
+          const uint32_t b = g % kStages;
+          failed = failed || !mbar_wait(full0 + 8u * b, (g / kStages) & 1u, status);
+        }
+        if (cs == 0) {
+          if (tb == 0) used0 = true; else used1 = true;
+        }
+        if (cs == kChunkStages - 1 || s == nst - 1) ++gc;
+        if (s % kGateTiles == kGateTiles - 1 || s == nst - 1) {
           __syncwarp();
+          mma_gate_sync(failed);
         }
       }
-      // after a failure: the MMAs already issued complete before the tensor
-      // memory is released
-      if (lane == 0 && failed) {
-        mma_commit(done0);
-        mbar_wait_own(done0, 0);
-      }
-      __syncwarp();
     }
+    // every accumulator pair in use drained
+    if (lane == 0 && !failed) {
+      if (used0) mbar_wait(acce0, ph_acce0, status);
+      if (used1) mbar_wait(acce0 + 8u, ph_acce1, status);
+    }
+    __syncwarp();
+  } else if (warp == kMmaWarp) {
+    // ------------------------------------------------ tensor-core issue (lane 0)
+    uint32_t g = 0;   // tiles consumed by this CTA
+    uint32_t gc = 0;  // accumulator lifetimes started
+    bool failed = false;
+    // group: the next item's tile count is loaded one item ahead
+    int nst_next = kGroup && L.begin + (int)blockIdx.x < n_items ? (grp.items[L.begin + blockIdx.x].w & 0xFFFF) : 0;
+    for (int item = L.begin + blockIdx.x; item < n_items; item += gridDim.x) {
+      int nst;
+      if (kGroup) {
+        nst = nst_next;
+        if (item + (int)gridDim.x < n_items) nst_next = grp.items[item + gridDim.x].w & 0xFFFF;
+      } else {
+        nst = oz_decode(oz, item).nst;
+      }
+      for (int s = 0; s < nst; ++s, ++g) {
+        const int cs = s % kChunkStages;
+        const uint32_t tb = gc & 1u;
+        // stages full, accumulator pair free (or the gate warp gave up)
+        if (s % kGateTiles == 0) failed = mma_gate_sync(false) || failed;
+        if (lane == 0 && !failed) {
+          tc_fence_after();
+          const uint32_t b = g % kStages;
+          const uint32_t a_addr = sbase + b * kStageBytes;
+          const uint32_t b_addr = a_addr + kOperandBytes;
+          const uint32_t d_big = tmem + tb * 256u, d_small = d_big + 128u;
+#pragma unroll
+          for (int kk = 0; kk < kOzKTile / 16; ++kk) {
+            const uint64_t a1 = sw64_desc(a_addr + kk * 32);
+            const uint64_t a2 = sw64_desc(a_addr + kSliceBytes + kk * 32);
+            const uint64_t a3 = sw64_desc(a_addr + 2 * kSliceBytes + kk * 32);
+            const uint64_t b1 = sw64_desc(b_addr + kk * 32);
+            const uint64_t b2 = sw64_desc(b_addr + kSliceBytes + kk * 32);
+            const uint64_t b3 = sw64_desc(b_addr + 2 * kSliceBytes + kk * 32);
+            const uint32_t acc = (cs > 0 || kk > 0) ? 1u : 0u;
+            mma_f16(d_big, a1, b1, kIdesc, acc);
+            mma_f16(d_small, a1, b2, kIdesc, acc);
+            mma_f16(d_small, a2, b1, kIdesc, 1u);
+            mma_f16(d_small, a1, b3, kIdesc, 1u);
+            mma_f16(d_small, a2, b2, kIdesc, 1u);
+            mma_f16(d_small, a3, b1, kIdesc, 1u);
+          }
+          mma_commit(empty0 + 8u * b);  // stage b free once these MMAs complete
+          if (cs == kChunkStages - 1 || s == nst - 1) mma_commit(accf0 + 8u * tb);  // pair tb complete
+        }
+        if (cs == kChunkStages - 1 || s == nst - 1) ++gc;
+        __syncwarp();
+      }
+    }
+    // after a failure: the MMAs already issued complete before the tensor
+    // memory is released
+    if (lane == 0 && failed) {
+      mma_commit(done0);
+      mbar_wait_own(done0, 0);
+    }
+    __syncwarp();
   } else {
     // ------------------------------------------------ drain + epilogue (warps 0-3)
-    if constexpr (Side::kWarps > 0) reg_alloc<kDrainRegs>();
     uint32_t ph_accf0 = 0, ph_accf1 = 0;
     uint32_t gc = 0;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);

@@ -310,6 +310,10 @@ def test_production_stress_mixed_within_bar(sigma_lib):
 TENSOR_CASES = [c for c in RANDOM_CASES if c[3] >= 20] + [
     (50, 2, 2080, 128, 31, False),      # 3 x 128 contraction rows: no padding rows to zero
     (24, 0, 1000, 128, 32, True),       # the same with a ragged last K tile and no occupied band
+    # more columns and g-vectors: several factor items per column block and
+    # several contraction K splits
+    (40, 3, 8192, 300, 33, False),
+    (37, 2, 8000, 300, 34, True),       # ragged last K tile, stress fill
 ]
 
 
