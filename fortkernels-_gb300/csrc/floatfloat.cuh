@@ -101,6 +101,46 @@ __device__ __forceinline__ bool ff_gt_fast(FF x, FF y, bool& near) {
   return clear ? d > 0.f : full > 0.f;
 }
 
+// x - y as an unnormalised pair (TwoSum of the hi parts plus the lo
+// parts): exact to ~2^-46 of the operands, for a product or square next.
+__device__ __forceinline__ FF ff_sub_raw(FF x, FF y) {
+  float s, e;
+  two_sum_f(x.hi, -y.hi, s, e);
+  return FF{s, e + (x.lo - y.lo)};
+}
+// c^2 + b2 (b2 normalised), normalised: the square's exact error by FMA.
+__device__ __forceinline__ FF ff_sq_add(FF c, FF b2) {
+  const float p = c.hi * c.hi;
+  const float e = fmaf(2.f * c.hi, c.lo, fmaf(c.hi, c.hi, -p));
+  float s, t;
+  two_sum_f(p, b2.hi, s, t);
+  return ff_norm(s, t + (e + b2.lo));
+}
+// Unnormalised float-float results (hi, lo) for operands that feed only
+// further products, TwoSums or one final rounding: the pair's value is the
+// same as the normalised one's, its lo may exceed half an ulp of hi.
+// x y: the exact product of the hi parts (FMA) plus the cross terms.
+__device__ __forceinline__ FF ff_mul_raw(FF x, FF y) {
+  const float p = x.hi * y.hi;
+  return FF{p, fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)))};
+}
+// a g - b h: the hi products' difference by TwoSum, their exact errors and
+// the cross terms in lo (lo * lo terms dropped, ~2^-46 of the products).
+__device__ __forceinline__ FF ff_dot2_raw(FF a, FF g, FF b, FF h) {
+  const float p1 = a.hi * g.hi, p2 = b.hi * h.hi;
+  const float e1 = fmaf(a.hi, g.hi, -p1), e2 = fmaf(b.hi, h.hi, -p2);
+  const float t = fmaf(a.hi, g.lo, fmaf(a.lo, g.hi, e1)) - fmaf(b.hi, h.lo, fmaf(b.lo, h.hi, e2));
+  float s, es;
+  two_sum_f(p1, -p2, s, es);
+  return FF{s, es + t};
+}
+// 1 / x for x > 0 (x normalised): FP32 reciprocal and one float-float
+// correction, unnormalised.
+__device__ __forceinline__ FF ff_rcp_raw(FF x) {
+  const float r0 = rcp_f32(x.hi);
+  return FF{r0, r0 * (fmaf(-x.hi, r0, 1.0f) - x.lo * r0)};
+}
+
 // The pole-guard decisions of the FP64 path (guard_w / guard_thr /
 // guard_thr2), for the float-float kernels' rare values near a threshold.
 // Out of line so that those kernels branch to them instead of running their

@@ -21,6 +21,7 @@
 // g-vector) threshold on the integer pipe and a select of r (exact poles give
 // r = inf and are dropped by the select, never multiplied).
 #include "sigma_internal.cuh"
+#include "floatfloat.cuh"
 #include "gpp_batch.cuh"
 
 namespace sigma {
@@ -475,21 +476,44 @@ __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchVi
 //                              (= -Omega2 conj(cden) delw / |cden|^2, cden = 4 wtilde^2 (delw + 1/2))
 //   otherwise (incl. exact poles, where the reference's delw is NaN): 0
 // and asxtemp[iw] += occ vcoul[igp] conj(aqsm[n1][igp]) sum_ig aqsn[n1][ig] ssx.
+// The factors are formed in float-float arithmetic (FP32 pairs, ~2^-44
+// relative, from exact splits of the FP64 inputs) on the FP32 pipe, then
+// widened to FP64 once: GB300's FP64 pipe, at 1/64 of the FP32 rate, keeps
+// the guard decisions (the FP64 path's own expressions), the widening and
+// the band sums.  Both branches are formed for every term (about a fifth of
+// the terms take the second one, so a warp almost always needs both).
 constexpr int kSsxCK = 8;      // g-vectors per staged chunk
 
 struct SsxSmem {
   double a[kSsxCK][kSsxBP];
   double b[kSsxCK][kSsxBP];
-  double2 g[kSsxCK][kSsxBP];
-  double2 om[kSsxCK][kSsxBP];
+  double2 ie[kSsxCK][kSsxBP];
   double2 n[kSsxCK][kSsxBN];
+  double ns[kSsxCK][kSsxBN];  // n.x + n.y
 };
 static_assert(sizeof(SsxSmem) <= 200 * 1024, "shared memory budget");
 
 struct SsxShared {
   double2 red[kSsxBN][kNW][kThreads / 32];
-  double wx[kSsxBN][kNW], iwx2[kSsxBN][kNW];
+  double wx[kSsxBN][kNW];
+  float wxf[kSsxBN][kNW][2], iwx2f[kSsxBN][kNW][2];  // wx and 1 / wx^2 as float-float
 };
+
+// One term's ssx factor from the element's float-float values (a + i b =
+// wtilde, G = I_eps wtilde, Omega2 = wtilde G): Omega2 / wx^2 when kept,
+// -G conj(z) / (2 |z|^2) with z = wtilde + wx in the second branch, else 0;
+// widened to FP64 once.
+__device__ __forceinline__ double2 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy, FF omx, FF omy, FF wx,
+                                                 FF iwx2, bool keep, bool second) {
+  const FF k1x = ff_mul_raw(omx, iwx2), k1y = ff_mul_raw(omy, iwx2);
+  const FF zr = ff_add(a, wx);
+  const FF r = ff_rcp_raw(ff_sq_add(zr, b2));
+  const FF tx = ff_dot2_raw(gx, zr, gy, ff_neg(b)), ty = ff_dot2_raw(gy, zr, gx, b);  // G conj(z)
+  const FF k2x = ff_mul_raw(tx, r), k2y = ff_mul_raw(ty, r);
+  const FF sx = keep ? k1x : (second ? FF{-0.5f * k2x.hi, -0.5f * k2x.lo} : FF{0.f, 0.f});
+  const FF sy = keep ? k1y : (second ? FF{-0.5f * k2y.hi, -0.5f * k2y.lo} : FF{0.f, 0.f});
+  return make_double2((double)sx.hi + (double)sx.lo, (double)sy.hi + (double)sy.lo);
+}
 
 __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w, int item,
                                               unsigned char* smem_raw, SsxShared& sh, int tid) {
@@ -505,14 +529,21 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
     const int i = tid / kNW, iw = tid % kNW;
     const double wx = i < nbl ? p.wx[(size_t)(n1_0 + i) * p.wx_stride + iw] : 1.0;
     sh.wx[i][iw] = wx;
-    sh.iwx2[i][iw] = rcp_f64(wx * wx);
+    const FF f = ff_of(wx), g = ff_of(rcp_f64(wx * wx));
+    sh.wxf[i][iw][0] = f.hi;
+    sh.wxf[i][iw][1] = f.lo;
+    sh.iwx2f[i][iw][0] = g.hi;
+    sh.iwx2f[i][iw][1] = g.lo;
   }
 
-  double2 acc[kSsxBN][kNW];
+  // each complex multiply-add as three real products (as in the main pass):
+  // P1 = sum n.x s.x, P2 = sum n.y s.y, P3 = sum (n.x + n.y)(s.x + s.y),
+  // sum n s = (P1 - P2) + i (P3 - P1 - P2)
+  double p1[kSsxBN][kNW], p2[kSsxBN][kNW], p3[kSsxBN][kNW];
 #pragma unroll
   for (int i = 0; i < kSsxBN; ++i)
 #pragma unroll
-    for (int iw = 0; iw < kNW; ++iw) acc[i][iw] = make_double2(0.0, 0.0);
+    for (int iw = 0; iw < kNW; ++iw) p1[i][iw] = p2[i][iw] = p3[i][iw] = 0.0;
 
   for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kSsxCK) {
     __syncthreads();
@@ -527,8 +558,7 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       }
       sm.a[k][pl] = wt.x;
       sm.b[k][pl] = wt.y;
-      sm.g[k][pl] = cmul(ie, wt);
-      sm.om[k][pl] = cmul(cmul(wt, wt), ie);
+      sm.ie[k][pl] = ie;
     }
     for (int e = tid; e < kSsxCK * kSsxBN; e += kThreads) {
       const int k = e % kSsxCK, bl = e / kSsxCK;
@@ -536,58 +566,58 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
       sm.n[k][bl] = v;
+      sm.ns[k][bl] = __dadd_rn(v.x, v.y);
     }
     __syncthreads();
 
     for (int k = 0; k < kSsxCK; ++k) {
       const double a = sm.a[k][tid], b = sm.b[k][tid];
-      const double2 g = sm.g[k][tid], om = sm.om[k][tid];
+      const double2 ie = sm.ie[k][tid];
       const double b2 = guard_b2(b);
       const double thr = guard_thr(a, b2), thr2 = guard_thr2(a, b2);
+      const FF fa = ff_of(a), fb = ff_of(b), er = ff_of(ie.x), ei = ff_of(ie.y);
+      const FF gx = ff_dot2_raw(er, fa, ei, fb), gy = ff_dot2_raw(er, fb, ff_neg(ei), fa);  // G
+      const FF omx = ff_dot2_raw(fa, gx, fb, gy), omy = ff_dot2_raw(fa, gy, ff_neg(fb), gx);  // Omega2
+      const FF fb2 = ff_mul_raw(fb, fb);
       // ssx factor of band i and frequency iw (band-independent when the
-      // frequencies are shared)
+      // frequencies are shared); decisions from the FP64 expressions
       auto factor = [&](int i, int iw) {
-        const double wx = sh.wx[i][iw];
-        const double wv = guard_w(wx, a, b2);
+        const double wv = guard_w(sh.wx[i][iw], a, b2);
         const bool keep = keep_nonneg(wv, thr);
-        const bool br2 = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
-        // branch 1: Omega2 / wx^2
-        const double iwx2 = sh.iwx2[i][iw];
-        const double2 s1 = make_double2(om.x * iwx2, om.y * iwx2);
-        // branch 2: -G conj(z) / (2 |z|^2), z = wtilde + wx
-        const double zr = a + wx;
-        const double q = -0.5 * rcp_f64(fma(zr, zr, b2));
-        const double2 s2 = make_double2(fma(g.x, zr, g.y * b) * q, fma(g.y, zr, -g.x * b) * q);
-        return keep ? s1 : (br2 ? s2 : make_double2(0.0, 0.0));
+        const bool second = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
+        return ssx_factor_ff(fa, fb, fb2, gx, gy, omx, omy, FF{sh.wxf[i][iw][0], sh.wxf[i][iw][1]},
+                             FF{sh.iwx2f[i][iw][0], sh.iwx2f[i][iw][1]}, keep, second);
+      };
+      auto mac = [&](int i, int iw, double2 s, double s_sum) {
+        const double2 an = sm.n[k][i];
+        p1[i][iw] = fma(an.x, s.x, p1[i][iw]);
+        p2[i][iw] = fma(an.y, s.y, p2[i][iw]);
+        p3[i][iw] = fma(sm.ns[k][i], s_sum, p3[i][iw]);
       };
       if (p.wx_stride == 0) {
         double2 sv[kNW];
+        double ss[kNW];
 #pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) sv[iw] = factor(0, iw);
-#pragma unroll
-        for (int i = 0; i < kSsxBN; ++i) {
-          if (i < nbl) {
-            const double2 an = sm.n[k][i];
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) {
-              acc[i][iw].x = fma(an.x, sv[iw].x, fma(-an.y, sv[iw].y, acc[i][iw].x));
-              acc[i][iw].y = fma(an.x, sv[iw].y, fma(an.y, sv[iw].x, acc[i][iw].y));
-            }
-          }
+        for (int iw = 0; iw < kNW; ++iw) {
+          sv[iw] = factor(0, iw);
+          ss[iw] = __dadd_rn(sv[iw].x, sv[iw].y);
         }
+#pragma unroll
+        for (int i = 0; i < kSsxBN; ++i)
+          if (i < nbl) {
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) mac(i, iw, sv[iw], ss[iw]);
+          }
       } else {
 #pragma unroll
-        for (int i = 0; i < kSsxBN; ++i) {
+        for (int i = 0; i < kSsxBN; ++i)
           if (i < nbl) {
-            const double2 an = sm.n[k][i];
 #pragma unroll
             for (int iw = 0; iw < kNW; ++iw) {
               const double2 s = factor(i, iw);
-              acc[i][iw].x = fma(an.x, s.x, fma(-an.y, s.y, acc[i][iw].x));
-              acc[i][iw].y = fma(an.x, s.y, fma(an.y, s.x, acc[i][iw].y));
+              mac(i, iw, s, __dadd_rn(s.x, s.y));
             }
           }
-        }
       }
     }
   }
@@ -604,7 +634,9 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       if (i < nbl && igp >= 0) {
         const double2 am = p.aqsm[(size_t)(n1_0 + i) * p.nc + igp];
         const double f = p.occ * p.vcoul[igp];
-        v = cmul(acc[i][iw], make_double2(am.x, -am.y));
+        const double2 acc = make_double2(__dsub_rn(p1[i][iw], p2[i][iw]),
+                                         __dsub_rn(__dsub_rn(p3[i][iw], p1[i][iw]), p2[i][iw]));
+        v = cmul(acc, make_double2(am.x, -am.y));
         v.x *= f;
         v.y *= f;
       }
