@@ -639,7 +639,8 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
            "tiles": {"table": autotune.load_table() is not None,
                      "counts": {autotune.TILES[t] if t >= 0 else "library": tiles.count(t)
                                 for t in sorted(set(tiles))},
-                     "items_per_cta": {f: autotune.sizing_for(f) for f in ("fp64", "mixed", "tensor")}}}
+                     "items_per_cta": {f: autotune.sizing_for(f) for f in ("fp64", "mixed")},
+                     "tensor_split_tiles": autotune.sizing_for("tensor")}}
     outs = {}
     gs = torch.cuda.Stream()  # graphs are captured on a non-default stream
     gptr = gs.cuda_stream
@@ -650,7 +651,7 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     for prec, name, steps in forms:
         b = S.GppBatch(dicts, precision=prec, tiles=tiles if prec == S.PREC_FP64 else None,
                        items_per_cta=autotune.sizing_for(name) if name != "tensor" else 0,
-                       tensor_items_per_cta=autotune.sizing_for("tensor") if name == "tensor" else 0)
+                       tensor_split_tiles=autotune.sizing_for("tensor") if name == "tensor" else 0)
         terms, items, launches = b.info()
         b.launch_graph(gptr)  # capture, and the warm-up replay
         ms = timed(torch, dist, world, lambda: b.launch_graph(gptr), steps, gs)

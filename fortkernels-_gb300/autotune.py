@@ -22,8 +22,9 @@ table; without it the library picks the least-padded tile itself.
 Sizing.  The g-vector split of every form's work items is set by how many
 items each resident CTA takes (sigma_gpp_batch_create_tuned): the FP64 and
 mixed main passes' items per CTA (band block x column block x g-vector
-split), and the tensor form's contraction items per CTA (the K split of
-each instance's 128-row x 64-band blocks).  The tuner times each candidate
+split), and the tensor form's contraction item length (the K split of every
+instance's 128-row x 64-band blocks; 0 sizes each instance as its single
+plan).  The tuner times each candidate
 on the 48-instance set through graph replays and keeps the fastest; a
 tensor candidate is kept only if every achtemp / asxtemp of the set stays
 within 1e-6 of the FP64 form's (the tensor form's error depends on where
@@ -74,21 +75,22 @@ def tile_for(number_bands: int, ngpown: int, table=None, shared=True) -> int:
 
 
 SIZING_INSTANCES = 48
-SIZING_CANDIDATES = {"fp64": (8, 16, 32), "mixed": (8, 16, 32), "tensor": (10, 20, 40)}
-SIZING_KEY = {"fp64": "fp64_items_per_cta", "mixed": "mixed_items_per_cta", "tensor": "tensor_items_per_cta"}
+SIZING_CANDIDATES = {"fp64": (8, 16, 32), "mixed": (8, 16, 32), "tensor": (0, 32, 64, 128)}
+SIZING_KEY = {"fp64": "fp64_items_per_cta", "mixed": "mixed_items_per_cta", "tensor": "tensor_split_tiles"}
 
 
 def sizing_for(form: str, table=None) -> int:
-    """Tuned items per CTA of a batched form ("fp64", "mixed", "tensor"); 0
-    selects the library's default."""
+    """Tuned sizing of a batched form: items per CTA ("fp64", "mixed") or
+    the contraction items' K tiles ("tensor"); 0 selects the library's
+    default."""
     t = table if table is not None else load_table()
     if not t:
         return 0
     return int(t.get(SIZING_KEY[form], 0))
 
 
-def _time_batch(S, torch, dicts, prec, stream, reps, tiles=None, ipc=0, tipc=0):
-    b = S.GppBatch(dicts, precision=prec, tiles=tiles, items_per_cta=ipc, tensor_items_per_cta=tipc)
+def _time_batch(S, torch, dicts, prec, stream, reps, tiles=None, ipc=0, tsplit=0):
+    b = S.GppBatch(dicts, precision=prec, tiles=tiles, items_per_cta=ipc, tensor_split_tiles=tsplit)
     b.launch_graph(stream.cuda_stream)  # capture + warm-up
     b.launch_graph(stream.cuda_stream)
     stream.synchronize()
@@ -125,7 +127,7 @@ def tune_sizing(classes, reps=3, log=print):
     for form, prec in (("fp64", S.PREC_FP64), ("mixed", S.PREC_MIXED), ("tensor", S.PREC_TENSOR)):
         ms = {}
         for c in SIZING_CANDIDATES[form]:
-            kw = dict(tipc=c) if form == "tensor" else dict(ipc=c)
+            kw = dict(tsplit=c) if form == "tensor" else dict(ipc=c)
             ms[c] = _time_batch(S, torch, dicts, prec, stream, 1 if form == "fp64" else reps,
                                 tiles=tiles if form == "fp64" else None, **kw)
             outs = [x.outputs() for x in xs]

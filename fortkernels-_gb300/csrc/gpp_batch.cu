@@ -49,7 +49,7 @@ struct sigma_gpp_batch_s {
   std::vector<sigma_gpp_instance> inst;
   long long terms = 0;
   int sch_grid = 0, ssx_grid = 0, launches = 0;
-  int tensor_items_per_cta = 0;  // GEMM items per CTA of each contraction (0: the plans' default)
+  int tensor_split_tiles = 0;  // K' tiles per contraction item, every instance (0: each sized as its plan)
   bool all_shared_wx = true;  // every instance has one frequency set for all bands
   bool mixedy = false;        // mixed main pass on the shared-factor kernel
   void* block = nullptr;
@@ -141,13 +141,15 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
     set_last_cuda_error(e, "cudaMalloc(batch slice images)", __LINE__);
     return SIGMA_ERR_ALLOC;
   }
-  // each instance's GEMM items sized as its single-instance plan sizes them
-  // (about 20 per CTA of the instance's own contraction): the tensor form's
-  // errors depend on where the K splits fall (the drain warps' FP32 sums
-  // span an item's accumulator lifetimes), and this sizing keeps them at the
-  // single plans' level on the 48-instance set
+  // GEMM items of tensor_split_tiles K' tiles in every instance (one static
+  // schedule of equal items), or each instance's items sized as its
+  // single-instance plan sizes them (about 20 per CTA of its own
+  // contraction).  The tensor form's errors depend on where the K splits
+  // fall (the drain warps' FP32 sums span an item's accumulator lifetimes):
+  // the tuner keeps a split size only if the 48-instance set stays within
+  // 1e-6 of FP64.
   (void)tiles;
-  const int hint = 0, ipc = b->tensor_items_per_cta;
+  const int hint = b->tensor_split_tiles;
   b->ff.assign(n, nullptr);
   b->fac_nvband = 0;
   for (int i = 0; i < n; ++i) b->fac_nvband = std::max(b->fac_nvband, inst[i].nvband);
@@ -162,14 +164,14 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
   for (int i = 0; i < n; ++i) {
     const sigma_gpp_instance& q = inst[i];
     int st = ff_plan_build(&b->ff[i], q.number_bands, q.ncouls, q.ngpown, kNW, igp[i], SIGMA_FF_OZAKI_BF16,
-                           static_cast<char*>(b->tensor_ws) + toff[i], nullptr, hint, ipc);
+                           static_cast<char*>(b->tensor_ws) + toff[i], nullptr, hint);
     if (st != SIGMA_OK) return st;
     const OzakiPrep& oz = *ff_plan_ozaki(b->ff[i]);
     // the plan's work entries, for the group's item table (with a split
     // size given, they depend on the shape and the split size only)
     OzakiTables t;
     OzakiPrep again{};
-    ozaki_size(again, *ff_plan_dev(b->ff[i]), sms, nullptr, &t, hint, ipc);
+    ozaki_size(again, *ff_plan_dev(b->ff[i]), sms, nullptr, &t, hint);
     if (again.n_items != oz.n_items || again.n_entries != oz.n_entries) return SIGMA_ERR_UNSUPPORTED;
     ozaki_group_items(i, oz, t, items);
 
@@ -275,11 +277,11 @@ extern "C" int sigma_gpp_batch_create(sigma_gpp_batch* out, int n_instances,
 extern "C" int sigma_gpp_batch_create_tuned(sigma_gpp_batch* out, int n_instances,
                                             const sigma_gpp_instance* inst, int precision,
                                             const int* tile_shape, int items_per_cta,
-                                            int tensor_items_per_cta) {
+                                            int tensor_split_tiles) {
   using namespace sigma;
   if (!out || !inst) return SIGMA_ERR_NULL;
   *out = nullptr;
-  if (n_instances <= 0 || items_per_cta < 0 || tensor_items_per_cta < 0) return SIGMA_ERR_INVALID_SHAPE;
+  if (n_instances <= 0 || items_per_cta < 0 || tensor_split_tiles < 0) return SIGMA_ERR_INVALID_SHAPE;
   if (precision != SIGMA_PREC_FP64 && precision != SIGMA_PREC_MIXED && precision != SIGMA_PREC_TENSOR)
     return SIGMA_ERR_UNSUPPORTED;
   const bool tensor = precision == SIGMA_PREC_TENSOR;
@@ -322,7 +324,7 @@ extern "C" int sigma_gpp_batch_create_tuned(sigma_gpp_batch* out, int n_instance
   auto* b = new sigma_gpp_batch_s();
   b->device = dev;
   b->grouped = grouped;
-  b->tensor_items_per_cta = tensor_items_per_cta;
+  b->tensor_split_tiles = tensor_split_tiles;
   b->n = n_instances;
   b->precision = precision;
   b->terms = terms;

@@ -407,10 +407,10 @@ class GppBatch:
     device pointer.  `tiles` (optional) gives the FP64 main-pass tile per
     instance (-1 library choice; per-band frequencies 0 = 32x32, 1 = 16x64,
     2 = 64x16; one frequency set 3 = 64x32, 4 = 32x64, 5 = 32x32, 6 =
-    128x16).  `items_per_cta` / `tensor_items_per_cta` (0: defaults) size the
+    128x16).  `items_per_cta` / `tensor_split_tiles` (0: defaults) size the
     work items (sigma_gpp_batch_create_tuned)."""
 
-    def __init__(self, instances, precision=PREC_FP64, tiles=None, items_per_cta=0, tensor_items_per_cta=0):
+    def __init__(self, instances, precision=PREC_FP64, tiles=None, items_per_cta=0, tensor_split_tiles=0):
         self.lib = load()
         self._keep = []
         arr = _instance_array(instances, self._keep)
@@ -422,7 +422,7 @@ class GppBatch:
         h = C.c_void_p()
         st = self.lib.sigma_gpp_batch_create_tuned(C.byref(h), len(instances), C.addressof(arr), precision,
                                                    None if t is None else _ptr(t), int(items_per_cta),
-                                                   int(tensor_items_per_cta))
+                                                   int(tensor_split_tiles))
         _check(st, "sigma_gpp_batch_create_tuned")
         self.handle = h
 

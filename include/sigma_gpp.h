@@ -224,14 +224,16 @@ int sigma_gpp_batch_create(sigma_gpp_batch* batch, int n_instances, const sigma_
 /* sigma_gpp_batch_create with the work sizing given (0 for the default of
  * each): items_per_cta, the FP64 and mixed main pass's work items per
  * resident CTA (each item a band block x column block x g-vector split;
- * default 16), and tensor_items_per_cta, the tensor form's contraction
- * items per CTA of each instance (default 20).  Results do not depend on
- * items_per_cta beyond the order of the g-vector sums; the tensor form's
- * error depends on tensor_items_per_cta through where its K splits fall.
- * fortkernels-_gb300/autotune.py tunes both with the tile shapes. */
+ * default 16), and tensor_split_tiles, the tensor form's contraction items'
+ * length in K tiles of 32 g-vectors (real and imaginary halves counted
+ * apart), the same for every instance (default: each instance's items
+ * sized as its single-instance plan's, about 20 per CTA).  Results do not
+ * depend on items_per_cta beyond the order of the g-vector sums; the tensor
+ * form's error depends on tensor_split_tiles through where its K splits
+ * fall.  fortkernels-_gb300/autotune.py tunes both with the tile shapes. */
 int sigma_gpp_batch_create_tuned(sigma_gpp_batch* batch, int n_instances, const sigma_gpp_instance* inst,
                                  int precision, const int* tile_shape, int items_per_cta,
-                                 int tensor_items_per_cta);
+                                 int tensor_split_tiles);
 
 /* Launches the batch on `stream` (asynchronous; allocates nothing). */
 int sigma_gpp_batch_execute(sigma_gpp_batch batch, void* stream);
