@@ -968,9 +968,10 @@ def run_ours(args, rank, world, local_rank):
                    "rel_err_vs_fp64": tensor_err, "stress_rel_err_vs_fp64": tensor_stress_err,
                    "max_rel_err": max(max(tensor_err["achtemp"]), max(tensor_err["asxtemp"]),
                                       max(tensor_stress_err["achtemp"]), max(tensor_stress_err["asxtemp"])),
-                   "path": "frequency factors in float-float arithmetic on the FP32 pipe, rounded to FP32; "
-                           "band sum as split-BF16 tcgen05 GEMM (FF kernel); occupied bands as in the "
-                           "mixed form"},
+                   "path": "one factor pass: frequency factors in float-float arithmetic on the FP32 pipe, "
+                           "rounded to FP32 and written as the contraction's split-BF16 slices, with the "
+                           "occupied bands' sums, the B slices and the epilogue factors; band sum as "
+                           "split-BF16 tcgen05 GEMM"},
         "ff": ff,
         "ff_sigma": ffs,
         "batched": batch,
