@@ -495,14 +495,24 @@ static_assert(sizeof(SsxSmem) <= 200 * 1024, "shared memory budget");
 
 struct SsxShared {
   double2 red[kSsxBN][kNW][kThreads / 32];
-  double wx[kSsxBN][kNW];
+  double wx[kSsxBN][kNW], iwx2[kSsxBN][kNW];
   float wxf[kSsxBN][kNW][2], iwx2f[kSsxBN][kNW][2];  // wx and 1 / wx^2 as float-float
 };
+
+// An FP32 value as a double, on the integer pipe (exponent rebiased,
+// mantissa shifted): exact for normal values and zero; FP32 subnormals (below
+// 1.2e-38, far below any term that matters next to the outputs) give zero.
+// cvt.f64.f32 would take the FP64 pipe, GB300's scarcest.
+__device__ __forceinline__ double f32_widen(float f) {
+  const unsigned u = __float_as_uint(f), mag = u & 0x7FFFFFFFu;
+  const unsigned hi = (u & 0x80000000u) | (mag >= 0x00800000u ? (mag >> 3) + 0x38000000u : 0u);
+  return __hiloint2double((int)hi, mag >= 0x00800000u ? (int)(mag << 29) : 0);
+}
 
 // One term's ssx factor from the element's float-float values (a + i b =
 // wtilde, G = I_eps wtilde, Omega2 = wtilde G): Omega2 / wx^2 when kept,
 // -G conj(z) / (2 |z|^2) with z = wtilde + wx in the second branch, else 0;
-// widened to FP64 once.
+// widened to FP64 once (hi and lo widened exactly, one FP64 addition).
 __device__ __forceinline__ double2 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy, FF omx, FF omy, FF wx,
                                                  FF iwx2, bool keep, bool second) {
   const FF k1x = ff_mul_raw(omx, iwx2), k1y = ff_mul_raw(omy, iwx2);
@@ -512,7 +522,33 @@ __device__ __forceinline__ double2 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy
   const FF k2x = ff_mul_raw(tx, r), k2y = ff_mul_raw(ty, r);
   const FF sx = keep ? k1x : (second ? FF{-0.5f * k2x.hi, -0.5f * k2x.lo} : FF{0.f, 0.f});
   const FF sy = keep ? k1y : (second ? FF{-0.5f * k2y.hi, -0.5f * k2y.lo} : FF{0.f, 0.f});
-  return make_double2((double)sx.hi + (double)sx.lo, (double)sy.hi + (double)sy.lo);
+  return make_double2(f32_widen(sx.hi) + f32_widen(sx.lo), f32_widen(sy.hi) + f32_widen(sy.lo));
+}
+
+// The same factor in FP64, for elements whose inputs leave the float-float
+// range: wtilde or I_eps nonzero with its larger component outside
+// [2^-20, 2^20), or an item frequency |wx| outside [2^-20, 2^20).  Inside it
+// every float-float intermediate (up to wtilde^2 I_eps / wx^2, within
+// 2^+-103) keeps both FP32 halves normal; outside it FP32 could overflow or
+// lose the low half.  Out of line, taken only by warps that hold such an
+// element.
+static __device__ __noinline__ double2 ssx_factor_fp64(double a, double b, double b2, double2 ie, double wx,
+                                                       double iwx2, bool keep, bool second) {
+  const double2 wt = make_double2(a, b);
+  const double2 g = cmul(ie, wt), om = cmul(wt, g);
+  if (keep) return make_double2(om.x * iwx2, om.y * iwx2);
+  if (!second) return make_double2(0.0, 0.0);
+  const double zr = a + wx;
+  const double q = -0.5 * rcp_f64(fma(zr, zr, b2));
+  return make_double2(fma(g.x, zr, g.y * b) * q, fma(g.y, zr, -g.x * b) * q);
+}
+// biased exponent of a double, on the integer pipe
+__device__ __forceinline__ int f64_exp(double x) { return (__double2hiint(x) >> 20) & 0x7FF; }
+// x + i y inside the float-float range: zero (or an FP64 subnormal, which the
+// split flushes), or its larger component in [2^-20, 2^20)
+__device__ __forceinline__ bool ff_range(double x, double y) {
+  const int e = max(f64_exp(x), f64_exp(y));
+  return e == 0 || (unsigned)(e - (1023 - 20)) < 40u;
 }
 
 __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w, int item,
@@ -525,16 +561,20 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
   const int p0 = ic.cb * kSsxBP;
   const int ig_begin = ic.s * w.split_len;
   const int ig_end = min(ig_begin + w.split_len, p.nc);
+  bool wx_out = false;
   if (tid < kSsxBN * kNW) {
     const int i = tid / kNW, iw = tid % kNW;
     const double wx = i < nbl ? p.wx[(size_t)(n1_0 + i) * p.wx_stride + iw] : 1.0;
+    wx_out = (unsigned)(f64_exp(wx) - (1023 - 20)) >= 40u;
     sh.wx[i][iw] = wx;
-    const FF f = ff_of(wx), g = ff_of(rcp_f64(wx * wx));
+    sh.iwx2[i][iw] = rcp_f64(wx * wx);
+    const FF f = ff_of(wx), g = ff_of(sh.iwx2[i][iw]);
     sh.wxf[i][iw][0] = f.hi;
     sh.wxf[i][iw][1] = f.lo;
     sh.iwx2f[i][iw][0] = g.hi;
     sh.iwx2f[i][iw][1] = g.lo;
   }
+  const bool item_wide = __syncthreads_or(wx_out);
 
   // each complex multiply-add as three real products (as in the main pass):
   // P1 = sum n.x s.x, P2 = sum n.y s.y, P3 = sum (n.x + n.y)(s.x + s.y),
@@ -581,12 +621,16 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       const FF fb2 = ff_mul_raw(fb, fb);
       // ssx factor of band i and frequency iw (band-independent when the
       // frequencies are shared); decisions from the FP64 expressions
+      const bool wide = item_wide || !(ff_range(a, b) && ff_range(ie.x, ie.y));
+      const bool any_wide = __any_sync(0xffffffffu, wide);
       auto factor = [&](int i, int iw) {
         const double wv = guard_w(sh.wx[i][iw], a, b2);
         const bool keep = keep_nonneg(wv, thr);
         const bool second = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
-        return ssx_factor_ff(fa, fb, fb2, gx, gy, omx, omy, FF{sh.wxf[i][iw][0], sh.wxf[i][iw][1]},
-                             FF{sh.iwx2f[i][iw][0], sh.iwx2f[i][iw][1]}, keep, second);
+        double2 s = ssx_factor_ff(fa, fb, fb2, gx, gy, omx, omy, FF{sh.wxf[i][iw][0], sh.wxf[i][iw][1]},
+                                  FF{sh.iwx2f[i][iw][0], sh.iwx2f[i][iw][1]}, keep, second);
+        if (any_wide && wide) s = ssx_factor_fp64(a, b, b2, ie, sh.wx[i][iw], sh.iwx2[i][iw], keep, second);
+        return s;
       };
       auto mac = [&](int i, int iw, double2 s, double s_sum) {
         const double2 an = sm.n[k][i];

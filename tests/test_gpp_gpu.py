@@ -127,6 +127,34 @@ def test_exact_poles_and_skipped_columns(sigma_lib, prec):
     _check(g, o, prec)
 
 
+@pytest.mark.parametrize("kind", ["huge-elements", "tiny-ieps", "tiny-frequency"])
+def test_fp64_occupied_bands_outside_float_range(sigma_lib, kind):
+    """The FP64 occupied-band pass forms its factors in float-float (FP32
+    pairs) when wtilde, I_eps and the frequency lie within 2^+-20; other
+    elements take its FP64 fallback.  Elements with |wtilde| ~ 2^45 and
+    |I_eps| ~ 2^40 (FP32 would overflow), an I_eps scaled by 2^-110 (the low
+    FP32 halves would fall below the normal range) and a frequency of 1e-7
+    must all stay within the FP64 bar of 1e-12."""
+    prob = W.gpp_random(24, 5, 1200, 40, 31)
+    prob.wtilde_array = prob.wtilde_array.copy()
+    prob.I_eps_array = prob.I_eps_array.copy()
+    if kind == "huge-elements":
+        prob.wtilde_array[3, 17] *= 2.0 ** 45
+        prob.wtilde_array[11, 400:404] *= 2.0 ** 30
+        prob.I_eps_array[7, 5] *= 2.0 ** 40
+        prob.I_eps_array[3, 17] *= 2.0 ** 21
+    elif kind == "tiny-ieps":
+        prob.I_eps_array *= 2.0 ** -110
+    else:
+        prob.wx_array = np.array([prob.wx_array[0], 1e-7, prob.wx_array[2]])
+    o = O.gpp(prob)
+    g = sigma_lib.gpp_host(prob, 0)
+    for x in g:
+        assert np.all(np.isfinite(x))
+    assert np.any(o[1] != 0)
+    _check(g, o, 0)
+
+
 def test_invalid_indices_are_errors(sigma_lib):
     prob = W.gpp_random(4, 1, 256, 8, 22)
     prob.inv_igp_index = prob.inv_igp_index.copy()
