@@ -16,7 +16,7 @@ device.  One step = one full evaluation of achtemp / asxtemp / acht_n1_loc.
              the relative error of every achtemp / asxtemp output against the
              FP64 path (and on the stress fill with 5% near-pole wtilde)
   roofline   the main FP64 kernel (sch_fp64y_kernel): the FP64 pipe work its
-             algorithm issues per term (3.13 operations: three real products
+             algorithm issues per term (3.06 operations: three real products
              per complex multiply-add plus the shared frequency factor) over
              its CUDA-event time, against the FP64 pipe peak (2 DFMA / clk / SM
              at the SM clock sampled during the timed region); the reference's
@@ -300,10 +300,12 @@ def timed(torch, dist, world, fn, steps, stream):
 
 # FP64 pipe operations of sch_fp64y_kernel per term, counted from its
 # algorithm: 3 DFMA (three-product complex multiply-add) + the shared
-# frequency factor and staged sums (~41 FP64 operations per column and
-# g-vector over 128 bands x 3 frequencies = 384 terms) + one band sum per
-# band and g-vector (over 16 columns x 3 frequencies = 48 terms).
-FP64_PIPE_OPS_PER_TERM = 3.0 + 41.0 / 384 + 1.0 / 48
+# frequency factor and staged sums (per column and g-vector: G and the three
+# c = wx - Re wtilde in FP64, 7; widening the three float-float factors and
+# their component sums, 9; over 128 bands x 3 frequencies = 384 terms) + one
+# band sum per band and g-vector (over 16 columns x 3 frequencies = 48
+# terms).
+FP64_PIPE_OPS_PER_TERM = 3.0 + 16.0 / 384 + 1.0 / 48
 # ncu, sch_fp64y_kernel, 128-band capture of the production instance
 # (--set full): dram__bytes_read.sum + dram__bytes_write.sum per term, and
 # sm__pipe_fp64_cycles_active over elapsed cycles.  Traffic scales with the

@@ -141,6 +141,34 @@ __device__ __forceinline__ FF ff_rcp_raw(FF x) {
   return FF{r0, r0 * (fmaf(-x.hi, r0, 1.0f) - x.lo * r0)};
 }
 
+// An FP32 value as a double, on the integer pipe (exponent rebiased,
+// mantissa shifted): exact for normal values and zero; FP32 subnormals (below
+// 1.2e-38) give zero.  cvt.f64.f32 would take the FP64 pipe, GB300's
+// scarcest.
+__device__ __forceinline__ double f32_widen(float f) {
+  const unsigned u = __float_as_uint(f), mag = u & 0x7FFFFFFFu;
+  const unsigned hi = (u & 0x80000000u) | (mag >= 0x00800000u ? (mag >> 3) + 0x38000000u : 0u);
+  return __hiloint2double((int)hi, mag >= 0x00800000u ? (int)(mag << 29) : 0);
+}
+// A float-float value as the nearest double: both halves widened exactly,
+// one FP64 addition.
+__device__ __forceinline__ double ff_widen(FF x) { return f32_widen(x.hi) + f32_widen(x.lo); }
+
+// The range in which the FP64 forms take float-float factors: a complex
+// input that is zero (or an FP64 subnormal, which the split flushes) or has
+// its larger component in [2^-20, 2^20), and a frequency with |wx| in
+// [2^-20, 2^20).  Inside it every float-float intermediate of a factor
+// keeps both FP32 halves normal and finite; elements outside it take the
+// FP64 expressions.  Biased exponents compared on the integer pipe.
+__device__ __forceinline__ int f64_exp(double x) { return (__double2hiint(x) >> 20) & 0x7FF; }
+__device__ __forceinline__ bool ff_range(double x, double y) {
+  const int e = max(f64_exp(x), f64_exp(y));
+  return e == 0 || (unsigned)(e - (1023 - 20)) < 40u;
+}
+__device__ __forceinline__ bool ff_freq_range(double wx) {
+  return (unsigned)(f64_exp(wx) - (1023 - 20)) < 40u;
+}
+
 // The pole-guard decisions of the FP64 path (guard_w / guard_thr /
 // guard_thr2), for the float-float kernels' rare values near a threshold.
 // Out of line so that those kernels branch to them instead of running their

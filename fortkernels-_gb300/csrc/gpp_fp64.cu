@@ -202,10 +202,19 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
 // frequency factor of a term,
 //   Y_iw = G (c + i b) r   (0 when the pole guard drops the term),
 // depends on the column and the g-vector only.  Each staged chunk forms Y
-// once for its columns (10 FP64 operations per column, g-vector and
-// frequency, shared by the item's BN bands), and every term is then one
-// complex multiply-add acc += aqsn * Y: 4 DFMA, against 10 FP64 operations
-// per term when the factor is rebuilt for every band.  The sum over
+// once for its columns, shared by the item's BN bands, and every term is
+// then one complex multiply-add acc += aqsn * Y: 4 DFMA, against 10 FP64
+// operations per term when the factor is rebuilt for every band.
+//
+// Y is formed in float-float arithmetic (FP32 pairs) from G = I_eps wtilde
+// and c = wx - Re wtilde taken in FP64 and split, and widened to FP64 once:
+// 3 FP64 operations per frequency instead of ~12 (the chunk's factor phase
+// is time in which the FP64 pipe does no band work).  Its error is about
+// twice the FP64 form's, whose reciprocal is itself an FP32 seed refined
+// once (within 2^-44.8).  The keep decisions are taken in float-float and re-taken with the
+// FP64 expressions, out of line, within 2^-30 of the threshold or where the
+// guard's second condition can bind (|wtilde|^2 >= 62000); elements outside
+// the float-float range take the FP64 factor.  The sum over
 // g-vectors is then a complex GEMM (bands x g-vectors times g-vectors x
 // (column, frequency)) on the FP64 pipe, 16 x 16 threads with a
 // (BN/16 bands x BP/16 columns x 3 frequencies) register tile each.
@@ -243,6 +252,36 @@ __device__ __forceinline__ bool wait_ready(const unsigned* flag, unsigned epoch,
   return false;
 }
 
+// The FP64 form of one element's three factors, for elements outside the
+// float-float range, out of line: Y of frequency iw and Y.x + Y.y are
+// stored at y[iw * stride] and ys[iw * stride].
+static __device__ __noinline__ void sch_factor_fp64(double2 wt, double2 ie, double wx0, double wx1, double wx2,
+                                                    double2* y, double* ys, int stride) {
+  const double2 g = cmul(ie, wt);
+  const double b = wt.y, b2 = guard_b2(b);
+  const double thr = guard_thr(wt.x, b2);
+  const double wx[kNW] = {wx0, wx1, wx2};
+  for (int iw = 0; iw < kNW; ++iw) {
+    const double c = __dsub_rn(wx[iw], wt.x);
+    const double wv = fma(c, c, b2);
+    const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
+    const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
+    const double2 v = make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
+    y[iw * stride] = v;
+    ys[iw * stride] = __dadd_rn(v.x, v.y);
+  }
+}
+
+// Keep decisions of the frequencies in `rare` (bits 0-2) re-taken with the
+// FP64 path's expressions; out of line.
+static __device__ __noinline__ unsigned sch_keep_rare(unsigned keep, unsigned rare, double wx0, double wx1,
+                                                      double wx2, double a, double b) {
+  const double wx[kNW] = {wx0, wx1, wx2};
+  for (int iw = 0; iw < kNW; ++iw)
+    if ((rare >> iw) & 1u) keep = (keep & ~(1u << iw)) | (keep_fp64(wx[iw], a, b) ? (1u << iw) : 0u);
+  return keep;
+}
+
 template <int BN, int BP>
 __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w, int item,
                                                unsigned char* smem_raw, int tid) {
@@ -264,6 +303,8 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const int ig_begin = ic.s * w.split_len;
   const int ig_end = min(ig_begin + w.split_len, p.nc);
   const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
+  const bool wx_wide = !(ff_freq_range(wx0) && ff_freq_range(wx1) && ff_freq_range(wx2));
+  const FF quarter{0.25f, 0.f};
 
   double p1[TB][TC][kNW], p2[TB][TC][kNW], p3[TB][TC][kNW];
 #pragma unroll
@@ -280,30 +321,51 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
     for (int e = tid; e < kCKY * BP; e += kThreads) {
       const int k = e % kCKY, pl = e / kCKY;
       const int ig = ig0 + k, my_igp = p0 + pl;
-      double2 y0 = make_double2(0.0, 0.0), y1 = y0, y2 = y0;
-      if (ig < ig_end && my_igp < p.ng) {
+      const bool valid = ig < ig_end && my_igp < p.ng;
+      double2 wt = make_double2(0.0, 0.0), ie = wt;
+      if (valid) {
         const size_t off = (size_t)my_igp * p.nc + ig;
-        const double2 wt = p.wt[off];
-        const double2 g = cmul(p.ieps[off], wt);
-        const double b = wt.y, b2 = guard_b2(b);
-        const double thr = guard_thr(wt.x, b2);
-        auto factor = [&](double wx) {
-          const double c = __dsub_rn(wx, wt.x);
-          const double wv = fma(c, c, b2);
-          const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
-          const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
-          return make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
-        };
-        y0 = factor(wx0);
-        y1 = factor(wx1);
-        y2 = factor(wx2);
+        wt = p.wt[off];
+        ie = p.ieps[off];
       }
-      sm.y[k][0][pl] = y0;
-      sm.y[k][1][pl] = y1;
-      sm.y[k][2][pl] = y2;
-      sm.ys[k][0][pl] = __dadd_rn(y0.x, y0.y);
-      sm.ys[k][1][pl] = __dadd_rn(y1.x, y1.y);
-      sm.ys[k][2][pl] = __dadd_rn(y2.x, y2.y);
+      // Y = G (c + i b) r, G = I_eps wtilde, c = wx - Re wtilde, b = Im wtilde;
+      // G and c in FP64 and split (4 + 3 FP64 operations): c = wx - a
+      // cancels near the poles, where a split of a's 2^-48 error would
+      // be amplified (~15 times the FP64 form's error in Y; with these
+      // two in FP64, ~1.8 times, from a float-float emulation of the
+      // element)
+      const double2 g = cmul(ie, wt);
+      const FF fb = ff_of(wt.y), gx = ff_of(g.x), gy = ff_of(g.y);
+      const FF b2 = ff_mul_raw(fb, fb);
+      // |wtilde|^2 * 4e-6 > 0.25 needs |wtilde|^2 > 62500
+      const float ah = ff_of(wt.x).hi;
+      const bool thr2_binds = fmaf(ah, ah, fb.hi * fb.hi) >= 62000.f;
+      double2 y[kNW];
+      unsigned keep = 0u, rare = 0u;
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        const FF c = ff_of(__dsub_rn(iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2), wt.x));
+        const FF wv = ff_sq_add(c, b2);  // |wdiff|^2
+        bool near;
+        keep |= ff_gt_fast(wv, quarter, near) ? (1u << iw) : 0u;
+        rare |= (near || thr2_binds) ? (1u << iw) : 0u;
+        const FF r = ff_rcp_raw(wv);
+        const FF ux = ff_dot2_raw(gx, c, gy, fb), uy = ff_dot2_raw(gx, fb, ff_neg(gy), c);
+        y[iw] = make_double2(ff_widen(ff_mul_raw(ux, r)), ff_widen(ff_mul_raw(uy, r)));
+      }
+      if (rare) keep = sch_keep_rare(keep, rare, wx0, wx1, wx2, wt.x, wt.y);
+      if (!valid) keep = 0u;
+      const bool wide = valid && (wx_wide || !(ff_range(wt.x, wt.y) && ff_range(ie.x, ie.y)));
+      if (__any_sync(0xffffffffu, wide) && wide) {
+        sch_factor_fp64(wt, ie, wx0, wx1, wx2, &sm.y[k][0][pl], &sm.ys[k][0][pl], BP);
+      } else {
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          const double2 v = (keep >> iw) & 1u ? y[iw] : make_double2(0.0, 0.0);
+          sm.y[k][iw][pl] = v;
+          sm.ys[k][iw][pl] = __dadd_rn(v.x, v.y);
+        }
+      }
     }
     for (int e = tid; e < kCKY * BN; e += kThreads) {
       const int k = e % kCKY, bl = e / kCKY;
@@ -499,16 +561,6 @@ struct SsxShared {
   float wxf[kSsxBN][kNW][2], iwx2f[kSsxBN][kNW][2];  // wx and 1 / wx^2 as float-float
 };
 
-// An FP32 value as a double, on the integer pipe (exponent rebiased,
-// mantissa shifted): exact for normal values and zero; FP32 subnormals (below
-// 1.2e-38, far below any term that matters next to the outputs) give zero.
-// cvt.f64.f32 would take the FP64 pipe, GB300's scarcest.
-__device__ __forceinline__ double f32_widen(float f) {
-  const unsigned u = __float_as_uint(f), mag = u & 0x7FFFFFFFu;
-  const unsigned hi = (u & 0x80000000u) | (mag >= 0x00800000u ? (mag >> 3) + 0x38000000u : 0u);
-  return __hiloint2double((int)hi, mag >= 0x00800000u ? (int)(mag << 29) : 0);
-}
-
 // One term's ssx factor from the element's float-float values (a + i b =
 // wtilde, G = I_eps wtilde, Omega2 = wtilde G): Omega2 / wx^2 when kept,
 // -G conj(z) / (2 |z|^2) with z = wtilde + wx in the second branch, else 0;
@@ -522,7 +574,7 @@ __device__ __forceinline__ double2 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy
   const FF k2x = ff_mul_raw(tx, r), k2y = ff_mul_raw(ty, r);
   const FF sx = keep ? k1x : (second ? FF{-0.5f * k2x.hi, -0.5f * k2x.lo} : FF{0.f, 0.f});
   const FF sy = keep ? k1y : (second ? FF{-0.5f * k2y.hi, -0.5f * k2y.lo} : FF{0.f, 0.f});
-  return make_double2(f32_widen(sx.hi) + f32_widen(sx.lo), f32_widen(sy.hi) + f32_widen(sy.lo));
+  return make_double2(ff_widen(sx), ff_widen(sy));
 }
 
 // The same factor in FP64, for elements whose inputs leave the float-float
@@ -542,14 +594,6 @@ static __device__ __noinline__ double2 ssx_factor_fp64(double a, double b, doubl
   const double q = -0.5 * rcp_f64(fma(zr, zr, b2));
   return make_double2(fma(g.x, zr, g.y * b) * q, fma(g.y, zr, -g.x * b) * q);
 }
-// biased exponent of a double, on the integer pipe
-__device__ __forceinline__ int f64_exp(double x) { return (__double2hiint(x) >> 20) & 0x7FF; }
-// x + i y inside the float-float range: zero (or an FP64 subnormal, which the
-// split flushes), or its larger component in [2^-20, 2^20)
-__device__ __forceinline__ bool ff_range(double x, double y) {
-  const int e = max(f64_exp(x), f64_exp(y));
-  return e == 0 || (unsigned)(e - (1023 - 20)) < 40u;
-}
 
 __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w, int item,
                                               unsigned char* smem_raw, SsxShared& sh, int tid) {
@@ -565,7 +609,7 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
   if (tid < kSsxBN * kNW) {
     const int i = tid / kNW, iw = tid % kNW;
     const double wx = i < nbl ? p.wx[(size_t)(n1_0 + i) * p.wx_stride + iw] : 1.0;
-    wx_out = (unsigned)(f64_exp(wx) - (1023 - 20)) >= 40u;
+    wx_out = !ff_freq_range(wx);
     sh.wx[i][iw] = wx;
     sh.iwx2[i][iw] = rcp_f64(wx * wx);
     const FF f = ff_of(wx), g = ff_of(sh.iwx2[i][iw]);

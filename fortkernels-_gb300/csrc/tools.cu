@@ -1,6 +1,7 @@
 // Seeded device fills (bit-identical to workload.py) and FMA peak probes.
 #include "sigma_tools.h"
 #include "sigma_internal.cuh"
+#include "floatfloat.cuh"
 
 namespace sigma {
 namespace {
@@ -146,8 +147,27 @@ __global__ void reciprocals_kernel(const double* w, double* out, long long n) {
     out[3 * i + 2] = __drcp_rn(x);  // IEEE 1/x, correctly rounded
   }
 }
+__global__ void split_kernel(const double* x, float* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const FF s = ff_of(x[i]);
+    out[2 * i] = s.hi;
+    out[2 * i + 1] = s.lo;
+  }
+}
 }  // namespace
 }  // namespace sigma
+
+extern "C" int sigma_eval_split(const double* x, float* out, long long n, void* stream) {
+  using namespace sigma;
+  if (!x || !out) return SIGMA_ERR_NULL;
+  if (n <= 0) return SIGMA_ERR_INVALID_SHAPE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  split_kernel<<<(int)blocks, 256, 0, s>>>(x, out, n);
+  SIGMA_CUDA_TRY(cudaGetLastError());
+  return SIGMA_OK;
+}
 
 extern "C" int sigma_eval_reciprocals(const double* w, double* out, long long n, void* stream) {
   using namespace sigma;

@@ -105,6 +105,7 @@ SIGNATURES = {
     "sigma_fill_stress": ([_P, _LL, _ULL, _ULL, _P, _I, _D, _D, _P], _I),
     "sigma_measure_fma_peaks": ([_P, _P, _P], _I),
     "sigma_eval_reciprocals": ([_P, _P, _LL, _P], _I),
+    "sigma_eval_split": ([_P, _P, _LL, _P], _I),
 }
 
 

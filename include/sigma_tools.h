@@ -46,6 +46,14 @@ int sigma_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops, void* stre
  * array of 3n doubles.  Asynchronous on `stream`. */
 int sigma_eval_reciprocals(const double* w, double* out, long long n, void* stream);
 
+/* The float-float split of n device doubles x (a check of the split the
+ * FP32-class forms and the FP64 forms' float-float factors build on; no
+ * counterpart in the reference): out[2i] = hi (x truncated to 24
+ * significant bits), out[2i+1] = lo (the remaining bits rounded to FP32), so
+ * |x - hi - lo| <= 2^-48 |x| for 2^-74 <= |x| < 2^128.  out is a device
+ * array of 2n floats.  Asynchronous on `stream`. */
+int sigma_eval_split(const double* x, float* out, long long n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

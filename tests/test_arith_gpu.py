@@ -67,3 +67,52 @@ def test_overflowing_wdiff_drops_the_term(sigma_lib):
     g = sigma_lib.gpp_host(prob, sigma_lib.PREC_FP64)
     assert g[0][2] == 0
     assert rel_err(g[0][:2], ach[:2]).max() <= 1e-12
+
+
+def _sample_split(n, seed):
+    """Doubles over the split's range and beyond, random mantissas, plus
+    remainders of exactly half an FP32 ulp of lo (ties), either side of a
+    tie, all-ones mantissas, the range edges, zeros, infinities, NaN."""
+    rng = np.random.default_rng(seed)
+    sign = rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63)
+    mant = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    ex = rng.integers(1023 - 160, 1023 + 160, n, dtype=np.uint64)
+    x = (sign | ex << np.uint64(52) | mant).view(np.float64)
+    special = []
+    for e in (-126, -100, -75, -74, -73, -1, 0, 1, 20, 127):
+        for m in (1 << 4, (1 << 4) | (1 << 5), (1 << 4) - 1, (1 << 4) + 1, (1 << 52) - 1, (1 << 29) - 1,
+                  1 << 29, 0):
+            for s in (0, 1):
+                special.append((s << 63) | ((e + 1023) << 52) | m)
+    sp = np.array(special, dtype=np.uint64).view(np.float64)
+    edge = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 3.4028235677973366e38, 1e-40, -1e-45])
+    return np.concatenate([x, sp, edge])
+
+
+def test_float_float_split(sigma_lib):
+    """The float-float split behind the FP32-class forms and the FP64 forms'
+    float-float factors: hi = x truncated to 24 significant bits and lo =
+    the remaining 29 bits rounded to FP32 (so |x - hi - lo| <= 2^-48 |x|)
+    over 2^-74 <= |x| < 2^128; below it a signed zero or hi alone, above it
+    an infinite hi."""
+    x = _sample_split(1 << 20, 7)
+    dx = torch.from_numpy(x).cuda()
+    out = torch.empty(2 * len(x), dtype=torch.float32, device="cuda")
+    assert sigma_lib.load().sigma_eval_split(dx.data_ptr(), out.data_ptr(), len(x), None) == 0
+    torch.cuda.synchronize()
+    o = out.cpu().numpy().reshape(-1, 2)
+    nan = np.isnan(x)
+    ax = np.abs(x)
+    inside = ~nan & (ax >= 2.0 ** -74) & (ax < 2.0 ** 128)
+    xs = x[inside]
+    hi = ((xs.view(np.uint64) >> np.uint64(29)) << np.uint64(29)).view(np.float64)  # truncated to 24 bits
+    assert np.array_equal(o[inside, 0].astype(np.float64), hi)
+    lo = (xs - hi).astype(np.float32)  # x - hi is exact in FP64; one rounding to FP32
+    assert np.array_equal(o[inside, 1], lo)  # (a zero lo carries x's sign)
+    err = np.abs(xs - o[inside, 0].astype(np.float64) - o[inside, 1].astype(np.float64))
+    assert np.all(err <= 2.0 ** -48 * np.abs(xs))
+    big = ~nan & (ax >= 2.0 ** 128)
+    assert np.all(np.isinf(o[big, 0])) and np.all(o[big, 1] == 0)
+    assert np.all(np.isnan(o[nan, 0]))
+    tiny = ~nan & (ax < 2.0 ** -126)
+    assert np.all(o[tiny, 0] == 0) and np.all(o[tiny, 1] == 0)
