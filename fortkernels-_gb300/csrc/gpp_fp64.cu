@@ -228,12 +228,15 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork
 // subtractions) stay near 1e-16 of the partial sums.
 constexpr int kCKY = 16;  // g-vectors per staged chunk
 
+// Rows padded by one element: the staging writes run along g-vectors (the
+// coalesced direction of the global reads), so unpadded rows, whose strides
+// are multiples of 128 bytes, put a warp's writes in one bank group.
 template <int BN, int BP>
 struct SchYSmem {
-  double2 y[kCKY][kNW][BP];
-  double ys[kCKY][kNW][BP];  // Y.x + Y.y
-  double2 n[kCKY][BN];
-  double ns[kCKY][BN];       // n.x + n.y
+  double2 y[kCKY][kNW * BP + 1];  // [k][iw * BP + column]
+  double ys[kCKY][kNW * BP + 1];  // Y.x + Y.y
+  double2 n[kCKY][BN + 1];
+  double ns[kCKY][BN + 1];        // n.x + n.y
 };
 
 // Bounded wait for a gate word written by a host-to-device copy (`polls`
@@ -357,13 +360,13 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       if (!valid) keep = 0u;
       const bool wide = valid && (wx_wide || !(ff_range(wt.x, wt.y) && ff_range(ie.x, ie.y)));
       if (__any_sync(0xffffffffu, wide) && wide) {
-        sch_factor_fp64(wt, ie, wx0, wx1, wx2, &sm.y[k][0][pl], &sm.ys[k][0][pl], BP);
+        sch_factor_fp64(wt, ie, wx0, wx1, wx2, &sm.y[k][pl], &sm.ys[k][pl], BP);
       } else {
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
           const double2 v = (keep >> iw) & 1u ? y[iw] : make_double2(0.0, 0.0);
-          sm.y[k][iw][pl] = v;
-          sm.ys[k][iw][pl] = __dadd_rn(v.x, v.y);
+          sm.y[k][iw * BP + pl] = v;
+          sm.ys[k][iw * BP + pl] = __dadd_rn(v.x, v.y);
         }
       }
     }
@@ -390,8 +393,8 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       for (int j = 0; j < TC; ++j)
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          y[j][iw] = sm.y[k][iw][tx + 16 * j];
-          ysum[j][iw] = sm.ys[k][iw][tx + 16 * j];
+          y[j][iw] = sm.y[k][iw * BP + tx + 16 * j];
+          ysum[j][iw] = sm.ys[k][iw * BP + tx + 16 * j];
         }
 #pragma unroll
       for (int i = 0; i < TB; ++i)
@@ -546,10 +549,10 @@ __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchVi
 // the terms take the second one, so a warp almost always needs both).
 constexpr int kSsxCK = 8;      // g-vectors per staged chunk
 
-struct SsxSmem {
-  double a[kSsxCK][kSsxBP];
-  double b[kSsxCK][kSsxBP];
-  double2 ie[kSsxCK][kSsxBP];
+struct SsxSmem {  // column rows padded by one element (see SchYSmem)
+  double a[kSsxCK][kSsxBP + 1];
+  double b[kSsxCK][kSsxBP + 1];
+  double2 ie[kSsxCK][kSsxBP + 1];
   double2 n[kSsxCK][kSsxBN];
   double ns[kSsxCK][kSsxBN];  // n.x + n.y
 };
