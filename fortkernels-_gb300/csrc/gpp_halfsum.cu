@@ -68,14 +68,17 @@ struct HalfDev {
   const int* brk;                          // [ng] occupied-band cut
 };
 
+// Rows padded by one element: the staging writes run along g-vectors (the
+// coalesced direction of the global reads), so unpadded rows, whose strides
+// are multiples of 128 bytes, put a warp's writes in one bank group.
 template <int NF>
 struct HalfSmem {
-  double2 z[kHCK][NF][kHBP];
-  double2 n[kHCK][kHBN];
-  double2 m[kHCK][kHBN];
-  double zs[kHCK][NF][kHBP];  // z.x + z.y
-  double ns[kHCK][kHBN];
-  double ms[kHCK][kHBN];
+  double2 z[kHCK][NF * kHBP + 1];  // [k][f * kHBP + column]
+  double2 n[kHCK][kHBN + 1];
+  double2 m[kHCK][kHBN + 1];
+  double zs[kHCK][NF * kHBP + 1];  // z.x + z.y
+  double ns[kHCK][kHBN + 1];
+  double ms[kHCK][kHBN + 1];
 };
 
 __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
@@ -168,8 +171,8 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
         }
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-          sm.z[k][f][pl] = z[f];
-          sm.zs[k][f][pl] = __dadd_rn(z[f].x, z[f].y);
+          sm.z[k][f * kHBP + pl] = z[f];
+          sm.zs[k][f * kHBP + pl] = __dadd_rn(z[f].x, z[f].y);
         }
       }
       for (int e = tid; e < kHCK * kHBN; e += kThreads) {
@@ -200,8 +203,8 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
         for (int j = 0; j < kHTC; ++j)
 #pragma unroll
           for (int f = 0; f < NF; ++f) {
-            z[j][f] = sm.z[k][f][tx + 16 * j];
-            zsum[j][f] = sm.zs[k][f][tx + 16 * j];
+            z[j][f] = sm.z[k][f * kHBP + tx + 16 * j];
+            zsum[j][f] = sm.zs[k][f * kHBP + tx + 16 * j];
           }
 #pragma unroll
         for (int i = 0; i < kHTB; ++i)

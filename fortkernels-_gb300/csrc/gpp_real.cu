@@ -39,9 +39,12 @@ struct GppRealDev {
   const int* igp_of;
 };
 
+// Rows padded by one element: the staging writes run along g-vectors (the
+// coalesced direction of the global reads), so unpadded rows, whose strides
+// are multiples of 128 bytes, put a warp's writes in one bank.
 struct RealSmem {
-  double y[kRCK][kNW][kRBP];
-  double n[kRCK][kRBN];
+  double y[kRCK][kNW * kRBP + 1];  // [k][iw * kRBP + column]
+  double n[kRCK][kRBN + 1];
 };
 
 __global__ void __launch_bounds__(kThreads, 1) sch_real_kernel(GppRealDev p, GppWork w) {
@@ -89,9 +92,9 @@ __global__ void __launch_bounds__(kThreads, 1) sch_real_kernel(GppRealDev p, Gpp
           y1 = factor(wx1);
           y2 = factor(wx2);
         }
-        sm.y[k][0][pl] = y0;
-        sm.y[k][1][pl] = y1;
-        sm.y[k][2][pl] = y2;
+        sm.y[k][pl] = y0;
+        sm.y[k][kRBP + pl] = y1;
+        sm.y[k][2 * kRBP + pl] = y2;
       }
       for (int e = tid; e < kRCK * kRBN; e += kThreads) {
         const int k = e % kRCK, bl = e / kRCK;
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(kThreads, 1) sch_real_kernel(GppRealDev p, Gpp
 #pragma unroll
         for (int j = 0; j < TC; ++j)
 #pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) y[j][iw] = sm.y[k][iw][tx + 16 * j];
+          for (int iw = 0; iw < kNW; ++iw) y[j][iw] = sm.y[k][iw * kRBP + tx + 16 * j];
 #pragma unroll
         for (int i = 0; i < TB; ++i)
 #pragma unroll
