@@ -672,15 +672,19 @@ def run_batched(S, W, torch, dist, world, stream, sptr, args, dropin_value):
     if ref is not None:
         off = ref["n1_offsets"]
         for name in outs:
-            worst, over, n1_worst = 0.0, 0, 0.0
+            worst, over, n1_worst, at = 0.0, 0, 0.0, ""
+            by = {"achtemp": 0.0, "asxtemp": 0.0}
             for i, o in enumerate(outs[name]):
                 for k, key in ((0, "achtemp"), (1, "asxtemp")):
                     e = np.abs(o[k] - ref[key][i]) / np.abs(ref[key][i])
-                    worst = max(worst, float(e.max()))
+                    if float(e.max()) > worst:
+                        worst, at = float(e.max()), f"instance {i} {key}[{int(np.argmax(e))}]"
+                    by[key] = max(by[key], float(e.max()))
                     over += int(np.sum(e > (1e-12 if name == "fp64" else 1e-6)))
                 r1 = ref["acht_n1_loc"][off[i]:off[i + 1]]
                 n1_worst = max(n1_worst, float(np.linalg.norm(o[2] - r1) / np.linalg.norm(r1)))
-            res[name]["rel_err_vs_oracle"] = {"max": worst, "outputs_over_bar": over,
+            res[name]["rel_err_vs_oracle"] = {"max": worst, "max_at": at, "max_by_output": by,
+                                              "outputs_over_bar": over,
                                               "bar": 1e-12 if name == "fp64" else 1e-6,
                                               "outputs": 6 * len(outs[name]),
                                               "acht_n1_loc_normwise_max": n1_worst}

@@ -141,6 +141,21 @@ __device__ __forceinline__ FF ff_rcp_raw(FF x) {
   return FF{r0, r0 * (fmaf(-x.hi, r0, 1.0f) - x.lo * r0)};
 }
 
+// Paired FP32 (f32x2) helpers: halves of a float4, and ff_add of two
+// independent float-float accumulators (hi.x, lo.x) += x.x, (hi.y, lo.y) +=
+// x.y with the same roundings as ff_add, one paired instruction per step
+// (differences as fma(a, -1, b) = b - a, exact up to the one rounding).
+__device__ __forceinline__ float2 f4_lo(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 f4_hi(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ void ff_add2(float2& hi, float2& lo, float2 x, float2 m1) {
+  const float2 s = __fadd2_rn(hi, x);
+  const float2 bv = __ffma2_rn(hi, m1, s);  // s - hi
+  const float2 av = __ffma2_rn(bv, m1, s);  // s - bv
+  const float2 e = __fadd2_rn(__fadd2_rn(__ffma2_rn(av, m1, hi), __ffma2_rn(bv, m1, x)), lo);
+  hi = __fadd2_rn(s, e);
+  lo = __ffma2_rn(__ffma2_rn(s, m1, hi), m1, e);  // e - (hi - s)
+}
+
 // An FP32 value as a double, on the integer pipe (exponent rebiased,
 // mantissa shifted): exact for normal values and zero; FP32 subnormals (below
 // 1.2e-38) give zero.  cvt.f64.f32 would take the FP64 pipe, GB300's

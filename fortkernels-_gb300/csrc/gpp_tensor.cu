@@ -42,13 +42,29 @@ namespace {
 constexpr int kFacThreads = 256;
 constexpr int kZeroTiles = 64;  // K tiles per padding-row item
 
+// Slot of g-vector k in the ssx planes: the middle two of every four are
+// swapped, so that a 16-byte read of g-vectors 4m .. 4m+3 holds the pairs
+// (4m, 4m+2) and (4m+1, 4m+3); their paired sum is then (t0 + t1, t2 + t3)
+// and the 4-term tree (t0 + t1) + (t2 + t3).
+__device__ __forceinline__ int ssx_slot(int k) { return (k & ~3) | ((k & 1) << 1) | ((k >> 1) & 1); }
+
+// Row stride of the ssx factor planes (floats): 16-byte rows, and the eight
+// columns x four g-vector quarters of a warp's 16-byte reads fall in distinct
+// bank groups (3 x 36 = 12 mod 32 banks per column).
+constexpr int kXS = kFacK + 4;
+
 struct FactorSmem {
   float2 y[kNW][kFacCols][kFacK + 1];          // the tile's factors for the slice writes
   union {
-    float2 x[kFacCols][kNW][kFacK + 1];        // the tile's ssx factors
+    struct {
+      float r[kFacCols][kNW][kXS];             // the tile's ssx factors, real parts
+      float i[kFacCols][kNW][kXS];             // and imaginary parts
+    } x;
     double2 red[kFusedBands][kNW][kFacCols];   // item epilogue: per-column ssx sums
   };
-  float2 an[kFusedBands][kFacK];               // occupied bands' aqsn over the tile's g-vectors
+  // occupied bands' aqsn over the tile's g-vectors: real parts, imaginary
+  // parts and their negatives (operands of paired FP32 products)
+  float anr[kFusedBands][kFacK], ani[kFusedBands][kFacK], anm[kFusedBands][kFacK];
   // the current job's frequency constants, formed once per CTA and job:
   // wx as float-float (hi, lo), its FP32 rounding and remainder, 1 / wx^2
   float wxc[kNW][5];
@@ -232,7 +248,10 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
           const double2 d = p.aqsn[(size_t)n1 * p.nc + ig];
           v = make_float2(__double2float_rn(d.x), __double2float_rn(d.y));
         }
-        sm.an[n1][k] = v;
+        const int ks = ssx_slot(k);
+        sm.anr[n1][ks] = v.x;
+        sm.ani[n1][ks] = v.y;
+        sm.anm[n1][ks] = -v.y;
       }
 #pragma unroll 1
       for (int j = 0; j < 2; ++j) {
@@ -303,7 +322,8 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
           sm.y[iw][pl][lane] = yt[iw];
-          sm.x[pl][iw][lane] = sv[iw];
+          sm.x.r[pl][iw][ssx_slot(lane)] = sv[iw].x;
+          sm.x.i[pl][iw][ssx_slot(lane)] = sv[iw].y;
         }
       }
       __syncthreads();
@@ -324,29 +344,38 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
       }
       // the tile's ssx products: output o = (band n1, frequency iw, column
       // pl); lane quarter q takes g-vectors 8q .. 8q+7 and folds two 4-term
-      // FP32 tree sums into its float-float accumulator
+      // FP32 tree sums into its float-float accumulator.  Paired FP32
+      // instructions: the products of g-vector pairs (4m, 4m + 2) and
+      // (4m + 1, 4m + 3) (the planes' slot order), then the x and y
+      // components' float-float additions as one pair.
+      const float2 m1 = make_float2(-1.f, -1.f);
 #pragma unroll 1
       for (int r = 0; r < kSsxRounds; ++r) {
         const int o = r * (kFacThreads / 4) + warp * 8 + (lane >> 2), q = lane & 3;
         if (o < outputs) {
           const int n1 = o / (kNW * kFacCols), iw = (o / kFacCols) % kNW, pl = o % kFacCols;
-          float4 a = acc_dyn[4 * o + q];
+          const float4 a = acc_dyn[4 * o + q];
+          float2 hi = make_float2(a.x, a.y), lo = make_float2(a.z, a.w);
 #pragma unroll
           for (int half = 0; half < 2; ++half) {
-            float2 t[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const int kk = 8 * q + 4 * half + k;
-              const float2 an = sm.an[n1][kk], x = sm.x[pl][iw][kk];
-              t[k] = make_float2(fmaf(an.x, x.x, -an.y * x.y), fmaf(an.x, x.y, an.y * x.x));
-            }
-            ff_add(a.x, a.z, (t[0].x + t[1].x) + (t[2].x + t[3].x));
-            ff_add(a.y, a.w, (t[0].y + t[1].y) + (t[2].y + t[3].y));
+            const int kk = 8 * q + 4 * half;
+            const float4 ar = *reinterpret_cast<const float4*>(&sm.anr[n1][kk]);
+            const float4 ai = *reinterpret_cast<const float4*>(&sm.ani[n1][kk]);
+            const float4 am = *reinterpret_cast<const float4*>(&sm.anm[n1][kk]);
+            const float4 xr = *reinterpret_cast<const float4*>(&sm.x.r[pl][iw][kk]);
+            const float4 xi = *reinterpret_cast<const float4*>(&sm.x.i[pl][iw][kk]);
+            // t = an x: t.x = an.x x.x - an.y x.y, t.y = an.x x.y + an.y x.x
+            const float2 px0 = __ffma2_rn(f4_lo(ar), f4_lo(xr), __fmul2_rn(f4_lo(am), f4_lo(xi)));
+            const float2 px1 = __ffma2_rn(f4_hi(ar), f4_hi(xr), __fmul2_rn(f4_hi(am), f4_hi(xi)));
+            const float2 py0 = __ffma2_rn(f4_lo(ar), f4_lo(xi), __fmul2_rn(f4_lo(ai), f4_lo(xr)));
+            const float2 py1 = __ffma2_rn(f4_hi(ar), f4_hi(xi), __fmul2_rn(f4_hi(ai), f4_hi(xr)));
+            const float2 tx = __fadd2_rn(px0, px1), ty = __fadd2_rn(py0, py1);
+            ff_add2(hi, lo, make_float2(tx.x + tx.y, ty.x + ty.y), m1);
           }
-          acc_dyn[4 * o + q] = a;
+          acc_dyn[4 * o + q] = make_float4(hi.x, hi.y, lo.x, lo.y);
         }
       }
-      __syncthreads();  // sm.an, sm.x and sm.y are refilled by the next tile
+      __syncthreads();  // the aqsn planes, sm.x and sm.y are refilled by the next tile
     }
 
     if (nvb > 0) {
