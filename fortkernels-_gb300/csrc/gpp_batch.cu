@@ -24,6 +24,7 @@
 // (two launches).
 #include <algorithm>
 #include <cstring>
+#include <numeric>
 #include <vector>
 
 #include "sigma_gpp.h"
@@ -113,6 +114,48 @@ void size_instance(GppWork& w, int band_count, int bn, int bp, int nc, int ng, d
   w.n_items = w.n_band_blocks * w.n_col_blocks * w.n_splits;
 }
 
+// Order of the grouped contraction's item table.  The kernel's static
+// schedule gives CTA c the items c, c + G, c + 2G, ... (G CTAs), and the
+// instances' items differ in length (K' tiles), so in table order some CTAs
+// would draw several long items.  Items are taken longest first, one round
+// of G at a time, each to the CTA with the least work so far (a K' tile plus
+// a fixed epilogue share per item); CTAs are then numbered so that those
+// holding an item of the last, partial round come first.  The reduction
+// sums each row block's pieces from fixed slots, so the order changes no
+// result.
+void balance_item_rounds(std::vector<int4>& items, int G) {
+  const int n = (int)items.size();
+  if (G <= 0 || n <= G) return;
+  constexpr long long kEpilogueTiles = 2;
+  auto cost = [](const int4& it) { return (long long)(it.w & 0xFFFF) + kEpilogueTiles; };
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(items[a]) > cost(items[b]); });
+  const int rounds = (n + G - 1) / G;
+  std::vector<long long> load(G, 0);
+  std::vector<std::vector<int>> held(G);
+  std::vector<int> ctas(G);
+  std::iota(ctas.begin(), ctas.end(), 0);
+  for (int r = 0; r < rounds; ++r) {
+    std::stable_sort(ctas.begin(), ctas.end(), [&](int a, int b) { return load[a] < load[b]; });
+    const int lo = r * G, hi = std::min(n, lo + G);
+    for (int k = 0; k < hi - lo; ++k) {
+      held[ctas[k]].push_back(order[lo + k]);
+      load[ctas[k]] += cost(items[order[lo + k]]);
+    }
+  }
+  std::vector<int> label(G);
+  int next = 0;
+  for (int c = 0; c < G; ++c)
+    if ((int)held[c].size() == rounds) label[c] = next++;
+  for (int c = 0; c < G; ++c)
+    if ((int)held[c].size() != rounds) label[c] = next++;
+  std::vector<int4> out(n);
+  for (int c = 0; c < G; ++c)
+    for (int r = 0; r < (int)held[c].size(); ++r) out[(size_t)r * G + label[c]] = items[held[c][r]];
+  items.swap(out);
+}
+
 // The grouped tensor form: every instance's contraction plan over its own
 // slice images (items of about the same number of K tiles in every plan),
 // the factor-pass jobs, the contraction jobs and the GEMM's item table in
@@ -197,6 +240,7 @@ int build_tensor_group(sigma_gpp_batch_s* b, const sigma_gpp_instance* inst,
     rwarps += q.number_bands * kNW;
     factor_job_operands(fj, J.d, J.oz);
   }
+  balance_item_rounds(items, sms);  // the contraction runs on `sms` CTAs
   const size_t o_fac = 0;
   const size_t o_jobs = o_fac + up256(sizeof(FactorJob) * n);
   const size_t o_items = o_jobs + up256(sizeof(OzGroupJob) * n);
