@@ -101,6 +101,16 @@ __device__ __forceinline__ bool ff_gt_fast(FF x, FF y, bool& near) {
   return clear ? d > 0.f : full > 0.f;
 }
 
+// x > 0.25 for a non-negative normalised float-float x, with `near` set
+// within 2^-30 of 0.25 (relative): ff_gt_fast(x, {0.25, 0}, near) in four
+// instructions.  x.hi - 0.25 is exact where x.hi is within a factor of two
+// of 0.25 (Sterbenz); elsewhere it and the sum keep the sign of x - 0.25.
+__device__ __forceinline__ bool ff_gt_quarter(FF x, bool& near) {
+  const float full = (x.hi - 0.25f) + x.lo;
+  near = fabsf(full) <= 2.3283064e-10f;  // 2^-32 = 2^-30 x 0.25
+  return full > 0.f;
+}
+
 // x - y as an unnormalised pair (TwoSum of the hi parts plus the lo
 // parts): exact to ~2^-46 of the operands, for a product or square next.
 __device__ __forceinline__ FF ff_sub_raw(FF x, FF y) {

@@ -307,7 +307,6 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const int ig_end = min(ig_begin + w.split_len, p.nc);
   const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
   const bool wx_wide = !(ff_freq_range(wx0) && ff_freq_range(wx1) && ff_freq_range(wx2));
-  const FF quarter{0.25f, 0.f};
 
   double p1[TB][TC][kNW], p2[TB][TC][kNW], p3[TB][TC][kNW];
 #pragma unroll
@@ -350,7 +349,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         const FF c = ff_of(__dsub_rn(iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2), wt.x));
         const FF wv = ff_sq_add(c, b2);  // |wdiff|^2
         bool near;
-        keep |= ff_gt_fast(wv, quarter, near) ? (1u << iw) : 0u;
+        keep |= ff_gt_quarter(wv, near) ? (1u << iw) : 0u;
         rare |= (near || thr2_binds) ? (1u << iw) : 0u;
         const FF r = ff_rcp_raw(wv);
         const FF ux = ff_dot2_raw(gx, c, gy, fb), uy = ff_dot2_raw(gx, fb, ff_neg(gy), c);

@@ -177,7 +177,6 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
   __shared__ FactorSmem sm;
   extern __shared__ float4 acc_dyn[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const FF quarter{0.25f, 0.f};
   int cached = -1;  // job whose frequency constants sm.wxc holds
   for (int item = blockIdx.x; item < total; item += gridDim.x) {
     const int ji = kGroup ? find_job(jobs, n_jobs, item) : 0;
@@ -284,7 +283,7 @@ __global__ void __launch_bounds__(kFacThreads, 4) factor_kernel(const FactorJob 
             // wv > 0.25 and wv * 250000 > |wtilde|^2 (250000 exact in FP32);
             // the second condition only binds for thr2_binds (rare path)
             bool near;
-            const bool keep = ff_gt_fast(wv, quarter, near);
+            const bool keep = ff_gt_quarter(wv, near);
             // the factor of every term (the warp's lanes almost always
             // disagree on keep), selected by the final keep bit below
             const FF r = ff_rcp_raw(wv);
