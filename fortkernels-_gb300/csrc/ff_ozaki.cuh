@@ -68,28 +68,49 @@ __device__ __forceinline__ void oz_split3(float x, unsigned short& a, unsigned s
   c = __bfloat16_as_ushort(s3);
 }
 
-// Slices of 8 consecutive K values of one row, written as three 16-byte
-// chunks (one per slice tile) of a 24 KB block.  Two values per paired
-// conversion (cvt.rn.bf16x2.f32 rounds each as __float2bfloat16_rn does, so
-// the slices are those of oz_split3), the pairs already packed.
-__device__ __forceinline__ void oz_put_row_chunk(unsigned char* blk, int r, int ch, const float (&v)[8]) {
+// Slices of 8 consecutive K values of one row: three 16-byte chunks (one
+// per slice tile of a 24 KB block).  Two values per paired conversion
+// (cvt.rn.bf16x2.f32 rounds each as __float2bfloat16_rn does, so the slices
+// are those of oz_split3), the pairs already packed; the residuals of a pair
+// as one paired FP32 instruction (fma(s, -1, v) = v - s, exact here).
+struct OzChunk {
+  uint4 s[3];
+};
+__device__ __forceinline__ OzChunk oz_slice_chunk(const float (&v)[8]) {
+  const float2 m1 = make_float2(-1.f, -1.f);
   uint32_t sl[3][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const __nv_bfloat162 h1 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-    const float2 f1 = __bfloat1622float2(h1);
-    const float r0 = v[2 * j] - f1.x, r1 = v[2 * j + 1] - f1.y;  // exact
-    const __nv_bfloat162 h2 = __floats2bfloat162_rn(r0, r1);
-    const float2 f2 = __bfloat1622float2(h2);
-    const __nv_bfloat162 h3 = __floats2bfloat162_rn(r0 - f2.x, r1 - f2.y);
+    const float2 x = make_float2(v[2 * j], v[2 * j + 1]);
+    const __nv_bfloat162 h1 = __float22bfloat162_rn(x);
+    const float2 r1 = __ffma2_rn(__bfloat1622float2(h1), m1, x);  // exact
+    const __nv_bfloat162 h2 = __float22bfloat162_rn(r1);
+    const __nv_bfloat162 h3 = __float22bfloat162_rn(__ffma2_rn(__bfloat1622float2(h2), m1, r1));
     sl[0][j] = *reinterpret_cast<const uint32_t*>(&h1);
     sl[1][j] = *reinterpret_cast<const uint32_t*>(&h2);
     sl[2][j] = *reinterpret_cast<const uint32_t*>(&h3);
   }
+  OzChunk c;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) c.s[s] = make_uint4(sl[s][0], sl[s][1], sl[s][2], sl[s][3]);
+  return c;
+}
+// The slices of -v: each slice negated (round to nearest even is symmetric).
+__device__ __forceinline__ OzChunk oz_negate_chunk(const OzChunk& c) {
+  OzChunk n;
 #pragma unroll
   for (int s = 0; s < 3; ++s)
-    *reinterpret_cast<uint4*>(blk + s * kOzSliceBytes + tma::sw64_offset(r, ch * 8)) =
-        make_uint4(sl[s][0], sl[s][1], sl[s][2], sl[s][3]);
+    n.s[s] = make_uint4(c.s[s].x ^ 0x80008000u, c.s[s].y ^ 0x80008000u, c.s[s].z ^ 0x80008000u,
+                        c.s[s].w ^ 0x80008000u);
+  return n;
+}
+__device__ __forceinline__ void oz_store_chunk(unsigned char* blk, int r, int ch, const OzChunk& c) {
+#pragma unroll
+  for (int s = 0; s < 3; ++s)
+    *reinterpret_cast<uint4*>(blk + s * kOzSliceBytes + tma::sw64_offset(r, ch * 8)) = c.s[s];
+}
+__device__ __forceinline__ void oz_put_row_chunk(unsigned char* blk, int r, int ch, const float (&v)[8]) {
+  oz_store_chunk(blk, r, ch, oz_slice_chunk(v));
 }
 
 // The slices of A'[R][k0 .. k0+8): real parts re (K' = k) and imaginary
@@ -179,22 +200,22 @@ __device__ __forceinline__ void oz_prep_b_elem(const FfDev& p, const OzakiPrep& 
   const int cb = (int)(rest / oz.kt);
   const int n = cb * kOzCols + nl;
   const int k0 = kt * kOzKTile + ch * 8;
-  float re[8], im[8], nim[8];
+  float re[8], im[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int k = k0 + j;
     const double2 v = (n < p.nb && k < p.nc) ? p.aqsn[(size_t)n * p.nc + k] : make_double2(0.0, 0.0);
     re[j] = __double2float_rn(v.x);
     im[j] = __double2float_rn(v.y);
-    nim[j] = -im[j];
   }
   unsigned char* base = oz.b_tiles + (size_t)cb * 2 * oz.kt * kOzOperandBytes;
   unsigned char* lo = base + (size_t)kt * kOzOperandBytes;            // K' < K: real parts of aqsn
   unsigned char* hi = base + (size_t)(oz.kt + kt) * kOzOperandBytes;  // K' >= K: imaginary parts
-  oz_put_row_chunk(lo, nl, ch, re);
-  oz_put_row_chunk(lo, 64 + nl, ch, im);
-  oz_put_row_chunk(hi, nl, ch, nim);
-  oz_put_row_chunk(hi, 64 + nl, ch, re);
+  const OzChunk cre = oz_slice_chunk(re), cim = oz_slice_chunk(im);
+  oz_store_chunk(lo, nl, ch, cre);
+  oz_store_chunk(lo, 64 + nl, ch, cim);
+  oz_store_chunk(hi, nl, ch, oz_negate_chunk(cim));
+  oz_store_chunk(hi, 64 + nl, ch, cre);
 }
 
 // Epilogue factors, element t of oz_weights_count: wtab[g][n] = aqsm[n][igp(g)]
