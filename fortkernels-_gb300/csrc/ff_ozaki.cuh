@@ -71,21 +71,20 @@ __device__ __forceinline__ void oz_split3(float x, unsigned short& a, unsigned s
 // Slices of 8 consecutive K values of one row: three 16-byte chunks (one
 // per slice tile of a 24 KB block).  Two values per paired conversion
 // (cvt.rn.bf16x2.f32 rounds each as __float2bfloat16_rn does, so the slices
-// are those of oz_split3), the pairs already packed; the residuals of a pair
-// as one paired FP32 instruction (fma(s, -1, v) = v - s, exact here).
+// are those of oz_split3), the pairs already packed.
 struct OzChunk {
   uint4 s[3];
 };
 __device__ __forceinline__ OzChunk oz_slice_chunk(const float (&v)[8]) {
-  const float2 m1 = make_float2(-1.f, -1.f);
   uint32_t sl[3][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const float2 x = make_float2(v[2 * j], v[2 * j + 1]);
-    const __nv_bfloat162 h1 = __float22bfloat162_rn(x);
-    const float2 r1 = __ffma2_rn(__bfloat1622float2(h1), m1, x);  // exact
-    const __nv_bfloat162 h2 = __float22bfloat162_rn(r1);
-    const __nv_bfloat162 h3 = __float22bfloat162_rn(__ffma2_rn(__bfloat1622float2(h2), m1, r1));
+    const __nv_bfloat162 h1 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+    const float2 f1 = __bfloat1622float2(h1);
+    const float r0 = v[2 * j] - f1.x, r1 = v[2 * j + 1] - f1.y;  // exact
+    const __nv_bfloat162 h2 = __floats2bfloat162_rn(r0, r1);
+    const float2 f2 = __bfloat1622float2(h2);
+    const __nv_bfloat162 h3 = __floats2bfloat162_rn(r0 - f2.x, r1 - f2.y);
     sl[0][j] = *reinterpret_cast<const uint32_t*>(&h1);
     sl[1][j] = *reinterpret_cast<const uint32_t*>(&h2);
     sl[2][j] = *reinterpret_cast<const uint32_t*>(&h3);
