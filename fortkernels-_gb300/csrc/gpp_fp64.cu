@@ -10,16 +10,22 @@
 // pick the one that pads least; the batched kernel takes a shape per instance.
 //
 // GB300 runs FP64 at 1/64 of its FP32 rate, so the term is rewritten to
-// spend as few FP64 pipe instructions as possible (8 per term plus 6 per
-// band/column/g-vector shared by the three frequencies; the reciprocal is an
-// FP32 hardware seed refined by one FP64 Newton step, rcp_f64_seed32):
+// spend as few FP64 pipe instructions as possible:
 //   scha / conj(aqsm[n1][igp]) = aqsn * I_eps * wtilde * conj(wdiff) / |wdiff|^2
 //                              = R * (c + i b) * r,   R = aqsn * (I_eps * wtilde),
 //   c = wx - Re wtilde, b = Im wtilde, r = 1 / (c^2 + b^2).
-// conj(aqsm[n1][igp]), 0.5 and vcoul[igp] are applied once per column after
-// the g-vector sum.  The pole guard is a compare against a per-(column,
-// g-vector) threshold on the integer pipe and a select of r (exact poles give
-// r = inf and are dropped by the select, never multiplied).
+// With per-band frequencies (this first pass) every term is formed in
+// float-float arithmetic (FP32 pairs on the FP32 pipe: G in FP64 per column
+// and g-vector, c = wx - Re wtilde in FP64 per term, the rest from exact
+// splits), its FP32 high half widened and added to an FP64 sum and its low
+// half to an FP32 sum: 3 FP64 operations per term instead of 10 (the FP64
+// form had 8 per term plus 6 per band, column and g-vector).  A term's error
+// is about twice the FP64 form's, whose reciprocal is itself an FP32 seed
+// refined once (rcp_f64_seed32, within 2^-44.8).  conj(aqsm[n1][igp]), 0.5
+// and vcoul[igp] are applied once per column after the g-vector sum.  The
+// pole guard's decisions are taken in float-float and re-taken with the FP64
+// expressions near a threshold; exact poles are dropped by a select, never
+// multiplied.
 #include "sigma_internal.cuh"
 #include "floatfloat.cuh"
 #include "gpp_batch.cuh"
@@ -29,18 +35,40 @@ namespace {
 
 constexpr int kPad = 1;
 
+// Staging of the per-band-frequency pass: per (g-vector, column) wtilde's
+// parts in FP64 (c = wx - Re wtilde is formed in FP64, and the rare FP64
+// decisions read them), Im wtilde and its square and G = I_eps wtilde as
+// float-float values, and flags (bit 0: the guard's second condition can
+// bind, bit 1: outside the float-float range, bit 2: no term); per
+// (g-vector, band) aqsn as a float-float pair and its range flag.
 template <int BN, int BP>
 struct SchSmem {
   double a[kCK][BP + kPad];
   double b[kCK][BP + kPad];
-  double b2[kCK][BP + kPad];
-  double thr[kCK][BP + kPad];
-  double2 g[kCK][BP + kPad];
-  double2 n[kCK][BN + kPad];
+  float4 fb[kCK][BP + kPad];  // (b.hi, b.lo, b^2.hi, b^2.lo)
+  float4 fg[kCK][BP + kPad];  // (G.x hi, lo, G.y hi, lo)
+  unsigned flag[kCK][BP + kPad];
+  float4 fn[kCK][BN + kPad];  // (aqsn.x hi, lo, aqsn.y hi, lo)
+  unsigned nflag[kCK][BN + kPad];
 };
+constexpr unsigned kFlagBinds = 1u, kFlagWide = 2u, kFlagDead = 4u;
 
 __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
   return make_double2(fma(x.x, y.x, -__dmul_rn(x.y, y.y)), fma(x.x, y.y, __dmul_rn(x.y, y.x)));
+}
+
+// One term of the per-band-frequency pass in FP64, for terms whose inputs
+// leave the float-float range; out of line, reading its inputs from global
+// memory (noff: aqsn's offset, ~0 for a padding band).
+static __device__ __noinline__ double2 sch_term_fp64(const double2* aqsn, const double2* wtp,
+                                                     const double2* ieps, size_t noff, size_t off, double wx) {
+  const double2 n = noff != ~size_t(0) ? aqsn[noff] : make_double2(0.0, 0.0);
+  const double2 wt = wtp[off], ie = ieps[off];
+  const double2 R = cmul(n, cmul(ie, wt));
+  const double b = wt.y, b2 = guard_b2(b);
+  const double c = __dsub_rn(wx, wt.x), wv = fma(c, c, b2);
+  const double r = keep_nonneg(wv, guard_thr(wt.x, b2)) ? rcp_f64_seed32(wv) : 0.0;
+  return make_double2(fma(R.x, c, -__dmul_rn(b, R.y)) * r, fma(R.y, c, __dmul_rn(b, R.x)) * r);
 }
 
 // One work item of the main pass.  Leaves the item's partial sums in
@@ -61,88 +89,143 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
   const int ig_end = min(ig_begin + w.split_len, p.nc);
 
   double wxr[2][kNW];
+  bool wx_wide[2];
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     const int n1 = n1_0 + ty + TYN * i;
+    wx_wide[i] = false;
 #pragma unroll
-    for (int iw = 0; iw < kNW; ++iw)
-      wxr[i][iw] = n1 < band_end ? p.wx[(size_t)n1 * p.wx_stride + iw] : 0.0;
+    for (int iw = 0; iw < kNW; ++iw) {
+      wxr[i][iw] = n1 < band_end ? p.wx[(size_t)n1 * p.wx_stride + iw] : 1.0;
+      wx_wide[i] = wx_wide[i] || !ff_freq_range(wxr[i][iw]);
+    }
   }
+  // FP64 sums of the terms' high halves; their low halves summed in FP32
+  // (below 2^-23 of the terms) and added at the item's end
   double2 acc[2][2][kNW];
+  float2 acl[2][2][kNW];
 #pragma unroll
   for (int i = 0; i < 2; ++i)
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = make_double2(0.0, 0.0);
+      for (int iw = 0; iw < kNW; ++iw) {
+        acc[i][j][iw] = make_double2(0.0, 0.0);
+        acl[i][j][iw] = make_float2(0.f, 0.f);
+      }
 
   for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCK) {
     __syncthreads();
     for (int e = tid; e < kCK * BP; e += kThreads) {
       const int k = e % kCK, pl = e / kCK;
       const int ig = ig0 + k, my_igp = p0 + pl;
-      double a = 0.0, b = 0.0, b2 = 0.0, thr = __longlong_as_double(0x7ff0000000000000LL);
-      double2 g = make_double2(0.0, 0.0);
+      double a = 0.0, b = 0.0;
+      float4 fb = make_float4(0.f, 0.f, 0.f, 0.f), fg = fb;
+      unsigned flag = kFlagDead;
       if (ig < ig_end && my_igp < p.ng) {
         const size_t off = (size_t)my_igp * p.nc + ig;
         const double2 wt = p.wt[off];
         const double2 ie = p.ieps[off];
+        const double2 g = cmul(ie, wt);
         a = wt.x;
         b = wt.y;
-        b2 = guard_b2(b);
-        thr = guard_thr(a, b2);
-        g = cmul(ie, wt);
+        const FF f = ff_of(b), f2 = ff_mul_raw(f, f), gx = ff_of(g.x), gy = ff_of(g.y);
+        fb = make_float4(f.hi, f.lo, f2.hi, f2.lo);
+        fg = make_float4(gx.hi, gx.lo, gy.hi, gy.lo);
+        const float ah = ff_of(a).hi;
+        // |wtilde|^2 * 4e-6 > 0.25 needs |wtilde|^2 > 62500
+        flag = (fmaf(ah, ah, f.hi * f.hi) >= 62000.f ? kFlagBinds : 0u) |
+               (ff_range(wt.x, wt.y) && ff_range(ie.x, ie.y) ? 0u : kFlagWide);
       }
       sm.a[k][pl] = a;
       sm.b[k][pl] = b;
-      sm.b2[k][pl] = b2;
-      sm.thr[k][pl] = thr;
-      sm.g[k][pl] = g;
+      sm.fb[k][pl] = fb;
+      sm.fg[k][pl] = fg;
+      sm.flag[k][pl] = flag;
     }
     for (int e = tid; e < kCK * BN; e += kThreads) {
       const int k = e % kCK, bl = e / kCK;
       const int ig = ig0 + k, n1 = n1_0 + bl;
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
-      sm.n[k][bl] = v;
+      const FF nx = ff_of(v.x), ny = ff_of(v.y);
+      sm.fn[k][bl] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
+      sm.nflag[k][bl] = ff_range(v.x, v.y) ? 0u : kFlagWide;
     }
     __syncthreads();
 
-#pragma unroll 2
+#pragma unroll 1
     for (int k = 0; k < kCK; ++k) {
-      double a[2], b[2], b2[2], thr[2];
-      double2 g[2], nn[2];
+      double a[2], b[2];
+      FF fb[2], fb2[2], gx[2], gy[2], nx[2], ny[2];
+      unsigned flag[2], nflag[2];
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int pl = tx + TXN * j;
         a[j] = sm.a[k][pl];
         b[j] = sm.b[k][pl];
-        b2[j] = sm.b2[k][pl];
-        thr[j] = sm.thr[k][pl];
-        g[j] = sm.g[k][pl];
+        const float4 v = sm.fb[k][pl], g = sm.fg[k][pl];
+        fb[j] = FF{v.x, v.y};
+        fb2[j] = FF{v.z, v.w};
+        gx[j] = FF{g.x, g.y};
+        gy[j] = FF{g.z, g.w};
+        flag[j] = sm.flag[k][pl];
       }
 #pragma unroll
-      for (int i = 0; i < 2; ++i) nn[i] = sm.n[k][ty + TYN * i];
+      for (int i = 0; i < 2; ++i) {
+        const float4 v = sm.fn[k][ty + TYN * i];
+        nx[i] = FF{v.x, v.y};
+        ny[i] = FF{v.z, v.w};
+        nflag[i] = sm.nflag[k][ty + TYN * i];
+      }
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-          const double2 R = cmul(nn[i], g[j]);
-          const double bRre = __dmul_rn(b[j], R.x), bRim = __dmul_rn(b[j], R.y);
+          // R = aqsn G, then per frequency (R (c + i b)) / |wdiff|^2
+          const FF rx = ff_dot2_raw(nx[i], gx[j], ny[i], gy[j]);
+          const FF ry = ff_dot2_raw(nx[i], gy[j], ff_neg(ny[i]), gx[j]);
+          const bool wide = (flag[j] & kFlagWide) || nflag[i] || wx_wide[i];
+          const bool any_wide = __any_sync(0xffffffffu, wide);
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            const double c = __dsub_rn(wxr[i][iw], a[j]);
-            const double wv = fma(c, c, b2[j]);
-            double r = rcp_f64_seed32(wv);
-            r = keep_nonneg(wv, thr[j]) ? r : 0.0;
-            const double ure = fma(R.x, c, -bRim);
-            const double uim = fma(R.y, c, bRre);
-            acc[i][j][iw].x = fma(ure, r, acc[i][j][iw].x);
-            acc[i][j][iw].y = fma(uim, r, acc[i][j][iw].y);
+            const FF c = ff_of(__dsub_rn(wxr[i][iw], a[j]));  // wx - Re wtilde in FP64
+            const FF wv = ff_sq_add(c, fb2[j]);               // |wdiff|^2
+            bool near;
+            bool keep = ff_gt_quarter(wv, near);
+            if (near || (flag[j] & kFlagBinds)) keep = keep_fp64(wxr[i][iw], a[j], b[j]);
+            keep = keep && !(flag[j] & kFlagDead);
+            const FF r = ff_rcp_raw(wv);
+            const FF ux = ff_dot2_raw(rx, c, ry, fb[j]), uy = ff_dot2_raw(rx, fb[j], ff_neg(ry), c);
+            const FF sx = ff_mul_raw(ux, r), sy = ff_mul_raw(uy, r);
+            if (any_wide && wide) {
+              if (!(flag[j] & kFlagDead)) {
+                const int n1 = n1_0 + ty + TYN * i, ig = ig0 + k, my_igp = p0 + tx + TXN * j;
+                const double2 s = sch_term_fp64(p.aqsn, p.wt, p.ieps,
+                                                n1 < band_end ? (size_t)n1 * p.nc + ig : ~size_t(0),
+                                                (size_t)my_igp * p.nc + ig, wxr[i][iw]);
+                acc[i][j][iw].x += s.x;
+                acc[i][j][iw].y += s.y;
+              }
+            } else {
+              acc[i][j][iw].x += f32_widen(keep ? sx.hi : 0.f);
+              acc[i][j][iw].y += f32_widen(keep ? sy.hi : 0.f);
+              acl[i][j][iw].x += keep ? sx.lo : 0.f;
+              acl[i][j][iw].y += keep ? sy.lo : 0.f;
+            }
           }
         }
     }
   }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        acc[i][j][iw].x += f32_widen(acl[i][j][iw].x);
+        acc[i][j][iw].y += f32_widen(acl[i][j][iw].y);
+      }
 
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp], then a fixed-order
   // sum over the tile's columns
@@ -182,7 +265,7 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
 }
 
 template <int BN, int BP>
-__global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork w) {
+__global__ void __launch_bounds__(kThreads, 1) sch_fp64_kernel(GppDev p, GppWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   const int tid = threadIdx.x;
@@ -769,7 +852,7 @@ constexpr size_t kSchBatchSmem =
     sizeof(SchSmem<16, 64>) > sizeof(SchSmem<64, 16>) ? sizeof(SchSmem<16, 64>) : sizeof(SchSmem<64, 16>);
 static_assert(kSchBatchSmem >= sizeof(SchSmem<32, 32>), "batched smem covers every tile shape");
 
-__global__ void __launch_bounds__(kThreads, 2) sch_fp64_batch_kernel(GppBatchView b) {
+__global__ void __launch_bounds__(kThreads, 1) sch_fp64_batch_kernel(GppBatchView b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   const int tid = threadIdx.x;

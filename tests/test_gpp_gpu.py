@@ -127,14 +127,17 @@ def test_exact_poles_and_skipped_columns(sigma_lib, prec):
     _check(g, o, prec)
 
 
+@pytest.mark.parametrize("per_band", [False, True], ids=["shared-wx", "per-band-wx"])
 @pytest.mark.parametrize("kind", ["huge-elements", "tiny-ieps", "tiny-frequency"])
-def test_fp64_occupied_bands_outside_float_range(sigma_lib, kind):
-    """The FP64 occupied-band pass forms its factors in float-float (FP32
-    pairs) when wtilde, I_eps and the frequency lie within 2^+-20; other
-    elements take its FP64 fallback.  Elements with |wtilde| ~ 2^45 and
-    |I_eps| ~ 2^40 (FP32 would overflow), an I_eps scaled by 2^-110 (the low
-    FP32 halves would fall below the normal range) and a frequency of 1e-7
-    must all stay within the FP64 bar of 1e-12."""
+def test_fp64_outside_float_range(sigma_lib, kind, per_band):
+    """The FP64 passes form their factors (the per-band pass: its whole
+    terms) in float-float (FP32 pairs) when wtilde, I_eps, aqsn and the
+    frequency lie within 2^+-20; other elements take their FP64 fallback.
+    Elements with |wtilde| ~ 2^45 and |I_eps| ~ 2^40 (FP32 would overflow),
+    an I_eps scaled by 2^-110 (the low FP32 halves would fall below the
+    normal range) and a frequency of 1e-7 must all stay within the FP64 bar
+    of 1e-12, with one frequency set for all bands and with per-band
+    frequencies."""
     prob = W.gpp_random(24, 5, 1200, 40, 31)
     prob.wtilde_array = prob.wtilde_array.copy()
     prob.I_eps_array = prob.I_eps_array.copy()
@@ -147,8 +150,16 @@ def test_fp64_occupied_bands_outside_float_range(sigma_lib, kind):
         prob.I_eps_array *= 2.0 ** -110
     else:
         prob.wx_array = np.array([prob.wx_array[0], 1e-7, prob.wx_array[2]])
-    o = O.gpp(prob)
-    g = sigma_lib.gpp_host(prob, 0)
+    if per_band:
+        # the same three frequencies stored once per band (stride 3), shifted per band
+        wxb = np.repeat(prob.wx_array[None, :], prob.number_bands, 0)
+        wxb[:, [0, 2]] += np.linspace(-0.3, 0.3, prob.number_bands)[:, None]
+        wxb = np.ascontiguousarray(wxb).reshape(-1)
+        o = O.gpp(W.GppProblem(**{**prob.__dict__, "wx_array": wxb}), wx_band_stride=3)
+        g = _run_plan(sigma_lib, prob, 0, wx=wxb, wx_stride=3)[0]
+    else:
+        o = O.gpp(prob)
+        g = sigma_lib.gpp_host(prob, 0)
     for x in g:
         assert np.all(np.isfinite(x))
     assert np.any(o[1] != 0)
@@ -199,16 +210,40 @@ def _run_plan(S, prob, prec, wx=None, wx_stride=0, reps=1):
     return outs
 
 
+@pytest.mark.parametrize("stress", [False, True], ids=["random", "stress"])
 @pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
-def test_per_band_frequencies(sigma_lib, prec):
+def test_per_band_frequencies(sigma_lib, prec, stress):
     # frequencies that differ per band (ekq(n1) of the Fortran original,
     # gppkernel.deslippe.09.30.2014.f90:238): wx_array[n1][3], stride 3
-    prob = W.gpp_random(37, 3, 900, 29, 23)
+    prob = W.gpp_random(37, 3, 900, 29, 23, stress=stress)
     rng = np.random.default_rng(0)
     wxb = np.repeat(prob.wx_array[None, :], prob.number_bands, 0) + rng.uniform(-0.7, 0.7, (prob.number_bands, 1))
     wxb = np.ascontiguousarray(wxb)
     o = O.gpp(W.GppProblem(**{**prob.__dict__, "wx_array": wxb.reshape(-1)}), wx_band_stride=3)
     g = _run_plan(sigma_lib, prob, prec, wx=wxb.reshape(-1), wx_stride=3)[0]
+    _check(g, o, prec)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
+def test_per_band_exact_poles_and_guard_edges(sigma_lib, prec):
+    """Per-band frequencies with an exact pole of one band's frequency, a
+    term exactly on the |wdiff|^2 = 0.25 boundary, a zero wtilde and
+    |wtilde|^2 >= 62000 (the guard's second condition binding): the
+    per-band pass takes these decisions with the FP64 expressions."""
+    prob = W.gpp_random(21, 3, 700, 26, 27)
+    rng = np.random.default_rng(1)
+    wxb = np.repeat(prob.wx_array[None, :], prob.number_bands, 0) + rng.uniform(-0.5, 0.5, (prob.number_bands, 1))
+    prob.wtilde_array = prob.wtilde_array.copy()
+    prob.wtilde_array[2, 10] = complex(wxb[4, 0], 0.0)        # exact pole of band 4
+    prob.wtilde_array[5, 11] = complex(wxb[17, 2], 0.0)       # exact pole of band 17
+    prob.wtilde_array[7, 12] = complex(wxb[9, 1] + 0.5, 0.0)  # |wdiff|^2 = 0.25 for band 9
+    prob.wtilde_array[8, 13] = 0.0
+    prob.wtilde_array[9, 14] = complex(300.0, 0.5)
+    wxb = np.ascontiguousarray(wxb).reshape(-1)
+    o = O.gpp(W.GppProblem(**{**prob.__dict__, "wx_array": wxb}), wx_band_stride=3)
+    g = _run_plan(sigma_lib, prob, prec, wx=wxb, wx_stride=3)[0]
+    for x in g:
+        assert np.all(np.isfinite(x))
     _check(g, o, prec)
 
 
