@@ -18,7 +18,8 @@
 // float-float arithmetic (FP32 pairs on the FP32 pipe: G in FP64 per column
 // and g-vector, c = wx - Re wtilde in FP64 per term, the rest from exact
 // splits), its FP32 high half widened and added to an FP64 sum and its low
-// half to an FP32 sum: 3 FP64 operations per term instead of 10 (the FP64
+// half to an FP32 sum of one staged chunk, added to the FP64 sum at the
+// chunk's end: ~3 FP64 operations per term instead of 10 (the FP64
 // form had 8 per term plus 6 per band, column and g-vector).  A term's error
 // is about twice the FP64 form's, whose reciprocal is itself an FP32 seed
 // refined once (rcp_f64_seed32, within 2^-44.8).  conj(aqsm[n1][igp]), 0.5
@@ -100,8 +101,10 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
       wx_wide[i] = wx_wide[i] || !ff_freq_range(wxr[i][iw]);
     }
   }
-  // FP64 sums of the terms' high halves; their low halves summed in FP32
-  // (below 2^-23 of the terms) and added at the item's end
+  // FP64 sums of the terms' high halves; their low halves (below 2^-23 of
+  // the terms) summed in FP32 over one staged chunk and then added to the
+  // FP64 sums (an FP32 sum over a whole item's thousands of terms would lose
+  // ~n 2^-47 of the output)
   double2 acc[2][2][kNW];
   float2 acl[2][2][kNW];
 #pragma unroll
@@ -216,16 +219,17 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
           }
         }
     }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          acc[i][j][iw].x += f32_widen(acl[i][j][iw].x);
+          acc[i][j][iw].y += f32_widen(acl[i][j][iw].y);
+          acl[i][j][iw] = make_float2(0.f, 0.f);
+        }
   }
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) {
-        acc[i][j][iw].x += f32_widen(acl[i][j][iw].x);
-        acc[i][j][iw].y += f32_widen(acl[i][j][iw].y);
-      }
 
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp], then a fixed-order
   // sum over the tile's columns

@@ -224,6 +224,18 @@ def test_per_band_frequencies(sigma_lib, prec, stress):
     _check(g, o, prec)
 
 
+def test_per_band_frequencies_long_g_sums(sigma_lib):
+    """Per-band frequencies with 16384 g-vectors per column (items summing
+    thousands of float-float terms), FP64 at the 1e-12 bar."""
+    prob = W.gpp_random(64, 2, 16384, 160, 29)
+    rng = np.random.default_rng(2)
+    wxb = np.repeat(prob.wx_array[None, :], prob.number_bands, 0) + rng.uniform(-0.6, 0.6, (prob.number_bands, 1))
+    wxb = np.ascontiguousarray(wxb).reshape(-1)
+    o = O.gpp(W.GppProblem(**{**prob.__dict__, "wx_array": wxb}), wx_band_stride=3)
+    g = _run_plan(sigma_lib, prob, 0, wx=wxb, wx_stride=3)[0]
+    _check(g, o, 0)
+
+
 @pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "mixed"])
 def test_per_band_exact_poles_and_guard_edges(sigma_lib, prec):
     """Per-band frequencies with an exact pole of one band's frequency, a
