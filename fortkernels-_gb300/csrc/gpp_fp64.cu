@@ -269,7 +269,7 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
 }
 
 template <int BN, int BP>
-__global__ void __launch_bounds__(kThreads, 1) sch_fp64_kernel(GppDev p, GppWork w) {
+__global__ void __launch_bounds__(kThreads, 2) sch_fp64_kernel(GppDev p, GppWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   const int tid = threadIdx.x;
