@@ -320,10 +320,11 @@ constexpr int kCKY = 16;  // g-vectors per staged chunk
 // are multiples of 128 bytes, put a warp's writes in one bank group.
 template <int BN, int BP>
 struct SchYSmem {
-  double2 y[kCKY][kNW * BP + 1];  // [k][iw * BP + column]
-  double ys[kCKY][kNW * BP + 1];  // Y.x + Y.y
-  double2 n[kCKY][BN + 1];
-  double ns[kCKY][BN + 1];        // n.x + n.y
+  float4 yf[kCKY][kNW * BP + 1];  // [k][iw * BP + column]: Y as float-float (x.hi, x.lo, y.hi, y.lo)
+  float4 nf[kCKY][BN + 1];        // aqsn as float-float
+  double2 y[kCKY][kNW * BP + 1];  // Y in FP64, for chunks with an input outside the float-float range
+  double2 n[kCKY][BN + 1];        // aqsn in FP64, for the same chunks
+  unsigned char wide[kCKY][BP];   // factor formed by the FP64 fallback
 };
 
 // Bounded wait for a gate word written by a host-to-device copy (`polls`
@@ -343,10 +344,10 @@ __device__ __forceinline__ bool wait_ready(const unsigned* flag, unsigned epoch,
 }
 
 // The FP64 form of one element's three factors, for elements outside the
-// float-float range, out of line: Y of frequency iw and Y.x + Y.y are
-// stored at y[iw * stride] and ys[iw * stride].
+// float-float range, out of line: Y of frequency iw is stored at
+// y[iw * stride] in FP64 and at yf[iw * stride] as a float-float pair.
 static __device__ __noinline__ void sch_factor_fp64(double2 wt, double2 ie, double wx0, double wx1, double wx2,
-                                                    double2* y, double* ys, int stride) {
+                                                    double2* y, float4* yf, int stride) {
   const double2 g = cmul(ie, wt);
   const double b = wt.y, b2 = guard_b2(b);
   const double thr = guard_thr(wt.x, b2);
@@ -357,8 +358,9 @@ static __device__ __noinline__ void sch_factor_fp64(double2 wt, double2 ie, doub
     const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
     const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
     const double2 v = make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
+    const FF vx = ff_of(v.x), vy = ff_of(v.y);
     y[iw * stride] = v;
-    ys[iw * stride] = __dadd_rn(v.x, v.y);
+    yf[iw * stride] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
   }
 }
 
@@ -395,16 +397,23 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
   const bool wx_wide = !(ff_freq_range(wx0) && ff_freq_range(wx1) && ff_freq_range(wx2));
 
-  double p1[TB][TC][kNW], p2[TB][TC][kNW], p3[TB][TC][kNW];
+  // FP64 sums of the terms' FP32 high halves; FP32 sums of their low halves
+  // over one staged chunk, added to the FP64 sums at the chunk's end
+  double2 acc[TB][TC][kNW];
+  float2 acl[TB][TC][kNW];
 #pragma unroll
   for (int i = 0; i < TB; ++i)
 #pragma unroll
     for (int j = 0; j < TC; ++j)
 #pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) p1[i][j][iw] = p2[i][j][iw] = p3[i][j][iw] = 0.0;
+      for (int iw = 0; iw < kNW; ++iw) {
+        acc[i][j][iw] = make_double2(0.0, 0.0);
+        acl[i][j][iw] = make_float2(0.f, 0.f);
+      }
 
   for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCKY) {
     __syncthreads();
+    bool chunk_wide = false;  // an input of the chunk outside the float-float range
     // frequency factors of the chunk's (g-vector, column) pairs; reads run
     // along g-vectors
     for (int e = tid; e < kCKY * BP; e += kThreads) {
@@ -429,7 +438,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       // |wtilde|^2 * 4e-6 > 0.25 needs |wtilde|^2 > 62500
       const float ah = ff_of(wt.x).hi;
       const bool thr2_binds = fmaf(ah, ah, fb.hi * fb.hi) >= 62000.f;
-      double2 y[kNW];
+      float4 y[kNW];
       unsigned keep = 0u, rare = 0u;
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) {
@@ -440,20 +449,20 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         rare |= (near || thr2_binds) ? (1u << iw) : 0u;
         const FF r = ff_rcp_raw(wv);
         const FF ux = ff_dot2_raw(gx, c, gy, fb), uy = ff_dot2_raw(gx, fb, ff_neg(gy), c);
-        y[iw] = make_double2(ff_widen(ff_mul_raw(ux, r)), ff_widen(ff_mul_raw(uy, r)));
+        const FF yx = ff_mul_raw(ux, r), yy = ff_mul_raw(uy, r);
+        y[iw] = make_float4(yx.hi, yx.lo, yy.hi, yy.lo);
       }
       if (rare) keep = sch_keep_rare(keep, rare, wx0, wx1, wx2, wt.x, wt.y);
       if (!valid) keep = 0u;
       const bool wide = valid && (wx_wide || !(ff_range(wt.x, wt.y) && ff_range(ie.x, ie.y)));
+      sm.wide[k][pl] = wide;
       if (__any_sync(0xffffffffu, wide) && wide) {
-        sch_factor_fp64(wt, ie, wx0, wx1, wx2, &sm.y[k][pl], &sm.ys[k][pl], BP);
+        sch_factor_fp64(wt, ie, wx0, wx1, wx2, &sm.y[k][pl], &sm.yf[k][pl], BP);
+        chunk_wide = true;
       } else {
 #pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) {
-          const double2 v = (keep >> iw) & 1u ? y[iw] : make_double2(0.0, 0.0);
-          sm.y[k][iw * BP + pl] = v;
-          sm.ys[k][iw * BP + pl] = __dadd_rn(v.x, v.y);
-        }
+        for (int iw = 0; iw < kNW; ++iw)
+          sm.yf[k][iw * BP + pl] = (keep >> iw) & 1u ? y[iw] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
     for (int e = tid; e < kCKY * BN; e += kThreads) {
@@ -461,37 +470,85 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       const int ig = ig0 + k, n1 = n1_0 + bl;
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
+      const FF nx = ff_of(v.x), ny = ff_of(v.y);
+      sm.nf[k][bl] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
       sm.n[k][bl] = v;
-      sm.ns[k][bl] = __dadd_rn(v.x, v.y);
+      chunk_wide = chunk_wide || !ff_range(v.x, v.y);
     }
-    __syncthreads();
+    chunk_wide = __syncthreads_or(chunk_wide);
 
-#pragma unroll 2
-    for (int k = 0; k < kCKY; ++k) {
-      double2 nn[TB], y[TC][kNW];
-      double nsum[TB], ysum[TC][kNW];
+    if (!chunk_wide) {
+      // every term n Y as a float-float product on the FP32 pipe, its high
+      // half widened on the integer pipe and added in FP64 (2 FP64
+      // operations per term), its low half added in FP32
+#pragma unroll 1
+      for (int k = 0; k < kCKY; ++k) {
+        FF nx[TB], ny[TB], yx[TC][kNW], yy[TC][kNW];
 #pragma unroll
-      for (int i = 0; i < TB; ++i) {
-        nn[i] = sm.n[k][ty + 16 * i];
-        nsum[i] = sm.ns[k][ty + 16 * i];
-      }
-#pragma unroll
-      for (int j = 0; j < TC; ++j)
-#pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) {
-          y[j][iw] = sm.y[k][iw * BP + tx + 16 * j];
-          ysum[j][iw] = sm.ys[k][iw * BP + tx + 16 * j];
+        for (int i = 0; i < TB; ++i) {
+          const float4 v = sm.nf[k][ty + 16 * i];
+          nx[i] = FF{v.x, v.y};
+          ny[i] = FF{v.z, v.w};
         }
+#pragma unroll
+        for (int j = 0; j < TC; ++j)
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            const float4 v = sm.yf[k][iw * BP + tx + 16 * j];
+            yx[j][iw] = FF{v.x, v.y};
+            yy[j][iw] = FF{v.z, v.w};
+          }
+#pragma unroll
+        for (int i = 0; i < TB; ++i)
+#pragma unroll
+          for (int j = 0; j < TC; ++j)
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const FF tr = ff_dot2_raw(nx[i], yx[j][iw], ny[i], yy[j][iw]);
+              const FF ti = ff_dot2_raw(nx[i], yy[j][iw], ff_neg(ny[i]), yx[j][iw]);
+              acc[i][j][iw].x += f32_widen(tr.hi);
+              acc[i][j][iw].y += f32_widen(ti.hi);
+              acl[i][j][iw].x += tr.lo;
+              acl[i][j][iw].y += ti.lo;
+            }
+      }
 #pragma unroll
       for (int i = 0; i < TB; ++i)
 #pragma unroll
         for (int j = 0; j < TC; ++j)
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            p1[i][j][iw] = fma(nn[i].x, y[j][iw].x, p1[i][j][iw]);
-            p2[i][j][iw] = fma(nn[i].y, y[j][iw].y, p2[i][j][iw]);
-            p3[i][j][iw] = fma(nsum[i], ysum[j][iw], p3[i][j][iw]);
+            acc[i][j][iw].x += f32_widen(acl[i][j][iw].x);
+            acc[i][j][iw].y += f32_widen(acl[i][j][iw].y);
+            acl[i][j][iw] = make_float2(0.f, 0.f);
           }
+    } else {
+      // a chunk with an input outside the float-float range: FP64 factors
+      // (those of the in-range elements widened) and FP64 multiply-adds
+      for (int e = tid; e < kCKY * BP; e += kThreads) {
+        const int k = e % kCKY, pl = e / kCKY;
+        if (!sm.wide[k][pl]) {
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            const float4 v = sm.yf[k][iw * BP + pl];
+            sm.y[k][iw * BP + pl] = make_double2(ff_widen(FF{v.x, v.y}), ff_widen(FF{v.z, v.w}));
+          }
+        }
+      }
+      __syncthreads();
+      for (int k = 0; k < kCKY; ++k)
+#pragma unroll
+        for (int i = 0; i < TB; ++i) {
+          const double2 nn = sm.n[k][ty + 16 * i];
+#pragma unroll
+          for (int j = 0; j < TC; ++j)
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const double2 yv = sm.y[k][iw * BP + tx + 16 * j];
+              acc[i][j][iw].x = fma(nn.x, yv.x, fma(-nn.y, yv.y, acc[i][j][iw].x));
+              acc[i][j][iw].y = fma(nn.x, yv.y, fma(nn.y, yv.x, acc[i][j][iw].y));
+            }
+        }
     }
   }
 
@@ -518,9 +575,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         const double f = 0.5 * p.vcoul[igp];
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          const double re = __dsub_rn(p1[i][j][iw], p2[i][j][iw]);
-          const double im = __dsub_rn(__dsub_rn(p3[i][j][iw], p1[i][j][iw]), p2[i][j][iw]);
-          const double2 v = cmul(make_double2(re, im), m);
+          const double2 v = cmul(acc[i][j][iw], m);
           part[iw].x = fma(v.x, f, part[iw].x);
           part[iw].y = fma(v.y, f, part[iw].y);
         }
@@ -541,7 +596,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
 }
 
 template <int BN, int BP>
-__global__ void __launch_bounds__(kThreads, 1) sch_fp64y_kernel(GppDev p, GppWork w) {
+__global__ void __launch_bounds__(kThreads, 2) sch_fp64y_kernel(GppDev p, GppWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   const int tid = threadIdx.x;

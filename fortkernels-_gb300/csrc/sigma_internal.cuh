@@ -88,7 +88,7 @@ constexpr int kBP = 32;    // columns (my_igp) per FP64 sch tile
 constexpr int kBPM = 16;   // columns per mixed sch tile
 constexpr int kCK = 32;    // g-vectors per staged chunk
 constexpr int kThreads = 256;
-constexpr int kBNY = 128;  // bands per FP64 item when the frequencies are shared
+constexpr int kBNY = 64;   // bands per FP64 item when the frequencies are shared
 constexpr int kBPY = 16;   // columns per FP64 item when the frequencies are shared
 constexpr int kSsxBN = 4;   // bands per occupied-band item
 constexpr int kSsxBP = 256; // columns per occupied-band item, one per thread
