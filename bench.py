@@ -16,8 +16,8 @@ device.  One step = one full evaluation of achtemp / asxtemp / acht_n1_loc.
              the relative error of every achtemp / asxtemp output against the
              FP64 path (and on the stress fill with 5% near-pole wtilde)
   roofline   the main FP64 kernel (sch_fp64y_kernel): the FP64 pipe work its
-             algorithm issues per term (2.16 operations: the FP64 sums of each
-             float-float term plus the shared frequency factor) over
+             algorithm issues per term (1.34 operations: the FP64 sums of the
+             float-float terms plus the shared frequency factor) over
              its CUDA-event time, against the FP64 pipe peak (2 DFMA / clk / SM
              at the SM clock sampled during the timed region); the reference's
              27 flop per term is reported beside it as a rate
@@ -299,12 +299,13 @@ def timed(torch, dist, world, fn, steps, stream):
 
 
 # FP64 pipe operations of sch_fp64y_kernel per term, counted from its
-# algorithm: 2 FP64 additions (the float-float term's high half into the
-# FP64 sums of its real and imaginary parts) + the fold of the low halves'
-# FP32 sums into the FP64 sums once per 16-g-vector chunk (2 per 16 terms) +
-# the shared frequency factor (per column and g-vector: G and the three
-# c = wx - Re wtilde in FP64, 7, over 64 bands x 3 frequencies = 192 terms).
-FP64_PIPE_OPS_PER_TERM = 2.0 + 2.0 / 16 + 7.0 / 192
+# algorithm: 1 FP64 addition (the exact sum of two g-vectors' float-float
+# terms' high halves, widened, into the FP64 sums of the real and imaginary
+# parts: 2 per 2 terms) + the fold of the low halves' FP32 sums into the FP64
+# sums once per 16-g-vector chunk (2 per 16 terms) + the shared frequency
+# factor in FP64 (~41 per column and g-vector over 64 bands x 3 frequencies
+# = 192 terms).
+FP64_PIPE_OPS_PER_TERM = 1.0 + 2.0 / 16 + 41.0 / 192
 # ncu, sch_fp64y_kernel, 128-band capture of the production instance
 # (--set full): dram__bytes_read.sum + dram__bytes_write.sum per term, and
 # sm__pipe_fp64_cycles_active over elapsed cycles.  Traffic scales with the
@@ -946,10 +947,11 @@ def run_ours(args, rank, world, local_rank):
                                              "term rate: a rate, not a pipe fraction"},
                      "note": "achieved = FP64 pipe work of the kernel's own algorithm (each FP64 pipe "
                              "instruction counted as one DFMA slot, 2 flop): with one frequency set for all "
-                             "bands the frequency factor is formed once per column and g-vector; every term "
-                             "is formed as a float-float product on the FP32 pipe and summed in FP64 (its "
-                             "high half widened and added, its low half summed in FP32 per 16-g-vector "
-                             "chunk and then added); traffic = ncu DRAM bytes per term x terms"},
+                             "bands the frequency factor is formed in FP64 once per column and g-vector; "
+                             "every term is formed as a float-float product on the FP32 pipe, the high "
+                             "halves of two g-vectors' terms added exactly and the sum added in FP64, the "
+                             "low halves and rounding errors summed in FP32 per 16-g-vector chunk and then "
+                             "added; traffic = ncu DRAM bytes per term x terms"},
         "rel_err_vs_oracle": oracle,
         "mixed": {"value": round(mixed_value, 4), "unit": UNIT,
                   "speedup_vs_fp64": round(mixed_value / value, 3),

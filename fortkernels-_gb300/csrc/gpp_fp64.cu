@@ -322,9 +322,8 @@ template <int BN, int BP>
 struct SchYSmem {
   float4 yf[kCKY][kNW * BP + 1];  // [k][iw * BP + column]: Y as float-float (x.hi, x.lo, y.hi, y.lo)
   float4 nf[kCKY][BN + 1];        // aqsn as float-float
-  double2 y[kCKY][kNW * BP + 1];  // Y in FP64, for chunks with an input outside the float-float range
+  double2 y[kCKY][kNW * BP + 1];  // Y in FP64, for chunks with a value outside the float-float range
   double2 n[kCKY][BN + 1];        // aqsn in FP64, for the same chunks
-  unsigned char wide[kCKY][BP];   // factor formed by the FP64 fallback
 };
 
 // Bounded wait for a gate word written by a host-to-device copy (`polls`
@@ -341,37 +340,6 @@ __device__ __forceinline__ bool wait_ready(const unsigned* flag, unsigned epoch,
   }
   atomicCAS(status, 0, (int)SIGMA_ERR_TIMEOUT);
   return false;
-}
-
-// The FP64 form of one element's three factors, for elements outside the
-// float-float range, out of line: Y of frequency iw is stored at
-// y[iw * stride] in FP64 and at yf[iw * stride] as a float-float pair.
-static __device__ __noinline__ void sch_factor_fp64(double2 wt, double2 ie, double wx0, double wx1, double wx2,
-                                                    double2* y, float4* yf, int stride) {
-  const double2 g = cmul(ie, wt);
-  const double b = wt.y, b2 = guard_b2(b);
-  const double thr = guard_thr(wt.x, b2);
-  const double wx[kNW] = {wx0, wx1, wx2};
-  for (int iw = 0; iw < kNW; ++iw) {
-    const double c = __dsub_rn(wx[iw], wt.x);
-    const double wv = fma(c, c, b2);
-    const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
-    const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
-    const double2 v = make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
-    const FF vx = ff_of(v.x), vy = ff_of(v.y);
-    y[iw * stride] = v;
-    yf[iw * stride] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
-  }
-}
-
-// Keep decisions of the frequencies in `rare` (bits 0-2) re-taken with the
-// FP64 path's expressions; out of line.
-static __device__ __noinline__ unsigned sch_keep_rare(unsigned keep, unsigned rare, double wx0, double wx1,
-                                                      double wx2, double a, double b) {
-  const double wx[kNW] = {wx0, wx1, wx2};
-  for (int iw = 0; iw < kNW; ++iw)
-    if ((rare >> iw) & 1u) keep = (keep & ~(1u << iw)) | (keep_fp64(wx[iw], a, b) ? (1u << iw) : 0u);
-  return keep;
 }
 
 template <int BN, int BP>
@@ -395,7 +363,6 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const int ig_begin = ic.s * w.split_len;
   const int ig_end = min(ig_begin + w.split_len, p.nc);
   const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
-  const bool wx_wide = !(ff_freq_range(wx0) && ff_freq_range(wx1) && ff_freq_range(wx2));
 
   // FP64 sums of the terms' FP32 high halves; FP32 sums of their low halves
   // over one staged chunk, added to the FP64 sums at the chunk's end
@@ -426,43 +393,24 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         wt = p.wt[off];
         ie = p.ieps[off];
       }
-      // Y = G (c + i b) r, G = I_eps wtilde, c = wx - Re wtilde, b = Im wtilde;
-      // G and c in FP64 and split (4 + 3 FP64 operations): c = wx - a
-      // cancels near the poles, where a split of a's 2^-48 error would
-      // be amplified (~15 times the FP64 form's error in Y; with these
-      // two in FP64, ~1.8 times, from a float-float emulation of the
-      // element)
+      // Y = G (c + i b) r in FP64 (~41 FP64 operations per column and
+      // g-vector, shared by the item's 64 bands x 3 frequencies), staged in
+      // FP64 and split as float-float pairs for the terms; the pole guard
+      // is the int64 compare against the per-element threshold
       const double2 g = cmul(ie, wt);
-      const FF fb = ff_of(wt.y), gx = ff_of(g.x), gy = ff_of(g.y);
-      const FF b2 = ff_mul_raw(fb, fb);
-      // |wtilde|^2 * 4e-6 > 0.25 needs |wtilde|^2 > 62500
-      const float ah = ff_of(wt.x).hi;
-      const bool thr2_binds = fmaf(ah, ah, fb.hi * fb.hi) >= 62000.f;
-      float4 y[kNW];
-      unsigned keep = 0u, rare = 0u;
+      const double b = wt.y, b2 = guard_b2(b);
+      const double thr = valid ? guard_thr(wt.x, b2) : __longlong_as_double(0x7ff0000000000000LL);
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) {
-        const FF c = ff_of(__dsub_rn(iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2), wt.x));
-        const FF wv = ff_sq_add(c, b2);  // |wdiff|^2
-        bool near;
-        keep |= ff_gt_quarter(wv, near) ? (1u << iw) : 0u;
-        rare |= (near || thr2_binds) ? (1u << iw) : 0u;
-        const FF r = ff_rcp_raw(wv);
-        const FF ux = ff_dot2_raw(gx, c, gy, fb), uy = ff_dot2_raw(gx, fb, ff_neg(gy), c);
-        const FF yx = ff_mul_raw(ux, r), yy = ff_mul_raw(uy, r);
-        y[iw] = make_float4(yx.hi, yx.lo, yy.hi, yy.lo);
-      }
-      if (rare) keep = sch_keep_rare(keep, rare, wx0, wx1, wx2, wt.x, wt.y);
-      if (!valid) keep = 0u;
-      const bool wide = valid && (wx_wide || !(ff_range(wt.x, wt.y) && ff_range(ie.x, ie.y)));
-      sm.wide[k][pl] = wide;
-      if (__any_sync(0xffffffffu, wide) && wide) {
-        sch_factor_fp64(wt, ie, wx0, wx1, wx2, &sm.y[k][pl], &sm.yf[k][pl], BP);
-        chunk_wide = true;
-      } else {
-#pragma unroll
-        for (int iw = 0; iw < kNW; ++iw)
-          sm.yf[k][iw * BP + pl] = (keep >> iw) & 1u ? y[iw] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const double c = __dsub_rn(iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2), wt.x);
+        const double wv = fma(c, c, b2);
+        const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
+        const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
+        const double2 v = make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
+        const FF vx = ff_of(v.x), vy = ff_of(v.y);
+        sm.y[k][iw * BP + pl] = v;
+        sm.yf[k][iw * BP + pl] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
+        chunk_wide = chunk_wide || !ff_range(v.x, v.y);
       }
     }
     for (int e = tid; e < kCKY * BN; e += kThreads) {
@@ -478,39 +426,45 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
     chunk_wide = __syncthreads_or(chunk_wide);
 
     if (!chunk_wide) {
-      // every term n Y as a float-float product on the FP32 pipe, its high
-      // half widened on the integer pipe and added in FP64 (2 FP64
-      // operations per term), its low half added in FP32
+      // every term n Y as a float-float product on the FP32 pipe; the high
+      // halves of two g-vectors' terms added exactly (TwoSum), the sum
+      // widened on the integer pipe and added in FP64 (1 FP64 operation
+      // per term), the rounding error and the low halves added in FP32
+      static_assert(kCKY % 2 == 0, "g-vector pairs");
 #pragma unroll 1
-      for (int k = 0; k < kCKY; ++k) {
-        FF nx[TB], ny[TB], yx[TC][kNW], yy[TC][kNW];
+      for (int k = 0; k < kCKY; k += 2) {
+        FF yx[2][TC][kNW], yy[2][TC][kNW];
 #pragma unroll
-        for (int i = 0; i < TB; ++i) {
-          const float4 v = sm.nf[k][ty + 16 * i];
-          nx[i] = FF{v.x, v.y};
-          ny[i] = FF{v.z, v.w};
-        }
-#pragma unroll
-        for (int j = 0; j < TC; ++j)
-#pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) {
-            const float4 v = sm.yf[k][iw * BP + tx + 16 * j];
-            yx[j][iw] = FF{v.x, v.y};
-            yy[j][iw] = FF{v.z, v.w};
-          }
-#pragma unroll
-        for (int i = 0; i < TB; ++i)
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
           for (int j = 0; j < TC; ++j)
 #pragma unroll
             for (int iw = 0; iw < kNW; ++iw) {
-              const FF tr = ff_dot2_raw(nx[i], yx[j][iw], ny[i], yy[j][iw]);
-              const FF ti = ff_dot2_raw(nx[i], yy[j][iw], ff_neg(ny[i]), yx[j][iw]);
-              acc[i][j][iw].x += f32_widen(tr.hi);
-              acc[i][j][iw].y += f32_widen(ti.hi);
-              acl[i][j][iw].x += tr.lo;
-              acl[i][j][iw].y += ti.lo;
+              const float4 v = sm.yf[k + h][iw * BP + tx + 16 * j];
+              yx[h][j][iw] = FF{v.x, v.y};
+              yy[h][j][iw] = FF{v.z, v.w};
             }
+#pragma unroll
+        for (int i = 0; i < TB; ++i) {
+          const float4 v0 = sm.nf[k][ty + 16 * i], v1 = sm.nf[k + 1][ty + 16 * i];
+          const FF nx[2] = {FF{v0.x, v0.y}, FF{v1.x, v1.y}}, ny[2] = {FF{v0.z, v0.w}, FF{v1.z, v1.w}};
+#pragma unroll
+          for (int j = 0; j < TC; ++j)
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const FF r0 = ff_dot2_raw(nx[0], yx[0][j][iw], ny[0], yy[0][j][iw]);
+              const FF i0 = ff_dot2_raw(nx[0], yy[0][j][iw], ff_neg(ny[0]), yx[0][j][iw]);
+              const FF r1 = ff_dot2_raw(nx[1], yx[1][j][iw], ny[1], yy[1][j][iw]);
+              const FF i1 = ff_dot2_raw(nx[1], yy[1][j][iw], ff_neg(ny[1]), yx[1][j][iw]);
+              float sr, er, si, ei;
+              two_sum_f(r0.hi, r1.hi, sr, er);
+              two_sum_f(i0.hi, i1.hi, si, ei);
+              acc[i][j][iw].x += f32_widen(sr);
+              acc[i][j][iw].y += f32_widen(si);
+              acl[i][j][iw].x += (er + r0.lo) + r1.lo;
+              acl[i][j][iw].y += (ei + i0.lo) + i1.lo;
+            }
+        }
       }
 #pragma unroll
       for (int i = 0; i < TB; ++i)
@@ -523,19 +477,8 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
             acl[i][j][iw] = make_float2(0.f, 0.f);
           }
     } else {
-      // a chunk with an input outside the float-float range: FP64 factors
-      // (those of the in-range elements widened) and FP64 multiply-adds
-      for (int e = tid; e < kCKY * BP; e += kThreads) {
-        const int k = e % kCKY, pl = e / kCKY;
-        if (!sm.wide[k][pl]) {
-#pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) {
-            const float4 v = sm.yf[k][iw * BP + pl];
-            sm.y[k][iw * BP + pl] = make_double2(ff_widen(FF{v.x, v.y}), ff_widen(FF{v.z, v.w}));
-          }
-        }
-      }
-      __syncthreads();
+      // a chunk with a factor or an aqsn element outside the float-float
+      // range: FP64 multiply-adds on the FP64 copies
       for (int k = 0; k < kCKY; ++k)
 #pragma unroll
         for (int i = 0; i < TB; ++i) {
