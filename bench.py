@@ -310,8 +310,8 @@ FP64_PIPE_OPS_PER_TERM = 1.0 + 2.0 / 16 + 41.0 / 192
 # (--set full): dram__bytes_read.sum + dram__bytes_write.sum per term, and
 # sm__pipe_fp64_cycles_active over elapsed cycles.  Traffic scales with the
 # band blocks, so the per-term figure carries to the 512-band launch.
-FP64_DRAM_BYTES_PER_TERM = 0.1696
-FP64_PIPE_ACTIVE_NCU = 0.819
+FP64_DRAM_BYTES_PER_TERM = 0.1957
+FP64_PIPE_ACTIVE_NCU = 0.719
 # FP32 pipe operations of sch_mixedy_kernel per term: 4 FFMA (complex
 # multiply-add) + the float-float fold of each accumulator every 8 g-vectors
 # (2 x 7 operations / 8) + the shared frequency factor (~10 per column,
