@@ -4,7 +4,8 @@ Tiles.
 Each work item of the main pass covers a (band block x column block x
 g-vector split) tile.  Two kernel families are compiled: the shared-frequency kernel (every band uses the same three
 frequencies, the mini-app's case): 64 bands x 32 columns, 32 x 64, 32 x 32,
-128 x 16 (tiles 3, 4, 5, 6); and the per-band-frequency kernel: 32 x 32,
+64 x 16 (tiles 3, 4, 5, 6; a batch whose instances all take 5 or 6 runs two
+CTAs per SM); and the per-band-frequency kernel: 32 x 32,
 16 x 64, 64 x 16 (tiles 0, 1, 2).  Which shape is fastest depends on how the
 instance's number_bands and ngpown pad to the block sizes and on how much
 staged data each item re-reads, so the choice is made per shape class:
@@ -41,7 +42,7 @@ import pathlib
 
 PKG = pathlib.Path(__file__).resolve().parent
 TABLE = PKG / "tuning" / "gpp_tiles_gb300.json"
-TILES = {0: "32x32", 1: "16x64", 2: "64x16", 3: "y64x32", 4: "y32x64", 5: "y32x32", 6: "y128x16"}
+TILES = {0: "32x32", 1: "16x64", 2: "64x16", 3: "y64x32", 4: "y32x64", 5: "y32x32", 6: "y64x16"}
 FAMILIES = {"shared": (3, 4, 5, 6), "per_band": (0, 1, 2)}
 TABLE_KEY = {"shared": "classes", "per_band": "classes_per_band"}
 _table = None

@@ -117,7 +117,7 @@ namespace {
 
 constexpr int kItemsPerSlot = 48;       // work items per resident CTA (load balance of the tail)
 constexpr int kItemsPerSlotMixed = 12;  // mixed items are 64x cheaper: fewer, longer items
-constexpr int kItemsPerSlotY = 24;      // shared-frequency FP64 items (128 x 16 tiles, 1 CTA per SM)
+constexpr int kItemsPerSlotY = 24;      // shared-frequency FP64 items (64 x 16 tiles, 2 CTAs per SM)
 constexpr int kItemsPerSlotMY = 12;     // shared-frequency mixed items (64 x 32 tiles, 1 CTA per SM)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }

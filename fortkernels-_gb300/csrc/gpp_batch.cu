@@ -52,6 +52,7 @@ struct sigma_gpp_batch_s {
   int sch_grid = 0, ssx_grid = 0, launches = 0;
   int tensor_split_tiles = 0;  // K' tiles per contraction item, every instance (0: each sized as its plan)
   bool all_shared_wx = true;  // every instance has one frequency set for all bands
+  bool fp64y_small = false;   // the shared-frequency FP64 pass runs its two-CTA kernel
   bool mixedy = false;        // mixed main pass on the shared-factor kernel
   void* block = nullptr;
   sigma::GppBatchView sch_view{}, ssx_view{};
@@ -377,9 +378,20 @@ extern "C" int sigma_gpp_batch_create_tuned(sigma_gpp_batch* out, int n_instance
   // mixed with one frequency set per instance: the shared-factor kernel
   const bool mixedy = precision == SIGMA_PREC_MIXED && all_shared;
   b->mixedy = mixedy;
+  // FP64 tiles first: the shared-frequency pass runs two CTAs per SM when
+  // every instance takes a tile of 12 outputs per thread
+  b->tile.resize(n_instances);
+  for (int i = 0; i < n_instances; ++i)
+    b->tile[i] = mixed ? kTile32x32
+                       : (tile_shape && tile_shape[i] >= 0
+                              ? tile_shape[i]
+                              : least_padding_tile(inst[i].number_bands, inst[i].ngpown, all_shared));
+  b->fp64y_small = !mixed && all_shared;
+  for (int i = 0; i < n_instances && b->fp64y_small; ++i)
+    b->fp64y_small = b->tile[i] == kTileY32x32 || b->tile[i] == kTileY64x16;
   b->sch_grid = sms * (mixedy ? sch_batch_blocks_per_sm_mixedy()
                               : mixed ? sch_batch_blocks_per_sm_mixed()
-                                      : (all_shared ? sch_batch_blocks_per_sm_fp64y()
+                                      : (all_shared ? sch_batch_blocks_per_sm_fp64y(b->fp64y_small)
                                                     : sch_batch_blocks_per_sm_fp64()));
   b->ssx_grid = sms * (mixed ? ssx_batch_blocks_per_sm_mixed() : ssx_batch_blocks_per_sm_fp64());
   b->dev.resize(n_instances);
@@ -387,7 +399,6 @@ extern "C" int sigma_gpp_batch_create_tuned(sigma_gpp_batch* out, int n_instance
   b->ssx.resize(n_instances);
   b->prep.resize(n_instances);
   b->prepw.resize(n_instances);
-  b->tile.resize(n_instances);
   b->acht_n1.resize(n_instances);
   b->sch_off.assign(n_instances + 1, 0);
   b->ssx_off.assign(n_instances + 1, 0);
@@ -406,11 +417,7 @@ extern "C" int sigma_gpp_batch_create_tuned(sigma_gpp_batch* out, int n_instance
   size_t total = 256;  // counters
   for (int i = 0; i < n_instances; ++i) {
     const sigma_gpp_instance& q = inst[i];
-    const int t = mixed ? kTile32x32
-                        : (tile_shape && tile_shape[i] >= 0
-                               ? tile_shape[i]
-                               : least_padding_tile(q.number_bands, q.ngpown, all_shared));
-    b->tile[i] = t;
+    const int t = b->tile[i];
     const int bn = mixedy ? 2 * kBN : (mixed ? kBN : tile_bn(t));
     const int bp = mixedy ? 2 * kBPM : (mixed ? kBPM : tile_bp(t));
     size_instance(b->sch[i], q.number_bands, bn, bp, q.ncouls, q.ngpown, target);
@@ -638,7 +645,7 @@ extern "C" int sigma_gpp_batch_execute(sigma_gpp_batch b, void* stream) {
   } else if (b->sch_view.total > 0)
     SIGMA_CUDA_TRY(b->mixedy ? launch_sch_mixedy_batch(b->sch_view, b->sch_grid, s)
                    : mixed ? launch_sch_mixed_batch(b->sch_view, b->sch_grid, s)
-                         : (b->all_shared_wx ? launch_sch_fp64y_batch(b->sch_view, b->sch_grid, s)
+                         : (b->all_shared_wx ? launch_sch_fp64y_batch(b->sch_view, b->sch_grid, b->fp64y_small, s)
                                              : launch_sch_fp64_batch(b->sch_view, b->sch_grid, s)));
   if (b->ssx_view.total > 0)
     SIGMA_CUDA_TRY(mixed ? launch_ssx_mixed_batch(b->ssx_view, b->ssx_grid, b->all_shared_wx, s)

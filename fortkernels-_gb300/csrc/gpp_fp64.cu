@@ -558,15 +558,34 @@ __global__ void __launch_bounds__(kThreads, 2) sch_fp64y_kernel(GppDev p, GppWor
 
 constexpr size_t smax(size_t a, size_t b) { return a > b ? a : b; }
 constexpr size_t kSchYBatchSmem =
-    smax(smax(sizeof(SchYSmem<64, 32>), sizeof(SchYSmem<32, 64>)), sizeof(SchYSmem<128, 16>));
+    smax(smax(sizeof(SchYSmem<64, 32>), sizeof(SchYSmem<32, 64>)), sizeof(SchYSmem<64, 16>));
+// the two-CTA kernel's tiles (32 x 32 and 64 x 16: 12 outputs per thread)
+constexpr size_t kSchYBatchSmallSmem = smax(sizeof(SchYSmem<32, 32>), sizeof(SchYSmem<64, 16>));
 
 // Item of an instance's shared-frequency pass with tile t: the last band
 // block runs the shortest item (a multiple of 16 bands) that holds its
 // remaining bands (less padded work; the slot layout stays the tile's).
+// kSmall: only the tiles of 12 outputs per thread (32 x 32, 64 x 16), for
+// the kernel that runs two CTAs per SM.
+template <bool kSmall>
 __device__ __forceinline__ void sch_fp64y_batch_item(const GppDev& p, const GppWork& w, int tile, int local,
                                                      unsigned char* smem_raw, int tid) {
   const ItemCoord ic = decode_item(w, local);
   const int slabs = (min(w.band_count - ic.bb * w.bn, w.bn) + 15) / 16;  // 16-band slabs of this block
+  if constexpr (kSmall) {
+    if (tile == kTileY32x32) {
+      if (slabs == 1) sch_fp64y_item<16, 32>(p, w, local, smem_raw, tid);
+      else sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid);
+    } else {
+      switch (slabs) {
+        case 1: sch_fp64y_item<16, 16>(p, w, local, smem_raw, tid); break;
+        case 2: sch_fp64y_item<32, 16>(p, w, local, smem_raw, tid); break;
+        case 3: sch_fp64y_item<48, 16>(p, w, local, smem_raw, tid); break;
+        default: sch_fp64y_item<64, 16>(p, w, local, smem_raw, tid); break;
+      }
+    }
+    return;
+  }
   switch (tile) {
     case kTileY32x64:
       if (slabs == 1) sch_fp64y_item<16, 64>(p, w, local, smem_raw, tid);
@@ -576,16 +595,12 @@ __device__ __forceinline__ void sch_fp64y_batch_item(const GppDev& p, const GppW
       if (slabs == 1) sch_fp64y_item<16, 32>(p, w, local, smem_raw, tid);
       else sch_fp64y_item<32, 32>(p, w, local, smem_raw, tid);
       break;
-    case kTileY128x16:
+    case kTileY64x16:
       switch (slabs) {
         case 1: sch_fp64y_item<16, 16>(p, w, local, smem_raw, tid); break;
         case 2: sch_fp64y_item<32, 16>(p, w, local, smem_raw, tid); break;
         case 3: sch_fp64y_item<48, 16>(p, w, local, smem_raw, tid); break;
-        case 4: sch_fp64y_item<64, 16>(p, w, local, smem_raw, tid); break;
-        case 5: sch_fp64y_item<80, 16>(p, w, local, smem_raw, tid); break;
-        case 6: sch_fp64y_item<96, 16>(p, w, local, smem_raw, tid); break;
-        case 7: sch_fp64y_item<112, 16>(p, w, local, smem_raw, tid); break;
-        default: sch_fp64y_item<128, 16>(p, w, local, smem_raw, tid); break;
+        default: sch_fp64y_item<64, 16>(p, w, local, smem_raw, tid); break;
       }
       break;
     default:
@@ -599,7 +614,8 @@ __device__ __forceinline__ void sch_fp64y_batch_item(const GppDev& p, const GppW
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchView b) {
+template <bool kSmall>
+__global__ void __launch_bounds__(kThreads, kSmall ? 2 : 1) sch_fp64y_batch_kernel(GppBatchView b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   const int tid = threadIdx.x;
@@ -613,7 +629,7 @@ __global__ void __launch_bounds__(kThreads, 1) sch_fp64y_batch_kernel(GppBatchVi
     const GppDev p = b.dev[inst];
     const GppWork w = b.work[inst];
     const int local = g - b.item_off[inst];
-    sch_fp64y_batch_item(p, w, b.tile[inst], local, smem_raw, tid);
+    sch_fp64y_batch_item<kSmall>(p, w, b.tile[inst], local, smem_raw, tid);
   }
 }
 
@@ -917,13 +933,23 @@ cudaError_t launch_sch_fp64y(const GppDev& p, const GppWork& w, int grid, cudaSt
 }
 int ssx_blocks_per_sm_fp64() { return blocks_per_sm(ssx_fp64_kernel, sizeof(SsxSmem)); }
 int sch_batch_blocks_per_sm_fp64() { return blocks_per_sm(sch_fp64_batch_kernel, kSchBatchSmem); }
-int sch_batch_blocks_per_sm_fp64y() { return blocks_per_sm(sch_fp64y_batch_kernel, kSchYBatchSmem); }
+int sch_batch_blocks_per_sm_fp64y(bool small) {
+  return small ? blocks_per_sm(sch_fp64y_batch_kernel<true>, kSchYBatchSmallSmem)
+               : blocks_per_sm(sch_fp64y_batch_kernel<false>, kSchYBatchSmem);
+}
 
-cudaError_t launch_sch_fp64y_batch(const GppBatchView& b, int grid, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(sch_fp64y_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+cudaError_t launch_sch_fp64y_batch(const GppBatchView& b, int grid, bool small, cudaStream_t s) {
+  if (small) {
+    cudaError_t e = cudaFuncSetAttribute(sch_fp64y_batch_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSchYBatchSmallSmem);
+    if (e != cudaSuccess) return e;
+    sch_fp64y_batch_kernel<true><<<grid, kThreads, kSchYBatchSmallSmem, s>>>(b);
+    return cudaGetLastError();
+  }
+  cudaError_t e = cudaFuncSetAttribute(sch_fp64y_batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kSchYBatchSmem);
   if (e != cudaSuccess) return e;
-  sch_fp64y_batch_kernel<<<grid, kThreads, kSchYBatchSmem, s>>>(b);
+  sch_fp64y_batch_kernel<false><<<grid, kThreads, kSchYBatchSmem, s>>>(b);
   return cudaGetLastError();
 }
 int ssx_batch_blocks_per_sm_fp64() { return blocks_per_sm(ssx_fp64_batch_kernel, sizeof(SsxSmem)); }

@@ -408,7 +408,7 @@ class GppBatch:
     device pointer.  `tiles` (optional) gives the FP64 main-pass tile per
     instance (-1 library choice; per-band frequencies 0 = 32x32, 1 = 16x64,
     2 = 64x16; one frequency set 3 = 64x32, 4 = 32x64, 5 = 32x32, 6 =
-    128x16).  `items_per_cta` / `tensor_split_tiles` (0: defaults) size the
+    64x16).  `items_per_cta` / `tensor_split_tiles` (0: defaults) size the
     work items (sigma_gpp_batch_create_tuned)."""
 
     def __init__(self, instances, precision=PREC_FP64, tiles=None, items_per_cta=0, tensor_split_tiles=0):

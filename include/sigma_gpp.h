@@ -206,7 +206,8 @@ typedef struct sigma_gpp_batch_s* sigma_gpp_batch;
  * for the library's choice (least padding).  A batch whose instances all
  * share one frequency set per instance (wx_band_stride 0) runs the
  * shared-frequency kernel: tiles 3 = 64 bands x 32 columns, 4 = 32 x 64,
- * 5 = 32 x 32, 6 = 128 x 16; otherwise the per-band kernel: 0 = 32 x 32,
+ * 5 = 32 x 32, 6 = 64 x 16 (5 and 6: two CTAs per SM when every instance
+ * takes one of them); otherwise the per-band kernel: 0 = 32 x 32,
  * 1 = 16 x 64, 2 = 64 x 16.  A tile of the other family is
  * SIGMA_ERR_UNSUPPORTED.  The tuning table of fortkernels-_gb300/autotune.py
  * chooses per shape class.  The mixed form has one tile shape.  precision
