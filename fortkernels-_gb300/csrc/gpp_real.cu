@@ -5,8 +5,14 @@
 // delw = wtilde / (wx - wtilde) and the pole guard of the complex path
 // (b = 0), so scha = aqsm[n1][igp] * aqsn[n1][ig] * Y_iw[my_igp][ig] with the
 // band-independent factor Y_iw = I_eps wtilde c / c^2 (c = wx - wtilde; 0 when
-// dropped).  The main pass forms Y per staged chunk and runs the g-vector sum
-// as a real FP64 GEMM: one DFMA per term.  Occupied bands add
+// dropped).  The main pass forms Y in FP64 per staged chunk and stages it, and
+// aqsn, also as float-float pairs; every term aqsn Y is then a float-float
+// product on the FP32 pipe, the high halves of two g-vectors' terms are added
+// exactly (TwoSum) and their sum widened and added in FP64 (half an FP64
+// operation per term, against one DFMA), the rounding errors and low halves
+// summed in FP32 and folded into the FP64 sums once per chunk.  A chunk with
+// a value outside the float-float range runs FP64 multiply-adds on the FP64
+// copies.  Occupied bands add
 //   ssx = Omega2 / wx^2 (kept), -G / (2 (wx + wtilde)) (dropped with
 //   delw^2 > to1), 0 otherwise,
 // in FP64 (G = I_eps wtilde, Omega2 = wtilde G).  Partial sums use the
@@ -24,12 +30,13 @@
 
 #include "sigma_gpp.h"
 #include "sigma_internal.cuh"
+#include "floatfloat.cuh"
 #include "runtime.h"
 
 namespace sigma {
 namespace {
 
-constexpr int kRBN = 128, kRBP = 32;  // bands x columns per main-pass item
+constexpr int kRBN = 64, kRBP = 32;   // bands x columns per main-pass item
 constexpr int kRCK = 32;             // g-vectors per staged chunk
 
 struct GppRealDev {
@@ -45,9 +52,11 @@ struct GppRealDev {
 struct RealSmem {
   double y[kRCK][kNW * kRBP + 1];  // [k][iw * kRBP + column]
   double n[kRCK][kRBN + 1];
+  float2 yf[kRCK][kNW * kRBP + 1];  // the same as float-float pairs
+  float2 nf[kRCK][kRBN + 1];
 };
 
-__global__ void __launch_bounds__(kThreads, 1) sch_real_kernel(GppRealDev p, GppWork w) {
+__global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, GppWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RealSmem& sm = *reinterpret_cast<RealSmem*>(smem_raw);
   __shared__ int s_item;
@@ -64,15 +73,20 @@ __global__ void __launch_bounds__(kThreads, 1) sch_real_kernel(GppRealDev p, Gpp
     const int n1_0 = ic.bb * kRBN, p0 = ic.cb * kRBP;
     const int ig_begin = ic.s * w.split_len, ig_end = min(ig_begin + w.split_len, p.nc);
     double acc[TB][TC][kNW];
+    float acl[TB][TC][kNW];
 #pragma unroll
     for (int i = 0; i < TB; ++i)
 #pragma unroll
       for (int j = 0; j < TC; ++j)
 #pragma unroll
-        for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = 0.0;
+        for (int iw = 0; iw < kNW; ++iw) {
+          acc[i][j][iw] = 0.0;
+          acl[i][j][iw] = 0.f;
+        }
 
     for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kRCK) {
       __syncthreads();
+      bool chunk_wide = false;  // a value of the chunk outside the float-float range
       for (int e = tid; e < kRCK * kRBP; e += kThreads) {
         const int k = e % kRCK, pl = e / kRCK;
         const int ig = ig0 + k, my_igp = p0 + pl;
@@ -92,31 +106,79 @@ __global__ void __launch_bounds__(kThreads, 1) sch_real_kernel(GppRealDev p, Gpp
           y1 = factor(wx1);
           y2 = factor(wx2);
         }
-        sm.y[k][pl] = y0;
-        sm.y[k][kRBP + pl] = y1;
-        sm.y[k][2 * kRBP + pl] = y2;
+        const double ys[kNW] = {y0, y1, y2};
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          const FF f = ff_of(ys[iw]);
+          sm.y[k][iw * kRBP + pl] = ys[iw];
+          sm.yf[k][iw * kRBP + pl] = make_float2(f.hi, f.lo);
+          chunk_wide = chunk_wide || !ff_range(ys[iw], 0.0);
+        }
       }
       for (int e = tid; e < kRCK * kRBN; e += kThreads) {
         const int k = e % kRCK, bl = e / kRCK;
         const int ig = ig0 + k, n1 = n1_0 + bl;
-        sm.n[k][bl] = (ig < ig_end && n1 < p.nb) ? p.aqsn[(size_t)n1 * p.nc + ig] : 0.0;
+        const double v = (ig < ig_end && n1 < p.nb) ? p.aqsn[(size_t)n1 * p.nc + ig] : 0.0;
+        const FF f = ff_of(v);
+        sm.n[k][bl] = v;
+        sm.nf[k][bl] = make_float2(f.hi, f.lo);
+        chunk_wide = chunk_wide || !ff_range(v, 0.0);
       }
-      __syncthreads();
-#pragma unroll 4
-      for (int k = 0; k < kRCK; ++k) {
-        double nn[TB], y[TC][kNW];
+      chunk_wide = __syncthreads_or(chunk_wide);
+      if (!chunk_wide) {
+        // the terms of two g-vectors: float-float products, their high
+        // halves added exactly, the sum added in FP64
+        static_assert(kRCK % 2 == 0, "g-vector pairs");
+#pragma unroll 1
+        for (int k = 0; k < kRCK; k += 2) {
+          float2 y[2][TC][kNW];
 #pragma unroll
-        for (int i = 0; i < TB; ++i) nn[i] = sm.n[k][ty + 16 * i];
+          for (int h = 0; h < 2; ++h)
 #pragma unroll
-        for (int j = 0; j < TC; ++j)
+            for (int j = 0; j < TC; ++j)
 #pragma unroll
-          for (int iw = 0; iw < kNW; ++iw) y[j][iw] = sm.y[k][iw * kRBP + tx + 16 * j];
+              for (int iw = 0; iw < kNW; ++iw) y[h][j][iw] = sm.yf[k + h][iw * kRBP + tx + 16 * j];
+#pragma unroll
+          for (int i = 0; i < TB; ++i) {
+            const float2 n0 = sm.nf[k][ty + 16 * i], n1v = sm.nf[k + 1][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < TC; ++j)
+#pragma unroll
+              for (int iw = 0; iw < kNW; ++iw) {
+                const FF t0 = ff_mul_raw(FF{n0.x, n0.y}, FF{y[0][j][iw].x, y[0][j][iw].y});
+                const FF t1 = ff_mul_raw(FF{n1v.x, n1v.y}, FF{y[1][j][iw].x, y[1][j][iw].y});
+                float s, e;
+                two_sum_f(t0.hi, t1.hi, s, e);
+                acc[i][j][iw] += f32_widen(s);
+                acl[i][j][iw] += (e + t0.lo) + t1.lo;
+              }
+          }
+        }
 #pragma unroll
         for (int i = 0; i < TB; ++i)
 #pragma unroll
           for (int j = 0; j < TC; ++j)
 #pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = fma(nn[i], y[j][iw], acc[i][j][iw]);
+            for (int iw = 0; iw < kNW; ++iw) {
+              acc[i][j][iw] += f32_widen(acl[i][j][iw]);
+              acl[i][j][iw] = 0.f;
+            }
+      } else {
+        for (int k = 0; k < kRCK; ++k) {
+          double nn[TB], y[TC][kNW];
+#pragma unroll
+          for (int i = 0; i < TB; ++i) nn[i] = sm.n[k][ty + 16 * i];
+#pragma unroll
+          for (int j = 0; j < TC; ++j)
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) y[j][iw] = sm.y[k][iw * kRBP + tx + 16 * j];
+#pragma unroll
+          for (int i = 0; i < TB; ++i)
+#pragma unroll
+            for (int j = 0; j < TC; ++j)
+#pragma unroll
+              for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = fma(nn[i], y[j][iw], acc[i][j][iw]);
+        }
       }
     }
     // epilogue: x aqsm[n1][igp] * 0.5 * vcoul[igp], half-warp butterfly over columns
@@ -270,7 +332,7 @@ extern "C" int sigma_gpp_real_plan_create(sigma_gpp_real_plan* out, int number_b
   p->nvband = nvband;
   p->nc = ncouls;
   p->ng = ngpown;
-  p->sch_grid = sms;
+  p->sch_grid = 2 * sms;  // two CTAs per SM
   p->ssx_grid = sms * 4;
   gpp_size_work(p->sch, 0, number_bands, kRBN, kRBP, ncouls, ngpown, p->sch_grid, 24);
   gpp_size_work(p->ssx, 0, nvband, kSsxBN, kSsxBP, ncouls, ngpown, p->ssx_grid, 8);
