@@ -44,12 +44,46 @@ __device__ __forceinline__ void split_exact(double x, float& hi, float& lo) {
   lo = 0.f;
 }
 
+// x = hi + lo with hi = x rounded to the nearest FP32 value (ties to even,
+// as cvt.rn.f32.f64) and lo = x - hi rounded to FP32, on the integer pipe,
+// for 2^-74 <= |x| < 2^128 (|x| at or above FLT_MAX + 1/2 ulp gives an
+// infinite hi, as the conversion does).  |lo| <= 2^-24 |x| and lo takes
+// either sign, so the lo parts that float-float products drop (lo * lo) and
+// the splits' own errors average out over long sums; the truncated split's
+// lo always carries x's sign, and those dropped parts then add up in one
+// direction (a bias of ~2^-46 per term in an FP64-class sum).  Outside the
+// range as split_exact.
+__device__ __forceinline__ void split_round(double x, float& hi, float& lo) {
+  const unsigned int whi = (unsigned int)__double2hiint(x), wlo = (unsigned int)__double2loint(x);
+  const unsigned int sign = whi & 0x80000000u;
+  const unsigned int ex = (whi >> 20) & 0x7FFu;
+  if (ex - 949u <= 201u) {
+    // round up when the dropped 29 bits exceed half an ulp, or equal it with
+    // an odd kept mantissa; the carry may run into the exponent field
+    const unsigned int rest = wlo & 0x1FFFFFFFu;
+    const unsigned int up = rest > 0x10000000u || (rest == 0x10000000u && ((wlo >> 29) & 1u));
+    const unsigned int f = __funnelshift_l(wlo, whi, 3) + up;
+    hi = __uint_as_float(((f + 0x40000000u) & 0x7FFFFFFFu) | sign);
+    const int m = (int)rest - (int)(up << 29);  // x - hi in units of 2^(ex - 1075), |m| <= 2^28
+    const float l = __int2float_rn(m) * __uint_as_float((ex - 948u) << 23);
+    lo = __uint_as_float(__float_as_uint(l) ^ sign);
+    return;
+  }
+  split_exact(x, hi, lo);
+}
+
 struct FF {
   float hi, lo;
 };
 __device__ __forceinline__ FF ff_of(double x) {
   FF r;
   split_exact(x, r.hi, r.lo);
+  return r;
+}
+// The rounded split, for the FP64 forms' float-float terms.
+__device__ __forceinline__ FF ff_of_rn(double x) {
+  FF r;
+  split_round(x, r.hi, r.lo);
   return r;
 }
 __device__ __forceinline__ FF ff_norm(float s, float e) {

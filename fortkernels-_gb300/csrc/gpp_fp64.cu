@@ -132,10 +132,10 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
         const double2 g = cmul(ie, wt);
         a = wt.x;
         b = wt.y;
-        const FF f = ff_of(b), f2 = ff_mul_raw(f, f), gx = ff_of(g.x), gy = ff_of(g.y);
+        const FF f = ff_of_rn(b), f2 = ff_mul_raw(f, f), gx = ff_of_rn(g.x), gy = ff_of_rn(g.y);
         fb = make_float4(f.hi, f.lo, f2.hi, f2.lo);
         fg = make_float4(gx.hi, gx.lo, gy.hi, gy.lo);
-        const float ah = ff_of(a).hi;
+        const float ah = ff_of_rn(a).hi;
         // |wtilde|^2 * 4e-6 > 0.25 needs |wtilde|^2 > 62500
         flag = (fmaf(ah, ah, f.hi * f.hi) >= 62000.f ? kFlagBinds : 0u) |
                (ff_range(wt.x, wt.y) && ff_range(ie.x, ie.y) ? 0u : kFlagWide);
@@ -151,7 +151,7 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
       const int ig = ig0 + k, n1 = n1_0 + bl;
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
-      const FF nx = ff_of(v.x), ny = ff_of(v.y);
+      const FF nx = ff_of_rn(v.x), ny = ff_of_rn(v.y);
       sm.fn[k][bl] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
       sm.nflag[k][bl] = ff_range(v.x, v.y) ? 0u : kFlagWide;
     }
@@ -192,7 +192,7 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
           const bool any_wide = __any_sync(0xffffffffu, wide);
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            const FF c = ff_of(__dsub_rn(wxr[i][iw], a[j]));  // wx - Re wtilde in FP64
+            const FF c = ff_of_rn(__dsub_rn(wxr[i][iw], a[j]));  // wx - Re wtilde in FP64
             const FF wv = ff_sq_add(c, fb2[j]);               // |wdiff|^2
             bool near;
             bool keep = ff_gt_quarter(wv, near);
@@ -407,7 +407,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
         const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
         const double2 v = make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
-        const FF vx = ff_of(v.x), vy = ff_of(v.y);
+        const FF vx = ff_of_rn(v.x), vy = ff_of_rn(v.y);
         sm.y[k][iw * BP + pl] = v;
         sm.yf[k][iw * BP + pl] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
         chunk_wide = chunk_wide || !ff_range(v.x, v.y);
@@ -418,7 +418,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       const int ig = ig0 + k, n1 = n1_0 + bl;
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
-      const FF nx = ff_of(v.x), ny = ff_of(v.y);
+      const FF nx = ff_of_rn(v.x), ny = ff_of_rn(v.y);
       sm.nf[k][bl] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
       sm.n[k][bl] = v;
       chunk_wide = chunk_wide || !ff_range(v.x, v.y);
@@ -641,12 +641,19 @@ __global__ void __launch_bounds__(kThreads, kSmall ? 2 : 1) sch_fp64y_batch_kern
 //                              (= -Omega2 conj(cden) delw / |cden|^2, cden = 4 wtilde^2 (delw + 1/2))
 //   otherwise (incl. exact poles, where the reference's delw is NaN): 0
 // and asxtemp[iw] += occ vcoul[igp] conj(aqsm[n1][igp]) sum_ig aqsn[n1][ig] ssx.
-// The factors are formed in float-float arithmetic (FP32 pairs, ~2^-44
-// relative, from exact splits of the FP64 inputs) on the FP32 pipe, then
-// widened to FP64 once: GB300's FP64 pipe, at 1/64 of the FP32 rate, keeps
-// the guard decisions (the FP64 path's own expressions), the widening and
-// the band sums.  Both branches are formed for every term (about a fifth of
-// the terms take the second one, so a warp almost always needs both).
+// With one frequency set for every band, the factors are formed in
+// float-float arithmetic (FP32 pairs, ~2^-44 relative, from exact splits of
+// the FP64 inputs) on the FP32 pipe and each term aqsn ssx is a float-float
+// product; the high halves of two g-vectors' terms are added exactly
+// (TwoSum) and then once in FP64, the rounding errors and low halves summed
+// in FP32 and folded into the FP64 sums once per staged chunk.  GB300's FP64
+// pipe, at 1/64 of the FP32 rate, keeps the guard decisions (the FP64 path's
+// own expressions) and those sums.  Both branches are formed for every term
+// (about a fifth of the terms take the second one, so a warp almost always
+// needs both).  With per-band frequencies each band forms its own factors
+// and each term's high halves are added in FP64 one at a time.  Chunks
+// holding a value outside the float-float range take FP64 factors and FP64
+// multiply-adds.
 constexpr int kSsxCK = 8;      // g-vectors per staged chunk
 
 struct SsxSmem {  // column rows padded by one element (see SchYSmem)
@@ -654,7 +661,7 @@ struct SsxSmem {  // column rows padded by one element (see SchYSmem)
   double b[kSsxCK][kSsxBP + 1];
   double2 ie[kSsxCK][kSsxBP + 1];
   double2 n[kSsxCK][kSsxBN];
-  double ns[kSsxCK][kSsxBN];  // n.x + n.y
+  float4 nf[kSsxCK][kSsxBN];  // aqsn as float-float pairs
 };
 static_assert(sizeof(SsxSmem) <= 200 * 1024, "shared memory budget");
 
@@ -667,9 +674,9 @@ struct SsxShared {
 // One term's ssx factor from the element's float-float values (a + i b =
 // wtilde, G = I_eps wtilde, Omega2 = wtilde G): Omega2 / wx^2 when kept,
 // -G conj(z) / (2 |z|^2) with z = wtilde + wx in the second branch, else 0;
-// widened to FP64 once (hi and lo widened exactly, one FP64 addition).
-__device__ __forceinline__ double2 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy, FF omx, FF omy, FF wx,
-                                                 FF iwx2, bool keep, bool second) {
+// as float-float pairs (x.hi, x.lo, y.hi, y.lo).
+__device__ __forceinline__ float4 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy, FF omx, FF omy, FF wx,
+                                                FF iwx2, bool keep, bool second) {
   const FF k1x = ff_mul_raw(omx, iwx2), k1y = ff_mul_raw(omy, iwx2);
   const FF zr = ff_add(a, wx);
   const FF r = ff_rcp_raw(ff_sq_add(zr, b2));
@@ -677,7 +684,7 @@ __device__ __forceinline__ double2 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy
   const FF k2x = ff_mul_raw(tx, r), k2y = ff_mul_raw(ty, r);
   const FF sx = keep ? k1x : (second ? FF{-0.5f * k2x.hi, -0.5f * k2x.lo} : FF{0.f, 0.f});
   const FF sy = keep ? k1y : (second ? FF{-0.5f * k2y.hi, -0.5f * k2y.lo} : FF{0.f, 0.f});
-  return make_double2(ff_widen(sx), ff_widen(sy));
+  return make_float4(sx.hi, sx.lo, sy.hi, sy.lo);
 }
 
 // The same factor in FP64, for elements whose inputs leave the float-float
@@ -685,7 +692,7 @@ __device__ __forceinline__ double2 ssx_factor_ff(FF a, FF b, FF b2, FF gx, FF gy
 // [2^-20, 2^20), or an item frequency |wx| outside [2^-20, 2^20).  Inside it
 // every float-float intermediate (up to wtilde^2 I_eps / wx^2, within
 // 2^+-103) keeps both FP32 halves normal; outside it FP32 could overflow or
-// lose the low half.  Out of line, taken only by warps that hold such an
+// lose the low half.  Out of line, taken only by chunks that hold such an
 // element.
 static __device__ __noinline__ double2 ssx_factor_fp64(double a, double b, double b2, double2 ie, double wx,
                                                        double iwx2, bool keep, bool second) {
@@ -715,7 +722,7 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
     wx_out = !ff_freq_range(wx);
     sh.wx[i][iw] = wx;
     sh.iwx2[i][iw] = rcp_f64(wx * wx);
-    const FF f = ff_of(wx), g = ff_of(sh.iwx2[i][iw]);
+    const FF f = ff_of_rn(wx), g = ff_of_rn(sh.iwx2[i][iw]);
     sh.wxf[i][iw][0] = f.hi;
     sh.wxf[i][iw][1] = f.lo;
     sh.iwx2f[i][iw][0] = g.hi;
@@ -723,17 +730,21 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
   }
   const bool item_wide = __syncthreads_or(wx_out);
 
-  // each complex multiply-add as three real products (as in the main pass):
-  // P1 = sum n.x s.x, P2 = sum n.y s.y, P3 = sum (n.x + n.y)(s.x + s.y),
-  // sum n s = (P1 - P2) + i (P3 - P1 - P2)
-  double p1[kSsxBN][kNW], p2[kSsxBN][kNW], p3[kSsxBN][kNW];
+  // FP64 sums of the terms' high halves (of g-vector pairs, added exactly),
+  // FP32 sums of the rounding errors and low halves folded in per chunk
+  double2 acc[kSsxBN][kNW];
+  float2 acl[kSsxBN][kNW];
 #pragma unroll
   for (int i = 0; i < kSsxBN; ++i)
 #pragma unroll
-    for (int iw = 0; iw < kNW; ++iw) p1[i][iw] = p2[i][iw] = p3[i][iw] = 0.0;
+    for (int iw = 0; iw < kNW; ++iw) {
+      acc[i][iw] = make_double2(0.0, 0.0);
+      acl[i][iw] = make_float2(0.f, 0.f);
+    }
 
   for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kSsxCK) {
     __syncthreads();
+    bool chunk_wide = item_wide;  // FP64 factors and multiply-adds
     for (int e = tid; e < kSsxCK * kSsxBP; e += kThreads) {
       const int k = e % kSsxCK, pl = e / kSsxCK;
       const int ig = ig0 + k, my_igp = p0 + pl;
@@ -746,67 +757,136 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       sm.a[k][pl] = wt.x;
       sm.b[k][pl] = wt.y;
       sm.ie[k][pl] = ie;
+      chunk_wide = chunk_wide || !(ff_range(wt.x, wt.y) && ff_range(ie.x, ie.y));
     }
     for (int e = tid; e < kSsxCK * kSsxBN; e += kThreads) {
       const int k = e % kSsxCK, bl = e / kSsxCK;
       const int ig = ig0 + k, n1 = n1_0 + bl;
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
+      const FF nx = ff_of_rn(v.x), ny = ff_of_rn(v.y);
       sm.n[k][bl] = v;
-      sm.ns[k][bl] = __dadd_rn(v.x, v.y);
+      sm.nf[k][bl] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
+      chunk_wide = chunk_wide || !ff_range(v.x, v.y);
     }
-    __syncthreads();
+    chunk_wide = __syncthreads_or(chunk_wide);
 
-    for (int k = 0; k < kSsxCK; ++k) {
-      const double a = sm.a[k][tid], b = sm.b[k][tid];
-      const double2 ie = sm.ie[k][tid];
-      const double b2 = guard_b2(b);
-      const double thr = guard_thr(a, b2), thr2 = guard_thr2(a, b2);
-      const FF fa = ff_of(a), fb = ff_of(b), er = ff_of(ie.x), ei = ff_of(ie.y);
-      const FF gx = ff_dot2_raw(er, fa, ei, fb), gy = ff_dot2_raw(er, fb, ff_neg(ei), fa);  // G
-      const FF omx = ff_dot2_raw(fa, gx, fb, gy), omy = ff_dot2_raw(fa, gy, ff_neg(fb), gx);  // Omega2
-      const FF fb2 = ff_mul_raw(fb, fb);
-      // ssx factor of band i and frequency iw (band-independent when the
-      // frequencies are shared); decisions from the FP64 expressions
-      const bool wide = item_wide || !(ff_range(a, b) && ff_range(ie.x, ie.y));
-      const bool any_wide = __any_sync(0xffffffffu, wide);
-      auto factor = [&](int i, int iw) {
-        const double wv = guard_w(sh.wx[i][iw], a, b2);
-        const bool keep = keep_nonneg(wv, thr);
-        const bool second = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
-        double2 s = ssx_factor_ff(fa, fb, fb2, gx, gy, omx, omy, FF{sh.wxf[i][iw][0], sh.wxf[i][iw][1]},
-                                  FF{sh.iwx2f[i][iw][0], sh.iwx2f[i][iw][1]}, keep, second);
-        if (any_wide && wide) s = ssx_factor_fp64(a, b, b2, ie, sh.wx[i][iw], sh.iwx2[i][iw], keep, second);
-        return s;
-      };
-      auto mac = [&](int i, int iw, double2 s, double s_sum) {
-        const double2 an = sm.n[k][i];
-        p1[i][iw] = fma(an.x, s.x, p1[i][iw]);
-        p2[i][iw] = fma(an.y, s.y, p2[i][iw]);
-        p3[i][iw] = fma(sm.ns[k][i], s_sum, p3[i][iw]);
-      };
-      if (p.wx_stride == 0) {
-        double2 sv[kNW];
-        double ss[kNW];
+    if (!chunk_wide && p.wx_stride != 0) {
+      // per-band frequencies: each band's float-float factor and term; the
+      // term's high halves added in FP64
+      for (int k = 0; k < kSsxCK; ++k) {
+        const double a = sm.a[k][tid], b = sm.b[k][tid];
+        const double2 ie = sm.ie[k][tid];
+        const double b2 = guard_b2(b);
+        const double thr = guard_thr(a, b2), thr2 = guard_thr2(a, b2);
+        const FF fa = ff_of_rn(a), fb = ff_of_rn(b), er = ff_of_rn(ie.x), ei = ff_of_rn(ie.y);
+        const FF gx = ff_dot2_raw(er, fa, ei, fb), gy = ff_dot2_raw(er, fb, ff_neg(ei), fa);  // G
+        const FF omx = ff_dot2_raw(fa, gx, fb, gy), omy = ff_dot2_raw(fa, gy, ff_neg(fb), gx);  // Omega2
+        const FF fb2 = ff_mul_raw(fb, fb);
+#pragma unroll
+        for (int i = 0; i < kSsxBN; ++i)
+          if (i < nbl) {
+            const float4 n0 = sm.nf[k][i];
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const double wv = guard_w(sh.wx[i][iw], a, b2);
+              const bool keep = keep_nonneg(wv, thr);
+              const bool second = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
+              const float4 s = ssx_factor_ff(fa, fb, fb2, gx, gy, omx, omy, FF{sh.wxf[i][iw][0], sh.wxf[i][iw][1]},
+                                             FF{sh.iwx2f[i][iw][0], sh.iwx2f[i][iw][1]}, keep, second);
+              const FF r0 = ff_dot2_raw(FF{n0.x, n0.y}, FF{s.x, s.y}, FF{n0.z, n0.w}, FF{s.z, s.w});
+              const FF i0 = ff_dot2_raw(FF{n0.x, n0.y}, FF{s.z, s.w}, FF{-n0.z, -n0.w}, FF{s.x, s.y});
+              acc[i][iw].x += f32_widen(r0.hi);
+              acc[i][iw].y += f32_widen(i0.hi);
+              acl[i][iw].x += r0.lo;
+              acl[i][iw].y += i0.lo;
+            }
+          }
+      }
+#pragma unroll
+      for (int i = 0; i < kSsxBN; ++i)
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          sv[iw] = factor(0, iw);
-          ss[iw] = __dadd_rn(sv[iw].x, sv[iw].y);
+          acc[i][iw].x += f32_widen(acl[i][iw].x);
+          acc[i][iw].y += f32_widen(acl[i][iw].y);
+          acl[i][iw] = make_float2(0.f, 0.f);
+        }
+    } else if (!chunk_wide) {
+      // one frequency set for every band: the element's factors are shared
+      // by the item's bands; each term a float-float product, the high
+      // halves of two g-vectors' terms added exactly and then in FP64
+      static_assert(kSsxCK % 2 == 0, "g-vector pairs");
+      for (int k = 0; k < kSsxCK; k += 2) {
+        float4 sv[2][kNW];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const double a = sm.a[k + h][tid], b = sm.b[k + h][tid];
+          const double2 ie = sm.ie[k + h][tid];
+          const double b2 = guard_b2(b);
+          const double thr = guard_thr(a, b2), thr2 = guard_thr2(a, b2);
+          const FF fa = ff_of_rn(a), fb = ff_of_rn(b), er = ff_of_rn(ie.x), ei = ff_of_rn(ie.y);
+          const FF gx = ff_dot2_raw(er, fa, ei, fb), gy = ff_dot2_raw(er, fb, ff_neg(ei), fa);  // G
+          const FF omx = ff_dot2_raw(fa, gx, fb, gy), omy = ff_dot2_raw(fa, gy, ff_neg(fb), gx);  // Omega2
+          const FF fb2 = ff_mul_raw(fb, fb);
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            // decisions from the FP64 expressions
+            const double wv = guard_w(sh.wx[0][iw], a, b2);
+            const bool keep = keep_nonneg(wv, thr);
+            const bool second = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
+            sv[h][iw] = ssx_factor_ff(fa, fb, fb2, gx, gy, omx, omy, FF{sh.wxf[0][iw][0], sh.wxf[0][iw][1]},
+                                      FF{sh.iwx2f[0][iw][0], sh.iwx2f[0][iw][1]}, keep, second);
+          }
         }
 #pragma unroll
         for (int i = 0; i < kSsxBN; ++i)
           if (i < nbl) {
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) mac(i, iw, sv[iw], ss[iw]);
-          }
-      } else {
-#pragma unroll
-        for (int i = 0; i < kSsxBN; ++i)
-          if (i < nbl) {
+            const float4 n0 = sm.nf[k][i], n1 = sm.nf[k + 1][i];
 #pragma unroll
             for (int iw = 0; iw < kNW; ++iw) {
-              const double2 s = factor(i, iw);
-              mac(i, iw, s, __dadd_rn(s.x, s.y));
+              const float4 s0 = sv[0][iw], s1 = sv[1][iw];
+              const FF r0 = ff_dot2_raw(FF{n0.x, n0.y}, FF{s0.x, s0.y}, FF{n0.z, n0.w}, FF{s0.z, s0.w});
+              const FF i0 = ff_dot2_raw(FF{n0.x, n0.y}, FF{s0.z, s0.w}, FF{-n0.z, -n0.w}, FF{s0.x, s0.y});
+              const FF r1 = ff_dot2_raw(FF{n1.x, n1.y}, FF{s1.x, s1.y}, FF{n1.z, n1.w}, FF{s1.z, s1.w});
+              const FF i1 = ff_dot2_raw(FF{n1.x, n1.y}, FF{s1.z, s1.w}, FF{-n1.z, -n1.w}, FF{s1.x, s1.y});
+              float sr, er2, si, ei2;
+              two_sum_f(r0.hi, r1.hi, sr, er2);
+              two_sum_f(i0.hi, i1.hi, si, ei2);
+              acc[i][iw].x += f32_widen(sr);
+              acc[i][iw].y += f32_widen(si);
+              acl[i][iw].x += (er2 + r0.lo) + r1.lo;
+              acl[i][iw].y += (ei2 + i0.lo) + i1.lo;
+            }
+          }
+      }
+#pragma unroll
+      for (int i = 0; i < kSsxBN; ++i)
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) {
+          acc[i][iw].x += f32_widen(acl[i][iw].x);
+          acc[i][iw].y += f32_widen(acl[i][iw].y);
+          acl[i][iw] = make_float2(0.f, 0.f);
+        }
+    } else {
+      // a value outside the float-float range: FP64 factors and FP64
+      // complex multiply-adds
+      for (int k = 0; k < kSsxCK; ++k) {
+        const double a = sm.a[k][tid], b = sm.b[k][tid];
+        const double2 ie = sm.ie[k][tid];
+        const double b2 = guard_b2(b);
+        const double thr = guard_thr(a, b2), thr2 = guard_thr2(a, b2);
+        for (int i = 0; i < kSsxBN; ++i)
+          if (i < nbl) {
+            const double2 an = sm.n[k][i];
+#pragma unroll
+            for (int iw = 0; iw < kNW; ++iw) {
+              const int ib = p.wx_stride == 0 ? 0 : i;
+              const double wv = guard_w(sh.wx[ib][iw], a, b2);
+              const bool keep = keep_nonneg(wv, thr);
+              const bool second = !keep && gt_nonneg(wv, 0.0) && gt_nonneg(thr2, wv);
+              const double2 s = ssx_factor_fp64(a, b, b2, ie, sh.wx[ib][iw], sh.iwx2[ib][iw], keep, second);
+              acc[i][iw].x = fma(an.x, s.x, fma(-an.y, s.y, acc[i][iw].x));
+              acc[i][iw].y = fma(an.x, s.y, fma(an.y, s.x, acc[i][iw].y));
             }
           }
       }
@@ -825,9 +905,7 @@ __device__ __forceinline__ void ssx_fp64_item(const GppDev& p, const GppWork& w,
       if (i < nbl && igp >= 0) {
         const double2 am = p.aqsm[(size_t)(n1_0 + i) * p.nc + igp];
         const double f = p.occ * p.vcoul[igp];
-        const double2 acc = make_double2(__dsub_rn(p1[i][iw], p2[i][iw]),
-                                         __dsub_rn(__dsub_rn(p3[i][iw], p1[i][iw]), p2[i][iw]));
-        v = cmul(acc, make_double2(am.x, -am.y));
+        v = cmul(acc[i][iw], make_double2(am.x, -am.y));
         v.x *= f;
         v.y *= f;
       }

@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, Gpp
         const double ys[kNW] = {y0, y1, y2};
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          const FF f = ff_of(ys[iw]);
+          const FF f = ff_of_rn(ys[iw]);
           sm.y[k][iw * kRBP + pl] = ys[iw];
           sm.yf[k][iw * kRBP + pl] = make_float2(f.hi, f.lo);
           chunk_wide = chunk_wide || !ff_range(ys[iw], 0.0);
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, Gpp
         const int k = e % kRCK, bl = e / kRCK;
         const int ig = ig0 + k, n1 = n1_0 + bl;
         const double v = (ig < ig_end && n1 < p.nb) ? p.aqsn[(size_t)n1 * p.nc + ig] : 0.0;
-        const FF f = ff_of(v);
+        const FF f = ff_of_rn(v);
         sm.n[k][bl] = v;
         sm.nf[k][bl] = make_float2(f.hi, f.lo);
         chunk_wide = chunk_wide || !ff_range(v, 0.0);

@@ -155,6 +155,14 @@ __global__ void split_kernel(const double* x, float* out, long long n) {
     out[2 * i + 1] = s.lo;
   }
 }
+__global__ void split_round_kernel(const double* x, float* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const FF s = ff_of_rn(x[i]);
+    out[2 * i] = s.hi;
+    out[2 * i + 1] = s.lo;
+  }
+}
 }  // namespace
 }  // namespace sigma
 
@@ -165,6 +173,17 @@ extern "C" int sigma_eval_split(const double* x, float* out, long long n, void* 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
   split_kernel<<<(int)blocks, 256, 0, s>>>(x, out, n);
+  SIGMA_CUDA_TRY(cudaGetLastError());
+  return SIGMA_OK;
+}
+
+extern "C" int sigma_eval_split_round(const double* x, float* out, long long n, void* stream) {
+  using namespace sigma;
+  if (!x || !out) return SIGMA_ERR_NULL;
+  if (n <= 0) return SIGMA_ERR_INVALID_SHAPE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  split_round_kernel<<<(int)blocks, 256, 0, s>>>(x, out, n);
   SIGMA_CUDA_TRY(cudaGetLastError());
   return SIGMA_OK;
 }

@@ -106,6 +106,7 @@ SIGNATURES = {
     "sigma_measure_fma_peaks": ([_P, _P, _P], _I),
     "sigma_eval_reciprocals": ([_P, _P, _LL, _P], _I),
     "sigma_eval_split": ([_P, _P, _LL, _P], _I),
+    "sigma_eval_split_round": ([_P, _P, _LL, _P], _I),
 }
 
 

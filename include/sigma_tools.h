@@ -54,6 +54,14 @@ int sigma_eval_reciprocals(const double* w, double* out, long long n, void* stre
  * array of 2n floats.  Asynchronous on `stream`. */
 int sigma_eval_split(const double* x, float* out, long long n, void* stream);
 
+/* The rounded float-float split the FP64 forms' float-float terms use (no
+ * counterpart in the reference): out[2i] = hi (x rounded to the nearest
+ * FP32 value, ties to even), out[2i+1] = lo (x - hi rounded to FP32), so
+ * |x - hi - lo| <= 2^-48 |x| and |lo| <= 2^-24 |x| for 2^-74 <= |x| < 2^128
+ * (an infinite hi from FLT_MAX + 1/2 ulp up).  out is a device array of 2n
+ * floats.  Asynchronous on `stream`. */
+int sigma_eval_split_round(const double* x, float* out, long long n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -116,3 +116,43 @@ def test_float_float_split(sigma_lib):
     assert np.all(np.isnan(o[nan, 0]))
     tiny = ~nan & (ax < 2.0 ** -126)
     assert np.all(o[tiny, 0] == 0) and np.all(o[tiny, 1] == 0)
+
+
+def test_float_float_split_round(sigma_lib):
+    """The rounded split of the FP64 forms' float-float terms: hi = x rounded
+    to the nearest FP32 value (ties to even, numpy's conversion) and lo = x -
+    hi rounded to FP32 over 2^-74 <= |x| < 2^128 (hi infinite from FLT_MAX +
+    1/2 ulp up); below 2^-74 as the truncated split."""
+    x = _sample_split(1 << 20, 8)
+    rng = np.random.default_rng(9)
+    # ties of hi: the dropped 29 bits exactly half an ulp, kept mantissa odd and even
+    ties = []
+    for e in (-74, -20, -1, 0, 1, 20, 127):
+        for k in rng.integers(0, 1 << 23, 8):
+            m = (int(k) << 29) | (1 << 28)
+            for s in (0, 1):
+                ties.append((s << 63) | ((e + 1023) << 52) | m)
+    x = np.concatenate([x, np.array(ties, dtype=np.uint64).view(np.float64)])
+    dx = torch.from_numpy(x).cuda()
+    out = torch.empty(2 * len(x), dtype=torch.float32, device="cuda")
+    assert sigma_lib.load().sigma_eval_split_round(dx.data_ptr(), out.data_ptr(), len(x), None) == 0
+    torch.cuda.synchronize()
+    o = out.cpu().numpy().reshape(-1, 2)
+    nan = np.isnan(x)
+    ax = np.abs(x)
+    inside = ~nan & (ax >= 2.0 ** -74) & (ax < 2.0 ** 128)
+    xs = x[inside]
+    with np.errstate(over="ignore"):
+        hi = xs.astype(np.float32)
+    assert np.array_equal(o[inside, 0], hi)
+    fin = np.isfinite(hi)
+    lo = (xs[fin] - hi[fin].astype(np.float64)).astype(np.float32)  # exact in FP64, one rounding
+    assert np.array_equal(o[inside, 1][fin], lo)
+    err = np.abs(xs[fin] - hi[fin].astype(np.float64) - lo.astype(np.float64))
+    assert np.all(err <= 2.0 ** -48 * np.abs(xs[fin]))
+    assert np.all(np.abs(lo.astype(np.float64)) <= 2.0 ** -24 * np.abs(xs[fin]))
+    big = ~nan & (ax >= 2.0 ** 128)
+    assert np.all(np.isinf(o[big, 0])) and np.all(o[big, 1] == 0)
+    assert np.all(np.isnan(o[nan, 0]))
+    tiny = ~nan & (ax < 2.0 ** -126)
+    assert np.all(o[tiny, 0] == 0) and np.all(o[tiny, 1] == 0)
