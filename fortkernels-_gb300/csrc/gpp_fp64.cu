@@ -320,11 +320,79 @@ constexpr int kCKY = 16;  // g-vectors per staged chunk
 // are multiples of 128 bytes, put a warp's writes in one bank group.
 template <int BN, int BP>
 struct SchYSmem {
+  // each thread's FP64 sums (its 16-column x 16-band register tile's outputs
+  // x 3 frequencies), one slot row per output: a warp's accesses are 512
+  // contiguous bytes
+  double2 acc[(BN / 16) * (BP / 16) * kNW][kThreads];
   float4 yf[kCKY][kNW * BP + 1];  // [k][iw * BP + column]: Y as float-float (x.hi, x.lo, y.hi, y.lo)
   float4 nf[kCKY][BN + 1];        // aqsn as float-float
-  double2 y[kCKY][kNW * BP + 1];  // Y in FP64, for chunks with a value outside the float-float range
-  double2 n[kCKY][BN + 1];        // aqsn in FP64, for the same chunks
 };
+
+// Y = G (c + i b) / |wdiff|^2 of one (column, g-vector) element at frequency
+// wx in FP64 (G = I_eps wtilde, a + i b = wtilde, c = wx - a, b2 = b^2, thr
+// the pole guard's threshold; 0 where the guard drops the term, and for
+// padding elements, whose thr is infinite): ~13 FP64 operations, shared by
+// every band of the item.
+__device__ __forceinline__ double2 sch_y_fp64(double2 g, double a, double b, double b2, double thr, double wx) {
+  const double c = __dsub_rn(wx, a);
+  const double wv = fma(c, c, b2);
+  const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
+  const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
+  return make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
+}
+
+// A chunk holding a factor or an aqsn element outside the float-float range:
+// FP64 complex multiply-adds of the thread's register tile, its factors
+// formed again from the inputs (as the staging formed them) and aqsn read
+// again, the chunk's sums added to the thread's FP64 sums.  Out of line: the
+// common path carries none of its registers.
+template <int BN, int BP>
+static __device__ __noinline__ void sch_fp64y_wide_chunk(const GppDev& p, double2 (*acc)[kThreads], int tid,
+                                                         int ig0, int ig_end, int n1_0, int band_end, int p0,
+                                                         double wx0, double wx1, double wx2) {
+  constexpr int TB = BN / 16, TC = BP / 16;
+  const int tx = tid & 15, ty = tid >> 4;
+  double2 aw[TB][TC][kNW];
+  for (int i = 0; i < TB; ++i)
+    for (int j = 0; j < TC; ++j)
+      for (int iw = 0; iw < kNW; ++iw) aw[i][j][iw] = make_double2(0.0, 0.0);
+  for (int k = 0; k < kCKY; ++k) {
+    const int ig = ig0 + k;
+    double2 y[TC][kNW];
+    for (int j = 0; j < TC; ++j) {
+      const int my_igp = p0 + tx + 16 * j;
+      const bool valid = ig < ig_end && my_igp < p.ng;
+      double2 wt = make_double2(0.0, 0.0), ie = wt;
+      if (valid) {
+        const size_t off = (size_t)my_igp * p.nc + ig;
+        wt = p.wt[off];
+        ie = p.ieps[off];
+      }
+      const double2 g = cmul(ie, wt);
+      const double b2 = guard_b2(wt.y);
+      const double thr = valid ? guard_thr(wt.x, b2) : __longlong_as_double(0x7ff0000000000000LL);
+      for (int iw = 0; iw < kNW; ++iw)
+        y[j][iw] = sch_y_fp64(g, wt.x, wt.y, b2, thr, iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2));
+    }
+    for (int i = 0; i < TB; ++i) {
+      const int n1 = n1_0 + ty + 16 * i;
+      const double2 nn = (ig < ig_end && n1 < band_end) ? p.aqsn[(size_t)n1 * p.nc + ig] : make_double2(0.0, 0.0);
+      for (int j = 0; j < TC; ++j)
+        for (int iw = 0; iw < kNW; ++iw) {
+          const double2 yv = y[j][iw];
+          aw[i][j][iw].x = fma(nn.x, yv.x, fma(-nn.y, yv.y, aw[i][j][iw].x));
+          aw[i][j][iw].y = fma(nn.x, yv.y, fma(nn.y, yv.x, aw[i][j][iw].y));
+        }
+    }
+  }
+  for (int i = 0; i < TB; ++i)
+    for (int j = 0; j < TC; ++j)
+      for (int iw = 0; iw < kNW; ++iw) {
+        double2& a = acc[(i * TC + j) * kNW + iw][tid];
+        a.x += aw[i][j][iw].x;
+        a.y += aw[i][j][iw].y;
+      }
+}
 
 // Bounded wait for a gate word written by a host-to-device copy (`polls`
 // polls 256 ns apart: about 1 s with the default bound).  False when it gave
@@ -364,19 +432,10 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const int ig_end = min(ig_begin + w.split_len, p.nc);
   const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
 
-  // FP64 sums of the terms' FP32 high halves; FP32 sums of their low halves
-  // over one staged chunk, added to the FP64 sums at the chunk's end
-  double2 acc[TB][TC][kNW];
-  float2 acl[TB][TC][kNW];
+  // the item's FP64 sums live in shared memory (registers hold one chunk's
+  // float-float sums); each thread touches only its own slots
 #pragma unroll
-  for (int i = 0; i < TB; ++i)
-#pragma unroll
-    for (int j = 0; j < TC; ++j)
-#pragma unroll
-      for (int iw = 0; iw < kNW; ++iw) {
-        acc[i][j][iw] = make_double2(0.0, 0.0);
-        acl[i][j][iw] = make_float2(0.f, 0.f);
-      }
+  for (int o = 0; o < TB * TC * kNW; ++o) sm.acc[o][tid] = make_double2(0.0, 0.0);
 
   for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCKY) {
     __syncthreads();
@@ -393,22 +452,17 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         wt = p.wt[off];
         ie = p.ieps[off];
       }
-      // Y = G (c + i b) r in FP64 (~41 FP64 operations per column and
-      // g-vector, shared by the item's 64 bands x 3 frequencies), staged in
-      // FP64 and split as float-float pairs for the terms; the pole guard
-      // is the int64 compare against the per-element threshold
+      // Y in FP64 (~41 FP64 operations per column and g-vector, shared by
+      // the item's 64 bands x 3 frequencies), split as float-float pairs
+      // for the terms; the pole guard is the int64 compare against the
+      // per-element threshold
       const double2 g = cmul(ie, wt);
-      const double b = wt.y, b2 = guard_b2(b);
+      const double b2 = guard_b2(wt.y);
       const double thr = valid ? guard_thr(wt.x, b2) : __longlong_as_double(0x7ff0000000000000LL);
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) {
-        const double c = __dsub_rn(iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2), wt.x);
-        const double wv = fma(c, c, b2);
-        const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
-        const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
-        const double2 v = make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
+        const double2 v = sch_y_fp64(g, wt.x, wt.y, b2, thr, iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2));
         const FF vx = ff_of_rn(v.x), vy = ff_of_rn(v.y);
-        sm.y[k][iw * BP + pl] = v;
         sm.yf[k][iw * BP + pl] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
         chunk_wide = chunk_wide || !ff_range(v.x, v.y);
       }
@@ -420,17 +474,28 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
       const FF nx = ff_of_rn(v.x), ny = ff_of_rn(v.y);
       sm.nf[k][bl] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
-      sm.n[k][bl] = v;
       chunk_wide = chunk_wide || !ff_range(v.x, v.y);
     }
     chunk_wide = __syncthreads_or(chunk_wide);
 
     if (!chunk_wide) {
       // every term n Y as a float-float product on the FP32 pipe; the high
-      // halves of two g-vectors' terms added exactly (TwoSum), the sum
-      // widened on the integer pipe and added in FP64 (1 FP64 operation
-      // per term), the rounding error and the low halves added in FP32
+      // halves of two g-vectors' terms added exactly (TwoSum) and their sum
+      // added exactly (TwoSum) to the chunk's FP32 sum, the rounding errors
+      // and the low halves summed in FP32; the chunk's pair of sums widened
+      // on the integer pipe and added to the FP64 sums at its end (4 FP64
+      // operations per output and chunk: 1/4 per term)
       static_assert(kCKY % 2 == 0, "g-vector pairs");
+      float2 ach[TB][TC][kNW], acl[TB][TC][kNW];
+#pragma unroll
+      for (int i = 0; i < TB; ++i)
+#pragma unroll
+        for (int j = 0; j < TC; ++j)
+#pragma unroll
+          for (int iw = 0; iw < kNW; ++iw) {
+            ach[i][j][iw] = make_float2(0.f, 0.f);
+            acl[i][j][iw] = make_float2(0.f, 0.f);
+          }
 #pragma unroll 1
       for (int k = 0; k < kCKY; k += 2) {
         FF yx[2][TC][kNW], yy[2][TC][kNW];
@@ -456,13 +521,14 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
               const FF i0 = ff_dot2_raw(nx[0], yy[0][j][iw], ff_neg(ny[0]), yx[0][j][iw]);
               const FF r1 = ff_dot2_raw(nx[1], yx[1][j][iw], ny[1], yy[1][j][iw]);
               const FF i1 = ff_dot2_raw(nx[1], yy[1][j][iw], ff_neg(ny[1]), yx[1][j][iw]);
-              float sr, er, si, ei;
+              float sr, er, si, ei, hr, gr, hi, gi;
               two_sum_f(r0.hi, r1.hi, sr, er);
               two_sum_f(i0.hi, i1.hi, si, ei);
-              acc[i][j][iw].x += f32_widen(sr);
-              acc[i][j][iw].y += f32_widen(si);
-              acl[i][j][iw].x += (er + r0.lo) + r1.lo;
-              acl[i][j][iw].y += (ei + i0.lo) + i1.lo;
+              two_sum_f(ach[i][j][iw].x, sr, hr, gr);
+              two_sum_f(ach[i][j][iw].y, si, hi, gi);
+              ach[i][j][iw] = make_float2(hr, hi);
+              acl[i][j][iw].x += ((er + r0.lo) + r1.lo) + gr;
+              acl[i][j][iw].y += ((ei + i0.lo) + i1.lo) + gi;
             }
         }
       }
@@ -472,26 +538,12 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         for (int j = 0; j < TC; ++j)
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            acc[i][j][iw].x += f32_widen(acl[i][j][iw].x);
-            acc[i][j][iw].y += f32_widen(acl[i][j][iw].y);
-            acl[i][j][iw] = make_float2(0.f, 0.f);
+            double2& a = sm.acc[(i * TC + j) * kNW + iw][tid];
+            a.x = (a.x + f32_widen(ach[i][j][iw].x)) + f32_widen(acl[i][j][iw].x);
+            a.y = (a.y + f32_widen(ach[i][j][iw].y)) + f32_widen(acl[i][j][iw].y);
           }
     } else {
-      // a chunk with a factor or an aqsn element outside the float-float
-      // range: FP64 multiply-adds on the FP64 copies
-      for (int k = 0; k < kCKY; ++k)
-#pragma unroll
-        for (int i = 0; i < TB; ++i) {
-          const double2 nn = sm.n[k][ty + 16 * i];
-#pragma unroll
-          for (int j = 0; j < TC; ++j)
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) {
-              const double2 yv = sm.y[k][iw * BP + tx + 16 * j];
-              acc[i][j][iw].x = fma(nn.x, yv.x, fma(-nn.y, yv.y, acc[i][j][iw].x));
-              acc[i][j][iw].y = fma(nn.x, yv.y, fma(nn.y, yv.x, acc[i][j][iw].y));
-            }
-        }
+      sch_fp64y_wide_chunk<BN, BP>(p, sm.acc, tid, ig0, ig_end, n1_0, band_end, p0, wx0, wx1, wx2);
     }
   }
 
@@ -518,7 +570,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         const double f = 0.5 * p.vcoul[igp];
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          const double2 v = cmul(acc[i][j][iw], m);
+          const double2 v = cmul(sm.acc[(i * TC + j) * kNW + iw][tid], m);
           part[iw].x = fma(v.x, f, part[iw].x);
           part[iw].y = fma(v.y, f, part[iw].y);
         }
@@ -986,9 +1038,12 @@ __global__ void __launch_bounds__(kThreads) ssx_fp64_batch_kernel(GppBatchView b
   }
 }
 
+// The shared-memory carve-out at its maximum: two CTAs of the main passes
+// hold up to ~210 KB between them.
 template <typename K>
 int blocks_per_sm(K kernel, size_t smem) {
   int n = 0;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kThreads, smem);
   return n > 0 ? n : 1;
@@ -1006,6 +1061,9 @@ cudaError_t launch_sch_fp64y(const GppDev& p, const GppWork& w, int grid, cudaSt
   cudaError_t e = cudaFuncSetAttribute(sch_fp64y_kernel<kBNY, kBPY>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(sch_fp64y_kernel<kBNY, kBPY>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
   sch_fp64y_kernel<kBNY, kBPY><<<grid, kThreads, smem, s>>>(p, w);
   return cudaGetLastError();
 }
@@ -1021,11 +1079,17 @@ cudaError_t launch_sch_fp64y_batch(const GppBatchView& b, int grid, bool small, 
     cudaError_t e = cudaFuncSetAttribute(sch_fp64y_batch_kernel<true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSchYBatchSmallSmem);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(sch_fp64y_batch_kernel<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
     sch_fp64y_batch_kernel<true><<<grid, kThreads, kSchYBatchSmallSmem, s>>>(b);
     return cudaGetLastError();
   }
   cudaError_t e = cudaFuncSetAttribute(sch_fp64y_batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kSchYBatchSmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(sch_fp64y_batch_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   sch_fp64y_batch_kernel<false><<<grid, kThreads, kSchYBatchSmem, s>>>(b);
   return cudaGetLastError();
