@@ -324,21 +324,26 @@ struct SchYSmem {
   // x 3 frequencies), one slot row per output: a warp's accesses are 512
   // contiguous bytes
   double2 acc[(BN / 16) * (BP / 16) * kNW][kThreads];
-  float4 yf[kCKY][kNW * BP + 1];  // [k][iw * BP + column]: Y as float-float (x.hi, x.lo, y.hi, y.lo)
-  float4 nf[kCKY][BN + 1];        // aqsn as float-float
+  // Y as float-float operands of paired (f32x2) instructions whose lanes are
+  // a term's real and imaginary parts: [k][iw * BP + column] holds (Re.hi,
+  // Im.hi, -Re.lo, -Im.lo) of Y and [k][kNW * BP + iw * BP + column] those of
+  // i Y, (-Im.hi, Re.hi, Im.lo, -Re.lo); one padding element per row
+  float4 y[kCKY][2 * kNW * BP + 1];
+  // aqsn: [k][band] (Re.hi, Re.hi, Re.lo, Re.lo), [k][BN + band] the same of Im
+  float4 n[kCKY][2 * BN + 1];
 };
 
 // Y = G (c + i b) / |wdiff|^2 of one (column, g-vector) element at frequency
-// wx in FP64 (G = I_eps wtilde, a + i b = wtilde, c = wx - a, b2 = b^2, thr
-// the pole guard's threshold; 0 where the guard drops the term, and for
-// padding elements, whose thr is infinite): ~13 FP64 operations, shared by
-// every band of the item.
-__device__ __forceinline__ double2 sch_y_fp64(double2 g, double a, double b, double b2, double thr, double wx) {
+// wx in FP64 (G = I_eps wtilde, a + i b = wtilde, c = wx - a, b2 = b^2, gb =
+// G b, thr the pole guard's threshold; 0 where the guard drops the term, and
+// for padding elements, whose thr is infinite): ~11 FP64 operations, shared
+// by every band of the item.
+__device__ __forceinline__ double2 sch_y_fp64(double2 g, double2 gb, double a, double b2, double thr, double wx) {
   const double c = __dsub_rn(wx, a);
   const double wv = fma(c, c, b2);
-  const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
-  const double zr = __dmul_rn(c, r), zi = __dmul_rn(b, r);
-  return make_double2(fma(g.x, zr, -__dmul_rn(g.y, zi)), fma(g.x, zi, __dmul_rn(g.y, zr)));
+  if (!keep_nonneg(wv, thr)) return make_double2(0.0, 0.0);
+  const double r = rcp_f64_seed32(wv);
+  return make_double2(__dmul_rn(fma(g.x, c, -gb.y), r), __dmul_rn(fma(g.y, c, gb.x), r));
 }
 
 // A chunk holding a factor or an aqsn element outside the float-float range:
@@ -369,10 +374,11 @@ static __device__ __noinline__ void sch_fp64y_wide_chunk(const GppDev& p, double
         ie = p.ieps[off];
       }
       const double2 g = cmul(ie, wt);
+      const double2 gb = make_double2(__dmul_rn(g.x, wt.y), __dmul_rn(g.y, wt.y));
       const double b2 = guard_b2(wt.y);
       const double thr = valid ? guard_thr(wt.x, b2) : __longlong_as_double(0x7ff0000000000000LL);
       for (int iw = 0; iw < kNW; ++iw)
-        y[j][iw] = sch_y_fp64(g, wt.x, wt.y, b2, thr, iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2));
+        y[j][iw] = sch_y_fp64(g, gb, wt.x, b2, thr, iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2));
     }
     for (int i = 0; i < TB; ++i) {
       const int n1 = n1_0 + ty + 16 * i;
@@ -432,10 +438,22 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   const int ig_end = min(ig_begin + w.split_len, p.nc);
   const double wx0 = p.wx[0], wx1 = p.wx[1], wx2 = p.wx[2];
 
-  // the item's FP64 sums live in shared memory (registers hold one chunk's
-  // float-float sums); each thread touches only its own slots
+  // the item's FP64 sums live in shared memory, each thread touching only
+  // its own slots; registers hold float-float sums (lanes: real and
+  // imaginary parts): the high pair is added to the FP64 sums after each
+  // chunk, the low pair carries the remainder into the next
 #pragma unroll
   for (int o = 0; o < TB * TC * kNW; ++o) sm.acc[o][tid] = make_double2(0.0, 0.0);
+  float2 ach[TB][TC][kNW], acl[TB][TC][kNW];
+#pragma unroll
+  for (int i = 0; i < TB; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        ach[i][j][iw] = make_float2(0.f, 0.f);
+        acl[i][j][iw] = make_float2(0.f, 0.f);
+      }
 
   for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCKY) {
     __syncthreads();
@@ -452,18 +470,20 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         wt = p.wt[off];
         ie = p.ieps[off];
       }
-      // Y in FP64 (~41 FP64 operations per column and g-vector, shared by
+      // Y in FP64 (~40 FP64 operations per column and g-vector, shared by
       // the item's 64 bands x 3 frequencies), split as float-float pairs
       // for the terms; the pole guard is the int64 compare against the
       // per-element threshold
       const double2 g = cmul(ie, wt);
+      const double2 gb = make_double2(__dmul_rn(g.x, wt.y), __dmul_rn(g.y, wt.y));
       const double b2 = guard_b2(wt.y);
       const double thr = valid ? guard_thr(wt.x, b2) : __longlong_as_double(0x7ff0000000000000LL);
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) {
-        const double2 v = sch_y_fp64(g, wt.x, wt.y, b2, thr, iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2));
+        const double2 v = sch_y_fp64(g, gb, wt.x, b2, thr, iw == 0 ? wx0 : (iw == 1 ? wx1 : wx2));
         const FF vx = ff_of_rn(v.x), vy = ff_of_rn(v.y);
-        sm.yf[k][iw * BP + pl] = make_float4(vx.hi, vx.lo, vy.hi, vy.lo);
+        sm.y[k][iw * BP + pl] = make_float4(vx.hi, vy.hi, -vx.lo, -vy.lo);
+        sm.y[k][kNW * BP + iw * BP + pl] = make_float4(-vy.hi, vx.hi, vy.lo, -vx.lo);
         chunk_wide = chunk_wide || !ff_range(v.x, v.y);
       }
     }
@@ -473,62 +493,71 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
       const FF nx = ff_of_rn(v.x), ny = ff_of_rn(v.y);
-      sm.nf[k][bl] = make_float4(nx.hi, nx.lo, ny.hi, ny.lo);
+      sm.n[k][bl] = make_float4(nx.hi, nx.hi, nx.lo, nx.lo);
+      sm.n[k][BN + bl] = make_float4(ny.hi, ny.hi, ny.lo, ny.lo);
       chunk_wide = chunk_wide || !ff_range(v.x, v.y);
     }
     chunk_wide = __syncthreads_or(chunk_wide);
 
     if (!chunk_wide) {
-      // every term n Y as a float-float product on the FP32 pipe; the high
-      // halves of two g-vectors' terms added exactly (TwoSum) and their sum
-      // added exactly (TwoSum) to the chunk's FP32 sum, the rounding errors
-      // and the low halves summed in FP32; the chunk's pair of sums widened
-      // on the integer pipe and added to the FP64 sums at its end (4 FP64
-      // operations per output and chunk: 1/4 per term)
-      static_assert(kCKY % 2 == 0, "g-vector pairs");
-      float2 ach[TB][TC][kNW], acl[TB][TC][kNW];
-#pragma unroll
-      for (int i = 0; i < TB; ++i)
+      // every term n Y as a float-float product on the FP32 pipe, in paired
+      // (f32x2) instructions whose two lanes are the term's real and
+      // imaginary parts: n Y = nr Y + ni (i Y), two products of a broadcast
+      // pair and a lane pair; the products' exact errors and cross terms
+      // formed negated (negated multiplicands: no instruction negates an
+      // addend); the term's high half added exactly (TwoSum) to the chunk's
+      // FP32 sum, the rounding errors and low halves summed in FP32; at the
+      // chunk's end the pair renormalised (Fast2Sum: |high| >= |low| up to
+      // cancellation, where the low pair's bits are few), the new high half
+      // widened on the integer pipe and added to the FP64 sums and the low
+      // half kept (2 FP64 operations per output and chunk: 1/8 per term).  Differences as fma(x, -1, y), exact up to their one
+      // rounding.
+      const float2 m1 = make_float2(-1.f, -1.f);
+#pragma unroll 1
+      for (int k = 0; k < kCKY; ++k) {
+        // per (column, frequency): Y's high pair and its negation, the
+        // negated low pair, and the same three of i Y
+        float2 ah[TC][kNW], anh[TC][kNW], anl[TC][kNW], bh[TC][kNW], bnh[TC][kNW], bnl[TC][kNW];
 #pragma unroll
         for (int j = 0; j < TC; ++j)
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
-            ach[i][j][iw] = make_float2(0.f, 0.f);
-            acl[i][j][iw] = make_float2(0.f, 0.f);
+            const float4 a = sm.y[k][iw * BP + tx + 16 * j];
+            const float4 b = sm.y[k][kNW * BP + iw * BP + tx + 16 * j];
+            ah[j][iw] = f4_lo(a);
+            anl[j][iw] = f4_hi(a);
+            anh[j][iw] = __fmul2_rn(ah[j][iw], m1);
+            bh[j][iw] = f4_lo(b);
+            bnl[j][iw] = f4_hi(b);
+            bnh[j][iw] = __fmul2_rn(bh[j][iw], m1);
           }
-#pragma unroll 1
-      for (int k = 0; k < kCKY; k += 2) {
-        FF yx[2][TC][kNW], yy[2][TC][kNW];
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-#pragma unroll
-          for (int j = 0; j < TC; ++j)
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) {
-              const float4 v = sm.yf[k + h][iw * BP + tx + 16 * j];
-              yx[h][j][iw] = FF{v.x, v.y};
-              yy[h][j][iw] = FF{v.z, v.w};
-            }
 #pragma unroll
         for (int i = 0; i < TB; ++i) {
-          const float4 v0 = sm.nf[k][ty + 16 * i], v1 = sm.nf[k + 1][ty + 16 * i];
-          const FF nx[2] = {FF{v0.x, v0.y}, FF{v1.x, v1.y}}, ny[2] = {FF{v0.z, v0.w}, FF{v1.z, v1.w}};
+          const float4 vr = sm.n[k][ty + 16 * i], vi = sm.n[k][BN + ty + 16 * i];
+          const float2 rh = f4_lo(vr), rl = f4_hi(vr), ih = f4_lo(vi), il = f4_hi(vi);
 #pragma unroll
           for (int j = 0; j < TC; ++j)
 #pragma unroll
             for (int iw = 0; iw < kNW; ++iw) {
-              const FF r0 = ff_dot2_raw(nx[0], yx[0][j][iw], ny[0], yy[0][j][iw]);
-              const FF i0 = ff_dot2_raw(nx[0], yy[0][j][iw], ff_neg(ny[0]), yx[0][j][iw]);
-              const FF r1 = ff_dot2_raw(nx[1], yx[1][j][iw], ny[1], yy[1][j][iw]);
-              const FF i1 = ff_dot2_raw(nx[1], yy[1][j][iw], ff_neg(ny[1]), yx[1][j][iw]);
-              float sr, er, si, ei, hr, gr, hi, gi;
-              two_sum_f(r0.hi, r1.hi, sr, er);
-              two_sum_f(i0.hi, i1.hi, si, ei);
-              two_sum_f(ach[i][j][iw].x, sr, hr, gr);
-              two_sum_f(ach[i][j][iw].y, si, hi, gi);
-              ach[i][j][iw] = make_float2(hr, hi);
-              acl[i][j][iw].x += ((er + r0.lo) + r1.lo) + gr;
-              acl[i][j][iw].y += ((ei + i0.lo) + i1.lo) + gi;
+              const float2 p1 = __fmul2_rn(rh, ah[j][iw]);
+              const float2 p2 = __fmul2_rn(ih, bh[j][iw]);
+              // -(exact errors of p1, p2 + cross terms)
+              const float2 g1 = __ffma2_rn(rh, anl[j][iw], __ffma2_rn(rl, anh[j][iw], __ffma2_rn(rh, anh[j][iw], p1)));
+              const float2 g2 = __ffma2_rn(ih, bnl[j][iw], __ffma2_rn(il, bnh[j][iw], __ffma2_rn(ih, bnh[j][iw], p2)));
+              // s + es = p1 + p2 (TwoSum)
+              const float2 s = __fadd2_rn(p1, p2);
+              const float2 bv = __ffma2_rn(p1, m1, s);
+              const float2 av = __ffma2_rn(bv, m1, s);
+              const float2 es = __fadd2_rn(__ffma2_rn(av, m1, p1), __ffma2_rn(bv, m1, p2));
+              const float2 lo = __ffma2_rn(__fadd2_rn(g1, g2), m1, es);
+              // chunk sum: high pair += s (TwoSum), low pair += its error + lo
+              float2& h = ach[i][j][iw];
+              const float2 hs = __fadd2_rn(h, s);
+              const float2 hb = __ffma2_rn(h, m1, hs);
+              const float2 ha = __ffma2_rn(hb, m1, hs);
+              const float2 he = __fadd2_rn(__ffma2_rn(ha, m1, h), __ffma2_rn(hb, m1, s));
+              h = hs;
+              acl[i][j][iw] = __fadd2_rn(acl[i][j][iw], __fadd2_rn(he, lo));
             }
         }
       }
@@ -538,14 +567,28 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         for (int j = 0; j < TC; ++j)
 #pragma unroll
           for (int iw = 0; iw < kNW; ++iw) {
+            const float2 s = __fadd2_rn(ach[i][j][iw], acl[i][j][iw]);
+            acl[i][j][iw] = __ffma2_rn(__ffma2_rn(ach[i][j][iw], m1, s), m1, acl[i][j][iw]);
+            ach[i][j][iw] = make_float2(0.f, 0.f);
             double2& a = sm.acc[(i * TC + j) * kNW + iw][tid];
-            a.x = (a.x + f32_widen(ach[i][j][iw].x)) + f32_widen(acl[i][j][iw].x);
-            a.y = (a.y + f32_widen(ach[i][j][iw].y)) + f32_widen(acl[i][j][iw].y);
+            a.x += f32_widen(s.x);
+            a.y += f32_widen(s.y);
           }
     } else {
       sch_fp64y_wide_chunk<BN, BP>(p, sm.acc, tid, ig0, ig_end, n1_0, band_end, p0, wx0, wx1, wx2);
     }
   }
+  // the low pairs' remainders
+#pragma unroll
+  for (int i = 0; i < TB; ++i)
+#pragma unroll
+    for (int j = 0; j < TC; ++j)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        double2& a = sm.acc[(i * TC + j) * kNW + iw][tid];
+        a.x += f32_widen(acl[i][j][iw].x);
+        a.y += f32_widen(acl[i][j][iw].y);
+      }
 
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp]; the 16 lanes of a
   // half-warp hold the item's columns for the same bands and sum them with
