@@ -336,13 +336,16 @@ struct SchYSmem {
 // Y = G (c + i b) / |wdiff|^2 of one (column, g-vector) element at frequency
 // wx in FP64 (G = I_eps wtilde, a + i b = wtilde, c = wx - a, b2 = b^2, gb =
 // G b, thr the pole guard's threshold; 0 where the guard drops the term, and
-// for padding elements, whose thr is infinite): ~11 FP64 operations, shared
-// by every band of the item.
+// for padding elements, whose thr is infinite): ~9 FP64 operations and a
+// reciprocal to the FP64 rounding unit, shared by every band of the item.
+// (A float-float quotient, or the reciprocal's two-DFMA form from an FP32
+// seed, measured 1.8 and 1.4 times the error in the most cancelling band
+// sums.)
 __device__ __forceinline__ double2 sch_y_fp64(double2 g, double2 gb, double a, double b2, double thr, double wx) {
   const double c = __dsub_rn(wx, a);
   const double wv = fma(c, c, b2);
   if (!keep_nonneg(wv, thr)) return make_double2(0.0, 0.0);
-  const double r = rcp_f64_seed32(wv);
+  const double r = rcp_f64(wv);
   return make_double2(__dmul_rn(fma(g.x, c, -gb.y), r), __dmul_rn(fma(g.y, c, gb.x), r));
 }
 
@@ -441,7 +444,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
   // the item's FP64 sums live in shared memory, each thread touching only
   // its own slots; registers hold float-float sums (lanes: real and
   // imaginary parts): the high pair is added to the FP64 sums after each
-  // chunk, the low pair carries the remainder into the next
+  // float-float chunk, the low pair carries the remainder on
 #pragma unroll
   for (int o = 0; o < TB * TC * kNW; ++o) sm.acc[o][tid] = make_double2(0.0, 0.0);
   float2 ach[TB][TC][kNW], acl[TB][TC][kNW];
@@ -470,10 +473,11 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
         wt = p.wt[off];
         ie = p.ieps[off];
       }
-      // Y in FP64 (~40 FP64 operations per column and g-vector, shared by
-      // the item's 64 bands x 3 frequencies), split as float-float pairs
-      // for the terms; the pole guard is the int64 compare against the
-      // per-element threshold
+      // Y in FP64 (~37 FP64 operations per column and g-vector, shared by
+      // the item's 64 bands x 3 frequencies; the pole guard the int64
+      // compare against the per-element threshold), split as float-float
+      // pairs for the terms; a factor outside the float-float range sends
+      // the chunk to the FP64 path
       const double2 g = cmul(ie, wt);
       const double2 gb = make_double2(__dmul_rn(g.x, wt.y), __dmul_rn(g.y, wt.y));
       const double b2 = guard_b2(wt.y);
@@ -510,7 +514,9 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       // chunk's end the pair renormalised (Fast2Sum: |high| >= |low| up to
       // cancellation, where the low pair's bits are few), the new high half
       // widened on the integer pipe and added to the FP64 sums and the low
-      // half kept (2 FP64 operations per output and chunk: 1/8 per term).  Differences as fma(x, -1, y), exact up to their one
+      // half kept (2 FP64 operations per output and chunk: 1/8 per term;
+      // a flush every second chunk measured 3 % slower, its registers
+      // spilling).  Differences as fma(x, -1, y), exact up to their one
       // rounding.
       const float2 m1 = make_float2(-1.f, -1.f);
 #pragma unroll 1
@@ -578,7 +584,7 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
       sch_fp64y_wide_chunk<BN, BP>(p, sm.acc, tid, ig0, ig_end, n1_0, band_end, p0, wx0, wx1, wx2);
     }
   }
-  // the low pairs' remainders
+  // what the float-float sums still hold
 #pragma unroll
   for (int i = 0; i < TB; ++i)
 #pragma unroll
@@ -586,8 +592,8 @@ __device__ __forceinline__ void sch_fp64y_item(const GppDev& p, const GppWork& w
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) {
         double2& a = sm.acc[(i * TC + j) * kNW + iw][tid];
-        a.x += f32_widen(acl[i][j][iw].x);
-        a.y += f32_widen(acl[i][j][iw].y);
+        a.x = (a.x + f32_widen(ach[i][j][iw].x)) + f32_widen(acl[i][j][iw].x);
+        a.y = (a.y + f32_widen(ach[i][j][iw].y)) + f32_widen(acl[i][j][iw].y);
       }
 
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp]; the 16 lanes of a
