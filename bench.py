@@ -298,20 +298,28 @@ def timed(torch, dist, world, fn, steps, stream):
     return ms
 
 
-# FP64 pipe operations of sch_fp64y_kernel per term, counted from its
-# algorithm: 1 FP64 addition (the exact sum of two g-vectors' float-float
-# terms' high halves, widened, into the FP64 sums of the real and imaginary
-# parts: 2 per 2 terms) + the fold of the low halves' FP32 sums into the FP64
-# sums once per 16-g-vector chunk (2 per 16 terms) + the shared frequency
-# factor in FP64 (~41 per column and g-vector over 64 bands x 3 frequencies
-# = 192 terms).
-FP64_PIPE_OPS_PER_TERM = 1.0 + 2.0 / 16 + 41.0 / 192
+# FMA-pipe (FP32) lane operations of sch_fp64y_kernel per term, counted from
+# its algorithm: 24 paired (f32x2) instructions per term (two products, six
+# FMAs of their exact errors and cross terms, one addition, a TwoSum of the
+# products, the low sum, a TwoSum into the chunk's float-float sum and two
+# additions of its low pair) = 48 lane operations, + the negated high pairs of
+# the frequency factors (2 paired per column, frequency and g-vector over 4
+# bands: 1 per term) + the chunk-end renormalisation (3 paired per output and
+# 16-g-vector chunk: 0.375 per term).
+FP64_FMA_LANE_OPS_PER_TERM = 48.0 + 1.0 + 6.0 / 16
+# FP64 pipe operations per term: the frequency factor in FP64 (~40 per column
+# and g-vector over 64 bands x 3 frequencies = 192 terms) + the chunk-end
+# addition of the float-float sums' high pairs (2 per output and 16-g-vector
+# chunk).
+FP64_PIPE_OPS_PER_TERM = 40.0 / 192 + 2.0 / 16
 # ncu, sch_fp64y_kernel, 128-band capture of the production instance
 # (--set full): dram__bytes_read.sum + dram__bytes_write.sum per term, and
-# sm__pipe_fp64_cycles_active over elapsed cycles.  Traffic scales with the
-# band blocks, so the per-term figure carries to the 512-band launch.
-FP64_DRAM_BYTES_PER_TERM = 0.1957
-FP64_PIPE_ACTIVE_NCU = 0.719
+# sm__pipe_fma_cycles_active / sm__pipe_fp64_cycles_active over elapsed
+# cycles.  Traffic scales with the band blocks, so the per-term figure
+# carries to the 512-band launch.
+FP64_DRAM_BYTES_PER_TERM = 0.1975
+FP64_FMA_PIPE_ACTIVE_NCU = 0.713
+FP64_PIPE_ACTIVE_NCU = 0.297
 # FP32 pipe operations of sch_mixedy_kernel per term: 4 FFMA (complex
 # multiply-add) + the float-float fold of each accumulator every 8 g-vectors
 # (2 x 7 operations / 8) + the shared frequency factor (~10 per column,
@@ -807,7 +815,8 @@ def run_ours(args, rank, world, local_rank):
     value = terms * world / (ms_step * 1e-3) / 1e9
     main_s = kt["main_ms"] / max(1, kt["executions"]) * 1e-3
     algorithmic_tflops = FLOP_PER_TERM * terms / main_s / 1e12
-    pipe_tflops = 2 * FP64_PIPE_OPS_PER_TERM * terms / main_s / 1e12
+    pipe_tflops = 2 * FP64_FMA_LANE_OPS_PER_TERM * terms / main_s / 1e12
+    fp64_pipe_tflops = 2 * FP64_PIPE_OPS_PER_TERM * terms / main_s / 1e12
     production = (NB, NVB, NC, NPG) == PRODUCTION
     ref_prod = golden("config_gpp_production.npz") if production else None
     ref_stress = golden("config_gpp_stress.npz") if production else None
@@ -939,29 +948,35 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": (round(e2e_value, 4) if e2e_steps else None), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                 "path": "sigma_gpp_fp64 host C ABI, pinned buffers", "matches_device_path": e2e_match},
-        "roofline": {"bound": "fp64_pipe", "kernel": "sch_fp64y_kernel",
-                     "achieved": round(pipe_tflops, 4), "peak": round(fp64_pipe_peak, 4), "unit": "TFLOP/s",
-                     "frac": round(pipe_tflops / fp64_pipe_peak, 4),
+        "roofline": {"bound": "fp32_pipe", "kernel": "sch_fp64y_kernel",
+                     "achieved": round(pipe_tflops, 4), "peak": round(fp32_pipe_peak, 4), "unit": "TFLOP/s",
+                     "frac": round(pipe_tflops / fp32_pipe_peak, 4),
                      "traffic": round(FP64_DRAM_BYTES_PER_TERM * terms),
                      "kernel_ms_per_launch": round(main_s * 1e3, 3),
-                     "fp64_pipe_ops_per_term": round(FP64_PIPE_OPS_PER_TERM, 4),
-                     "peak_source": f"FP64 pipe 2 DFMA/clk/SM x {sms} SMs x {clock_mhz:.0f} MHz "
-                                    "(SM clock sampled during the timed region; the measured-peaks file "
-                                    "has no FP64 figure); dependent-FMA probe on this device: "
-                                    f"{fp64_peak:.3f} TFLOP/s",
-                     "ncu_fp64_pipe_active": FP64_PIPE_ACTIVE_NCU,
+                     "fma_lane_ops_per_term": round(FP64_FMA_LANE_OPS_PER_TERM, 4),
+                     "peak_source": f"FMA pipe 128 lanes/clk/SM x {sms} SMs x {clock_mhz:.0f} MHz, 2 flop "
+                                    "per lane operation (SM clock sampled during the timed region; the "
+                                    "measured-peaks file has no FP32 figure)",
+                     "ncu_fma_pipe_active": FP64_FMA_PIPE_ACTIVE_NCU,
+                     "fp64_pipe": {"achieved": round(fp64_pipe_tflops, 4), "peak": round(fp64_pipe_peak, 4),
+                                   "frac": round(fp64_pipe_tflops / fp64_pipe_peak, 4),
+                                   "ops_per_term": round(FP64_PIPE_OPS_PER_TERM, 4),
+                                   "ncu_active": FP64_PIPE_ACTIVE_NCU,
+                                   "peak_source": f"FP64 pipe 2 DFMA/clk/SM x {sms} SMs at the sampled clock; "
+                                                  f"dependent-FMA probe on this device: {fp64_peak:.3f} TFLOP/s"},
                      "algorithmic": {"flop_per_term": FLOP_PER_TERM,
                                      "tflops": round(algorithmic_tflops, 4),
                                      "note": "the reference's 27 flop per term (its own formulation, which "
                                              "rebuilds the frequency factor for every band) at the measured "
                                              "term rate: a rate, not a pipe fraction"},
-                     "note": "achieved = FP64 pipe work of the kernel's own algorithm (each FP64 pipe "
-                             "instruction counted as one DFMA slot, 2 flop): with one frequency set for all "
-                             "bands the frequency factor is formed in FP64 once per column and g-vector; "
-                             "every term is formed as a float-float product on the FP32 pipe, the high "
-                             "halves of two g-vectors' terms added exactly and the sum added in FP64, the "
-                             "low halves and rounding errors summed in FP32 per 16-g-vector chunk and then "
-                             "added; traffic = ncu DRAM bytes per term x terms"},
+                     "note": "achieved = FMA-pipe work of the kernel's own algorithm (each lane operation "
+                             "one FMA slot, 2 flop): with one frequency set for all bands the frequency "
+                             "factor is formed in FP64 once per column and g-vector and split to float-float; "
+                             "every term is a float-float product in paired FP32 instructions (real and "
+                             "imaginary parts as the two lanes), added exactly (TwoSum) to a per-chunk "
+                             "float-float sum whose high pair is added to the FP64 sums every 16 g-vectors; "
+                             "the FP64 pipe carries the factor and those additions (fp64_pipe); "
+                             "traffic = ncu DRAM bytes per term x terms"},
         "rel_err_vs_oracle": oracle,
         "mixed": {"value": round(mixed_value, 4), "unit": UNIT,
                   "speedup_vs_fp64": round(mixed_value / value, 3),
