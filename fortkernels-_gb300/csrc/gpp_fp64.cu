@@ -42,15 +42,21 @@ constexpr int kPad = 1;
 // float-float values, and flags (bit 0: the guard's second condition can
 // bind, bit 1: outside the float-float range, bit 2: no term); per
 // (g-vector, band) aqsn as a float-float pair and its range flag.
+// Each thread's FP64 sums (its 2 x 2 tile x 3 frequencies) live in shared
+// memory, one slot row per output; 16-g-vector chunks keep two CTAs' staging
+// and sums within an SM.
+constexpr int kCKB = 16;
+static_assert(kCK % kCKB == 0, "split lengths are multiples of the chunk");
 template <int BN, int BP>
 struct SchSmem {
-  double a[kCK][BP + kPad];
-  double b[kCK][BP + kPad];
-  float4 fb[kCK][BP + kPad];  // (b.hi, b.lo, b^2.hi, b^2.lo)
-  float4 fg[kCK][BP + kPad];  // (G.x hi, lo, G.y hi, lo)
-  unsigned flag[kCK][BP + kPad];
-  float4 fn[kCK][BN + kPad];  // (aqsn.x hi, lo, aqsn.y hi, lo)
-  unsigned nflag[kCK][BN + kPad];
+  double2 acc[2 * 2 * kNW][kThreads];
+  double a[kCKB][BP + kPad];
+  double b[kCKB][BP + kPad];
+  float4 fb[kCKB][BP + kPad];  // (b.hi, b.lo, b^2.hi, b^2.lo)
+  float4 fg[kCKB][BP + kPad];  // (G.x hi, lo, G.y hi, lo)
+  unsigned flag[kCKB][BP + kPad];
+  float4 fn[kCKB][BN + kPad];  // (aqsn.x hi, lo, aqsn.y hi, lo)
+  unsigned nflag[kCKB][BN + kPad];
 };
 constexpr unsigned kFlagBinds = 1u, kFlagWide = 2u, kFlagDead = 4u;
 
@@ -101,26 +107,29 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
       wx_wide[i] = wx_wide[i] || !ff_freq_range(wxr[i][iw]);
     }
   }
-  // FP64 sums of the terms' high halves; their low halves (below 2^-23 of
-  // the terms) summed in FP32 over one staged chunk and then added to the
-  // FP64 sums (an FP32 sum over a whole item's thousands of terms would lose
-  // ~n 2^-47 of the output)
-  double2 acc[2][2][kNW];
-  float2 acl[2][2][kNW];
+  // float-float sums in registers (lanes: real and imaginary parts): each
+  // term's high pair added exactly (TwoSum) to the high pair, the errors and
+  // low halves to the low pair; after each chunk the pair renormalised
+  // (Fast2Sum), its high pair added to the FP64 sums in shared memory and
+  // its low pair carried on (an FP32 sum over a whole item's thousands of
+  // terms would lose ~n 2^-47 of the output)
+  const float2 m1 = make_float2(-1.f, -1.f);
+  float2 ach[2][2][kNW], acl[2][2][kNW];
 #pragma unroll
   for (int i = 0; i < 2; ++i)
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
       for (int iw = 0; iw < kNW; ++iw) {
-        acc[i][j][iw] = make_double2(0.0, 0.0);
+        sm.acc[(i * 2 + j) * kNW + iw][tid] = make_double2(0.0, 0.0);
+        ach[i][j][iw] = make_float2(0.f, 0.f);
         acl[i][j][iw] = make_float2(0.f, 0.f);
       }
 
-  for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCK) {
+  for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kCKB) {
     __syncthreads();
-    for (int e = tid; e < kCK * BP; e += kThreads) {
-      const int k = e % kCK, pl = e / kCK;
+    for (int e = tid; e < kCKB * BP; e += kThreads) {
+      const int k = e % kCKB, pl = e / kCKB;
       const int ig = ig0 + k, my_igp = p0 + pl;
       double a = 0.0, b = 0.0;
       float4 fb = make_float4(0.f, 0.f, 0.f, 0.f), fg = fb;
@@ -146,8 +155,8 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
       sm.fg[k][pl] = fg;
       sm.flag[k][pl] = flag;
     }
-    for (int e = tid; e < kCK * BN; e += kThreads) {
-      const int k = e % kCK, bl = e / kCK;
+    for (int e = tid; e < kCKB * BN; e += kThreads) {
+      const int k = e % kCKB, bl = e / kCKB;
       const int ig = ig0 + k, n1 = n1_0 + bl;
       double2 v = make_double2(0.0, 0.0);
       if (ig < ig_end && n1 < band_end) v = p.aqsn[(size_t)n1 * p.nc + ig];
@@ -158,7 +167,7 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
     __syncthreads();
 
 #pragma unroll 1
-    for (int k = 0; k < kCK; ++k) {
+    for (int k = 0; k < kCKB; ++k) {
       double a[2], b[2];
       FF fb[2], fb2[2], gx[2], gy[2], nx[2], ny[2];
       unsigned flag[2], nflag[2];
@@ -207,14 +216,20 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
                 const double2 s = sch_term_fp64(p.aqsn, p.wt, p.ieps,
                                                 n1 < band_end ? (size_t)n1 * p.nc + ig : ~size_t(0),
                                                 (size_t)my_igp * p.nc + ig, wxr[i][iw]);
-                acc[i][j][iw].x += s.x;
-                acc[i][j][iw].y += s.y;
+                double2& a = sm.acc[(i * 2 + j) * kNW + iw][tid];
+                a.x += s.x;
+                a.y += s.y;
               }
             } else {
-              acc[i][j][iw].x += f32_widen(keep ? sx.hi : 0.f);
-              acc[i][j][iw].y += f32_widen(keep ? sy.hi : 0.f);
-              acl[i][j][iw].x += keep ? sx.lo : 0.f;
-              acl[i][j][iw].y += keep ? sy.lo : 0.f;
+              const float2 hv = keep ? make_float2(sx.hi, sy.hi) : make_float2(0.f, 0.f);
+              const float2 lv = keep ? make_float2(sx.lo, sy.lo) : make_float2(0.f, 0.f);
+              float2& h = ach[i][j][iw];
+              const float2 hs = __fadd2_rn(h, hv);
+              const float2 hb = __ffma2_rn(h, m1, hs);
+              const float2 ha = __ffma2_rn(hb, m1, hs);
+              const float2 he = __fadd2_rn(__ffma2_rn(ha, m1, h), __ffma2_rn(hb, m1, hv));
+              h = hs;
+              acl[i][j][iw] = __fadd2_rn(acl[i][j][iw], __fadd2_rn(he, lv));
             }
           }
         }
@@ -225,11 +240,24 @@ __device__ __forceinline__ void sch_fp64_item(const GppDev& p, const GppWork& w,
       for (int j = 0; j < 2; ++j)
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          acc[i][j][iw].x += f32_widen(acl[i][j][iw].x);
-          acc[i][j][iw].y += f32_widen(acl[i][j][iw].y);
-          acl[i][j][iw] = make_float2(0.f, 0.f);
+          const float2 s = __fadd2_rn(ach[i][j][iw], acl[i][j][iw]);
+          acl[i][j][iw] = __ffma2_rn(__ffma2_rn(ach[i][j][iw], m1, s), m1, acl[i][j][iw]);
+          ach[i][j][iw] = make_float2(0.f, 0.f);
+          double2& a = sm.acc[(i * 2 + j) * kNW + iw][tid];
+          a.x += f32_widen(s.x);
+          a.y += f32_widen(s.y);
         }
   }
+  double2 acc[2][2][kNW];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int iw = 0; iw < kNW; ++iw) {
+        const double2 a = sm.acc[(i * 2 + j) * kNW + iw][tid];
+        acc[i][j][iw] = make_double2(a.x + f32_widen(acl[i][j][iw].x), a.y + f32_widen(acl[i][j][iw].y));
+      }
 
   // epilogue: x conj(aqsm[n1][igp]) * 0.5 * vcoul[igp], then a fixed-order
   // sum over the tile's columns
@@ -1149,6 +1177,9 @@ cudaError_t launch_sch_fp64(const GppDev& p, const GppWork& w, int grid, cudaStr
   constexpr size_t smem = sizeof(SchSmem<kBN, kBP>);
   cudaError_t e = cudaFuncSetAttribute(sch_fp64_kernel<kBN, kBP>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(sch_fp64_kernel<kBN, kBP>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   sch_fp64_kernel<kBN, kBP><<<grid, kThreads, smem, s>>>(p, w);
   return cudaGetLastError();
