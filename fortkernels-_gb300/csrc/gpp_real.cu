@@ -6,13 +6,14 @@
 // (b = 0), so scha = aqsm[n1][igp] * aqsn[n1][ig] * Y_iw[my_igp][ig] with the
 // band-independent factor Y_iw = I_eps wtilde c / c^2 (c = wx - wtilde; 0 when
 // dropped).  The main pass forms Y in FP64 per staged chunk and stages it, and
-// aqsn, also as float-float pairs; every term aqsn Y is then a float-float
-// product on the FP32 pipe, the high halves of two g-vectors' terms are added
-// exactly (TwoSum) and their sum widened and added in FP64 (half an FP64
-// operation per term, against one DFMA), the rounding errors and low halves
-// summed in FP32 and folded into the FP64 sums once per chunk.  A chunk with
-// a value outside the float-float range runs FP64 multiply-adds on the FP64
-// copies.  Occupied bands add
+// aqsn, as float-float pairs; every term aqsn Y is then a float-float product
+// on the FP32 pipe, the high halves of two g-vectors' terms are added exactly
+// (TwoSum) and their sum added exactly to the chunk's float-float sum, the
+// rounding errors and low halves summed in FP32; after each chunk that sum is
+// renormalised and its high half widened and added to the FP64 sums, kept in
+// shared memory (1/32 FP64 operation per term, against one DFMA).  A chunk
+// with a value outside the float-float range forms its factors again in FP64
+// and runs FP64 multiply-adds.  Occupied bands add
 //   ssx = Omega2 / wx^2 (kept), -G / (2 (wx + wtilde)) (dropped with
 //   delw^2 > to1), 0 otherwise,
 // in FP64 (G = I_eps wtilde, Omega2 = wtilde G).  Partial sums use the
@@ -50,11 +51,60 @@ struct GppRealDev {
 // coalesced direction of the global reads), so unpadded rows, whose strides
 // are multiples of 128 bytes, put a warp's writes in one bank.
 struct RealSmem {
-  double y[kRCK][kNW * kRBP + 1];  // [k][iw * kRBP + column]
-  double n[kRCK][kRBN + 1];
-  float2 yf[kRCK][kNW * kRBP + 1];  // the same as float-float pairs
-  float2 nf[kRCK][kRBN + 1];
+  // each thread's FP64 sums (4 bands x 2 columns x 3 frequencies), one slot
+  // row per output: a warp's accesses are contiguous
+  double acc[(kRBN / 16) * (kRBP / 16) * kNW][kThreads];
+  float2 yf[kRCK][kNW * kRBP + 1];  // [k][iw * kRBP + column]: Y as float-float
+  float2 nf[kRCK][kRBN + 1];        // aqsn as float-float
 };
+
+// Y = I_eps wtilde c / c^2 (c = wx - wtilde) of one (column, g-vector)
+// element in FP64, 0 where the guard drops the term or the element is
+// padding; the reciprocal to the FP64 rounding unit.
+__device__ __forceinline__ double real_y(double wt, double g, double thr, double wx) {
+  const double c = __dsub_rn(wx, wt);
+  const double wv = __dmul_rn(c, c);
+  return keep_nonneg(wv, thr) ? g * (c * rcp_f64(wv)) : 0.0;
+}
+
+// A chunk holding a factor or an aqsn element outside the float-float range:
+// FP64 multiply-adds of the thread's register tile, its factors formed again
+// from the inputs and aqsn read again, added to the thread's FP64 sums.  Out
+// of line: the common path carries none of its registers.
+static __device__ __noinline__ void real_wide_chunk(const GppRealDev& p, double (*acc)[kThreads], int tid,
+                                                    int ig0, int ig_end, int n1_0, int p0, double wx0,
+                                                    double wx1, double wx2) {
+  constexpr int TB = kRBN / 16, TC = kRBP / 16;
+  const int tx = tid & 15, ty = tid >> 4;
+  double aw[TB][TC][kNW];
+  for (int i = 0; i < TB; ++i)
+    for (int j = 0; j < TC; ++j)
+      for (int iw = 0; iw < kNW; ++iw) aw[i][j][iw] = 0.0;
+  for (int k = 0; k < kRCK; ++k) {
+    const int ig = ig0 + k;
+    double y[TC][kNW];
+    for (int j = 0; j < TC; ++j) {
+      const int my_igp = p0 + tx + 16 * j;
+      for (int iw = 0; iw < kNW; ++iw) y[j][iw] = 0.0;
+      if (ig < ig_end && my_igp < p.ng) {
+        const size_t off = (size_t)my_igp * p.nc + ig;
+        const double wt = p.wt[off], g = p.ieps[off] * wt, thr = guard_thr(wt, 0.0);
+        y[j][0] = real_y(wt, g, thr, wx0);
+        y[j][1] = real_y(wt, g, thr, wx1);
+        y[j][2] = real_y(wt, g, thr, wx2);
+      }
+    }
+    for (int i = 0; i < TB; ++i) {
+      const int n1 = n1_0 + ty + 16 * i;
+      const double nn = (ig < ig_end && n1 < p.nb) ? p.aqsn[(size_t)n1 * p.nc + ig] : 0.0;
+      for (int j = 0; j < TC; ++j)
+        for (int iw = 0; iw < kNW; ++iw) aw[i][j][iw] = fma(nn, y[j][iw], aw[i][j][iw]);
+    }
+  }
+  for (int i = 0; i < TB; ++i)
+    for (int j = 0; j < TC; ++j)
+      for (int iw = 0; iw < kNW; ++iw) acc[(i * TC + j) * kNW + iw][tid] += aw[i][j][iw];
+}
 
 __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, GppWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -72,15 +122,21 @@ __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, Gpp
     const ItemCoord ic = decode_item(w, item);
     const int n1_0 = ic.bb * kRBN, p0 = ic.cb * kRBP;
     const int ig_begin = ic.s * w.split_len, ig_end = min(ig_begin + w.split_len, p.nc);
-    double acc[TB][TC][kNW];
-    float acl[TB][TC][kNW];
+    // FP64 sums in shared memory (each thread its own slots); per-chunk
+    // float-float sums in registers: the high halves of two g-vectors' terms
+    // added exactly (TwoSum), their sum added exactly to the high half, the
+    // errors and low halves to the low half; after each chunk the pair
+    // renormalised (Fast2Sum), its high half added to the FP64 sum and its
+    // low half carried on
+    float ach[TB][TC][kNW], acl[TB][TC][kNW];
 #pragma unroll
     for (int i = 0; i < TB; ++i)
 #pragma unroll
       for (int j = 0; j < TC; ++j)
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
-          acc[i][j][iw] = 0.0;
+          sm.acc[(i * TC + j) * kNW + iw][tid] = 0.0;
+          ach[i][j][iw] = 0.f;
           acl[i][j][iw] = 0.f;
         }
 
@@ -93,24 +149,15 @@ __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, Gpp
         double y0 = 0.0, y1 = 0.0, y2 = 0.0;
         if (ig < ig_end && my_igp < p.ng) {
           const size_t off = (size_t)my_igp * p.nc + ig;
-          const double wt = p.wt[off];
-          const double g = p.ieps[off] * wt;
-          const double thr = guard_thr(wt, 0.0);
-          auto factor = [&](double wx) {
-            const double c = __dsub_rn(wx, wt);
-            const double wv = __dmul_rn(c, c);
-            const double r = keep_nonneg(wv, thr) ? rcp_f64_seed32(wv) : 0.0;
-            return g * (c * r);
-          };
-          y0 = factor(wx0);
-          y1 = factor(wx1);
-          y2 = factor(wx2);
+          const double wt = p.wt[off], g = p.ieps[off] * wt, thr = guard_thr(wt, 0.0);
+          y0 = real_y(wt, g, thr, wx0);
+          y1 = real_y(wt, g, thr, wx1);
+          y2 = real_y(wt, g, thr, wx2);
         }
         const double ys[kNW] = {y0, y1, y2};
 #pragma unroll
         for (int iw = 0; iw < kNW; ++iw) {
           const FF f = ff_of_rn(ys[iw]);
-          sm.y[k][iw * kRBP + pl] = ys[iw];
           sm.yf[k][iw * kRBP + pl] = make_float2(f.hi, f.lo);
           chunk_wide = chunk_wide || !ff_range(ys[iw], 0.0);
         }
@@ -120,14 +167,14 @@ __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, Gpp
         const int ig = ig0 + k, n1 = n1_0 + bl;
         const double v = (ig < ig_end && n1 < p.nb) ? p.aqsn[(size_t)n1 * p.nc + ig] : 0.0;
         const FF f = ff_of_rn(v);
-        sm.n[k][bl] = v;
         sm.nf[k][bl] = make_float2(f.hi, f.lo);
         chunk_wide = chunk_wide || !ff_range(v, 0.0);
       }
       chunk_wide = __syncthreads_or(chunk_wide);
       if (!chunk_wide) {
         // the terms of two g-vectors: float-float products, their high
-        // halves added exactly, the sum added in FP64
+        // halves added exactly, the sum added exactly to the chunk's
+        // float-float sum
         static_assert(kRCK % 2 == 0, "g-vector pairs");
 #pragma unroll 1
         for (int k = 0; k < kRCK; k += 2) {
@@ -147,10 +194,11 @@ __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, Gpp
               for (int iw = 0; iw < kNW; ++iw) {
                 const FF t0 = ff_mul_raw(FF{n0.x, n0.y}, FF{y[0][j][iw].x, y[0][j][iw].y});
                 const FF t1 = ff_mul_raw(FF{n1v.x, n1v.y}, FF{y[1][j][iw].x, y[1][j][iw].y});
-                float s, e;
+                float s, e, hs, he;
                 two_sum_f(t0.hi, t1.hi, s, e);
-                acc[i][j][iw] += f32_widen(s);
-                acl[i][j][iw] += (e + t0.lo) + t1.lo;
+                two_sum_f(ach[i][j][iw], s, hs, he);
+                ach[i][j][iw] = hs;
+                acl[i][j][iw] += ((e + t0.lo) + t1.lo) + he;
               }
           }
         }
@@ -160,27 +208,22 @@ __global__ void __launch_bounds__(kThreads, 2) sch_real_kernel(GppRealDev p, Gpp
           for (int j = 0; j < TC; ++j)
 #pragma unroll
             for (int iw = 0; iw < kNW; ++iw) {
-              acc[i][j][iw] += f32_widen(acl[i][j][iw]);
-              acl[i][j][iw] = 0.f;
+              const float s = __fadd_rn(ach[i][j][iw], acl[i][j][iw]);
+              acl[i][j][iw] = __fsub_rn(acl[i][j][iw], __fsub_rn(s, ach[i][j][iw]));
+              ach[i][j][iw] = 0.f;
+              sm.acc[(i * TC + j) * kNW + iw][tid] += f32_widen(s);
             }
       } else {
-        for (int k = 0; k < kRCK; ++k) {
-          double nn[TB], y[TC][kNW];
-#pragma unroll
-          for (int i = 0; i < TB; ++i) nn[i] = sm.n[k][ty + 16 * i];
-#pragma unroll
-          for (int j = 0; j < TC; ++j)
-#pragma unroll
-            for (int iw = 0; iw < kNW; ++iw) y[j][iw] = sm.y[k][iw * kRBP + tx + 16 * j];
-#pragma unroll
-          for (int i = 0; i < TB; ++i)
-#pragma unroll
-            for (int j = 0; j < TC; ++j)
-#pragma unroll
-              for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = fma(nn[i], y[j][iw], acc[i][j][iw]);
-        }
+        real_wide_chunk(p, sm.acc, tid, ig0, ig_end, n1_0, p0, wx0, wx1, wx2);
       }
     }
+    double acc[TB][TC][kNW];
+#pragma unroll
+    for (int i = 0; i < TB; ++i)
+#pragma unroll
+      for (int j = 0; j < TC; ++j)
+#pragma unroll
+        for (int iw = 0; iw < kNW; ++iw) acc[i][j][iw] = sm.acc[(i * TC + j) * kNW + iw][tid] + f32_widen(acl[i][j][iw]);
     // epilogue: x aqsm[n1][igp] * 0.5 * vcoul[igp], half-warp butterfly over columns
 #pragma unroll
     for (int i = 0; i < TB; ++i) {
@@ -401,6 +444,9 @@ extern "C" int sigma_gpp_real_execute(sigma_gpp_real_plan plan, const double* wx
   if (plan->sch.n_items > 0) {
     SIGMA_CUDA_TRY(cudaFuncSetAttribute(sch_real_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)sizeof(RealSmem)));
+    // two CTAs per SM hold ~180 KB of shared memory between them
+    SIGMA_CUDA_TRY(cudaFuncSetAttribute(sch_real_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                        cudaSharedmemCarveoutMaxShared));
     sch_real_kernel<<<plan->sch_grid, kThreads, sizeof(RealSmem), s>>>(p, plan->sch);
     SIGMA_CUDA_TRY(cudaGetLastError());
   }
