@@ -73,13 +73,42 @@ struct HalfDev {
 // are multiples of 128 bytes, put a warp's writes in one bank group.
 template <int NF>
 struct HalfSmem {
-  double2 z[kHCK][NF * kHBP + 1];  // [k][f * kHBP + column]
-  double2 n[kHCK][kHBN + 1];
-  double2 m[kHCK][kHBN + 1];
-  double zs[kHCK][NF * kHBP + 1];  // z.x + z.y
-  double ns[kHCK][kHBN + 1];
-  double ms[kHCK][kHBN + 1];
+  // each thread's FP64 sums T and U (4 bands x 1 column x NF frequencies),
+  // one slot row per output
+  double2 acc[2 * kHTB * kHTC * NF][kThreads];
+  // Z as float-float operands of paired instructions (lanes: real and
+  // imaginary parts): [k][f * kHBP + column] (Re.hi, Im.hi, -Re.lo, -Im.lo)
+  // of Z, [k][NF * kHBP + f * kHBP + column] those of i Z
+  float4 z[kHCK][2 * NF * kHBP + 1];
+  // aqsn and aqsm as broadcast pairs: [k][band] (Re.hi, Re.hi, Re.lo, Re.lo),
+  // [k][kHBN + band] the same of Im
+  float4 n[kHCK][2 * kHBN + 1];
+  float4 m[kHCK][2 * kHBN + 1];
 };
+
+// n Z + (float-float sum h, l): the paired float-float product of a
+// broadcast pair n (high rh, ih; low rl, il) and a staged factor (a: high
+// pair, its negation, negated low pair; the same three of i Z), its high
+// pair added exactly to h (TwoSum), the errors and low halves to l.
+__device__ __forceinline__ void half_ff_mac(float2& h, float2& l, float2 rh, float2 rl, float2 ih, float2 il,
+                                            float2 ah, float2 anh, float2 anl, float2 bh, float2 bnh,
+                                            float2 bnl) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 p1 = __fmul2_rn(rh, ah), p2 = __fmul2_rn(ih, bh);
+  const float2 g1 = __ffma2_rn(rh, anl, __ffma2_rn(rl, anh, __ffma2_rn(rh, anh, p1)));
+  const float2 g2 = __ffma2_rn(ih, bnl, __ffma2_rn(il, bnh, __ffma2_rn(ih, bnh, p2)));
+  const float2 s = __fadd2_rn(p1, p2);
+  const float2 bv = __ffma2_rn(p1, m1, s);
+  const float2 av = __ffma2_rn(bv, m1, s);
+  const float2 es = __fadd2_rn(__ffma2_rn(av, m1, p1), __ffma2_rn(bv, m1, p2));
+  const float2 lo = __ffma2_rn(__fadd2_rn(g1, g2), m1, es);
+  const float2 hs = __fadd2_rn(h, s);
+  const float2 hb = __ffma2_rn(h, m1, hs);
+  const float2 ha = __ffma2_rn(hb, m1, hs);
+  const float2 he = __fadd2_rn(__ffma2_rn(ha, m1, h), __ffma2_rn(hb, m1, s));
+  h = hs;
+  l = __fadd2_rn(l, __fadd2_rn(he, lo));
+}
 
 __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
   acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
@@ -116,6 +145,56 @@ __device__ __forceinline__ void half_factor(double2 wt, double2 ie, const double
   }
 }
 
+// A chunk holding a value outside the float-float range: FP64 complex
+// multiply-adds of the thread's tile, Z formed again from the inputs and
+// aqsn / aqsm read again, added to the FP64 sums.  Out of line.
+template <int NF>
+static __device__ __noinline__ void half_wide_chunk(const HalfDev& p, double2 (*acc)[kThreads], int tid, int ig0,
+                                                    int ig_end, int n1_0, int p0, const double* wx) {
+  constexpr int NO = kHTB * kHTC * NF;
+  const int tx = tid & 15, ty = tid >> 4;
+  double2 ta[NO], ua[NO];
+  for (int o = 0; o < NO; ++o) ta[o] = ua[o] = make_double2(0.0, 0.0);
+  for (int k = 0; k < kHCK; ++k) {
+    const int ig = ig0 + k;
+    double2 z[kHTC][3];
+    for (int j = 0; j < kHTC; ++j) {
+      const int col = p0 + tx + 16 * j;
+      const int lim = column_limit<NF>(col < p.ng ? p.igp_of[col] : -1);
+      bool in = ig < ig_end && ig < lim;
+      if (NF == 3) in = in && (ig % kIgBlk) != kIgBlk - 1;
+      for (int f = 0; f < 3; ++f) z[j][f] = make_double2(0.0, 0.0);
+      if (in) {
+        const size_t off = (size_t)col * p.nc + ig;
+        const double2 ie = p.ieps[off];
+        if (NF == 1)
+          z[j][0] = make_double2(-ie.x, -ie.y);
+        else
+          half_factor(p.wt[off], ie, wx, z[j]);
+      }
+    }
+    for (int i = 0; i < kHTB; ++i) {
+      const int n1 = n1_0 + ty + 16 * i;
+      const bool in = ig < ig_end && n1 < p.nb;
+      const size_t off = (size_t)n1 * p.nc + ig;
+      const double2 nv = in ? p.aqsn[off] : make_double2(0.0, 0.0);
+      const double2 mv = in ? p.aqsm[off] : make_double2(0.0, 0.0);
+      for (int j = 0; j < kHTC; ++j)
+        for (int f = 0; f < NF; ++f) {
+          const int o = (i * kHTC + j) * NF + f;
+          cfma(ta[o], nv, z[j][f]);
+          cfma(ua[o], mv, z[j][f]);
+        }
+    }
+  }
+  for (int o = 0; o < NO; ++o) {
+    acc[o][tid].x += ta[o].x;
+    acc[o][tid].y += ta[o].y;
+    acc[NO + o][tid].x += ua[o].x;
+    acc[NO + o][tid].y += ua[o].y;
+  }
+}
+
 template <int NF>
 __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -141,19 +220,25 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
     const int ig_begin = ic.s * w.split_len;
     const int ig_end = min(min(ig_begin + w.split_len, p.nc), s_kmax);
 
-    // three real sums per complex sum: T from (t1, t2, t3), U from (u1, u2, u3)
-    double t1[kHTB][kHTC][NF], t2[kHTB][kHTC][NF], t3[kHTB][kHTC][NF];
-    double u1[kHTB][kHTC][NF], u2[kHTB][kHTC][NF], u3[kHTB][kHTC][NF];
+    // T = sum aqsn Z, U = sum aqsm Z: every term a float-float product in
+    // paired instructions (real and imaginary parts as the lanes) added to a
+    // per-chunk float-float sum; after each chunk the sum is renormalised,
+    // its high pair added to the FP64 sums in shared memory and its low pair
+    // carried on.  A chunk with a value outside the float-float range runs
+    // FP64 multiply-adds on factors formed again from the inputs.
+    constexpr int NO = kHTB * kHTC * NF;  // outputs of each of T and U
+    const float2 m1 = make_float2(-1.f, -1.f);
+    float2 th[NO], tl[NO], uh[NO], ul[NO];
 #pragma unroll
-    for (int i = 0; i < kHTB; ++i)
-#pragma unroll
-      for (int j = 0; j < kHTC; ++j)
-#pragma unroll
-        for (int f = 0; f < NF; ++f)
-          t1[i][j][f] = t2[i][j][f] = t3[i][j][f] = u1[i][j][f] = u2[i][j][f] = u3[i][j][f] = 0.0;
+    for (int o = 0; o < NO; ++o) {
+      sm.acc[o][tid] = make_double2(0.0, 0.0);
+      sm.acc[NO + o][tid] = make_double2(0.0, 0.0);
+      th[o] = tl[o] = uh[o] = ul[o] = make_float2(0.f, 0.f);
+    }
 
     for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kHCK) {
       __syncthreads();
+      bool chunk_wide = false;
       for (int e = tid; e < kHCK * kHBP; e += kThreads) {
         const int k = e % kHCK, pl = e / kHCK;
         const int ig = ig0 + k, col = p0 + pl;
@@ -171,8 +256,10 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
         }
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-          sm.z[k][f * kHBP + pl] = z[f];
-          sm.zs[k][f * kHBP + pl] = __dadd_rn(z[f].x, z[f].y);
+          const FF vx = ff_of_rn(z[f].x), vy = ff_of_rn(z[f].y);
+          sm.z[k][f * kHBP + pl] = make_float4(vx.hi, vy.hi, -vx.lo, -vy.lo);
+          sm.z[k][NF * kHBP + f * kHBP + pl] = make_float4(-vy.hi, vx.hi, vy.lo, -vx.lo);
+          chunk_wide = chunk_wide || !ff_range(z[f].x, z[f].y);
         }
       }
       for (int e = tid; e < kHCK * kHBN; e += kThreads) {
@@ -182,44 +269,72 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
         const size_t off = (size_t)n1 * p.nc + ig;
         const double2 nv = in ? p.aqsn[off] : make_double2(0.0, 0.0);
         const double2 mv = in ? p.aqsm[off] : make_double2(0.0, 0.0);
-        sm.n[k][bl] = nv;
-        sm.m[k][bl] = mv;
-        sm.ns[k][bl] = __dadd_rn(nv.x, nv.y);
-        sm.ms[k][bl] = __dadd_rn(mv.x, mv.y);
+        const FF nx = ff_of_rn(nv.x), ny = ff_of_rn(nv.y), mx = ff_of_rn(mv.x), my = ff_of_rn(mv.y);
+        sm.n[k][bl] = make_float4(nx.hi, nx.hi, nx.lo, nx.lo);
+        sm.n[k][kHBN + bl] = make_float4(ny.hi, ny.hi, ny.lo, ny.lo);
+        sm.m[k][bl] = make_float4(mx.hi, mx.hi, mx.lo, mx.lo);
+        sm.m[k][kHBN + bl] = make_float4(my.hi, my.hi, my.lo, my.lo);
+        chunk_wide = chunk_wide || !ff_range(nv.x, nv.y) || !ff_range(mv.x, mv.y);
       }
-      __syncthreads();
-#pragma unroll 2
-      for (int k = 0; k < kHCK; ++k) {
-        double2 nn[kHTB], mm[kHTB], z[kHTC][NF];
-        double nsum[kHTB], msum[kHTB], zsum[kHTC][NF];
-#pragma unroll
-        for (int i = 0; i < kHTB; ++i) {
-          nn[i] = sm.n[k][ty + 16 * i];
-          mm[i] = sm.m[k][ty + 16 * i];
-          nsum[i] = sm.ns[k][ty + 16 * i];
-          msum[i] = sm.ms[k][ty + 16 * i];
-        }
-#pragma unroll
-        for (int j = 0; j < kHTC; ++j)
-#pragma unroll
-          for (int f = 0; f < NF; ++f) {
-            z[j][f] = sm.z[k][f * kHBP + tx + 16 * j];
-            zsum[j][f] = sm.zs[k][f * kHBP + tx + 16 * j];
-          }
-#pragma unroll
-        for (int i = 0; i < kHTB; ++i)
+      chunk_wide = __syncthreads_or(chunk_wide);
+      if (!chunk_wide) {
+#pragma unroll 1
+        for (int k = 0; k < kHCK; ++k) {
+          float2 ah[kHTC][NF], anh[kHTC][NF], anl[kHTC][NF], bh[kHTC][NF], bnh[kHTC][NF], bnl[kHTC][NF];
 #pragma unroll
           for (int j = 0; j < kHTC; ++j)
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-              t1[i][j][f] = fma(nn[i].x, z[j][f].x, t1[i][j][f]);
-              t2[i][j][f] = fma(nn[i].y, z[j][f].y, t2[i][j][f]);
-              t3[i][j][f] = fma(nsum[i], zsum[j][f], t3[i][j][f]);
-              u1[i][j][f] = fma(mm[i].x, z[j][f].x, u1[i][j][f]);
-              u2[i][j][f] = fma(mm[i].y, z[j][f].y, u2[i][j][f]);
-              u3[i][j][f] = fma(msum[i], zsum[j][f], u3[i][j][f]);
+              const float4 a = sm.z[k][f * kHBP + tx + 16 * j];
+              const float4 b = sm.z[k][NF * kHBP + f * kHBP + tx + 16 * j];
+              ah[j][f] = f4_lo(a);
+              anl[j][f] = f4_hi(a);
+              anh[j][f] = __fmul2_rn(ah[j][f], m1);
+              bh[j][f] = f4_lo(b);
+              bnl[j][f] = f4_hi(b);
+              bnh[j][f] = __fmul2_rn(bh[j][f], m1);
             }
+#pragma unroll
+          for (int i = 0; i < kHTB; ++i) {
+            const float4 nr = sm.n[k][ty + 16 * i], ni = sm.n[k][kHBN + ty + 16 * i];
+            const float4 mr = sm.m[k][ty + 16 * i], mi = sm.m[k][kHBN + ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < kHTC; ++j)
+#pragma unroll
+              for (int f = 0; f < NF; ++f) {
+                const int o = (i * kHTC + j) * NF + f;
+                half_ff_mac(th[o], tl[o], f4_lo(nr), f4_hi(nr), f4_lo(ni), f4_hi(ni), ah[j][f], anh[j][f],
+                            anl[j][f], bh[j][f], bnh[j][f], bnl[j][f]);
+                half_ff_mac(uh[o], ul[o], f4_lo(mr), f4_hi(mr), f4_lo(mi), f4_hi(mi), ah[j][f], anh[j][f],
+                            anl[j][f], bh[j][f], bnh[j][f], bnl[j][f]);
+              }
+          }
+        }
+#pragma unroll
+        for (int o = 0; o < NO; ++o) {
+          const float2 s = __fadd2_rn(th[o], tl[o]);
+          tl[o] = __ffma2_rn(__ffma2_rn(th[o], m1, s), m1, tl[o]);
+          th[o] = make_float2(0.f, 0.f);
+          double2& a = sm.acc[o][tid];
+          a.x += f32_widen(s.x);
+          a.y += f32_widen(s.y);
+          const float2 su = __fadd2_rn(uh[o], ul[o]);
+          ul[o] = __ffma2_rn(__ffma2_rn(uh[o], m1, su), m1, ul[o]);
+          uh[o] = make_float2(0.f, 0.f);
+          double2& b = sm.acc[NO + o][tid];
+          b.x += f32_widen(su.x);
+          b.y += f32_widen(su.y);
+        }
+      } else {
+        half_wide_chunk<NF>(p, sm.acc, tid, ig0, ig_end, n1_0, p0, wx);
       }
+    }
+    double2 tsum[NO], usum[NO];
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+      const double2 a = sm.acc[o][tid], b = sm.acc[NO + o][tid];
+      tsum[o] = make_double2(a.x + f32_widen(tl[o].x), a.y + f32_widen(tl[o].y));
+      usum[o] = make_double2(b.x + f32_widen(ul[o].x), b.y + f32_widen(ul[o].y));
     }
     // epilogue: 0.5 vcoul (conj(aqsm_p) T + v_p conj(U)) [+ the diagonal term
     // in the first split], half-warp butterfly over the columns
@@ -241,10 +356,8 @@ __global__ void __launch_bounds__(kThreads, 1) half_main_kernel(HalfDev p, GppWo
           double2 val[NF];
 #pragma unroll
           for (int f = 0; f < NF; ++f) {
-            const double2 T = make_double2(__dsub_rn(t1[i][j][f], t2[i][j][f]),
-                                           __dsub_rn(__dsub_rn(t3[i][j][f], t1[i][j][f]), t2[i][j][f]));
-            const double2 U = make_double2(__dsub_rn(u1[i][j][f], u2[i][j][f]),
-                                           __dsub_rn(__dsub_rn(u3[i][j][f], u1[i][j][f]), u2[i][j][f]));
+            const double2 T = tsum[(i * kHTC + j) * NF + f];
+            const double2 U = usum[(i * kHTC + j) * NF + f];
             val[f] = cmul(cconj(am), T);
             cfma(val[f], vp, cconj(U));
           }
